@@ -1,0 +1,183 @@
+/*
+ * mgmc_gb300.h -- C ABI of the GB300 Multigrid Monte Carlo sampler.
+ *
+ * The library samples the Gaussian distribution
+ *
+ *     pi(x) ~ exp(-1/2 x^T A x + f^T x),   A = A_0 + B Sigma^{-1} B^T,
+ *
+ * where A_0 is a constant-coefficient stencil operator on a structured
+ * 1d/2d/3d lattice with homogeneous Dirichlet boundaries and B is a sparse
+ * n x m measurement matrix.  It replaces the reference's sampler classes:
+ *
+ *   mgmc_sampler_create      MultigridMCSampler ctor  src/sampler/multigridmc_sampler.cc:8-106
+ *                            (nlevel == 1 with coarse_solver SSOR gives
+ *                            SSORSampler, src/sampler/ssor_sampler.hh:29-37;
+ *                            with coarse_solver CHOLESKY the dense
+ *                            CholeskySampler, src/sampler/cholesky_sampler.cc:25-37)
+ *   mgmc_sampler_apply       Sampler::apply(f, x)     src/sampler/sampler.hh:52-55,
+ *                                                     multigridmc_sampler.cc:139-145
+ *   mgmc_sampler_fix_rhs     Sampler::fix_rhs         src/sampler/sampler.hh:64-71
+ *   mgmc_level_apply         LinearOperator::apply    src/linear_operator/linear_operator.hh:78-88
+ *   mgmc_level_restrict      IntergridOperator::restrict        src/intergrid/intergrid_operator.hh:74-88
+ *   mgmc_level_prolongate_add IntergridOperator::prolongate_add src/intergrid/intergrid_operator.hh:106-120
+ *   mgmc_level_sor           SORSampler::apply / SORSmoother::apply
+ *                                                     src/sampler/sor_sampler.cc:37-59,
+ *                                                     src/smoother/sor_smoother.cc:40-78
+ *   mgmc_fd_stencil          ShiftedLaplaceFDOperator src/linear_operator/shiftedlaplace_fd_operator.cc:9-57
+ *   mgmc_measurement_vector  MeasuredOperator::measurement_vector
+ *                                                     src/linear_operator/measured_operator.cc:69-171
+ *   mgmc_galerkin_stencil    LinearOperator::coarsen  src/linear_operator/linear_operator.cc:10-23
+ *
+ * Conventions
+ *  - Every entry point returns an mgmc_status; none exits, throws or traps
+ *    (the reference calls exit(-1) on errors).  mgmc_last_error() gives a
+ *    message for the calling thread.
+ *  - Vectors crossing the ABI are FP64 in the reference's vertex order
+ *    (lexicographic, x fastest, interior vertices only,
+ *    src/lattice/lattice3d.hh:118-141).  Pointers are host pointers unless the
+ *    argument `on_device` is non-zero, in which case they are device
+ *    pointers of the GPU the sampler was created on.
+ *  - A sampler is not thread-safe (the reference's samplers keep mutable
+ *    work vectors too); use one sampler per host thread.  All of a sampler's
+ *    GPU work runs on its own CUDA stream (mgmc_sampler_stream).
+ */
+#ifndef MGMC_GB300_H
+#define MGMC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGMC_ABI_VERSION 1
+
+typedef enum mgmc_status {
+    MGMC_OK = 0,
+    MGMC_ERR_INVALID_ARGUMENT = 1,
+    MGMC_ERR_LATTICE = 2,          /* extent odd / nothing left to coarsen (lattice3d.hh:248-263) */
+    MGMC_ERR_NOT_SPD = 3,          /* coarse precision matrix not positive definite */
+    MGMC_ERR_CUDA = 4,             /* a CUDA runtime call failed */
+    MGMC_ERR_OUT_OF_MEMORY = 5,
+    MGMC_ERR_NOISE_EXHAUSTED = 6,  /* injected-noise mode: not enough normals queued */
+    MGMC_ERR_NONFINITE = 7,        /* NaN/Inf seen in the chain state */
+    MGMC_ERR_UNSUPPORTED = 8
+} mgmc_status;
+
+/* sweep ordering */
+enum {
+    MGMC_ORDER_LEXICOGRAPHIC = 0, /* the reference's order (sor_smoother.cc:66-76), run as a hyperplane wavefront */
+    MGMC_ORDER_MULTICOLOUR = 1    /* 2 colours for axis-only stencils, 2^dim colours otherwise */
+};
+/* arithmetic */
+enum {
+    MGMC_FP64 = 0,      /* every level in FP64 */
+    MGMC_FP32_MIXED = 1 /* sweeps, residuals, transfers in FP32; coarse Cholesky and m x m system FP64 */
+};
+/* noise source */
+enum {
+    MGMC_NOISE_PHILOX = 0,  /* counter-based Philox4x32-10 normals generated inside the kernels */
+    MGMC_NOISE_INJECTED = 1 /* caller-supplied N(0,1) values consumed in the reference's draw order */
+};
+/* smoother / coarse solver (MultigridParameters, src/auxilliary/parameters.hh:150-179) */
+enum { MGMC_SMOOTHER_SOR = 0, MGMC_SMOOTHER_SSOR = 1 };
+enum { MGMC_COARSE_CHOLESKY = 0, MGMC_COARSE_SSOR = 1 };
+enum { MGMC_FORWARD = 1, MGMC_BACKWARD = 2 }; /* Direction, src/smoother/sor_smoother.hh:14-18 */
+
+/* Problem: lattice, fine-level stencil and the optional low-rank term. */
+typedef struct mgmc_operator_desc {
+    int dim;            /* 1, 2 or 3 */
+    int nx, ny, nz;     /* cells per direction (unused directions ignored); n = prod (n_d - 1) unknowns */
+    double stencil[27]; /* constant fine-level stencil, entry (dz+1)*9 + (dy+1)*3 + (dx+1) */
+    int m;              /* number of measurement columns, 0 for none */
+    const int64_t *B_colptr; /* m+1 column pointers of B (CSC, row indices ascending) */
+    const int64_t *B_rowidx; /* vertex indices in the reference's order */
+    const double *B_val;
+    const double *Sigma;     /* m diagonal entries of the measurement covariance */
+} mgmc_operator_desc;
+
+/* Sampler parameters: MultigridParameters plus the GB300 execution choices. */
+typedef struct mgmc_sampler_params {
+    int nlevel;
+    int smoother;      /* MGMC_SMOOTHER_SOR | MGMC_SMOOTHER_SSOR */
+    int coarse_solver; /* MGMC_COARSE_CHOLESKY | MGMC_COARSE_SSOR */
+    int npresmooth;
+    int npostsmooth;
+    int ncoarsesmooth;
+    double omega;
+    int cycle;         /* 1 = V-cycle, 2 = W-cycle */
+    double coarse_scaling;
+    int ordering;      /* MGMC_ORDER_* */
+    int precision;     /* MGMC_FP64 | MGMC_FP32_MIXED */
+    int noise;         /* MGMC_NOISE_* */
+    uint64_t seed;     /* Philox key */
+    int device;        /* CUDA device ordinal */
+} mgmc_sampler_params;
+
+typedef struct mgmc_sampler mgmc_sampler;
+
+/* ---------------------------------------------------------------- info */
+int mgmc_abi_version(void);
+const char *mgmc_last_error(void);
+
+/* -------------------------------------------------------- host set-up */
+/* ShiftedLaplaceFDOperator stencil (shiftedlaplace_fd_operator.cc:9-57):
+ * diag h^d kappa^2 + sum_d 2 h^d / h_d^2, neighbours -h^d / h_d^2. */
+mgmc_status mgmc_fd_stencil(int dim, int nx, int ny, int nz, double kappa_sq, double stencil[27]);
+/* MeasuredOperator::measurement_vector (measured_operator.cc:69-171): FE
+ * quadrature of 1{|x-x0|<R}/V_d(R); radius < 1e-12 selects the nearest
+ * vertex.  Writes at most `capacity` entries and sets *nnz to the count. */
+mgmc_status mgmc_measurement_vector(int dim, int nx, int ny, int nz, const double *x0, double radius,
+                                    int64_t *idx, double *val, int64_t capacity, int64_t *nnz);
+/* Galerkin triple product R A R^T of a constant stencil with the linear
+ * intergrid operator (linear_operator.cc:10-23, intergrid_operator_linear.cc:8-31). */
+mgmc_status mgmc_galerkin_stencil(int dim, const double fine[27], double coarse[27]);
+
+/* ------------------------------------------------------------- sampler */
+mgmc_status mgmc_sampler_create(const mgmc_operator_desc *op, const mgmc_sampler_params *params,
+                                mgmc_sampler **out);
+mgmc_status mgmc_sampler_destroy(mgmc_sampler *s);
+/* One sample: x <- MGMC step(f, x), both length n. */
+mgmc_status mgmc_sampler_apply(mgmc_sampler *s, const double *f, double *x, int on_device);
+/* Keep f on the device for mgmc_sampler_step. */
+mgmc_status mgmc_sampler_fix_rhs(mgmc_sampler *s, const double *f, int on_device);
+mgmc_status mgmc_sampler_set_state(mgmc_sampler *s, const double *x, int on_device);
+mgmc_status mgmc_sampler_get_state(mgmc_sampler *s, double *x, int on_device);
+/* nsteps samples with the state and right hand side resident on the GPU;
+ * asynchronous on the sampler's stream. */
+mgmc_status mgmc_sampler_step(mgmc_sampler *s, int64_t nsteps);
+/* Observable z_k = b^T x after every step (measure_sampling_time,
+ * src/measurements/sampling_time.cc:37-41); up to `capacity` values are
+ * kept on the device until read. */
+mgmc_status mgmc_sampler_set_observable(mgmc_sampler *s, int64_t nnz, const int64_t *idx, const double *val,
+                                        int64_t capacity);
+mgmc_status mgmc_sampler_read_observations(mgmc_sampler *s, double *out, int64_t capacity, int64_t *count);
+/* Injected-noise mode: queue `count` N(0,1) values; each step consumes
+ * mgmc_sampler_noise_per_step() of them in the reference's draw order. */
+mgmc_status mgmc_sampler_inject_noise(mgmc_sampler *s, const double *normals, int64_t count, int on_device);
+mgmc_status mgmc_sampler_noise_per_step(mgmc_sampler *s, int64_t *count);
+mgmc_status mgmc_sampler_synchronize(mgmc_sampler *s);
+mgmc_status mgmc_sampler_stream(mgmc_sampler *s, void **cuda_stream);
+mgmc_status mgmc_sampler_nlevel(mgmc_sampler *s, int *nlevel);
+mgmc_status mgmc_sampler_level_size(mgmc_sampler *s, int level, int64_t *n);
+/* Number of kernel launches one step issues (measurement bookkeeping). */
+mgmc_status mgmc_sampler_launches_per_step(mgmc_sampler *s, int64_t *count);
+
+/* -------------------------------------------- level building blocks */
+mgmc_status mgmc_level_stencil(mgmc_sampler *s, int level, double stencil[27]);
+/* y = A x on level `level` (including B Sigma^{-1} B^T x). */
+mgmc_status mgmc_level_apply(mgmc_sampler *s, int level, const double *x, double *y);
+/* xc = R x from `level` to level+1. */
+mgmc_status mgmc_level_restrict(mgmc_sampler *s, int level, const double *x, double *xc);
+/* x += alpha P xc from level+1 to `level`. */
+mgmc_status mgmc_level_prolongate_add(mgmc_sampler *s, int level, double alpha, const double *xc, double *x);
+/* One SOR sweep in `direction` with the low-rank update: with_noise != 0
+ * is SORSampler::apply (noise from the sampler's source), 0 is
+ * SORSmoother::apply with right hand side f. */
+mgmc_status mgmc_level_sor(mgmc_sampler *s, int level, int direction, int with_noise, const double *f, double *x);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MGMC_GB300_H */

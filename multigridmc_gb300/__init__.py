@@ -1,0 +1,431 @@
+"""GB300 Multigrid Monte Carlo sampler -- Python front end.
+
+Mirrors the reference's class surface for the sampling path:
+
+=======================  ==========================================================
+this module              reference (eikehmueller/MultigridMC)
+=======================  ==========================================================
+``fd_stencil``           ShiftedLaplaceFDOperator (linear_operator/shiftedlaplace_fd_operator.cc:9-57)
+``measurement_vector``   MeasuredOperator::measurement_vector (linear_operator/measured_operator.cc:69-171)
+``LinearOperator``       LinearOperator / MeasuredOperator (linear_operator/linear_operator.hh:19-213,
+                         measured_operator.cc:9-47)
+``MultigridParameters``  MultigridParameters (auxilliary/parameters.hh:150-179)
+``MultigridMCSampler``   MultigridMCSampler (sampler/multigridmc_sampler.cc:8-145)
+``SSORSampler``          SSORSampler (sampler/ssor_sampler.{hh,cc})
+``CholeskySampler``      DenseCholeskySampler (sampler/cholesky_sampler.cc:25-37)
+=======================  ==========================================================
+
+Every call goes through the C ABI of ``libmgmc_gb300.so``
+(``include/mgmc_gb300.h``); there is no CPU implementation behind this
+module.  If the library cannot be loaded, import of the sampler classes
+raises -- nothing falls back to the host.
+"""
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = [
+    "MGMCError", "load", "fd_stencil", "galerkin_stencil", "measurement_vector", "LinearOperator",
+    "MultigridParameters", "MultigridMCSampler", "SSORSampler", "CholeskySampler",
+    "FP64", "FP32_MIXED", "LEXICOGRAPHIC", "MULTICOLOUR", "PHILOX", "INJECTED", "FORWARD", "BACKWARD",
+]
+
+OK = 0
+STATUS = {0: "MGMC_OK", 1: "MGMC_ERR_INVALID_ARGUMENT", 2: "MGMC_ERR_LATTICE", 3: "MGMC_ERR_NOT_SPD",
+          4: "MGMC_ERR_CUDA", 5: "MGMC_ERR_OUT_OF_MEMORY", 6: "MGMC_ERR_NOISE_EXHAUSTED",
+          7: "MGMC_ERR_NONFINITE", 8: "MGMC_ERR_UNSUPPORTED"}
+LEXICOGRAPHIC, MULTICOLOUR = 0, 1
+FP64, FP32_MIXED = 0, 1
+PHILOX, INJECTED = 0, 1
+FORWARD, BACKWARD = 1, 2
+
+
+class MGMCError(RuntimeError):
+    """A C-ABI call returned a status other than MGMC_OK."""
+
+    def __init__(self, status, message):
+        self.status = status
+        self.name = STATUS.get(status, str(status))
+        super().__init__(f"{self.name}: {message}")
+
+
+class _OpDesc(C.Structure):
+    _fields_ = [("dim", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("stencil", C.c_double * 27), ("m", C.c_int),
+                ("B_colptr", C.POINTER(C.c_int64)), ("B_rowidx", C.POINTER(C.c_int64)),
+                ("B_val", C.POINTER(C.c_double)), ("Sigma", C.POINTER(C.c_double))]
+
+
+class _Params(C.Structure):
+    _fields_ = [("nlevel", C.c_int), ("smoother", C.c_int), ("coarse_solver", C.c_int),
+                ("npresmooth", C.c_int), ("npostsmooth", C.c_int), ("ncoarsesmooth", C.c_int),
+                ("omega", C.c_double), ("cycle", C.c_int), ("coarse_scaling", C.c_double),
+                ("ordering", C.c_int), ("precision", C.c_int), ("noise", C.c_int),
+                ("seed", C.c_uint64), ("device", C.c_int)]
+
+
+_lib = None
+_D = C.POINTER(C.c_double)
+_I64 = C.POINTER(C.c_int64)
+_P = C.c_void_p
+
+# name -> (restype, argtypes); the list is the complete set of symbols the
+# header declares
+SIGNATURES = {
+    "mgmc_abi_version": (C.c_int, []),
+    "mgmc_last_error": (C.c_char_p, []),
+    "mgmc_fd_stencil": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _D]),
+    "mgmc_measurement_vector": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _D, C.c_double, _I64, _D,
+                                          C.c_int64, _I64]),
+    "mgmc_galerkin_stencil": (C.c_int, [C.c_int, _D, _D]),
+    "mgmc_sampler_create": (C.c_int, [C.POINTER(_OpDesc), C.POINTER(_Params), C.POINTER(_P)]),
+    "mgmc_sampler_destroy": (C.c_int, [_P]),
+    "mgmc_sampler_apply": (C.c_int, [_P, _D, _D, C.c_int]),
+    "mgmc_sampler_fix_rhs": (C.c_int, [_P, _D, C.c_int]),
+    "mgmc_sampler_set_state": (C.c_int, [_P, _D, C.c_int]),
+    "mgmc_sampler_get_state": (C.c_int, [_P, _D, C.c_int]),
+    "mgmc_sampler_step": (C.c_int, [_P, C.c_int64]),
+    "mgmc_sampler_set_observable": (C.c_int, [_P, C.c_int64, _I64, _D, C.c_int64]),
+    "mgmc_sampler_read_observations": (C.c_int, [_P, _D, C.c_int64, _I64]),
+    "mgmc_sampler_inject_noise": (C.c_int, [_P, _D, C.c_int64, C.c_int]),
+    "mgmc_sampler_noise_per_step": (C.c_int, [_P, _I64]),
+    "mgmc_sampler_synchronize": (C.c_int, [_P]),
+    "mgmc_sampler_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "mgmc_sampler_nlevel": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "mgmc_sampler_level_size": (C.c_int, [_P, C.c_int, _I64]),
+    "mgmc_sampler_launches_per_step": (C.c_int, [_P, _I64]),
+    "mgmc_level_stencil": (C.c_int, [_P, C.c_int, _D]),
+    "mgmc_level_apply": (C.c_int, [_P, C.c_int, _D, _D]),
+    "mgmc_level_restrict": (C.c_int, [_P, C.c_int, _D, _D]),
+    "mgmc_level_prolongate_add": (C.c_int, [_P, C.c_int, C.c_double, _D, _D]),
+    "mgmc_level_sor": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _D, _D]),
+}
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libmgmc_gb300.so (building it in-tree if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise ImportError(f"{path} is missing; run multigridmc_gb300.build.build()")
+        _build.build()
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(status):
+    if status != OK:
+        msg = load().mgmc_last_error()
+        raise MGMCError(status, msg.decode() if msg else "")
+
+
+def _dp(a):
+    return a.ctypes.data_as(_D)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _shape3(shape):
+    s = list(shape) + [2] * (3 - len(shape))
+    return int(s[0]), int(s[1]), int(s[2])
+
+
+# ------------------------------------------------------------- host set-up
+def fd_stencil(shape, kappa_sq):
+    """27-entry stencil of ShiftedLaplaceFDOperator on a lattice of `shape` cells."""
+    st = np.zeros(27)
+    _check(load().mgmc_fd_stencil(len(shape), *_shape3(shape), float(kappa_sq), _dp(st)))
+    return st
+
+
+def galerkin_stencil(dim, fine):
+    fine = _f64(fine)
+    out = np.zeros(27)
+    _check(load().mgmc_galerkin_stencil(dim, _dp(fine), _dp(out)))
+    return out
+
+
+def measurement_vector(shape, x0, radius):
+    """(indices, values) of MeasuredOperator::measurement_vector."""
+    x0 = _f64(x0)
+    nnz = C.c_int64(0)
+    L = load()
+    _check(L.mgmc_measurement_vector(len(shape), *_shape3(shape), _dp(x0), float(radius), None, None, 0,
+                                     C.byref(nnz)))
+    idx = np.zeros(nnz.value, np.int64)
+    val = np.zeros(nnz.value)
+    _check(L.mgmc_measurement_vector(len(shape), *_shape3(shape), _dp(x0), float(radius),
+                                     idx.ctypes.data_as(_I64), _dp(val), nnz.value, C.byref(nnz)))
+    return idx, val
+
+
+@dataclass
+class LinearOperator:
+    """A = A_0 + B Sigma^{-1} B^T with a constant stencil A_0 on `shape` cells.
+
+    ``B`` is held column-compressed (``B_ptr``, ``B_idx``, ``B_val``) in the
+    reference's vertex order.
+    """
+    shape: tuple
+    stencil: np.ndarray
+    B_ptr: np.ndarray = field(default_factory=lambda: np.zeros(1, np.int64))
+    B_idx: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
+    B_val: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    Sigma: np.ndarray = field(default_factory=lambda: np.zeros(0))
+
+    @property
+    def dim(self):
+        return len(self.shape)
+
+    @property
+    def m(self):
+        return len(self.B_ptr) - 1
+
+    @property
+    def n(self):
+        return int(np.prod([s - 1 for s in self.shape]))
+
+    @classmethod
+    def shifted_laplace_fd(cls, shape, kappa_sq=None, Lambda=None):
+        """ShiftedLaplaceFDOperator with kappa^2 = 1/Lambda^2 (correlationlength_model.hh:52)."""
+        if kappa_sq is None:
+            kappa_sq = 1.0 / Lambda ** 2
+        return cls(tuple(int(s) for s in shape), fd_stencil(shape, kappa_sq))
+
+    def with_lowrank(self, Bdense_or_cols, Sigma):
+        """Attach B (dense n x m array, or list of (idx, val) columns) and Sigma."""
+        cols = Bdense_or_cols
+        if isinstance(cols, np.ndarray):
+            cols = [(np.nonzero(cols[:, j])[0], cols[np.nonzero(cols[:, j])[0], j]) for j in range(cols.shape[1])]
+        ptr, idx, val = [0], [], []
+        for (i, v) in cols:
+            order = np.argsort(i, kind="stable")
+            idx.extend(np.asarray(i, np.int64)[order].tolist())
+            val.extend(np.asarray(v, np.float64)[order].tolist())
+            ptr.append(len(idx))
+        return LinearOperator(self.shape, self.stencil, np.array(ptr, np.int64), np.array(idx, np.int64),
+                              np.array(val, np.float64), _f64(Sigma))
+
+    def with_measurements(self, locations, variance, variance_scaling=1.0, radius=0.05, measure_global=False,
+                          variance_global=0.0):
+        """MeasuredOperator (measured_operator.cc:9-47)."""
+        locations = np.asarray(locations, np.float64).reshape(-1, self.dim)
+        cols = [measurement_vector(self.shape, x0, radius) for x0 in locations]
+        sigma = list(variance_scaling * np.asarray(variance, np.float64))
+        if measure_global:
+            cv = 1.0
+            for s in self.shape:
+                cv /= float(s)
+            cols.append((np.arange(self.n, dtype=np.int64), np.full(self.n, cv)))
+            sigma.append(variance_global)
+        return self.with_lowrank(cols, sigma)
+
+    def B_dense(self):
+        B = np.zeros((self.n, self.m))
+        for j in range(self.m):
+            B[self.B_idx[self.B_ptr[j]:self.B_ptr[j + 1]], j] = self.B_val[self.B_ptr[j]:self.B_ptr[j + 1]]
+        return B
+
+    def _desc(self):
+        d = _OpDesc()
+        d.dim = self.dim
+        d.nx, d.ny, d.nz = _shape3(self.shape)
+        for k in range(27):
+            d.stencil[k] = float(self.stencil[k])
+        d.m = self.m
+        self._keep = (np.ascontiguousarray(self.B_ptr, np.int64), np.ascontiguousarray(self.B_idx, np.int64),
+                      _f64(self.B_val), _f64(self.Sigma))
+        d.B_colptr = self._keep[0].ctypes.data_as(_I64)
+        d.B_rowidx = self._keep[1].ctypes.data_as(_I64)
+        d.B_val = self._keep[2].ctypes.data_as(_D)
+        d.Sigma = self._keep[3].ctypes.data_as(_D)
+        return d
+
+
+@dataclass
+class MultigridParameters:
+    """MultigridParameters (auxilliary/parameters.hh:150-179)."""
+    nlevel: int = 4
+    smoother: str = "SSOR"
+    coarse_solver: str = "Cholesky"
+    npresmooth: int = 1
+    npostsmooth: int = 1
+    ncoarsesmooth: int = 1
+    omega: float = 1.0
+    cycle: int = 1
+    coarse_scaling: float = 1.0
+
+
+# ------------------------------------------------------------------ sampler
+class MultigridMCSampler:
+    """GPU MultigridMCSampler: the chain state lives on the GPU.
+
+    ``apply(f, x)`` follows Sampler::apply (sampler.hh:52-55): one sample,
+    ``x`` (numpy float64, length n) is updated in place.
+    """
+
+    def __init__(self, linear_operator, params=None, ordering=MULTICOLOUR, precision=FP64, noise=PHILOX,
+                 seed=0, device=0):
+        params = params or MultigridParameters()
+        self.op = linear_operator
+        self.params = params
+        self.n = linear_operator.n
+        p = _Params()
+        p.nlevel = params.nlevel
+        p.smoother = {"SOR": 0, "SSOR": 1}[params.smoother]
+        p.coarse_solver = {"Cholesky": 0, "SSOR": 1}[params.coarse_solver]
+        p.npresmooth, p.npostsmooth, p.ncoarsesmooth = params.npresmooth, params.npostsmooth, params.ncoarsesmooth
+        p.omega = params.omega
+        p.cycle = params.cycle
+        p.coarse_scaling = params.coarse_scaling
+        p.ordering, p.precision, p.noise = ordering, precision, noise
+        p.seed = seed
+        p.device = device
+        self._h = C.c_void_p()
+        desc = linear_operator._desc()
+        self._L = load()
+        _check(self._L.mgmc_sampler_create(C.byref(desc), C.byref(p), C.byref(self._h)))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.mgmc_sampler_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- Sampler surface
+    def apply(self, f, x):
+        f = _f64(f)
+        assert x.dtype == np.float64 and x.flags.c_contiguous and x.size == self.n
+        _check(self._L.mgmc_sampler_apply(self._h, _dp(f), _dp(x), 0))
+        return x
+
+    def fix_rhs(self, f):
+        f = _f64(f)
+        _check(self._L.mgmc_sampler_fix_rhs(self._h, _dp(f), 0))
+
+    def set_state(self, x):
+        x = _f64(x)
+        _check(self._L.mgmc_sampler_set_state(self._h, _dp(x), 0))
+
+    def get_state(self):
+        x = np.zeros(self.n)
+        _check(self._L.mgmc_sampler_get_state(self._h, _dp(x), 0))
+        return x
+
+    def step(self, nsteps=1):
+        _check(self._L.mgmc_sampler_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        _check(self._L.mgmc_sampler_synchronize(self._h))
+
+    @property
+    def stream(self):
+        s = C.c_void_p()
+        _check(self._L.mgmc_sampler_stream(self._h, C.byref(s)))
+        return s.value
+
+    def set_observable(self, idx, val, capacity):
+        idx = np.ascontiguousarray(idx, np.int64)
+        val = _f64(val)
+        _check(self._L.mgmc_sampler_set_observable(self._h, len(idx), idx.ctypes.data_as(_I64), _dp(val),
+                                                   int(capacity)))
+
+    def read_observations(self, capacity):
+        out = np.zeros(max(int(capacity), 1))
+        cnt = C.c_int64(0)
+        _check(self._L.mgmc_sampler_read_observations(self._h, _dp(out), int(capacity), C.byref(cnt)))
+        return out[:min(cnt.value, capacity)]
+
+    def inject_noise(self, normals):
+        normals = _f64(normals)
+        _check(self._L.mgmc_sampler_inject_noise(self._h, _dp(normals), len(normals), 0))
+
+    @property
+    def noise_per_step(self):
+        c = C.c_int64(0)
+        _check(self._L.mgmc_sampler_noise_per_step(self._h, C.byref(c)))
+        return c.value
+
+    @property
+    def nlevel(self):
+        c = C.c_int(0)
+        _check(self._L.mgmc_sampler_nlevel(self._h, C.byref(c)))
+        return c.value
+
+    def level_size(self, level):
+        c = C.c_int64(0)
+        _check(self._L.mgmc_sampler_level_size(self._h, level, C.byref(c)))
+        return c.value
+
+    @property
+    def launches_per_step(self):
+        c = C.c_int64(0)
+        _check(self._L.mgmc_sampler_launches_per_step(self._h, C.byref(c)))
+        return c.value
+
+    # --- level building blocks
+    def level_stencil(self, level):
+        st = np.zeros(27)
+        _check(self._L.mgmc_level_stencil(self._h, level, _dp(st)))
+        return st
+
+    def level_apply(self, level, x):
+        x = _f64(x)
+        y = np.zeros(self.level_size(level))
+        _check(self._L.mgmc_level_apply(self._h, level, _dp(x), _dp(y)))
+        return y
+
+    def restrict(self, level, x):
+        x = _f64(x)
+        xc = np.zeros(self.level_size(level + 1))
+        _check(self._L.mgmc_level_restrict(self._h, level, _dp(x), _dp(xc)))
+        return xc
+
+    def prolongate_add(self, level, alpha, xc, x):
+        xc = _f64(xc)
+        assert x.dtype == np.float64 and x.flags.c_contiguous
+        _check(self._L.mgmc_level_prolongate_add(self._h, level, float(alpha), _dp(xc), _dp(x)))
+        return x
+
+    def sor(self, level, direction, f, x, with_noise=True):
+        f = _f64(f)
+        assert x.dtype == np.float64 and x.flags.c_contiguous
+        _check(self._L.mgmc_level_sor(self._h, level, direction, int(with_noise), _dp(f), _dp(x)))
+        return x
+
+
+def SSORSampler(linear_operator, omega=1.0, nsmooth=1, **kw):
+    """SSORSampler (ssor_sampler.hh:29-37): a one-level hierarchy whose
+    coarse solver is SSOR with `nsmooth` forward/backward pairs."""
+    p = MultigridParameters(nlevel=1, coarse_solver="SSOR", ncoarsesmooth=nsmooth, omega=omega)
+    return MultigridMCSampler(linear_operator, p, **kw)
+
+
+def CholeskySampler(linear_operator, **kw):
+    """Exact sampler with the dense natural-order Cholesky factor
+    (DenseCholeskySampler, cholesky_sampler.cc:25-37)."""
+    p = MultigridParameters(nlevel=1, coarse_solver="Cholesky")
+    return MultigridMCSampler(linear_operator, p, **kw)

@@ -1,0 +1,1179 @@
+// api.cu -- C ABI, hierarchy set-up and step orchestration of the GB300
+// Multigrid Monte Carlo sampler.
+//
+// One mgmc_sampler owns one chain: the level hierarchy (stencils, B, the
+// low-rank factors C = M^{-1} B, the coarse Cholesky factor) and the chain
+// state stay resident in device memory; a step is a fixed sequence of
+// kernel launches on the sampler's stream, captured once into a CUDA graph
+// when the noise comes from the in-kernel Philox generator.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/mgmc_gb300.h"
+#include "kernels.cuh"
+#include "setup.h"
+
+namespace mgmc {
+
+static thread_local std::string g_err;
+
+struct Error {
+    mgmc_status st;
+    std::string msg;
+};
+
+#define CK(call)                                                                                         \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess)                                                                           \
+            throw Error{e_ == cudaErrorMemoryAllocation ? MGMC_ERR_OUT_OF_MEMORY : MGMC_ERR_CUDA,          \
+                        std::string(#call) + ": " + cudaGetErrorString(e_)};                           \
+    } while (0)
+
+static void fail(mgmc_status st, const std::string &msg) { throw Error{st, msg}; }
+
+template <typename P>
+static P *dalloc(size_t count) {
+    void *p = nullptr;
+    if (count == 0) count = 1;
+    CK(cudaMalloc(&p, count * sizeof(P)));
+    return (P *)p;
+}
+
+template <typename P>
+static P *dupload(const std::vector<P> &v, cudaStream_t s) {
+    P *p = dalloc<P>(v.size());
+    if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(P), cudaMemcpyHostToDevice, s));
+    return p;
+}
+
+static inline unsigned nblk(i64 n, int bs) { return (unsigned)std::max<i64>(1, (n + bs - 1) / bs); }
+
+// Row-compressed sparse n x m matrix over its support rows (padded indices).
+struct RowCsr {
+    i64 nrows = 0;
+    i64 *rows = nullptr, *ptr = nullptr;
+    int *col = nullptr;
+    void *val = nullptr;  // T for C, double for B
+};
+
+struct Level {
+    Geometry geo;
+    Grid3 g;
+    double st[27];
+    int ncol = 2, npt = 7;
+    double diag = 0, sd = 0;
+    void *x = nullptr, *f = nullptr;    // state and right hand side (T, padded)
+    void *s1 = nullptr, *s2 = nullptr;  // scratch for the building-block calls
+    SparseCols Bh;                      // B on this level (compact indices)
+    i64 *Bptr = nullptr, *Bidx = nullptr;
+    double *Bval = nullptr;
+    RowCsr Br;          // B by rows (double values)
+    RowCsr C[2];        // C = M^{-1} B, forward / backward (T values)
+    double *Sinv[2] = {nullptr, nullptr}, *G[2] = {nullptr, nullptr};
+    double *y = nullptr, *z = nullptr;
+    unsigned *counter = nullptr;
+};
+
+struct Sampler {
+    mgmc_sampler_params P;
+    int dim = 3, m = 0;
+    bool fp32 = false, exact = false;
+    int noise_mode = NOISE_PHILOX;
+    std::vector<Level> L;
+    std::vector<double> Sigma;
+    double *d_sigma_inv = nullptr, *d_sinv_sqrt = nullptr;
+    // coarse Cholesky
+    bool chol = false;
+    double *dL = nullptr, *dLinv = nullptr, *dLinvT = nullptr, *dgv = nullptr;
+    size_t chol_smem = 0;
+    // bookkeeping
+    cudaStream_t stream = nullptr;
+    u64 *d_step = nullptr, *d_obs_count = nullptr;
+    unsigned *d_err = nullptr;
+    double *d_obs = nullptr;
+    i64 obs_cap = 0, nb = 0;
+    i64 *d_bidx = nullptr;
+    double *d_bval = nullptr;
+    double *d_cvec = nullptr;  // compact n_0 doubles for transfers
+    // injected noise queue
+    double *d_noise = nullptr;
+    i64 noise_cap = 0, noise_len = 0, noise_pos = 0, noise_per_step = 0;
+    // step construction
+    unsigned inv = 0;
+    i64 noise_off = 0;
+    i64 launches = 0;
+    bool counting = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<void *> owned;  // every device allocation
+
+    template <typename P_>
+    P_ *alloc(size_t count) {
+        P_ *p = dalloc<P_>(count);
+        owned.push_back(p);
+        return p;
+    }
+    template <typename P_>
+    P_ *upload(const std::vector<P_> &v) {
+        P_ *p = dupload(v, stream);
+        owned.push_back(p);
+        return p;
+    }
+    size_t tsize() const { return fp32 ? sizeof(float) : sizeof(double); }
+    void *talloc(i64 count) {
+        void *p = alloc<char>((size_t)count * tsize());
+        CK(cudaMemsetAsync(p, 0, (size_t)count * tsize(), stream));
+        return p;
+    }
+    ~Sampler() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        for (void *p : owned) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    void build(const mgmc_operator_desc &op);
+    void build_lowrank(int lev);
+    void build_coarse();
+    void launch_step();
+    void sor(int lev, bool forward, bool noisy, void *x, void *f);
+    void sample(int lev);
+    void coarse_sample(int lev);
+    void resid_restrict(int lev);
+    void prolong(int lev, double alpha, void *xc, void *x);
+    void step_end();
+    void ensure_scratch(int lev);
+    void check_launch();
+    NoiseArgs noise_args(int lev, i64 count);
+};
+
+template <typename T>
+static StencilArg<T> stencil_arg(const Level &lv, double omega) {
+    StencilArg<T> s;
+    for (int k = 0; k < 27; ++k) s.w[k] = (T)lv.st[k];
+    s.diag = (T)lv.diag;
+    s.omega = (T)omega;
+    s.sd = (T)lv.sd;
+    s.omega_diag = (T)(omega / lv.diag);
+    return s;
+}
+
+void Sampler::check_launch() {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) fail(MGMC_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+}
+
+NoiseArgs Sampler::noise_args(int lev, i64 count) {
+    NoiseArgs nz;
+    nz.buf = nullptr;
+    nz.seed = P.seed;
+    nz.d_step = d_step;
+    nz.invocation = inv;
+    nz.level = (unsigned)lev;
+    if (noise_mode == NOISE_INJECTED) {
+        nz.buf = d_noise + noise_off;
+        noise_off += count;
+    }
+    return nz;
+}
+
+// ----------------------------------------------------------- sweep launch
+template <typename T, int NPT, bool EXACT, int NOISE>
+static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, const T *f, const NoiseArgs &nz) {
+    StencilArg<T> s = stencil_arg<T>(lv, S.P.omega);
+    if (S.P.ordering == MGMC_ORDER_LEXICOGRAPHIC) {
+        int hb = lv.ncol == 2 ? 1 : 2, hc = lv.ncol == 2 ? 1 : 4;
+        k_sweep_wavefront<T, NPT, EXACT, NOISE><<<1, 1024, 0, S.stream>>>(x, f, lv.g, s, forward ? 1 : 0, hb, hc, nz);
+        S.launches++;
+    } else {
+        const i64 G0 = (lv.g.N0 + 7) / 8;
+        for (int cc = 0; cc < lv.ncol; ++cc) {
+            int colour = forward ? cc : lv.ncol - 1 - cc;
+            i64 rows = (lv.ncol == 2) ? (i64)lv.g.N1 * lv.g.N2
+                                      : (i64)((lv.g.N1 - ((colour >> 1) & 1) + 1) / 2) * ((lv.g.N2 - ((colour >> 2) & 1) + 1) / 2);
+            if (rows <= 0) continue;
+            k_sweep_colour<T, NPT, EXACT, NOISE><<<nblk(G0 * rows, 256), 256, 0, S.stream>>>(x, f, lv.g, s, colour, lv.ncol, nz);
+            S.launches++;
+        }
+    }
+}
+
+template <typename T, bool EXACT, int NOISE>
+static void launch_sweep_npt(Sampler &S, const Level &lv, bool forward, T *x, const T *f, const NoiseArgs &nz) {
+    if (lv.npt == 7)
+        launch_sweep_t<T, 7, EXACT, NOISE>(S, lv, forward, x, f, nz);
+    else
+        launch_sweep_t<T, 27, EXACT, NOISE>(S, lv, forward, x, f, nz);
+}
+
+template <typename T, bool EXACT>
+static void launch_sweep_noise(Sampler &S, const Level &lv, bool forward, int noise, T *x, const T *f, const NoiseArgs &nz) {
+    if (noise == NOISE_NONE)
+        launch_sweep_npt<T, EXACT, NOISE_NONE>(S, lv, forward, x, f, nz);
+    else if (noise == NOISE_PHILOX)
+        launch_sweep_npt<T, EXACT, NOISE_PHILOX>(S, lv, forward, x, f, nz);
+    else
+        launch_sweep_npt<T, EXACT, NOISE_INJECTED>(S, lv, forward, x, f, nz);
+}
+
+static void launch_sweep(Sampler &S, const Level &lv, bool forward, int noise, void *x, const void *f, const NoiseArgs &nz,
+                         bool fp32, bool exact) {
+    if (fp32)
+        launch_sweep_noise<float, false>(S, lv, forward, noise, (float *)x, (const float *)f, nz);
+    else if (exact)
+        launch_sweep_noise<double, true>(S, lv, forward, noise, (double *)x, (const double *)f, nz);
+    else
+        launch_sweep_noise<double, false>(S, lv, forward, noise, (double *)x, (const double *)f, nz);
+}
+
+template <typename T>
+static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, const NoiseArgs &nz) {
+    LowRankArg lr;
+    lr.m = S.m;
+    lr.Bptr = lv.Bptr;
+    lr.Bidx = lv.Bidx;
+    lr.Bval = lv.Bval;
+    lr.Sinv = lv.Sinv[dir];
+    lr.G = lv.G[dir];
+    lr.sinv_sqrt = S.d_sinv_sqrt;
+    lr.y = lv.y;
+    lr.z = lv.z;
+    lr.counter = lv.counter;
+    size_t smem = 2 * sizeof(double) * S.m;
+    if (noise == NOISE_NONE)
+        k_bt_x_z<T, NOISE_NONE, true><<<S.m, 256, smem, S.stream>>>(x, lr, nz);
+    else if (noise == NOISE_PHILOX)
+        k_bt_x_z<T, NOISE_PHILOX, true><<<S.m, 256, smem, S.stream>>>(x, lr, nz);
+    else
+        k_bt_x_z<T, NOISE_INJECTED, true><<<S.m, 256, smem, S.stream>>>(x, lr, nz);
+    const RowCsr &C = lv.C[dir];
+    if (C.nrows > 0)
+        k_lr_scatter<T><<<nblk(C.nrows, 256), 256, 0, S.stream>>>(x, C.nrows, C.rows, C.ptr, C.col, (const T *)C.val, lv.z);
+    S.launches += 2;
+}
+
+// SORSampler::apply (sor_sampler.cc:37-59) / SORSmoother::apply
+// (sor_smoother.cc:40-54) on level `lev`: noise draw order n point normals,
+// then m low-rank normals.
+void Sampler::sor(int lev, bool forward, bool noisy, void *x, void *f) {
+    Level &lv = L[lev];
+    int noise = noisy ? noise_mode : NOISE_NONE;
+    NoiseArgs nz = noisy ? noise_args(lev, lv.geo.n) : noise_args(lev, 0);
+    if (!noisy) nz.buf = nullptr;
+    launch_sweep(*this, lv, forward, noise, x, f, nz, fp32, exact);
+    if (m > 0) {
+        NoiseArgs nzl = noisy ? noise_args(lev, m) : noise_args(lev, 0);
+        if (!noisy) nzl.buf = nullptr;
+        if (fp32)
+            launch_lowrank<float>(*this, lv, forward ? 0 : 1, noise, (float *)x, nzl);
+        else
+            launch_lowrank<double>(*this, lv, forward ? 0 : 1, noise, (double *)x, nzl);
+    }
+    if (noisy) inv++;
+}
+
+template <typename T>
+static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void *f, void *fc, bool zero_stencil) {
+    Level &lv = S.L[lev], &lc = S.L[lev + 1];
+    StencilArg<T> s = stencil_arg<T>(lv, S.P.omega);
+    if (zero_stencil)
+        for (int k = 0; k < 27; ++k) s.w[k] = T(0);
+    const i64 nc = lc.geo.n;
+    if (lv.npt == 7 && !zero_stencil)
+        k_resid_restrict<T, 7><<<nblk(nc, 256), 256, 0, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, S.dim);
+    else
+        k_resid_restrict<T, 27><<<nblk(nc, 256), 256, 0, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, S.dim);
+    S.launches++;
+}
+
+template <typename T>
+static void launch_bt_plain(Sampler &S, Level &lv, const void *x) {
+    LowRankArg lr{};
+    lr.m = S.m;
+    lr.Bptr = lv.Bptr;
+    lr.Bidx = lv.Bidx;
+    lr.Bval = lv.Bval;
+    lr.y = lv.y;
+    NoiseArgs nz{};
+    k_bt_x_z<T, NOISE_NONE, false><<<S.m, 256, 0, S.stream>>>((const T *)x, lr, nz);
+    S.launches++;
+}
+
+template <typename T>
+static void launch_add_Bq(Sampler &S, Level &lv, void *dst, const double *y, double sign) {
+    const RowCsr &B = lv.Br;
+    if (B.nrows == 0) return;
+    k_add_Bq<T><<<nblk(B.nrows, 256), 256, 0, S.stream>>>((T *)dst, B.nrows, B.rows, B.ptr, B.col, (const double *)B.val, y,
+                                                          S.d_sigma_inv, sign);
+    S.launches++;
+}
+
+// residual f - A x of multigridmc_sampler.cc:124-125 restricted to the
+// next level (:126): R (f - A_0 x) - B_c Sigma^{-1} B^T x.
+void Sampler::resid_restrict(int lev) {
+    Level &lv = L[lev], &lc = L[lev + 1];
+    if (fp32) {
+        launch_resid_restrict<float>(*this, lev, lv.x, lv.f, lc.f, false);
+        if (m > 0) {
+            launch_bt_plain<float>(*this, lv, lv.x);
+            launch_add_Bq<float>(*this, lc, lc.f, lv.y, -1.0);
+        }
+    } else {
+        launch_resid_restrict<double>(*this, lev, lv.x, lv.f, lc.f, false);
+        if (m > 0) {
+            launch_bt_plain<double>(*this, lv, lv.x);
+            launch_add_Bq<double>(*this, lc, lc.f, lv.y, -1.0);
+        }
+    }
+}
+
+void Sampler::prolong(int lev, double alpha, void *xc, void *x) {
+    Level &lv = L[lev], &lc = L[lev + 1];
+    if (fp32)
+        k_prolong_add<float><<<nblk(lv.geo.n, 256), 256, 0, stream>>>((float *)x, (const float *)xc, lv.g, lc.g, (float)alpha, dim);
+    else
+        k_prolong_add<double><<<nblk(lv.geo.n, 256), 256, 0, stream>>>((double *)x, (const double *)xc, lv.g, lc.g, alpha, dim);
+    launches++;
+}
+
+template <typename T, int NOISE>
+static void launch_chol(Sampler &S, Level &lv, const NoiseArgs &nz) {
+    if (S.exact) {
+        k_chol_subst<T, NOISE><<<1, 1024, 0, S.stream>>>((const T *)lv.f, (T *)lv.x, lv.g, S.dL, S.dgv, nz);
+        S.launches++;
+    } else {
+        const i64 n = lv.geo.n;
+        unsigned blocks = (unsigned)std::min<i64>(4 * 152, (n + 7) / 8);
+        k_chol_gemv_lower<T, NOISE><<<blocks, 256, S.chol_smem, S.stream>>>((const T *)lv.f, lv.g, S.dLinv, S.dgv, nz);
+        k_chol_gemv_upper<T><<<blocks, 256, S.chol_smem, S.stream>>>(S.dgv, lv.g, S.dLinvT, (T *)lv.x);
+        S.launches += 2;
+    }
+}
+
+// coarsest level: CholeskySampler::apply or SSORSampler with ncoarsesmooth
+// (multigridmc_sampler.cc:54-79, 112-116)
+void Sampler::coarse_sample(int lev) {
+    Level &lv = L[lev];
+    if (chol) {
+        NoiseArgs nz = noise_args(lev, lv.geo.n);
+        if (fp32) {
+            if (noise_mode == NOISE_PHILOX)
+                launch_chol<float, NOISE_PHILOX>(*this, lv, nz);
+            else
+                launch_chol<float, NOISE_INJECTED>(*this, lv, nz);
+        } else {
+            if (noise_mode == NOISE_PHILOX)
+                launch_chol<double, NOISE_PHILOX>(*this, lv, nz);
+            else
+                launch_chol<double, NOISE_INJECTED>(*this, lv, nz);
+        }
+        inv++;
+    } else {
+        for (int k = 0; k < P.ncoarsesmooth; ++k) {
+            sor(lev, true, true, lv.x, lv.f);
+            sor(lev, false, true, lv.x, lv.f);
+        }
+    }
+}
+
+// MultigridMCSampler::sample (multigridmc_sampler.cc:109-136)
+void Sampler::sample(int lev) {
+    const int nlev = (int)L.size();
+    if (lev == nlev - 1) {
+        coarse_sample(lev);
+        return;
+    }
+    Level &lv = L[lev], &lc = L[lev + 1];
+    const int cyc = lev > 0 ? P.cycle : 1;
+    for (int j = 0; j < cyc; ++j) {
+        if (P.smoother == MGMC_SMOOTHER_SSOR) {
+            for (int k = 0; k < P.npresmooth; ++k) {
+                sor(lev, true, true, lv.x, lv.f);
+                sor(lev, false, true, lv.x, lv.f);
+            }
+        } else {
+            for (int k = 0; k < P.npresmooth; ++k) sor(lev, true, true, lv.x, lv.f);
+        }
+        resid_restrict(lev);
+        CK(cudaMemsetAsync(lc.x, 0, (size_t)lc.geo.nalloc * tsize(), stream));
+        sample(lev + 1);
+        prolong(lev, P.coarse_scaling, lc.x, lv.x);
+        if (P.smoother == MGMC_SMOOTHER_SSOR) {
+            for (int k = 0; k < P.npostsmooth; ++k) {
+                sor(lev, true, true, lv.x, lv.f);
+                sor(lev, false, true, lv.x, lv.f);
+            }
+        } else {
+            for (int k = 0; k < P.npostsmooth; ++k) sor(lev, false, true, lv.x, lv.f);
+        }
+    }
+}
+
+void Sampler::step_end() {
+    if (fp32)
+        k_step_end<float><<<1, 256, 0, stream>>>((const float *)L[0].x, nb, d_bidx, d_bval, d_obs, obs_cap, d_obs_count, d_step, d_err);
+    else
+        k_step_end<double><<<1, 256, 0, stream>>>((const double *)L[0].x, nb, d_bidx, d_bval, d_obs, obs_cap, d_obs_count, d_step, d_err);
+    launches++;
+}
+
+void Sampler::launch_step() {
+    inv = 0;
+    noise_off = noise_pos;
+    launches = 0;
+    sample(0);
+    step_end();
+}
+
+// ------------------------------------------------------------- set-up
+static int stencil_npt(int ncol, const double st[27]) {
+    if (ncol != 2) return 27;
+    for (int k = 0; k < 27; ++k) {
+        int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+        if ((dx != 0) + (dy != 0) + (dz != 0) > 1 && st[k] != 0.0) return 27;
+    }
+    return 7;
+}
+
+__global__ void k_scatter(const i64 *__restrict__ idx, const double *__restrict__ val, i64 cnt, double *__restrict__ dst) {
+    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < cnt) dst[idx[t]] = val[t];
+}
+
+__global__ void k_nonzeros(const double *__restrict__ x, Grid3 g, i64 *__restrict__ idx, double *__restrict__ val,
+                           unsigned long long *__restrict__ count) {
+    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    i64 n = (i64)g.N0 * g.N1 * g.N2;
+    if (t >= n) return;
+    int a = (int)(t % g.N0), b = (int)((t / g.N0) % g.N1), c = (int)(t / ((i64)g.N0 * g.N1));
+    double v = x[g.pad(a, b, c)];
+    if (v != 0.0) {
+        unsigned long long k = atomicAdd(count, 1ull);
+        idx[k] = t;
+        val[k] = v;
+    }
+}
+
+// C = M^{-1} B for both sweep directions, M = D/omega + (strictly lower
+// part of A_0 in the sweep order): column j is one noise-free sweep from
+// x = 0 with right hand side B e_j (sor_smoother.cc:17-37 in solve form).
+// S = Sigma + B^T C and G = B^T C feed k_bt_x_z.
+void Sampler::build_lowrank(int lev) {
+    Level &lv = L[lev];
+    const Geometry &geo = lv.geo;
+    const i64 n = geo.n;
+    // B on this level: CSC with padded indices, and row-compressed form
+    {
+        std::vector<i64> bidx(lv.Bh.row.size());
+        for (size_t e = 0; e < bidx.size(); ++e) bidx[e] = geo.pad(lv.Bh.row[e]);
+        std::vector<i64> bptr(lv.Bh.ptr.begin(), lv.Bh.ptr.end());
+        lv.Bptr = upload(bptr);
+        lv.Bidx = upload(bidx);
+        lv.Bval = upload(lv.Bh.val);
+        std::vector<std::tuple<i64, int, double>> trip;
+        for (int j = 0; j < m; ++j)
+            for (i64 e = lv.Bh.ptr[j]; e < lv.Bh.ptr[j + 1]; ++e) trip.emplace_back(lv.Bh.row[e], j, lv.Bh.val[e]);
+        std::sort(trip.begin(), trip.end());
+        std::vector<i64> rows, ptr{0};
+        std::vector<int> col;
+        std::vector<double> val;
+        for (size_t e = 0; e < trip.size(); ++e) {
+            if (e == 0 || std::get<0>(trip[e]) != std::get<0>(trip[e - 1])) {
+                if (e > 0) ptr.push_back((i64)col.size());
+                rows.push_back(geo.pad(std::get<0>(trip[e])));
+            }
+            col.push_back(std::get<1>(trip[e]));
+            val.push_back(std::get<2>(trip[e]));
+        }
+        if (!trip.empty()) ptr.push_back((i64)col.size());
+        lv.Br.nrows = (i64)rows.size();
+        lv.Br.rows = upload(rows);
+        lv.Br.ptr = upload(ptr);
+        lv.Br.col = upload(col);
+        lv.Br.val = upload(val);
+    }
+    lv.y = alloc<double>(m);
+    lv.z = alloc<double>(m);
+    lv.counter = alloc<unsigned>(1);
+    CK(cudaMemsetAsync(lv.counter, 0, sizeof(unsigned), stream));
+    // FP64 work arrays
+    double *xs = alloc<double>(geo.nalloc), *fs = alloc<double>(geo.nalloc);
+    i64 *nzi = alloc<i64>(n);
+    double *nzv = alloc<double>(n);
+    unsigned long long *cnt = alloc<unsigned long long>(1);
+    std::vector<double> yh(m);
+    for (int dir = 0; dir < 2; ++dir) {
+        std::vector<std::tuple<i64, int, double>> trip;
+        std::vector<double> Sh((size_t)m * m), Gh((size_t)m * m);
+        for (int j = 0; j < m; ++j) {
+            CK(cudaMemsetAsync(xs, 0, geo.nalloc * sizeof(double), stream));
+            CK(cudaMemsetAsync(fs, 0, geo.nalloc * sizeof(double), stream));
+            const i64 b0 = lv.Bh.ptr[j], cntj = lv.Bh.ptr[j + 1] - lv.Bh.ptr[j];
+            if (cntj > 0) k_scatter<<<nblk(cntj, 256), 256, 0, stream>>>(lv.Bidx + b0, lv.Bval + b0, cntj, fs);
+            NoiseArgs nz{};
+            nz.d_step = d_step;
+            launch_sweep(*this, lv, dir == 0, NOISE_NONE, xs, fs, nz, false, exact);
+            // G[:, j] = B^T C e_j
+            LowRankArg lr{};
+            lr.m = m;
+            lr.Bptr = lv.Bptr;
+            lr.Bidx = lv.Bidx;
+            lr.Bval = lv.Bval;
+            lr.y = lv.y;
+            k_bt_x_z<double, NOISE_NONE, false><<<m, 256, 0, stream>>>(xs, lr, nz);
+            CK(cudaMemcpyAsync(yh.data(), lv.y, m * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), stream));
+            k_nonzeros<<<nblk(n, 256), 256, 0, stream>>>(xs, lv.g, nzi, nzv, cnt);
+            unsigned long long hc = 0;
+            CK(cudaMemcpyAsync(&hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+            check_launch();
+            std::vector<i64> ii(hc);
+            std::vector<double> vv(hc);
+            if (hc) {
+                CK(cudaMemcpy(ii.data(), nzi, hc * sizeof(i64), cudaMemcpyDeviceToHost));
+                CK(cudaMemcpy(vv.data(), nzv, hc * sizeof(double), cudaMemcpyDeviceToHost));
+            }
+            for (unsigned long long e = 0; e < hc; ++e) trip.emplace_back(ii[e], j, vv[e]);
+            for (int a = 0; a < m; ++a) {
+                Gh[(size_t)a * m + j] = yh[a];
+                Sh[(size_t)a * m + j] = yh[a] + (a == j ? Sigma[a] : 0.0);
+            }
+        }
+        std::sort(trip.begin(), trip.end());
+        std::vector<i64> rows, ptr{0};
+        std::vector<int> col;
+        std::vector<double> val;
+        for (size_t e = 0; e < trip.size(); ++e) {
+            if (e == 0 || std::get<0>(trip[e]) != std::get<0>(trip[e - 1])) {
+                if (e > 0) ptr.push_back((i64)col.size());
+                rows.push_back(geo.pad(std::get<0>(trip[e])));
+            }
+            col.push_back(std::get<1>(trip[e]));
+            val.push_back(std::get<2>(trip[e]));
+        }
+        if (!trip.empty()) ptr.push_back((i64)col.size());
+        RowCsr &C = lv.C[dir];
+        C.nrows = (i64)rows.size();
+        C.rows = upload(rows);
+        C.ptr = upload(ptr);
+        C.col = upload(col);
+        if (fp32) {
+            std::vector<float> vf(val.begin(), val.end());
+            C.val = upload(vf);
+        } else {
+            C.val = upload(val);
+        }
+        lv.Sinv[dir] = upload(small_inverse(Sh, m));
+        lv.G[dir] = upload(Gh);
+    }
+    CK(cudaStreamSynchronize(stream));
+}
+
+void Sampler::build_coarse() {
+    Level &lv = L.back();
+    const i64 n = lv.geo.n;
+    if (n > 12000) fail(MGMC_ERR_UNSUPPORTED, "coarse level has " + std::to_string(n) + " unknowns; the dense Cholesky sampler takes at most 12000");
+    std::vector<double> Q = dense_precision(lv.geo, lv.st, lv.Bh, Sigma);
+    if (!dense_cholesky(Q, n)) fail(MGMC_ERR_NOT_SPD, "coarse precision matrix is not positive definite");
+    dgv = alloc<double>(n);
+    chol_smem = (size_t)n * sizeof(double);
+    if (exact) {
+        dL = upload(Q);
+    } else {
+        std::vector<double> T = inverse_factor_transposed(Q, n);  // (L^{-1})^T
+        std::vector<double> Li((size_t)n * n);
+        for (i64 i = 0; i < n; ++i)
+            for (i64 j = 0; j < n; ++j) Li[(size_t)i * n + j] = T[(size_t)j * n + i];
+        dLinvT = upload(T);
+        dLinv = upload(Li);
+        if (chol_smem > 48 * 1024) {
+            CK(cudaFuncSetAttribute(k_chol_gemv_lower<float, NOISE_PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
+            CK(cudaFuncSetAttribute(k_chol_gemv_lower<double, NOISE_PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
+            CK(cudaFuncSetAttribute(k_chol_gemv_lower<float, NOISE_INJECTED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
+            CK(cudaFuncSetAttribute(k_chol_gemv_lower<double, NOISE_INJECTED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
+            CK(cudaFuncSetAttribute(k_chol_gemv_upper<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
+            CK(cudaFuncSetAttribute(k_chol_gemv_upper<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
+        }
+    }
+}
+
+void Sampler::build(const mgmc_operator_desc &op) {
+    if (op.dim < 1 || op.dim > 3) fail(MGMC_ERR_INVALID_ARGUMENT, "dim must be 1, 2 or 3");
+    dim = op.dim;
+    int cells[3] = {op.nx, op.dim > 1 ? op.ny : 2, op.dim > 2 ? op.nz : 2};
+    for (int d = 0; d < dim; ++d)
+        if (cells[d] < 2) fail(MGMC_ERR_LATTICE, "every active direction needs at least 2 cells");
+    if (P.nlevel < 1) fail(MGMC_ERR_INVALID_ARGUMENT, "nlevel must be >= 1");
+    if (P.smoother != MGMC_SMOOTHER_SOR && P.smoother != MGMC_SMOOTHER_SSOR) fail(MGMC_ERR_INVALID_ARGUMENT, "invalid smoother");
+    if (P.coarse_solver != MGMC_COARSE_CHOLESKY && P.coarse_solver != MGMC_COARSE_SSOR) fail(MGMC_ERR_INVALID_ARGUMENT, "invalid coarse solver");
+    if (P.ordering != MGMC_ORDER_LEXICOGRAPHIC && P.ordering != MGMC_ORDER_MULTICOLOUR) fail(MGMC_ERR_INVALID_ARGUMENT, "invalid ordering");
+    if (P.precision != MGMC_FP64 && P.precision != MGMC_FP32_MIXED) fail(MGMC_ERR_INVALID_ARGUMENT, "invalid precision");
+    if (P.noise != MGMC_NOISE_PHILOX && P.noise != MGMC_NOISE_INJECTED) fail(MGMC_ERR_INVALID_ARGUMENT, "invalid noise source");
+    if (!(P.omega > 0.0 && P.omega < 2.0)) fail(MGMC_ERR_INVALID_ARGUMENT, "omega must lie in (0, 2)");
+    if (P.cycle < 1 || P.npresmooth < 0 || P.npostsmooth < 0 || P.ncoarsesmooth < 0)
+        fail(MGMC_ERR_INVALID_ARGUMENT, "cycle >= 1 and non-negative smoothing counts required");
+    if (op.m < 0 || (op.m > 0 && (!op.B_colptr || !op.B_rowidx || !op.B_val || !op.Sigma)))
+        fail(MGMC_ERR_INVALID_ARGUMENT, "low-rank term needs B and Sigma");
+    if (op.m > 3072) fail(MGMC_ERR_UNSUPPORTED, "at most 3072 measurement columns");
+    fp32 = P.precision == MGMC_FP32_MIXED;
+    noise_mode = P.noise == MGMC_NOISE_INJECTED ? NOISE_INJECTED : NOISE_PHILOX;
+    exact = !fp32 && noise_mode == NOISE_INJECTED;
+    chol = P.coarse_solver == MGMC_COARSE_CHOLESKY;
+    m = op.m;
+    CK(cudaSetDevice(P.device));
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    d_step = alloc<u64>(1);
+    d_obs_count = alloc<u64>(1);
+    d_err = alloc<unsigned>(1);
+    CK(cudaMemsetAsync(d_step, 0, sizeof(u64), stream));
+    CK(cudaMemsetAsync(d_obs_count, 0, sizeof(u64), stream));
+    CK(cudaMemsetAsync(d_err, 0, sizeof(unsigned), stream));
+    // levels
+    Geometry geo(dim, cells[0], cells[1], cells[2]);
+    double st[27];
+    std::memcpy(st, op.stencil, sizeof(st));
+    for (int lev = 0; lev < P.nlevel; ++lev) {
+        if (lev > 0) {
+            if (!geo.coarsenable())
+                fail(MGMC_ERR_LATTICE, "cannot coarsen lattice level " + std::to_string(lev - 1) + " [odd extent or no interior vertices left]");
+            geo = geo.coarse();
+            double stc[27];
+            galerkin_stencil(dim, st, stc);
+            std::memcpy(st, stc, sizeof(st));
+        }
+        Level lv;
+        lv.geo = geo;
+        lv.g.N0 = geo.N[0];
+        lv.g.N1 = geo.N[1];
+        lv.g.N2 = geo.N[2];
+        lv.g.sy = geo.sy;
+        lv.g.sz = geo.sz;
+        std::memcpy(lv.st, st, sizeof(st));
+        lv.diag = st[13];
+        if (!(lv.diag > 0.0)) fail(MGMC_ERR_NOT_SPD, "stencil diagonal must be positive");
+        lv.sd = std::sqrt(lv.diag * (2. - P.omega) / P.omega);
+        lv.ncol = colour_count(dim, st);
+        lv.npt = stencil_npt(lv.ncol, st);
+        L.push_back(lv);
+    }
+    for (auto &lv : L) {
+        lv.x = talloc(lv.geo.nalloc);
+        lv.f = talloc(lv.geo.nalloc);
+    }
+    d_cvec = alloc<double>(L[0].geo.n);
+    // low-rank term on every level: B_{l+1} = R B_l
+    if (m > 0) {
+        SparseCols B;
+        B.m = m;
+        B.ptr.assign(op.B_colptr, op.B_colptr + m + 1);
+        for (int j = 0; j < m; ++j) {
+            for (i64 e = op.B_colptr[j]; e < op.B_colptr[j + 1]; ++e) {
+                if (op.B_rowidx[e] < 0 || op.B_rowidx[e] >= L[0].geo.n) fail(MGMC_ERR_INVALID_ARGUMENT, "B row index out of range");
+                if (e > op.B_colptr[j] && op.B_rowidx[e] <= op.B_rowidx[e - 1]) fail(MGMC_ERR_INVALID_ARGUMENT, "B row indices must ascend within a column");
+            }
+        }
+        B.row.assign(op.B_rowidx, op.B_rowidx + op.B_colptr[m]);
+        B.val.assign(op.B_val, op.B_val + op.B_colptr[m]);
+        Sigma.assign(op.Sigma, op.Sigma + m);
+        for (double s : Sigma)
+            if (!(s > 0.0)) fail(MGMC_ERR_INVALID_ARGUMENT, "Sigma entries must be positive");
+        L[0].Bh = B;
+        for (size_t lev = 1; lev < L.size(); ++lev) L[lev].Bh = restrict_columns(L[lev - 1].geo, L[lev - 1].Bh);
+        std::vector<double> si(m), ss(m);
+        for (int j = 0; j < m; ++j) {
+            si[j] = 1.0 / Sigma[j];
+            ss[j] = std::sqrt(1.0 / Sigma[j]);  // Sigma^{-1/2} (sor_sampler.cc:29-33)
+        }
+        d_sigma_inv = upload(si);
+        d_sinv_sqrt = upload(ss);
+        for (size_t lev = 0; lev < L.size(); ++lev) build_lowrank((int)lev);
+    }
+    if (chol) build_coarse();
+    // noise per step (dry count)
+    noise_per_step = 0;
+    {
+        counting = true;
+        i64 off0 = noise_off;
+        noise_off = 0;
+        // count without launching: replicate the recursion on the host
+        std::function<void(int)> cnt = [&](int lev) {
+            const int nlev = (int)L.size();
+            const i64 per_sor = L[lev].geo.n + m;
+            if (lev == nlev - 1) {
+                noise_per_step += chol ? L[lev].geo.n : 2 * P.ncoarsesmooth * per_sor;
+                return;
+            }
+            const int cyc = lev > 0 ? P.cycle : 1;
+            for (int j = 0; j < cyc; ++j) {
+                noise_per_step += (P.smoother == MGMC_SMOOTHER_SSOR ? 2 : 1) * (i64)P.npresmooth * per_sor;
+                cnt(lev + 1);
+                noise_per_step += (P.smoother == MGMC_SMOOTHER_SSOR ? 2 : 1) * (i64)P.npostsmooth * per_sor;
+            }
+        };
+        cnt(0);
+        noise_off = off0;
+        counting = false;
+    }
+    CK(cudaStreamSynchronize(stream));
+    check_launch();
+}
+
+void Sampler::ensure_scratch(int lev) {
+    Level &lv = L[lev];
+    if (!lv.s1) lv.s1 = talloc(lv.geo.nalloc);
+    if (!lv.s2) lv.s2 = talloc(lv.geo.nalloc);
+}
+
+// host / device compact FP64 vector -> padded T array of level lev
+static void put_vec(Sampler &S, int lev, const double *src, int on_device, void *dst) {
+    Level &lv = S.L[lev];
+    const i64 n = lv.geo.n;
+    if (n > S.L[0].geo.n) fail(MGMC_ERR_INVALID_ARGUMENT, "level size");
+    const double *d = src;
+    if (!on_device) {
+        CK(cudaMemcpyAsync(S.d_cvec, src, n * sizeof(double), cudaMemcpyHostToDevice, S.stream));
+        d = S.d_cvec;
+    }
+    if (S.fp32)
+        k_unpack<float><<<nblk(n, 256), 256, 0, S.stream>>>(d, (float *)dst, lv.g);
+    else
+        k_unpack<double><<<nblk(n, 256), 256, 0, S.stream>>>(d, (double *)dst, lv.g);
+    S.check_launch();
+}
+
+static void get_vec(Sampler &S, int lev, const void *src, double *dst, int on_device) {
+    Level &lv = S.L[lev];
+    const i64 n = lv.geo.n;
+    double *d = on_device ? dst : S.d_cvec;
+    if (S.fp32)
+        k_pack<float><<<nblk(n, 256), 256, 0, S.stream>>>((const float *)src, d, lv.g);
+    else
+        k_pack<double><<<nblk(n, 256), 256, 0, S.stream>>>((const double *)src, d, lv.g);
+    S.check_launch();
+    if (!on_device) {
+        CK(cudaMemcpyAsync(dst, S.d_cvec, n * sizeof(double), cudaMemcpyDeviceToHost, S.stream));
+        CK(cudaStreamSynchronize(S.stream));
+    }
+}
+
+// Capture one step into a CUDA graph (Philox noise: the step's launches and
+// arguments never change; the noise streams advance through the device
+// step counter).
+static void ensure_graph(Sampler &S) {
+    if (S.gexec) return;
+    CK(cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal));
+    try {
+        S.launch_step();
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(S.stream, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    CK(cudaStreamEndCapture(S.stream, &S.graph));
+    CK(cudaGraphInstantiate(&S.gexec, S.graph, 0));
+}
+
+static void run_steps(Sampler &S, i64 nsteps) {
+    if (S.noise_mode == NOISE_INJECTED) {
+        for (i64 k = 0; k < nsteps; ++k) {
+            if (S.noise_len - S.noise_pos < S.noise_per_step)
+                fail(MGMC_ERR_NOISE_EXHAUSTED, "injected noise exhausted: " + std::to_string(S.noise_len - S.noise_pos) +
+                                                   " queued, " + std::to_string(S.noise_per_step) + " needed per step");
+            S.launch_step();
+            S.check_launch();
+            S.noise_pos += S.noise_per_step;
+        }
+        return;
+    }
+    ensure_graph(S);
+    for (i64 k = 0; k < nsteps; ++k) CK(cudaGraphLaunch(S.gexec, S.stream));
+}
+
+}  // namespace mgmc
+
+// ===================================================================== ABI
+using namespace mgmc;
+
+struct mgmc_sampler {
+    Sampler *impl;
+};
+
+#define API_BEGIN try {
+#define API_END                                \
+    }                                          \
+    catch (const Error &e) {                   \
+        g_err = e.msg;                         \
+        return e.st;                           \
+    }                                          \
+    catch (const std::bad_alloc &) {           \
+        g_err = "host allocation failed";      \
+        return MGMC_ERR_OUT_OF_MEMORY;         \
+    }                                          \
+    catch (const std::exception &e) {          \
+        g_err = e.what();                      \
+        return MGMC_ERR_INVALID_ARGUMENT;      \
+    }                                          \
+    return MGMC_OK;
+
+static Sampler &impl(mgmc_sampler *s) {
+    if (!s || !s->impl) fail(MGMC_ERR_INVALID_ARGUMENT, "null sampler");
+    CK(cudaSetDevice(s->impl->P.device));
+    return *s->impl;
+}
+
+static void check_level(Sampler &S, int level, bool need_coarser) {
+    if (level < 0 || level >= (int)S.L.size() || (need_coarser && level + 1 >= (int)S.L.size()))
+        fail(MGMC_ERR_INVALID_ARGUMENT, "level out of range");
+}
+
+extern "C" {
+
+int mgmc_abi_version(void) { return MGMC_ABI_VERSION; }
+
+const char *mgmc_last_error(void) { return g_err.c_str(); }
+
+mgmc_status mgmc_fd_stencil(int dim, int nx, int ny, int nz, double kappa_sq, double stencil[27]) {
+    API_BEGIN
+    if (dim < 1 || dim > 3 || !stencil) fail(MGMC_ERR_INVALID_ARGUMENT, "dim must be 1, 2 or 3");
+    Geometry g(dim, nx, ny, nz);
+    fd_stencil(g, kappa_sq, stencil);
+    API_END
+}
+
+mgmc_status mgmc_measurement_vector(int dim, int nx, int ny, int nz, const double *x0, double radius, int64_t *idx,
+                                    double *val, int64_t capacity, int64_t *nnz) {
+    API_BEGIN
+    if (dim < 1 || dim > 3 || !x0 || !nnz) fail(MGMC_ERR_INVALID_ARGUMENT, "bad arguments");
+    Geometry g(dim, nx, ny, nz);
+    auto r = measurement_vector(g, x0, radius);
+    int64_t k = 0;
+    for (auto &e : r) {
+        if (k < capacity && idx && val) {
+            idx[k] = e.first;
+            val[k] = e.second;
+        }
+        ++k;
+    }
+    *nnz = k;
+    API_END
+}
+
+mgmc_status mgmc_galerkin_stencil(int dim, const double fine[27], double coarse[27]) {
+    API_BEGIN
+    if (dim < 1 || dim > 3 || !fine || !coarse) fail(MGMC_ERR_INVALID_ARGUMENT, "bad arguments");
+    galerkin_stencil(dim, fine, coarse);
+    API_END
+}
+
+mgmc_status mgmc_sampler_create(const mgmc_operator_desc *op, const mgmc_sampler_params *params, mgmc_sampler **out) {
+    Sampler *S = nullptr;
+    API_BEGIN
+    if (!op || !params || !out) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    S = new Sampler();
+    S->P = *params;
+    S->build(*op);
+    *out = new mgmc_sampler{S};
+    S = nullptr;
+    }
+    catch (const Error &e) {
+        delete S;
+        g_err = e.msg;
+        return e.st;
+    }
+    catch (const std::exception &e) {
+        delete S;
+        g_err = e.what();
+        return MGMC_ERR_INVALID_ARGUMENT;
+    }
+    return MGMC_OK;
+}
+
+mgmc_status mgmc_sampler_destroy(mgmc_sampler *s) {
+    API_BEGIN
+    if (!s) return MGMC_OK;
+    if (s->impl) {
+        cudaSetDevice(s->impl->P.device);
+        cudaStreamSynchronize(s->impl->stream);
+    }
+    delete s->impl;
+    delete s;
+    API_END
+}
+
+mgmc_status mgmc_sampler_fix_rhs(mgmc_sampler *s, const double *f, int on_device) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!f) fail(MGMC_ERR_INVALID_ARGUMENT, "null f");
+    put_vec(S, 0, f, on_device, S.L[0].f);
+    API_END
+}
+
+mgmc_status mgmc_sampler_set_state(mgmc_sampler *s, const double *x, int on_device) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!x) fail(MGMC_ERR_INVALID_ARGUMENT, "null x");
+    put_vec(S, 0, x, on_device, S.L[0].x);
+    API_END
+}
+
+mgmc_status mgmc_sampler_get_state(mgmc_sampler *s, double *x, int on_device) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!x) fail(MGMC_ERR_INVALID_ARGUMENT, "null x");
+    get_vec(S, 0, S.L[0].x, x, on_device);
+    API_END
+}
+
+mgmc_status mgmc_sampler_step(mgmc_sampler *s, int64_t nsteps) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (nsteps < 0) fail(MGMC_ERR_INVALID_ARGUMENT, "nsteps < 0");
+    run_steps(S, nsteps);
+    API_END
+}
+
+mgmc_status mgmc_sampler_apply(mgmc_sampler *s, const double *f, double *x, int on_device) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!f || !x) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    put_vec(S, 0, f, on_device, S.L[0].f);
+    put_vec(S, 0, x, on_device, S.L[0].x);
+    run_steps(S, 1);
+    get_vec(S, 0, S.L[0].x, x, on_device);
+    CK(cudaStreamSynchronize(S.stream));
+    unsigned err = 0;
+    CK(cudaMemcpy(&err, S.d_err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err) fail(MGMC_ERR_NONFINITE, "non-finite observable in the chain");
+    API_END
+}
+
+mgmc_status mgmc_sampler_set_observable(mgmc_sampler *s, int64_t nnz, const int64_t *idx, const double *val,
+                                        int64_t capacity) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (nnz < 0 || capacity < 0 || (nnz > 0 && (!idx || !val))) fail(MGMC_ERR_INVALID_ARGUMENT, "bad observable");
+    CK(cudaStreamSynchronize(S.stream));
+    std::vector<i64> pidx(nnz);
+    for (i64 e = 0; e < nnz; ++e) {
+        if (idx[e] < 0 || idx[e] >= S.L[0].geo.n) fail(MGMC_ERR_INVALID_ARGUMENT, "observable index out of range");
+        pidx[e] = S.L[0].geo.pad(idx[e]);
+    }
+    std::vector<double> v(val, val + nnz);
+    S.d_bidx = S.upload(pidx);
+    S.d_bval = S.upload(v);
+    S.d_obs = S.alloc<double>(std::max<int64_t>(capacity, 1));
+    S.nb = nnz;
+    S.obs_cap = capacity;
+    CK(cudaMemsetAsync(S.d_obs_count, 0, sizeof(u64), S.stream));
+    // the captured step embeds the observable arguments: capture again
+    if (S.gexec) {
+        cudaGraphExecDestroy(S.gexec);
+        cudaGraphDestroy(S.graph);
+        S.gexec = nullptr;
+        S.graph = nullptr;
+    }
+    CK(cudaStreamSynchronize(S.stream));
+    API_END
+}
+
+mgmc_status mgmc_sampler_read_observations(mgmc_sampler *s, double *out, int64_t capacity, int64_t *count) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!count) fail(MGMC_ERR_INVALID_ARGUMENT, "null count");
+    CK(cudaStreamSynchronize(S.stream));
+    u64 c = 0;
+    CK(cudaMemcpy(&c, S.d_obs_count, sizeof(c), cudaMemcpyDeviceToHost));
+    i64 k = std::min<i64>((i64)c, S.obs_cap);
+    k = std::min<i64>(k, capacity);
+    if (k > 0 && out) CK(cudaMemcpy(out, S.d_obs, k * sizeof(double), cudaMemcpyDeviceToHost));
+    *count = (int64_t)c;
+    CK(cudaMemset(S.d_obs_count, 0, sizeof(u64)));
+    unsigned err = 0;
+    CK(cudaMemcpy(&err, S.d_err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err) fail(MGMC_ERR_NONFINITE, "non-finite observable in the chain");
+    API_END
+}
+
+mgmc_status mgmc_sampler_inject_noise(mgmc_sampler *s, const double *normals, int64_t count, int on_device) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (S.noise_mode != NOISE_INJECTED) fail(MGMC_ERR_INVALID_ARGUMENT, "sampler was not created with MGMC_NOISE_INJECTED");
+    if (count < 0 || (count > 0 && !normals)) fail(MGMC_ERR_INVALID_ARGUMENT, "bad noise buffer");
+    CK(cudaStreamSynchronize(S.stream));
+    i64 keep = S.noise_len - S.noise_pos;
+    if (keep + count > S.noise_cap) {
+        i64 cap = std::max<i64>(keep + count, 2 * S.noise_cap);
+        double *nb = dalloc<double>(cap);
+        if (keep > 0) CK(cudaMemcpy(nb, S.d_noise + S.noise_pos, keep * sizeof(double), cudaMemcpyDeviceToDevice));
+        if (S.d_noise) {
+            auto it = std::find(S.owned.begin(), S.owned.end(), (void *)S.d_noise);
+            if (it != S.owned.end()) S.owned.erase(it);
+            cudaFree(S.d_noise);
+        }
+        S.owned.push_back(nb);
+        S.d_noise = nb;
+        S.noise_cap = cap;
+    } else if (S.noise_pos > 0 && keep > 0) {
+        CK(cudaMemcpy(S.d_noise, S.d_noise + S.noise_pos, keep * sizeof(double), cudaMemcpyDeviceToDevice));
+    }
+    S.noise_pos = 0;
+    S.noise_len = keep;
+    if (count > 0)
+        CK(cudaMemcpy(S.d_noise + S.noise_len, normals, count * sizeof(double),
+                      on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
+    S.noise_len += count;
+    API_END
+}
+
+mgmc_status mgmc_sampler_noise_per_step(mgmc_sampler *s, int64_t *count) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!count) fail(MGMC_ERR_INVALID_ARGUMENT, "null count");
+    *count = S.noise_per_step;
+    API_END
+}
+
+mgmc_status mgmc_sampler_synchronize(mgmc_sampler *s) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    CK(cudaStreamSynchronize(S.stream));
+    API_END
+}
+
+mgmc_status mgmc_sampler_stream(mgmc_sampler *s, void **cuda_stream) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!cuda_stream) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    *cuda_stream = (void *)S.stream;
+    API_END
+}
+
+mgmc_status mgmc_sampler_nlevel(mgmc_sampler *s, int *nlevel) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!nlevel) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    *nlevel = (int)S.L.size();
+    API_END
+}
+
+mgmc_status mgmc_sampler_level_size(mgmc_sampler *s, int level, int64_t *n) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    check_level(S, level, false);
+    if (!n) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    *n = S.L[level].geo.n;
+    API_END
+}
+
+mgmc_status mgmc_sampler_launches_per_step(mgmc_sampler *s, int64_t *count) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!count) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    if (S.noise_mode == NOISE_PHILOX) ensure_graph(S);
+    *count = S.launches;
+    API_END
+}
+
+mgmc_status mgmc_level_stencil(mgmc_sampler *s, int level, double stencil[27]) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    check_level(S, level, false);
+    if (!stencil) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    std::memcpy(stencil, S.L[level].st, 27 * sizeof(double));
+    API_END
+}
+
+mgmc_status mgmc_level_apply(mgmc_sampler *s, int level, const double *x, double *y) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    check_level(S, level, false);
+    if (!x || !y) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    S.ensure_scratch(level);
+    Level &lv = S.L[level];
+    put_vec(S, level, x, 0, lv.s1);
+    if (S.fp32) {
+        k_apply_stencil<float><<<nblk(lv.geo.n, 256), 256, 0, S.stream>>>((const float *)lv.s1, (float *)lv.s2, lv.g, stencil_arg<float>(lv, S.P.omega));
+        if (S.m > 0 && lv.Bptr) {
+            launch_bt_plain<float>(S, lv, lv.s1);
+            launch_add_Bq<float>(S, lv, lv.s2, lv.y, 1.0);
+        }
+    } else {
+        k_apply_stencil<double><<<nblk(lv.geo.n, 256), 256, 0, S.stream>>>((const double *)lv.s1, (double *)lv.s2, lv.g, stencil_arg<double>(lv, S.P.omega));
+        if (S.m > 0 && lv.Bptr) {
+            launch_bt_plain<double>(S, lv, lv.s1);
+            launch_add_Bq<double>(S, lv, lv.s2, lv.y, 1.0);
+        }
+    }
+    S.check_launch();
+    get_vec(S, level, lv.s2, y, 0);
+    API_END
+}
+
+mgmc_status mgmc_level_restrict(mgmc_sampler *s, int level, const double *x, double *xc) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    check_level(S, level, true);
+    if (!x || !xc) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    S.ensure_scratch(level);
+    S.ensure_scratch(level + 1);
+    Level &lv = S.L[level], &lc = S.L[level + 1];
+    put_vec(S, level, x, 0, lv.s1);
+    if (S.fp32)
+        launch_resid_restrict<float>(S, level, lv.s1, lv.s1, lc.s1, true);
+    else
+        launch_resid_restrict<double>(S, level, lv.s1, lv.s1, lc.s1, true);
+    S.check_launch();
+    get_vec(S, level + 1, lc.s1, xc, 0);
+    API_END
+}
+
+mgmc_status mgmc_level_prolongate_add(mgmc_sampler *s, int level, double alpha, const double *xc, double *x) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    check_level(S, level, true);
+    if (!x || !xc) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    S.ensure_scratch(level);
+    S.ensure_scratch(level + 1);
+    Level &lv = S.L[level], &lc = S.L[level + 1];
+    put_vec(S, level + 1, xc, 0, lc.s1);
+    put_vec(S, level, x, 0, lv.s1);
+    S.prolong(level, alpha, lc.s1, lv.s1);
+    S.check_launch();
+    get_vec(S, level, lv.s1, x, 0);
+    API_END
+}
+
+mgmc_status mgmc_level_sor(mgmc_sampler *s, int level, int direction, int with_noise, const double *f, double *x) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    check_level(S, level, false);
+    if (!x || !f) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    if (direction != MGMC_FORWARD && direction != MGMC_BACKWARD) fail(MGMC_ERR_INVALID_ARGUMENT, "direction must be MGMC_FORWARD or MGMC_BACKWARD");
+    Level &lv = S.L[level];
+    S.ensure_scratch(level);
+    put_vec(S, level, f, 0, lv.s1);
+    put_vec(S, level, x, 0, lv.s2);
+    i64 need = with_noise ? lv.geo.n + S.m : 0;
+    if (with_noise && S.noise_mode == NOISE_INJECTED && S.noise_len - S.noise_pos < need)
+        fail(MGMC_ERR_NOISE_EXHAUSTED, "injected noise exhausted");
+    S.inv = 4095;
+    S.noise_off = S.noise_pos;
+    S.sor(level, direction == MGMC_FORWARD, with_noise != 0, lv.s2, lv.s1);
+    S.check_launch();
+    if (with_noise && S.noise_mode == NOISE_INJECTED) S.noise_pos += need;
+    get_vec(S, level, lv.s2, x, 0);
+    API_END
+}
+
+}  // extern "C"

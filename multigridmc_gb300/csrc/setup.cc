@@ -1,0 +1,394 @@
+// setup.cc -- host-side set-up of the multigrid hierarchy.
+#include "setup.h"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace mgmc {
+
+Geometry::Geometry(int dim_, int nx, int ny, int nz) : dim(dim_) {
+    c[0] = nx;
+    c[1] = dim > 1 ? ny : 2;
+    c[2] = dim > 2 ? nz : 2;
+    for (int d = 0; d < 3; ++d) N[d] = c[d] - 1;
+    n = (int64_t)N[0] * N[1] * N[2];
+    sy = c[0];
+    sz = (int64_t)c[0] * c[1];
+    nalloc = (int64_t)(c[2] + 2) * sz + 32;
+}
+
+// Lattice3d::get_coarse_lattice (src/lattice/lattice3d.hh:248-263)
+bool Geometry::coarsenable() const {
+    for (int d = 0; d < dim; ++d)
+        if (c[d] % 2 != 0 || c[d] / 2 <= 1) return false;
+    return true;
+}
+
+Geometry Geometry::coarse() const { return Geometry(dim, c[0] / 2, c[1] / 2, c[2] / 2); }
+
+double Geometry::cell_volume() const {  // Lattice::cell_volume, src/lattice/lattice.hh:36-44
+    double v = 1.0;
+    for (int d = 0; d < dim; ++d) v /= c[d];
+    return v;
+}
+
+static inline int sidx(int dx, int dy, int dz) { return (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1); }
+
+// ShiftedLaplaceFDOperator (src/linear_operator/shiftedlaplace_fd_operator.cc:9-57):
+// every operation in the order of the reference so that the FP64 values are
+// the reference's bit for bit.
+void fd_stencil(const Geometry &g, double kappa_sq, double st[27]) {
+    for (int k = 0; k < 27; ++k) st[k] = 0.0;
+    double hinv2[3] = {0.0, 0.0, 0.0};
+    double cell_volume = 1.0;
+    for (int d = 0; d < g.dim; ++d) {
+        double h = 1. / double(g.c[d]);
+        hinv2[d] = 1. / (h * h);
+        cell_volume *= h;
+    }
+    double diagonal = cell_volume * kappa_sq;
+    for (int d = 0; d < g.dim; ++d) {
+        int o[3] = {0, 0, 0};
+        o[d] = -1;
+        st[sidx(o[0], o[1], o[2])] = -cell_volume * hinv2[d];
+        o[d] = 1;
+        st[sidx(o[0], o[1], o[2])] = -cell_volume * hinv2[d];
+        diagonal += 2. * cell_volume * hinv2[d];
+    }
+    st[13] = diagonal;
+}
+
+// 1d weight of the linear intergrid stencil {1/2, 1, 1/2}
+// (src/intergrid/intergrid_operator_linear.cc:13-29); inactive directions
+// carry the identity.
+static inline double rweight(int o, bool active) {
+    if (!active) return o == 0 ? 1.0 : 0.0;
+    if (o == 0) return 1.0;
+    if (o == 1 || o == -1) return 0.5;
+    return 0.0;
+}
+
+// Galerkin product A_c = R A P for a translation-invariant stencil:
+//   W_c(s) = sum_{a,b} r(a) W(b) r(a + b - 2 s).
+// With homogeneous Dirichlet boundaries the zero-extended fine field equals
+// the reference's truncated stencil rows, so the coarse operator of
+// linear_operator.cc:10-23 is this stencil on every coarse vertex.
+void galerkin_stencil(int dim, const double fine[27], double coarse[27]) {
+    bool act[3] = {dim > 0, dim > 1, dim > 2};
+    for (int sz = -1; sz <= 1; ++sz)
+        for (int sy = -1; sy <= 1; ++sy)
+            for (int sx = -1; sx <= 1; ++sx) {
+                double acc = 0.0;
+                for (int az = -1; az <= 1; ++az)
+                    for (int ay = -1; ay <= 1; ++ay)
+                        for (int ax = -1; ax <= 1; ++ax) {
+                            double ra = rweight(ax, act[0]) * rweight(ay, act[1]) * rweight(az, act[2]);
+                            if (ra == 0.0) continue;
+                            for (int bz = -1; bz <= 1; ++bz)
+                                for (int by = -1; by <= 1; ++by)
+                                    for (int bx = -1; bx <= 1; ++bx) {
+                                        double w = fine[sidx(bx, by, bz)];
+                                        if (w == 0.0) continue;
+                                        double rp = rweight(ax + bx - 2 * sx, act[0]) * rweight(ay + by - 2 * sy, act[1]) *
+                                                    rweight(az + bz - 2 * sz, act[2]);
+                                        acc += ra * w * rp;
+                                    }
+                        }
+                coarse[sidx(sx, sy, sz)] = acc;
+            }
+}
+
+int colour_count(int dim, const double st[27]) {
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                int nz = (dx != 0) + (dy != 0) + (dz != 0);
+                if (nz > 1 && st[sidx(dx, dy, dz)] != 0.0) return 1 << dim;
+            }
+    return 2;
+}
+
+// ------------------------------------------------ measurement quadrature
+// V_d(R) recursion (src/linear_operator/measured_operator.cc:50-66)
+static double V_sphere(double radius, int dim) {
+    if (dim == 0) return 1.0;
+    if (dim == 1) return 2. * radius;
+    return 2. * M_PI / double(dim) * radius * radius * V_sphere(radius, dim - 2);
+}
+
+static double dist(const double *a, const double *b, int dim) {
+    double s = 0.0;
+    for (int d = 0; d < dim; ++d) s += (a[d] - b[d]) * (a[d] - b[d]);
+    return std::sqrt(s);
+}
+
+// measurement_vector (src/linear_operator/measured_operator.cc:69-171) with
+// the 2-point Gauss-Legendre rule of src/auxilliary/quadrature.cc:11-56.
+// Only cells within the bounding box of the ball are visited; every cell
+// outside it fails the reference's overlap test.
+std::map<int64_t, double> measurement_vector(const Geometry &g, const double *x0, double radius) {
+    std::map<int64_t, double> r;
+    const int dim = g.dim;
+    if (radius < 1.E-12) {  // nearest vertex, first one wins on ties
+        double d_min = double(dim);
+        int64_t best = 0;
+        for (int64_t ell = 0; ell < g.n; ++ell) {
+            int64_t nxy = (int64_t)g.N[0] * g.N[1];
+            int64_t idx[3] = {(ell % nxy) % g.N[0] + 1, (ell % nxy) / g.N[0] + 1, ell / nxy + 1};
+            double x[3];
+            for (int d = 0; d < dim; ++d) x[d] = idx[d] * (1. / double(g.c[d]));
+            double dd = dist(x, x0, dim);
+            if (dd < d_min) {
+                d_min = dd;
+                best = ell;
+            }
+        }
+        r[best] = 1.0;
+        return r;
+    }
+    double h[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d) h[d] = 1. / double(g.c[d]);
+    const double cell_volume = g.cell_volume();
+    const double normalisation = 1. / V_sphere(radius, dim);
+    // quadrature points/weights on [0,1]^d, first direction slowest
+    const double q1[2] = {0.5 * (-1.0 / std::sqrt(3.0) + 1.0), 0.5 * (1.0 / std::sqrt(3.0) + 1.0)};
+    const int nq = 1 << dim;
+    std::vector<std::array<double, 3>> qp(nq);
+    std::vector<double> qw(nq);
+    for (int q = 0; q < nq; ++q) {
+        double w = 1.0;
+        for (int d = 0; d < dim; ++d) {
+            int bit = (q >> (dim - 1 - d)) & 1;
+            qp[q][d] = q1[bit];
+            w *= 0.5 * 1.0;
+        }
+        qw[q] = w;
+    }
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int d = 0; d < 3; ++d) {
+        if (d < dim) {
+            lo[d] = std::max(0, (int)std::floor((x0[d] - radius) / h[d]) - 1);
+            hi[d] = std::min(g.c[d] - 1, (int)std::floor((x0[d] + radius) / h[d]) + 1);
+        }
+    }
+    for (int cz = lo[2]; cz <= hi[2]; ++cz)
+        for (int cy = lo[1]; cy <= hi[1]; ++cy)
+            for (int cx = lo[0]; cx <= hi[0]; ++cx) {
+                int cc[3] = {cx, cy, cz};
+                bool overlap = false;
+                double xmin[3] = {2.0, 2.0, 2.0}, xmax[3] = {-1.0, -1.0, -1.0};
+                for (int q = 0; q < nq; ++q) {
+                    double xc[3];
+                    for (int d = 0; d < dim; ++d) {
+                        int om = (q >> (dim - 1 - d)) & 1;
+                        xc[d] = h[d] * double(cc[d] + om);
+                        xmin[d] = std::min(xmin[d], xc[d]);
+                        xmax[d] = std::max(xmax[d], xc[d]);
+                    }
+                    overlap = overlap || (dist(xc, x0, dim) < radius);
+                }
+                bool centre_in_cell = true;
+                for (int d = 0; d < dim; ++d)
+                    centre_in_cell = centre_in_cell && (xmin[d] <= x0[d]) && (x0[d] <= xmax[d]);
+                overlap = overlap || centre_in_cell;
+                if (!overlap) continue;
+                for (int a = 0; a < nq; ++a) {  // corners, first direction slowest
+                    int alpha[3] = {0, 0, 0};
+                    int v[3] = {1, 1, 1};
+                    bool interior = true;
+                    for (int d = 0; d < dim; ++d) {
+                        alpha[d] = (a >> (dim - 1 - d)) & 1;
+                        v[d] = cc[d] + alpha[d];
+                        if (v[d] <= 0 || v[d] >= g.c[d]) interior = false;
+                    }
+                    if (!interior) continue;
+                    int64_t ell = ((int64_t)(v[2] - 1) * g.N[1] + (v[1] - 1)) * g.N[0] + (v[0] - 1);
+                    double local_entry = 0.0;
+                    for (int q = 0; q < nq; ++q) {
+                        double x[3];
+                        for (int d = 0; d < dim; ++d) x[d] = h[d] * (qp[q][d] + double(cc[d]));
+                        double xi = dist(x, x0, dim) / radius;
+                        if (xi < 1.0) {
+                            double phihat = 1.0;
+                            for (int d = 0; d < dim; ++d) phihat *= (alpha[d] == 0) ? (1.0 - qp[q][d]) : qp[q][d];
+                            local_entry += phihat * qw[q] * cell_volume * normalisation;
+                        }
+                    }
+                    r[ell] += local_entry;
+                }
+            }
+    return r;
+}
+
+// B_c = R B (src/linear_operator/linear_operator.cc:19): coarse vertex ic
+// gathers fine vertices 2 ic + a with weight prod_d {1/2, 1, 1/2}[a_d].
+SparseCols restrict_columns(const Geometry &fine, const SparseCols &B) {
+    Geometry cg = fine.coarse();
+    SparseCols out;
+    out.m = B.m;
+    out.ptr.assign(1, 0);
+    const int64_t nxy = (int64_t)fine.N[0] * fine.N[1];
+    for (int j = 0; j < B.m; ++j) {
+        std::map<int64_t, double> col;
+        for (int64_t e = B.ptr[j]; e < B.ptr[j + 1]; ++e) {
+            int64_t ell = B.row[e];
+            int f[3] = {(int)((ell % nxy) % fine.N[0]) + 1, (int)((ell % nxy) / fine.N[0]) + 1, (int)(ell / nxy) + 1};
+            // candidate coarse parents in each direction
+            int cand[3][2], w2[3][2], nc[3];
+            double wt[3][2];
+            for (int d = 0; d < 3; ++d) {
+                if (d >= fine.dim) {
+                    nc[d] = 1;
+                    cand[d][0] = 1;
+                    wt[d][0] = 1.0;
+                    continue;
+                }
+                if (f[d] % 2 == 0) {
+                    nc[d] = 1;
+                    cand[d][0] = f[d] / 2;
+                    wt[d][0] = 1.0;
+                } else {
+                    nc[d] = 2;
+                    cand[d][0] = (f[d] - 1) / 2;
+                    cand[d][1] = (f[d] + 1) / 2;
+                    wt[d][0] = wt[d][1] = 0.5;
+                }
+            }
+            (void)w2;
+            for (int a = 0; a < nc[0]; ++a)
+                for (int b = 0; b < nc[1]; ++b)
+                    for (int c = 0; c < nc[2]; ++c) {
+                        int ic[3] = {cand[0][a], cand[1][b], cand[2][c]};
+                        bool ok = true;
+                        for (int d = 0; d < 3; ++d)
+                            if (ic[d] <= 0 || ic[d] >= cg.c[d]) ok = false;
+                        if (!ok) continue;
+                        int64_t cidx = ((int64_t)(ic[2] - 1) * cg.N[1] + (ic[1] - 1)) * cg.N[0] + (ic[0] - 1);
+                        col[cidx] += wt[0][a] * wt[1][b] * wt[2][c] * B.val[e];
+                    }
+        }
+        for (auto &kv : col) {
+            out.row.push_back(kv.first);
+            out.val.push_back(kv.second);
+        }
+        out.ptr.push_back((int64_t)out.row.size());
+    }
+    return out;
+}
+
+std::vector<double> dense_precision(const Geometry &g, const double st[27], const SparseCols &B,
+                                    const std::vector<double> &Sigma) {
+    const int64_t n = g.n;
+    std::vector<double> Q((size_t)(n * n), 0.0);
+    const int64_t nxy = (int64_t)g.N[0] * g.N[1];
+    for (int64_t ell = 0; ell < n; ++ell) {
+        int v[3] = {(int)((ell % nxy) % g.N[0]) + 1, (int)((ell % nxy) / g.N[0]) + 1, (int)(ell / nxy) + 1};
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    double w = st[sidx(dx, dy, dz)];
+                    if (w == 0.0) continue;
+                    int u[3] = {v[0] + dx, v[1] + dy, v[2] + dz};
+                    bool ok = true;
+                    for (int d = 0; d < 3; ++d)
+                        if (u[d] <= 0 || u[d] >= g.c[d]) ok = false;
+                    if (!ok) continue;
+                    int64_t col = ((int64_t)(u[2] - 1) * g.N[1] + (u[1] - 1)) * g.N[0] + (u[0] - 1);
+                    Q[ell * n + col] = w;
+                }
+    }
+    for (int j = 0; j < B.m; ++j) {
+        double sinv = 1.0 / Sigma[j];
+        for (int64_t a = B.ptr[j]; a < B.ptr[j + 1]; ++a)
+            for (int64_t b = B.ptr[j]; b < B.ptr[j + 1]; ++b)
+                Q[B.row[a] * n + B.row[b]] += B.val[a] * sinv * B.val[b];
+    }
+    return Q;
+}
+
+// Left-looking Cholesky: L_ij = (Q_ij - sum_{k<j} L_ik L_jk) / L_jj with the
+// inner sums in ascending k.
+bool dense_cholesky(std::vector<double> &Q, int64_t n) {
+    bool ok = true;
+    for (int64_t j = 0; j < n && ok; ++j) {
+        const double *Lj = &Q[j * n];
+        double s = Q[j * n + j];
+        for (int64_t k = 0; k < j; ++k) s -= Lj[k] * Lj[k];
+        if (!(s > 0.0)) {
+            ok = false;
+            break;
+        }
+        const double d = std::sqrt(s);
+        Q[j * n + j] = d;
+#pragma omp parallel for schedule(static) if (n - j > 256)
+        for (int64_t i = j + 1; i < n; ++i) {
+            double *Li = &Q[i * n];
+            double t = Li[j];
+            for (int64_t k = 0; k < j; ++k) t -= Li[k] * Lj[k];
+            Li[j] = t / d;
+        }
+    }
+    if (!ok) return false;
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t j = i + 1; j < n; ++j) Q[i * n + j] = 0.0;
+    return true;
+}
+
+// Column c of L^{-1} by forward substitution; stored as row c of the
+// transposed inverse.
+std::vector<double> inverse_factor_transposed(const std::vector<double> &L, int64_t n) {
+    std::vector<double> T((size_t)(n * n), 0.0);
+#pragma omp parallel for schedule(dynamic, 8) if (n > 256)
+    for (int64_t c = 0; c < n; ++c) {
+        double *w = &T[c * n];
+        w[c] = 1.0 / L[c * n + c];
+        for (int64_t i = c + 1; i < n; ++i) {
+            const double *Li = &L[i * n];
+            double s = 0.0;
+            for (int64_t k = c; k < i; ++k) s -= Li[k] * w[k];
+            w[i] = s / Li[i];
+        }
+    }
+    return T;
+}
+
+std::vector<double> small_inverse(const std::vector<double> &S, int m) {
+    std::vector<double> LU = S, inv((size_t)m * m, 0.0);
+    std::vector<int> piv(m);
+    for (int i = 0; i < m; ++i) piv[i] = i;
+    for (int k = 0; k < m; ++k) {
+        int p = k;
+        for (int i = k + 1; i < m; ++i)
+            if (std::fabs(LU[i * m + k]) > std::fabs(LU[p * m + k])) p = i;
+        if (p != k) {
+            for (int j = 0; j < m; ++j) std::swap(LU[k * m + j], LU[p * m + j]);
+            std::swap(piv[k], piv[p]);
+        }
+        for (int i = k + 1; i < m; ++i) {
+            LU[i * m + k] /= LU[k * m + k];
+            for (int j = k + 1; j < m; ++j) LU[i * m + j] -= LU[i * m + k] * LU[k * m + j];
+        }
+    }
+    for (int c = 0; c < m; ++c) {
+        std::vector<double> y(m);
+        for (int i = 0; i < m; ++i) {
+            double s = (piv[i] == c) ? 1.0 : 0.0;
+            for (int j = 0; j < i; ++j) s -= LU[i * m + j] * y[j];
+            y[i] = s;
+        }
+        for (int i = m - 1; i >= 0; --i) {
+            double s = y[i];
+            for (int j = i + 1; j < m; ++j) s -= LU[i * m + j] * inv[j * m + c];
+            inv[i * m + c] = s / LU[i * m + i];
+        }
+    }
+    return inv;
+}
+
+}  // namespace mgmc

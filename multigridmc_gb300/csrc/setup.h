@@ -1,0 +1,72 @@
+// setup.h -- host-side set-up of the multigrid hierarchy (no CUDA).
+//
+// Everything here runs once per sampler: the fine stencil, the Galerkin
+// coarse stencils, the measurement matrix B on every level, and the dense
+// FP64 factor of the coarse precision matrix.  The per-step work lives in
+// kernels.cu.
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+namespace mgmc {
+
+// Lattice geometry of one level plus its padded device layout.
+//
+// Interior vertices (i, j, k), 1 <= i <= c[0]-1 etc., are stored at
+//   p = k * sz + j * sy + i,   sy = c[0], sz = c[0] * c[1].
+// Index 0 of every row is a ghost that is also the right-hand ghost of the
+// previous row, row 0 of every plane is a ghost that is also the top ghost
+// row of the previous plane, and planes 0 and c[2] are ghost planes; one
+// extra ghost plane absorbs the diagonal offsets of the last interior
+// plane.  Ghosts hold zero (homogeneous Dirichlet) and are never written.
+// Inactive directions of 1d/2d lattices have c = 2, i.e. one interior layer.
+struct Geometry {
+    int dim = 3;
+    int c[3] = {2, 2, 2};  // cells per direction
+    int N[3] = {1, 1, 1};  // interior vertices per direction
+    int64_t n = 0;         // interior vertices
+    int64_t sy = 0, sz = 0, nalloc = 0;
+
+    Geometry() = default;
+    Geometry(int dim_, int nx, int ny, int nz);
+    bool coarsenable() const;
+    Geometry coarse() const;
+    // compact (reference) index -> padded index
+    int64_t pad(int64_t ell) const {
+        int64_t nxy = (int64_t)N[0] * N[1];
+        int64_t i = (ell % nxy) % N[0] + 1, j = (ell % nxy) / N[0] + 1, k = ell / nxy + 1;
+        return k * sz + j * sy + i;
+    }
+    double cell_volume() const;
+};
+
+// Column-compressed n x m matrix (row indices ascending in each column).
+struct SparseCols {
+    int m = 0;
+    std::vector<int64_t> ptr{0};
+    std::vector<int64_t> row;
+    std::vector<double> val;
+};
+
+void fd_stencil(const Geometry &g, double kappa_sq, double st[27]);
+void galerkin_stencil(int dim, const double fine[27], double coarse[27]);
+// 2 if the stencil couples axis neighbours only, otherwise 2^dim
+int colour_count(int dim, const double st[27]);
+std::map<int64_t, double> measurement_vector(const Geometry &g, const double *x0, double radius);
+// B_c = R B with the linear restriction (weights prod {1/2, 1, 1/2})
+SparseCols restrict_columns(const Geometry &fine, const SparseCols &B);
+// dense row-major precision matrix A_0 + B Sigma^{-1} B^T of one level
+std::vector<double> dense_precision(const Geometry &g, const double st[27], const SparseCols &B,
+                                    const std::vector<double> &Sigma);
+// natural-order Cholesky Q = L L^T in place (lower triangle, zeros above);
+// false if a pivot is not positive
+bool dense_cholesky(std::vector<double> &Q, int64_t n);
+// L^{-1} of a lower-triangular row-major factor; returns (L^{-1})^T row-major
+std::vector<double> inverse_factor_transposed(const std::vector<double> &L, int64_t n);
+// inverse of a small dense matrix by LU with partial pivoting
+std::vector<double> small_inverse(const std::vector<double> &S, int m);
+
+}  // namespace mgmc
