@@ -1056,14 +1056,14 @@ int64_t orc_lattice_vertex_linear(int dim, int nx, int ny, int nz, const int *id
     for (int d = 0; d < dim; ++d) v[d] = idx[d];
     return Lattice(dim, nx, ny, nz).vertex_linear(v);
 }
-// shift_vertexidx (lattice3d.hh:164-179); returns -1 if the shifted vertex
-// is not interior (where the reference asserts)
+// shift_vertexidx (lattice3d.hh:164-179): the linear index of the shifted
+// Euclidean index; like the reference's release build it does not check
+// that the shifted vertex is interior (its asserts are debug-only)
 int64_t orc_lattice_shift_vertex(int dim, int nx, int ny, int nz, int64_t ell, const int *shift) {
     Lattice lat(dim, nx, ny, nz);
     int v[3];
     lat.vertex_euclid(ell, v);
     for (int d = 0; d < dim; ++d) v[d] += shift[d];
-    if (!lat.is_interior(v)) return -1;
     return lat.vertex_linear(v);
 }
 void orc_lattice_cell_euclid(int dim, int nx, int ny, int nz, int64_t ell, int *idx) {

@@ -1,0 +1,71 @@
+"""Host-side set-up of the GB300 library (no GPU needed): FD stencil,
+measurement vectors and Galerkin coarse stencils against the oracle, and the
+C ABI's exported symbols against include/mgmc_gb300.h."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import multigridmc_gb300 as M
+import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = M.load()
+    hdr = open(os.path.join(ROOT, "include", "mgmc_gb300.h")).read()
+    names = set(re.findall(r"\b(mgmc_[a-z0-9_]+)\s*\(", hdr))
+    assert names, "no declarations found"
+    for n in sorted(names):
+        assert hasattr(lib, n), n
+    assert names == set(M.SIGNATURES), "binding table and header differ"
+    assert lib.mgmc_abi_version() == 1
+
+
+@pytest.mark.parametrize("shape", [(8,), (64, 64), (16, 16, 16), (6, 10, 4), (256, 256, 256)])
+def test_fd_stencil_bitwise(shape):
+    assert np.array_equal(M.fd_stencil(shape, 10.0), O.fd_stencil(shape, 10.0))
+
+
+@pytest.mark.parametrize("shape", [(32, 32), (16, 16, 16), (64, 64, 64), (24, 40, 32)])
+def test_measurement_vector_bitwise(shape):
+    rng = np.random.default_rng(11)
+    for _ in range(4):
+        x0 = rng.uniform(0.1, 0.9, len(shape))
+        for r in (0.05, 0.0, 0.13):
+            i1, v1 = M.measurement_vector(shape, x0, r)
+            i2, v2 = O.measurement_vector(shape, x0, r)
+            assert np.array_equal(i1, i2) and np.array_equal(v1, v2)
+
+
+def test_measurement_vector_integrates_to_one():
+    # B columns approximate the ball average: sum of weights ~ 1 for R >> h
+    i, v = M.measurement_vector((128, 128, 128), [0.5, 0.5, 0.5], 0.05)
+    assert abs(v.sum() - 1.0) < 2e-2
+
+
+@pytest.mark.parametrize("shape", [(16,), (16, 16), (8, 8, 8), (8, 12, 16)])
+def test_galerkin_stencil_matches_sparse_rap(shape):
+    op = O.Operator.fd(list(shape), 10.0)
+    st = M.fd_stencil(shape, 10.0)
+    for _ in range(2):
+        cop = op.coarsen()
+        st = M.galerkin_stencil(len(shape), st)
+        ref = O.Operator.from_stencil(cop.shape, st)
+        A, R = cop.dense(), ref.dense()
+        assert np.abs(A - R).max() <= 4e-15 * np.abs(A).max()
+        op = cop
+
+
+def test_operator_description():
+    op = M.LinearOperator.shifted_laplace_fd((16, 16, 16), Lambda=0.31622776601683794)
+    assert abs(op.stencil[13] - (10.0 + 6 * 256) / 4096) < 1e-12
+    loc = np.array([[0.3, 0.4, 0.5], [0.6, 0.5, 0.4]])
+    op = op.with_measurements(loc, [1.0, 2.0], variance_scaling=1e-4, radius=0.1)
+    assert op.m == 2 and np.allclose(op.Sigma, [1e-4, 2e-4])
+    oo = O.Operator.fd([16, 16, 16], 10.0)
+    oo.add_measurements(loc, [1.0, 2.0], variance_scaling=1e-4, radius=0.1)
+    Bd, sig = oo.B_dense()
+    assert np.array_equal(Bd, op.B_dense()) and np.array_equal(sig, op.Sigma)
