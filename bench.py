@@ -1,0 +1,344 @@
+"""Benchmark: independent samples/s of GPU MGMC on the 3D 256^3 posterior.
+
+Workload (synthetic, seeded): Q = h^3(-Delta_h + kappa^2) on 256^3 cells
+(255^3 = 16,581,375 unknowns, kappa^2 = 10), 64 ball measurements of radius
+0.05 with centres uniform in [0.1, 0.9]^3 (seed 1), Sigma = 1e-4 I, values
+y ~ N(0, 1) (seed 1), right hand side f = B Sigma^{-1} y; V(1,1) cycle with
+SSOR (omega = 1) on 5 levels and the dense FP64 Cholesky sampler on the
+16^3-cell coarse level (3,375 unknowns).
+
+A step is one MGMC V-cycle (one sample).  value = steps/s / IACT of the
+FP32-mixed chain, IACT from the observable z = b^T x (ball average at the
+centre of the domain, radius 0.05) with the reference's tau_int estimator
+(window 50).  The FP64 chain is timed the same way and reported beside it.
+
+Run:  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+Under torchrun every rank runs an independent chain on its own GPU
+(replicas; no collective on the data path).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SHAPE = (256, 256, 256)
+KAPPA_SQ = 10.0
+M_MEAS = 64
+RADIUS = 0.05
+VARIANCE = 1e-4
+NLEVEL = 5
+IACT_WINDOW = 50
+METRIC = "indep. samples/s (rate/IACT), 3D 256³ posterior: mixed vs FP64 plain, 1 GB300"
+UNIT = "indep_samples/s"
+PUBLISHED_MGMC_IACT = 1.28  # python/plot_summary.py:28-29, MGMC at 64^3
+
+
+def problem():
+    """The seeded 256^3 posterior: (LinearOperator, f, observable)."""
+    import multigridmc_gb300 as M
+    rng = np.random.default_rng(1)
+    loc = rng.uniform(0.1, 0.9, size=(M_MEAS, 3))
+    y = rng.standard_normal(M_MEAS)
+    op = M.LinearOperator.shifted_laplace_fd(SHAPE, KAPPA_SQ).with_measurements(
+        loc, np.ones(M_MEAS), variance_scaling=VARIANCE, radius=RADIUS)
+    f = np.zeros(op.n)
+    for j in range(op.m):
+        sl = slice(op.B_ptr[j], op.B_ptr[j + 1])
+        f[op.B_idx[sl]] += op.B_val[sl] * (y[j] / op.Sigma[j])
+    bidx, bval = M.measurement_vector(SHAPE, [0.5, 0.5, 0.5], RADIUS)
+    return op, f, (bidx, bval), loc, y
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            pk = json.load(fh)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def time_chain(M, torch, op, f, obs, precision, steps, warmup, iact_extra, dist, seed):
+    """Timed K steps with the state and f resident on the GPU."""
+    s = M.MultigridMCSampler(op, M.MultigridParameters(nlevel=NLEVEL), ordering=M.MULTICOLOUR,
+                             precision=precision, noise=M.PHILOX, seed=seed)
+    s.fix_rhs(f)
+    s.set_observable(obs[0], obs[1], capacity=warmup + steps + iact_extra + 8)
+    s.step(warmup)
+    s.synchronize()
+    st = torch.cuda.ExternalStream(s.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(st)
+    s.step(steps)
+    e1.record(st)
+    s.synchronize()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    ms = e0.elapsed_time(e1) / steps
+    if iact_extra > 0:
+        s.step(iact_extra)
+    z = s.read_observations(warmup + steps + iact_extra + 8)[warmup:]
+    return s, ms, z
+
+
+def sweep_roofline(M, torch, s, precision, peak):
+    """Fine-level red-black SOR sweep (both colour kernels, Philox noise,
+    no low-rank update) timed alone on the sampler's stream."""
+    n = s.level_size(0)
+    sz = 4 if precision == M.FP32_MIXED else 8
+    s.sweep_device(0, nrepeat=5, with_lowrank=False)
+    s.synchronize()
+    st = torch.cuda.ExternalStream(s.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    rep = 40
+    e0.record(st)
+    s.sweep_device(0, nrepeat=rep, with_lowrank=False)
+    e1.record(st)
+    s.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / rep / 2  # seconds per colour launch
+    bytes_per_launch = 3 * n * sz / 2      # read x, read f, write x; half the points per colour
+    achieved = bytes_per_launch / t / 1e9
+    return achieved, bytes_per_launch, t
+
+
+def time_e2e(M, torch, op, f, precision, steps, seed, iact):
+    """The same metric through Sampler::apply with host buffers: per step
+    f and x go host->device (pinned) and x comes back device->host."""
+    s = M.MultigridMCSampler(op, M.MultigridParameters(nlevel=NLEVEL), ordering=M.MULTICOLOUR,
+                             precision=precision, noise=M.PHILOX, seed=seed + 7)
+    fh = torch.empty(op.n, dtype=torch.float64, pin_memory=True).numpy()
+    xh = torch.empty(op.n, dtype=torch.float64, pin_memory=True).numpy()
+    fh[:] = f
+    xh[:] = 0.0
+    for _ in range(3):
+        s.apply(fh, xh)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.apply(fh, xh)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    s.close()
+    return 1.0 / dt / iact, dt, 2 * op.n * 8, op.n * 8
+
+
+def cpu_reference(seconds_budget=25.0, nsteps=None):
+    """The oracle's restatement of the reference MGMC (lexicographic SOR,
+    dense B-bar, CLCG noise) on the host cores, one chain, OpenMP threads in
+    the dense products; a bounded number of steps."""
+    import oracle as O
+    import multigridmc_gb300 as M
+    rng = np.random.default_rng(1)
+    loc = rng.uniform(0.1, 0.9, size=(M_MEAS, 3))
+    y = rng.standard_normal(M_MEAS)
+    t0 = time.perf_counter()
+    op = O.Operator.fd(list(SHAPE), KAPPA_SQ)
+    op.add_measurements(loc, np.ones(M_MEAS), variance_scaling=VARIANCE, radius=RADIUS)
+    Bd_ptr, Brow, Bval, sig = op.B()
+    f = np.zeros(op.n)
+    for j in range(M_MEAS):
+        f[Brow[Bd_ptr[j]:Bd_ptr[j + 1]]] += Bval[Bd_ptr[j]:Bd_ptr[j + 1]] * (y[j] / sig[j])
+    s = O.mgmc_sampler(op, O.Source(), NLEVEL, ordering=0)
+    setup = time.perf_counter() - t0
+    x = np.zeros(op.n)
+    s.apply(f, x, 1)  # first step (touches every array)
+    times = []
+    t_start = time.perf_counter()
+    while True:
+        t1 = time.perf_counter()
+        s.apply(f, x, 1)
+        times.append(time.perf_counter() - t1)
+        if nsteps is not None and len(times) >= nsteps:
+            break
+        if nsteps is None and time.perf_counter() - t_start > seconds_budget:
+            break
+    per_step = float(np.mean(times))
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"per_step_s": per_step, "steps": len(times), "setup_s": setup, "threads": threads}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--iact-samples", type=int, default=6000)
+    ap.add_argument("--e2e-steps", type=int, default=30)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        r = cpu_reference(seconds_budget=max(5.0, args.cpu_seconds), nsteps=None)
+        val = 1.0 / r["per_step_s"] / PUBLISHED_MGMC_IACT
+        sample = (f"{r['steps']} MGMC steps of the oracle's reference restatement at 256^3, m=64 (lexicographic "
+                  f"SOR, dense B-bar, CLCG), one chain, {r['threads']} OpenMP threads in the dense products; "
+                  f"IACT {PUBLISHED_MGMC_IACT} = the reference's published MGMC IACT (python/plot_summary.py:28); "
+                  f"setup {r['setup_s']:.1f} s untimed")
+        line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": r["steps"], "warmup": 1, "ms_per_step": r["per_step_s"] * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "3D 256^3 posterior MGMC V(1,1) SSOR, 5 levels, m=64", "precision": "fp64",
+                           "ordering": "lexicographic"},
+                "cpu_baseline": {"value": val, "unit": UNIT, "cores": r["threads"], "kind": "port", "sample": sample},
+                "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+        dist = tdist
+    import multigridmc_gb300 as M
+
+    op, f, obs, _, _ = problem()
+    peak, peak_kind = measured_peaks()
+    clocks = ClockSampler(local)
+    extra = max(0, args.iact_samples - args.steps)
+
+    # FP32-mixed headline chain (clocks sampled during its timed region)
+    clocks.start()
+    s32, ms32, z32 = time_chain(M, torch, op, f, obs, M.FP32_MIXED, args.steps, args.warmup, extra, dist, 1000 + rank)
+    clk = clocks.stop()
+    launches = s32.launches_per_step
+    iact32 = M.statistics.tau_int(z32, IACT_WINDOW)
+    ach, bpl, tl = sweep_roofline(M, torch, s32, M.FP32_MIXED, peak)
+    s32.close()
+    # FP64 chain
+    s64, ms64, z64 = time_chain(M, torch, op, f, obs, M.FP64, args.steps, args.warmup, extra, dist, 2000 + rank)
+    iact64 = M.statistics.tau_int(z64, IACT_WINDOW)
+    ach64, bpl64, tl64 = sweep_roofline(M, torch, s64, M.FP64, peak)
+    s64.close()
+
+    ms_t = torch.tensor([ms32, ms64], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms32, ms64 = ms_t.tolist()
+    value = world * 1000.0 / ms32 / iact32
+    value64 = world * 1000.0 / ms64 / iact64
+
+    e2e_val, e2e_dt, h2d, d2h = time_e2e(M, torch, op, f, M.FP32_MIXED, args.e2e_steps, 1000 + rank, iact32)
+    e2e_t = torch.tensor([e2e_dt], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_val = world / e2e_t.item() / iact32
+
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        try:
+            r = cpu_reference(seconds_budget=args.cpu_seconds)
+            cv = 1.0 / r["per_step_s"] / PUBLISHED_MGMC_IACT
+            cpu = {"value": cv, "unit": UNIT, "cores": r["threads"], "kind": "port",
+                   "sample": (f"{r['steps']} oracle MGMC steps at 256^3 m=64 (reference algorithm: lexicographic "
+                              f"SOR, dense B-bar, CLCG), {r['per_step_s']:.2f} s/step, IACT "
+                              f"{PUBLISHED_MGMC_IACT} (published, python/plot_summary.py:28)")}
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 coarse Cholesky and m x m system)", "data": "synthetic",
+        "config": {"workload": "3D 256^3 posterior MGMC V(1,1) SSOR omega=1, 5 levels, coarse dense Cholesky 16^3, "
+                               "64 measurements r=0.05 Sigma=1e-4, kappa^2=10",
+                   "unknowns": int(op.n), "ordering": "multicolour (red-black fine, 8-colour coarse)",
+                   "noise": "in-kernel Philox4x32-10", "parallelism": f"replicas x{world}",
+                   "l2": "per-step working set > L2 (x and f alone 134 MB FP32 / 268 MB FP64)",
+                   "iact_window": IACT_WINDOW, "iact_samples": int(len(z32))},
+        "iact": iact32, "steps_per_s": 1000.0 / ms32,
+        "fp64": {"value": value64, "ms_per_step": ms64, "iact": iact64, "steps_per_s": 1000.0 / ms64,
+                 "sweep_gbs": ach64},
+        "mixed_vs_fp64": value / value64,
+        "clocks": clk,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_dt * 1e3, "api": "mgmc_sampler_apply (pinned host f, x)"},
+        "gpu_launches": int(launches * args.steps),
+        "launches_per_step": int(launches),
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                     "traffic": None, "kernel": "k_sweep_colour<float,7> (fine-level red-black SOR, one colour)",
+                     "algorithmic_bytes_per_launch": bpl, "launch_s": tl, "peak_kind": peak_kind},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -175,6 +175,12 @@ mgmc_status mgmc_level_prolongate_add(mgmc_sampler *s, int level, double alpha, 
  * is SORSampler::apply (noise from the sampler's source), 0 is
  * SORSmoother::apply with right hand side f. */
 mgmc_status mgmc_level_sor(mgmc_sampler *s, int level, int direction, int with_noise, const double *f, double *x);
+/* `nrepeat` SOR sweeps on the level's device-resident state and right hand
+ * side (SORSampler::apply, sor_sampler.cc:37-59), asynchronous on the
+ * sampler's stream; with_lowrank == 0 runs the stencil sweep kernels only.
+ * Used to time the sweep kernels in isolation. */
+mgmc_status mgmc_level_sweep_device(mgmc_sampler *s, int level, int direction, int with_noise, int with_lowrank,
+                                    int64_t nrepeat);
 
 #ifdef __cplusplus
 }

@@ -26,6 +26,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import statistics  # noqa: F401  (tau_int for chain observables)
+
 from . import build as _build
 
 __all__ = [
@@ -103,6 +105,7 @@ SIGNATURES = {
     "mgmc_level_restrict": (C.c_int, [_P, C.c_int, _D, _D]),
     "mgmc_level_prolongate_add": (C.c_int, [_P, C.c_int, C.c_double, _D, _D]),
     "mgmc_level_sor": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _D, _D]),
+    "mgmc_level_sweep_device": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64]),
 }
 
 
@@ -409,6 +412,11 @@ class MultigridMCSampler:
         assert x.dtype == np.float64 and x.flags.c_contiguous
         _check(self._L.mgmc_level_prolongate_add(self._h, level, float(alpha), _dp(xc), _dp(x)))
         return x
+
+    def sweep_device(self, level, direction=FORWARD, nrepeat=1, with_noise=True, with_lowrank=True):
+        """SOR sweeps on the level's device-resident vectors (asynchronous)."""
+        _check(self._L.mgmc_level_sweep_device(self._h, level, direction, int(with_noise), int(with_lowrank),
+                                               int(nrepeat)))
 
     def sor(self, level, direction, f, x, with_noise=True):
         f = _f64(f)

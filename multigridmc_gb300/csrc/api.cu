@@ -1176,4 +1176,24 @@ mgmc_status mgmc_level_sor(mgmc_sampler *s, int level, int direction, int with_n
     API_END
 }
 
+mgmc_status mgmc_level_sweep_device(mgmc_sampler *s, int level, int direction, int with_noise, int with_lowrank,
+                                    int64_t nrepeat) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    check_level(S, level, false);
+    if (direction != MGMC_FORWARD && direction != MGMC_BACKWARD) fail(MGMC_ERR_INVALID_ARGUMENT, "direction must be MGMC_FORWARD or MGMC_BACKWARD");
+    if (with_noise && S.noise_mode != NOISE_PHILOX) fail(MGMC_ERR_UNSUPPORTED, "device sweeps draw Philox noise only");
+    if (nrepeat < 0) fail(MGMC_ERR_INVALID_ARGUMENT, "nrepeat < 0");
+    Level &lv = S.L[level];
+    const int saved_m = S.m;
+    for (int64_t r = 0; r < nrepeat; ++r) {
+        S.inv = 4094;
+        if (!with_lowrank) S.m = 0;
+        S.sor(level, direction == MGMC_FORWARD, with_noise != 0, lv.x, lv.f);
+        S.m = saved_m;
+    }
+    S.check_launch();
+    API_END
+}
+
 }  // extern "C"
