@@ -71,7 +71,11 @@ struct Level {
     int ncol = 2, npt = 7;
     double diag = 0, sd = 0;
     void *x = nullptr, *f = nullptr;    // state and right hand side (T, padded)
-    void *s1 = nullptr, *s2 = nullptr;  // scratch for the building-block calls
+    void *x_home = nullptr;             // buffer holding the state between steps
+    void *x_alt = nullptr;              // second state buffer of the fused red-black sweep
+    bool fused = false;                 // fine-level red-black sweeps run as one pass
+    int rb_cz = 32;                     // z-planes per CTA of the fused sweep
+    void *s1 = nullptr, *s2 = nullptr, *s3 = nullptr;  // scratch for the building-block calls
     SparseCols Bh;                      // B on this level (compact indices)
     i64 *Bptr = nullptr, *Bidx = nullptr;
     double *Bval = nullptr;
@@ -144,7 +148,7 @@ struct Sampler {
     void build_lowrank(int lev);
     void build_coarse();
     void launch_step();
-    void sor(int lev, bool forward, bool noisy, void *x, void *f);
+    void sor(int lev, bool forward, bool noisy, void *&x, void *&alt, void *f);
     void sample(int lev);
     void coarse_sample(int lev);
     void resid_restrict(int lev);
@@ -187,8 +191,18 @@ NoiseArgs Sampler::noise_args(int lev, i64 count) {
 
 // ----------------------------------------------------------- sweep launch
 template <typename T, int NPT, bool EXACT, int NOISE>
-static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, const T *f, const NoiseArgs &nz) {
+static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *&x, T *&alt, const T *f, const NoiseArgs &nz) {
     StencilArg<T> s = stencil_arg<T>(lv, S.P.omega);
+    if (NPT == 7 && lv.fused && alt != nullptr) {
+        // one pass over both colours, x -> alt, then the buffers swap
+        dim3 grid((lv.g.N0 + RB_TX - 1) / RB_TX, (lv.g.N1 + RB_TY - 1) / RB_TY, (lv.g.N2 + lv.rb_cz - 1) / lv.rb_cz);
+        k_sweep_rb<T, EXACT, NOISE><<<grid, RB_THREADS, 0, S.stream>>>(x, alt, f, lv.g, s, forward ? 0 : 1, lv.rb_cz, nz);
+        S.launches++;
+        T *t = x;
+        x = alt;
+        alt = t;
+        return;
+    }
     if (S.P.ordering == MGMC_ORDER_LEXICOGRAPHIC) {
         int hb = lv.ncol == 2 ? 1 : 2, hc = lv.ncol == 2 ? 1 : 4;
         k_sweep_wavefront<T, NPT, EXACT, NOISE><<<1, 1024, 0, S.stream>>>(x, f, lv.g, s, forward ? 1 : 0, hb, hc, nz);
@@ -207,31 +221,42 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
 }
 
 template <typename T, bool EXACT, int NOISE>
-static void launch_sweep_npt(Sampler &S, const Level &lv, bool forward, T *x, const T *f, const NoiseArgs &nz) {
+static void launch_sweep_npt(Sampler &S, const Level &lv, bool forward, T *&x, T *&alt, const T *f, const NoiseArgs &nz) {
     if (lv.npt == 7)
-        launch_sweep_t<T, 7, EXACT, NOISE>(S, lv, forward, x, f, nz);
+        launch_sweep_t<T, 7, EXACT, NOISE>(S, lv, forward, x, alt, f, nz);
     else
-        launch_sweep_t<T, 27, EXACT, NOISE>(S, lv, forward, x, f, nz);
+        launch_sweep_t<T, 27, EXACT, NOISE>(S, lv, forward, x, alt, f, nz);
 }
 
 template <typename T, bool EXACT>
-static void launch_sweep_noise(Sampler &S, const Level &lv, bool forward, int noise, T *x, const T *f, const NoiseArgs &nz) {
+static void launch_sweep_noise(Sampler &S, const Level &lv, bool forward, int noise, T *&x, T *&alt, const T *f,
+                               const NoiseArgs &nz) {
     if (noise == NOISE_NONE)
-        launch_sweep_npt<T, EXACT, NOISE_NONE>(S, lv, forward, x, f, nz);
+        launch_sweep_npt<T, EXACT, NOISE_NONE>(S, lv, forward, x, alt, f, nz);
     else if (noise == NOISE_PHILOX)
-        launch_sweep_npt<T, EXACT, NOISE_PHILOX>(S, lv, forward, x, f, nz);
+        launch_sweep_npt<T, EXACT, NOISE_PHILOX>(S, lv, forward, x, alt, f, nz);
     else
-        launch_sweep_npt<T, EXACT, NOISE_INJECTED>(S, lv, forward, x, f, nz);
+        launch_sweep_npt<T, EXACT, NOISE_INJECTED>(S, lv, forward, x, alt, f, nz);
 }
 
-static void launch_sweep(Sampler &S, const Level &lv, bool forward, int noise, void *x, const void *f, const NoiseArgs &nz,
-                         bool fp32, bool exact) {
-    if (fp32)
-        launch_sweep_noise<float, false>(S, lv, forward, noise, (float *)x, (const float *)f, nz);
-    else if (exact)
-        launch_sweep_noise<double, true>(S, lv, forward, noise, (double *)x, (const double *)f, nz);
-    else
-        launch_sweep_noise<double, false>(S, lv, forward, noise, (double *)x, (const double *)f, nz);
+// One sweep of x with right hand side f.  On the fused red-black path the
+// result lands in `alt` and the two pointers are swapped.
+static void launch_sweep(Sampler &S, const Level &lv, bool forward, int noise, void *&x, void *&alt, const void *f,
+                         const NoiseArgs &nz, bool fp32, bool exact) {
+    if (fp32) {
+        float *xx = (float *)x, *aa = (float *)alt;
+        launch_sweep_noise<float, false>(S, lv, forward, noise, xx, aa, (const float *)f, nz);
+        x = xx;
+        alt = aa;
+    } else {
+        double *xx = (double *)x, *aa = (double *)alt;
+        if (exact)
+            launch_sweep_noise<double, true>(S, lv, forward, noise, xx, aa, (const double *)f, nz);
+        else
+            launch_sweep_noise<double, false>(S, lv, forward, noise, xx, aa, (const double *)f, nz);
+        x = xx;
+        alt = aa;
+    }
 }
 
 template <typename T>
@@ -263,12 +288,12 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
 // SORSampler::apply (sor_sampler.cc:37-59) / SORSmoother::apply
 // (sor_smoother.cc:40-54) on level `lev`: noise draw order n point normals,
 // then m low-rank normals.
-void Sampler::sor(int lev, bool forward, bool noisy, void *x, void *f) {
+void Sampler::sor(int lev, bool forward, bool noisy, void *&x, void *&alt, void *f) {
     Level &lv = L[lev];
     int noise = noisy ? noise_mode : NOISE_NONE;
     NoiseArgs nz = noisy ? noise_args(lev, lv.geo.n) : noise_args(lev, 0);
     if (!noisy) nz.buf = nullptr;
-    launch_sweep(*this, lv, forward, noise, x, f, nz, fp32, exact);
+    launch_sweep(*this, lv, forward, noise, x, alt, f, nz, fp32, exact);
     if (m > 0) {
         NoiseArgs nzl = noisy ? noise_args(lev, m) : noise_args(lev, 0);
         if (!noisy) nzl.buf = nullptr;
@@ -378,8 +403,8 @@ void Sampler::coarse_sample(int lev) {
         inv++;
     } else {
         for (int k = 0; k < P.ncoarsesmooth; ++k) {
-            sor(lev, true, true, lv.x, lv.f);
-            sor(lev, false, true, lv.x, lv.f);
+            sor(lev, true, true, lv.x, lv.x_alt, lv.f);
+            sor(lev, false, true, lv.x, lv.x_alt, lv.f);
         }
     }
 }
@@ -396,11 +421,11 @@ void Sampler::sample(int lev) {
     for (int j = 0; j < cyc; ++j) {
         if (P.smoother == MGMC_SMOOTHER_SSOR) {
             for (int k = 0; k < P.npresmooth; ++k) {
-                sor(lev, true, true, lv.x, lv.f);
-                sor(lev, false, true, lv.x, lv.f);
+                sor(lev, true, true, lv.x, lv.x_alt, lv.f);
+                sor(lev, false, true, lv.x, lv.x_alt, lv.f);
             }
         } else {
-            for (int k = 0; k < P.npresmooth; ++k) sor(lev, true, true, lv.x, lv.f);
+            for (int k = 0; k < P.npresmooth; ++k) sor(lev, true, true, lv.x, lv.x_alt, lv.f);
         }
         resid_restrict(lev);
         CK(cudaMemsetAsync(lc.x, 0, (size_t)lc.geo.nalloc * tsize(), stream));
@@ -408,11 +433,11 @@ void Sampler::sample(int lev) {
         prolong(lev, P.coarse_scaling, lc.x, lv.x);
         if (P.smoother == MGMC_SMOOTHER_SSOR) {
             for (int k = 0; k < P.npostsmooth; ++k) {
-                sor(lev, true, true, lv.x, lv.f);
-                sor(lev, false, true, lv.x, lv.f);
+                sor(lev, true, true, lv.x, lv.x_alt, lv.f);
+                sor(lev, false, true, lv.x, lv.x_alt, lv.f);
             }
         } else {
-            for (int k = 0; k < P.npostsmooth; ++k) sor(lev, false, true, lv.x, lv.f);
+            for (int k = 0; k < P.npostsmooth; ++k) sor(lev, false, true, lv.x, lv.x_alt, lv.f);
         }
     }
 }
@@ -430,6 +455,14 @@ void Sampler::launch_step() {
     noise_off = noise_pos;
     launches = 0;
     sample(0);
+    // an odd number of fused sweeps leaves a level's state in its second
+    // buffer: copy it home so that every step starts from the same buffers
+    for (auto &lv : L) {
+        if (lv.x != lv.x_home) {
+            CK(cudaMemcpyAsync(lv.x_home, lv.x, (size_t)lv.geo.nalloc * tsize(), cudaMemcpyDeviceToDevice, stream));
+            std::swap(lv.x, lv.x_alt);
+        }
+    }
     step_end();
 }
 
@@ -506,6 +539,8 @@ void Sampler::build_lowrank(int lev) {
     CK(cudaMemsetAsync(lv.counter, 0, sizeof(unsigned), stream));
     // FP64 work arrays
     double *xs = alloc<double>(geo.nalloc), *fs = alloc<double>(geo.nalloc);
+    double *xs2 = lv.fused ? alloc<double>(geo.nalloc) : nullptr;
+    if (xs2) CK(cudaMemsetAsync(xs2, 0, geo.nalloc * sizeof(double), stream));
     i64 *nzi = alloc<i64>(n);
     double *nzv = alloc<double>(n);
     unsigned long long *cnt = alloc<unsigned long long>(1);
@@ -520,7 +555,9 @@ void Sampler::build_lowrank(int lev) {
             if (cntj > 0) k_scatter<<<nblk(cntj, 256), 256, 0, stream>>>(lv.Bidx + b0, lv.Bval + b0, cntj, fs);
             NoiseArgs nz{};
             nz.d_step = d_step;
-            launch_sweep(*this, lv, dir == 0, NOISE_NONE, xs, fs, nz, false, exact);
+            void *xa = xs, *xb = xs2;
+            launch_sweep(*this, lv, dir == 0, NOISE_NONE, xa, xb, fs, nz, false, exact);
+            if (xa != (void *)xs) std::swap(xs, xs2);
             // G[:, j] = B^T C e_j
             LowRankArg lr{};
             lr.m = m;
@@ -667,7 +704,14 @@ void Sampler::build(const mgmc_operator_desc &op) {
     }
     for (auto &lv : L) {
         lv.x = talloc(lv.geo.nalloc);
+        lv.x_home = lv.x;
         lv.f = talloc(lv.geo.nalloc);
+        lv.fused = P.ordering == MGMC_ORDER_MULTICOLOUR && lv.npt == 7 && lv.ncol == 2;
+        if (lv.fused) {
+            lv.x_alt = talloc(lv.geo.nalloc);
+            const char *cz = getenv("MGMC_RB_CZ");
+            lv.rb_cz = cz ? std::max(1, atoi(cz)) : 32;
+        }
     }
     d_cvec = alloc<double>(L[0].geo.n);
     // low-rank term on every level: B_{l+1} = R B_l
@@ -731,6 +775,7 @@ void Sampler::ensure_scratch(int lev) {
     Level &lv = L[lev];
     if (!lv.s1) lv.s1 = talloc(lv.geo.nalloc);
     if (!lv.s2) lv.s2 = talloc(lv.geo.nalloc);
+    if (!lv.s3) lv.s3 = talloc(lv.geo.nalloc);
 }
 
 // host / device compact FP64 vector -> padded T array of level lev
@@ -1169,7 +1214,7 @@ mgmc_status mgmc_level_sor(mgmc_sampler *s, int level, int direction, int with_n
         fail(MGMC_ERR_NOISE_EXHAUSTED, "injected noise exhausted");
     S.inv = 4095;
     S.noise_off = S.noise_pos;
-    S.sor(level, direction == MGMC_FORWARD, with_noise != 0, lv.s2, lv.s1);
+    S.sor(level, direction == MGMC_FORWARD, with_noise != 0, lv.s2, lv.s3, lv.s1);
     S.check_launch();
     if (with_noise && S.noise_mode == NOISE_INJECTED) S.noise_pos += need;
     get_vec(S, level, lv.s2, x, 0);
@@ -1189,8 +1234,12 @@ mgmc_status mgmc_level_sweep_device(mgmc_sampler *s, int level, int direction, i
     for (int64_t r = 0; r < nrepeat; ++r) {
         S.inv = 4094;
         if (!with_lowrank) S.m = 0;
-        S.sor(level, direction == MGMC_FORWARD, with_noise != 0, lv.x, lv.f);
+        S.sor(level, direction == MGMC_FORWARD, with_noise != 0, lv.x, lv.x_alt, lv.f);
         S.m = saved_m;
+    }
+    if (lv.x != lv.x_home) {
+        CK(cudaMemcpyAsync(lv.x_home, lv.x, (size_t)lv.geo.nalloc * S.tsize(), cudaMemcpyDeviceToDevice, S.stream));
+        std::swap(lv.x, lv.x_alt);
     }
     S.check_launch();
     API_END

@@ -203,6 +203,130 @@ __global__ void __launch_bounds__(256) k_sweep_colour(T *__restrict__ x, const T
     }
 }
 
+// ------------------------------------------- fused red-black SOR sweep
+// Both colours of a red-black SOR sweep in one pass over HBM (axis-only
+// stencils, i.e. the fine FD level).  A CTA owns an x-y tile of RB_TX x RB_TY
+// interior columns and a range of z-planes; it streams the planes through
+// shared memory and, plane by plane,
+//   1. computes the first colour's new values F on the tile plus a
+//      one-point halo (the halo is recomputed by the neighbouring CTAs:
+//      every CTA reads only old values, so no inter-CTA ordering exists),
+//   2. computes the second colour from F and writes both colours.
+// Old state and new state live in different buffers (xin -> xout), so
+// halos read by other CTAs are never overwritten.  With in-kernel noise the
+// normal of a point is a function of its coordinates only (Philox block per
+// (x, y) column and group of 4 planes), so recomputed halo points get the
+// same noise.  In exact mode the arithmetic is sor_point's: identical to
+// the per-colour kernels and to the oracle's multicolour sweep.
+constexpr int RB_TX = 30, RB_TY = 14;          // interior tile
+constexpr int RB_W1 = RB_TX + 2, RB_H1 = RB_TY + 2;  // tile + halo 1 (F)
+constexpr int RB_W2 = RB_TX + 4, RB_H2 = RB_TY + 4;  // tile + halo 2 (old x)
+constexpr int RB_THREADS = RB_W1 * RB_H1;       // 512: one thread per halo-1 column
+
+__device__ __forceinline__ float4 column_normals(const NoiseArgs &nz, const Grid3 &g, int a, int b, int cq) {
+    u64 sc = (*nz.d_step) * 4096ull + nz.invocation;
+    uint4 ctr = make_uint4((unsigned)((u64)b * g.N0 + a), (PURPOSE_POINT << 28) | (nz.level << 24) | (unsigned)cq,
+                           (unsigned)sc, (unsigned)(sc >> 32));
+    return normals4(philox4x32_10(ctr, noise_key(nz)));
+}
+
+template <typename T, bool EXACT>
+__device__ __forceinline__ T rb_update(T xo, T xm, T xp, T ym, T yp, T zm, T zp, const StencilArg<T> &s, T fv,
+                                       bool noisy, T xi) {
+    typedef Ar<EXACT> A;
+    // ascending linear index: z-, y-, x-, centre, x+, y+, z+
+    T res = A::mul(s.w[4], zm);
+    res = A::add(res, A::mul(s.w[10], ym));
+    res = A::add(res, A::mul(s.w[12], xm));
+    res = A::add(res, A::mul(s.w[13], xo));
+    res = A::add(res, A::mul(s.w[14], xp));
+    res = A::add(res, A::mul(s.w[16], yp));
+    res = A::add(res, A::mul(s.w[22], zp));
+    T cval = fv;
+    if (noisy) cval = A::add(A::mul(s.sd, xi), cval);
+    if (EXACT) return A::add(xo, A::mul(s.omega, A::sub(cval, res)) / s.diag);
+    return xo + s.omega_diag * (cval - res);
+}
+
+template <typename T, bool EXACT, int NOISE>
+__global__ void __launch_bounds__(RB_THREADS, 2) k_sweep_rb(const T *__restrict__ xin, T *__restrict__ xout,
+                                                           const T *__restrict__ f, Grid3 g, StencilArg<T> s,
+                                                           int first, int cz, NoiseArgs nz) {
+    __shared__ T xo[3][RB_H2][RB_W2];
+    __shared__ T Fr[3][RB_H1][RB_W1];
+    const int a0 = blockIdx.x * RB_TX, b0 = blockIdx.y * RB_TY;
+    const int c0 = blockIdx.z * cz, c1 = min(c0 + cz, g.N2);
+    const int tx = threadIdx.x % RB_W1, ty = threadIdx.x / RB_W1;
+    const int a = a0 - 1 + tx, b = b0 - 1 + ty;  // this thread's halo-1 column
+    const bool col_in = (a >= 0 && a < g.N0 && b >= 0 && b < g.N1);
+    const bool col_tile = col_in && tx >= 1 && tx <= RB_TX && ty >= 1 && ty <= RB_TY;
+    auto slot = [](int c) { return ((c % 3) + 3) % 3; };
+    // load old plane c (halo-2 region; ghosts read from the padded array,
+    // positions beyond the ghost frame set to zero)
+    auto load_plane = [&](int c) {
+        T(*dst)[RB_W2] = xo[slot(c)];
+        for (int i = threadIdx.x; i < RB_H2 * RB_W2; i += RB_THREADS) {
+            int la = i % RB_W2, lb = i / RB_W2;
+            int ga = a0 - 2 + la, gb = b0 - 2 + lb;
+            T v = T(0);
+            if (c >= 0 && c < g.N2 && ga >= 0 && ga < g.N0 && gb >= 0 && gb < g.N1) v = xin[g.pad(ga, gb, c)];
+            dst[lb][la] = v;
+        }
+    };
+    float4 nb_cur = make_float4(0.f, 0.f, 0.f, 0.f), nb_prev = nb_cur;
+    int q_cur = -1000, q_prev = -1000;
+    auto normal_at = [&](int c) -> T {
+        int q = c >> 2;
+        if (q == q_cur) return (T)pick(nb_cur, c & 3);
+        if (q == q_prev) return (T)pick(nb_prev, c & 3);
+        nb_prev = nb_cur;
+        q_prev = q_cur;
+        nb_cur = column_normals(nz, g, a, b, q);
+        q_cur = q;
+        return (T)pick(nb_cur, c & 3);
+    };
+    load_plane(c0 - 2);
+    load_plane(c0 - 1);
+    for (int kk = c0 - 1; kk <= c1; ++kk) {
+        load_plane(kk + 1);
+        __syncthreads();
+        // 1. first colour of plane kk on the halo-1 region
+        {
+            T fval = T(0);
+            if (kk >= 0 && kk < g.N2 && col_in && ((a + b + kk) & 1) == first) {
+                const int lx = tx + 1, ly = ty + 1;
+                const T(*P0)[RB_W2] = xo[slot(kk)];
+                T xi = T(0);
+                if (NOISE == NOISE_PHILOX) xi = normal_at(kk);
+                if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, kk)];
+                fval = rb_update<T, EXACT>(P0[ly][lx], P0[ly][lx - 1], P0[ly][lx + 1], P0[ly - 1][lx], P0[ly + 1][lx],
+                                           xo[slot(kk - 1)][ly][lx], xo[slot(kk + 1)][ly][lx], s, f[g.pad(a, b, kk)],
+                                           NOISE != NOISE_NONE, xi);
+            }
+            Fr[slot(kk)][ty][tx] = fval;  // zero off the first colour / outside
+        }
+        __syncthreads();
+        // 2. finalise plane kk-1 on the tile
+        const int c = kk - 1;
+        if (c >= c0 && c < c1 && col_tile) {
+            T out;
+            if (((a + b + c) & 1) == first) {
+                out = Fr[slot(c)][ty][tx];
+            } else {
+                const T(*F0)[RB_W1] = Fr[slot(c)];
+                T xi = T(0);
+                if (NOISE == NOISE_PHILOX) xi = normal_at(c);
+                if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
+                out = rb_update<T, EXACT>(xo[slot(c)][ty + 1][tx + 1], F0[ty][tx - 1], F0[ty][tx + 1], F0[ty - 1][tx],
+                                          F0[ty + 1][tx], Fr[slot(c - 1)][ty][tx], Fr[slot(c + 1)][ty][tx], s,
+                                          f[g.pad(a, b, c)], NOISE != NOISE_NONE, xi);
+            }
+            xout[g.pad(a, b, c)] = out;
+        }
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------ lexicographic wavefront
 // Lexicographic order as hyperplanes t = a + hb b + hc c: every neighbour
 // that precedes a point lexicographically lies on an earlier hyperplane

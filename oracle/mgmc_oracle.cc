@@ -42,6 +42,7 @@
 #include <vector>
 #include <algorithm>
 #include <array>
+#include <tuple>
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -159,25 +160,6 @@ struct Csc {
     std::vector<double> val;
 };
 
-static Csr csr_from_rows(int64_t n, std::vector<std::map<int64_t, double>> &rows) {
-    Csr A;
-    A.n = n;
-    A.ptr.assign(n + 1, 0);
-    for (int64_t i = 0; i < n; ++i) A.ptr[i + 1] = A.ptr[i] + (int64_t)rows[i].size();
-    A.col.resize(A.ptr[n]);
-    A.val.resize(A.ptr[n]);
-    for (int64_t i = 0; i < n; ++i) {
-        int64_t k = A.ptr[i];
-        for (auto &e : rows[i]) {
-            A.col[k] = e.first;
-            A.val[k] = e.second;
-            ++k;
-        }
-    }
-    A.finish_diag();
-    return A;
-}
-
 // ---------------------------------------------------------------------------
 // LinearOperator: A = A_0 + B Sigma^{-1} B^T (linear_operator.hh:19-26).
 // ---------------------------------------------------------------------------
@@ -191,10 +173,15 @@ struct LinOp {
     int64_t n() const { return A.n; }
     // linear_operator.hh:78-88: y = A_0 x (+ B (Sigma^{-1} B^T x))
     void apply(const double *x, double *y) const {
-        for (int64_t i = 0; i < A.n; ++i) y[i] = 0.0;
-        // Eigen column-major sparse * dense: y[row] += val * x[col], col ascending
-        for (int64_t c = 0; c < A.n; ++c)
-            for (int64_t k = A.ptr[c]; k < A.ptr[c + 1]; ++k) y[A.col[k]] += A.val[k] * x[c];
+        // Eigen's column-major sparse * dense adds val * x[col] into
+        // y[row] for col ascending; for the symmetric A that is the row sum
+        // over ascending columns, computed here row by row
+#pragma omp parallel for schedule(static) if (A.n > 100000)
+        for (int64_t i = 0; i < A.n; ++i) {
+            double acc = 0.0;
+            for (int64_t k = A.ptr[i]; k < A.ptr[i + 1]; ++k) acc += A.val[k] * x[A.col[k]];
+            y[i] = acc;
+        }
         if (m() > 0) {
             std::vector<double> s(m(), 0.0);
             for (int j = 0; j < m(); ++j) {
@@ -229,21 +216,27 @@ struct LinOp {
 static std::shared_ptr<LinOp> stencil_operator(const Lattice &lat, const double *st) {
     auto op = std::make_shared<LinOp>(lat);
     int64_t n = lat.nvertex();
-    std::vector<std::map<int64_t, double>> rows(n);
+    Csr &A = op->A;
+    A.n = n;
+    A.ptr.assign(n + 1, 0);
+    // offsets in ascending linear-index order ((dz, dy, dx) lexicographic)
+    std::vector<int> offs;
+    for (int k = 0; k < 27; ++k)
+        if (st[k] != 0.0) offs.push_back(k);
+    A.col.reserve(n * offs.size());
+    A.val.reserve(n * offs.size());
     for (int64_t ell = 0; ell < n; ++ell) {
         int idx[3];
         lat.vertex_euclid(ell, idx);
-        for (int dz = -1; dz <= 1; ++dz)
-            for (int dy = -1; dy <= 1; ++dy)
-                for (int dx = -1; dx <= 1; ++dx) {
-                    double w = st[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)];
-                    if (w == 0.0) continue;
-                    int j[3] = {idx[0] + dx, idx[1] + dy, idx[2] + dz};
-                    if (!lat.is_interior(j)) continue;
-                    rows[ell][lat.vertex_linear(j)] = w;
-                }
+        for (int k : offs) {
+            int j[3] = {idx[0] + k % 3 - 1, idx[1] + (k / 3) % 3 - 1, idx[2] + k / 9 - 1};
+            if (!lat.is_interior(j)) continue;
+            A.col.push_back(lat.vertex_linear(j));
+            A.val.push_back(st[k]);
+        }
+        A.ptr[ell + 1] = (int64_t)A.col.size();
     }
-    op->A = csr_from_rows(n, rows);
+    A.finish_diag();
     op->B.nrow = n;
     op->B.m = 0;
     op->B.ptr.assign(1, 0);
@@ -362,9 +355,24 @@ static std::map<int64_t, double> measurement_vector(const Lattice &lat, const do
     for (int d = 0; d < dim; ++d) h[d] = 1. / double(lat.n[d]);
     Quadrature quad(dim, 1);
     auto basis_idx = cartesian_product(std::vector<int>{0, 1}, dim);
+    // cells outside the bounding box of the ball fail the overlap test
+    // below; visiting only the box (in ascending cell order) changes nothing
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d) {
+        lo[d] = std::max(0, (int)std::floor((x0[d] - radius) / h[d]) - 1);
+        hi[d] = std::min(lat.n[d] - 1, (int)std::floor((x0[d] + radius) / h[d]) + 1);
+    }
     for (int64_t cell_idx = 0; cell_idx < lat.ncell(); ++cell_idx) {
         int cc[3];
         lat.cell_euclid(cell_idx, cc);
+        bool inbox = true;
+        for (int d = 0; d < dim; ++d) inbox = inbox && cc[d] >= lo[d] && cc[d] <= hi[d];
+        if (!inbox) {
+            // jump to the next row of the box
+            if (cc[0] < lo[0]) cell_idx += lo[0] - cc[0] - 1;
+            else if (cc[0] > hi[0]) cell_idx += lat.n[0] - cc[0] - 1;
+            continue;
+        }
         bool overlap = false;
         double xmin[3] = {2.0, 2.0, 2.0}, xmax[3] = {-1.0, -1.0, -1.0};
         for (auto &om : basis_idx) {
@@ -444,6 +452,7 @@ struct Intergrid {
         }
     }
     void restrict_(const double *x, double *xc) const {  // intergrid_operator.hh:74-88
+#pragma omp parallel for schedule(static) if (crs.nvertex() > 100000)
         for (int64_t ic = 0; ic < crs.nvertex(); ++ic) {
             double result = 0;
             for (int k = 0; k < S; ++k) result += matrix[k] * x[colidx[ic * S + k]];
@@ -459,58 +468,136 @@ struct Intergrid {
 };
 
 // linear_operator.cc:10-23: A_c = R A R^T, B_c = R B, Sigma copied.
+// Sparse triple product row by row: (R A)[ic, g] accumulates over the
+// restriction entries k (ascending) and the CSR entries of each fine row,
+// then A_c[ic, jc] accumulates (R A)[ic, g] R[jc, g] over g ascending and
+// the parents jc of g in ascending order.  Every operator here is at most a
+// 27-point stencil, so the work arrays are small boxes around the coarse
+// vertex: (R A)[ic, .] lives within +-2 fine cells of 2 ic and A_c[ic, .]
+// within +-1 coarse cells of ic.
 static std::shared_ptr<LinOp> coarsen(const LinOp &op, const Intergrid &ig) {
     auto cop = std::make_shared<LinOp>(ig.crs);
-    int64_t nf = op.n(), nc = ig.crs.nvertex();
+    const Lattice &fl = op.lat, &cl = ig.crs;
+    int64_t nc = cl.nvertex();
     int S = ig.S;
-    // transpose of R: fine row -> list of (coarse col, weight)
-    std::vector<std::vector<std::pair<int64_t, double>>> RT(nf);
-    for (int64_t ic = 0; ic < nc; ++ic)
-        for (int k = 0; k < S; ++k) RT[ig.colidx[ic * S + k]].push_back({ic, ig.matrix[k]});
-    std::vector<std::map<int64_t, double>> rows(nc);
+    Csr &Ac = cop->A;
+    Ac.n = nc;
+    std::vector<std::vector<int64_t>> colv(nc);
+    std::vector<std::vector<double>> valv(nc);
+#pragma omp parallel for schedule(dynamic, 256)
     for (int64_t ic = 0; ic < nc; ++ic) {
-        // (R A)[ic, g] then times P
-        std::map<int64_t, double> RA;
+        double RA[125];
+        bool hitRA[125];
+        double AC[27];
+        bool hitAC[27];
+        for (int q = 0; q < 125; ++q) {
+            RA[q] = 0.0;
+            hitRA[q] = false;
+        }
+        for (int q = 0; q < 27; ++q) {
+            AC[q] = 0.0;
+            hitAC[q] = false;
+        }
+        int c[3];
+        cl.vertex_euclid(ic, c);
+        int ctr[3] = {2 * c[0], fl.dim > 1 ? 2 * c[1] : 1, fl.dim > 2 ? 2 * c[2] : 1};
         for (int k = 0; k < S; ++k) {
             int64_t f = ig.colidx[ic * S + k];
             double w = ig.matrix[k];
-            for (int64_t e = op.A.ptr[f]; e < op.A.ptr[f + 1]; ++e) RA[op.A.col[e]] += w * op.A.val[e];
+            for (int64_t e = op.A.ptr[f]; e < op.A.ptr[f + 1]; ++e) {
+                int g[3];
+                fl.vertex_euclid(op.A.col[e], g);
+                int q = (g[2] - ctr[2] + 2) * 25 + (g[1] - ctr[1] + 2) * 5 + (g[0] - ctr[0] + 2);
+                RA[q] += w * op.A.val[e];
+                hitRA[q] = true;
+            }
         }
-        for (auto &ga : RA)
-            for (auto &jw : RT[ga.first]) rows[ic][jw.first] += ga.second * jw.second;
-    }
-    cop->A = csr_from_rows(nc, rows);
-    // B_c = R B
-    cop->B.nrow = nc;
-    cop->B.m = op.B.m;
-    cop->B.ptr.assign(op.B.m + 1, 0);
-    std::vector<double> dense(nf, 0.0);
-    std::vector<char> mask(nf, 0);
-    for (int j = 0; j < op.B.m; ++j) {
-        for (int64_t k = op.B.ptr[j]; k < op.B.ptr[j + 1]; ++k) {
-            dense[op.B.row[k]] = op.B.val[k];
-            mask[op.B.row[k]] = 1;
-        }
-        for (int64_t ic = 0; ic < nc; ++ic) {
-            bool hit = false;
-            double acc = 0.0;
-            for (int k = 0; k < S; ++k) {
-                int64_t f = ig.colidx[ic * S + k];
-                if (mask[f]) {
-                    hit = true;
-                    acc += ig.matrix[k] * dense[f];
+        // slots in ascending global index order = (z, y, x) lexicographic
+        for (int q = 0; q < 125; ++q) {
+            if (!hitRA[q]) continue;
+            int g[3] = {ctr[0] + q % 5 - 2, ctr[1] + (q / 5) % 5 - 2, ctr[2] + q / 25 - 2};
+            // coarse parents jc of g: R[jc, g] = prod_d {1/2, 1, 1/2}[g_d - 2 jc_d]
+            int pc[3][2], np_[3];
+            double pw[3][2];
+            for (int d = 0; d < 3; ++d) {
+                if (d >= fl.dim) {
+                    np_[d] = 1;
+                    pc[d][0] = 1;
+                    pw[d][0] = 1.0;
+                } else if (g[d] % 2 == 0) {
+                    np_[d] = 1;
+                    pc[d][0] = g[d] / 2;
+                    pw[d][0] = 1.0;
+                } else {
+                    np_[d] = 2;
+                    pc[d][0] = (g[d] - 1) / 2;
+                    pc[d][1] = (g[d] + 1) / 2;
+                    pw[d][0] = pw[d][1] = 0.5;
                 }
             }
-            if (hit) {
-                cop->B.row.push_back(ic);
-                cop->B.val.push_back(acc);
-            }
+            for (int a2 = 0; a2 < np_[2]; ++a2)
+                for (int a1 = 0; a1 < np_[1]; ++a1)
+                    for (int a0 = 0; a0 < np_[0]; ++a0) {
+                        int jc[3] = {pc[0][a0], pc[1][a1], pc[2][a2]};
+                        if (!cl.is_interior(jc)) continue;
+                        // weight product in the order of intergrid_operator_linear.cc:16-29
+                        double w = 1.0;
+                        w *= pw[0][a0];
+                        if (fl.dim > 1) w *= pw[1][a1];
+                        if (fl.dim > 2) w *= pw[2][a2];
+                        int qc = (jc[2] - c[2] + 1) * 9 + (jc[1] - c[1] + 1) * 3 + (jc[0] - c[0] + 1);
+                        AC[qc] += RA[q] * w;
+                        hitAC[qc] = true;
+                    }
         }
-        cop->B.ptr[j + 1] = (int64_t)cop->B.row.size();
-        for (int64_t k = op.B.ptr[j]; k < op.B.ptr[j + 1]; ++k) {
-            dense[op.B.row[k]] = 0.0;
-            mask[op.B.row[k]] = 0;
+        for (int qc = 0; qc < 27; ++qc) {
+            if (!hitAC[qc]) continue;
+            int jc[3] = {c[0] + qc % 3 - 1, c[1] + (qc / 3) % 3 - 1, c[2] + qc / 9 - 1};
+            colv[ic].push_back(cl.vertex_linear(jc));
+            valv[ic].push_back(AC[qc]);
         }
+    }
+    Ac.ptr.assign(nc + 1, 0);
+    for (int64_t ic = 0; ic < nc; ++ic) Ac.ptr[ic + 1] = Ac.ptr[ic] + (int64_t)colv[ic].size();
+    Ac.col.resize(Ac.ptr[nc]);
+    Ac.val.resize(Ac.ptr[nc]);
+    for (int64_t ic = 0; ic < nc; ++ic) {
+        std::copy(colv[ic].begin(), colv[ic].end(), Ac.col.begin() + Ac.ptr[ic]);
+        std::copy(valv[ic].begin(), valv[ic].end(), Ac.val.begin() + Ac.ptr[ic]);
+    }
+    Ac.finish_diag();
+    // B_c = R B: coarse vertex ic collects the fine entries 2 ic + a of each
+    // column; structural entries are kept even where the sum is zero
+    cop->B.nrow = nc;
+    cop->B.m = op.B.m;
+    cop->B.ptr.assign(1, 0);
+    for (int j = 0; j < op.B.m; ++j) {
+        std::map<int64_t, std::vector<std::pair<int, double>>> contrib;  // ic -> (k, value)
+        for (int64_t e = op.B.ptr[j]; e < op.B.ptr[j + 1]; ++e) {
+            int g[3];
+            fl.vertex_euclid(op.B.row[e], g);
+            for (int dz = -1; dz <= 1; ++dz)
+                for (int dy = -1; dy <= 1; ++dy)
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        if ((fl.dim < 2 && dy) || (fl.dim < 3 && dz)) continue;
+                        int f2[3] = {g[0] - dx, g[1] - dy, g[2] - dz};  // candidate 2 ic
+                        if ((f2[0] % 2) || (fl.dim > 1 && f2[1] % 2) || (fl.dim > 2 && f2[2] % 2)) continue;
+                        int jc[3] = {f2[0] / 2, fl.dim > 1 ? f2[1] / 2 : 1, fl.dim > 2 ? f2[2] / 2 : 1};
+                        if (!cl.is_interior(jc)) continue;
+                        int k = (dx + 1) + (fl.dim > 1 ? 3 * (dy + 1) : 0) + (fl.dim > 2 ? 9 * (dz + 1) : 0);
+                        contrib[cl.vertex_linear(jc)].push_back({k, op.B.val[e]});
+                    }
+        }
+        for (auto &kv : contrib) {
+            // restrict(): sum over the stencil entries k in ascending order
+            std::sort(kv.second.begin(), kv.second.end(),
+                      [](const std::pair<int, double> &a, const std::pair<int, double> &b) { return a.first < b.first; });
+            double acc = 0.0;
+            for (auto &kvv : kv.second) acc += ig.matrix[kvv.first] * kvv.second;
+            cop->B.row.push_back(kv.first);
+            cop->B.val.push_back(acc);
+        }
+        cop->B.ptr.push_back((int64_t)cop->B.row.size());
     }
     cop->Sigma = op.Sigma;
     return cop;
@@ -690,65 +777,83 @@ static std::vector<int64_t> sweep_order(const LinOp &op, int ordering, bool forw
 // ---------------------------------------------------------------------------
 // SOR smoother: sor_smoother.cc:9-78
 // ---------------------------------------------------------------------------
+// Bbar is a function of (operator, direction, ordering, omega); samplers of
+// one hierarchy share it instead of holding the reference's four identical
+// pairs per level (ssor_sampler.hh:37-38, multigridmc_sampler.cc:92-95).
+typedef std::map<std::tuple<const LinOp *, bool, int, double>, std::shared_ptr<std::vector<double>>> BbarCache;
+
 struct SORSmoother {
     std::shared_ptr<LinOp> op;
     double omega;
     bool forward;
     int ordering;
     std::vector<int64_t> order;
-    std::vector<double> Bbar;  // n x m row-major, dense (sor_smoother.cc:25-35)
-    SORSmoother(std::shared_ptr<LinOp> op_, double omega_, bool forward_, int ordering_)
+    std::shared_ptr<std::vector<double>> Bbar;  // n x m row-major, dense (sor_smoother.cc:25-35)
+    SORSmoother(std::shared_ptr<LinOp> op_, double omega_, bool forward_, int ordering_, BbarCache *cache = nullptr)
         : op(op_), omega(omega_), forward(forward_), ordering(ordering_) {
-        std::vector<int> rank;
-        order = sweep_order(*op, ordering, forward, &rank);
+        order = sweep_order(*op, ordering, forward, nullptr);
         int m = op->m();
         if (m == 0) return;
-        int64_t n = op->n();
-        // position of every vertex in the forward visiting order defines the
-        // triangle: lower part = earlier in the sweep
+        auto key = std::make_tuple((const LinOp *)op.get(), forward, ordering, omega);
+        if (cache && cache->count(key)) {
+            Bbar = (*cache)[key];
+            return;
+        }
+        Bbar = std::make_shared<std::vector<double>>(build_bbar());
+        if (cache) (*cache)[key] = Bbar;
+    }
+    std::vector<double> build_bbar() const {
+        const int m = op->m();
+        const int64_t n = op->n();
         std::vector<int64_t> pos(n);
         for (int64_t p = 0; p < n; ++p) pos[order[p]] = p;
-        // dense B
-        std::vector<double> LDinvB(n * m, 0.0);
+        std::vector<double> X((size_t)n * m, 0.0);  // (L + D/omega)^{-1} B, row-major
         for (int j = 0; j < m; ++j)
-            for (int64_t k = op->B.ptr[j]; k < op->B.ptr[j + 1]; ++k) LDinvB[op->B.row[k] * m + j] = op->B.val[k];
-        // (L + D/omega)^{-1} B: diag entries a + (1-omega)/omega * a
-        // (sor_smoother.cc:22-23), forward substitution along the sweep.
+            for (int64_t k = op->B.ptr[j]; k < op->B.ptr[j + 1]; ++k) X[(size_t)op->B.row[k] * m + j] = op->B.val[k];
+        // diag entries a + (1-omega)/omega * a (sor_smoother.cc:22-23);
+        // substitution along the sweep, earlier entries subtracted in the
+        // order they were computed (Eigen's column-oriented triangular solve)
         const double scal = (1. - omega) / omega;
+        std::vector<std::pair<int64_t, double>> prev;
         for (int64_t p = 0; p < n; ++p) {
             int64_t i = order[p];
             double dii = op->A.diag[i] + scal * op->A.diag[i];
-            // subtract earlier entries in the order they were computed
-            std::vector<std::pair<int64_t, double>> prev;
+            prev.clear();
             for (int64_t k = op->A.ptr[i]; k < op->A.ptr[i + 1]; ++k) {
                 int64_t c = op->A.col[k];
                 if (c != i && pos[c] < p) prev.push_back({pos[c], op->A.val[k]});
             }
             std::sort(prev.begin(), prev.end());
-            for (int j = 0; j < m; ++j) {
-                double t = LDinvB[i * m + j];
-                for (auto &e : prev) t -= e.second * LDinvB[order[e.first] * m + j];
-                LDinvB[i * m + j] = t / dii;
+            double *Xi = &X[(size_t)i * m];
+            for (auto &e : prev) {
+                const double *Xc = &X[(size_t)order[e.first] * m];
+                for (int j = 0; j < m; ++j) Xi[j] -= e.second * Xc[j];
             }
+            for (int j = 0; j < m; ++j) Xi[j] = Xi[j] / dii;
         }
-        // S = Sigma + B^T (L + D/omega)^{-1} B;  Bbar = LDinvB S^{-1}
-        std::vector<double> S(m * m, 0.0);
+        // S = Sigma + B^T (L + D/omega)^{-1} B;  Bbar = X S^{-1}
+        std::vector<double> S((size_t)m * m, 0.0);
         for (int a = 0; a < m; ++a) {
             for (int b = 0; b < m; ++b) {
                 double acc = 0.0;
-                for (int64_t k = op->B.ptr[a]; k < op->B.ptr[a + 1]; ++k) acc += op->B.val[k] * LDinvB[op->B.row[k] * m + b];
+                for (int64_t k = op->B.ptr[a]; k < op->B.ptr[a + 1]; ++k) acc += op->B.val[k] * X[(size_t)op->B.row[k] * m + b];
                 S[a * m + b] = acc;
             }
             S[a * m + a] += op->Sigma[a];
         }
         std::vector<double> Sinv = dense_inverse(S, m);
-        Bbar.assign(n * m, 0.0);
-        for (int64_t i = 0; i < n; ++i)
+#pragma omp parallel for schedule(static) if (n > 100000)
+        for (int64_t i = 0; i < n; ++i) {
+            double row[4096];
+            double *Xi = &X[(size_t)i * m];
             for (int b = 0; b < m; ++b) {
                 double acc = 0.0;
-                for (int a = 0; a < m; ++a) acc += LDinvB[i * m + a] * Sinv[a * m + b];
-                Bbar[i * m + b] = acc;
+                for (int a = 0; a < m; ++a) acc += Xi[a] * Sinv[a * m + b];
+                row[b] = acc;
             }
+            for (int b = 0; b < m; ++b) Xi[b] = row[b];
+        }
+        return X;
     }
     // sor_smoother.cc:56-78
     void apply_sparse(const double *b, double *x) const {
@@ -771,10 +876,12 @@ struct SORSmoother {
                 for (int64_t k = op->B.ptr[j]; k < op->B.ptr[j + 1]; ++k) acc += op->B.val[k] * x[op->B.row[k]];
                 y[j] = acc;
             }
-            int64_t n = op->n();
+            const int64_t n = op->n();
+            const double *Bb = Bbar->data();
+#pragma omp parallel for schedule(static) if (n > 100000)
             for (int64_t i = 0; i < n; ++i) {
                 double acc = 0.0;
-                for (int j = 0; j < m; ++j) acc += Bbar[i * m + j] * y[j];
+                for (int j = 0; j < m; ++j) acc += Bb[(size_t)i * m + j] * y[j];
                 x[i] -= acc;
             }
         }
@@ -797,8 +904,9 @@ struct SORSampler : Sampler {
     int nsmooth;
     SORSmoother smoother;
     std::vector<double> sqrt_precision_diag, Sigma_inv_sqrt, c_rhs, xi;
-    SORSampler(std::shared_ptr<LinOp> op_, NormalSource *rng_, double omega_, int nsmooth_, bool forward, int ordering)
-        : op(op_), rng(rng_), omega(omega_), nsmooth(nsmooth_), smoother(op_, omega_, forward, ordering) {
+    SORSampler(std::shared_ptr<LinOp> op_, NormalSource *rng_, double omega_, int nsmooth_, bool forward, int ordering,
+               BbarCache *cache = nullptr)
+        : op(op_), rng(rng_), omega(omega_), nsmooth(nsmooth_), smoother(op_, omega_, forward, ordering, cache) {
         int64_t n = op->n();
         sqrt_precision_diag.resize(n);
         for (int64_t ell = 0; ell < n; ++ell)
@@ -832,8 +940,9 @@ struct SORSampler : Sampler {
 struct SSORSampler : Sampler {
     SORSampler fwd, bwd;
     int nsmooth;
-    SSORSampler(std::shared_ptr<LinOp> op, NormalSource *rng, double omega, int nsmooth_, int ordering)
-        : fwd(op, rng, omega, 1, true, ordering), bwd(op, rng, omega, 1, false, ordering), nsmooth(nsmooth_) {}
+    SSORSampler(std::shared_ptr<LinOp> op, NormalSource *rng, double omega, int nsmooth_, int ordering,
+                BbarCache *cache = nullptr)
+        : fwd(op, rng, omega, 1, true, ordering, cache), bwd(op, rng, omega, 1, false, ordering, cache), nsmooth(nsmooth_) {}
     void apply(const double *f, double *x) override {
         for (int k = 0; k < nsmooth; ++k) {
             fwd.apply(f, x);
@@ -896,6 +1005,7 @@ struct MGMCSampler : Sampler {
     std::vector<std::unique_ptr<Intergrid>> ig;
     std::unique_ptr<Sampler> coarse;
     std::vector<std::vector<double>> x_ell, f_ell, r_ell;
+    BbarCache cache;
     MGMCSampler(std::shared_ptr<LinOp> op, NormalSource *rng_, const MGParams &p_) : p(p_), rng(rng_) {
         std::shared_ptr<LinOp> lin_op = op;
         for (int level = 0; level < p.nlevel; ++level) {
@@ -905,11 +1015,11 @@ struct MGMCSampler : Sampler {
             r_ell.emplace_back(n, 0.0);
             ops.push_back(lin_op);
             if (p.smoother == 1) {
-                pre.emplace_back(new SSORSampler(lin_op, rng, p.omega, p.npresmooth, p.ordering));
-                post.emplace_back(new SSORSampler(lin_op, rng, p.omega, p.npostsmooth, p.ordering));
+                pre.emplace_back(new SSORSampler(lin_op, rng, p.omega, p.npresmooth, p.ordering, &cache));
+                post.emplace_back(new SSORSampler(lin_op, rng, p.omega, p.npostsmooth, p.ordering, &cache));
             } else {
-                pre.emplace_back(new SORSampler(lin_op, rng, p.omega, p.npresmooth, true, p.ordering));
-                post.emplace_back(new SORSampler(lin_op, rng, p.omega, p.npostsmooth, false, p.ordering));
+                pre.emplace_back(new SORSampler(lin_op, rng, p.omega, p.npresmooth, true, p.ordering, &cache));
+                post.emplace_back(new SORSampler(lin_op, rng, p.omega, p.npostsmooth, false, p.ordering, &cache));
             }
             if (level < p.nlevel - 1) {
                 if (!lin_op->lat.coarsenable()) throw std::runtime_error("cannot coarsen lattice");
@@ -920,7 +1030,7 @@ struct MGMCSampler : Sampler {
         if (p.coarse_solver == 0)
             coarse.reset(new CholeskySampler(lin_op, rng));
         else
-            coarse.reset(new SSORSampler(lin_op, rng, p.omega, p.ncoarsesmooth, p.ordering));
+            coarse.reset(new SSORSampler(lin_op, rng, p.omega, p.ncoarsesmooth, p.ordering, &cache));
     }
     void sample(int level) {
         if (level == p.nlevel - 1) {
