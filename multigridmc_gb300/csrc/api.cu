@@ -82,8 +82,9 @@ struct Level {
     RowCsr Br;          // B by rows (double values)
     RowCsr C[2];        // C = M^{-1} B, forward / backward (T values)
     double *Sinv[2] = {nullptr, nullptr}, *G[2] = {nullptr, nullptr};
-    double *y = nullptr, *z = nullptr;
+    double *y = nullptr, *z = nullptr, *part = nullptr;
     unsigned *counter = nullptr;
+    int bt_split = 1;  // blocks per column of the B^T x reduction
 };
 
 struct Sampler {
@@ -193,30 +194,32 @@ NoiseArgs Sampler::noise_args(int lev, i64 count) {
 template <typename T, int NPT, bool EXACT, int NOISE>
 static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *&x, T *&alt, const T *f, const NoiseArgs &nz) {
     StencilArg<T> s = stencil_arg<T>(lv, S.P.omega);
-    if (NPT == 7 && lv.fused && alt != nullptr) {
+    if (S.P.ordering == MGMC_ORDER_LEXICOGRAPHIC) {
+        int hb = lv.ncol == 2 ? 1 : 2, hc = lv.ncol == 2 ? 1 : 4;
+        k_sweep_wavefront<T, NPT, EXACT, NOISE><<<1, 1024, 0, S.stream>>>(x, f, lv.g, s, forward ? 1 : 0, hb, hc, nz);
+        S.launches++;
+        return;
+    }
+    if (NPT == 7) {
+        if (!lv.fused || alt == nullptr) fail(MGMC_ERR_UNSUPPORTED, "red-black sweep needs a second state buffer");
         // one pass over both colours, x -> alt, then the buffers swap
         dim3 grid((lv.g.N0 + RB_TX - 1) / RB_TX, (lv.g.N1 + RB_TY - 1) / RB_TY, (lv.g.N2 + lv.rb_cz - 1) / lv.rb_cz);
-        k_sweep_rb<T, EXACT, NOISE><<<grid, RB_THREADS, 0, S.stream>>>(x, alt, f, lv.g, s, forward ? 0 : 1, lv.rb_cz, nz);
+        k_sweep_rb<T, EXACT, NOISE><<<grid, RB_THREADS, rb_smem_bytes<T>(), S.stream>>>(x, alt, f, lv.g, s, forward ? 0 : 1,
+                                                                                      lv.rb_cz, nz);
         S.launches++;
         T *t = x;
         x = alt;
         alt = t;
         return;
     }
-    if (S.P.ordering == MGMC_ORDER_LEXICOGRAPHIC) {
-        int hb = lv.ncol == 2 ? 1 : 2, hc = lv.ncol == 2 ? 1 : 4;
-        k_sweep_wavefront<T, NPT, EXACT, NOISE><<<1, 1024, 0, S.stream>>>(x, f, lv.g, s, forward ? 1 : 0, hb, hc, nz);
+    // 2^dim colours: one launch per plane parity (2d: a single plane)
+    const int nphase = lv.geo.dim == 3 ? 2 : 1;
+    for (int ph = 0; ph < nphase; ++ph) {
+        const int zpar = forward ? ph : nphase - 1 - ph;
+        const unsigned nplanes = (unsigned)((lv.g.N2 - zpar + 1) / 2);
+        if (nplanes == 0) continue;
+        k_sweep_planes<T, EXACT, NOISE><<<nplanes, 512, 0, S.stream>>>(x, f, lv.g, s, zpar, forward ? 1 : 0, nz);
         S.launches++;
-    } else {
-        const i64 G0 = (lv.g.N0 + 7) / 8;
-        for (int cc = 0; cc < lv.ncol; ++cc) {
-            int colour = forward ? cc : lv.ncol - 1 - cc;
-            i64 rows = (lv.ncol == 2) ? (i64)lv.g.N1 * lv.g.N2
-                                      : (i64)((lv.g.N1 - ((colour >> 1) & 1) + 1) / 2) * ((lv.g.N2 - ((colour >> 2) & 1) + 1) / 2);
-            if (rows <= 0) continue;
-            k_sweep_colour<T, NPT, EXACT, NOISE><<<nblk(G0 * rows, 256), 256, 0, S.stream>>>(x, f, lv.g, s, colour, lv.ncol, nz);
-            S.launches++;
-        }
     }
 }
 
@@ -241,6 +244,22 @@ static void launch_sweep_noise(Sampler &S, const Level &lv, bool forward, int no
 
 // One sweep of x with right hand side f.  On the fused red-black path the
 // result lands in `alt` and the two pointers are swapped.
+template <typename T, bool EXACT>
+static void rb_attr_t() {
+    const int b = (int)rb_smem_bytes<T>();
+    CK(cudaFuncSetAttribute(k_sweep_rb<T, EXACT, NOISE_NONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    CK(cudaFuncSetAttribute(k_sweep_rb<T, EXACT, NOISE_PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    CK(cudaFuncSetAttribute(k_sweep_rb<T, EXACT, NOISE_INJECTED>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+}
+
+// The fused sweep's shared memory exceeds the 48 KB default in FP64: raise
+// the limit of every instantiation (per device, before the first launch).
+static void rb_set_smem_attributes() {
+    rb_attr_t<float, false>();
+    rb_attr_t<double, false>();
+    rb_attr_t<double, true>();
+}
+
 static void launch_sweep(Sampler &S, const Level &lv, bool forward, int noise, void *&x, void *&alt, const void *f,
                          const NoiseArgs &nz, bool fp32, bool exact) {
     if (fp32) {
@@ -271,14 +290,16 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     lr.sinv_sqrt = S.d_sinv_sqrt;
     lr.y = lv.y;
     lr.z = lv.z;
+    lr.part = lv.part;
     lr.counter = lv.counter;
     size_t smem = 2 * sizeof(double) * S.m;
+    dim3 grid(S.m, lv.bt_split);
     if (noise == NOISE_NONE)
-        k_bt_x_z<T, NOISE_NONE, true><<<S.m, 256, smem, S.stream>>>(x, lr, nz);
+        k_bt_x_z<T, NOISE_NONE, true><<<grid, 256, smem, S.stream>>>(x, lr, nz);
     else if (noise == NOISE_PHILOX)
-        k_bt_x_z<T, NOISE_PHILOX, true><<<S.m, 256, smem, S.stream>>>(x, lr, nz);
+        k_bt_x_z<T, NOISE_PHILOX, true><<<grid, 256, smem, S.stream>>>(x, lr, nz);
     else
-        k_bt_x_z<T, NOISE_INJECTED, true><<<S.m, 256, smem, S.stream>>>(x, lr, nz);
+        k_bt_x_z<T, NOISE_INJECTED, true><<<grid, 256, smem, S.stream>>>(x, lr, nz);
     const RowCsr &C = lv.C[dir];
     if (C.nrows > 0)
         k_lr_scatter<T><<<nblk(C.nrows, 256), 256, 0, S.stream>>>(x, C.nrows, C.rows, C.ptr, C.col, (const T *)C.val, lv.z);
@@ -312,6 +333,16 @@ static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void
     if (zero_stencil)
         for (int k = 0; k < 27; ++k) s.w[k] = T(0);
     const i64 nc = lc.geo.n;
+    if (S.dim == 3 && !zero_stencil) {
+        const int czc = 8;
+        dim3 grid((lc.g.N0 + RR_TX - 1) / RR_TX, (lc.g.N1 + RR_TY - 1) / RR_TY, (lc.g.N2 + czc - 1) / czc);
+        if (lv.npt == 7)
+            k_resid_restrict_tiled<T, 7><<<grid, RR_THREADS, 0, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, czc);
+        else
+            k_resid_restrict_tiled<T, 27><<<grid, RR_THREADS, 0, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, czc);
+        S.launches++;
+        return;
+    }
     if (lv.npt == 7 && !zero_stencil)
         k_resid_restrict<T, 7><<<nblk(nc, 256), 256, 0, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, S.dim);
     else
@@ -327,8 +358,10 @@ static void launch_bt_plain(Sampler &S, Level &lv, const void *x) {
     lr.Bidx = lv.Bidx;
     lr.Bval = lv.Bval;
     lr.y = lv.y;
+    lr.part = lv.part;
+    lr.counter = lv.counter;
     NoiseArgs nz{};
-    k_bt_x_z<T, NOISE_NONE, false><<<S.m, 256, 0, S.stream>>>((const T *)x, lr, nz);
+    k_bt_x_z<T, NOISE_NONE, false><<<dim3(S.m, lv.bt_split), 256, 0, S.stream>>>((const T *)x, lr, nz);
     S.launches++;
 }
 
@@ -362,10 +395,11 @@ void Sampler::resid_restrict(int lev) {
 
 void Sampler::prolong(int lev, double alpha, void *xc, void *x) {
     Level &lv = L[lev], &lc = L[lev + 1];
+    dim3 grid((lv.g.N0 + 127) / 128, lv.g.N1, lv.g.N2);
     if (fp32)
-        k_prolong_add<float><<<nblk(lv.geo.n, 256), 256, 0, stream>>>((float *)x, (const float *)xc, lv.g, lc.g, (float)alpha, dim);
+        k_prolong_add<float><<<grid, 128, 0, stream>>>((float *)x, (const float *)xc, lv.g, lc.g, (float)alpha, dim);
     else
-        k_prolong_add<double><<<nblk(lv.geo.n, 256), 256, 0, stream>>>((double *)x, (const double *)xc, lv.g, lc.g, alpha, dim);
+        k_prolong_add<double><<<grid, 128, 0, stream>>>((double *)x, (const double *)xc, lv.g, lc.g, alpha, dim);
     launches++;
 }
 
@@ -535,6 +569,12 @@ void Sampler::build_lowrank(int lev) {
     }
     lv.y = alloc<double>(m);
     lv.z = alloc<double>(m);
+    {
+        i64 maxcol = 1;
+        for (int j = 0; j < m; ++j) maxcol = std::max<i64>(maxcol, lv.Bh.ptr[j + 1] - lv.Bh.ptr[j]);
+        lv.bt_split = (int)std::min<i64>(32, std::max<i64>(1, (maxcol + 1023) / 1024));
+    }
+    lv.part = alloc<double>((size_t)m * lv.bt_split);
     lv.counter = alloc<unsigned>(1);
     CK(cudaMemsetAsync(lv.counter, 0, sizeof(unsigned), stream));
     // FP64 work arrays
@@ -565,7 +605,9 @@ void Sampler::build_lowrank(int lev) {
             lr.Bidx = lv.Bidx;
             lr.Bval = lv.Bval;
             lr.y = lv.y;
-            k_bt_x_z<double, NOISE_NONE, false><<<m, 256, 0, stream>>>(xs, lr, nz);
+            lr.part = lv.part;
+            lr.counter = lv.counter;
+            k_bt_x_z<double, NOISE_NONE, false><<<dim3(m, lv.bt_split), 256, 0, stream>>>(xs, lr, nz);
             CK(cudaMemcpyAsync(yh.data(), lv.y, m * sizeof(double), cudaMemcpyDeviceToHost, stream));
             CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), stream));
             k_nonzeros<<<nblk(n, 256), 256, 0, stream>>>(xs, lv.g, nzi, nzv, cnt);
@@ -709,8 +751,21 @@ void Sampler::build(const mgmc_operator_desc &op) {
         lv.fused = P.ordering == MGMC_ORDER_MULTICOLOUR && lv.npt == 7 && lv.ncol == 2;
         if (lv.fused) {
             lv.x_alt = talloc(lv.geo.nalloc);
+            rb_set_smem_attributes();
+            // one wave: z-chunks so that every CTA is resident at once
+            int nsm = 0, per_sm = 0;
+            CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, P.device));
+            if (fp32)
+                CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_rb<float, false, NOISE_PHILOX>, RB_THREADS,
+                                                                 rb_smem_bytes<float>()));
+            else
+                CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_rb<double, false, NOISE_PHILOX>, RB_THREADS,
+                                                                 rb_smem_bytes<double>()));
+            const i64 cols = (i64)((lv.g.N0 + RB_TX - 1) / RB_TX) * ((lv.g.N1 + RB_TY - 1) / RB_TY);
+            const i64 chunks = std::max<i64>(1, (i64)nsm * std::max(per_sm, 1) / cols);
+            lv.rb_cz = (int)std::max<i64>(2, (lv.g.N2 + chunks - 1) / chunks);
             const char *cz = getenv("MGMC_RB_CZ");
-            lv.rb_cz = cz ? std::max(1, atoi(cz)) : 32;
+            if (cz) lv.rb_cz = std::max(1, atoi(cz));
         }
     }
     d_cvec = alloc<double>(L[0].geo.n);

@@ -6,12 +6,15 @@
 // zero, so stencil loads need no boundary tests.
 //
 // Kernels (one V-cycle at level l uses them in this order):
-//   k_sweep_colour      multicolour SOR / Gibbs sweep of one colour
+//   k_sweep_rb          red-black SOR sweep of the fine 7-point level, both
+//                       colours in one pass (multicolour order)
+//   k_sweep_planes      8-colour SOR sweep of a 27-point level, one launch per
+//                       plane parity (multicolour order)
 //   k_sweep_wavefront   lexicographic SOR sweep as a hyperplane wavefront
 //                       (one CTA; parity mode)
 //   k_bt_x_z            y = B^T x and the m x m low-rank solve
 //   k_lr_scatter        x += C z over the rows of C = M^{-1} B
-//   k_resid_restrict    f_c = R (f - A_0 x)  (fused residual + restriction)
+//   k_resid_restrict_tiled  f_c = R (f - A_0 x)  (fused residual + restriction)
 //   k_sub_Bq            f_c -= B_c Sigma^{-1} y
 //   k_prolong_add       x += alpha P x_c
 //   k_chol_*            coarse-level FP64 Cholesky sample
@@ -165,44 +168,6 @@ __device__ __forceinline__ void sor_point(T *__restrict__ x, const T *__restrict
         x[P] = xo + s.omega_diag * (cval - res);
 }
 
-// --------------------------------------------------- multicolour sweep
-// Thread = (8-point x-group g, row (b, c)); it updates the <= 4 points of
-// the colour in that group.  ncolour == 2: colour (a + b + c) & 1;
-// otherwise the colour bits are (a & 1, b & 1, c & 1).
-template <typename T, int NPT, bool EXACT, int NOISE>
-__global__ void __launch_bounds__(256) k_sweep_colour(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
-                                                       StencilArg<T> s, int colour, int ncolour, NoiseArgs nz) {
-    const int G0 = (g.N0 + 7) >> 3;
-    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    int grp = (int)(t % G0);
-    i64 row = t / G0;
-    int b, c, p;
-    if (ncolour == 2) {
-        if (row >= (i64)g.N1 * g.N2) return;
-        b = (int)(row % g.N1);
-        c = (int)(row / g.N1);
-        p = (colour + b + c) & 1;
-    } else {
-        int pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
-        int nb = (g.N1 - pb + 1) >> 1, ncc = (g.N2 - pc + 1) >> 1;
-        if (row >= (i64)nb * ncc) return;
-        b = 2 * (int)(row % nb) + pb;
-        c = 2 * (int)(row / nb) + pc;
-        p = colour & 1;
-    }
-    float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (NOISE == NOISE_PHILOX) nrm = point_normals(nz, g, 8 * grp + p, b, c);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        int a = 8 * grp + p + 2 * q;
-        if (a >= g.N0) break;
-        T xi = T(0);
-        if (NOISE == NOISE_PHILOX) xi = (T)pick(nrm, q);
-        if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
-        sor_point<T, NPT, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
-    }
-}
-
 // ------------------------------------------- fused red-black SOR sweep
 // Both colours of a red-black SOR sweep in one pass over HBM (axis-only
 // stencils, i.e. the fine FD level).  A CTA owns an x-y tile of RB_TX x RB_TY
@@ -218,10 +183,11 @@ __global__ void __launch_bounds__(256) k_sweep_colour(T *__restrict__ x, const T
 // (x, y) column and group of 4 planes), so recomputed halo points get the
 // same noise.  In exact mode the arithmetic is sor_point's: identical to
 // the per-colour kernels and to the oracle's multicolour sweep.
-constexpr int RB_TX = 30, RB_TY = 14;          // interior tile
-constexpr int RB_W1 = RB_TX + 2, RB_H1 = RB_TY + 2;  // tile + halo 1 (F)
-constexpr int RB_W2 = RB_TX + 4, RB_H2 = RB_TY + 4;  // tile + halo 2 (old x)
-constexpr int RB_THREADS = RB_W1 * RB_H1;       // 512: one thread per halo-1 column
+constexpr int RB_TX = 62, RB_TY = 14;                 // interior tile
+constexpr int RB_W1 = RB_TX + 2, RB_H1 = RB_TY + 2;  // tile + halo 1 (F): 64 x 16
+constexpr int RB_W2 = RB_TX + 4, RB_H2 = RB_TY + 4;  // tile + halo 2 (old x): 66 x 18
+constexpr int RB_THREADS = (RB_W1 / 2) * RB_H1;       // 512: one thread per pair of halo-1 columns
+constexpr int RB_NLD = (RB_W2 * RB_H2 + RB_THREADS - 1) / RB_THREADS;
 
 __device__ __forceinline__ float4 column_normals(const NoiseArgs &nz, const Grid3 &g, int a, int b, int cq) {
     u64 sc = (*nz.d_step) * 4096ull + nz.invocation;
@@ -229,6 +195,27 @@ __device__ __forceinline__ float4 column_normals(const NoiseArgs &nz, const Grid
                            (unsigned)sc, (unsigned)(sc >> 32));
     return normals4(philox4x32_10(ctr, noise_key(nz)));
 }
+
+// Normals of one lattice column, four planes per Philox block; planes are
+// requested in (nearly) ascending order, so two cached blocks suffice.
+struct ColumnNoise {
+    float4 cur, prev;
+    int qcur, qprev;
+    __device__ void init() {
+        qcur = qprev = -1000;
+        cur = prev = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __device__ __forceinline__ float get(const NoiseArgs &nz, const Grid3 &g, int a, int b, int c) {
+        int q = c >> 2;
+        if (q == qcur) return pick(cur, c & 3);
+        if (q == qprev) return pick(prev, c & 3);
+        prev = cur;
+        qprev = qcur;
+        cur = column_normals(nz, g, a, b, q);
+        qcur = q;
+        return pick(cur, c & 3);
+    }
+};
 
 template <typename T, bool EXACT>
 __device__ __forceinline__ T rb_update(T xo, T xm, T xp, T ym, T yp, T zm, T zp, const StencilArg<T> &s, T fv,
@@ -248,80 +235,150 @@ __device__ __forceinline__ T rb_update(T xo, T xm, T xp, T ym, T yp, T zm, T zp,
     return xo + s.omega_diag * (cval - res);
 }
 
+// Thread = pair of adjacent halo-1 columns (one of each colour on every
+// plane), so both colours' work is spread evenly over the lanes.  Per plane
+// kk:  [A] first colour of plane kk on the halo-1 region,  [B] sync,
+// [C] second colour of plane kk-1 and both colours written out,  [D] the
+// old plane kk+2 (loaded into registers one plane earlier) stored to shared
+// memory,  [E] plane kk+3 loaded into registers,  [F] sync.  The global
+// load latency is hidden behind one plane of work.
+template <typename T>
+constexpr size_t rb_smem_bytes() {
+    return sizeof(T) * (4 * RB_H2 * RB_W2 + 3 * RB_H1 * RB_W1);
+}
+
 template <typename T, bool EXACT, int NOISE>
 __global__ void __launch_bounds__(RB_THREADS, 2) k_sweep_rb(const T *__restrict__ xin, T *__restrict__ xout,
                                                            const T *__restrict__ f, Grid3 g, StencilArg<T> s,
                                                            int first, int cz, NoiseArgs nz) {
-    __shared__ T xo[3][RB_H2][RB_W2];
-    __shared__ T Fr[3][RB_H1][RB_W1];
+    extern __shared__ __align__(16) unsigned char rb_smem[];
+    T(*xo)[RB_H2][RB_W2] = reinterpret_cast<T(*)[RB_H2][RB_W2]>(rb_smem);
+    T(*Fr)[RB_H1][RB_W1] = reinterpret_cast<T(*)[RB_H1][RB_W1]>(rb_smem + sizeof(T) * 4 * RB_H2 * RB_W2);
     const int a0 = blockIdx.x * RB_TX, b0 = blockIdx.y * RB_TY;
     const int c0 = blockIdx.z * cz, c1 = min(c0 + cz, g.N2);
-    const int tx = threadIdx.x % RB_W1, ty = threadIdx.x / RB_W1;
-    const int a = a0 - 1 + tx, b = b0 - 1 + ty;  // this thread's halo-1 column
-    const bool col_in = (a >= 0 && a < g.N0 && b >= 0 && b < g.N1);
-    const bool col_tile = col_in && tx >= 1 && tx <= RB_TX && ty >= 1 && ty <= RB_TY;
-    auto slot = [](int c) { return ((c % 3) + 3) % 3; };
-    // load old plane c (halo-2 region; ghosts read from the padded array,
-    // positions beyond the ghost frame set to zero)
-    auto load_plane = [&](int c) {
-        T(*dst)[RB_W2] = xo[slot(c)];
-        for (int i = threadIdx.x; i < RB_H2 * RB_W2; i += RB_THREADS) {
-            int la = i % RB_W2, lb = i / RB_W2;
-            int ga = a0 - 2 + la, gb = b0 - 2 + lb;
+    const int px = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int b = b0 - 1 + ty;
+    const bool row_in = b >= 0 && b < g.N1;
+    const bool row_tile = row_in && ty >= 1 && ty <= RB_TY;
+    int ac[2];
+    bool cin[2], ctile[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int tx = 2 * px + h;
+        ac[h] = a0 - 1 + tx;
+        cin[h] = row_in && ac[h] >= 0 && ac[h] < g.N0;
+        ctile[h] = row_tile && cin[h] && tx >= 1 && tx <= RB_TX;
+    }
+    ColumnNoise cn[2];
+    cn[0].init();
+    cn[1].init();
+    T pre[RB_NLD];
+    auto fetch = [&](int c) {
+#pragma unroll
+        for (int j = 0; j < RB_NLD; ++j) {
+            const int i = threadIdx.x + j * RB_THREADS;
             T v = T(0);
-            if (c >= 0 && c < g.N2 && ga >= 0 && ga < g.N0 && gb >= 0 && gb < g.N1) v = xin[g.pad(ga, gb, c)];
-            dst[lb][la] = v;
+            if (i < RB_W2 * RB_H2) {
+                const int la = i % RB_W2, lb = i / RB_W2;
+                const int ga = a0 - 2 + la, gb = b0 - 2 + lb;
+                if (c >= 0 && c < g.N2 && ga >= 0 && ga < g.N0 && gb >= 0 && gb < g.N1) v = xin[g.pad(ga, gb, c)];
+            }
+            pre[j] = v;
         }
     };
-    float4 nb_cur = make_float4(0.f, 0.f, 0.f, 0.f), nb_prev = nb_cur;
-    int q_cur = -1000, q_prev = -1000;
-    auto normal_at = [&](int c) -> T {
-        int q = c >> 2;
-        if (q == q_cur) return (T)pick(nb_cur, c & 3);
-        if (q == q_prev) return (T)pick(nb_prev, c & 3);
-        nb_prev = nb_cur;
-        q_prev = q_cur;
-        nb_cur = column_normals(nz, g, a, b, q);
-        q_cur = q;
-        return (T)pick(nb_cur, c & 3);
+    auto commit = [&](int c) {
+#pragma unroll
+        for (int j = 0; j < RB_NLD; ++j) {
+            const int i = threadIdx.x + j * RB_THREADS;
+            if (i < RB_W2 * RB_H2) xo[c & 3][i / RB_W2][i % RB_W2] = pre[j];
+        }
     };
-    load_plane(c0 - 2);
-    load_plane(c0 - 1);
+    auto s3 = [](int c) { return ((c % 3) + 3) % 3; };
+    fetch(c0 - 2);
+    commit(c0 - 2);
+    fetch(c0 - 1);
+    commit(c0 - 1);
+    fetch(c0);
+    commit(c0);
+    fetch(c0 + 1);
+    __syncthreads();
     for (int kk = c0 - 1; kk <= c1; ++kk) {
-        load_plane(kk + 1);
-        __syncthreads();
-        // 1. first colour of plane kk on the halo-1 region
-        {
+        // [A] first colour of plane kk
+        const bool plane_in = kk >= 0 && kk < g.N2;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int tx = 2 * px + h, a = ac[h];
             T fval = T(0);
-            if (kk >= 0 && kk < g.N2 && col_in && ((a + b + kk) & 1) == first) {
+            if (plane_in && cin[h] && ((a + b + kk) & 1) == first) {
                 const int lx = tx + 1, ly = ty + 1;
-                const T(*P0)[RB_W2] = xo[slot(kk)];
                 T xi = T(0);
-                if (NOISE == NOISE_PHILOX) xi = normal_at(kk);
+                if (NOISE == NOISE_PHILOX) xi = (T)cn[h].get(nz, g, a, b, kk);
                 if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, kk)];
-                fval = rb_update<T, EXACT>(P0[ly][lx], P0[ly][lx - 1], P0[ly][lx + 1], P0[ly - 1][lx], P0[ly + 1][lx],
-                                           xo[slot(kk - 1)][ly][lx], xo[slot(kk + 1)][ly][lx], s, f[g.pad(a, b, kk)],
-                                           NOISE != NOISE_NONE, xi);
+                fval = rb_update<T, EXACT>(xo[kk & 3][ly][lx], xo[kk & 3][ly][lx - 1], xo[kk & 3][ly][lx + 1],
+                                           xo[kk & 3][ly - 1][lx], xo[kk & 3][ly + 1][lx], xo[(kk - 1) & 3][ly][lx],
+                                           xo[(kk + 1) & 3][ly][lx], s, f[g.pad(a, b, kk)], NOISE != NOISE_NONE, xi);
             }
-            Fr[slot(kk)][ty][tx] = fval;  // zero off the first colour / outside
+            Fr[s3(kk)][ty][tx] = fval;
         }
         __syncthreads();
-        // 2. finalise plane kk-1 on the tile
+        // [C] second colour of plane c = kk-1, both colours written
         const int c = kk - 1;
-        if (c >= c0 && c < c1 && col_tile) {
-            T out;
-            if (((a + b + c) & 1) == first) {
-                out = Fr[slot(c)][ty][tx];
-            } else {
-                const T(*F0)[RB_W1] = Fr[slot(c)];
-                T xi = T(0);
-                if (NOISE == NOISE_PHILOX) xi = normal_at(c);
-                if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
-                out = rb_update<T, EXACT>(xo[slot(c)][ty + 1][tx + 1], F0[ty][tx - 1], F0[ty][tx + 1], F0[ty - 1][tx],
-                                          F0[ty + 1][tx], Fr[slot(c - 1)][ty][tx], Fr[slot(c + 1)][ty][tx], s,
-                                          f[g.pad(a, b, c)], NOISE != NOISE_NONE, xi);
+        if (c >= c0 && c < c1) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (!ctile[h]) continue;
+                const int tx = 2 * px + h, a = ac[h];
+                T out;
+                if (((a + b + c) & 1) == first) {
+                    out = Fr[s3(c)][ty][tx];
+                } else {
+                    T xi = T(0);
+                    if (NOISE == NOISE_PHILOX) xi = (T)cn[h].get(nz, g, a, b, c);
+                    if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
+                    out = rb_update<T, EXACT>(xo[c & 3][ty + 1][tx + 1], Fr[s3(c)][ty][tx - 1], Fr[s3(c)][ty][tx + 1],
+                                              Fr[s3(c)][ty - 1][tx], Fr[s3(c)][ty + 1][tx], Fr[s3(c - 1)][ty][tx],
+                                              Fr[s3(c + 1)][ty][tx], s, f[g.pad(a, b, c)], NOISE != NOISE_NONE, xi);
+                }
+                xout[g.pad(a, b, c)] = out;
             }
-            xout[g.pad(a, b, c)] = out;
+        }
+        // [D], [E]
+        commit(kk + 2);
+        fetch(kk + 3);
+        __syncthreads();
+    }
+}
+
+// Multicolour sweep of a 2^dim-colour (9- / 27-point) level organised by
+// planes: the colours with z-parity p touch no other plane of parity p, so
+// one launch updates all planes of one parity, one CTA per plane running the
+// plane's four in-plane colours separated by __syncthreads.  The update
+// order and the noise are those of the colour-by-colour sweep (colour index
+// (a & 1) | (b & 1) << 1 | (c & 1) << 2, ascending forward, descending
+// backward), so the chain is the same.
+template <typename T, bool EXACT, int NOISE>
+__global__ void __launch_bounds__(512) k_sweep_planes(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
+                                                       StencilArg<T> s, int zpar, int forward, NoiseArgs nz) {
+    const int c = 2 * blockIdx.x + zpar;
+    if (c >= g.N2) return;
+    const int G0 = (g.N0 + 7) >> 3;
+    for (int cc = 0; cc < 4; ++cc) {
+        const int col2 = forward ? cc : 3 - cc;
+        const int pa = col2 & 1, pb = col2 >> 1;
+        const int nb = (g.N1 - pb + 1) >> 1;
+        for (int t = threadIdx.x; t < nb * G0; t += blockDim.x) {
+            const int grp = t % G0, b = 2 * (t / G0) + pb;
+            float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (NOISE == NOISE_PHILOX) nrm = point_normals(nz, g, 8 * grp + pa, b, c);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int a = 8 * grp + pa + 2 * q;
+                if (a >= g.N0) break;
+                T xi = T(0);
+                if (NOISE == NOISE_PHILOX) xi = (T)pick(nrm, q);
+                if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
+                sor_point<T, 27, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
+            }
         }
         __syncthreads();
     }
@@ -380,11 +437,14 @@ struct LowRankArg {
     const double *sinv_sqrt; // Sigma^{-1/2}
     double *y;          // m scratch: B^T x
     double *z;          // m scratch: coefficients of C
+    double *part;       // m x gridDim.y scratch: partial sums of B^T x
     unsigned *counter;  // block-completion counter (self-resetting)
 };
 
-// y_j = sum_i B_ij x_i (one block per column j).  The last block to finish
-// then forms
+// y_j = sum_i B_ij x_i with gridDim.y blocks per column j (partial sums in
+// `part`, combined in a fixed order by the last block to finish, so the
+// result does not depend on block timing).  With SOLVE the same block then
+// forms
 //   w = Sigma^{-1/2} xi',  z = w - S^{-1} (y + G w)
 // (with_noise == 0: z = -S^{-1} y, the smoother's correction
 // x -= Bbar B^T x of sor_smoother.cc:47-51, Bbar = C S^{-1}).
@@ -392,23 +452,33 @@ template <typename T, int NOISE, bool SOLVE>
 __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRankArg lr, NoiseArgs nz) {
     __shared__ double sh[32];
     __shared__ bool last;
-    const int j = blockIdx.x;
+    const int j = blockIdx.x, p = blockIdx.y, P = gridDim.y;
+    const i64 e0 = lr.Bptr[j], e1 = lr.Bptr[j + 1];
+    const i64 len = (e1 - e0 + P - 1) / P;
+    const i64 lo = e0 + p * len, hi = min(e1, lo + len);
     double acc = 0.0;
-    for (i64 e = lr.Bptr[j] + threadIdx.x; e < lr.Bptr[j + 1]; e += blockDim.x) acc += lr.Bval[e] * (double)x[lr.Bidx[e]];
+    for (i64 e = lo + threadIdx.x; e < hi; e += blockDim.x) acc += lr.Bval[e] * (double)x[lr.Bidx[e]];
     acc = block_sum<256>(acc, sh);
-    if (threadIdx.x == 0) lr.y[j] = acc;
-    if (!SOLVE) return;
+    if (threadIdx.x == 0) lr.part[j * P + p] = acc;
     __threadfence();
     if (threadIdx.x == 0) {
         unsigned done = atomicAdd(lr.counter, 1u);
-        last = (done == (unsigned)gridDim.x - 1);
+        last = (done == gridDim.x * gridDim.y - 1);
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
-    extern __shared__ double dyn[];
-    double *w = dyn, *v = dyn + lr.m;
     const int m = lr.m;
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        double t = 0.0;
+        for (int q = 0; q < P; ++q) t += ((volatile double *)lr.part)[k * P + q];
+        lr.y[k] = t;
+    }
+    if (threadIdx.x == 0) *lr.counter = 0u;
+    if (!SOLVE) return;
+    __syncthreads();
+    extern __shared__ double dyn[];
+    double *w = dyn, *v = dyn + m;
     for (int k = threadIdx.x; k < m; k += blockDim.x) {
         double xi = 0.0;
         if (NOISE == NOISE_PHILOX) {
@@ -420,17 +490,16 @@ __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRank
     }
     __syncthreads();
     for (int k = threadIdx.x; k < m; k += blockDim.x) {
-        double s = ((volatile double *)lr.y)[k];
-        for (int q = 0; q < m; ++q) s += lr.G[(i64)k * m + q] * w[q];
-        v[k] = s;
+        double t = lr.y[k];
+        for (int q = 0; q < m; ++q) t += lr.G[(i64)k * m + q] * w[q];
+        v[k] = t;
     }
     __syncthreads();
     for (int k = threadIdx.x; k < m; k += blockDim.x) {
-        double s = 0.0;
-        for (int q = 0; q < m; ++q) s += lr.Sinv[(i64)k * m + q] * v[q];
-        lr.z[k] = w[k] - s;
+        double t = 0.0;
+        for (int q = 0; q < m; ++q) t += lr.Sinv[(i64)k * m + q] * v[q];
+        lr.z[k] = w[k] - t;
     }
-    if (threadIdx.x == 0) *lr.counter = 0u;
 }
 
 // x[row] += sum_e C_e z_{col_e} over the support rows of C = M^{-1} B.
@@ -485,6 +554,98 @@ __global__ void __launch_bounds__(256) k_resid_restrict(const T *__restrict__ x,
     fc[gc.pad(a, b, c)] = acc;
 }
 
+// Plane-streaming variant: a CTA owns a tile of RR_TX x RR_TY coarse
+// columns and a range of coarse planes.  Fine residual planes are computed
+// once each on the (2 RR_TX + 1) x (2 RR_TY + 1) fine footprint of the tile
+// and kept in a ring of three planes; every coarse plane then restricts from
+// the ring.  x is staged plane by plane with a one-point halo.
+constexpr int RR_TX = 16, RR_TY = 8;
+constexpr int RR_FW = 2 * RR_TX + 1, RR_FH = 2 * RR_TY + 1;  // fine residual footprint
+constexpr int RR_XW = RR_FW + 2, RR_XH = RR_FH + 2;          // x with halo
+constexpr int RR_THREADS = 256;
+
+template <typename T, int NPT>
+__global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tiled(const T *__restrict__ x, const T *__restrict__ f,
+                                                                      T *__restrict__ fc, Grid3 gf, Grid3 gc,
+                                                                      StencilArg<T> s, int czc) {
+    __shared__ T xs[3][RR_XH][RR_XW];
+    __shared__ T rs[3][RR_FH][RR_FW];
+    const int ca0 = blockIdx.x * RR_TX, cb0 = blockIdx.y * RR_TY;
+    const int cc0 = blockIdx.z * czc, cc1 = min(cc0 + czc, gc.N2);
+    // fine 0-based origin of the footprint: centre of coarse (ca0, cb0) is
+    // fine 2 ca0 + 1, its left neighbour 2 ca0
+    const int fa0 = 2 * ca0, fb0 = 2 * cb0;
+    auto slot = [](int p) { return ((p % 3) + 3) % 3; };
+    auto load_x = [&](int p) {
+        T(*dst)[RR_XW] = xs[slot(p)];
+        for (int i = threadIdx.x; i < RR_XH * RR_XW; i += RR_THREADS) {
+            int la = i % RR_XW, lb = i / RR_XW;
+            int ga = fa0 - 1 + la, gb = fb0 - 1 + lb;
+            T v = T(0);
+            if (p >= 0 && p < gf.N2 && ga >= 0 && ga < gf.N0 && gb >= 0 && gb < gf.N1) v = x[gf.pad(ga, gb, p)];
+            dst[lb][la] = v;
+        }
+    };
+    auto resid_plane = [&](int p) {  // fine residual of plane p on the footprint
+        T(*dst)[RR_FW] = rs[slot(p)];
+        for (int i = threadIdx.x; i < RR_FH * RR_FW; i += RR_THREADS) {
+            int la = i % RR_FW, lb = i / RR_FW;
+            int ga = fa0 + la, gb = fb0 + lb;
+            T r = T(0);
+            if (p >= 0 && p < gf.N2 && ga < gf.N0 && gb < gf.N1) {
+                const int X = la + 1, Y = lb + 1;
+                T res;
+                if (NPT == 7) {
+                    res = s.w[4] * xs[slot(p - 1)][Y][X] + s.w[10] * xs[slot(p)][Y - 1][X] + s.w[12] * xs[slot(p)][Y][X - 1] +
+                          s.w[13] * xs[slot(p)][Y][X] + s.w[14] * xs[slot(p)][Y][X + 1] + s.w[16] * xs[slot(p)][Y + 1][X] +
+                          s.w[22] * xs[slot(p + 1)][Y][X];
+                } else {
+                    res = T(0);
+#pragma unroll
+                    for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+                        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+                            for (int dx = -1; dx <= 1; ++dx)
+                                res += s.w[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)] * xs[slot(p + dz)][Y + dy][X + dx];
+                }
+                r = f[gf.pad(ga, gb, p)] - res;
+            }
+            dst[lb][la] = r;
+        }
+    };
+    // coarse plane cc needs fine residual planes 2cc, 2cc+1, 2cc+2
+    const int p_lo = 2 * cc0, p_hi = 2 * (cc1 - 1) + 2;
+    load_x(p_lo - 1);
+    load_x(p_lo);
+    for (int p = p_lo; p <= p_hi; ++p) {
+        load_x(p + 1);
+        __syncthreads();
+        resid_plane(p);
+        __syncthreads();
+        if (p >= p_lo + 2 && ((p - p_lo) & 1) == 0) {  // restrict coarse plane (p - 2) / 2
+            const int cc = (p - 2) / 2;
+            for (int i = threadIdx.x; i < RR_TX * RR_TY; i += RR_THREADS) {
+                int la = i % RR_TX, lb = i / RR_TX;
+                int ca = ca0 + la, cb = cb0 + lb;
+                if (ca >= gc.N0 || cb >= gc.N1) continue;
+                T acc = T(0);
+#pragma unroll
+                for (int az = 0; az < 3; ++az)
+#pragma unroll
+                    for (int ay = 0; ay < 3; ++ay)
+#pragma unroll
+                        for (int ax = 0; ax < 3; ++ax) {
+                            T wr = T((ax == 1 ? 1.0 : 0.5) * (ay == 1 ? 1.0 : 0.5) * (az == 1 ? 1.0 : 0.5));
+                            acc += wr * rs[slot(2 * cc + az)][2 * lb + ay][2 * la + ax];
+                        }
+                fc[gc.pad(ca, cb, cc)] = acc;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // dst[row] += sign * sum_e B_e y_{col_e} / Sigma_{col_e} over the rows of B
 // (row-compressed): the B Sigma^{-1} B^T x part of A x.
 template <typename T>
@@ -504,14 +665,14 @@ __global__ void __launch_bounds__(256) k_add_Bq(T *__restrict__ dst, i64 nrows, 
 // gathers its <= 2^d coarse parents, weight 1 (even coordinate) or 1/2 for
 // each of the two parents (odd coordinate).
 template <typename T>
-__global__ void __launch_bounds__(256) k_prolong_add(T *__restrict__ x, const T *__restrict__ xc, Grid3 gf, Grid3 gc,
+__global__ void __launch_bounds__(128) k_prolong_add(T *__restrict__ x, const T *__restrict__ xc, Grid3 gf, Grid3 gc,
                                                       T alpha, int dim) {
-    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    i64 n = (i64)gf.N0 * gf.N1 * gf.N2;
-    if (t >= n) return;
-    int co[3] = {(int)(t % gf.N0) + 1, (int)((t / gf.N0) % gf.N1) + 1, (int)(t / ((i64)gf.N0 * gf.N1)) + 1};
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= gf.N0) return;
+    int co[3] = {a + 1, (int)blockIdx.y + 1, (int)blockIdx.z + 1};
     int lo[3], np[3];
     T wt[3];
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
         if (d >= dim) {
             lo[d] = 1;
@@ -532,7 +693,7 @@ __global__ void __launch_bounds__(256) k_prolong_add(T *__restrict__ x, const T 
         for (int j = 0; j < np[1]; ++j)
             for (int i = 0; i < np[0]; ++i)
                 acc += wt[0] * wt[1] * wt[2] * xc[(i64)(lo[2] + k) * gc.sz + (i64)(lo[1] + j) * gc.sy + (lo[0] + i)];
-    i64 P = (i64)co[2] * gf.sz + (i64)co[1] * gf.sy + co[0];
+    const i64 P = (i64)co[2] * gf.sz + (i64)co[1] * gf.sy + co[0];
     x[P] += alpha * acc;
 }
 
