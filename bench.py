@@ -221,6 +221,44 @@ def cpu_reference(seconds_budget=25.0, nsteps=None):
     return {"per_step_s": per_step, "steps": len(times), "setup_s": setup, "threads": threads}
 
 
+def covariance_study(nsamples, nprobe=256, warmup=50, seed=1000):
+    """Coupled FP32-mixed and FP64 chains on the 256^3 posterior: the same
+    Philox streams (the FP64 chain widens the FP32 normals), so the two
+    chains see identical noise.  Reports the relative Frobenius difference of
+    the nprobe x nprobe probe-point sample covariances and each chain's
+    IACT."""
+    import multigridmc_gb300 as M
+    op, f, obs, _, _ = problem()
+    rng = np.random.default_rng(2)
+    pts = rng.choice(op.n, size=nprobe, replace=False)
+    probes = [(np.array([p], np.int64), np.array([1.0])) for p in pts] + [obs]
+    res = {}
+    Z = {}
+    for name, prec in (("fp32", M.FP32_MIXED), ("fp64", M.FP64)):
+        s = M.MultigridMCSampler(op, M.MultigridParameters(nlevel=NLEVEL), ordering=M.MULTICOLOUR,
+                                 precision=prec, noise=M.PHILOX, seed=seed)
+        s.fix_rhs(f)
+        s.step(warmup)
+        s.set_probes(probes, nsamples)
+        t0 = time.perf_counter()
+        s.step(nsamples)
+        s.synchronize()
+        dt = time.perf_counter() - t0
+        Z[name] = s.read_observations(nsamples)
+        res[name] = {"ms_per_step": dt / nsamples * 1e3, "iact": M.statistics.tau_int(Z[name][:, -1], IACT_WINDOW)}
+        s.close()
+    C32 = np.cov(Z["fp32"][:, :nprobe].T)
+    C64 = np.cov(Z["fp64"][:, :nprobe].T)
+    res["cov_rel_frobenius"] = float(np.linalg.norm(C32 - C64) / np.linalg.norm(C64))
+    res["mean_rel_diff"] = float(np.linalg.norm(Z["fp32"][:, :nprobe].mean(0) - Z["fp64"][:, :nprobe].mean(0))
+                                 / np.linalg.norm(Z["fp64"][:, :nprobe].mean(0)))
+    res["pathwise_rel_diff_last"] = float(np.linalg.norm(Z["fp32"][-1, :nprobe] - Z["fp64"][-1, :nprobe])
+                                          / np.linalg.norm(Z["fp64"][-1, :nprobe]))
+    res["nsamples"] = nsamples
+    res["nprobe"] = nprobe
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -231,7 +269,12 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--covariance-study", type=int, default=0, metavar="NSAMPLES",
+                    help="run the coupled FP32/FP64 covariance comparison instead of the benchmark")
     args = ap.parse_args()
+    if args.covariance_study > 0:
+        print(json.dumps({"covariance_study": covariance_study(args.covariance_study)}), flush=True)
+        return
     if args.warmup < 3:
         args.warmup = 3
 

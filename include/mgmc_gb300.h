@@ -61,7 +61,8 @@ typedef enum mgmc_status {
     MGMC_ERR_OUT_OF_MEMORY = 5,
     MGMC_ERR_NOISE_EXHAUSTED = 6,  /* injected-noise mode: not enough normals queued */
     MGMC_ERR_NONFINITE = 7,        /* NaN/Inf seen in the chain state */
-    MGMC_ERR_UNSUPPORTED = 8
+    MGMC_ERR_UNSUPPORTED = 8,
+    MGMC_ERR_TIMEOUT = 9           /* a bounded wait inside a kernel gave up (grid barrier) */
 } mgmc_status;
 
 /* sweep ordering */
@@ -151,6 +152,14 @@ mgmc_status mgmc_sampler_step(mgmc_sampler *s, int64_t nsteps);
  * kept on the device until read. */
 mgmc_status mgmc_sampler_set_observable(mgmc_sampler *s, int64_t nnz, const int64_t *idx, const double *val,
                                         int64_t capacity);
+/* Several observables at once: probe p is b_p (entries ptr[p]..ptr[p+1] of
+ * idx/val); after every step the nprobe values are appended, step-major.
+ * Replaces any observable set before. */
+mgmc_status mgmc_sampler_set_probes(mgmc_sampler *s, int nprobe, const int64_t *ptr, const int64_t *idx,
+                                    const double *val, int64_t capacity);
+/* Copies min(count, capacity / nprobe) steps of observations into out
+ * (step-major, nprobe values per step), sets *count to the number of steps
+ * recorded since the last read and starts a new record. */
 mgmc_status mgmc_sampler_read_observations(mgmc_sampler *s, double *out, int64_t capacity, int64_t *count);
 /* Injected-noise mode: queue `count` N(0,1) values; each step consumes
  * mgmc_sampler_noise_per_step() of them in the reference's draw order. */

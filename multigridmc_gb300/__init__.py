@@ -39,7 +39,7 @@ __all__ = [
 OK = 0
 STATUS = {0: "MGMC_OK", 1: "MGMC_ERR_INVALID_ARGUMENT", 2: "MGMC_ERR_LATTICE", 3: "MGMC_ERR_NOT_SPD",
           4: "MGMC_ERR_CUDA", 5: "MGMC_ERR_OUT_OF_MEMORY", 6: "MGMC_ERR_NOISE_EXHAUSTED",
-          7: "MGMC_ERR_NONFINITE", 8: "MGMC_ERR_UNSUPPORTED"}
+          7: "MGMC_ERR_NONFINITE", 8: "MGMC_ERR_UNSUPPORTED", 9: "MGMC_ERR_TIMEOUT"}
 LEXICOGRAPHIC, MULTICOLOUR = 0, 1
 FP64, FP32_MIXED = 0, 1
 PHILOX, INJECTED = 0, 1
@@ -93,6 +93,7 @@ SIGNATURES = {
     "mgmc_sampler_step": (C.c_int, [_P, C.c_int64]),
     "mgmc_sampler_set_observable": (C.c_int, [_P, C.c_int64, _I64, _D, C.c_int64]),
     "mgmc_sampler_read_observations": (C.c_int, [_P, _D, C.c_int64, _I64]),
+    "mgmc_sampler_set_probes": (C.c_int, [_P, C.c_int, _I64, _I64, _D, C.c_int64]),
     "mgmc_sampler_inject_noise": (C.c_int, [_P, _D, C.c_int64, C.c_int]),
     "mgmc_sampler_noise_per_step": (C.c_int, [_P, _I64]),
     "mgmc_sampler_synchronize": (C.c_int, [_P]),
@@ -351,16 +352,35 @@ class MultigridMCSampler:
         return s.value
 
     def set_observable(self, idx, val, capacity):
+        self._nprobe = 1
         idx = np.ascontiguousarray(idx, np.int64)
         val = _f64(val)
         _check(self._L.mgmc_sampler_set_observable(self._h, len(idx), idx.ctypes.data_as(_I64), _dp(val),
                                                    int(capacity)))
 
+    def set_probes(self, probes, capacity):
+        """probes: list of (idx, val); after every step all b_p^T x are kept."""
+        ptr, idx, val = [0], [], []
+        for (i, v) in probes:
+            idx.extend(np.asarray(i, np.int64).tolist())
+            val.extend(np.asarray(v, np.float64).tolist())
+            ptr.append(len(idx))
+        ptr = np.array(ptr, np.int64)
+        idx = np.array(idx, np.int64)
+        val = np.array(val, np.float64)
+        self._nprobe = len(probes)
+        _check(self._L.mgmc_sampler_set_probes(self._h, len(probes), ptr.ctypes.data_as(_I64),
+                                               idx.ctypes.data_as(_I64), _dp(val), int(capacity)))
+
     def read_observations(self, capacity):
-        out = np.zeros(max(int(capacity), 1))
+        """Observations since the last read: shape (steps,) for one
+        observable, (steps, nprobe) after set_probes."""
+        np_ = getattr(self, "_nprobe", 1) or 1
+        out = np.zeros(max(int(capacity), 1) * np_)
         cnt = C.c_int64(0)
-        _check(self._L.mgmc_sampler_read_observations(self._h, _dp(out), int(capacity), C.byref(cnt)))
-        return out[:min(cnt.value, capacity)]
+        _check(self._L.mgmc_sampler_read_observations(self._h, _dp(out), int(capacity) * np_, C.byref(cnt)))
+        k = min(cnt.value, capacity)
+        return out[:k] if np_ == 1 else out[:k * np_].reshape(k, np_)
 
     def inject_noise(self, normals):
         normals = _f64(normals)

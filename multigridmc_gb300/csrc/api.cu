@@ -24,6 +24,8 @@ namespace mgmc {
 
 static thread_local std::string g_err;
 
+void set_last_error(const std::string &msg) { g_err = msg; }
+
 struct Error {
     mgmc_status st;
     std::string msg;
@@ -85,6 +87,8 @@ struct Level {
     double *y = nullptr, *z = nullptr, *part = nullptr;
     unsigned *counter = nullptr;
     int bt_split = 1;  // blocks per column of the B^T x reduction
+    unsigned *bar = nullptr;  // grid barrier of the cooperative sweep
+    int coop_blocks = 1;      // co-resident CTAs of the cooperative sweep
 };
 
 struct Sampler {
@@ -104,9 +108,11 @@ struct Sampler {
     u64 *d_step = nullptr, *d_obs_count = nullptr;
     unsigned *d_err = nullptr;
     double *d_obs = nullptr;
-    i64 obs_cap = 0, nb = 0;
-    i64 *d_bidx = nullptr;
+    i64 obs_cap = 0;
+    int nprobe = 0;
+    i64 *d_bptr = nullptr, *d_bidx = nullptr;
     double *d_bval = nullptr;
+    unsigned *d_done = nullptr;
     double *d_cvec = nullptr;  // compact n_0 doubles for transfers
     // injected noise queue
     double *d_noise = nullptr;
@@ -212,13 +218,23 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *&x, T *
         alt = t;
         return;
     }
-    // 2^dim colours: one launch per plane parity (2d: a single plane)
-    const int nphase = lv.geo.dim == 3 ? 2 : 1;
-    for (int ph = 0; ph < nphase; ++ph) {
-        const int zpar = forward ? ph : nphase - 1 - ph;
-        const unsigned nplanes = (unsigned)((lv.g.N2 - zpar + 1) / 2);
-        if (nplanes == 0) continue;
-        k_sweep_planes<T, EXACT, NOISE><<<nplanes, 512, 0, S.stream>>>(x, f, lv.g, s, zpar, forward ? 1 : 0, nz);
+    // 2^dim colours: all colours in one cooperative launch
+    {
+        const int G0 = (lv.g.N0 + 7) / 8;
+        const i64 items = (i64)((lv.g.N1 + 1) / 2) * ((lv.g.N2 + 1) / 2) * G0;
+        const unsigned grid = (unsigned)std::max<i64>(1, std::min<i64>((items + 255) / 256, lv.coop_blocks));
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(256);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = S.stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int forward_i = forward ? 1 : 0;
+        CK(cudaLaunchKernelEx(&cfg, k_sweep_coop<T, EXACT, NOISE>, x, f, lv.g, s, lv.ncol, forward_i, nz, lv.bar, S.d_err));
         S.launches++;
     }
 }
@@ -334,7 +350,9 @@ static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void
         for (int k = 0; k < 27; ++k) s.w[k] = T(0);
     const i64 nc = lc.geo.n;
     if (S.dim == 3 && !zero_stencil) {
-        const int czc = 8;
+        const int cols = ((lc.g.N0 + RR_TX - 1) / RR_TX) * ((lc.g.N1 + RR_TY - 1) / RR_TY);
+        const int want = std::max(1, (2 * 152 + cols - 1) / cols);  // chunks for about two CTAs per SM
+        const int czc = std::max(1, (lc.g.N2 + want - 1) / want);
         dim3 grid((lc.g.N0 + RR_TX - 1) / RR_TX, (lc.g.N1 + RR_TY - 1) / RR_TY, (lc.g.N2 + czc - 1) / czc);
         if (lv.npt == 7)
             k_resid_restrict_tiled<T, 7><<<grid, RR_THREADS, 0, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, czc);
@@ -395,7 +413,7 @@ void Sampler::resid_restrict(int lev) {
 
 void Sampler::prolong(int lev, double alpha, void *xc, void *x) {
     Level &lv = L[lev], &lc = L[lev + 1];
-    dim3 grid((lv.g.N0 + 127) / 128, lv.g.N1, lv.g.N2);
+    dim3 grid((lc.g.N0 + 1 + 127) / 128, dim > 1 ? lc.g.N1 + 1 : 1, dim > 2 ? lc.g.N2 + 1 : 1);
     if (fp32)
         k_prolong_add<float><<<grid, 128, 0, stream>>>((float *)x, (const float *)xc, lv.g, lc.g, (float)alpha, dim);
     else
@@ -478,9 +496,11 @@ void Sampler::sample(int lev) {
 
 void Sampler::step_end() {
     if (fp32)
-        k_step_end<float><<<1, 256, 0, stream>>>((const float *)L[0].x, nb, d_bidx, d_bval, d_obs, obs_cap, d_obs_count, d_step, d_err);
+        k_step_end<float><<<std::max(nprobe, 1), 256, 0, stream>>>((const float *)L[0].x, nprobe, d_bptr, d_bidx, d_bval, d_obs,
+                                                                  obs_cap, d_obs_count, d_step, d_err, d_done);
     else
-        k_step_end<double><<<1, 256, 0, stream>>>((const double *)L[0].x, nb, d_bidx, d_bval, d_obs, obs_cap, d_obs_count, d_step, d_err);
+        k_step_end<double><<<std::max(nprobe, 1), 256, 0, stream>>>((const double *)L[0].x, nprobe, d_bptr, d_bidx, d_bval,
+                                                                   d_obs, obs_cap, d_obs_count, d_step, d_err, d_done);
     launches++;
 }
 
@@ -713,6 +733,8 @@ void Sampler::build(const mgmc_operator_desc &op) {
     d_step = alloc<u64>(1);
     d_obs_count = alloc<u64>(1);
     d_err = alloc<unsigned>(1);
+    d_done = alloc<unsigned>(1);
+    CK(cudaMemsetAsync(d_done, 0, sizeof(unsigned), stream));
     CK(cudaMemsetAsync(d_step, 0, sizeof(u64), stream));
     CK(cudaMemsetAsync(d_obs_count, 0, sizeof(u64), stream));
     CK(cudaMemsetAsync(d_err, 0, sizeof(unsigned), stream));
@@ -749,6 +771,17 @@ void Sampler::build(const mgmc_operator_desc &op) {
         lv.x_home = lv.x;
         lv.f = talloc(lv.geo.nalloc);
         lv.fused = P.ordering == MGMC_ORDER_MULTICOLOUR && lv.npt == 7 && lv.ncol == 2;
+        if (P.ordering == MGMC_ORDER_MULTICOLOUR && lv.npt == 27) {
+            lv.bar = alloc<unsigned>(2);
+            CK(cudaMemsetAsync(lv.bar, 0, 2 * sizeof(unsigned), stream));
+            int nsm = 0, per_sm = 0;
+            CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, P.device));
+            if (fp32)
+                CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_coop<float, false, NOISE_PHILOX>, 256, 0));
+            else
+                CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_coop<double, false, NOISE_PHILOX>, 256, 0));
+            lv.coop_blocks = std::max(1, nsm * std::min(per_sm, 2));
+        }
         if (lv.fused) {
             lv.x_alt = talloc(lv.geo.nalloc);
             rb_set_smem_attributes();
@@ -1054,26 +1087,31 @@ mgmc_status mgmc_sampler_apply(mgmc_sampler *s, const double *f, double *x, int 
     CK(cudaStreamSynchronize(S.stream));
     unsigned err = 0;
     CK(cudaMemcpy(&err, S.d_err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err & 2u) fail(MGMC_ERR_TIMEOUT, "a grid barrier wait timed out in a cooperative sweep");
     if (err) fail(MGMC_ERR_NONFINITE, "non-finite observable in the chain");
     API_END
 }
 
-mgmc_status mgmc_sampler_set_observable(mgmc_sampler *s, int64_t nnz, const int64_t *idx, const double *val,
-                                        int64_t capacity) {
-    API_BEGIN
-    Sampler &S = impl(s);
-    if (nnz < 0 || capacity < 0 || (nnz > 0 && (!idx || !val))) fail(MGMC_ERR_INVALID_ARGUMENT, "bad observable");
+static void set_probes(Sampler &S, int nprobe, const int64_t *ptr, const int64_t *idx, const double *val,
+                       int64_t capacity) {
+    if (nprobe < 0 || capacity < 0 || (nprobe > 0 && (!ptr || !idx || !val))) fail(MGMC_ERR_INVALID_ARGUMENT, "bad observable");
+    if (nprobe > 65535) fail(MGMC_ERR_UNSUPPORTED, "at most 65535 probes");
     CK(cudaStreamSynchronize(S.stream));
-    std::vector<i64> pidx(nnz);
+    const i64 nnz = nprobe > 0 ? ptr[nprobe] : 0;
+    std::vector<i64> pptr(ptr, ptr + nprobe + 1), pidx(nnz);
+    if (nprobe == 0) pptr.assign(1, 0);
     for (i64 e = 0; e < nnz; ++e) {
         if (idx[e] < 0 || idx[e] >= S.L[0].geo.n) fail(MGMC_ERR_INVALID_ARGUMENT, "observable index out of range");
         pidx[e] = S.L[0].geo.pad(idx[e]);
     }
+    for (int q = 0; q < nprobe; ++q)
+        if (pptr[q + 1] < pptr[q]) fail(MGMC_ERR_INVALID_ARGUMENT, "probe pointers must not decrease");
     std::vector<double> v(val, val + nnz);
+    S.d_bptr = S.upload(pptr);
     S.d_bidx = S.upload(pidx);
     S.d_bval = S.upload(v);
-    S.d_obs = S.alloc<double>(std::max<int64_t>(capacity, 1));
-    S.nb = nnz;
+    S.d_obs = S.alloc<double>((size_t)std::max<int64_t>(capacity, 1) * std::max(nprobe, 1));
+    S.nprobe = nprobe;
     S.obs_cap = capacity;
     CK(cudaMemsetAsync(S.d_obs_count, 0, sizeof(u64), S.stream));
     // the captured step embeds the observable arguments: capture again
@@ -1084,6 +1122,23 @@ mgmc_status mgmc_sampler_set_observable(mgmc_sampler *s, int64_t nnz, const int6
         S.graph = nullptr;
     }
     CK(cudaStreamSynchronize(S.stream));
+}
+
+mgmc_status mgmc_sampler_set_observable(mgmc_sampler *s, int64_t nnz, const int64_t *idx, const double *val,
+                                        int64_t capacity) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (nnz < 0) fail(MGMC_ERR_INVALID_ARGUMENT, "bad observable");
+    const int64_t ptr[2] = {0, nnz};
+    set_probes(S, nnz > 0 ? 1 : 0, ptr, idx, val, capacity);
+    API_END
+}
+
+mgmc_status mgmc_sampler_set_probes(mgmc_sampler *s, int nprobe, const int64_t *ptr, const int64_t *idx,
+                                    const double *val, int64_t capacity) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    set_probes(S, nprobe, ptr, idx, val, capacity);
     API_END
 }
 
@@ -1095,12 +1150,14 @@ mgmc_status mgmc_sampler_read_observations(mgmc_sampler *s, double *out, int64_t
     u64 c = 0;
     CK(cudaMemcpy(&c, S.d_obs_count, sizeof(c), cudaMemcpyDeviceToHost));
     i64 k = std::min<i64>((i64)c, S.obs_cap);
-    k = std::min<i64>(k, capacity);
-    if (k > 0 && out) CK(cudaMemcpy(out, S.d_obs, k * sizeof(double), cudaMemcpyDeviceToHost));
+    const int np = std::max(S.nprobe, 1);
+    k = std::min<i64>(k, capacity / np);
+    if (k > 0 && out) CK(cudaMemcpy(out, S.d_obs, (size_t)k * np * sizeof(double), cudaMemcpyDeviceToHost));
     *count = (int64_t)c;
     CK(cudaMemset(S.d_obs_count, 0, sizeof(u64)));
     unsigned err = 0;
     CK(cudaMemcpy(&err, S.d_err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err & 2u) fail(MGMC_ERR_TIMEOUT, "a grid barrier wait timed out in a cooperative sweep");
     if (err) fail(MGMC_ERR_NONFINITE, "non-finite observable in the chain");
     API_END
 }

@@ -8,8 +8,8 @@
 // Kernels (one V-cycle at level l uses them in this order):
 //   k_sweep_rb          red-black SOR sweep of the fine 7-point level, both
 //                       colours in one pass (multicolour order)
-//   k_sweep_planes      8-colour SOR sweep of a 27-point level, one launch per
-//                       plane parity (multicolour order)
+//   k_sweep_coop        8-colour SOR sweep of a 27-point level in one
+//                       cooperative launch, grid barrier between colours
 //   k_sweep_wavefront   lexicographic SOR sweep as a hyperplane wavefront
 //                       (one CTA; parity mode)
 //   k_bt_x_z            y = B^T x and the m x m low-rank solve
@@ -75,19 +75,25 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 ctr, uint2 key) {
     return ctr;
 }
 
-// Two Box-Muller pairs in FP32 (Box & Muller 1958).  u1 is in (0, 1]: the
-// product of a value <= 2^32 with 2^-32 plus 2^-33 rounds to at most 1.0f,
-// so the logarithm is never positive.
+// Two Box-Muller pairs in FP32 (Box & Muller 1958) with the SFU
+// approximations of log2, reciprocal square root and sine/cosine (absolute
+// error of order 1e-6 per normal).  u1 is in (0, 1]: the product of a
+// value <= 2^32 with 2^-32 plus 2^-33 rounds to at most 1.0f, so -log2(u1)
+// is never negative; the angle lies in [-pi, pi), the accurate range of the
+// fast sine and cosine.
 __device__ __forceinline__ float4 normals4(uint4 r) {
     const float two_m32 = 2.3283064365386963e-10f;  // 2^-32
     const float two_m33 = 1.1641532182693481e-10f;  // 2^-33
+    const float m2ln2 = -1.3862943611198906f;       // -2 ln 2
+    const float twopi = 6.283185307179586f;
     float u1a = __fmaf_rn(__uint2float_rn(r.x), two_m32, two_m33);
     float u1b = __fmaf_rn(__uint2float_rn(r.z), two_m32, two_m33);
-    float ra = sqrtf(-2.0f * logf(u1a));
-    float rb = sqrtf(-2.0f * logf(u1b));
+    float qa = fmaxf(m2ln2 * __log2f(u1a), 1e-30f);
+    float qb = fmaxf(m2ln2 * __log2f(u1b), 1e-30f);
+    float ra = qa * rsqrtf(qa), rb = qb * rsqrtf(qb);
     float sa, ca, sb, cb;
-    sincospif(__uint2float_rz(r.y) * (2.0f * two_m32), &sa, &ca);
-    sincospif(__uint2float_rz(r.w) * (2.0f * two_m32), &sb, &cb);
+    __sincosf(__fmaf_rn(__uint2float_rz(r.y), two_m32, -0.5f) * twopi, &sa, &ca);
+    __sincosf(__fmaf_rn(__uint2float_rz(r.w), two_m32, -0.5f) * twopi, &sb, &cb);
     return make_float4(ra * ca, ra * sa, rb * cb, rb * sb);
 }
 
@@ -235,32 +241,36 @@ __device__ __forceinline__ T rb_update(T xo, T xm, T xp, T ym, T yp, T zm, T zp,
     return xo + s.omega_diag * (cval - res);
 }
 
+template <typename T>
+constexpr size_t rb_smem_bytes() {
+    return sizeof(T) * (4 * RB_H2 * RB_W2 + 3 * RB_H1 * RB_W1);
+}
+
 // Thread = pair of adjacent halo-1 columns (one of each colour on every
 // plane), so both colours' work is spread evenly over the lanes.  Per plane
 // kk:  [A] first colour of plane kk on the halo-1 region,  [B] sync,
 // [C] second colour of plane kk-1 and both colours written out,  [D] the
 // old plane kk+2 (loaded into registers one plane earlier) stored to shared
 // memory,  [E] plane kk+3 loaded into registers,  [F] sync.  The global
-// load latency is hidden behind one plane of work.
-template <typename T>
-constexpr size_t rb_smem_bytes() {
-    return sizeof(T) * (4 * RB_H2 * RB_W2 + 3 * RB_H1 * RB_W1);
-}
-
+// load latency is hidden behind one plane of work; every address is a
+// per-thread in-plane offset computed once plus the plane offset.
 template <typename T, bool EXACT, int NOISE>
 __global__ void __launch_bounds__(RB_THREADS, 2) k_sweep_rb(const T *__restrict__ xin, T *__restrict__ xout,
                                                            const T *__restrict__ f, Grid3 g, StencilArg<T> s,
                                                            int first, int cz, NoiseArgs nz) {
     extern __shared__ __align__(16) unsigned char rb_smem[];
-    T(*xo)[RB_H2][RB_W2] = reinterpret_cast<T(*)[RB_H2][RB_W2]>(rb_smem);
-    T(*Fr)[RB_H1][RB_W1] = reinterpret_cast<T(*)[RB_H1][RB_W1]>(rb_smem + sizeof(T) * 4 * RB_H2 * RB_W2);
+    T *xo = reinterpret_cast<T *>(rb_smem);                          // [4][RB_H2][RB_W2]
+    T *Fr = reinterpret_cast<T *>(rb_smem + sizeof(T) * 4 * RB_H2 * RB_W2);  // [3][RB_H1][RB_W1]
+    constexpr int P2 = RB_H2 * RB_W2, P1 = RB_H1 * RB_W1;
     const int a0 = blockIdx.x * RB_TX, b0 = blockIdx.y * RB_TY;
     const int c0 = blockIdx.z * cz, c1 = min(c0 + cz, g.N2);
     const int px = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int b = b0 - 1 + ty;
+    const int sy = (int)g.sy;
+    // this thread's two columns
     const bool row_in = b >= 0 && b < g.N1;
     const bool row_tile = row_in && ty >= 1 && ty <= RB_TY;
-    int ac[2];
+    int ac[2], foff[2], s2[2], s1[2];
     bool cin[2], ctile[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -268,30 +278,37 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_sweep_rb(const T *__restrict_
         ac[h] = a0 - 1 + tx;
         cin[h] = row_in && ac[h] >= 0 && ac[h] < g.N0;
         ctile[h] = row_tile && cin[h] && tx >= 1 && tx <= RB_TX;
+        foff[h] = (b + 1) * sy + (ac[h] + 1);  // in-plane padded offset
+        s2[h] = (ty + 1) * RB_W2 + (tx + 1);   // halo-2 tile index
+        s1[h] = ty * RB_W1 + tx;               // halo-1 tile index
+    }
+    // the thread's share of the halo-2 plane
+    int goff[RB_NLD], soff[RB_NLD];
+    bool gok[RB_NLD];
+#pragma unroll
+    for (int j = 0; j < RB_NLD; ++j) {
+        const int i = threadIdx.x + j * RB_THREADS;
+        const int la = i % RB_W2, lb = i / RB_W2;
+        const int ga = a0 - 2 + la, gb = b0 - 2 + lb;
+        gok[j] = i < P2 && ga >= 0 && ga < g.N0 && gb >= 0 && gb < g.N1;
+        goff[j] = (gb + 1) * sy + (ga + 1);
+        soff[j] = i < P2 ? i : -1;
     }
     ColumnNoise cn[2];
     cn[0].init();
     cn[1].init();
     T pre[RB_NLD];
     auto fetch = [&](int c) {
+        const bool pin = c >= 0 && c < g.N2;
+        const T *base = xin + (i64)(c + 1) * g.sz;
 #pragma unroll
-        for (int j = 0; j < RB_NLD; ++j) {
-            const int i = threadIdx.x + j * RB_THREADS;
-            T v = T(0);
-            if (i < RB_W2 * RB_H2) {
-                const int la = i % RB_W2, lb = i / RB_W2;
-                const int ga = a0 - 2 + la, gb = b0 - 2 + lb;
-                if (c >= 0 && c < g.N2 && ga >= 0 && ga < g.N0 && gb >= 0 && gb < g.N1) v = xin[g.pad(ga, gb, c)];
-            }
-            pre[j] = v;
-        }
+        for (int j = 0; j < RB_NLD; ++j) pre[j] = (pin && gok[j]) ? base[goff[j]] : T(0);
     };
     auto commit = [&](int c) {
+        T *dst = xo + (c & 3) * P2;
 #pragma unroll
-        for (int j = 0; j < RB_NLD; ++j) {
-            const int i = threadIdx.x + j * RB_THREADS;
-            if (i < RB_W2 * RB_H2) xo[c & 3][i / RB_W2][i % RB_W2] = pre[j];
-        }
+        for (int j = 0; j < RB_NLD; ++j)
+            if (soff[j] >= 0) dst[soff[j]] = pre[j];
     };
     auto s3 = [](int c) { return ((c % 3) + 3) % 3; };
     fetch(c0 - 2);
@@ -304,42 +321,48 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_sweep_rb(const T *__restrict_
     __syncthreads();
     for (int kk = c0 - 1; kk <= c1; ++kk) {
         // [A] first colour of plane kk
-        const bool plane_in = kk >= 0 && kk < g.N2;
+        {
+            const bool plane_in = kk >= 0 && kk < g.N2;
+            const T *X0 = xo + (kk & 3) * P2, *Xm = xo + ((kk - 1) & 3) * P2, *Xp = xo + ((kk + 1) & 3) * P2;
+            const T *fk = f + (i64)(kk + 1) * g.sz;
+            T *F = Fr + s3(kk) * P1;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int tx = 2 * px + h, a = ac[h];
-            T fval = T(0);
-            if (plane_in && cin[h] && ((a + b + kk) & 1) == first) {
-                const int lx = tx + 1, ly = ty + 1;
-                T xi = T(0);
-                if (NOISE == NOISE_PHILOX) xi = (T)cn[h].get(nz, g, a, b, kk);
-                if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, kk)];
-                fval = rb_update<T, EXACT>(xo[kk & 3][ly][lx], xo[kk & 3][ly][lx - 1], xo[kk & 3][ly][lx + 1],
-                                           xo[kk & 3][ly - 1][lx], xo[kk & 3][ly + 1][lx], xo[(kk - 1) & 3][ly][lx],
-                                           xo[(kk + 1) & 3][ly][lx], s, f[g.pad(a, b, kk)], NOISE != NOISE_NONE, xi);
+            for (int h = 0; h < 2; ++h) {
+                T fval = T(0);
+                if (plane_in && cin[h] && ((ac[h] + b + kk) & 1) == first) {
+                    const int q = s2[h];
+                    T xi = T(0);
+                    if (NOISE == NOISE_PHILOX) xi = (T)cn[h].get(nz, g, ac[h], b, kk);
+                    if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(ac[h], b, kk)];
+                    fval = rb_update<T, EXACT>(X0[q], X0[q - 1], X0[q + 1], X0[q - RB_W2], X0[q + RB_W2], Xm[q], Xp[q], s,
+                                               fk[foff[h]], NOISE != NOISE_NONE, xi);
+                }
+                F[s1[h]] = fval;
             }
-            Fr[s3(kk)][ty][tx] = fval;
         }
         __syncthreads();
         // [C] second colour of plane c = kk-1, both colours written
         const int c = kk - 1;
         if (c >= c0 && c < c1) {
+            const T *F0 = Fr + s3(c) * P1, *Fm = Fr + s3(c - 1) * P1, *Fp = Fr + s3(c + 1) * P1;
+            const T *X0 = xo + (c & 3) * P2;
+            const T *fc = f + (i64)(c + 1) * g.sz;
+            T *out = xout + (i64)(c + 1) * g.sz;
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 if (!ctile[h]) continue;
-                const int tx = 2 * px + h, a = ac[h];
-                T out;
-                if (((a + b + c) & 1) == first) {
-                    out = Fr[s3(c)][ty][tx];
+                const int q = s1[h];
+                T v;
+                if (((ac[h] + b + c) & 1) == first) {
+                    v = F0[q];
                 } else {
                     T xi = T(0);
-                    if (NOISE == NOISE_PHILOX) xi = (T)cn[h].get(nz, g, a, b, c);
-                    if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
-                    out = rb_update<T, EXACT>(xo[c & 3][ty + 1][tx + 1], Fr[s3(c)][ty][tx - 1], Fr[s3(c)][ty][tx + 1],
-                                              Fr[s3(c)][ty - 1][tx], Fr[s3(c)][ty + 1][tx], Fr[s3(c - 1)][ty][tx],
-                                              Fr[s3(c + 1)][ty][tx], s, f[g.pad(a, b, c)], NOISE != NOISE_NONE, xi);
+                    if (NOISE == NOISE_PHILOX) xi = (T)cn[h].get(nz, g, ac[h], b, c);
+                    if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(ac[h], b, c)];
+                    v = rb_update<T, EXACT>(X0[s2[h]], F0[q - 1], F0[q + 1], F0[q - RB_W1], F0[q + RB_W1], Fm[q], Fp[q], s,
+                                            fc[foff[h]], NOISE != NOISE_NONE, xi);
                 }
-                xout[g.pad(a, b, c)] = out;
+                out[foff[h]] = v;
             }
         }
         // [D], [E]
@@ -349,25 +372,60 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_sweep_rb(const T *__restrict_
     }
 }
 
-// Multicolour sweep of a 2^dim-colour (9- / 27-point) level organised by
-// planes: the colours with z-parity p touch no other plane of parity p, so
-// one launch updates all planes of one parity, one CTA per plane running the
-// plane's four in-plane colours separated by __syncthreads.  The update
-// order and the noise are those of the colour-by-colour sweep (colour index
+// ---------------------------------------------------------- grid barrier
+// Barrier across the CTAs of one cooperative launch (all CTAs co-resident).
+// bar[0] counts arrivals, bar[1] is the generation.  A wait gives up after
+// GRID_BARRIER_SPINS polls (well over a second), raises bit 2 of *err and
+// returns, so a missing CTA costs a wrong sample and an error status, never
+// a hung GPU.
+constexpr long long GRID_BARRIER_SPINS = 1ll << 24;
+
+__device__ __forceinline__ void grid_barrier(unsigned *bar, unsigned *err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = bar + 1;
+        const unsigned gen = *vgen;
+        __threadfence();
+        const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+        if (atomicAdd(bar, 1u) == nb - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long it = 0;
+            while (*vgen == gen) {
+                if (++it > GRID_BARRIER_SPINS) {
+                    atomicOr(err, 2u);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// Multicolour sweep of a 2^dim-colour (9- / 27-point) level in one
+// cooperative launch: the colours run in order, separated by grid barriers.
+// Thread work item = (8-point x-group, row of the colour); the <= 4 points of
+// the colour in the group share one Philox block.  Colour index
 // (a & 1) | (b & 1) << 1 | (c & 1) << 2, ascending forward, descending
-// backward), so the chain is the same.
+// backward.
 template <typename T, bool EXACT, int NOISE>
-__global__ void __launch_bounds__(512) k_sweep_planes(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
-                                                       StencilArg<T> s, int zpar, int forward, NoiseArgs nz) {
-    const int c = 2 * blockIdx.x + zpar;
-    if (c >= g.N2) return;
+__global__ void __launch_bounds__(256) k_sweep_coop(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
+                                                     StencilArg<T> s, int ncol, int forward, NoiseArgs nz,
+                                                     unsigned *bar, unsigned *err) {
     const int G0 = (g.N0 + 7) >> 3;
-    for (int cc = 0; cc < 4; ++cc) {
-        const int col2 = forward ? cc : 3 - cc;
-        const int pa = col2 & 1, pb = col2 >> 1;
-        const int nb = (g.N1 - pb + 1) >> 1;
-        for (int t = threadIdx.x; t < nb * G0; t += blockDim.x) {
-            const int grp = t % G0, b = 2 * (t / G0) + pb;
+    const int nthreads = gridDim.x * blockDim.x;
+    for (int cc = 0; cc < ncol; ++cc) {
+        const int col = forward ? cc : ncol - 1 - cc;
+        const int pa = col & 1, pb = (col >> 1) & 1, pc = (col >> 2) & 1;
+        const int nb = (g.N1 - pb + 1) >> 1, nc = (g.N2 - pc + 1) >> 1;
+        const int items = nb * nc * G0;
+        for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < items; t += nthreads) {
+            const int grp = t % G0, row = t / G0;
+            const int b = 2 * (row % nb) + pb, c = 2 * (row / nb) + pc;
             float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f);
             if (NOISE == NOISE_PHILOX) nrm = point_normals(nz, g, 8 * grp + pa, b, c);
 #pragma unroll
@@ -380,7 +438,7 @@ __global__ void __launch_bounds__(512) k_sweep_planes(T *__restrict__ x, const T
                 sor_point<T, 27, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
             }
         }
-        __syncthreads();
+        if (cc + 1 < ncol) grid_barrier(bar, err);
     }
 }
 
@@ -489,16 +547,27 @@ __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRank
         w[k] = lr.sinv_sqrt[k] * xi;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < m; k += blockDim.x) {
-        double t = lr.y[k];
-        for (int q = 0; q < m; ++q) t += lr.G[(i64)k * m + q] * w[q];
-        v[k] = t;
+    // m x m products, four threads per row (partial dot products combined
+    // with shuffles inside aligned groups of four lanes)
+    const int sub = threadIdx.x & 3;
+    for (int k0 = 0; k0 < m; k0 += blockDim.x / 4) {
+        const int k = k0 + (threadIdx.x >> 2);
+        double t = 0.0;
+        if (k < m)
+            for (int q = sub; q < m; q += 4) t += lr.G[(i64)k * m + q] * w[q];
+        t += __shfl_xor_sync(0xffffffffu, t, 1);
+        t += __shfl_xor_sync(0xffffffffu, t, 2);
+        if (k < m && sub == 0) v[k] = lr.y[k] + t;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    for (int k0 = 0; k0 < m; k0 += blockDim.x / 4) {
+        const int k = k0 + (threadIdx.x >> 2);
         double t = 0.0;
-        for (int q = 0; q < m; ++q) t += lr.Sinv[(i64)k * m + q] * v[q];
-        lr.z[k] = w[k] - t;
+        if (k < m)
+            for (int q = sub; q < m; q += 4) t += lr.Sinv[(i64)k * m + q] * v[q];
+        t += __shfl_xor_sync(0xffffffffu, t, 1);
+        t += __shfl_xor_sync(0xffffffffu, t, 2);
+        if (k < m && sub == 0) lr.z[k] = w[k] - t;
     }
 }
 
@@ -667,34 +736,62 @@ __global__ void __launch_bounds__(256) k_add_Bq(T *__restrict__ dst, i64 nrows, 
 template <typename T>
 __global__ void __launch_bounds__(128) k_prolong_add(T *__restrict__ x, const T *__restrict__ xc, Grid3 gf, Grid3 gc,
                                                       T alpha, int dim) {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= gf.N0) return;
-    int co[3] = {a + 1, (int)blockIdx.y + 1, (int)blockIdx.z + 1};
-    int lo[3], np[3];
-    T wt[3];
+    // coarse cell (i, j, k), 0 <= i <= Nc0 etc., owns the fine vertices with
+    // 1-based coordinates 2 i + {0, 1} (those inside the interior); its
+    // corners are the coarse vertices i, i+1 (1-based, ghosts are zero)
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = dim > 1 ? (int)blockIdx.y : 0, k = dim > 2 ? (int)blockIdx.z : 0;
+    if (i > gc.N0) return;
+    const int ny = dim > 1 ? 2 : 1, nz = dim > 2 ? 2 : 1;
+    T cv[2][2][2];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        if (d >= dim) {
-            lo[d] = 1;
-            np[d] = 1;
-            wt[d] = T(1);
-        } else if ((co[d] & 1) == 0) {
-            lo[d] = co[d] >> 1;
-            np[d] = 1;
-            wt[d] = T(1);
-        } else {
-            lo[d] = co[d] >> 1;
-            np[d] = 2;
-            wt[d] = T(0.5);
+    for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+            for (int dx = 0; dx < 2; ++dx) {
+                const int ci = i + dx, cj = dim > 1 ? j + dy : 1, ck = dim > 2 ? k + dz : 1;
+                const bool use = (dy < ny) && (dz < nz);
+                cv[dz][dy][dx] = use ? xc[(i64)ck * gc.sz + (i64)cj * gc.sy + ci] : T(0);
+            }
+#pragma unroll
+    for (int oz = 0; oz < 2; ++oz) {
+        if (oz >= nz) break;
+        const int fk = dim > 2 ? 2 * k + oz : 1;
+        if (fk < 1 || fk > gf.N2) continue;
+#pragma unroll
+        for (int oy = 0; oy < 2; ++oy) {
+            if (oy >= ny) break;
+            const int fj = dim > 1 ? 2 * j + oy : 1;
+            if (fj < 1 || fj > gf.N1) continue;
+#pragma unroll
+            for (int ox = 0; ox < 2; ++ox) {
+                const int fi = 2 * i + ox;
+                if (fi < 1 || fi > gf.N0) continue;
+                // even coordinate: the vertex itself (weight 1); odd: half
+                // of each neighbour
+                T acc = T(0);
+#pragma unroll
+                for (int dz = 0; dz < 2; ++dz) {
+                    const T wz = dim > 2 ? (oz == 0 ? (dz == 0 ? T(1) : T(0)) : T(0.5)) : (dz == 0 ? T(1) : T(0));
+                    if (wz == T(0)) continue;
+#pragma unroll
+                    for (int dy = 0; dy < 2; ++dy) {
+                        const T wy = dim > 1 ? (oy == 0 ? (dy == 0 ? T(1) : T(0)) : T(0.5)) : (dy == 0 ? T(1) : T(0));
+                        if (wy == T(0)) continue;
+#pragma unroll
+                        for (int dx = 0; dx < 2; ++dx) {
+                            const T wx = ox == 0 ? (dx == 0 ? T(1) : T(0)) : T(0.5);
+                            if (wx == T(0)) continue;
+                            acc += wx * wy * wz * cv[dz][dy][dx];
+                        }
+                    }
+                }
+                const i64 P = (i64)fk * gf.sz + (i64)fj * gf.sy + fi;
+                x[P] += alpha * acc;
+            }
         }
     }
-    T acc = T(0);
-    for (int k = 0; k < np[2]; ++k)
-        for (int j = 0; j < np[1]; ++j)
-            for (int i = 0; i < np[0]; ++i)
-                acc += wt[0] * wt[1] * wt[2] * xc[(i64)(lo[2] + k) * gc.sz + (i64)(lo[1] + j) * gc.sy + (lo[0] + i)];
-    const i64 P = (i64)co[2] * gf.sz + (i64)co[1] * gf.sy + co[0];
-    x[P] += alpha * acc;
 }
 
 // ----------------------------------------------------- stencil apply
@@ -850,27 +947,38 @@ __global__ void __launch_bounds__(256) k_chol_gemv_upper(const double *__restric
 }
 
 // ------------------------------------------------------------ step end
-// Observable z = b^T x of measure_sampling_time (sampling_time.cc:40),
-// stored at obs[count] while count < capacity; a non-finite value raises
-// the error flag.  Then the step counter that keys the Philox streams
-// advances.  One CTA; runs after every other kernel of the step.
+// Observables z_p = b_p^T x of measure_sampling_time (sampling_time.cc:40),
+// one CTA per probe p (probe p's entries are bptr[p]..bptr[p+1]), stored at
+// obs[k * nprobe + p] for step k while k < capacity; a non-finite value
+// raises the error flag.  The last CTA to finish advances the observation
+// count and the step counter that keys the Philox streams.  Runs after
+// every other kernel of the step.
 template <typename T>
-__global__ void __launch_bounds__(256) k_step_end(const T *__restrict__ x, i64 nb, const i64 *__restrict__ bidx,
-                                                   const double *__restrict__ bval, double *__restrict__ obs,
-                                                   i64 capacity, u64 *__restrict__ obs_count,
-                                                   u64 *__restrict__ d_step, unsigned *__restrict__ err) {
+__global__ void __launch_bounds__(256) k_step_end(const T *__restrict__ x, int nprobe, const i64 *__restrict__ bptr,
+                                                   const i64 *__restrict__ bidx, const double *__restrict__ bval,
+                                                   double *__restrict__ obs, i64 capacity, u64 *__restrict__ obs_count,
+                                                   u64 *__restrict__ d_step, unsigned *__restrict__ err,
+                                                   unsigned *__restrict__ done) {
     __shared__ double sh[32];
-    double acc = 0.0;
-    for (i64 e = threadIdx.x; e < nb; e += blockDim.x) acc += bval[e] * (double)x[bidx[e]];
-    acc = block_sum<256>(acc, sh);
-    if (threadIdx.x == 0) {
-        if (nb > 0) {
-            u64 k = *obs_count;
-            if ((i64)k < capacity) obs[k] = acc;
-            *obs_count = k + 1;
+    __shared__ bool last;
+    const int p = blockIdx.x;
+    if (nprobe > 0) {
+        double acc = 0.0;
+        for (i64 e = bptr[p] + threadIdx.x; e < bptr[p + 1]; e += blockDim.x) acc += bval[e] * (double)x[bidx[e]];
+        acc = block_sum<256>(acc, sh);
+        if (threadIdx.x == 0) {
+            const u64 k = *obs_count;
+            if ((i64)k < capacity) obs[k * nprobe + p] = acc;
             if (!isfinite(acc)) atomicOr(err, 1u);
         }
+    }
+    __threadfence();
+    if (threadIdx.x == 0) last = (atomicAdd(done, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        if (nprobe > 0) *obs_count += 1ull;
         *d_step += 1ull;
+        *done = 0u;
     }
 }
 
