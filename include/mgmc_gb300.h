@@ -191,6 +191,30 @@ mgmc_status mgmc_level_sor(mgmc_sampler *s, int level, int direction, int with_n
 mgmc_status mgmc_level_sweep_device(mgmc_sampler *s, int level, int direction, int with_noise, int with_lowrank,
                                     int64_t nrepeat);
 
+/* ------------------------------------------- no-allocation operator apply */
+/* No counterpart in the reference.  y = A x for A = A_0 + B Sigma^{-1} B^T
+ * (the product LinearOperator::apply computes) without allocating device
+ * memory, for callers that cannot call cudaMalloc: work captured into a
+ * CUDA graph in global capture mode, applications whose device memory is
+ * owned by their own pool and lent to the library buffer by buffer, and
+ * latency-critical loops that cannot afford cudaMalloc's device-wide
+ * synchronisation.  `stencil` is a host array; B_colptr/B_rowidx/B_val
+ * (column-compressed, as in mgmc_operator_desc), Sigma, x and y are device
+ * pointers of the current device, vectors in the reference's vertex order.
+ * Work is queued on `cuda_stream` (NULL = default stream) and the call
+ * returns without waiting for it.
+ * The only scratch, B^T x, lives in a static device array of
+ * MGMC_NOALLOC_MAX_M doubles (32 KiB) that every GPU loading the library
+ * holds until the process exits; m > MGMC_NOALLOC_MAX_M is rejected with
+ * MGMC_ERR_INVALID_ARGUMENT.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  All calls on a device share the array: calls
+ * that overlap on the GPU race and must be ordered by the caller. */
+#define MGMC_NOALLOC_MAX_M 4096
+mgmc_status mgmc_measured_apply_noalloc(int dim, int nx, int ny, int nz, const double stencil[27], int m,
+                                        const int64_t *B_colptr, const int64_t *B_rowidx, const double *B_val,
+                                        const double *Sigma, const double *x, double *y, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

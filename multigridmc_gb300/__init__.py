@@ -107,6 +107,8 @@ SIGNATURES = {
     "mgmc_level_prolongate_add": (C.c_int, [_P, C.c_int, C.c_double, _D, _D]),
     "mgmc_level_sor": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _D, _D]),
     "mgmc_level_sweep_device": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64]),
+    "mgmc_measured_apply_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _D, C.c_int, _P, _P, _P, _P,
+                                              _P, _P, _P]),
 }
 
 
@@ -165,6 +167,15 @@ def galerkin_stencil(dim, fine):
     out = np.zeros(27)
     _check(load().mgmc_galerkin_stencil(dim, _dp(fine), _dp(out)))
     return out
+
+
+def measured_apply_noalloc(op, B_colptr, B_rowidx, B_val, Sigma, x, y, stream=0):
+    """mgmc_measured_apply_noalloc: y = A x with device buffers given as raw
+    addresses (integers); nothing is allocated by the library.  Asynchronous
+    on `stream` (a cudaStream_t address, 0 = default stream)."""
+    st = _f64(op.stencil)
+    _check(load().mgmc_measured_apply_noalloc(op.dim, *_shape3(op.shape), _dp(st), op.m, B_colptr, B_rowidx,
+                                              B_val, Sigma, x, y, stream))
 
 
 def measurement_vector(shape, x0, radius):

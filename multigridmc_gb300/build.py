@@ -19,6 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SOURCES = {
     "api.o": ("api.cu", ["kernels.cuh", "setup.h"]),
+    "noalloc.o": ("noalloc.cu", []),
     "setup.o": ("setup.cc", ["setup.h"]),
 }
 
