@@ -351,8 +351,8 @@ static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void
     const i64 nc = lc.geo.n;
     if (S.dim == 3 && !zero_stencil) {
         const int cols = ((lc.g.N0 + RR_TX - 1) / RR_TX) * ((lc.g.N1 + RR_TY - 1) / RR_TY);
-        const int want = std::max(1, (2 * 152 + cols - 1) / cols);  // chunks for about two CTAs per SM
-        const int czc = std::max(1, (lc.g.N2 + want - 1) / want);
+        const int want = std::max(1, (4 * 152 + cols - 1) / cols);  // chunks for about four CTAs per SM
+        const int czc = std::max(2, (lc.g.N2 + want - 1) / want);
         dim3 grid((lc.g.N0 + RR_TX - 1) / RR_TX, (lc.g.N1 + RR_TY - 1) / RR_TY, (lc.g.N2 + czc - 1) / czc);
         if (lv.npt == 7)
             k_resid_restrict_tiled<T, 7><<<grid, RR_THREADS, 0, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, czc);

@@ -253,13 +253,16 @@ constexpr size_t rb_smem_bytes() {
 // old plane kk+2 (loaded into registers one plane earlier) stored to shared
 // memory,  [E] plane kk+3 loaded into registers,  [F] sync.  The global
 // load latency is hidden behind one plane of work; every address is a
-// per-thread in-plane offset computed once plus the plane offset.
+// per-thread in-plane offset computed once plus the plane offset.  Each
+// column's normals come four planes per Philox block; the blocks of both
+// columns are generated together whenever the plane index enters a new
+// group of four, so the control flow stays uniform across the warp.
 template <typename T, bool EXACT, int NOISE>
-__global__ void __launch_bounds__(RB_THREADS, 2) k_sweep_rb(const T *__restrict__ xin, T *__restrict__ xout,
+__global__ void __launch_bounds__(RB_THREADS, 3) k_sweep_rb(const T *__restrict__ xin, T *__restrict__ xout,
                                                            const T *__restrict__ f, Grid3 g, StencilArg<T> s,
                                                            int first, int cz, NoiseArgs nz) {
     extern __shared__ __align__(16) unsigned char rb_smem[];
-    T *xo = reinterpret_cast<T *>(rb_smem);                          // [4][RB_H2][RB_W2]
+    T *xo = reinterpret_cast<T *>(rb_smem);                                   // [4][RB_H2][RB_W2]
     T *Fr = reinterpret_cast<T *>(rb_smem + sizeof(T) * 4 * RB_H2 * RB_W2);  // [3][RB_H1][RB_W1]
     constexpr int P2 = RB_H2 * RB_W2, P1 = RB_H1 * RB_W1;
     const int a0 = blockIdx.x * RB_TX, b0 = blockIdx.y * RB_TY;
@@ -267,7 +270,6 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_sweep_rb(const T *__restrict_
     const int px = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int b = b0 - 1 + ty;
     const int sy = (int)g.sy;
-    // this thread's two columns
     const bool row_in = b >= 0 && b < g.N1;
     const bool row_tile = row_in && ty >= 1 && ty <= RB_TY;
     int ac[2], foff[2], s2[2], s1[2];
@@ -282,7 +284,9 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_sweep_rb(const T *__restrict_
         s2[h] = (ty + 1) * RB_W2 + (tx + 1);   // halo-2 tile index
         s1[h] = ty * RB_W1 + tx;               // halo-1 tile index
     }
-    // the thread's share of the halo-2 plane
+    // the column of the pair that holds the first colour on plane kk is
+    // column fc0 for even kk, 1 - fc0 for odd kk
+    const int fc0 = ((ac[0] + b) & 1) == first ? 0 : 1;
     int goff[RB_NLD], soff[RB_NLD];
     bool gok[RB_NLD];
 #pragma unroll
@@ -294,9 +298,6 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_sweep_rb(const T *__restrict_
         goff[j] = (gb + 1) * sy + (ga + 1);
         soff[j] = i < P2 ? i : -1;
     }
-    ColumnNoise cn[2];
-    cn[0].init();
-    cn[1].init();
     T pre[RB_NLD];
     auto fetch = [&](int c) {
         const bool pin = c >= 0 && c < g.N2;
@@ -304,71 +305,92 @@ __global__ void __launch_bounds__(RB_THREADS, 2) k_sweep_rb(const T *__restrict_
 #pragma unroll
         for (int j = 0; j < RB_NLD; ++j) pre[j] = (pin && gok[j]) ? base[goff[j]] : T(0);
     };
-    auto commit = [&](int c) {
-        T *dst = xo + (c & 3) * P2;
+    auto commit = [&](T *dst) {
 #pragma unroll
         for (int j = 0; j < RB_NLD; ++j)
             if (soff[j] >= 0) dst[soff[j]] = pre[j];
     };
-    auto s3 = [](int c) { return ((c % 3) + 3) % 3; };
+    // ring slots: old planes kk-1, kk, kk+1 (and kk+2 being stored), F planes
+    // kk-2, kk-1, kk; rotated by one every plane
+    T *Xm = xo, *X0 = xo + P2, *Xp = xo + 2 * P2, *Xn = xo + 3 * P2;
+    T *Fm = Fr, *F0 = Fr + P1, *Fp = Fr + 2 * P1;
     fetch(c0 - 2);
-    commit(c0 - 2);
+    commit(Xm);  // plane c0-2 goes to the slot that is plane kk-1 at kk = c0-1
     fetch(c0 - 1);
-    commit(c0 - 1);
+    commit(X0);
     fetch(c0);
-    commit(c0);
+    commit(Xp);
     fetch(c0 + 1);
+    // with the loop starting at kk = c0-1 the slots must read kk-1 = c0-2,
+    // kk = c0-1, kk+1 = c0
     __syncthreads();
+    float4 nb_cur[2], nb_prev[2];
+    int q_cur = -1000;
+    nb_cur[0] = nb_cur[1] = nb_prev[0] = nb_prev[1] = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int kk = c0 - 1; kk <= c1; ++kk) {
+        if (NOISE == NOISE_PHILOX && (kk >> 2) != q_cur) {
+            q_cur = kk >> 2;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                nb_prev[h] = nb_cur[h];
+                nb_cur[h] = cin[h] ? column_normals(nz, g, ac[h], b, q_cur) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+        // column A: first colour on plane kk, second colour on plane kk-1;
+        // column B the other one (selects, not indexing, keep them in registers)
+        const bool a1 = ((kk & 1) ? 1 - fc0 : fc0) == 1;
+        const int aA = a1 ? ac[1] : ac[0];
+        const int s2A = a1 ? s2[1] : s2[0], s1A = a1 ? s1[1] : s1[0], s1B = a1 ? s1[0] : s1[1];
+        const int foA = a1 ? foff[1] : foff[0], foB = a1 ? foff[0] : foff[1];
+        const bool cinA = a1 ? cin[1] : cin[0];
+        const bool tA = a1 ? ctile[1] : ctile[0], tB = a1 ? ctile[0] : ctile[1];
         // [A] first colour of plane kk
         {
             const bool plane_in = kk >= 0 && kk < g.N2;
-            const T *X0 = xo + (kk & 3) * P2, *Xm = xo + ((kk - 1) & 3) * P2, *Xp = xo + ((kk + 1) & 3) * P2;
             const T *fk = f + (i64)(kk + 1) * g.sz;
-            T *F = Fr + s3(kk) * P1;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                T fval = T(0);
-                if (plane_in && cin[h] && ((ac[h] + b + kk) & 1) == first) {
-                    const int q = s2[h];
-                    T xi = T(0);
-                    if (NOISE == NOISE_PHILOX) xi = (T)cn[h].get(nz, g, ac[h], b, kk);
-                    if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(ac[h], b, kk)];
-                    fval = rb_update<T, EXACT>(X0[q], X0[q - 1], X0[q + 1], X0[q - RB_W2], X0[q + RB_W2], Xm[q], Xp[q], s,
-                                               fk[foff[h]], NOISE != NOISE_NONE, xi);
-                }
-                F[s1[h]] = fval;
+            T fval = T(0);
+            if (plane_in && cinA) {
+                T xi = T(0);
+                if (NOISE == NOISE_PHILOX) xi = (T)pick(a1 ? nb_cur[1] : nb_cur[0], kk & 3);
+                if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(aA, b, kk)];
+                fval = rb_update<T, EXACT>(X0[s2A], X0[s2A - 1], X0[s2A + 1], X0[s2A - RB_W2], X0[s2A + RB_W2], Xm[s2A],
+                                           Xp[s2A], s, fk[foA], NOISE != NOISE_NONE, xi);
             }
+            Fp[s1A] = fval;
+            Fp[s1B] = T(0);
         }
         __syncthreads();
-        // [C] second colour of plane c = kk-1, both colours written
+        // [C] plane c = kk-1: column A holds the second colour there
         const int c = kk - 1;
         if (c >= c0 && c < c1) {
-            const T *F0 = Fr + s3(c) * P1, *Fm = Fr + s3(c - 1) * P1, *Fp = Fr + s3(c + 1) * P1;
-            const T *X0 = xo + (c & 3) * P2;
             const T *fc = f + (i64)(c + 1) * g.sz;
             T *out = xout + (i64)(c + 1) * g.sz;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                if (!ctile[h]) continue;
-                const int q = s1[h];
-                T v;
-                if (((ac[h] + b + c) & 1) == first) {
-                    v = F0[q];
-                } else {
-                    T xi = T(0);
-                    if (NOISE == NOISE_PHILOX) xi = (T)cn[h].get(nz, g, ac[h], b, c);
-                    if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(ac[h], b, c)];
-                    v = rb_update<T, EXACT>(X0[s2[h]], F0[q - 1], F0[q + 1], F0[q - RB_W1], F0[q + RB_W1], Fm[q], Fp[q], s,
-                                            fc[foff[h]], NOISE != NOISE_NONE, xi);
+            if (tB) out[foB] = F0[s1B];
+            if (tA) {
+                T xi = T(0);
+                if (NOISE == NOISE_PHILOX) {
+                    const float4 cur = a1 ? nb_cur[1] : nb_cur[0], prv = a1 ? nb_prev[1] : nb_prev[0];
+                    xi = (T)pick((c >> 2) == q_cur ? cur : prv, c & 3);
                 }
-                out[foff[h]] = v;
+                if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(aA, b, c)];
+                out[foA] = rb_update<T, EXACT>(Xm[s2A], F0[s1A - 1], F0[s1A + 1], F0[s1A - RB_W1], F0[s1A + RB_W1], Fm[s1A],
+                                               Fp[s1A], s, fc[foA], NOISE != NOISE_NONE, xi);
             }
         }
-        // [D], [E]
-        commit(kk + 2);
+        // [D] plane kk+2 into the free slot, [E] plane kk+3 into registers
+        commit(Xn);
         fetch(kk + 3);
         __syncthreads();
+        // rotate: old planes (kk, kk+1, kk+2, free), F planes (kk-1, kk, free)
+        T *t = Xm;
+        Xm = X0;
+        X0 = Xp;
+        Xp = Xn;
+        Xn = t;
+        T *u = Fm;
+        Fm = F0;
+        F0 = Fp;
+        Fp = u;
     }
 }
 
@@ -626,77 +648,119 @@ __global__ void __launch_bounds__(256) k_resid_restrict(const T *__restrict__ x,
 // Plane-streaming variant: a CTA owns a tile of RR_TX x RR_TY coarse
 // columns and a range of coarse planes.  Fine residual planes are computed
 // once each on the (2 RR_TX + 1) x (2 RR_TY + 1) fine footprint of the tile
-// and kept in a ring of three planes; every coarse plane then restricts from
-// the ring.  x is staged plane by plane with a one-point halo.
+// and kept in a ring of three planes; every second fine plane completes a
+// coarse plane, which is restricted from the ring.  x (with a one-point
+// halo) and f are loaded into registers one plane ahead of their use, so the
+// global load latency overlaps the work on the current plane.
 constexpr int RR_TX = 16, RR_TY = 8;
 constexpr int RR_FW = 2 * RR_TX + 1, RR_FH = 2 * RR_TY + 1;  // fine residual footprint
 constexpr int RR_XW = RR_FW + 2, RR_XH = RR_FH + 2;          // x with halo
 constexpr int RR_THREADS = 256;
+constexpr int RR_NX = (RR_XW * RR_XH + RR_THREADS - 1) / RR_THREADS;
+constexpr int RR_NF = (RR_FW * RR_FH + RR_THREADS - 1) / RR_THREADS;
 
 template <typename T, int NPT>
 __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tiled(const T *__restrict__ x, const T *__restrict__ f,
                                                                       T *__restrict__ fc, Grid3 gf, Grid3 gc,
                                                                       StencilArg<T> s, int czc) {
-    __shared__ T xs[3][RR_XH][RR_XW];
-    __shared__ T rs[3][RR_FH][RR_FW];
+    __shared__ T xs[4][RR_XH * RR_XW];
+    __shared__ T rs[3][RR_FH * RR_FW];
     const int ca0 = blockIdx.x * RR_TX, cb0 = blockIdx.y * RR_TY;
     const int cc0 = blockIdx.z * czc, cc1 = min(cc0 + czc, gc.N2);
-    // fine 0-based origin of the footprint: centre of coarse (ca0, cb0) is
-    // fine 2 ca0 + 1, its left neighbour 2 ca0
+    // fine 0-based origin of the footprint: the centre of coarse (ca0, cb0)
+    // is fine 2 ca0 + 1, its left neighbour 2 ca0
     const int fa0 = 2 * ca0, fb0 = 2 * cb0;
-    auto slot = [](int p) { return ((p % 3) + 3) % 3; };
-    auto load_x = [&](int p) {
-        T(*dst)[RR_XW] = xs[slot(p)];
-        for (int i = threadIdx.x; i < RR_XH * RR_XW; i += RR_THREADS) {
-            int la = i % RR_XW, lb = i / RR_XW;
-            int ga = fa0 - 1 + la, gb = fb0 - 1 + lb;
-            T v = T(0);
-            if (p >= 0 && p < gf.N2 && ga >= 0 && ga < gf.N0 && gb >= 0 && gb < gf.N1) v = x[gf.pad(ga, gb, p)];
-            dst[lb][la] = v;
-        }
+    const int sy = (int)gf.sy;
+    int xoff[RR_NX], xsi[RR_NX];
+    bool xok[RR_NX];
+#pragma unroll
+    for (int j = 0; j < RR_NX; ++j) {
+        const int i = threadIdx.x + j * RR_THREADS;
+        const int la = i % RR_XW, lb = i / RR_XW;
+        const int ga = fa0 - 1 + la, gb = fb0 - 1 + lb;
+        xok[j] = i < RR_XW * RR_XH && ga >= 0 && ga < gf.N0 && gb >= 0 && gb < gf.N1;
+        xoff[j] = (gb + 1) * sy + (ga + 1);
+        xsi[j] = i < RR_XW * RR_XH ? i : -1;
+    }
+    int foff[RR_NF], fsi[RR_NF], fx[RR_NF];
+    bool fok[RR_NF];
+#pragma unroll
+    for (int j = 0; j < RR_NF; ++j) {
+        const int i = threadIdx.x + j * RR_THREADS;
+        const int la = i % RR_FW, lb = i / RR_FW;
+        const int ga = fa0 + la, gb = fb0 + lb;
+        fok[j] = i < RR_FW * RR_FH && ga < gf.N0 && gb < gf.N1;
+        foff[j] = (gb + 1) * sy + (ga + 1);
+        fsi[j] = i < RR_FW * RR_FH ? i : -1;
+        fx[j] = (lb + 1) * RR_XW + (la + 1);  // centre in the x tile
+    }
+    T xr[RR_NX], fr[RR_NF];
+    auto fetch_x = [&](int p) {
+        const bool pin = p >= 0 && p < gf.N2;
+        const T *base = x + (i64)(p + 1) * gf.sz;
+#pragma unroll
+        for (int j = 0; j < RR_NX; ++j) xr[j] = (pin && xok[j]) ? base[xoff[j]] : T(0);
     };
-    auto resid_plane = [&](int p) {  // fine residual of plane p on the footprint
-        T(*dst)[RR_FW] = rs[slot(p)];
-        for (int i = threadIdx.x; i < RR_FH * RR_FW; i += RR_THREADS) {
-            int la = i % RR_FW, lb = i / RR_FW;
-            int ga = fa0 + la, gb = fb0 + lb;
+    auto fetch_f = [&](int p) {
+        const bool pin = p >= 0 && p < gf.N2;
+        const T *base = f + (i64)(p + 1) * gf.sz;
+#pragma unroll
+        for (int j = 0; j < RR_NF; ++j) fr[j] = (pin && fok[j]) ? base[foff[j]] : T(0);
+    };
+    auto commit_x = [&](T *dst) {
+#pragma unroll
+        for (int j = 0; j < RR_NX; ++j)
+            if (xsi[j] >= 0) dst[xsi[j]] = xr[j];
+    };
+    // coarse plane cc needs fine residual planes 2cc, 2cc+1, 2cc+2
+    const int p_lo = 2 * cc0, p_hi = 2 * (cc1 - 1) + 2;
+    T *Xm = xs[0], *X0 = xs[1], *Xp = xs[2], *Xn = xs[3];
+    T *Rm = rs[0], *R0 = rs[1], *Rp = rs[2];
+    fetch_x(p_lo - 1);
+    commit_x(Xm);
+    fetch_x(p_lo);
+    commit_x(X0);
+    fetch_x(p_lo + 1);
+    commit_x(Xp);
+    fetch_x(p_lo + 2);
+    fetch_f(p_lo);
+    __syncthreads();
+    for (int p = p_lo; p <= p_hi; ++p) {
+        // fine residual of plane p on the footprint (ring slot Rp)
+        const bool pin = p >= 0 && p < gf.N2;
+#pragma unroll
+        for (int j = 0; j < RR_NF; ++j) {
+            if (fsi[j] < 0) continue;
             T r = T(0);
-            if (p >= 0 && p < gf.N2 && ga < gf.N0 && gb < gf.N1) {
-                const int X = la + 1, Y = lb + 1;
+            if (pin && fok[j]) {
+                const int q = fx[j];
                 T res;
                 if (NPT == 7) {
-                    res = s.w[4] * xs[slot(p - 1)][Y][X] + s.w[10] * xs[slot(p)][Y - 1][X] + s.w[12] * xs[slot(p)][Y][X - 1] +
-                          s.w[13] * xs[slot(p)][Y][X] + s.w[14] * xs[slot(p)][Y][X + 1] + s.w[16] * xs[slot(p)][Y + 1][X] +
-                          s.w[22] * xs[slot(p + 1)][Y][X];
+                    res = s.w[4] * Xm[q] + s.w[10] * X0[q - RR_XW] + s.w[12] * X0[q - 1] + s.w[13] * X0[q] +
+                          s.w[14] * X0[q + 1] + s.w[16] * X0[q + RR_XW] + s.w[22] * Xp[q];
                 } else {
                     res = T(0);
+                    const T *Pl[3] = {Xm, X0, Xp};
 #pragma unroll
-                    for (int dz = -1; dz <= 1; ++dz)
+                    for (int dz = 0; dz < 3; ++dz)
 #pragma unroll
                         for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
                             for (int dx = -1; dx <= 1; ++dx)
-                                res += s.w[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)] * xs[slot(p + dz)][Y + dy][X + dx];
+                                res += s.w[dz * 9 + (dy + 1) * 3 + (dx + 1)] * Pl[dz][q + dy * RR_XW + dx];
                 }
-                r = f[gf.pad(ga, gb, p)] - res;
+                r = fr[j] - res;
             }
-            dst[lb][la] = r;
+            Rp[fsi[j]] = r;
         }
-    };
-    // coarse plane cc needs fine residual planes 2cc, 2cc+1, 2cc+2
-    const int p_lo = 2 * cc0, p_hi = 2 * (cc1 - 1) + 2;
-    load_x(p_lo - 1);
-    load_x(p_lo);
-    for (int p = p_lo; p <= p_hi; ++p) {
-        load_x(p + 1);
         __syncthreads();
-        resid_plane(p);
-        __syncthreads();
-        if (p >= p_lo + 2 && ((p - p_lo) & 1) == 0) {  // restrict coarse plane (p - 2) / 2
+        if (p >= p_lo + 2 && ((p - p_lo) & 1) == 0) {  // coarse plane (p - 2) / 2 from Rm, R0, Rp
             const int cc = (p - 2) / 2;
+            T *out = fc + (i64)(cc + 1) * gc.sz;
+            const T *Rl[3] = {Rm, R0, Rp};
             for (int i = threadIdx.x; i < RR_TX * RR_TY; i += RR_THREADS) {
-                int la = i % RR_TX, lb = i / RR_TX;
-                int ca = ca0 + la, cb = cb0 + lb;
+                const int la = i % RR_TX, lb = i / RR_TX;
+                const int ca = ca0 + la, cb = cb0 + lb;
                 if (ca >= gc.N0 || cb >= gc.N1) continue;
                 T acc = T(0);
 #pragma unroll
@@ -705,13 +769,26 @@ __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tiled(const T *__
                     for (int ay = 0; ay < 3; ++ay)
 #pragma unroll
                         for (int ax = 0; ax < 3; ++ax) {
-                            T wr = T((ax == 1 ? 1.0 : 0.5) * (ay == 1 ? 1.0 : 0.5) * (az == 1 ? 1.0 : 0.5));
-                            acc += wr * rs[slot(2 * cc + az)][2 * lb + ay][2 * la + ax];
+                            const T wr = T((ax == 1 ? 1.0 : 0.5) * (ay == 1 ? 1.0 : 0.5) * (az == 1 ? 1.0 : 0.5));
+                            acc += wr * Rl[az][(2 * lb + ay) * RR_FW + 2 * la + ax];
                         }
-                fc[gc.pad(ca, cb, cc)] = acc;
+                out[(cb + 1) * (int)gc.sy + ca + 1] = acc;
             }
         }
+        // x plane p+2 into the free slot, x plane p+3 and f plane p+1 into registers
+        commit_x(Xn);
+        fetch_x(p + 3);
+        fetch_f(p + 1);
         __syncthreads();
+        T *t = Xm;
+        Xm = X0;
+        X0 = Xp;
+        Xp = Xn;
+        Xn = t;
+        T *u = Rm;
+        Rm = R0;
+        R0 = Rp;
+        Rp = u;
     }
 }
 
@@ -907,8 +984,16 @@ __global__ void __launch_bounds__(256) k_chol_gemv_lower(const T *__restrict__ f
     const i64 warps = (i64)gridDim.x * (blockDim.x >> 5);
     for (i64 i = (i64)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
         const double *row = Linv + i * n;
-        double acc = 0.0;
-        for (i64 k = lane; k <= i; k += 32) acc += row[k] * fs[k];
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        i64 k = lane;
+        for (; k + 96 <= i; k += 128) {
+            a0 += row[k] * fs[k];
+            a1 += row[k + 32] * fs[k + 32];
+            a2 += row[k + 64] * fs[k + 64];
+            a3 += row[k + 96] * fs[k + 96];
+        }
+        for (; k <= i; k += 32) a0 += row[k] * fs[k];
+        double acc = (a0 + a1) + (a2 + a3);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0) {
@@ -935,8 +1020,16 @@ __global__ void __launch_bounds__(256) k_chol_gemv_upper(const double *__restric
     const i64 warps = (i64)gridDim.x * (blockDim.x >> 5);
     for (i64 j = (i64)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < n; j += warps) {
         const double *row = LinvT + j * n;
-        double acc = 0.0;
-        for (i64 k = j + lane; k < n; k += 32) acc += row[k] * vs[k];
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        i64 k = j + lane;
+        for (; k + 96 < n; k += 128) {
+            a0 += row[k] * vs[k];
+            a1 += row[k + 32] * vs[k + 32];
+            a2 += row[k + 64] * vs[k + 64];
+            a3 += row[k + 96] * vs[k + 96];
+        }
+        for (; k < n; k += 32) a0 += row[k] * vs[k];
+        double acc = (a0 + a1) + (a2 + a3);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0) {
