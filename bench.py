@@ -146,8 +146,9 @@ def time_chain(M, torch, op, f, obs, precision, steps, warmup, iact_extra, dist,
 
 
 def sweep_roofline(M, torch, s, precision, peak):
-    """Fine-level red-black SOR sweep (both colour kernels, Philox noise,
-    no low-rank update) timed alone on the sampler's stream."""
+    """Fine-level red-black SOR sweep (k_sweep_rb: both colours in one
+    launch, Philox noise, no low-rank update) timed alone on the sampler's
+    stream; algorithmic bytes 3 n s (read x, read f, write x)."""
     n = s.level_size(0)
     sz = 4 if precision == M.FP32_MIXED else 8
     s.sweep_device(0, nrepeat=5, with_lowrank=False)
@@ -159,8 +160,8 @@ def sweep_roofline(M, torch, s, precision, peak):
     s.sweep_device(0, nrepeat=rep, with_lowrank=False)
     e1.record(st)
     s.synchronize()
-    t = e0.elapsed_time(e1) / 1e3 / rep / 2  # seconds per colour launch
-    bytes_per_launch = 3 * n * sz / 2      # read x, read f, write x; half the points per colour
+    t = e0.elapsed_time(e1) / 1e3 / rep    # seconds per sweep launch
+    bytes_per_launch = 3 * n * sz          # read x, read f, write x
     achieved = bytes_per_launch / t / 1e9
     return achieved, bytes_per_launch, t
 
@@ -259,6 +260,61 @@ def covariance_study(nsamples, nprobe=256, warmup=50, seed=1000):
     return res
 
 
+def batch_study(nchain, steps, warmup=5, seed=3):
+    """Batching: nchain independent chains, cubic lattices drawn from
+    {32,48,64,96,128}^3 cells, kappa^2 log-uniform in [1, 100], 0-64
+    measurements (centres U[0.1,0.9]^3, radius 0.05, variance 1e-4, values
+    N(0,1)), FP32 fine levels / FP64 coarse, V(1,1) SSOR, 5 levels, all
+    stepped by one CUDA graph.  Reports aggregate samples/s and the per-chain
+    IACT distribution."""
+    import torch
+    import multigridmc_gb300 as M
+    rng = np.random.default_rng(seed)
+    sizes = rng.choice([32, 48, 64, 96, 128], size=nchain)
+    ksq = np.exp(rng.uniform(np.log(1.0), np.log(100.0), size=nchain))
+    ms = rng.integers(0, 65, size=nchain)
+    chains = []
+    t0 = time.perf_counter()
+    unknowns = 0
+    for i in range(nchain):
+        shape = (int(sizes[i]),) * 3
+        op = M.LinearOperator.shifted_laplace_fd(shape, float(ksq[i]))
+        m = int(ms[i])
+        y = rng.standard_normal(m)
+        if m > 0:
+            op = op.with_measurements(rng.uniform(0.1, 0.9, size=(m, 3)), np.ones(m), VARIANCE, RADIUS)
+        f = np.zeros(op.n)
+        for j in range(op.m):
+            sl = slice(op.B_ptr[j], op.B_ptr[j + 1])
+            f[op.B_idx[sl]] += op.B_val[sl] * (y[j] / op.Sigma[j])
+        s = M.MultigridMCSampler(op, M.MultigridParameters(nlevel=NLEVEL), precision=M.FP32_MIXED, seed=10000 + i)
+        s.fix_rhs(f)
+        bidx, bval = M.measurement_vector(shape, [0.5, 0.5, 0.5], RADIUS)
+        s.set_observable(bidx, bval, warmup + steps + 8)
+        chains.append(s)
+        unknowns += op.n
+    setup = time.perf_counter() - t0
+    batch = M.MultigridMCBatch(chains)
+    batch.step(warmup)
+    batch.synchronize()
+    st = torch.cuda.ExternalStream(batch.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    batch.step(steps)
+    e1.record(st)
+    batch.synchronize()
+    ms_step = e0.elapsed_time(e1) / steps
+    taus = []
+    for s in chains:
+        z = s.read_observations(warmup + steps + 8)[warmup:]
+        if len(z) > 60 and np.std(z) > 0:
+            taus.append(M.statistics.tau_int(z, 20))
+    batch.close()
+    return {"nchain": nchain, "ms_per_batched_step": ms_step, "samples_per_s": nchain * 1000.0 / ms_step,
+            "unknowns_total": int(unknowns), "setup_s": setup, "iact_median": float(np.median(taus)) if taus else None,
+            "iact_p90": float(np.percentile(taus, 90)) if taus else None, "iact_window": 20, "steps": steps}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -271,7 +327,12 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--covariance-study", type=int, default=0, metavar="NSAMPLES",
                     help="run the coupled FP32/FP64 covariance comparison instead of the benchmark")
+    ap.add_argument("--batch-chains", type=int, default=0, metavar="N",
+                    help="run the batched-chains study (N chains of mixed sizes) instead of the benchmark")
     args = ap.parse_args()
+    if args.batch_chains > 0:
+        print(json.dumps({"batch_study": batch_study(args.batch_chains, args.steps)}), flush=True)
+        return
     if args.covariance_study > 0:
         print(json.dumps({"covariance_study": covariance_study(args.covariance_study)}), flush=True)
         return
@@ -376,7 +437,7 @@ def main():
         "gpu_launches": int(launches * args.steps),
         "launches_per_step": int(launches),
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                     "traffic": None, "kernel": "k_sweep_colour<float,7> (fine-level red-black SOR, one colour)",
+                     "traffic": None, "kernel": "k_sweep_rb<float> (fine-level red-black SOR sweep, both colours, Philox noise)",
                      "algorithmic_bytes_per_launch": bpl, "launch_s": tl, "peak_kind": peak_kind},
         "cpu_baseline": cpu,
     }

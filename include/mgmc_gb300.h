@@ -191,6 +191,22 @@ mgmc_status mgmc_level_sor(mgmc_sampler *s, int level, int direction, int with_n
 mgmc_status mgmc_level_sweep_device(mgmc_sampler *s, int level, int direction, int with_noise, int with_lowrank,
                                     int64_t nrepeat);
 
+/* ----------------------------------------------------------------- batch */
+/* Many independent chains (the reference's only parallel mode: independent
+ * chains per OpenMP thread, src/measurements/convergence.cc:29-78) stepped
+ * together: one CUDA graph holds every chain's step as a child graph, so
+ * the chains run concurrently.  Chains keep their own state, right hand
+ * side and observables; they must use MGMC_NOISE_PHILOX and one device.
+ * Inside a batch each chain's coarse-level cooperative sweeps run on a
+ * single CTA.  The samplers must outlive the batch; while it exists, step
+ * them only through mgmc_batch_step. */
+typedef struct mgmc_batch mgmc_batch;
+mgmc_status mgmc_batch_create(int nchain, mgmc_sampler *const *samplers, mgmc_batch **out);
+mgmc_status mgmc_batch_step(mgmc_batch *b, int64_t nsteps);
+mgmc_status mgmc_batch_synchronize(mgmc_batch *b);
+mgmc_status mgmc_batch_stream(mgmc_batch *b, void **cuda_stream);
+mgmc_status mgmc_batch_destroy(mgmc_batch *b);
+
 /* ------------------------------------------- no-allocation operator apply */
 /* No counterpart in the reference.  y = A x for A = A_0 + B Sigma^{-1} B^T
  * (the product LinearOperator::apply computes) without allocating device

@@ -32,7 +32,7 @@ from . import build as _build
 
 __all__ = [
     "MGMCError", "load", "fd_stencil", "galerkin_stencil", "measurement_vector", "LinearOperator",
-    "MultigridParameters", "MultigridMCSampler", "SSORSampler", "CholeskySampler",
+    "MultigridParameters", "MultigridMCSampler", "MultigridMCBatch", "SSORSampler", "CholeskySampler",
     "FP64", "FP32_MIXED", "LEXICOGRAPHIC", "MULTICOLOUR", "PHILOX", "INJECTED", "FORWARD", "BACKWARD",
 ]
 
@@ -107,6 +107,11 @@ SIGNATURES = {
     "mgmc_level_prolongate_add": (C.c_int, [_P, C.c_int, C.c_double, _D, _D]),
     "mgmc_level_sor": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _D, _D]),
     "mgmc_level_sweep_device": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64]),
+    "mgmc_batch_create": (C.c_int, [C.c_int, C.POINTER(_P), C.POINTER(_P)]),
+    "mgmc_batch_step": (C.c_int, [_P, C.c_int64]),
+    "mgmc_batch_synchronize": (C.c_int, [_P]),
+    "mgmc_batch_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "mgmc_batch_destroy": (C.c_int, [_P]),
     "mgmc_measured_apply_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _D, C.c_int, _P, _P, _P, _P,
                                               _P, _P, _P]),
 }
@@ -454,6 +459,40 @@ class MultigridMCSampler:
         assert x.dtype == np.float64 and x.flags.c_contiguous
         _check(self._L.mgmc_level_sor(self._h, level, direction, int(with_noise), _dp(f), _dp(x)))
         return x
+
+
+class MultigridMCBatch:
+    """Independent chains stepped together in one CUDA graph (mgmc_batch_*)."""
+
+    def __init__(self, samplers):
+        self.samplers = list(samplers)  # keep alive
+        self._L = load()
+        arr = (C.c_void_p * len(self.samplers))(*[s._h.value for s in self.samplers])
+        self._h = C.c_void_p()
+        _check(self._L.mgmc_batch_create(len(self.samplers), arr, C.byref(self._h)))
+
+    def step(self, nsteps=1):
+        _check(self._L.mgmc_batch_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        _check(self._L.mgmc_batch_synchronize(self._h))
+
+    @property
+    def stream(self):
+        s = C.c_void_p()
+        _check(self._L.mgmc_batch_stream(self._h, C.byref(s)))
+        return s.value
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.mgmc_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def SSORSampler(linear_operator, omega=1.0, nsmooth=1, **kw):

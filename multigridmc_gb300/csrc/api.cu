@@ -124,6 +124,7 @@ struct Sampler {
     bool counting = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    bool batched = false;  // member of an mgmc_batch: single-CTA cooperative sweeps
     std::vector<void *> owned;  // every device allocation
 
     template <typename P_>
@@ -220,9 +221,9 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *&x, T *
     }
     // 2^dim colours: all colours in one cooperative launch
     {
-        const int G0 = (lv.g.N0 + 7) / 8;
-        const i64 items = (i64)((lv.g.N1 + 1) / 2) * ((lv.g.N2 + 1) / 2) * G0;
-        const unsigned grid = (unsigned)std::max<i64>(1, std::min<i64>((items + 255) / 256, lv.coop_blocks));
+        const i64 items = (i64)((lv.g.N0 + 1) / 2) * ((lv.g.N1 + 1) / 2) * ((lv.g.N2 + 1) / 2);
+        const unsigned grid =
+            (unsigned)std::max<i64>(1, std::min<i64>((items + 255) / 256, S.batched ? 1 : lv.coop_blocks));
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(grid);
         cfg.blockDim = dim3(256);
@@ -780,7 +781,7 @@ void Sampler::build(const mgmc_operator_desc &op) {
                 CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_coop<float, false, NOISE_PHILOX>, 256, 0));
             else
                 CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_coop<double, false, NOISE_PHILOX>, 256, 0));
-            lv.coop_blocks = std::max(1, nsm * std::min(per_sm, 2));
+            lv.coop_blocks = std::max(1, nsm * std::min(per_sm, 4));
         }
         if (lv.fused) {
             lv.x_alt = talloc(lv.geo.nalloc);
@@ -1354,6 +1355,100 @@ mgmc_status mgmc_level_sweep_device(mgmc_sampler *s, int level, int direction, i
         std::swap(lv.x, lv.x_alt);
     }
     S.check_launch();
+    API_END
+}
+
+// ------------------------------------------------------------------- batch
+struct mgmc_batch {
+    std::vector<Sampler *> chains;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int device = 0;
+};
+
+mgmc_status mgmc_batch_create(int nchain, mgmc_sampler *const *samplers, mgmc_batch **out) {
+    mgmc_batch *B = nullptr;
+    API_BEGIN
+    if (nchain < 1 || !samplers || !out) fail(MGMC_ERR_INVALID_ARGUMENT, "need at least one sampler");
+    *out = nullptr;
+    B = new mgmc_batch();
+    for (int i = 0; i < nchain; ++i) {
+        Sampler &S = impl(samplers[i]);
+        if (S.noise_mode != NOISE_PHILOX) fail(MGMC_ERR_UNSUPPORTED, "batched chains draw Philox noise");
+        if (i == 0) B->device = S.P.device;
+        if (S.P.device != B->device) fail(MGMC_ERR_INVALID_ARGUMENT, "batched chains must share one device");
+        if (std::find(B->chains.begin(), B->chains.end(), &S) != B->chains.end())
+            fail(MGMC_ERR_INVALID_ARGUMENT, "a sampler appears twice in the batch");
+        B->chains.push_back(&S);
+    }
+    CK(cudaSetDevice(B->device));
+    CK(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+    CK(cudaGraphCreate(&B->graph, 0));
+    for (Sampler *S : B->chains) {
+        CK(cudaStreamSynchronize(S->stream));
+        // every chain's cooperative sweeps use one CTA, so that concurrent
+        // branches never wait on CTAs that cannot become resident
+        if (!S->batched && S->gexec) {
+            cudaGraphExecDestroy(S->gexec);
+            cudaGraphDestroy(S->graph);
+            S->gexec = nullptr;
+            S->graph = nullptr;
+        }
+        S->batched = true;
+        ensure_graph(*S);
+        cudaGraphNode_t node;
+        CK(cudaGraphAddChildGraphNode(&node, B->graph, nullptr, 0, S->graph));
+    }
+    CK(cudaGraphInstantiate(&B->gexec, B->graph, 0));
+    *out = B;
+    B = nullptr;
+    }
+    catch (const Error &e) {
+        if (B) {
+            if (B->gexec) cudaGraphExecDestroy(B->gexec);
+            if (B->graph) cudaGraphDestroy(B->graph);
+            if (B->stream) cudaStreamDestroy(B->stream);
+            delete B;
+        }
+        g_err = e.msg;
+        return e.st;
+    }
+    return MGMC_OK;
+}
+
+mgmc_status mgmc_batch_step(mgmc_batch *b, int64_t nsteps) {
+    API_BEGIN
+    if (!b || nsteps < 0) fail(MGMC_ERR_INVALID_ARGUMENT, "bad arguments");
+    CK(cudaSetDevice(b->device));
+    for (int64_t k = 0; k < nsteps; ++k) CK(cudaGraphLaunch(b->gexec, b->stream));
+    API_END
+}
+
+mgmc_status mgmc_batch_synchronize(mgmc_batch *b) {
+    API_BEGIN
+    if (!b) fail(MGMC_ERR_INVALID_ARGUMENT, "null batch");
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamSynchronize(b->stream));
+    API_END
+}
+
+mgmc_status mgmc_batch_stream(mgmc_batch *b, void **cuda_stream) {
+    API_BEGIN
+    if (!b || !cuda_stream) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    *cuda_stream = (void *)b->stream;
+    API_END
+}
+
+mgmc_status mgmc_batch_destroy(mgmc_batch *b) {
+    API_BEGIN
+    if (!b) return MGMC_OK;
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->stream);
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
     API_END
 }
 

@@ -305,6 +305,15 @@ __global__ void __launch_bounds__(RB_THREADS, 3) k_sweep_rb(const T *__restrict_
 #pragma unroll
         for (int j = 0; j < RB_NLD; ++j) pre[j] = (pin && gok[j]) ? base[goff[j]] : T(0);
     };
+    // f of the column that is first colour on plane c, at planes c and c-1
+    // (the values steps [A] and [C] of plane c need), loaded one plane early
+    auto fetch_f = [&](int c, T &fa, T &fc) {
+        const bool b1 = ((c & 1) ? 1 - fc0 : fc0) == 1;
+        const bool in = b1 ? cin[1] : cin[0];
+        const int fo = b1 ? foff[1] : foff[0];
+        fa = (in && c >= 0 && c < g.N2) ? f[(i64)(c + 1) * g.sz + fo] : T(0);
+        fc = (in && c - 1 >= 0 && c - 1 < g.N2) ? f[(i64)c * g.sz + fo] : T(0);
+    };
     auto commit = [&](T *dst) {
 #pragma unroll
         for (int j = 0; j < RB_NLD; ++j)
@@ -324,6 +333,8 @@ __global__ void __launch_bounds__(RB_THREADS, 3) k_sweep_rb(const T *__restrict_
     // with the loop starting at kk = c0-1 the slots must read kk-1 = c0-2,
     // kk = c0-1, kk+1 = c0
     __syncthreads();
+    T fA_next, fC_next;
+    fetch_f(c0 - 1, fA_next, fC_next);
     float4 nb_cur[2], nb_prev[2];
     int q_cur = -1000;
     nb_cur[0] = nb_cur[1] = nb_prev[0] = nb_prev[1] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -344,17 +355,18 @@ __global__ void __launch_bounds__(RB_THREADS, 3) k_sweep_rb(const T *__restrict_
         const int foA = a1 ? foff[1] : foff[0], foB = a1 ? foff[0] : foff[1];
         const bool cinA = a1 ? cin[1] : cin[0];
         const bool tA = a1 ? ctile[1] : ctile[0], tB = a1 ? ctile[0] : ctile[1];
+        const T fA = fA_next, fC = fC_next;
+        fetch_f(kk + 1, fA_next, fC_next);
         // [A] first colour of plane kk
         {
             const bool plane_in = kk >= 0 && kk < g.N2;
-            const T *fk = f + (i64)(kk + 1) * g.sz;
             T fval = T(0);
             if (plane_in && cinA) {
                 T xi = T(0);
                 if (NOISE == NOISE_PHILOX) xi = (T)pick(a1 ? nb_cur[1] : nb_cur[0], kk & 3);
                 if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(aA, b, kk)];
                 fval = rb_update<T, EXACT>(X0[s2A], X0[s2A - 1], X0[s2A + 1], X0[s2A - RB_W2], X0[s2A + RB_W2], Xm[s2A],
-                                           Xp[s2A], s, fk[foA], NOISE != NOISE_NONE, xi);
+                                           Xp[s2A], s, fA, NOISE != NOISE_NONE, xi);
             }
             Fp[s1A] = fval;
             Fp[s1B] = T(0);
@@ -363,7 +375,6 @@ __global__ void __launch_bounds__(RB_THREADS, 3) k_sweep_rb(const T *__restrict_
         // [C] plane c = kk-1: column A holds the second colour there
         const int c = kk - 1;
         if (c >= c0 && c < c1) {
-            const T *fc = f + (i64)(c + 1) * g.sz;
             T *out = xout + (i64)(c + 1) * g.sz;
             if (tB) out[foB] = F0[s1B];
             if (tA) {
@@ -374,7 +385,7 @@ __global__ void __launch_bounds__(RB_THREADS, 3) k_sweep_rb(const T *__restrict_
                 }
                 if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(aA, b, c)];
                 out[foA] = rb_update<T, EXACT>(Xm[s2A], F0[s1A - 1], F0[s1A + 1], F0[s1A - RB_W1], F0[s1A + RB_W1], Fm[s1A],
-                                               Fp[s1A], s, fc[foA], NOISE != NOISE_NONE, xi);
+                                               Fp[s1A], s, fC, NOISE != NOISE_NONE, xi);
             }
         }
         // [D] plane kk+2 into the free slot, [E] plane kk+3 into registers
@@ -405,25 +416,27 @@ constexpr long long GRID_BARRIER_SPINS = 1ll << 24;
 __device__ __forceinline__ void grid_barrier(unsigned *bar, unsigned *err) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned *vgen = bar + 1;
-        const unsigned gen = *vgen;
-        __threadfence();
+        unsigned gen;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(gen) : "l"(bar + 1) : "memory");
         const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
-        if (atomicAdd(bar, 1u) == nb - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
+        unsigned arrived;
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(arrived) : "l"(bar) : "memory");
+        if (arrived == nb - 1) {
+            asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(bar) : "memory");
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar + 1) : "memory");
         } else {
             long long it = 0;
-            while (*vgen == gen) {
+            unsigned now;
+            do {
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(now) : "l"(bar + 1) : "memory");
+                if (now != gen) break;
                 if (++it > GRID_BARRIER_SPINS) {
                     atomicOr(err, 2u);
                     break;
                 }
-                __nanosleep(64);
-            }
+                if (it > 64) __nanosleep(32);
+            } while (true);
         }
-        __threadfence();
     }
     __syncthreads();
 }
@@ -438,27 +451,21 @@ template <typename T, bool EXACT, int NOISE>
 __global__ void __launch_bounds__(256) k_sweep_coop(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
                                                      StencilArg<T> s, int ncol, int forward, NoiseArgs nz,
                                                      unsigned *bar, unsigned *err) {
-    const int G0 = (g.N0 + 7) >> 3;
     const int nthreads = gridDim.x * blockDim.x;
     for (int cc = 0; cc < ncol; ++cc) {
         const int col = forward ? cc : ncol - 1 - cc;
         const int pa = col & 1, pb = (col >> 1) & 1, pc = (col >> 2) & 1;
-        const int nb = (g.N1 - pb + 1) >> 1, nc = (g.N2 - pc + 1) >> 1;
-        const int items = nb * nc * G0;
+        const int na = (g.N0 - pa + 1) >> 1, nb = (g.N1 - pb + 1) >> 1, nc = (g.N2 - pc + 1) >> 1;
+        const int items = na * nb * nc;
         for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < items; t += nthreads) {
-            const int grp = t % G0, row = t / G0;
-            const int b = 2 * (row % nb) + pb, c = 2 * (row / nb) + pc;
-            float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (NOISE == NOISE_PHILOX) nrm = point_normals(nz, g, 8 * grp + pa, b, c);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int a = 8 * grp + pa + 2 * q;
-                if (a >= g.N0) break;
-                T xi = T(0);
-                if (NOISE == NOISE_PHILOX) xi = (T)pick(nrm, q);
-                if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
-                sor_point<T, 27, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
-            }
+            const int ia = t % na, r = t / na;
+            const int a = 2 * ia + pa, b = 2 * (r % nb) + pb, c = 2 * (r / nb) + pc;
+            T xi = T(0);
+            // the normal of the point is lane (a & 7) >> 1 of its group's block,
+            // the same value the group-per-thread mapping draws
+            if (NOISE == NOISE_PHILOX) xi = (T)pick(point_normals(nz, g, a, b, c), (a & 7) >> 1);
+            if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
+            sor_point<T, 27, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
         }
         if (cc + 1 < ncol) grid_barrier(bar, err);
     }
@@ -536,9 +543,11 @@ __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRank
     const i64 e0 = lr.Bptr[j], e1 = lr.Bptr[j + 1];
     const i64 len = (e1 - e0 + P - 1) / P;
     const i64 lo = e0 + p * len, hi = min(e1, lo + len);
-    double acc = 0.0;
-    for (i64 e = lo + threadIdx.x; e < hi; e += blockDim.x) acc += lr.Bval[e] * (double)x[lr.Bidx[e]];
-    acc = block_sum<256>(acc, sh);
+    // per-thread sums in the state's precision (FP32 products for the FP32
+    // chain), combined across the block and the partial sums in FP64
+    T tacc = T(0);
+    for (i64 e = lo + threadIdx.x; e < hi; e += blockDim.x) tacc += (T)lr.Bval[e] * x[lr.Bidx[e]];
+    double acc = block_sum<256>((double)tacc, sh);
     if (threadIdx.x == 0) lr.part[j * P + p] = acc;
     __threadfence();
     if (threadIdx.x == 0) {
