@@ -85,6 +85,7 @@ struct Level {
     RowCsr C[2];        // C = M^{-1} B, forward / backward (T values)
     double *Sinv[2] = {nullptr, nullptr}, *G[2] = {nullptr, nullptr};
     double *y = nullptr, *z = nullptr, *part = nullptr;
+    float *zf = nullptr, *Bvalf = nullptr;
     unsigned *counter = nullptr;
     int bt_split = 1;  // blocks per column of the B^T x reduction
     unsigned *bar = nullptr;  // grid barrier of the cooperative sweep
@@ -302,6 +303,8 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     lr.Bptr = lv.Bptr;
     lr.Bidx = lv.Bidx;
     lr.Bval = lv.Bval;
+    lr.Bvalf = lv.Bvalf;
+    lr.zf = lv.zf;
     lr.Sinv = lv.Sinv[dir];
     lr.G = lv.G[dir];
     lr.sinv_sqrt = S.d_sinv_sqrt;
@@ -318,8 +321,13 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     else
         k_bt_x_z<T, NOISE_INJECTED, true><<<grid, 256, smem, S.stream>>>(x, lr, nz);
     const RowCsr &C = lv.C[dir];
-    if (C.nrows > 0)
-        k_lr_scatter<T><<<nblk(C.nrows, 256), 256, 0, S.stream>>>(x, C.nrows, C.rows, C.ptr, C.col, (const T *)C.val, lv.z);
+    if (C.nrows > 0) {
+        if (sizeof(T) == 4)
+            k_lr_scatter_f<T><<<nblk(C.nrows, 256), 256, 0, S.stream>>>(x, C.nrows, C.rows, C.ptr, C.col, (const T *)C.val,
+                                                                         lv.zf);
+        else
+            k_lr_scatter<T><<<nblk(C.nrows, 256), 256, 0, S.stream>>>(x, C.nrows, C.rows, C.ptr, C.col, (const T *)C.val, lv.z);
+    }
     S.launches += 2;
 }
 
@@ -376,6 +384,7 @@ static void launch_bt_plain(Sampler &S, Level &lv, const void *x) {
     lr.Bptr = lv.Bptr;
     lr.Bidx = lv.Bidx;
     lr.Bval = lv.Bval;
+    lr.Bvalf = lv.Bvalf;
     lr.y = lv.y;
     lr.part = lv.part;
     lr.counter = lv.counter;
@@ -566,6 +575,8 @@ void Sampler::build_lowrank(int lev) {
         lv.Bptr = upload(bptr);
         lv.Bidx = upload(bidx);
         lv.Bval = upload(lv.Bh.val);
+        std::vector<float> bvf(lv.Bh.val.begin(), lv.Bh.val.end());
+        lv.Bvalf = upload(bvf);
         std::vector<std::tuple<i64, int, double>> trip;
         for (int j = 0; j < m; ++j)
             for (i64 e = lv.Bh.ptr[j]; e < lv.Bh.ptr[j + 1]; ++e) trip.emplace_back(lv.Bh.row[e], j, lv.Bh.val[e]);
@@ -590,6 +601,7 @@ void Sampler::build_lowrank(int lev) {
     }
     lv.y = alloc<double>(m);
     lv.z = alloc<double>(m);
+    lv.zf = alloc<float>(m);
     {
         i64 maxcol = 1;
         for (int j = 0; j < m; ++j) maxcol = std::max<i64>(maxcol, lv.Bh.ptr[j + 1] - lv.Bh.ptr[j]);
@@ -625,6 +637,7 @@ void Sampler::build_lowrank(int lev) {
             lr.Bptr = lv.Bptr;
             lr.Bidx = lv.Bidx;
             lr.Bval = lv.Bval;
+            lr.Bvalf = lv.Bvalf;
             lr.y = lv.y;
             lr.part = lv.part;
             lr.counter = lv.counter;

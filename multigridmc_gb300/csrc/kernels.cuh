@@ -314,24 +314,22 @@ __global__ void __launch_bounds__(RB_THREADS, 3) k_sweep_rb(const T *__restrict_
         fa = (in && c >= 0 && c < g.N2) ? f[(i64)(c + 1) * g.sz + fo] : T(0);
         fc = (in && c - 1 >= 0 && c - 1 < g.N2) ? f[(i64)c * g.sz + fo] : T(0);
     };
-    auto commit = [&](T *dst) {
+    auto commit = [&](int base) {
 #pragma unroll
         for (int j = 0; j < RB_NLD; ++j)
-            if (soff[j] >= 0) dst[soff[j]] = pre[j];
+            if (soff[j] >= 0) xo[base + soff[j]] = pre[j];
     };
-    // ring slots: old planes kk-1, kk, kk+1 (and kk+2 being stored), F planes
-    // kk-2, kk-1, kk; rotated by one every plane
-    T *Xm = xo, *X0 = xo + P2, *Xp = xo + 2 * P2, *Xn = xo + 3 * P2;
-    T *Fm = Fr, *F0 = Fr + P1, *Fp = Fr + 2 * P1;
+    // ring slots as offsets into shared memory: old planes kk-1, kk, kk+1
+    // (and kk+2 being stored), F planes kk-2, kk-1, kk; rotated every plane
+    int om = 0, o0 = P2, op = 2 * P2, on = 3 * P2;
+    int fm = 0, f0 = P1, fp = 2 * P1;
     fetch(c0 - 2);
-    commit(Xm);  // plane c0-2 goes to the slot that is plane kk-1 at kk = c0-1
+    commit(om);
     fetch(c0 - 1);
-    commit(X0);
+    commit(o0);
     fetch(c0);
-    commit(Xp);
+    commit(op);
     fetch(c0 + 1);
-    // with the loop starting at kk = c0-1 the slots must read kk-1 = c0-2,
-    // kk = c0-1, kk+1 = c0
     __syncthreads();
     T fA_next, fC_next;
     fetch_f(c0 - 1, fA_next, fC_next);
@@ -359,24 +357,24 @@ __global__ void __launch_bounds__(RB_THREADS, 3) k_sweep_rb(const T *__restrict_
         fetch_f(kk + 1, fA_next, fC_next);
         // [A] first colour of plane kk
         {
-            const bool plane_in = kk >= 0 && kk < g.N2;
             T fval = T(0);
-            if (plane_in && cinA) {
+            if (kk >= 0 && kk < g.N2 && cinA) {
                 T xi = T(0);
                 if (NOISE == NOISE_PHILOX) xi = (T)pick(a1 ? nb_cur[1] : nb_cur[0], kk & 3);
                 if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(aA, b, kk)];
-                fval = rb_update<T, EXACT>(X0[s2A], X0[s2A - 1], X0[s2A + 1], X0[s2A - RB_W2], X0[s2A + RB_W2], Xm[s2A],
-                                           Xp[s2A], s, fA, NOISE != NOISE_NONE, xi);
+                const int q = o0 + s2A;
+                fval = rb_update<T, EXACT>(xo[q], xo[q - 1], xo[q + 1], xo[q - RB_W2], xo[q + RB_W2], xo[om + s2A],
+                                           xo[op + s2A], s, fA, NOISE != NOISE_NONE, xi);
             }
-            Fp[s1A] = fval;
-            Fp[s1B] = T(0);
+            Fr[fp + s1A] = fval;
+            Fr[fp + s1B] = T(0);
         }
         __syncthreads();
         // [C] plane c = kk-1: column A holds the second colour there
         const int c = kk - 1;
         if (c >= c0 && c < c1) {
             T *out = xout + (i64)(c + 1) * g.sz;
-            if (tB) out[foB] = F0[s1B];
+            if (tB) out[foB] = Fr[f0 + s1B];
             if (tA) {
                 T xi = T(0);
                 if (NOISE == NOISE_PHILOX) {
@@ -384,24 +382,25 @@ __global__ void __launch_bounds__(RB_THREADS, 3) k_sweep_rb(const T *__restrict_
                     xi = (T)pick((c >> 2) == q_cur ? cur : prv, c & 3);
                 }
                 if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(aA, b, c)];
-                out[foA] = rb_update<T, EXACT>(Xm[s2A], F0[s1A - 1], F0[s1A + 1], F0[s1A - RB_W1], F0[s1A + RB_W1], Fm[s1A],
-                                               Fp[s1A], s, fC, NOISE != NOISE_NONE, xi);
+                const int q = f0 + s1A;
+                out[foA] = rb_update<T, EXACT>(xo[om + s2A], Fr[q - 1], Fr[q + 1], Fr[q - RB_W1], Fr[q + RB_W1],
+                                               Fr[fm + s1A], Fr[fp + s1A], s, fC, NOISE != NOISE_NONE, xi);
             }
         }
         // [D] plane kk+2 into the free slot, [E] plane kk+3 into registers
-        commit(Xn);
+        commit(on);
         fetch(kk + 3);
         __syncthreads();
         // rotate: old planes (kk, kk+1, kk+2, free), F planes (kk-1, kk, free)
-        T *t = Xm;
-        Xm = X0;
-        X0 = Xp;
-        Xp = Xn;
-        Xn = t;
-        T *u = Fm;
-        Fm = F0;
-        F0 = Fp;
-        Fp = u;
+        const int t = om;
+        om = o0;
+        o0 = op;
+        op = on;
+        on = t;
+        const int u = fm;
+        fm = f0;
+        f0 = fp;
+        fp = u;
     }
 }
 
@@ -524,6 +523,8 @@ struct LowRankArg {
     const double *sinv_sqrt; // Sigma^{-1/2}
     double *y;          // m scratch: B^T x
     double *z;          // m scratch: coefficients of C
+    float *zf;          // the same coefficients rounded to FP32 (FP32 chain)
+    const float *Bvalf; // B values rounded to FP32 (FP32 chain)
     double *part;       // m x gridDim.y scratch: partial sums of B^T x
     unsigned *counter;  // block-completion counter (self-resetting)
 };
@@ -546,7 +547,11 @@ __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRank
     // per-thread sums in the state's precision (FP32 products for the FP32
     // chain), combined across the block and the partial sums in FP64
     T tacc = T(0);
-    for (i64 e = lo + threadIdx.x; e < hi; e += blockDim.x) tacc += (T)lr.Bval[e] * x[lr.Bidx[e]];
+    if (sizeof(T) == 4) {
+        for (i64 e = lo + threadIdx.x; e < hi; e += blockDim.x) tacc += (T)lr.Bvalf[e] * x[lr.Bidx[e]];
+    } else {
+        for (i64 e = lo + threadIdx.x; e < hi; e += blockDim.x) tacc += (T)lr.Bval[e] * x[lr.Bidx[e]];
+    }
     double acc = block_sum<256>((double)tacc, sh);
     if (threadIdx.x == 0) lr.part[j * P + p] = acc;
     __threadfence();
@@ -578,27 +583,41 @@ __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRank
         w[k] = lr.sinv_sqrt[k] * xi;
     }
     __syncthreads();
-    // m x m products, four threads per row (partial dot products combined
-    // with shuffles inside aligned groups of four lanes)
-    const int sub = threadIdx.x & 3;
-    for (int k0 = 0; k0 < m; k0 += blockDim.x / 4) {
-        const int k = k0 + (threadIdx.x >> 2);
+    // m x m products, one warp per row (coalesced row loads, shuffle sums)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int k = warp; k < m; k += nwarp) {
+        const double *row = lr.G + (i64)k * m;
         double t = 0.0;
-        if (k < m)
-            for (int q = sub; q < m; q += 4) t += lr.G[(i64)k * m + q] * w[q];
-        t += __shfl_xor_sync(0xffffffffu, t, 1);
-        t += __shfl_xor_sync(0xffffffffu, t, 2);
-        if (k < m && sub == 0) v[k] = lr.y[k] + t;
+        for (int q = lane; q < m; q += 32) t += row[q] * w[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) v[k] = lr.y[k] + t;
     }
     __syncthreads();
-    for (int k0 = 0; k0 < m; k0 += blockDim.x / 4) {
-        const int k = k0 + (threadIdx.x >> 2);
+    for (int k = warp; k < m; k += nwarp) {
+        const double *row = lr.Sinv + (i64)k * m;
         double t = 0.0;
-        if (k < m)
-            for (int q = sub; q < m; q += 4) t += lr.Sinv[(i64)k * m + q] * v[q];
-        t += __shfl_xor_sync(0xffffffffu, t, 1);
-        t += __shfl_xor_sync(0xffffffffu, t, 2);
-        if (k < m && sub == 0) lr.z[k] = w[k] - t;
+        for (int q = lane; q < m; q += 32) t += row[q] * v[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) {
+            const double zk = w[k] - t;
+            lr.z[k] = zk;
+            if (lr.zf) lr.zf[k] = (float)zk;
+        }
+    }
+}
+
+// x[row] += sum_e C_e z_{col_e} over the support rows of C = M^{-1} B
+// (FP32 chain: FP32 coefficients, no FP64 conversion in the loop).
+template <typename T>
+__global__ void __launch_bounds__(256) k_lr_scatter_f(T *__restrict__ x, i64 nrows, const i64 *__restrict__ rows,
+                                                       const i64 *__restrict__ ptr, const int *__restrict__ col,
+                                                       const T *__restrict__ val, const float *__restrict__ z) {
+    for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += (i64)gridDim.x * blockDim.x) {
+        T acc = T(0);
+        for (i64 e = ptr[r]; e < ptr[r + 1]; ++e) acc += val[e] * (T)z[col[e]];
+        x[rows[r]] += acc;
     }
 }
 
