@@ -73,11 +73,7 @@ struct Level {
     int ncol = 2, npt = 7;
     double diag = 0, sd = 0;
     void *x = nullptr, *f = nullptr;    // state and right hand side (T, padded)
-    void *x_home = nullptr;             // buffer holding the state between steps
-    void *x_alt = nullptr;              // second state buffer of the fused red-black sweep
-    bool fused = false;                 // fine-level red-black sweeps run as one pass
-    int rb_cz = 32;                     // z-planes per CTA of the fused sweep
-    void *s1 = nullptr, *s2 = nullptr, *s3 = nullptr;  // scratch for the building-block calls
+    void *s1 = nullptr, *s2 = nullptr;  // scratch for the building-block calls
     SparseCols Bh;                      // B on this level (compact indices)
     i64 *Bptr = nullptr, *Bidx = nullptr;
     double *Bval = nullptr;
@@ -90,6 +86,7 @@ struct Level {
     int bt_split = 1;  // blocks per column of the B^T x reduction
     unsigned *bar = nullptr;  // grid barrier of the cooperative sweep
     int coop_blocks = 1;      // co-resident CTAs of the cooperative sweep
+    bool colour_passes = false;  // 27-point sweeps as one launch per colour
 };
 
 struct Sampler {
@@ -157,7 +154,7 @@ struct Sampler {
     void build_lowrank(int lev);
     void build_coarse();
     void launch_step();
-    void sor(int lev, bool forward, bool noisy, void *&x, void *&alt, void *f);
+    void sor(int lev, bool forward, bool noisy, void *x, void *f);
     void sample(int lev);
     void coarse_sample(int lev);
     void resid_restrict(int lev);
@@ -200,7 +197,7 @@ NoiseArgs Sampler::noise_args(int lev, i64 count) {
 
 // ----------------------------------------------------------- sweep launch
 template <typename T, int NPT, bool EXACT, int NOISE>
-static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *&x, T *&alt, const T *f, const NoiseArgs &nz) {
+static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, const T *f, const NoiseArgs &nz) {
     StencilArg<T> s = stencil_arg<T>(lv, S.P.omega);
     if (S.P.ordering == MGMC_ORDER_LEXICOGRAPHIC) {
         int hb = lv.ncol == 2 ? 1 : 2, hc = lv.ncol == 2 ? 1 : 4;
@@ -209,15 +206,26 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *&x, T *
         return;
     }
     if (NPT == 7) {
-        if (!lv.fused || alt == nullptr) fail(MGMC_ERR_UNSUPPORTED, "red-black sweep needs a second state buffer");
-        // one pass over both colours, x -> alt, then the buffers swap
-        dim3 grid((lv.g.N0 + RB_TX - 1) / RB_TX, (lv.g.N1 + RB_TY - 1) / RB_TY, (lv.g.N2 + lv.rb_cz - 1) / lv.rb_cz);
-        k_sweep_rb<T, EXACT, NOISE><<<grid, RB_THREADS, rb_smem_bytes<T>(), S.stream>>>(x, alt, f, lv.g, s, forward ? 0 : 1,
-                                                                                      lv.rb_cz, nz);
-        S.launches++;
-        T *t = x;
-        x = alt;
-        alt = t;
+        // red-black: two passes, the second walking the planes downwards
+        dim3 grid((lv.g.N0 + 2 * RBP_THREADS - 1) / (2 * RBP_THREADS), lv.g.N1, lv.g.N2);
+        for (int pass = 0; pass < 2; ++pass) {
+            const int colour = forward ? pass : 1 - pass;
+            k_sweep_rb_pass<T, EXACT, NOISE><<<grid, RBP_THREADS, 0, S.stream>>>(x, f, lv.g, s, colour, pass, nz);
+            S.launches++;
+        }
+        return;
+    }
+    if (lv.colour_passes) {
+        // 2^dim colours, one launch per colour
+        for (int cc = 0; cc < lv.ncol; ++cc) {
+            const int colour = forward ? cc : lv.ncol - 1 - cc;
+            const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
+            const int na = (lv.g.N0 - pa + 1) / 2, nb = (lv.g.N1 - pb + 1) / 2, nc = (lv.g.N2 - pc + 1) / 2;
+            if (na <= 0 || nb <= 0 || nc <= 0) continue;
+            dim3 grid((na + RBP_THREADS - 1) / RBP_THREADS, nb, nc);
+            k_sweep_c27_pass<T, EXACT, NOISE><<<grid, RBP_THREADS, 0, S.stream>>>(x, f, lv.g, s, colour, nz);
+            S.launches++;
+        }
         return;
     }
     // 2^dim colours: all colours in one cooperative launch
@@ -242,58 +250,33 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *&x, T *
 }
 
 template <typename T, bool EXACT, int NOISE>
-static void launch_sweep_npt(Sampler &S, const Level &lv, bool forward, T *&x, T *&alt, const T *f, const NoiseArgs &nz) {
+static void launch_sweep_npt(Sampler &S, const Level &lv, bool forward, T *x, const T *f, const NoiseArgs &nz) {
     if (lv.npt == 7)
-        launch_sweep_t<T, 7, EXACT, NOISE>(S, lv, forward, x, alt, f, nz);
+        launch_sweep_t<T, 7, EXACT, NOISE>(S, lv, forward, x, f, nz);
     else
-        launch_sweep_t<T, 27, EXACT, NOISE>(S, lv, forward, x, alt, f, nz);
+        launch_sweep_t<T, 27, EXACT, NOISE>(S, lv, forward, x, f, nz);
 }
 
 template <typename T, bool EXACT>
-static void launch_sweep_noise(Sampler &S, const Level &lv, bool forward, int noise, T *&x, T *&alt, const T *f,
+static void launch_sweep_noise(Sampler &S, const Level &lv, bool forward, int noise, T *x, const T *f,
                                const NoiseArgs &nz) {
     if (noise == NOISE_NONE)
-        launch_sweep_npt<T, EXACT, NOISE_NONE>(S, lv, forward, x, alt, f, nz);
+        launch_sweep_npt<T, EXACT, NOISE_NONE>(S, lv, forward, x, f, nz);
     else if (noise == NOISE_PHILOX)
-        launch_sweep_npt<T, EXACT, NOISE_PHILOX>(S, lv, forward, x, alt, f, nz);
+        launch_sweep_npt<T, EXACT, NOISE_PHILOX>(S, lv, forward, x, f, nz);
     else
-        launch_sweep_npt<T, EXACT, NOISE_INJECTED>(S, lv, forward, x, alt, f, nz);
+        launch_sweep_npt<T, EXACT, NOISE_INJECTED>(S, lv, forward, x, f, nz);
 }
 
-// One sweep of x with right hand side f.  On the fused red-black path the
-// result lands in `alt` and the two pointers are swapped.
-template <typename T, bool EXACT>
-static void rb_attr_t() {
-    const int b = (int)rb_smem_bytes<T>();
-    CK(cudaFuncSetAttribute(k_sweep_rb<T, EXACT, NOISE_NONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
-    CK(cudaFuncSetAttribute(k_sweep_rb<T, EXACT, NOISE_PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
-    CK(cudaFuncSetAttribute(k_sweep_rb<T, EXACT, NOISE_INJECTED>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
-}
-
-// The fused sweep's shared memory exceeds the 48 KB default in FP64: raise
-// the limit of every instantiation (per device, before the first launch).
-static void rb_set_smem_attributes() {
-    rb_attr_t<float, false>();
-    rb_attr_t<double, false>();
-    rb_attr_t<double, true>();
-}
-
-static void launch_sweep(Sampler &S, const Level &lv, bool forward, int noise, void *&x, void *&alt, const void *f,
-                         const NoiseArgs &nz, bool fp32, bool exact) {
-    if (fp32) {
-        float *xx = (float *)x, *aa = (float *)alt;
-        launch_sweep_noise<float, false>(S, lv, forward, noise, xx, aa, (const float *)f, nz);
-        x = xx;
-        alt = aa;
-    } else {
-        double *xx = (double *)x, *aa = (double *)alt;
-        if (exact)
-            launch_sweep_noise<double, true>(S, lv, forward, noise, xx, aa, (const double *)f, nz);
-        else
-            launch_sweep_noise<double, false>(S, lv, forward, noise, xx, aa, (const double *)f, nz);
-        x = xx;
-        alt = aa;
-    }
+// One sweep of x with right hand side f.
+static void launch_sweep(Sampler &S, const Level &lv, bool forward, int noise, void *x, const void *f, const NoiseArgs &nz,
+                         bool fp32, bool exact) {
+    if (fp32)
+        launch_sweep_noise<float, false>(S, lv, forward, noise, (float *)x, (const float *)f, nz);
+    else if (exact)
+        launch_sweep_noise<double, true>(S, lv, forward, noise, (double *)x, (const double *)f, nz);
+    else
+        launch_sweep_noise<double, false>(S, lv, forward, noise, (double *)x, (const double *)f, nz);
 }
 
 template <typename T>
@@ -334,12 +317,12 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
 // SORSampler::apply (sor_sampler.cc:37-59) / SORSmoother::apply
 // (sor_smoother.cc:40-54) on level `lev`: noise draw order n point normals,
 // then m low-rank normals.
-void Sampler::sor(int lev, bool forward, bool noisy, void *&x, void *&alt, void *f) {
+void Sampler::sor(int lev, bool forward, bool noisy, void *x, void *f) {
     Level &lv = L[lev];
     int noise = noisy ? noise_mode : NOISE_NONE;
     NoiseArgs nz = noisy ? noise_args(lev, lv.geo.n) : noise_args(lev, 0);
     if (!noisy) nz.buf = nullptr;
-    launch_sweep(*this, lv, forward, noise, x, alt, f, nz, fp32, exact);
+    launch_sweep(*this, lv, forward, noise, x, f, nz, fp32, exact);
     if (m > 0) {
         NoiseArgs nzl = noisy ? noise_args(lev, m) : noise_args(lev, 0);
         if (!noisy) nzl.buf = nullptr;
@@ -465,8 +448,8 @@ void Sampler::coarse_sample(int lev) {
         inv++;
     } else {
         for (int k = 0; k < P.ncoarsesmooth; ++k) {
-            sor(lev, true, true, lv.x, lv.x_alt, lv.f);
-            sor(lev, false, true, lv.x, lv.x_alt, lv.f);
+            sor(lev, true, true, lv.x, lv.f);
+            sor(lev, false, true, lv.x, lv.f);
         }
     }
 }
@@ -483,11 +466,11 @@ void Sampler::sample(int lev) {
     for (int j = 0; j < cyc; ++j) {
         if (P.smoother == MGMC_SMOOTHER_SSOR) {
             for (int k = 0; k < P.npresmooth; ++k) {
-                sor(lev, true, true, lv.x, lv.x_alt, lv.f);
-                sor(lev, false, true, lv.x, lv.x_alt, lv.f);
+                sor(lev, true, true, lv.x, lv.f);
+                sor(lev, false, true, lv.x, lv.f);
             }
         } else {
-            for (int k = 0; k < P.npresmooth; ++k) sor(lev, true, true, lv.x, lv.x_alt, lv.f);
+            for (int k = 0; k < P.npresmooth; ++k) sor(lev, true, true, lv.x, lv.f);
         }
         resid_restrict(lev);
         CK(cudaMemsetAsync(lc.x, 0, (size_t)lc.geo.nalloc * tsize(), stream));
@@ -495,11 +478,11 @@ void Sampler::sample(int lev) {
         prolong(lev, P.coarse_scaling, lc.x, lv.x);
         if (P.smoother == MGMC_SMOOTHER_SSOR) {
             for (int k = 0; k < P.npostsmooth; ++k) {
-                sor(lev, true, true, lv.x, lv.x_alt, lv.f);
-                sor(lev, false, true, lv.x, lv.x_alt, lv.f);
+                sor(lev, true, true, lv.x, lv.f);
+                sor(lev, false, true, lv.x, lv.f);
             }
         } else {
-            for (int k = 0; k < P.npostsmooth; ++k) sor(lev, false, true, lv.x, lv.x_alt, lv.f);
+            for (int k = 0; k < P.npostsmooth; ++k) sor(lev, false, true, lv.x, lv.f);
         }
     }
 }
@@ -519,14 +502,6 @@ void Sampler::launch_step() {
     noise_off = noise_pos;
     launches = 0;
     sample(0);
-    // an odd number of fused sweeps leaves a level's state in its second
-    // buffer: copy it home so that every step starts from the same buffers
-    for (auto &lv : L) {
-        if (lv.x != lv.x_home) {
-            CK(cudaMemcpyAsync(lv.x_home, lv.x, (size_t)lv.geo.nalloc * tsize(), cudaMemcpyDeviceToDevice, stream));
-            std::swap(lv.x, lv.x_alt);
-        }
-    }
     step_end();
 }
 
@@ -612,8 +587,6 @@ void Sampler::build_lowrank(int lev) {
     CK(cudaMemsetAsync(lv.counter, 0, sizeof(unsigned), stream));
     // FP64 work arrays
     double *xs = alloc<double>(geo.nalloc), *fs = alloc<double>(geo.nalloc);
-    double *xs2 = lv.fused ? alloc<double>(geo.nalloc) : nullptr;
-    if (xs2) CK(cudaMemsetAsync(xs2, 0, geo.nalloc * sizeof(double), stream));
     i64 *nzi = alloc<i64>(n);
     double *nzv = alloc<double>(n);
     unsigned long long *cnt = alloc<unsigned long long>(1);
@@ -628,9 +601,7 @@ void Sampler::build_lowrank(int lev) {
             if (cntj > 0) k_scatter<<<nblk(cntj, 256), 256, 0, stream>>>(lv.Bidx + b0, lv.Bval + b0, cntj, fs);
             NoiseArgs nz{};
             nz.d_step = d_step;
-            void *xa = xs, *xb = xs2;
-            launch_sweep(*this, lv, dir == 0, NOISE_NONE, xa, xb, fs, nz, false, exact);
-            if (xa != (void *)xs) std::swap(xs, xs2);
+            launch_sweep(*this, lv, dir == 0, NOISE_NONE, xs, fs, nz, false, exact);
             // G[:, j] = B^T C e_j
             LowRankArg lr{};
             lr.m = m;
@@ -782,9 +753,7 @@ void Sampler::build(const mgmc_operator_desc &op) {
     }
     for (auto &lv : L) {
         lv.x = talloc(lv.geo.nalloc);
-        lv.x_home = lv.x;
         lv.f = talloc(lv.geo.nalloc);
-        lv.fused = P.ordering == MGMC_ORDER_MULTICOLOUR && lv.npt == 7 && lv.ncol == 2;
         if (P.ordering == MGMC_ORDER_MULTICOLOUR && lv.npt == 27) {
             lv.bar = alloc<unsigned>(2);
             CK(cudaMemsetAsync(lv.bar, 0, 2 * sizeof(unsigned), stream));
@@ -795,24 +764,8 @@ void Sampler::build(const mgmc_operator_desc &op) {
             else
                 CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_coop<double, false, NOISE_PHILOX>, 256, 0));
             lv.coop_blocks = std::max(1, nsm * std::min(per_sm, 4));
-        }
-        if (lv.fused) {
-            lv.x_alt = talloc(lv.geo.nalloc);
-            rb_set_smem_attributes();
-            // one wave: z-chunks so that every CTA is resident at once
-            int nsm = 0, per_sm = 0;
-            CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, P.device));
-            if (fp32)
-                CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_rb<float, false, NOISE_PHILOX>, RB_THREADS,
-                                                                 rb_smem_bytes<float>()));
-            else
-                CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_rb<double, false, NOISE_PHILOX>, RB_THREADS,
-                                                                 rb_smem_bytes<double>()));
-            const i64 cols = (i64)((lv.g.N0 + RB_TX - 1) / RB_TX) * ((lv.g.N1 + RB_TY - 1) / RB_TY);
-            const i64 chunks = std::max<i64>(1, (i64)nsm * std::max(per_sm, 1) / cols);
-            lv.rb_cz = (int)std::max<i64>(2, (lv.g.N2 + chunks - 1) / chunks);
-            const char *cz = getenv("MGMC_RB_CZ");
-            if (cz) lv.rb_cz = std::max(1, atoi(cz));
+            const char *cp = getenv("MGMC_COARSE_PASSES");
+            if (cp && atoi(cp) > 0 && lv.geo.n >= atol(cp)) lv.colour_passes = true;
         }
     }
     d_cvec = alloc<double>(L[0].geo.n);
@@ -877,7 +830,6 @@ void Sampler::ensure_scratch(int lev) {
     Level &lv = L[lev];
     if (!lv.s1) lv.s1 = talloc(lv.geo.nalloc);
     if (!lv.s2) lv.s2 = talloc(lv.geo.nalloc);
-    if (!lv.s3) lv.s3 = talloc(lv.geo.nalloc);
 }
 
 // host / device compact FP64 vector -> padded T array of level lev
@@ -1340,7 +1292,7 @@ mgmc_status mgmc_level_sor(mgmc_sampler *s, int level, int direction, int with_n
         fail(MGMC_ERR_NOISE_EXHAUSTED, "injected noise exhausted");
     S.inv = 4095;
     S.noise_off = S.noise_pos;
-    S.sor(level, direction == MGMC_FORWARD, with_noise != 0, lv.s2, lv.s3, lv.s1);
+    S.sor(level, direction == MGMC_FORWARD, with_noise != 0, lv.s2, lv.s1);
     S.check_launch();
     if (with_noise && S.noise_mode == NOISE_INJECTED) S.noise_pos += need;
     get_vec(S, level, lv.s2, x, 0);
@@ -1360,12 +1312,8 @@ mgmc_status mgmc_level_sweep_device(mgmc_sampler *s, int level, int direction, i
     for (int64_t r = 0; r < nrepeat; ++r) {
         S.inv = 4094;
         if (!with_lowrank) S.m = 0;
-        S.sor(level, direction == MGMC_FORWARD, with_noise != 0, lv.x, lv.x_alt, lv.f);
+        S.sor(level, direction == MGMC_FORWARD, with_noise != 0, lv.x, lv.f);
         S.m = saved_m;
-    }
-    if (lv.x != lv.x_home) {
-        CK(cudaMemcpyAsync(lv.x_home, lv.x, (size_t)lv.geo.nalloc * S.tsize(), cudaMemcpyDeviceToDevice, S.stream));
-        std::swap(lv.x, lv.x_alt);
     }
     S.check_launch();
     API_END

@@ -6,8 +6,7 @@
 // zero, so stencil loads need no boundary tests.
 //
 // Kernels (one V-cycle at level l uses them in this order):
-//   k_sweep_rb          red-black SOR sweep of the fine 7-point level, both
-//                       colours in one pass (multicolour order)
+//   k_sweep_rb_pass     one colour of the red-black SOR sweep of a 7-point level
 //   k_sweep_coop        8-colour SOR sweep of a 27-point level in one
 //                       cooperative launch, grid barrier between colours
 //   k_sweep_wavefront   lexicographic SOR sweep as a hyperplane wavefront
@@ -174,234 +173,44 @@ __device__ __forceinline__ void sor_point(T *__restrict__ x, const T *__restrict
         x[P] = xo + s.omega_diag * (cval - res);
 }
 
-// ------------------------------------------- fused red-black SOR sweep
-// Both colours of a red-black SOR sweep in one pass over HBM (axis-only
-// stencils, i.e. the fine FD level).  A CTA owns an x-y tile of RB_TX x RB_TY
-// interior columns and a range of z-planes; it streams the planes through
-// shared memory and, plane by plane,
-//   1. computes the first colour's new values F on the tile plus a
-//      one-point halo (the halo is recomputed by the neighbouring CTAs:
-//      every CTA reads only old values, so no inter-CTA ordering exists),
-//   2. computes the second colour from F and writes both colours.
-// Old state and new state live in different buffers (xin -> xout), so
-// halos read by other CTAs are never overwritten.  With in-kernel noise the
-// normal of a point is a function of its coordinates only (Philox block per
-// (x, y) column and group of 4 planes), so recomputed halo points get the
-// same noise.  In exact mode the arithmetic is sor_point's: identical to
-// the per-colour kernels and to the oracle's multicolour sweep.
-constexpr int RB_TX = 62, RB_TY = 14;                 // interior tile
-constexpr int RB_W1 = RB_TX + 2, RB_H1 = RB_TY + 2;  // tile + halo 1 (F): 64 x 16
-constexpr int RB_W2 = RB_TX + 4, RB_H2 = RB_TY + 4;  // tile + halo 2 (old x): 66 x 18
-constexpr int RB_THREADS = (RB_W1 / 2) * RB_H1;       // 512: one thread per pair of halo-1 columns
-constexpr int RB_NLD = (RB_W2 * RB_H2 + RB_THREADS - 1) / RB_THREADS;
+// ------------------------------------------------- red-black SOR sweep
+// One colour of a red-black sweep of an axis-only (7-point) level: one
+// thread per point of the colour, a CTA covers 2 * RBP_THREADS consecutive
+// x-positions of one row (b, c), so every load instruction of a warp reads a
+// contiguous span.  The four points of the colour in an 8-point x-group
+// share one Philox block (each thread derives it; SIMT executes the four
+// copies together).  `reverse` walks the planes from the top so that the
+// second colour finds the data the first colour touched last in L2.
+constexpr int RBP_THREADS = 128;
 
-__device__ __forceinline__ float4 column_normals(const NoiseArgs &nz, const Grid3 &g, int a, int b, int cq) {
-    u64 sc = (*nz.d_step) * 4096ull + nz.invocation;
-    uint4 ctr = make_uint4((unsigned)((u64)b * g.N0 + a), (PURPOSE_POINT << 28) | (nz.level << 24) | (unsigned)cq,
-                           (unsigned)sc, (unsigned)(sc >> 32));
-    return normals4(philox4x32_10(ctr, noise_key(nz)));
-}
-
-// Normals of one lattice column, four planes per Philox block; planes are
-// requested in (nearly) ascending order, so two cached blocks suffice.
-struct ColumnNoise {
-    float4 cur, prev;
-    int qcur, qprev;
-    __device__ void init() {
-        qcur = qprev = -1000;
-        cur = prev = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    __device__ __forceinline__ float get(const NoiseArgs &nz, const Grid3 &g, int a, int b, int c) {
-        int q = c >> 2;
-        if (q == qcur) return pick(cur, c & 3);
-        if (q == qprev) return pick(prev, c & 3);
-        prev = cur;
-        qprev = qcur;
-        cur = column_normals(nz, g, a, b, q);
-        qcur = q;
-        return pick(cur, c & 3);
-    }
-};
-
-template <typename T, bool EXACT>
-__device__ __forceinline__ T rb_update(T xo, T xm, T xp, T ym, T yp, T zm, T zp, const StencilArg<T> &s, T fv,
-                                       bool noisy, T xi) {
-    typedef Ar<EXACT> A;
-    // ascending linear index: z-, y-, x-, centre, x+, y+, z+
-    T res = A::mul(s.w[4], zm);
-    res = A::add(res, A::mul(s.w[10], ym));
-    res = A::add(res, A::mul(s.w[12], xm));
-    res = A::add(res, A::mul(s.w[13], xo));
-    res = A::add(res, A::mul(s.w[14], xp));
-    res = A::add(res, A::mul(s.w[16], yp));
-    res = A::add(res, A::mul(s.w[22], zp));
-    T cval = fv;
-    if (noisy) cval = A::add(A::mul(s.sd, xi), cval);
-    if (EXACT) return A::add(xo, A::mul(s.omega, A::sub(cval, res)) / s.diag);
-    return xo + s.omega_diag * (cval - res);
-}
-
-template <typename T>
-constexpr size_t rb_smem_bytes() {
-    return sizeof(T) * (4 * RB_H2 * RB_W2 + 3 * RB_H1 * RB_W1);
-}
-
-// Thread = pair of adjacent halo-1 columns (one of each colour on every
-// plane), so both colours' work is spread evenly over the lanes.  Per plane
-// kk:  [A] first colour of plane kk on the halo-1 region,  [B] sync,
-// [C] second colour of plane kk-1 and both colours written out,  [D] the
-// old plane kk+2 (loaded into registers one plane earlier) stored to shared
-// memory,  [E] plane kk+3 loaded into registers,  [F] sync.  The global
-// load latency is hidden behind one plane of work; every address is a
-// per-thread in-plane offset computed once plus the plane offset.  Each
-// column's normals come four planes per Philox block; the blocks of both
-// columns are generated together whenever the plane index enters a new
-// group of four, so the control flow stays uniform across the warp.
 template <typename T, bool EXACT, int NOISE>
-__global__ void __launch_bounds__(RB_THREADS, 3) k_sweep_rb(const T *__restrict__ xin, T *__restrict__ xout,
-                                                           const T *__restrict__ f, Grid3 g, StencilArg<T> s,
-                                                           int first, int cz, NoiseArgs nz) {
-    extern __shared__ __align__(16) unsigned char rb_smem[];
-    T *xo = reinterpret_cast<T *>(rb_smem);                                   // [4][RB_H2][RB_W2]
-    T *Fr = reinterpret_cast<T *>(rb_smem + sizeof(T) * 4 * RB_H2 * RB_W2);  // [3][RB_H1][RB_W1]
-    constexpr int P2 = RB_H2 * RB_W2, P1 = RB_H1 * RB_W1;
-    const int a0 = blockIdx.x * RB_TX, b0 = blockIdx.y * RB_TY;
-    const int c0 = blockIdx.z * cz, c1 = min(c0 + cz, g.N2);
-    const int px = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int b = b0 - 1 + ty;
-    const int sy = (int)g.sy;
-    const bool row_in = b >= 0 && b < g.N1;
-    const bool row_tile = row_in && ty >= 1 && ty <= RB_TY;
-    int ac[2], foff[2], s2[2], s1[2];
-    bool cin[2], ctile[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int tx = 2 * px + h;
-        ac[h] = a0 - 1 + tx;
-        cin[h] = row_in && ac[h] >= 0 && ac[h] < g.N0;
-        ctile[h] = row_tile && cin[h] && tx >= 1 && tx <= RB_TX;
-        foff[h] = (b + 1) * sy + (ac[h] + 1);  // in-plane padded offset
-        s2[h] = (ty + 1) * RB_W2 + (tx + 1);   // halo-2 tile index
-        s1[h] = ty * RB_W1 + tx;               // halo-1 tile index
-    }
-    // the column of the pair that holds the first colour on plane kk is
-    // column fc0 for even kk, 1 - fc0 for odd kk
-    const int fc0 = ((ac[0] + b) & 1) == first ? 0 : 1;
-    int goff[RB_NLD], soff[RB_NLD];
-    bool gok[RB_NLD];
-#pragma unroll
-    for (int j = 0; j < RB_NLD; ++j) {
-        const int i = threadIdx.x + j * RB_THREADS;
-        const int la = i % RB_W2, lb = i / RB_W2;
-        const int ga = a0 - 2 + la, gb = b0 - 2 + lb;
-        gok[j] = i < P2 && ga >= 0 && ga < g.N0 && gb >= 0 && gb < g.N1;
-        goff[j] = (gb + 1) * sy + (ga + 1);
-        soff[j] = i < P2 ? i : -1;
-    }
-    T pre[RB_NLD];
-    auto fetch = [&](int c) {
-        const bool pin = c >= 0 && c < g.N2;
-        const T *base = xin + (i64)(c + 1) * g.sz;
-#pragma unroll
-        for (int j = 0; j < RB_NLD; ++j) pre[j] = (pin && gok[j]) ? base[goff[j]] : T(0);
-    };
-    // f of the column that is first colour on plane c, at planes c and c-1
-    // (the values steps [A] and [C] of plane c need), loaded one plane early
-    auto fetch_f = [&](int c, T &fa, T &fc) {
-        const bool b1 = ((c & 1) ? 1 - fc0 : fc0) == 1;
-        const bool in = b1 ? cin[1] : cin[0];
-        const int fo = b1 ? foff[1] : foff[0];
-        fa = (in && c >= 0 && c < g.N2) ? f[(i64)(c + 1) * g.sz + fo] : T(0);
-        fc = (in && c - 1 >= 0 && c - 1 < g.N2) ? f[(i64)c * g.sz + fo] : T(0);
-    };
-    auto commit = [&](int base) {
-#pragma unroll
-        for (int j = 0; j < RB_NLD; ++j)
-            if (soff[j] >= 0) xo[base + soff[j]] = pre[j];
-    };
-    // ring slots as offsets into shared memory: old planes kk-1, kk, kk+1
-    // (and kk+2 being stored), F planes kk-2, kk-1, kk; rotated every plane
-    int om = 0, o0 = P2, op = 2 * P2, on = 3 * P2;
-    int fm = 0, f0 = P1, fp = 2 * P1;
-    fetch(c0 - 2);
-    commit(om);
-    fetch(c0 - 1);
-    commit(o0);
-    fetch(c0);
-    commit(op);
-    fetch(c0 + 1);
-    __syncthreads();
-    T fA_next, fC_next;
-    fetch_f(c0 - 1, fA_next, fC_next);
-    float4 nb_cur[2], nb_prev[2];
-    int q_cur = -1000;
-    nb_cur[0] = nb_cur[1] = nb_prev[0] = nb_prev[1] = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int kk = c0 - 1; kk <= c1; ++kk) {
-        if (NOISE == NOISE_PHILOX && (kk >> 2) != q_cur) {
-            q_cur = kk >> 2;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                nb_prev[h] = nb_cur[h];
-                nb_cur[h] = cin[h] ? column_normals(nz, g, ac[h], b, q_cur) : make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-        }
-        // column A: first colour on plane kk, second colour on plane kk-1;
-        // column B the other one (selects, not indexing, keep them in registers)
-        const bool a1 = ((kk & 1) ? 1 - fc0 : fc0) == 1;
-        const int aA = a1 ? ac[1] : ac[0];
-        const int s2A = a1 ? s2[1] : s2[0], s1A = a1 ? s1[1] : s1[0], s1B = a1 ? s1[0] : s1[1];
-        const int foA = a1 ? foff[1] : foff[0], foB = a1 ? foff[0] : foff[1];
-        const bool cinA = a1 ? cin[1] : cin[0];
-        const bool tA = a1 ? ctile[1] : ctile[0], tB = a1 ? ctile[0] : ctile[1];
-        const T fA = fA_next, fC = fC_next;
-        fetch_f(kk + 1, fA_next, fC_next);
-        // [A] first colour of plane kk
-        {
-            T fval = T(0);
-            if (kk >= 0 && kk < g.N2 && cinA) {
-                T xi = T(0);
-                if (NOISE == NOISE_PHILOX) xi = (T)pick(a1 ? nb_cur[1] : nb_cur[0], kk & 3);
-                if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(aA, b, kk)];
-                const int q = o0 + s2A;
-                fval = rb_update<T, EXACT>(xo[q], xo[q - 1], xo[q + 1], xo[q - RB_W2], xo[q + RB_W2], xo[om + s2A],
-                                           xo[op + s2A], s, fA, NOISE != NOISE_NONE, xi);
-            }
-            Fr[fp + s1A] = fval;
-            Fr[fp + s1B] = T(0);
-        }
-        __syncthreads();
-        // [C] plane c = kk-1: column A holds the second colour there
-        const int c = kk - 1;
-        if (c >= c0 && c < c1) {
-            T *out = xout + (i64)(c + 1) * g.sz;
-            if (tB) out[foB] = Fr[f0 + s1B];
-            if (tA) {
-                T xi = T(0);
-                if (NOISE == NOISE_PHILOX) {
-                    const float4 cur = a1 ? nb_cur[1] : nb_cur[0], prv = a1 ? nb_prev[1] : nb_prev[0];
-                    xi = (T)pick((c >> 2) == q_cur ? cur : prv, c & 3);
-                }
-                if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(aA, b, c)];
-                const int q = f0 + s1A;
-                out[foA] = rb_update<T, EXACT>(xo[om + s2A], Fr[q - 1], Fr[q + 1], Fr[q - RB_W1], Fr[q + RB_W1],
-                                               Fr[fm + s1A], Fr[fp + s1A], s, fC, NOISE != NOISE_NONE, xi);
-            }
-        }
-        // [D] plane kk+2 into the free slot, [E] plane kk+3 into registers
-        commit(on);
-        fetch(kk + 3);
-        __syncthreads();
-        // rotate: old planes (kk, kk+1, kk+2, free), F planes (kk-1, kk, free)
-        const int t = om;
-        om = o0;
-        o0 = op;
-        op = on;
-        on = t;
-        const int u = fm;
-        fm = f0;
-        f0 = fp;
-        fp = u;
-    }
+__global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_pass(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
+                                                               StencilArg<T> s, int colour, int reverse, NoiseArgs nz) {
+    const int b = blockIdx.y;
+    const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
+    const int p = (colour + b + c) & 1;
+    const int a = 2 * (blockIdx.x * RBP_THREADS + threadIdx.x) + p;
+    T xi = T(0);
+    if (NOISE == NOISE_PHILOX) xi = (T)pick(point_normals(nz, g, a, b, c), (a & 7) >> 1);
+    if (a >= g.N0) return;
+    if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
+    sor_point<T, 7, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
+}
+
+// One colour of an 8-colour (27-point) sweep, one thread per point; the
+// launch-per-colour alternative to k_sweep_coop.
+template <typename T, bool EXACT, int NOISE>
+__global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
+                                                                StencilArg<T> s, int colour, NoiseArgs nz) {
+    const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
+    const int a = 2 * (blockIdx.x * RBP_THREADS + threadIdx.x) + pa;
+    const int b = 2 * blockIdx.y + pb, c = 2 * blockIdx.z + pc;
+    if (b >= g.N1 || c >= g.N2) return;
+    T xi = T(0);
+    if (NOISE == NOISE_PHILOX) xi = (T)pick(point_normals(nz, g, a, b, c), (a & 7) >> 1);
+    if (a >= g.N0) return;
+    if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
+    sor_point<T, 27, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
 }
 
 // ---------------------------------------------------------- grid barrier
