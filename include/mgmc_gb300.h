@@ -61,8 +61,7 @@ typedef enum mgmc_status {
     MGMC_ERR_OUT_OF_MEMORY = 5,
     MGMC_ERR_NOISE_EXHAUSTED = 6,  /* injected-noise mode: not enough normals queued */
     MGMC_ERR_NONFINITE = 7,        /* NaN/Inf seen in the chain state */
-    MGMC_ERR_UNSUPPORTED = 8,
-    MGMC_ERR_TIMEOUT = 9           /* a bounded wait inside a kernel gave up (grid barrier) */
+    MGMC_ERR_UNSUPPORTED = 8
 } mgmc_status;
 
 /* sweep ordering */
@@ -197,9 +196,8 @@ mgmc_status mgmc_level_sweep_device(mgmc_sampler *s, int level, int direction, i
  * together: one CUDA graph holds every chain's step as a child graph, so
  * the chains run concurrently.  Chains keep their own state, right hand
  * side and observables; they must use MGMC_NOISE_PHILOX and one device.
- * Inside a batch each chain's coarse-level cooperative sweeps run on a
- * single CTA.  The samplers must outlive the batch; while it exists, step
- * them only through mgmc_batch_step. */
+ * The samplers must outlive the batch; while it exists, step them only
+ * through mgmc_batch_step. */
 typedef struct mgmc_batch mgmc_batch;
 mgmc_status mgmc_batch_create(int nchain, mgmc_sampler *const *samplers, mgmc_batch **out);
 mgmc_status mgmc_batch_step(mgmc_batch *b, int64_t nsteps);

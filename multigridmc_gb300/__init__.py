@@ -39,7 +39,7 @@ __all__ = [
 OK = 0
 STATUS = {0: "MGMC_OK", 1: "MGMC_ERR_INVALID_ARGUMENT", 2: "MGMC_ERR_LATTICE", 3: "MGMC_ERR_NOT_SPD",
           4: "MGMC_ERR_CUDA", 5: "MGMC_ERR_OUT_OF_MEMORY", 6: "MGMC_ERR_NOISE_EXHAUSTED",
-          7: "MGMC_ERR_NONFINITE", 8: "MGMC_ERR_UNSUPPORTED", 9: "MGMC_ERR_TIMEOUT"}
+          7: "MGMC_ERR_NONFINITE", 8: "MGMC_ERR_UNSUPPORTED"}
 LEXICOGRAPHIC, MULTICOLOUR = 0, 1
 FP64, FP32_MIXED = 0, 1
 PHILOX, INJECTED = 0, 1

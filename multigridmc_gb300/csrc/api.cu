@@ -14,6 +14,7 @@
 #include <map>
 #include <string>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/mgmc_gb300.h"
@@ -84,9 +85,6 @@ struct Level {
     float *zf = nullptr, *Bvalf = nullptr;
     unsigned *counter = nullptr;
     int bt_split = 1;  // blocks per column of the B^T x reduction
-    unsigned *bar = nullptr;  // grid barrier of the cooperative sweep
-    int coop_blocks = 1;      // co-resident CTAs of the cooperative sweep
-    bool colour_passes = false;  // 27-point sweeps as one launch per colour
 };
 
 struct Sampler {
@@ -122,7 +120,6 @@ struct Sampler {
     bool counting = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
-    bool batched = false;  // member of an mgmc_batch: single-CTA cooperative sweeps
     std::vector<void *> owned;  // every device allocation
 
     template <typename P_>
@@ -196,6 +193,10 @@ NoiseArgs Sampler::noise_args(int lev, i64 count) {
 }
 
 // ----------------------------------------------------------- sweep launch
+template <typename T, bool EXACT, int NOISE>
+static void launch_colour_passes(Sampler &S, const Level &lv, bool forward, T *x, const T *f, const StencilArg<T> &s,
+                                 const NoiseArgs &nz);
+
 template <typename T, int NPT, bool EXACT, int NOISE>
 static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, const T *f, const NoiseArgs &nz) {
     StencilArg<T> s = stencil_arg<T>(lv, S.P.omega);
@@ -206,45 +207,41 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
         return;
     }
     if (NPT == 7) {
-        // red-black: two passes, the second walking the planes downwards
-        dim3 grid((lv.g.N0 + 2 * RBP_THREADS - 1) / (2 * RBP_THREADS), lv.g.N1, lv.g.N2);
+        // red-black: two passes, the second walking the planes downwards;
+        // FP32 rows padded to a multiple of 4 floats use the vector pass
+        const bool vec = sizeof(T) == 4 && !EXACT && (lv.g.sy % 4) == 0 && (lv.g.sz % 4) == 0;
         for (int pass = 0; pass < 2; ++pass) {
             const int colour = forward ? pass : 1 - pass;
-            k_sweep_rb_pass<T, EXACT, NOISE><<<grid, RBP_THREADS, 0, S.stream>>>(x, f, lv.g, s, colour, pass, nz);
+            if constexpr (std::is_same<T, float>::value) {
+                if (vec) {
+                    dim3 grid(((lv.g.N0 + 8) / 8 + RBP_THREADS - 1) / RBP_THREADS, lv.g.N1, lv.g.N2);
+                    k_sweep_rb_vec<NOISE><<<grid, RBP_THREADS, 0, S.stream>>>(x, f, lv.g, s, colour, pass, nz);
+                    S.launches++;
+                    continue;
+                }
+            }
+            {
+                dim3 grid((lv.g.N0 + 2 * RBP_THREADS - 1) / (2 * RBP_THREADS), lv.g.N1, lv.g.N2);
+                k_sweep_rb_pass<T, EXACT, NOISE><<<grid, RBP_THREADS, 0, S.stream>>>(x, f, lv.g, s, colour, pass, nz);
+            }
             S.launches++;
         }
-        return;
+    } else {
+        launch_colour_passes<T, EXACT, NOISE>(S, lv, forward, x, f, s, nz);
     }
-    if (lv.colour_passes) {
-        // 2^dim colours, one launch per colour
-        for (int cc = 0; cc < lv.ncol; ++cc) {
-            const int colour = forward ? cc : lv.ncol - 1 - cc;
-            const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
-            const int na = (lv.g.N0 - pa + 1) / 2, nb = (lv.g.N1 - pb + 1) / 2, nc = (lv.g.N2 - pc + 1) / 2;
-            if (na <= 0 || nb <= 0 || nc <= 0) continue;
-            dim3 grid((na + RBP_THREADS - 1) / RBP_THREADS, nb, nc);
-            k_sweep_c27_pass<T, EXACT, NOISE><<<grid, RBP_THREADS, 0, S.stream>>>(x, f, lv.g, s, colour, nz);
-            S.launches++;
-        }
-        return;
-    }
-    // 2^dim colours: all colours in one cooperative launch
-    {
-        const i64 items = (i64)((lv.g.N0 + 1) / 2) * ((lv.g.N1 + 1) / 2) * ((lv.g.N2 + 1) / 2);
-        const unsigned grid =
-            (unsigned)std::max<i64>(1, std::min<i64>((items + 255) / 256, S.batched ? 1 : lv.coop_blocks));
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(grid);
-        cfg.blockDim = dim3(256);
-        cfg.dynamicSmemBytes = 0;
-        cfg.stream = S.stream;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeCooperative;
-        attr[0].val.cooperative = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        int forward_i = forward ? 1 : 0;
-        CK(cudaLaunchKernelEx(&cfg, k_sweep_coop<T, EXACT, NOISE>, x, f, lv.g, s, lv.ncol, forward_i, nz, lv.bar, S.d_err));
+}
+
+// 2^dim colours, one launch per colour
+template <typename T, bool EXACT, int NOISE>
+static void launch_colour_passes(Sampler &S, const Level &lv, bool forward, T *x, const T *f, const StencilArg<T> &s,
+                                 const NoiseArgs &nz) {
+    for (int cc = 0; cc < lv.ncol; ++cc) {
+        const int colour = forward ? cc : lv.ncol - 1 - cc;
+        const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
+        const int na = (lv.g.N0 - pa + 1) / 2, nb = (lv.g.N1 - pb + 1) / 2, nc = (lv.g.N2 - pc + 1) / 2;
+        if (na <= 0 || nb <= 0 || nc <= 0) continue;
+        dim3 grid((na + RBP_THREADS - 1) / RBP_THREADS, nb, nc);
+        k_sweep_c27_pass<T, EXACT, NOISE><<<grid, RBP_THREADS, 0, S.stream>>>(x, f, lv.g, s, colour, nz);
         S.launches++;
     }
 }
@@ -295,7 +292,7 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     lr.z = lv.z;
     lr.part = lv.part;
     lr.counter = lv.counter;
-    size_t smem = 2 * sizeof(double) * S.m;
+    size_t smem = 3 * sizeof(double) * S.m;
     dim3 grid(S.m, lv.bt_split);
     if (noise == NOISE_NONE)
         k_bt_x_z<T, NOISE_NONE, true><<<grid, 256, smem, S.stream>>>(x, lr, nz);
@@ -342,14 +339,12 @@ static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void
         for (int k = 0; k < 27; ++k) s.w[k] = T(0);
     const i64 nc = lc.geo.n;
     if (S.dim == 3 && !zero_stencil) {
-        const int cols = ((lc.g.N0 + RR_TX - 1) / RR_TX) * ((lc.g.N1 + RR_TY - 1) / RR_TY);
-        const int want = std::max(1, (4 * 152 + cols - 1) / cols);  // chunks for about four CTAs per SM
-        const int czc = std::max(2, (lc.g.N2 + want - 1) / want);
-        dim3 grid((lc.g.N0 + RR_TX - 1) / RR_TX, (lc.g.N1 + RR_TY - 1) / RR_TY, (lc.g.N2 + czc - 1) / czc);
+        dim3 grid((lc.g.N0 + RR_TX - 1) / RR_TX, (lc.g.N1 + RR_TY - 1) / RR_TY, (lc.g.N2 + RR_TZ - 1) / RR_TZ);
+        const size_t sm = rr_smem_bytes<T>();
         if (lv.npt == 7)
-            k_resid_restrict_tiled<T, 7><<<grid, RR_THREADS, 0, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, czc);
+            k_resid_restrict_tiled<T, 7><<<grid, RR_THREADS, sm, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s);
         else
-            k_resid_restrict_tiled<T, 27><<<grid, RR_THREADS, 0, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, czc);
+            k_resid_restrict_tiled<T, 27><<<grid, RR_THREADS, sm, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s);
         S.launches++;
         return;
     }
@@ -715,6 +710,10 @@ void Sampler::build(const mgmc_operator_desc &op) {
     m = op.m;
     CK(cudaSetDevice(P.device));
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaFuncSetAttribute(k_resid_restrict_tiled<double, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)rr_smem_bytes<double>()));
+    CK(cudaFuncSetAttribute(k_resid_restrict_tiled<double, 27>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)rr_smem_bytes<double>()));
     d_step = alloc<u64>(1);
     d_obs_count = alloc<u64>(1);
     d_err = alloc<unsigned>(1);
@@ -754,19 +753,6 @@ void Sampler::build(const mgmc_operator_desc &op) {
     for (auto &lv : L) {
         lv.x = talloc(lv.geo.nalloc);
         lv.f = talloc(lv.geo.nalloc);
-        if (P.ordering == MGMC_ORDER_MULTICOLOUR && lv.npt == 27) {
-            lv.bar = alloc<unsigned>(2);
-            CK(cudaMemsetAsync(lv.bar, 0, 2 * sizeof(unsigned), stream));
-            int nsm = 0, per_sm = 0;
-            CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, P.device));
-            if (fp32)
-                CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_coop<float, false, NOISE_PHILOX>, 256, 0));
-            else
-                CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_coop<double, false, NOISE_PHILOX>, 256, 0));
-            lv.coop_blocks = std::max(1, nsm * std::min(per_sm, 4));
-            const char *cp = getenv("MGMC_COARSE_PASSES");
-            if (cp && atoi(cp) > 0 && lv.geo.n >= atol(cp)) lv.colour_passes = true;
-        }
     }
     d_cvec = alloc<double>(L[0].geo.n);
     // low-rank term on every level: B_{l+1} = R B_l
@@ -1053,7 +1039,6 @@ mgmc_status mgmc_sampler_apply(mgmc_sampler *s, const double *f, double *x, int 
     CK(cudaStreamSynchronize(S.stream));
     unsigned err = 0;
     CK(cudaMemcpy(&err, S.d_err, sizeof(err), cudaMemcpyDeviceToHost));
-    if (err & 2u) fail(MGMC_ERR_TIMEOUT, "a grid barrier wait timed out in a cooperative sweep");
     if (err) fail(MGMC_ERR_NONFINITE, "non-finite observable in the chain");
     API_END
 }
@@ -1123,7 +1108,6 @@ mgmc_status mgmc_sampler_read_observations(mgmc_sampler *s, double *out, int64_t
     CK(cudaMemset(S.d_obs_count, 0, sizeof(u64)));
     unsigned err = 0;
     CK(cudaMemcpy(&err, S.d_err, sizeof(err), cudaMemcpyDeviceToHost));
-    if (err & 2u) fail(MGMC_ERR_TIMEOUT, "a grid barrier wait timed out in a cooperative sweep");
     if (err) fail(MGMC_ERR_NONFINITE, "non-finite observable in the chain");
     API_END
 }
@@ -1348,15 +1332,6 @@ mgmc_status mgmc_batch_create(int nchain, mgmc_sampler *const *samplers, mgmc_ba
     CK(cudaGraphCreate(&B->graph, 0));
     for (Sampler *S : B->chains) {
         CK(cudaStreamSynchronize(S->stream));
-        // every chain's cooperative sweeps use one CTA, so that concurrent
-        // branches never wait on CTAs that cannot become resident
-        if (!S->batched && S->gexec) {
-            cudaGraphExecDestroy(S->gexec);
-            cudaGraphDestroy(S->graph);
-            S->gexec = nullptr;
-            S->graph = nullptr;
-        }
-        S->batched = true;
         ensure_graph(*S);
         cudaGraphNode_t node;
         CK(cudaGraphAddChildGraphNode(&node, B->graph, nullptr, 0, S->graph));

@@ -7,8 +7,7 @@
 //
 // Kernels (one V-cycle at level l uses them in this order):
 //   k_sweep_rb_pass     one colour of the red-black SOR sweep of a 7-point level
-//   k_sweep_coop        8-colour SOR sweep of a 27-point level in one
-//                       cooperative launch, grid barrier between colours
+//   k_sweep_c27_pass    one colour of the 8-colour SOR sweep of a 27-point level
 //   k_sweep_wavefront   lexicographic SOR sweep as a hyperplane wavefront
 //                       (one CTA; parity mode)
 //   k_bt_x_z            y = B^T x and the m x m low-rank solve
@@ -174,13 +173,20 @@ __device__ __forceinline__ void sor_point(T *__restrict__ x, const T *__restrict
 }
 
 // ------------------------------------------------- red-black SOR sweep
-// One colour of a red-black sweep of an axis-only (7-point) level: one
-// thread per point of the colour, a CTA covers 2 * RBP_THREADS consecutive
-// x-positions of one row (b, c), so every load instruction of a warp reads a
-// contiguous span.  The four points of the colour in an 8-point x-group
-// share one Philox block (each thread derives it; SIMT executes the four
-// copies together).  `reverse` walks the planes from the top so that the
-// second colour finds the data the first colour touched last in L2.
+// Noise of a 7-point level: the normals of the 4 points of one x-parity in
+// the 8-aligned group of padded positions P = a + 1 in [8q, 8q + 8) of row
+// (b, c) come from one Philox block, lane (P & 7) >> 1.
+__device__ __forceinline__ float4 fine_normals(const NoiseArgs &nz, const Grid3 &g, int P, int b, int c) {
+    const unsigned G0 = (unsigned)((g.N0 + 1) >> 3) + 1u;
+    const unsigned grp = (unsigned)(((u64)c * g.N1 + b) * G0 + (P >> 3));
+    return normals4(philox4x32_10(noise_ctr(nz, grp, PURPOSE_POINT, P & 1), noise_key(nz)));
+}
+
+// One colour of a red-black sweep of an axis-only (7-point) level, one
+// thread per point of the colour; a CTA covers 2 * RBP_THREADS consecutive
+// x-positions of one row (b, c), so each warp load reads a contiguous span.
+// `reverse` walks the planes from the top so that the second colour finds
+// the data the first colour touched last in L2.
 constexpr int RBP_THREADS = 128;
 
 template <typename T, bool EXACT, int NOISE>
@@ -191,14 +197,85 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_pass(T *__restrict__ x
     const int p = (colour + b + c) & 1;
     const int a = 2 * (blockIdx.x * RBP_THREADS + threadIdx.x) + p;
     T xi = T(0);
-    if (NOISE == NOISE_PHILOX) xi = (T)pick(point_normals(nz, g, a, b, c), (a & 7) >> 1);
+    if (NOISE == NOISE_PHILOX) xi = (T)pick(fine_normals(nz, g, a + 1, b, c), ((a + 1) & 7) >> 1);
     if (a >= g.N0) return;
     if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
     sor_point<T, 7, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
 }
 
-// One colour of an 8-colour (27-point) sweep, one thread per point; the
-// launch-per-colour alternative to k_sweep_coop.
+// FP32 variant with vector loads (rows padded to a multiple of 4 floats): a
+// thread owns the 8 padded positions [8q, 8q + 8) of a row, loads them and
+// the matching spans of the four neighbouring rows and f as float4, draws
+// one Philox block for its 4 points of the colour and stores those 4 points.
+template <int NOISE>
+__global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict__ x, const float *__restrict__ f,
+                                                              Grid3 g, StencilArg<float> s, int colour, int reverse,
+                                                              NoiseArgs nz) {
+    const int b = blockIdx.y;
+    const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
+    const int q = blockIdx.x * RBP_THREADS + threadIdx.x;
+    const int ngrp = (g.N0 + 8) >> 3;
+    if (q >= ngrp) return;
+    const int P0 = 8 * q;
+    const i64 rb = (i64)(c + 1) * g.sz + (i64)(b + 1) * g.sy;
+    const float4 *xr = reinterpret_cast<const float4 *>(x + rb + P0);
+    const float4 *xn = reinterpret_cast<const float4 *>(x + rb - g.sy + P0);
+    const float4 *xs_ = reinterpret_cast<const float4 *>(x + rb + g.sy + P0);
+    const float4 *xd = reinterpret_cast<const float4 *>(x + rb - g.sz + P0);
+    const float4 *xu = reinterpret_cast<const float4 *>(x + rb + g.sz + P0);
+    const float4 *fr = reinterpret_cast<const float4 *>(f + rb + P0);
+    float v[10], ym[8], yp[8], zm[8], zp[8], fv[8];
+    {
+        const float4 a0 = xr[0], a1 = xr[1];
+        v[0] = P0 > 0 ? x[rb + P0 - 1] : 0.f;  // P0 - 1 is a ghost column for q = 0 (read 0 directly)
+        v[1] = a0.x; v[2] = a0.y; v[3] = a0.z; v[4] = a0.w;
+        v[5] = a1.x; v[6] = a1.y; v[7] = a1.z; v[8] = a1.w;
+        v[9] = x[rb + P0 + 8];
+        const float4 n0 = xn[0], n1 = xn[1], s0 = xs_[0], s1 = xs_[1], d0 = xd[0], d1 = xd[1], u0 = xu[0], u1 = xu[1];
+        const float4 f0 = fr[0], f1 = fr[1];
+        ym[0] = n0.x; ym[1] = n0.y; ym[2] = n0.z; ym[3] = n0.w; ym[4] = n1.x; ym[5] = n1.y; ym[6] = n1.z; ym[7] = n1.w;
+        yp[0] = s0.x; yp[1] = s0.y; yp[2] = s0.z; yp[3] = s0.w; yp[4] = s1.x; yp[5] = s1.y; yp[6] = s1.z; yp[7] = s1.w;
+        zm[0] = d0.x; zm[1] = d0.y; zm[2] = d0.z; zm[3] = d0.w; zm[4] = d1.x; zm[5] = d1.y; zm[6] = d1.z; zm[7] = d1.w;
+        zp[0] = u0.x; zp[1] = u0.y; zp[2] = u0.z; zp[3] = u0.w; zp[4] = u1.x; zp[5] = u1.y; zp[6] = u1.z; zp[7] = u1.w;
+        fv[0] = f0.x; fv[1] = f0.y; fv[2] = f0.z; fv[3] = f0.w; fv[4] = f1.x; fv[5] = f1.y; fv[6] = f1.z; fv[7] = f1.w;
+    }
+    // points of the colour: padded P with (P - 1 + b + c) & 1 == colour; the
+    // two parities get separate code so that every register index is static
+    const int j0 = (colour + b + c + 1) & 1;  // first local index j (P = P0 + j) of the colour
+    float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (NOISE == NOISE_PHILOX) nrm = fine_normals(nz, g, P0 + j0, b, c);
+    auto upd = [&](int j, int k) {
+        const int a = P0 + j - 1;
+        if (a < 0 || a >= g.N0) return;
+        float xi = 0.f;
+        if (NOISE == NOISE_PHILOX) xi = pick(nrm, k);
+        if (NOISE == NOISE_INJECTED) xi = (float)nz.buf[g.compact(a, b, c)];
+        float res = s.w[4] * zm[j];
+        res = fmaf(s.w[10], ym[j], res);
+        res = fmaf(s.w[12], v[j], res);
+        res = fmaf(s.w[13], v[j + 1], res);
+        res = fmaf(s.w[14], v[j + 2], res);
+        res = fmaf(s.w[16], yp[j], res);
+        res = fmaf(s.w[22], zp[j], res);
+        float cval = fv[j];
+        if (NOISE != NOISE_NONE) cval = fmaf(s.sd, xi, cval);
+        x[rb + P0 + j] = v[j + 1] + s.omega_diag * (cval - res);
+    };
+    if (j0 == 0) {
+        upd(0, 0);
+        upd(2, 1);
+        upd(4, 2);
+        upd(6, 3);
+    } else {
+        upd(1, 0);
+        upd(3, 1);
+        upd(5, 2);
+        upd(7, 3);
+    }
+}
+
+// One colour of an 8-colour (27-point) sweep, one thread per point (colour
+// index (a & 1) | (b & 1) << 1 | (c & 1) << 2).
 template <typename T, bool EXACT, int NOISE>
 __global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
                                                                 StencilArg<T> s, int colour, NoiseArgs nz) {
@@ -211,72 +288,6 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ 
     if (a >= g.N0) return;
     if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
     sor_point<T, 27, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
-}
-
-// ---------------------------------------------------------- grid barrier
-// Barrier across the CTAs of one cooperative launch (all CTAs co-resident).
-// bar[0] counts arrivals, bar[1] is the generation.  A wait gives up after
-// GRID_BARRIER_SPINS polls (well over a second), raises bit 2 of *err and
-// returns, so a missing CTA costs a wrong sample and an error status, never
-// a hung GPU.
-constexpr long long GRID_BARRIER_SPINS = 1ll << 24;
-
-__device__ __forceinline__ void grid_barrier(unsigned *bar, unsigned *err) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned gen;
-        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(gen) : "l"(bar + 1) : "memory");
-        const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
-        unsigned arrived;
-        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(arrived) : "l"(bar) : "memory");
-        if (arrived == nb - 1) {
-            asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(bar) : "memory");
-            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar + 1) : "memory");
-        } else {
-            long long it = 0;
-            unsigned now;
-            do {
-                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(now) : "l"(bar + 1) : "memory");
-                if (now != gen) break;
-                if (++it > GRID_BARRIER_SPINS) {
-                    atomicOr(err, 2u);
-                    break;
-                }
-                if (it > 64) __nanosleep(32);
-            } while (true);
-        }
-    }
-    __syncthreads();
-}
-
-// Multicolour sweep of a 2^dim-colour (9- / 27-point) level in one
-// cooperative launch: the colours run in order, separated by grid barriers.
-// Thread work item = (8-point x-group, row of the colour); the <= 4 points of
-// the colour in the group share one Philox block.  Colour index
-// (a & 1) | (b & 1) << 1 | (c & 1) << 2, ascending forward, descending
-// backward.
-template <typename T, bool EXACT, int NOISE>
-__global__ void __launch_bounds__(256) k_sweep_coop(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
-                                                     StencilArg<T> s, int ncol, int forward, NoiseArgs nz,
-                                                     unsigned *bar, unsigned *err) {
-    const int nthreads = gridDim.x * blockDim.x;
-    for (int cc = 0; cc < ncol; ++cc) {
-        const int col = forward ? cc : ncol - 1 - cc;
-        const int pa = col & 1, pb = (col >> 1) & 1, pc = (col >> 2) & 1;
-        const int na = (g.N0 - pa + 1) >> 1, nb = (g.N1 - pb + 1) >> 1, nc = (g.N2 - pc + 1) >> 1;
-        const int items = na * nb * nc;
-        for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < items; t += nthreads) {
-            const int ia = t % na, r = t / na;
-            const int a = 2 * ia + pa, b = 2 * (r % nb) + pb, c = 2 * (r / nb) + pc;
-            T xi = T(0);
-            // the normal of the point is lane (a & 7) >> 1 of its group's block,
-            // the same value the group-per-thread mapping draws
-            if (NOISE == NOISE_PHILOX) xi = (T)pick(point_normals(nz, g, a, b, c), (a & 7) >> 1);
-            if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
-            sor_point<T, 27, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
-        }
-        if (cc + 1 < ncol) grid_barrier(bar, err);
-    }
 }
 
 // ------------------------------------------------ lexicographic wavefront
@@ -372,16 +383,20 @@ __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRank
     if (!last) return;
     __threadfence();
     const int m = lr.m;
-    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    // y_k: warp per column, lanes over the P partial sums
+    for (int k = warp; k < m; k += nwarp) {
         double t = 0.0;
-        for (int q = 0; q < P; ++q) t += ((volatile double *)lr.part)[k * P + q];
-        lr.y[k] = t;
+        for (int q = lane; q < P; q += 32) t += ((volatile double *)lr.part)[k * P + q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) lr.y[k] = t;
     }
     if (threadIdx.x == 0) *lr.counter = 0u;
     if (!SOLVE) return;
-    __syncthreads();
     extern __shared__ double dyn[];
-    double *w = dyn, *v = dyn + m;
+    double *w = dyn, *v = dyn + m, *ys = dyn + 2 * m;
+    __syncthreads();
     for (int k = threadIdx.x; k < m; k += blockDim.x) {
         double xi = 0.0;
         if (NOISE == NOISE_PHILOX) {
@@ -390,29 +405,45 @@ __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRank
         }
         if (NOISE == NOISE_INJECTED) xi = nz.buf[k];
         w[k] = lr.sinv_sqrt[k] * xi;
+        ys[k] = lr.y[k];
     }
     __syncthreads();
-    // m x m products, one warp per row (coalesced row loads, shuffle sums)
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    for (int k = warp; k < m; k += nwarp) {
-        const double *row = lr.G + (i64)k * m;
-        double t = 0.0;
-        for (int q = lane; q < m; q += 32) t += row[q] * w[q];
+    // m x m products, one warp per row, four rows in flight per warp
+    for (int k0 = warp; k0 < m; k0 += 4 * nwarp) {
+        double t[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) v[k] = lr.y[k] + t;
+        for (int r = 0; r < 4; ++r) {
+            const int k = k0 + r * nwarp;
+            if (k < m)
+                for (int q = lane; q < m; q += 32) t[r] += lr.G[(i64)k * m + q] * w[q];
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t[r] += __shfl_xor_sync(0xffffffffu, t[r], o);
+            const int k = k0 + r * nwarp;
+            if (lane == 0 && k < m) v[k] = ys[k] + t[r];
+        }
     }
     __syncthreads();
-    for (int k = warp; k < m; k += nwarp) {
-        const double *row = lr.Sinv + (i64)k * m;
-        double t = 0.0;
-        for (int q = lane; q < m; q += 32) t += row[q] * v[q];
+    for (int k0 = warp; k0 < m; k0 += 4 * nwarp) {
+        double t[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) {
-            const double zk = w[k] - t;
-            lr.z[k] = zk;
-            if (lr.zf) lr.zf[k] = (float)zk;
+        for (int r = 0; r < 4; ++r) {
+            const int k = k0 + r * nwarp;
+            if (k < m)
+                for (int q = lane; q < m; q += 32) t[r] += lr.Sinv[(i64)k * m + q] * v[q];
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t[r] += __shfl_xor_sync(0xffffffffu, t[r], o);
+            const int k = k0 + r * nwarp;
+            if (lane == 0 && k < m) {
+                const double zk = w[k] - t[r];
+                lr.z[k] = zk;
+                if (lr.zf) lr.zf[k] = (float)zk;
+            }
         }
     }
 }
@@ -482,151 +513,79 @@ __global__ void __launch_bounds__(256) k_resid_restrict(const T *__restrict__ x,
     fc[gc.pad(a, b, c)] = acc;
 }
 
-// Plane-streaming variant: a CTA owns a tile of RR_TX x RR_TY coarse
-// columns and a range of coarse planes.  Fine residual planes are computed
-// once each on the (2 RR_TX + 1) x (2 RR_TY + 1) fine footprint of the tile
-// and kept in a ring of three planes; every second fine plane completes a
-// coarse plane, which is restricted from the ring.  x (with a one-point
-// halo) and f are loaded into registers one plane ahead of their use, so the
-// global load latency overlaps the work on the current plane.
-constexpr int RR_TX = 16, RR_TY = 8;
-constexpr int RR_FW = 2 * RR_TX + 1, RR_FH = 2 * RR_TY + 1;  // fine residual footprint
-constexpr int RR_XW = RR_FW + 2, RR_XH = RR_FH + 2;          // x with halo
-constexpr int RR_THREADS = 256;
-constexpr int RR_NX = (RR_XW * RR_XH + RR_THREADS - 1) / RR_THREADS;
-constexpr int RR_NF = (RR_FW * RR_FH + RR_THREADS - 1) / RR_THREADS;
+// 3D-tiled variant: a CTA owns RR_TX x RR_TY x RR_TZ coarse points (one per
+// thread).  It stages the x values of the tile's fine footprint plus a
+// one-point halo in shared memory (all loads issued at once), computes each
+// fine residual of the footprint once, and restricts.
+constexpr int RR_TX = 8, RR_TY = 8, RR_TZ = 4;
+constexpr int RR_FW = 2 * RR_TX + 1, RR_FH = 2 * RR_TY + 1, RR_FD = 2 * RR_TZ + 1;  // residual footprint
+constexpr int RR_XW = RR_FW + 2, RR_XH = RR_FH + 2, RR_XD = RR_FD + 2;             // x with halo
+constexpr int RR_THREADS = RR_TX * RR_TY * RR_TZ;                                   // 256
+
+template <typename T>
+constexpr size_t rr_smem_bytes() {
+    return sizeof(T) * (RR_XW * RR_XH * RR_XD + RR_FW * RR_FH * RR_FD);
+}
 
 template <typename T, int NPT>
 __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tiled(const T *__restrict__ x, const T *__restrict__ f,
                                                                       T *__restrict__ fc, Grid3 gf, Grid3 gc,
-                                                                      StencilArg<T> s, int czc) {
-    __shared__ T xs[4][RR_XH * RR_XW];
-    __shared__ T rs[3][RR_FH * RR_FW];
-    const int ca0 = blockIdx.x * RR_TX, cb0 = blockIdx.y * RR_TY;
-    const int cc0 = blockIdx.z * czc, cc1 = min(cc0 + czc, gc.N2);
-    // fine 0-based origin of the footprint: the centre of coarse (ca0, cb0)
-    // is fine 2 ca0 + 1, its left neighbour 2 ca0
-    const int fa0 = 2 * ca0, fb0 = 2 * cb0;
-    const int sy = (int)gf.sy;
-    int xoff[RR_NX], xsi[RR_NX];
-    bool xok[RR_NX];
-#pragma unroll
-    for (int j = 0; j < RR_NX; ++j) {
-        const int i = threadIdx.x + j * RR_THREADS;
-        const int la = i % RR_XW, lb = i / RR_XW;
-        const int ga = fa0 - 1 + la, gb = fb0 - 1 + lb;
-        xok[j] = i < RR_XW * RR_XH && ga >= 0 && ga < gf.N0 && gb >= 0 && gb < gf.N1;
-        xoff[j] = (gb + 1) * sy + (ga + 1);
-        xsi[j] = i < RR_XW * RR_XH ? i : -1;
+                                                                      StencilArg<T> s) {
+    extern __shared__ __align__(16) unsigned char rr_smem[];
+    T *xs = reinterpret_cast<T *>(rr_smem);             // [RR_XD][RR_XH][RR_XW]
+    T *rs = xs + RR_XW * RR_XH * RR_XD;                  // [RR_FD][RR_FH][RR_FW]
+    const int ca0 = blockIdx.x * RR_TX, cb0 = blockIdx.y * RR_TY, cc0 = blockIdx.z * RR_TZ;
+    // fine 0-based origin of the footprint: the centre of coarse ca0 is fine
+    // 2 ca0 + 1, its lower neighbour 2 ca0
+    const int fa0 = 2 * ca0, fb0 = 2 * cb0, fz0 = 2 * cc0;
+    for (int i = threadIdx.x; i < RR_XW * RR_XH * RR_XD; i += RR_THREADS) {
+        const int la = i % RR_XW, lb = (i / RR_XW) % RR_XH, lc = i / (RR_XW * RR_XH);
+        const int ga = fa0 - 1 + la, gb = fb0 - 1 + lb, gz = fz0 - 1 + lc;
+        T v = T(0);
+        if (ga >= 0 && ga < gf.N0 && gb >= 0 && gb < gf.N1 && gz >= 0 && gz < gf.N2) v = x[gf.pad(ga, gb, gz)];
+        xs[i] = v;
     }
-    int foff[RR_NF], fsi[RR_NF], fx[RR_NF];
-    bool fok[RR_NF];
-#pragma unroll
-    for (int j = 0; j < RR_NF; ++j) {
-        const int i = threadIdx.x + j * RR_THREADS;
-        const int la = i % RR_FW, lb = i / RR_FW;
-        const int ga = fa0 + la, gb = fb0 + lb;
-        fok[j] = i < RR_FW * RR_FH && ga < gf.N0 && gb < gf.N1;
-        foff[j] = (gb + 1) * sy + (ga + 1);
-        fsi[j] = i < RR_FW * RR_FH ? i : -1;
-        fx[j] = (lb + 1) * RR_XW + (la + 1);  // centre in the x tile
-    }
-    T xr[RR_NX], fr[RR_NF];
-    auto fetch_x = [&](int p) {
-        const bool pin = p >= 0 && p < gf.N2;
-        const T *base = x + (i64)(p + 1) * gf.sz;
-#pragma unroll
-        for (int j = 0; j < RR_NX; ++j) xr[j] = (pin && xok[j]) ? base[xoff[j]] : T(0);
-    };
-    auto fetch_f = [&](int p) {
-        const bool pin = p >= 0 && p < gf.N2;
-        const T *base = f + (i64)(p + 1) * gf.sz;
-#pragma unroll
-        for (int j = 0; j < RR_NF; ++j) fr[j] = (pin && fok[j]) ? base[foff[j]] : T(0);
-    };
-    auto commit_x = [&](T *dst) {
-#pragma unroll
-        for (int j = 0; j < RR_NX; ++j)
-            if (xsi[j] >= 0) dst[xsi[j]] = xr[j];
-    };
-    // coarse plane cc needs fine residual planes 2cc, 2cc+1, 2cc+2
-    const int p_lo = 2 * cc0, p_hi = 2 * (cc1 - 1) + 2;
-    T *Xm = xs[0], *X0 = xs[1], *Xp = xs[2], *Xn = xs[3];
-    T *Rm = rs[0], *R0 = rs[1], *Rp = rs[2];
-    fetch_x(p_lo - 1);
-    commit_x(Xm);
-    fetch_x(p_lo);
-    commit_x(X0);
-    fetch_x(p_lo + 1);
-    commit_x(Xp);
-    fetch_x(p_lo + 2);
-    fetch_f(p_lo);
     __syncthreads();
-    for (int p = p_lo; p <= p_hi; ++p) {
-        // fine residual of plane p on the footprint (ring slot Rp)
-        const bool pin = p >= 0 && p < gf.N2;
+    for (int i = threadIdx.x; i < RR_FW * RR_FH * RR_FD; i += RR_THREADS) {
+        const int la = i % RR_FW, lb = (i / RR_FW) % RR_FH, lc = i / (RR_FW * RR_FH);
+        const int ga = fa0 + la, gb = fb0 + lb, gz = fz0 + lc;
+        T r = T(0);
+        if (ga < gf.N0 && gb < gf.N1 && gz < gf.N2) {
+            const int q = ((lc + 1) * RR_XH + (lb + 1)) * RR_XW + (la + 1);
+            constexpr int SY = RR_XW, SZ = RR_XW * RR_XH;
+            T res;
+            if (NPT == 7) {
+                res = s.w[4] * xs[q - SZ] + s.w[10] * xs[q - SY] + s.w[12] * xs[q - 1] + s.w[13] * xs[q] +
+                      s.w[14] * xs[q + 1] + s.w[16] * xs[q + SY] + s.w[22] * xs[q + SZ];
+            } else {
+                res = T(0);
 #pragma unroll
-        for (int j = 0; j < RR_NF; ++j) {
-            if (fsi[j] < 0) continue;
-            T r = T(0);
-            if (pin && fok[j]) {
-                const int q = fx[j];
-                T res;
-                if (NPT == 7) {
-                    res = s.w[4] * Xm[q] + s.w[10] * X0[q - RR_XW] + s.w[12] * X0[q - 1] + s.w[13] * X0[q] +
-                          s.w[14] * X0[q + 1] + s.w[16] * X0[q + RR_XW] + s.w[22] * Xp[q];
-                } else {
-                    res = T(0);
-                    const T *Pl[3] = {Xm, X0, Xp};
+                for (int dz = -1; dz <= 1; ++dz)
 #pragma unroll
-                    for (int dz = 0; dz < 3; ++dz)
+                    for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
-                        for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-                            for (int dx = -1; dx <= 1; ++dx)
-                                res += s.w[dz * 9 + (dy + 1) * 3 + (dx + 1)] * Pl[dz][q + dy * RR_XW + dx];
-                }
-                r = fr[j] - res;
+                        for (int dx = -1; dx <= 1; ++dx)
+                            res += s.w[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)] * xs[q + dz * SZ + dy * SY + dx];
             }
-            Rp[fsi[j]] = r;
+            r = f[gf.pad(ga, gb, gz)] - res;
         }
-        __syncthreads();
-        if (p >= p_lo + 2 && ((p - p_lo) & 1) == 0) {  // coarse plane (p - 2) / 2 from Rm, R0, Rp
-            const int cc = (p - 2) / 2;
-            T *out = fc + (i64)(cc + 1) * gc.sz;
-            const T *Rl[3] = {Rm, R0, Rp};
-            for (int i = threadIdx.x; i < RR_TX * RR_TY; i += RR_THREADS) {
-                const int la = i % RR_TX, lb = i / RR_TX;
-                const int ca = ca0 + la, cb = cb0 + lb;
-                if (ca >= gc.N0 || cb >= gc.N1) continue;
-                T acc = T(0);
-#pragma unroll
-                for (int az = 0; az < 3; ++az)
-#pragma unroll
-                    for (int ay = 0; ay < 3; ++ay)
-#pragma unroll
-                        for (int ax = 0; ax < 3; ++ax) {
-                            const T wr = T((ax == 1 ? 1.0 : 0.5) * (ay == 1 ? 1.0 : 0.5) * (az == 1 ? 1.0 : 0.5));
-                            acc += wr * Rl[az][(2 * lb + ay) * RR_FW + 2 * la + ax];
-                        }
-                out[(cb + 1) * (int)gc.sy + ca + 1] = acc;
-            }
-        }
-        // x plane p+2 into the free slot, x plane p+3 and f plane p+1 into registers
-        commit_x(Xn);
-        fetch_x(p + 3);
-        fetch_f(p + 1);
-        __syncthreads();
-        T *t = Xm;
-        Xm = X0;
-        X0 = Xp;
-        Xp = Xn;
-        Xn = t;
-        T *u = Rm;
-        Rm = R0;
-        R0 = Rp;
-        Rp = u;
+        rs[i] = r;
     }
+    __syncthreads();
+    const int la = threadIdx.x % RR_TX, lb = (threadIdx.x / RR_TX) % RR_TY, lc = threadIdx.x / (RR_TX * RR_TY);
+    const int ca = ca0 + la, cb = cb0 + lb, cc = cc0 + lc;
+    if (ca >= gc.N0 || cb >= gc.N1 || cc >= gc.N2) return;
+    T acc = T(0);
+#pragma unroll
+    for (int az = 0; az < 3; ++az)
+#pragma unroll
+        for (int ay = 0; ay < 3; ++ay)
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                const T wr = T((ax == 1 ? 1.0 : 0.5) * (ay == 1 ? 1.0 : 0.5) * (az == 1 ? 1.0 : 0.5));
+                acc += wr * rs[((2 * lc + az) * RR_FH + (2 * lb + ay)) * RR_FW + 2 * la + ax];
+            }
+    fc[gc.pad(ca, cb, cc)] = acc;
 }
 
 // dst[row] += sign * sum_e B_e y_{col_e} / Sigma_{col_e} over the rows of B
@@ -819,7 +778,10 @@ __global__ void __launch_bounds__(256) k_chol_gemv_lower(const T *__restrict__ f
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const i64 warps = (i64)gridDim.x * (blockDim.x >> 5);
-    for (i64 i = (i64)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+    // warp w owns rows w and n-1-w (together n+1 entries): balanced work
+    for (i64 ii = (i64)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ii < n; ii += warps) {
+        const i64 half = ii >> 1;
+        const i64 i = (ii & 1) ? n - 1 - half : half;
         const double *row = Linv + i * n;
         double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
         i64 k = lane;
@@ -855,7 +817,9 @@ __global__ void __launch_bounds__(256) k_chol_gemv_upper(const double *__restric
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const i64 warps = (i64)gridDim.x * (blockDim.x >> 5);
-    for (i64 j = (i64)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < n; j += warps) {
+    for (i64 jj = (i64)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); jj < n; jj += warps) {
+        const i64 half = jj >> 1;
+        const i64 j = (jj & 1) ? n - 1 - half : half;
         const double *row = LinvT + j * n;
         double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
         i64 k = j + lane;
