@@ -146,9 +146,12 @@ def time_chain(M, torch, op, f, obs, precision, steps, warmup, iact_extra, dist,
 
 
 def sweep_roofline(M, torch, s, precision, peak):
-    """Fine-level red-black SOR sweep (k_sweep_rb: both colours in one
-    launch, Philox noise, no low-rank update) timed alone on the sampler's
-    stream; algorithmic bytes 3 n s (read x, read f, write x)."""
+    """Fine-level red-black SOR colour pass (``k_sweep_rb_vec`` in FP32,
+    ``k_sweep_rb_pass`` in FP64; Philox noise, no low-rank update) timed on
+    the sampler's stream.  One sweep is two launches, one per colour; the
+    algorithmic bytes of one launch are 2 n s: every x value is read as a
+    neighbour or centre, and f is read and x written at the n/2 points of
+    the colour."""
     n = s.level_size(0)
     sz = 4 if precision == M.FP32_MIXED else 8
     s.sweep_device(0, nrepeat=5, with_lowrank=False)
@@ -160,8 +163,8 @@ def sweep_roofline(M, torch, s, precision, peak):
     s.sweep_device(0, nrepeat=rep, with_lowrank=False)
     e1.record(st)
     s.synchronize()
-    t = e0.elapsed_time(e1) / 1e3 / rep    # seconds per sweep launch
-    bytes_per_launch = 3 * n * sz          # read x, read f, write x
+    t = e0.elapsed_time(e1) / 1e3 / (2 * rep)   # seconds per colour-pass launch
+    bytes_per_launch = 2 * n * sz
     achieved = bytes_per_launch / t / 1e9
     return achieved, bytes_per_launch, t
 
@@ -315,6 +318,26 @@ def batch_study(nchain, steps, warmup=5, seed=3):
             "iact_p90": float(np.percentile(taus, 90)) if taus else None, "iact_window": 20, "steps": steps}
 
 
+def profile_steps(nsteps, warmup, precision):
+    """The benchmark chain for a profiler: warm-up steps, then `nsteps` steps
+    inside the NVTX range "timed"."""
+    import torch
+    import multigridmc_gb300 as M
+    op, f, _, _, _ = problem()
+    prec = M.FP32_MIXED if precision == "fp32" else M.FP64
+    s = M.MultigridMCSampler(op, M.MultigridParameters(nlevel=NLEVEL), ordering=M.MULTICOLOUR, precision=prec,
+                             noise=M.PHILOX, seed=1)
+    s.fix_rhs(f)
+    s.step(warmup)
+    s.synchronize()
+    torch.cuda.nvtx.range_push("timed")
+    s.step(nsteps)
+    s.synchronize()
+    torch.cuda.nvtx.range_pop()
+    print(f"profiled {nsteps} steps, {s.launches_per_step} launches per step", flush=True)
+    s.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -329,7 +352,14 @@ def main():
                     help="run the coupled FP32/FP64 covariance comparison instead of the benchmark")
     ap.add_argument("--batch-chains", type=int, default=0, metavar="N",
                     help="run the batched-chains study (N chains of mixed sizes) instead of the benchmark")
+    ap.add_argument("--profile-steps", type=int, default=0, metavar="K",
+                    help="profiling mode: K steps of the benchmark chain inside an NVTX range 'timed' "
+                         "(after --warmup steps), for ncu --nvtx-include timed/; prints no JSON")
+    ap.add_argument("--profile-precision", default="fp32", choices=["fp32", "fp64"])
     args = ap.parse_args()
+    if args.profile_steps > 0:
+        profile_steps(args.profile_steps, max(3, args.warmup), args.profile_precision)
+        return
     if args.batch_chains > 0:
         print(json.dumps({"batch_study": batch_study(args.batch_chains, args.steps)}), flush=True)
         return
@@ -437,7 +467,7 @@ def main():
         "gpu_launches": int(launches * args.steps),
         "launches_per_step": int(launches),
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                     "traffic": None, "kernel": "k_sweep_rb<float> (fine-level red-black SOR sweep, both colours, Philox noise)",
+                     "traffic": None, "kernel": "k_sweep_rb_vec<float> (one colour pass of the fine-level red-black SOR sweep, Philox noise)",
                      "algorithmic_bytes_per_launch": bpl, "launch_s": tl, "peak_kind": peak_kind},
         "cpu_baseline": cpu,
     }

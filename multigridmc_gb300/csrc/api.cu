@@ -80,7 +80,7 @@ struct Level {
     double *Bval = nullptr;
     RowCsr Br;          // B by rows (double values)
     RowCsr C[2];        // C = M^{-1} B, forward / backward (T values)
-    double *Sinv[2] = {nullptr, nullptr}, *G[2] = {nullptr, nullptr};
+    double *Sinv[2] = {nullptr, nullptr};
     double *y = nullptr, *z = nullptr, *part = nullptr;
     float *zf = nullptr, *Bvalf = nullptr;
     unsigned *counter = nullptr;
@@ -94,7 +94,7 @@ struct Sampler {
     int noise_mode = NOISE_PHILOX;
     std::vector<Level> L;
     std::vector<double> Sigma;
-    double *d_sigma_inv = nullptr, *d_sinv_sqrt = nullptr;
+    double *d_sigma_inv = nullptr, *d_sigma_sqrt = nullptr;
     // coarse Cholesky
     bool chol = false;
     double *dL = nullptr, *dLinv = nullptr, *dLinvT = nullptr, *dgv = nullptr;
@@ -286,13 +286,12 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     lr.Bvalf = lv.Bvalf;
     lr.zf = lv.zf;
     lr.Sinv = lv.Sinv[dir];
-    lr.G = lv.G[dir];
-    lr.sinv_sqrt = S.d_sinv_sqrt;
+    lr.sigma_sqrt = S.d_sigma_sqrt;
     lr.y = lv.y;
     lr.z = lv.z;
     lr.part = lv.part;
     lr.counter = lv.counter;
-    size_t smem = 3 * sizeof(double) * S.m;
+    size_t smem = sizeof(double) * S.m;
     dim3 grid(S.m, lv.bt_split);
     if (noise == NOISE_NONE)
         k_bt_x_z<T, NOISE_NONE, true><<<grid, 256, smem, S.stream>>>(x, lr, nz);
@@ -588,7 +587,7 @@ void Sampler::build_lowrank(int lev) {
     std::vector<double> yh(m);
     for (int dir = 0; dir < 2; ++dir) {
         std::vector<std::tuple<i64, int, double>> trip;
-        std::vector<double> Sh((size_t)m * m), Gh((size_t)m * m);
+        std::vector<double> Sh((size_t)m * m);
         for (int j = 0; j < m; ++j) {
             CK(cudaMemsetAsync(xs, 0, geo.nalloc * sizeof(double), stream));
             CK(cudaMemsetAsync(fs, 0, geo.nalloc * sizeof(double), stream));
@@ -622,10 +621,7 @@ void Sampler::build_lowrank(int lev) {
                 CK(cudaMemcpy(vv.data(), nzv, hc * sizeof(double), cudaMemcpyDeviceToHost));
             }
             for (unsigned long long e = 0; e < hc; ++e) trip.emplace_back(ii[e], j, vv[e]);
-            for (int a = 0; a < m; ++a) {
-                Gh[(size_t)a * m + j] = yh[a];
-                Sh[(size_t)a * m + j] = yh[a] + (a == j ? Sigma[a] : 0.0);
-            }
+            for (int a = 0; a < m; ++a) Sh[(size_t)a * m + j] = yh[a] + (a == j ? Sigma[a] : 0.0);
         }
         std::sort(trip.begin(), trip.end());
         std::vector<i64> rows, ptr{0};
@@ -652,7 +648,6 @@ void Sampler::build_lowrank(int lev) {
             C.val = upload(val);
         }
         lv.Sinv[dir] = upload(small_inverse(Sh, m));
-        lv.G[dir] = upload(Gh);
     }
     CK(cudaStreamSynchronize(stream));
 }
@@ -776,10 +771,10 @@ void Sampler::build(const mgmc_operator_desc &op) {
         std::vector<double> si(m), ss(m);
         for (int j = 0; j < m; ++j) {
             si[j] = 1.0 / Sigma[j];
-            ss[j] = std::sqrt(1.0 / Sigma[j]);  // Sigma^{-1/2} (sor_sampler.cc:29-33)
+            ss[j] = std::sqrt(Sigma[j]);  // Sigma^{1/2}: scale of the low-rank noise term Sigma w
         }
         d_sigma_inv = upload(si);
-        d_sinv_sqrt = upload(ss);
+        d_sigma_sqrt = upload(ss);
         for (size_t lev = 0; lev < L.size(); ++lev) build_lowrank((int)lev);
     }
     if (chol) build_coarse();

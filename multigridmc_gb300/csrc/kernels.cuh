@@ -338,9 +338,8 @@ struct LowRankArg {
     const i64 *Bptr;    // m+1, CSC of B (padded indices)
     const i64 *Bidx;
     const double *Bval;
-    const double *Sinv; // m x m, (Sigma + B^T M^{-1} B)^{-1}
-    const double *G;    // m x m, B^T M^{-1} B
-    const double *sinv_sqrt; // Sigma^{-1/2}
+    const double *Sinv; // m x m, S^{-1} = (Sigma + B^T M^{-1} B)^{-1}
+    const double *sigma_sqrt; // Sigma^{1/2}
     double *y;          // m scratch: B^T x
     double *z;          // m scratch: coefficients of C
     float *zf;          // the same coefficients rounded to FP32 (FP32 chain)
@@ -349,13 +348,31 @@ struct LowRankArg {
     unsigned *counter;  // block-completion counter (self-resetting)
 };
 
+// Warp sums of RW per-lane row partials; lane 0 writes rows
+// base + warp + NWARP r of z (and of its FP32 copy).
+template <int RW, int NWARP>
+__device__ __forceinline__ void store_rows(double (&t)[RW], const LowRankArg &lr, int m, int warp, int lane, int base) {
+#pragma unroll
+    for (int r = 0; r < RW; ++r) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t[r] += __shfl_xor_sync(0xffffffffu, t[r], o);
+        const int k = base + warp + NWARP * r;
+        if (lane == 0 && k < m) {
+            lr.z[k] = t[r];
+            if (lr.zf) lr.zf[k] = (float)t[r];
+        }
+    }
+}
+
 // y_j = sum_i B_ij x_i with gridDim.y blocks per column j (partial sums in
 // `part`, combined in a fixed order by the last block to finish, so the
 // result does not depend on block timing).  With SOLVE the same block then
-// forms
-//   w = Sigma^{-1/2} xi',  z = w - S^{-1} (y + G w)
-// (with_noise == 0: z = -S^{-1} y, the smoother's correction
-// x -= Bbar B^T x of sor_smoother.cc:47-51, Bbar = C S^{-1}).
+// forms the coefficients z of the correction x += C z,
+//   z = w - S^{-1} (y + G w) = S^{-1} (Sigma w - y) = S^{-1} (Sigma^{1/2} xi' - y)
+// with w = Sigma^{-1/2} xi' the low-rank noise of sor_sampler.cc:29-33,
+// G = B^T C and S = Sigma + G (so S - G = Sigma and a single m x m product
+// remains); with_noise == 0 gives z = -S^{-1} y, the smoother's correction
+// x -= Bbar B^T x of sor_smoother.cc:47-51, Bbar = C S^{-1}.
 template <typename T, int NOISE, bool SOLVE>
 __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRankArg lr, NoiseArgs nz) {
     __shared__ double sh[32];
@@ -383,67 +400,100 @@ __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRank
     if (!last) return;
     __threadfence();
     const int m = lr.m;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    // y_k: warp per column, lanes over the P partial sums
-    for (int k = warp; k < m; k += nwarp) {
-        double t = 0.0;
-        for (int q = lane; q < P; q += 32) t += ((volatile double *)lr.part)[k * P + q];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int NWARP = 8, RW = 8, QC = 4;  // rows per warp and 32-column chunks per lane in one batch
+    extern __shared__ double dyn[];
+    double *u = dyn;
+    // Rows warp + NWARP r (r < RW) of S^{-1}, columns lane + 32 c (c < QC):
+    // for m <= 64 the whole matrix is loaded here, before the partial sums
+    // are combined, so that every load of the block is in flight at once.
+    const bool onebatch = SOLVE && m <= NWARP * RW && m <= 32 * QC;
+    double a[RW][QC];
+    if (onebatch) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) lr.y[k] = t;
+        for (int r = 0; r < RW; ++r)
+#pragma unroll
+            for (int c = 0; c < QC; ++c) {
+                const int k = warp + NWARP * r, q = lane + 32 * c;
+                a[r][c] = (k < m && q < m) ? __ldg(lr.Sinv + (i64)k * m + q) : 0.0;
+            }
+    }
+    // y_k: warp per column, lanes over the P partial sums (P <= 32: one load
+    // per lane), eight columns in flight per warp; with SOLVE also
+    // u_k = Sigma_k^{1/2} xi'_k - y_k
+    for (int k0 = warp; k0 < m; k0 += 8 * NWARP) {
+        double t[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int k = k0 + NWARP * r;
+            t[r] = 0.0;
+            if (k < m)
+                for (int q = lane; q < P; q += 32) t[r] += __ldcg(lr.part + (i64)k * P + q);
+        }
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t[r] += __shfl_xor_sync(0xffffffffu, t[r], o);
+        }
+        if (lane < 8) {
+            const int k = k0 + NWARP * lane;
+            double tk = t[0];
+#pragma unroll
+            for (int r = 1; r < 8; ++r) tk = lane == r ? t[r] : tk;
+            if (k < m) {
+                lr.y[k] = tk;
+                if (SOLVE) {
+                    double xi = 0.0;
+                    if (NOISE == NOISE_PHILOX) {
+                        float4 rn = normals4(
+                            philox4x32_10(noise_ctr(nz, (unsigned)(k >> 2), PURPOSE_LOWRANK, 0), noise_key(nz)));
+                        xi = (double)pick(rn, k & 3);
+                    }
+                    if (NOISE == NOISE_INJECTED) xi = nz.buf[k];
+                    u[k] = lr.sigma_sqrt[k] * xi - tk;
+                }
+            }
+        }
     }
     if (threadIdx.x == 0) *lr.counter = 0u;
     if (!SOLVE) return;
-    extern __shared__ double dyn[];
-    double *w = dyn, *v = dyn + m, *ys = dyn + 2 * m;
     __syncthreads();
-    for (int k = threadIdx.x; k < m; k += blockDim.x) {
-        double xi = 0.0;
-        if (NOISE == NOISE_PHILOX) {
-            float4 r = normals4(philox4x32_10(noise_ctr(nz, (unsigned)(k >> 2), PURPOSE_LOWRANK, 0), noise_key(nz)));
-            xi = (double)pick(r, k & 3);
-        }
-        if (NOISE == NOISE_INJECTED) xi = nz.buf[k];
-        w[k] = lr.sinv_sqrt[k] * xi;
-        ys[k] = lr.y[k];
-    }
-    __syncthreads();
-    // m x m products, one warp per row, four rows in flight per warp
-    for (int k0 = warp; k0 < m; k0 += 4 * nwarp) {
-        double t[4] = {0.0, 0.0, 0.0, 0.0};
+    // z = S^{-1} u: warp per row, RW rows per warp in flight
+    if (onebatch) {
+        double t[RW];
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int k = k0 + r * nwarp;
-            if (k < m)
-                for (int q = lane; q < m; q += 32) t[r] += lr.G[(i64)k * m + q] * w[q];
-        }
+        for (int r = 0; r < RW; ++r) {
+            t[r] = 0.0;
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t[r] += __shfl_xor_sync(0xffffffffu, t[r], o);
-            const int k = k0 + r * nwarp;
-            if (lane == 0 && k < m) v[k] = ys[k] + t[r];
-        }
-    }
-    __syncthreads();
-    for (int k0 = warp; k0 < m; k0 += 4 * nwarp) {
-        double t[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int k = k0 + r * nwarp;
-            if (k < m)
-                for (int q = lane; q < m; q += 32) t[r] += lr.Sinv[(i64)k * m + q] * v[q];
-        }
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t[r] += __shfl_xor_sync(0xffffffffu, t[r], o);
-            const int k = k0 + r * nwarp;
-            if (lane == 0 && k < m) {
-                const double zk = w[k] - t[r];
-                lr.z[k] = zk;
-                if (lr.zf) lr.zf[k] = (float)zk;
+            for (int c = 0; c < QC; ++c) {
+                const int q = lane + 32 * c;
+                if (q < m) t[r] += a[r][c] * u[q];
             }
+        }
+        store_rows<RW, NWARP>(t, lr, m, warp, lane, 0);
+    } else {
+        for (int k0 = warp; k0 < m; k0 += RW * NWARP) {
+            double t[RW];
+#pragma unroll
+            for (int r = 0; r < RW; ++r) t[r] = 0.0;
+            for (int q0 = 0; q0 < m; q0 += 32 * QC) {
+                double b[RW][QC];
+#pragma unroll
+                for (int r = 0; r < RW; ++r)
+#pragma unroll
+                    for (int c = 0; c < QC; ++c) {
+                        const int k = k0 + NWARP * r, q = q0 + lane + 32 * c;
+                        b[r][c] = (k < m && q < m) ? __ldg(lr.Sinv + (i64)k * m + q) : 0.0;
+                    }
+#pragma unroll
+                for (int r = 0; r < RW; ++r)
+#pragma unroll
+                    for (int c = 0; c < QC; ++c) {
+                        const int q = q0 + lane + 32 * c;
+                        if (q < m) t[r] += b[r][c] * u[q];
+                    }
+            }
+            store_rows<RW, NWARP>(t, lr, m, warp, lane, k0 - warp);
         }
     }
 }
