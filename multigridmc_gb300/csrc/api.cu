@@ -9,12 +9,14 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <map>
 #include <string>
 #include <tuple>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "../../include/mgmc_gb300.h"
@@ -91,13 +93,16 @@ struct Sampler {
     mgmc_sampler_params P;
     int dim = 3, m = 0;
     bool fp32 = false, exact = false;
+    bool pdl = true;  // programmatic dependent launch between step kernels (MGMC_NO_PDL=1 turns it off)
     int noise_mode = NOISE_PHILOX;
     std::vector<Level> L;
     std::vector<double> Sigma;
     double *d_sigma_inv = nullptr, *d_sigma_sqrt = nullptr;
     // coarse Cholesky
     bool chol = false;
-    double *dL = nullptr, *dLinv = nullptr, *dLinvT = nullptr, *dgv = nullptr;
+    double *dL = nullptr, *dgv = nullptr;
+    void *dLinv = nullptr, *dLinvT = nullptr;  // L^{-1}, L^{-T}: double (FP64 chain) or float (FP32 chain)
+    int chol_ld = 0;                           // their leading dimension (16-byte rows)
     size_t chol_smem = 0;
     // bookkeeping
     cudaStream_t stream = nullptr;
@@ -192,6 +197,28 @@ NoiseArgs Sampler::noise_args(int lev, i64 count) {
     return nz;
 }
 
+// Launch with programmatic stream serialization (pdl): the kernel's CTAs
+// may be scheduled while its predecessor on the stream drains; every step
+// kernel starts with griddepcontrol.launch_dependents / griddepcontrol.wait
+// (pdl_begin), so no kernel touches memory before its predecessor has
+// completed and flushed.  This hides the launch latency between the short
+// dependent kernels of a multigrid step.
+template <typename... KArgs, typename... Args>
+static void plaunch(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                    Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    CK(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
+}
+
 // ----------------------------------------------------------- sweep launch
 template <typename T, bool EXACT, int NOISE>
 static void launch_colour_passes(Sampler &S, const Level &lv, bool forward, T *x, const T *f, const StencilArg<T> &s,
@@ -202,7 +229,7 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
     StencilArg<T> s = stencil_arg<T>(lv, S.P.omega);
     if (S.P.ordering == MGMC_ORDER_LEXICOGRAPHIC) {
         int hb = lv.ncol == 2 ? 1 : 2, hc = lv.ncol == 2 ? 1 : 4;
-        k_sweep_wavefront<T, NPT, EXACT, NOISE><<<1, 1024, 0, S.stream>>>(x, f, lv.g, s, forward ? 1 : 0, hb, hc, nz);
+        plaunch(S.pdl, k_sweep_wavefront<T, NPT, EXACT, NOISE>, 1, 1024, 0, S.stream, x, f, lv.g, s, forward ? 1 : 0, hb, hc, nz);
         S.launches++;
         return;
     }
@@ -215,14 +242,14 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
             if constexpr (std::is_same<T, float>::value) {
                 if (vec) {
                     dim3 grid(((lv.g.N0 + 8) / 8 + RBP_THREADS - 1) / RBP_THREADS, lv.g.N1, lv.g.N2);
-                    k_sweep_rb_vec<NOISE><<<grid, RBP_THREADS, 0, S.stream>>>(x, f, lv.g, s, colour, pass, nz);
+                    plaunch(S.pdl, k_sweep_rb_vec<NOISE>, grid, RBP_THREADS, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
                     S.launches++;
                     continue;
                 }
             }
             {
                 dim3 grid((lv.g.N0 + 2 * RBP_THREADS - 1) / (2 * RBP_THREADS), lv.g.N1, lv.g.N2);
-                k_sweep_rb_pass<T, EXACT, NOISE><<<grid, RBP_THREADS, 0, S.stream>>>(x, f, lv.g, s, colour, pass, nz);
+                plaunch(S.pdl, k_sweep_rb_pass<T, EXACT, NOISE>, grid, RBP_THREADS, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
             }
             S.launches++;
         }
@@ -241,7 +268,7 @@ static void launch_colour_passes(Sampler &S, const Level &lv, bool forward, T *x
         const int na = (lv.g.N0 - pa + 1) / 2, nb = (lv.g.N1 - pb + 1) / 2, nc = (lv.g.N2 - pc + 1) / 2;
         if (na <= 0 || nb <= 0 || nc <= 0) continue;
         dim3 grid((na + RBP_THREADS - 1) / RBP_THREADS, nb, nc);
-        k_sweep_c27_pass<T, EXACT, NOISE><<<grid, RBP_THREADS, 0, S.stream>>>(x, f, lv.g, s, colour, nz);
+        plaunch(S.pdl, k_sweep_c27_pass<T, EXACT, NOISE>, grid, RBP_THREADS, 0, S.stream, x, f, lv.g, s, colour, nz);
         S.launches++;
     }
 }
@@ -294,18 +321,18 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     size_t smem = sizeof(double) * S.m;
     dim3 grid(S.m, lv.bt_split);
     if (noise == NOISE_NONE)
-        k_bt_x_z<T, NOISE_NONE, true><<<grid, 256, smem, S.stream>>>(x, lr, nz);
+        plaunch(S.pdl, k_bt_x_z<T, NOISE_NONE, true>, grid, 256, smem, S.stream, x, lr, nz);
     else if (noise == NOISE_PHILOX)
-        k_bt_x_z<T, NOISE_PHILOX, true><<<grid, 256, smem, S.stream>>>(x, lr, nz);
+        plaunch(S.pdl, k_bt_x_z<T, NOISE_PHILOX, true>, grid, 256, smem, S.stream, x, lr, nz);
     else
-        k_bt_x_z<T, NOISE_INJECTED, true><<<grid, 256, smem, S.stream>>>(x, lr, nz);
+        plaunch(S.pdl, k_bt_x_z<T, NOISE_INJECTED, true>, grid, 256, smem, S.stream, x, lr, nz);
     const RowCsr &C = lv.C[dir];
     if (C.nrows > 0) {
         if (sizeof(T) == 4)
-            k_lr_scatter_f<T><<<nblk(C.nrows, 256), 256, 0, S.stream>>>(x, C.nrows, C.rows, C.ptr, C.col, (const T *)C.val,
+            plaunch(S.pdl, k_lr_scatter_f<T>, nblk(C.nrows, 256), 256, 0, S.stream, x, C.nrows, C.rows, C.ptr, C.col, (const T *)C.val,
                                                                          lv.zf);
         else
-            k_lr_scatter<T><<<nblk(C.nrows, 256), 256, 0, S.stream>>>(x, C.nrows, C.rows, C.ptr, C.col, (const T *)C.val, lv.z);
+            plaunch(S.pdl, k_lr_scatter<T>, nblk(C.nrows, 256), 256, 0, S.stream, x, C.nrows, C.rows, C.ptr, C.col, (const T *)C.val, lv.z);
     }
     S.launches += 2;
 }
@@ -341,16 +368,16 @@ static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void
         dim3 grid((lc.g.N0 + RR_TX - 1) / RR_TX, (lc.g.N1 + RR_TY - 1) / RR_TY, (lc.g.N2 + RR_TZ - 1) / RR_TZ);
         const size_t sm = rr_smem_bytes<T>();
         if (lv.npt == 7)
-            k_resid_restrict_tiled<T, 7><<<grid, RR_THREADS, sm, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s);
+            plaunch(S.pdl, k_resid_restrict_tiled<T, 7>, grid, RR_THREADS, sm, S.stream, (const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s);
         else
-            k_resid_restrict_tiled<T, 27><<<grid, RR_THREADS, sm, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s);
+            plaunch(S.pdl, k_resid_restrict_tiled<T, 27>, grid, RR_THREADS, sm, S.stream, (const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s);
         S.launches++;
         return;
     }
     if (lv.npt == 7 && !zero_stencil)
-        k_resid_restrict<T, 7><<<nblk(nc, 256), 256, 0, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, S.dim);
+        plaunch(S.pdl, k_resid_restrict<T, 7>, nblk(nc, 256), 256, 0, S.stream, (const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, S.dim);
     else
-        k_resid_restrict<T, 27><<<nblk(nc, 256), 256, 0, S.stream>>>((const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, S.dim);
+        plaunch(S.pdl, k_resid_restrict<T, 27>, nblk(nc, 256), 256, 0, S.stream, (const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, S.dim);
     S.launches++;
 }
 
@@ -366,7 +393,7 @@ static void launch_bt_plain(Sampler &S, Level &lv, const void *x) {
     lr.part = lv.part;
     lr.counter = lv.counter;
     NoiseArgs nz{};
-    k_bt_x_z<T, NOISE_NONE, false><<<dim3(S.m, lv.bt_split), 256, 0, S.stream>>>((const T *)x, lr, nz);
+    plaunch(S.pdl, k_bt_x_z<T, NOISE_NONE, false>, dim3(S.m, lv.bt_split), 256, 0, S.stream, (const T *)x, lr, nz);
     S.launches++;
 }
 
@@ -374,7 +401,7 @@ template <typename T>
 static void launch_add_Bq(Sampler &S, Level &lv, void *dst, const double *y, double sign) {
     const RowCsr &B = lv.Br;
     if (B.nrows == 0) return;
-    k_add_Bq<T><<<nblk(B.nrows, 256), 256, 0, S.stream>>>((T *)dst, B.nrows, B.rows, B.ptr, B.col, (const double *)B.val, y,
+    plaunch(S.pdl, k_add_Bq<T>, nblk(B.nrows, 256), 256, 0, S.stream, (T *)dst, B.nrows, B.rows, B.ptr, B.col, (const double *)B.val, y,
                                                           S.d_sigma_inv, sign);
     S.launches++;
 }
@@ -402,22 +429,28 @@ void Sampler::prolong(int lev, double alpha, void *xc, void *x) {
     Level &lv = L[lev], &lc = L[lev + 1];
     dim3 grid((lc.g.N0 + 1 + 127) / 128, dim > 1 ? lc.g.N1 + 1 : 1, dim > 2 ? lc.g.N2 + 1 : 1);
     if (fp32)
-        k_prolong_add<float><<<grid, 128, 0, stream>>>((float *)x, (const float *)xc, lv.g, lc.g, (float)alpha, dim);
+        plaunch(pdl, k_prolong_add<float>, grid, 128, 0, stream, (float *)x, (const float *)xc, lv.g, lc.g, (float)alpha, dim);
     else
-        k_prolong_add<double><<<grid, 128, 0, stream>>>((double *)x, (const double *)xc, lv.g, lc.g, alpha, dim);
+        plaunch(pdl, k_prolong_add<double>, grid, 128, 0, stream, (double *)x, (const double *)xc, lv.g, lc.g, alpha, dim);
     launches++;
 }
 
 template <typename T, int NOISE>
 static void launch_chol(Sampler &S, Level &lv, const NoiseArgs &nz) {
     if (S.exact) {
-        k_chol_subst<T, NOISE><<<1, 1024, 0, S.stream>>>((const T *)lv.f, (T *)lv.x, lv.g, S.dL, S.dgv, nz);
+        plaunch(S.pdl, k_chol_subst<T, NOISE>, 1, 1024, 0, S.stream, (const T *)lv.f, (T *)lv.x, lv.g, S.dL, S.dgv, nz);
         S.launches++;
     } else {
+        // FP32 chain: FP32 factor products (the state itself is FP32);
+        // FP64 chain: FP64
+        typedef T MT;
         const i64 n = lv.geo.n;
-        unsigned blocks = (unsigned)std::min<i64>(4 * 152, (n + 7) / 8);
-        k_chol_gemv_lower<T, NOISE><<<blocks, 256, S.chol_smem, S.stream>>>((const T *)lv.f, lv.g, S.dLinv, S.dgv, nz);
-        k_chol_gemv_upper<T><<<blocks, 256, S.chol_smem, S.stream>>>(S.dgv, lv.g, S.dLinvT, (T *)lv.x);
+        unsigned blocks = (unsigned)((n + 7) / 8);
+        plaunch(S.pdl, k_chol_gemv_lower<T, MT, NOISE>, blocks, 256, S.chol_smem, S.stream, (const T *)lv.f, lv.g,
+                                                                                (const MT *)S.dLinv, S.chol_ld,
+                                                                                (MT *)S.dgv, nz);
+        plaunch(S.pdl, k_chol_gemv_upper<T, MT>, blocks, 256, S.chol_smem, S.stream, (const MT *)S.dgv, lv.g, (const MT *)S.dLinvT,
+                                                                         S.chol_ld, (T *)lv.x);
         S.launches += 2;
     }
 }
@@ -483,10 +516,10 @@ void Sampler::sample(int lev) {
 
 void Sampler::step_end() {
     if (fp32)
-        k_step_end<float><<<std::max(nprobe, 1), 256, 0, stream>>>((const float *)L[0].x, nprobe, d_bptr, d_bidx, d_bval, d_obs,
+        plaunch(pdl, k_step_end<float>, std::max(nprobe, 1), 256, 0, stream, (const float *)L[0].x, nprobe, d_bptr, d_bidx, d_bval, d_obs,
                                                                   obs_cap, d_obs_count, d_step, d_err, d_done);
     else
-        k_step_end<double><<<std::max(nprobe, 1), 256, 0, stream>>>((const double *)L[0].x, nprobe, d_bptr, d_bidx, d_bval,
+        plaunch(pdl, k_step_end<double>, std::max(nprobe, 1), 256, 0, stream, (const double *)L[0].x, nprobe, d_bptr, d_bidx, d_bval,
                                                                    d_obs, obs_cap, d_obs_count, d_step, d_err, d_done);
     launches++;
 }
@@ -664,18 +697,31 @@ void Sampler::build_coarse() {
         dL = upload(Q);
     } else {
         std::vector<double> T = inverse_factor_transposed(Q, n);  // (L^{-1})^T
-        std::vector<double> Li((size_t)n * n);
-        for (i64 i = 0; i < n; ++i)
-            for (i64 j = 0; j < n; ++j) Li[(size_t)i * n + j] = T[(size_t)j * n + i];
-        dLinvT = upload(T);
-        dLinv = upload(Li);
+        const size_t esz = fp32 ? sizeof(float) : sizeof(double);
+        const i64 ld = (i64)((n * esz + 15) / 16 * 16 / esz);
+        chol_ld = (int)ld;
+        chol_smem = (size_t)ld * esz;
+        auto put = [&](bool transpose) -> void * {
+            if (fp32) {
+                std::vector<float> M((size_t)n * ld, 0.0f);
+                for (i64 i = 0; i < n; ++i)
+                    for (i64 j = 0; j < n; ++j) M[(size_t)i * ld + j] = (float)(transpose ? T[(size_t)i * n + j] : T[(size_t)j * n + i]);
+                return upload(M);
+            }
+            std::vector<double> M((size_t)n * ld, 0.0);
+            for (i64 i = 0; i < n; ++i)
+                for (i64 j = 0; j < n; ++j) M[(size_t)i * ld + j] = transpose ? T[(size_t)i * n + j] : T[(size_t)j * n + i];
+            return upload(M);
+        };
+        dLinvT = put(true);
+        dLinv = put(false);
         if (chol_smem > 48 * 1024) {
-            CK(cudaFuncSetAttribute(k_chol_gemv_lower<float, NOISE_PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
-            CK(cudaFuncSetAttribute(k_chol_gemv_lower<double, NOISE_PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
-            CK(cudaFuncSetAttribute(k_chol_gemv_lower<float, NOISE_INJECTED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
-            CK(cudaFuncSetAttribute(k_chol_gemv_lower<double, NOISE_INJECTED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
-            CK(cudaFuncSetAttribute(k_chol_gemv_upper<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
-            CK(cudaFuncSetAttribute(k_chol_gemv_upper<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
+            CK(cudaFuncSetAttribute(k_chol_gemv_lower<float, float, NOISE_PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
+            CK(cudaFuncSetAttribute(k_chol_gemv_lower<double, double, NOISE_PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
+            CK(cudaFuncSetAttribute(k_chol_gemv_lower<float, float, NOISE_INJECTED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
+            CK(cudaFuncSetAttribute(k_chol_gemv_lower<double, double, NOISE_INJECTED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
+            CK(cudaFuncSetAttribute(k_chol_gemv_upper<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
+            CK(cudaFuncSetAttribute(k_chol_gemv_upper<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
         }
     }
 }
@@ -704,6 +750,10 @@ void Sampler::build(const mgmc_operator_desc &op) {
     chol = P.coarse_solver == MGMC_COARSE_CHOLESKY;
     m = op.m;
     CK(cudaSetDevice(P.device));
+    {
+        const char *e = std::getenv("MGMC_NO_PDL");
+        pdl = !(e && e[0] == '1');
+    }
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaFuncSetAttribute(k_resid_restrict_tiled<double, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)rr_smem_bytes<double>()));
@@ -1327,6 +1377,15 @@ mgmc_status mgmc_batch_create(int nchain, mgmc_sampler *const *samplers, mgmc_ba
     CK(cudaGraphCreate(&B->graph, 0));
     for (Sampler *S : B->chains) {
         CK(cudaStreamSynchronize(S->stream));
+        // a chain's step graph becomes a child graph: captured with plain
+        // (non-programmatic) dependencies
+        if (S->pdl) {
+            S->pdl = false;
+            if (S->gexec) cudaGraphExecDestroy(S->gexec);
+            if (S->graph) cudaGraphDestroy(S->graph);
+            S->gexec = nullptr;
+            S->graph = nullptr;
+        }
         ensure_graph(*S);
         cudaGraphNode_t node;
         CK(cudaGraphAddChildGraphNode(&node, B->graph, nullptr, 0, S->graph));

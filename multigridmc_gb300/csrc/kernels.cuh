@@ -27,6 +27,14 @@ namespace mgmc {
 typedef long long i64;
 typedef unsigned long long u64;
 
+// Programmatic dependent launch: let the next kernel on the stream be
+// scheduled now, then wait until the previous kernel has completed and its
+// writes are visible.  Without the launch attribute both are no-ops.
+__device__ __forceinline__ void pdl_begin() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // ------------------------------------------------------------- geometry
 struct Grid3 {
     int N0, N1, N2;  // interior vertices per direction
@@ -192,6 +200,7 @@ constexpr int RBP_THREADS = 128;
 template <typename T, bool EXACT, int NOISE>
 __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_pass(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
                                                                StencilArg<T> s, int colour, int reverse, NoiseArgs nz) {
+    pdl_begin();
     const int b = blockIdx.y;
     const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
     const int p = (colour + b + c) & 1;
@@ -211,6 +220,7 @@ template <int NOISE>
 __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict__ x, const float *__restrict__ f,
                                                               Grid3 g, StencilArg<float> s, int colour, int reverse,
                                                               NoiseArgs nz) {
+    pdl_begin();
     const int b = blockIdx.y;
     const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
     const int q = blockIdx.x * RBP_THREADS + threadIdx.x;
@@ -279,6 +289,7 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
 template <typename T, bool EXACT, int NOISE>
 __global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
                                                                 StencilArg<T> s, int colour, NoiseArgs nz) {
+    pdl_begin();
     const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
     const int a = 2 * (blockIdx.x * RBP_THREADS + threadIdx.x) + pa;
     const int b = 2 * blockIdx.y + pb, c = 2 * blockIdx.z + pc;
@@ -298,6 +309,7 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ 
 template <typename T, int NPT, bool EXACT, int NOISE>
 __global__ void __launch_bounds__(1024) k_sweep_wavefront(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
                                                            StencilArg<T> s, int forward, int hb, int hc, NoiseArgs nz) {
+    pdl_begin();
     const int tmax = (g.N0 - 1) + hb * (g.N1 - 1) + hc * (g.N2 - 1);
     const int npair = g.N1 * g.N2;
     for (int step = 0; step <= tmax; ++step) {
@@ -375,6 +387,7 @@ __device__ __forceinline__ void store_rows(double (&t)[RW], const LowRankArg &lr
 // x -= Bbar B^T x of sor_smoother.cc:47-51, Bbar = C S^{-1}.
 template <typename T, int NOISE, bool SOLVE>
 __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRankArg lr, NoiseArgs nz) {
+    pdl_begin();
     __shared__ double sh[32];
     __shared__ bool last;
     const int j = blockIdx.x, p = blockIdx.y, P = gridDim.y;
@@ -504,6 +517,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_lr_scatter_f(T *__restrict__ x, i64 nrows, const i64 *__restrict__ rows,
                                                        const i64 *__restrict__ ptr, const int *__restrict__ col,
                                                        const T *__restrict__ val, const float *__restrict__ z) {
+    pdl_begin();
     for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += (i64)gridDim.x * blockDim.x) {
         T acc = T(0);
         for (i64 e = ptr[r]; e < ptr[r + 1]; ++e) acc += val[e] * (T)z[col[e]];
@@ -516,6 +530,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_lr_scatter(T *__restrict__ x, i64 nrows, const i64 *__restrict__ rows,
                                                      const i64 *__restrict__ ptr, const int *__restrict__ col,
                                                      const T *__restrict__ val, const double *__restrict__ z) {
+    pdl_begin();
     for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += (i64)gridDim.x * blockDim.x) {
         T acc = T(0);
         for (i64 e = ptr[r]; e < ptr[r + 1]; ++e) acc += val[e] * (T)z[col[e]];
@@ -532,6 +547,7 @@ template <typename T, int NPT>
 __global__ void __launch_bounds__(256) k_resid_restrict(const T *__restrict__ x, const T *__restrict__ f,
                                                          T *__restrict__ fc, Grid3 gf, Grid3 gc, StencilArg<T> s,
                                                          int dim) {
+    pdl_begin();
     i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     i64 nc = (i64)gc.N0 * gc.N1 * gc.N2;
     if (t >= nc) return;
@@ -581,6 +597,7 @@ template <typename T, int NPT>
 __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tiled(const T *__restrict__ x, const T *__restrict__ f,
                                                                       T *__restrict__ fc, Grid3 gf, Grid3 gc,
                                                                       StencilArg<T> s) {
+    pdl_begin();
     extern __shared__ __align__(16) unsigned char rr_smem[];
     T *xs = reinterpret_cast<T *>(rr_smem);             // [RR_XD][RR_XH][RR_XW]
     T *rs = xs + RR_XW * RR_XH * RR_XD;                  // [RR_FD][RR_FH][RR_FW]
@@ -645,6 +662,7 @@ __global__ void __launch_bounds__(256) k_add_Bq(T *__restrict__ dst, i64 nrows, 
                                                  const i64 *__restrict__ ptr, const int *__restrict__ col,
                                                  const double *__restrict__ val, const double *__restrict__ y,
                                                  const double *__restrict__ sigma_inv, double sign) {
+    pdl_begin();
     for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += (i64)gridDim.x * blockDim.x) {
         double acc = 0.0;
         for (i64 e = ptr[r]; e < ptr[r + 1]; ++e) acc += val[e] * (y[col[e]] * sigma_inv[col[e]]);
@@ -659,6 +677,7 @@ __global__ void __launch_bounds__(256) k_add_Bq(T *__restrict__ dst, i64 nrows, 
 template <typename T>
 __global__ void __launch_bounds__(128) k_prolong_add(T *__restrict__ x, const T *__restrict__ xc, Grid3 gf, Grid3 gc,
                                                       T alpha, int dim) {
+    pdl_begin();
     // coarse cell (i, j, k), 0 <= i <= Nc0 etc., owns the fine vertices with
     // 1-based coordinates 2 i + {0, 1} (those inside the interior); its
     // corners are the coarse vertices i, i+1 (1-based, ghosts are zero)
@@ -722,6 +741,7 @@ __global__ void __launch_bounds__(128) k_prolong_add(T *__restrict__ x, const T 
 template <typename T>
 __global__ void __launch_bounds__(256) k_apply_stencil(const T *__restrict__ x, T *__restrict__ y, Grid3 g,
                                                         StencilArg<T> s) {
+    pdl_begin();
     i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     i64 n = (i64)g.N0 * g.N1 * g.N2;
     if (t >= n) return;
@@ -737,6 +757,7 @@ __global__ void __launch_bounds__(256) k_apply_stencil(const T *__restrict__ x, 
 // ---------------------------------------------------- layout conversion
 template <typename T>
 __global__ void k_unpack(const double *__restrict__ src, T *__restrict__ dst, Grid3 g) {
+    pdl_begin();
     i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     i64 n = (i64)g.N0 * g.N1 * g.N2;
     if (t >= n) return;
@@ -746,6 +767,7 @@ __global__ void k_unpack(const double *__restrict__ src, T *__restrict__ dst, Gr
 
 template <typename T>
 __global__ void k_pack(const T *__restrict__ src, double *__restrict__ dst, Grid3 g) {
+    pdl_begin();
     i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     i64 n = (i64)g.N0 * g.N1 * g.N2;
     if (t >= n) return;
@@ -755,6 +777,7 @@ __global__ void k_pack(const T *__restrict__ src, double *__restrict__ dst, Grid
 
 template <typename T>
 __global__ void k_zero_interior(T *__restrict__ x, Grid3 g) {
+    pdl_begin();
     i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     i64 n = (i64)g.N0 * g.N1 * g.N2;
     if (t >= n) return;
@@ -771,6 +794,7 @@ template <typename T, int NOISE>
 __global__ void __launch_bounds__(1024) k_chol_subst(const T *__restrict__ f, T *__restrict__ x, Grid3 g,
                                                       const double *__restrict__ L, double *__restrict__ gv,
                                                       NoiseArgs nz) {
+    pdl_begin();
     const i64 n = (i64)g.N0 * g.N1 * g.N2;
     for (i64 i = threadIdx.x; i < n; i += blockDim.x) {
         int a = (int)(i % g.N0), b = (int)((i / g.N0) % g.N1), c = (int)(i / ((i64)g.N0 * g.N1));
@@ -814,78 +838,106 @@ __global__ void __launch_bounds__(1024) k_chol_subst(const T *__restrict__ f, T 
     }
 }
 
-// Throughput form with the explicit inverse factor Linv = L^{-1}:
-// v = xi + Linv f (warp per row, row i has i+1 non-zeros) ...
-template <typename T, int NOISE>
-__global__ void __launch_bounds__(256) k_chol_gemv_lower(const T *__restrict__ f, Grid3 g, const double *__restrict__ Linv,
-                                                          double *__restrict__ v, NoiseArgs nz) {
-    extern __shared__ double fs[];
-    const i64 n = (i64)g.N0 * g.N1 * g.N2;
-    for (i64 i = threadIdx.x; i < n; i += blockDim.x) {
-        int a = (int)(i % g.N0), b = (int)((i / g.N0) % g.N1), c = (int)(i / ((i64)g.N0 * g.N1));
-        fs[i] = (double)f[g.pad(a, b, c)];
+// Throughput form with the explicit inverse factor Linv = L^{-1}, stored
+// row-major in the matrix type MT (double for the FP64 chain, float for the
+// FP32 chain) with a leading dimension ld that is a multiple of 16 bytes and
+// explicit zeros outside the triangle (and in columns n..ld-1), so that rows
+// are read in aligned 16-byte vectors and a vector that straddles the
+// diagonal multiplies zeros.  One warp per row; rows i and n-1-i go to
+// neighbouring warps, so that every CTA gets the same number of non-zeros.
+template <typename MT>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    typedef float4 type;
+    static constexpr int N = 4;
+    static __device__ __forceinline__ float dot(float4 a, const float *v) {
+        return a.x * v[0] + a.y * v[1] + a.z * v[2] + a.w * v[3];
+    }
+};
+template <>
+struct Vec16<double> {
+    typedef double2 type;
+    static constexpr int N = 2;
+    static __device__ __forceinline__ double dot(double2 a, const double *v) { return a.x * v[0] + a.y * v[1]; }
+};
+
+// sum over vectors q0..q1-1 of row . vs, lanes strided, four vectors in flight
+template <typename MT>
+__device__ __forceinline__ MT warp_row_dot(const MT *__restrict__ row, const MT *vs, int q0, int q1, int lane) {
+    typedef typename Vec16<MT>::type V;
+    constexpr int NV = Vec16<MT>::N;
+    const V *r = reinterpret_cast<const V *>(row);
+    MT a0 = MT(0), a1 = MT(0), a2 = MT(0), a3 = MT(0);
+    int q = q0 + lane;
+    for (; q + 96 < q1; q += 128) {
+        V v0 = __ldg(r + q), v1 = __ldg(r + q + 32), v2 = __ldg(r + q + 64), v3 = __ldg(r + q + 96);
+        a0 += Vec16<MT>::dot(v0, vs + NV * q);
+        a1 += Vec16<MT>::dot(v1, vs + NV * (q + 32));
+        a2 += Vec16<MT>::dot(v2, vs + NV * (q + 64));
+        a3 += Vec16<MT>::dot(v3, vs + NV * (q + 96));
+    }
+    for (; q < q1; q += 32) a0 += Vec16<MT>::dot(__ldg(r + q), vs + NV * q);
+    MT acc = (a0 + a1) + (a2 + a3);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    return acc;
+}
+
+// v = xi + Linv f (row i: vectors 0 .. i / NV)
+template <typename T, typename MT, int NOISE>
+__global__ void __launch_bounds__(256) k_chol_gemv_lower(const T *__restrict__ f, Grid3 g, const MT *__restrict__ Linv,
+                                                          int ld, MT *__restrict__ v, NoiseArgs nz) {
+    pdl_begin();
+    extern __shared__ __align__(16) unsigned char chol_sm[];
+    MT *fs = reinterpret_cast<MT *>(chol_sm);
+    const int n = g.N0 * g.N1 * g.N2;
+    for (int i = threadIdx.x; i < ld; i += blockDim.x) {
+        MT val = MT(0);
+        if (i < n) {
+            const int a = i % g.N0, t = i / g.N0;
+            val = (MT)f[g.pad(a, t % g.N1, t / g.N1)];
+        }
+        fs[i] = val;
     }
     __syncthreads();
+    constexpr int NV = Vec16<MT>::N;
     const int lane = threadIdx.x & 31;
-    const i64 warps = (i64)gridDim.x * (blockDim.x >> 5);
-    // warp w owns rows w and n-1-w (together n+1 entries): balanced work
-    for (i64 ii = (i64)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ii < n; ii += warps) {
-        const i64 half = ii >> 1;
-        const i64 i = (ii & 1) ? n - 1 - half : half;
-        const double *row = Linv + i * n;
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-        i64 k = lane;
-        for (; k + 96 <= i; k += 128) {
-            a0 += row[k] * fs[k];
-            a1 += row[k + 32] * fs[k + 32];
-            a2 += row[k + 64] * fs[k + 64];
-            a3 += row[k + 96] * fs[k + 96];
-        }
-        for (; k <= i; k += 32) a0 += row[k] * fs[k];
-        double acc = (a0 + a1) + (a2 + a3);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int ii = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ii < n; ii += warps) {
+        const int i = (ii & 1) ? n - 1 - (ii >> 1) : (ii >> 1);
+        const MT acc = warp_row_dot<MT>(Linv + (i64)i * ld, fs, 0, i / NV + 1, lane);
         if (lane == 0) {
             double xi = 0.0;
             if (NOISE == NOISE_INJECTED) xi = nz.buf[i];
             if (NOISE == NOISE_PHILOX) {
                 float4 r = normals4(philox4x32_10(noise_ctr(nz, (unsigned)(i >> 2), PURPOSE_COARSE, 0), noise_key(nz)));
-                xi = (double)pick(r, (int)(i & 3));
+                xi = (double)pick(r, i & 3);
             }
-            v[i] = xi + acc;
+            v[i] = (MT)xi + acc;
         }
     }
 }
 
-// ... x = Linv^T v (row j of Linv^T has non-zeros j..n-1).
-template <typename T>
-__global__ void __launch_bounds__(256) k_chol_gemv_upper(const double *__restrict__ v, Grid3 g,
-                                                          const double *__restrict__ LinvT, T *__restrict__ x) {
-    extern __shared__ double vs[];
-    const i64 n = (i64)g.N0 * g.N1 * g.N2;
-    for (i64 i = threadIdx.x; i < n; i += blockDim.x) vs[i] = v[i];
+// ... x = Linv^T v (row j of Linv^T: vectors j / NV .. ld / NV - 1).
+template <typename T, typename MT>
+__global__ void __launch_bounds__(256) k_chol_gemv_upper(const MT *__restrict__ v, Grid3 g,
+                                                          const MT *__restrict__ LinvT, int ld, T *__restrict__ x) {
+    pdl_begin();
+    extern __shared__ __align__(16) unsigned char chol_sm[];
+    MT *vs = reinterpret_cast<MT *>(chol_sm);
+    const int n = g.N0 * g.N1 * g.N2;
+    for (int i = threadIdx.x; i < ld; i += blockDim.x) vs[i] = i < n ? v[i] : MT(0);
     __syncthreads();
+    constexpr int NV = Vec16<MT>::N;
     const int lane = threadIdx.x & 31;
-    const i64 warps = (i64)gridDim.x * (blockDim.x >> 5);
-    for (i64 jj = (i64)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); jj < n; jj += warps) {
-        const i64 half = jj >> 1;
-        const i64 j = (jj & 1) ? n - 1 - half : half;
-        const double *row = LinvT + j * n;
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-        i64 k = j + lane;
-        for (; k + 96 < n; k += 128) {
-            a0 += row[k] * vs[k];
-            a1 += row[k + 32] * vs[k + 32];
-            a2 += row[k + 64] * vs[k + 64];
-            a3 += row[k + 96] * vs[k + 96];
-        }
-        for (; k < n; k += 32) a0 += row[k] * vs[k];
-        double acc = (a0 + a1) + (a2 + a3);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int jj = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); jj < n; jj += warps) {
+        const int j = (jj & 1) ? n - 1 - (jj >> 1) : (jj >> 1);
+        const MT acc = warp_row_dot<MT>(LinvT + (i64)j * ld, vs, j / NV, ld / NV, lane);
         if (lane == 0) {
-            int a = (int)(j % g.N0), b = (int)((j / g.N0) % g.N1), c = (int)(j / ((i64)g.N0 * g.N1));
-            x[g.pad(a, b, c)] = (T)acc;
+            const int a = j % g.N0, t = j / g.N0;
+            x[g.pad(a, t % g.N1, t / g.N1)] = (T)acc;
         }
     }
 }
@@ -903,6 +955,7 @@ __global__ void __launch_bounds__(256) k_step_end(const T *__restrict__ x, int n
                                                    double *__restrict__ obs, i64 capacity, u64 *__restrict__ obs_count,
                                                    u64 *__restrict__ d_step, unsigned *__restrict__ err,
                                                    unsigned *__restrict__ done) {
+    pdl_begin();
     __shared__ double sh[32];
     __shared__ bool last;
     const int p = blockIdx.x;
