@@ -267,7 +267,7 @@ def batch_study(nchain, steps, warmup=5, seed=3):
     """Batching: nchain independent chains, cubic lattices drawn from
     {32,48,64,96,128}^3 cells, kappa^2 log-uniform in [1, 100], 0-64
     measurements (centres U[0.1,0.9]^3, radius 0.05, variance 1e-4, values
-    N(0,1)), FP32 fine levels / FP64 coarse, V(1,1) SSOR, 5 levels, all
+    N(0,1)), FP32-mixed precision, V(1,1) SSOR, 5 levels, all
     stepped by one CUDA graph.  Reports aggregate samples/s and the per-chain
     IACT distribution."""
     import torch
@@ -450,7 +450,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (FP64 coarse Cholesky and m x m system)", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f32 (FP64 Cholesky factorisation and m x m low-rank system)", "data": "synthetic",
         "config": {"workload": "3D 256^3 posterior MGMC V(1,1) SSOR omega=1, 5 levels, coarse dense Cholesky 16^3, "
                                "64 measurements r=0.05 Sigma=1e-4, kappa^2=10",
                    "unknowns": int(op.n), "ordering": "multicolour (red-black fine, 8-colour coarse)",

@@ -87,6 +87,8 @@ struct Level {
     float *zf = nullptr, *Bvalf = nullptr;
     unsigned *counter = nullptr;
     int bt_split = 1;  // blocks per column of the B^T x reduction
+    CUtensorMap xmap{}, fmap{};  // 3D tile maps of x and f for the residual-restriction
+    bool tma = false;            // maps valid (3D, rows of a multiple of 16 bytes)
 };
 
 struct Sampler {
@@ -154,6 +156,7 @@ struct Sampler {
 
     void build(const mgmc_operator_desc &op);
     void build_lowrank(int lev);
+    void make_tile_maps(Level &lv);
     void build_coarse();
     void launch_step();
     void sor(int lev, bool forward, bool noisy, void *x, void *f);
@@ -364,6 +367,18 @@ static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void
     if (zero_stencil)
         for (int k = 0; k < 27; ++k) s.w[k] = T(0);
     const i64 nc = lc.geo.n;
+    if (S.dim == 3 && !zero_stencil && lv.tma && x == lv.x && f == lv.f) {
+        dim3 grid((lc.g.N0 + RR_TX - 1) / RR_TX, (lc.g.N1 + RR_TY - 1) / RR_TY, (lc.g.N2 + RR_TZ - 1) / RR_TZ);
+        const size_t sm = rr_tma_smem_bytes<T>();
+        if (lv.npt == 7)
+            plaunch(S.pdl, k_resid_restrict_tma<T, 7>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap, (T *)fc, lv.g, lc.g, s,
+                    S.d_err);
+        else
+            plaunch(S.pdl, k_resid_restrict_tma<T, 27>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap, (T *)fc, lv.g, lc.g,
+                    s, S.d_err);
+        S.launches++;
+        return;
+    }
     if (S.dim == 3 && !zero_stencil) {
         dim3 grid((lc.g.N0 + RR_TX - 1) / RR_TX, (lc.g.N1 + RR_TY - 1) / RR_TY, (lc.g.N2 + RR_TZ - 1) / RR_TZ);
         const size_t sm = rr_smem_bytes<T>();
@@ -726,6 +741,51 @@ void Sampler::build_coarse() {
     }
 }
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// Tile maps of a level's padded x and f as 3D tensors (row of sy elements
+// including the shared ghost, sz / sy rows per plane, N2 + 2 planes) for
+// k_resid_restrict_tma; levels whose row or plane pitch is not a multiple of
+// 16 bytes keep the plain-load kernel.
+void Sampler::make_tile_maps(Level &lv) {
+    if (dim != 3) return;
+    const size_t esz = fp32 ? sizeof(float) : sizeof(double);
+    if ((lv.g.sy * esz) % 16 != 0 || (lv.g.sz * esz) % 16 != 0) return;
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return;
+    const cuuint64_t dims[3] = {(cuuint64_t)lv.g.sy, (cuuint64_t)(lv.g.sz / lv.g.sy), (cuuint64_t)lv.g.N2 + 2};
+    const cuuint64_t strides[2] = {(cuuint64_t)(lv.g.sy * esz), (cuuint64_t)(lv.g.sz * esz)};
+    const cuuint32_t xbox[3] = {RR_BW, RR_XH, RR_XD}, fbox[3] = {RR_BW, RR_FH, RR_FD}, es[3] = {1, 1, 1};
+    const CUtensorMapDataType dt = fp32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    if (enc(&lv.xmap, dt, 3, lv.x, dims, strides, xbox, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return;
+    if (enc(&lv.fmap, dt, 3, lv.f, dims, strides, fbox, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return;
+    lv.tma = true;
+}
+
 void Sampler::build(const mgmc_operator_desc &op) {
     if (op.dim < 1 || op.dim > 3) fail(MGMC_ERR_INVALID_ARGUMENT, "dim must be 1, 2 or 3");
     dim = op.dim;
@@ -759,6 +819,10 @@ void Sampler::build(const mgmc_operator_desc &op) {
                             (int)rr_smem_bytes<double>()));
     CK(cudaFuncSetAttribute(k_resid_restrict_tiled<double, 27>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)rr_smem_bytes<double>()));
+    CK(cudaFuncSetAttribute(k_resid_restrict_tma<double, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)rr_tma_smem_bytes<double>()));
+    CK(cudaFuncSetAttribute(k_resid_restrict_tma<double, 27>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)rr_tma_smem_bytes<double>()));
     d_step = alloc<u64>(1);
     d_obs_count = alloc<u64>(1);
     d_err = alloc<unsigned>(1);
@@ -799,6 +863,7 @@ void Sampler::build(const mgmc_operator_desc &op) {
         lv.x = talloc(lv.geo.nalloc);
         lv.f = talloc(lv.geo.nalloc);
     }
+    for (size_t lev = 0; lev + 1 < L.size(); ++lev) make_tile_maps(L[lev]);
     d_cvec = alloc<double>(L[0].geo.n);
     // low-rank term on every level: B_{l+1} = R B_l
     if (m > 0) {
@@ -898,6 +963,15 @@ static void get_vec(Sampler &S, int lev, const void *src, double *dst, int on_de
 // Capture one step into a CUDA graph (Philox noise: the step's launches and
 // arguments never change; the noise streams advance through the device
 // step counter).
+// Error bits raised on the device: 1 = non-finite observable, 2 = a tile
+// copy wait ran out.
+static void check_device_errors(Sampler &S) {
+    unsigned err = 0;
+    CK(cudaMemcpy(&err, S.d_err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err & ERR_TILE_TIMEOUT) fail(MGMC_ERR_CUDA, "a shared-memory tile copy did not complete in time");
+    if (err) fail(MGMC_ERR_NONFINITE, "non-finite observable in the chain");
+}
+
 static void ensure_graph(Sampler &S) {
     if (S.gexec) return;
     CK(cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal));
@@ -1082,9 +1156,7 @@ mgmc_status mgmc_sampler_apply(mgmc_sampler *s, const double *f, double *x, int 
     run_steps(S, 1);
     get_vec(S, 0, S.L[0].x, x, on_device);
     CK(cudaStreamSynchronize(S.stream));
-    unsigned err = 0;
-    CK(cudaMemcpy(&err, S.d_err, sizeof(err), cudaMemcpyDeviceToHost));
-    if (err) fail(MGMC_ERR_NONFINITE, "non-finite observable in the chain");
+    check_device_errors(S);
     API_END
 }
 
@@ -1151,9 +1223,7 @@ mgmc_status mgmc_sampler_read_observations(mgmc_sampler *s, double *out, int64_t
     if (k > 0 && out) CK(cudaMemcpy(out, S.d_obs, (size_t)k * np * sizeof(double), cudaMemcpyDeviceToHost));
     *count = (int64_t)c;
     CK(cudaMemset(S.d_obs_count, 0, sizeof(u64)));
-    unsigned err = 0;
-    CK(cudaMemcpy(&err, S.d_err, sizeof(err), cudaMemcpyDeviceToHost));
-    if (err) fail(MGMC_ERR_NONFINITE, "non-finite observable in the chain");
+    check_device_errors(S);
     API_END
 }
 
@@ -1200,6 +1270,9 @@ mgmc_status mgmc_sampler_synchronize(mgmc_sampler *s) {
     API_BEGIN
     Sampler &S = impl(s);
     CK(cudaStreamSynchronize(S.stream));
+    unsigned err = 0;
+    CK(cudaMemcpy(&err, S.d_err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err & ERR_TILE_TIMEOUT) fail(MGMC_ERR_CUDA, "a shared-memory tile copy did not complete in time");
     API_END
 }
 

@@ -20,6 +20,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h>  // CUtensorMap (type only; the driver entry point is resolved at run time)
 #include <cuda_runtime.h>
 
 namespace mgmc {
@@ -651,6 +652,143 @@ __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tiled(const T *__
             for (int ax = 0; ax < 3; ++ax) {
                 const T wr = T((ax == 1 ? 1.0 : 0.5) * (ay == 1 ? 1.0 : 0.5) * (az == 1 ? 1.0 : 0.5));
                 acc += wr * rs[((2 * lc + az) * RR_FH + (2 * lb + ay)) * RR_FW + 2 * la + ax];
+            }
+    fc[gc.pad(ca, cb, cc)] = acc;
+}
+
+// ---------------------------------------------- bulk tensor copies (TMA)
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// 3D tiled copy of the tensor map's box at element coordinates (x, y, z)
+// into shared memory; completion is counted on `bar` in bytes.
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
+                                            unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<u64>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ u64 global_ns() {
+    u64 t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for phase `parity` of `bar`, giving up after limit_ns nanoseconds.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity, u64 limit_ns) {
+    const u64 t0 = global_ns();
+    while (!mbar_try_wait(bar, parity))
+        if (global_ns() - t0 > limit_ns) return false;
+    return true;
+}
+
+constexpr u64 TILE_WAIT_NS = 200000000ull;  // 0.2 s: a tile copy that has not landed by then is reported
+constexpr unsigned ERR_TILE_TIMEOUT = 2u;    // error bit: a tile copy wait ran out
+
+// TMA variant of the residual-restriction (rows of x and f that are
+// multiples of 16 bytes): thread 0 issues two 3D bulk tensor copies of the
+// padded arrays -- x over the footprint plus a one-point halo, f over the
+// footprint -- with rows widened to RR_BW elements (the copy's x coordinate
+// 2 * 8 * blockIdx.x stays 16-byte aligned); points outside the arrays read
+// as zero, like the ghost layer.  The residual overwrites f in shared
+// memory, then each thread restricts to its coarse point.
+constexpr int RR_BW = 20;
+
+template <typename T>
+__host__ __device__ constexpr size_t rr_tma_xbytes() {
+    return (sizeof(T) * RR_BW * RR_XH * RR_XD + 127) / 128 * 128;
+}
+template <typename T>
+__host__ __device__ constexpr size_t rr_tma_smem_bytes() {
+    return rr_tma_xbytes<T>() + sizeof(T) * RR_BW * RR_FH * RR_FD;
+}
+
+template <typename T, int NPT>
+__global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tma(const __grid_constant__ CUtensorMap xmap,
+                                                                   const __grid_constant__ CUtensorMap fmap,
+                                                                   T *__restrict__ fc, Grid3 gf, Grid3 gc,
+                                                                   StencilArg<T> s, unsigned *__restrict__ err) {
+    pdl_begin();
+    extern __shared__ __align__(1024) unsigned char rr_tma_smem[];
+    __shared__ unsigned long long bar;
+    T *xs = reinterpret_cast<T *>(rr_tma_smem);                      // [RR_XD][RR_XH][RR_BW]
+    T *fs = reinterpret_cast<T *>(rr_tma_smem + rr_tma_xbytes<T>()); // [RR_FD][RR_FH][RR_BW]
+    const int ca0 = blockIdx.x * RR_TX, cb0 = blockIdx.y * RR_TY, cc0 = blockIdx.z * RR_TZ;
+    const int fa0 = 2 * ca0, fb0 = 2 * cb0, fz0 = 2 * cc0;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&bar, (unsigned)(sizeof(T) * RR_BW * (RR_XH * RR_XD + RR_FH * RR_FD)));
+        // padded coordinates: fine vertex a sits at a + 1
+        tma_load_3d(xs, &xmap, fa0, fb0, fz0, &bar);         // fine (fa0-1, fb0-1, fz0-1) ...
+        tma_load_3d(fs, &fmap, fa0, fb0 + 1, fz0 + 1, &bar); // fine (fa0-1, fb0, fz0) ...
+    }
+    const bool ok = mbar_wait_bounded(&bar, 0, TILE_WAIT_NS);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicOr(err, ERR_TILE_TIMEOUT);
+        mbar_wait_bounded(&bar, 0, TILE_WAIT_NS);  // let copies in flight land before the CTA exits
+        return;
+    }
+    constexpr int SY = RR_BW, SZ = RR_BW * RR_XH;
+    for (int i = threadIdx.x; i < RR_FW * RR_FH * RR_FD; i += RR_THREADS) {
+        const int la = i % RR_FW, lb = (i / RR_FW) % RR_FH, lc = i / (RR_FW * RR_FH);
+        const int qf = (lc * RR_FH + lb) * RR_BW + la + 1;
+        T r = T(0);
+        if (fa0 + la < gf.N0 && fb0 + lb < gf.N1 && fz0 + lc < gf.N2) {
+            const int q = ((lc + 1) * RR_XH + (lb + 1)) * RR_BW + (la + 1);
+            T res;
+            if (NPT == 7) {
+                res = s.w[4] * xs[q - SZ] + s.w[10] * xs[q - SY] + s.w[12] * xs[q - 1] + s.w[13] * xs[q] +
+                      s.w[14] * xs[q + 1] + s.w[16] * xs[q + SY] + s.w[22] * xs[q + SZ];
+            } else {
+                res = T(0);
+#pragma unroll
+                for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+                    for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+                        for (int dx = -1; dx <= 1; ++dx)
+                            res += s.w[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)] * xs[q + dz * SZ + dy * SY + dx];
+            }
+            r = fs[qf] - res;
+        }
+        fs[qf] = r;
+    }
+    __syncthreads();
+    const int la = threadIdx.x % RR_TX, lb = (threadIdx.x / RR_TX) % RR_TY, lc = threadIdx.x / (RR_TX * RR_TY);
+    const int ca = ca0 + la, cb = cb0 + lb, cc = cc0 + lc;
+    if (ca >= gc.N0 || cb >= gc.N1 || cc >= gc.N2) return;
+    T acc = T(0);
+#pragma unroll
+    for (int az = 0; az < 3; ++az)
+#pragma unroll
+        for (int ay = 0; ay < 3; ++ay)
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                const T wr = T((ax == 1 ? 1.0 : 0.5) * (ay == 1 ? 1.0 : 0.5) * (az == 1 ? 1.0 : 0.5));
+                acc += wr * fs[((2 * lc + az) * RR_FH + (2 * lb + ay)) * RR_BW + 2 * la + ax + 1];
             }
     fc[gc.pad(ca, cb, cc)] = acc;
 }
