@@ -85,7 +85,6 @@ struct Level {
     double *Sinv[2] = {nullptr, nullptr};
     double *y = nullptr, *z = nullptr, *part = nullptr;
     float *zf = nullptr, *Bvalf = nullptr;
-    unsigned *counter = nullptr;
     int bt_split = 1;  // blocks per column of the B^T x reduction
     CUtensorMap xmap{}, fmap{};  // 3D tile maps of x and f for the residual-restriction
     bool tma = false;            // maps valid (3D, rows of a multiple of 16 bytes)
@@ -244,15 +243,19 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
             const int colour = forward ? pass : 1 - pass;
             if constexpr (std::is_same<T, float>::value) {
                 if (vec) {
-                    dim3 grid(((lv.g.N0 + 8) / 8 + RBP_THREADS - 1) / RBP_THREADS, lv.g.N1, lv.g.N2);
-                    plaunch(S.pdl, k_sweep_rb_vec<NOISE>, grid, RBP_THREADS, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
+                    const int ngrp = (lv.g.N0 + 8) / 8;
+                    const dim3 blk = sweep_block(ngrp);
+                    dim3 grid((ngrp + blk.x - 1) / blk.x, (lv.g.N1 + blk.y - 1) / blk.y, lv.g.N2);
+                    plaunch(S.pdl, k_sweep_rb_vec<NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
                     S.launches++;
                     continue;
                 }
             }
             {
-                dim3 grid((lv.g.N0 + 2 * RBP_THREADS - 1) / (2 * RBP_THREADS), lv.g.N1, lv.g.N2);
-                plaunch(S.pdl, k_sweep_rb_pass<T, EXACT, NOISE>, grid, RBP_THREADS, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
+                const int na = (lv.g.N0 + 1) / 2;
+                const dim3 blk = sweep_block(na);
+                dim3 grid((na + blk.x - 1) / blk.x, (lv.g.N1 + blk.y - 1) / blk.y, lv.g.N2);
+                plaunch(S.pdl, k_sweep_rb_pass<T, EXACT, NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
             }
             S.launches++;
         }
@@ -270,8 +273,9 @@ static void launch_colour_passes(Sampler &S, const Level &lv, bool forward, T *x
         const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
         const int na = (lv.g.N0 - pa + 1) / 2, nb = (lv.g.N1 - pb + 1) / 2, nc = (lv.g.N2 - pc + 1) / 2;
         if (na <= 0 || nb <= 0 || nc <= 0) continue;
-        dim3 grid((na + RBP_THREADS - 1) / RBP_THREADS, nb, nc);
-        plaunch(S.pdl, k_sweep_c27_pass<T, EXACT, NOISE>, grid, RBP_THREADS, 0, S.stream, x, f, lv.g, s, colour, nz);
+        const dim3 blk = sweep_block(na);
+        dim3 grid((na + blk.x - 1) / blk.x, (nb + blk.y - 1) / blk.y, nc);
+        plaunch(S.pdl, k_sweep_c27_pass<T, EXACT, NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, nz);
         S.launches++;
     }
 }
@@ -320,15 +324,14 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     lr.y = lv.y;
     lr.z = lv.z;
     lr.part = lv.part;
-    lr.counter = lv.counter;
-    size_t smem = sizeof(double) * S.m;
-    dim3 grid(S.m, lv.bt_split);
+    const size_t smem = sizeof(double) * S.m;
+    plaunch(S.pdl, k_bt_partial<T>, dim3(S.m, lv.bt_split), 256, 0, S.stream, (const T *)x, lr);
     if (noise == NOISE_NONE)
-        plaunch(S.pdl, k_bt_x_z<T, NOISE_NONE, true>, grid, 256, smem, S.stream, x, lr, nz);
+        plaunch(S.pdl, k_lr_solve<NOISE_NONE, true>, 1, 256, smem, S.stream, lr, lv.bt_split, nz);
     else if (noise == NOISE_PHILOX)
-        plaunch(S.pdl, k_bt_x_z<T, NOISE_PHILOX, true>, grid, 256, smem, S.stream, x, lr, nz);
+        plaunch(S.pdl, k_lr_solve<NOISE_PHILOX, true>, 1, 256, smem, S.stream, lr, lv.bt_split, nz);
     else
-        plaunch(S.pdl, k_bt_x_z<T, NOISE_INJECTED, true>, grid, 256, smem, S.stream, x, lr, nz);
+        plaunch(S.pdl, k_lr_solve<NOISE_INJECTED, true>, 1, 256, smem, S.stream, lr, lv.bt_split, nz);
     const RowCsr &C = lv.C[dir];
     if (C.nrows > 0) {
         if (sizeof(T) == 4)
@@ -336,6 +339,7 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
                                                                          lv.zf);
         else
             plaunch(S.pdl, k_lr_scatter<T>, nblk(C.nrows, 256), 256, 0, S.stream, x, C.nrows, C.rows, C.ptr, C.col, (const T *)C.val, lv.z);
+        S.launches++;
     }
     S.launches += 2;
 }
@@ -406,10 +410,10 @@ static void launch_bt_plain(Sampler &S, Level &lv, const void *x) {
     lr.Bvalf = lv.Bvalf;
     lr.y = lv.y;
     lr.part = lv.part;
-    lr.counter = lv.counter;
     NoiseArgs nz{};
-    plaunch(S.pdl, k_bt_x_z<T, NOISE_NONE, false>, dim3(S.m, lv.bt_split), 256, 0, S.stream, (const T *)x, lr, nz);
-    S.launches++;
+    plaunch(S.pdl, k_bt_partial<T>, dim3(S.m, lv.bt_split), 256, 0, S.stream, (const T *)x, lr);
+    plaunch(S.pdl, k_lr_solve<NOISE_NONE, false>, 1, 256, 0, S.stream, lr, lv.bt_split, nz);
+    S.launches += 2;
 }
 
 template <typename T>
@@ -579,7 +583,7 @@ __global__ void k_nonzeros(const double *__restrict__ x, Grid3 g, i64 *__restric
 // C = M^{-1} B for both sweep directions, M = D/omega + (strictly lower
 // part of A_0 in the sweep order): column j is one noise-free sweep from
 // x = 0 with right hand side B e_j (sor_smoother.cc:17-37 in solve form).
-// S = Sigma + B^T C and G = B^T C feed k_bt_x_z.
+// S = Sigma + B^T C (with G = B^T C) gives the m x m system of k_lr_solve.
 void Sampler::build_lowrank(int lev) {
     Level &lv = L[lev];
     const Geometry &geo = lv.geo;
@@ -622,11 +626,9 @@ void Sampler::build_lowrank(int lev) {
     {
         i64 maxcol = 1;
         for (int j = 0; j < m; ++j) maxcol = std::max<i64>(maxcol, lv.Bh.ptr[j + 1] - lv.Bh.ptr[j]);
-        lv.bt_split = (int)std::min<i64>(32, std::max<i64>(1, (maxcol + 1023) / 1024));
+        lv.bt_split = (int)std::min<i64>(32, std::max<i64>(1, (maxcol + 511) / 512));
     }
     lv.part = alloc<double>((size_t)m * lv.bt_split);
-    lv.counter = alloc<unsigned>(1);
-    CK(cudaMemsetAsync(lv.counter, 0, sizeof(unsigned), stream));
     // FP64 work arrays
     double *xs = alloc<double>(geo.nalloc), *fs = alloc<double>(geo.nalloc);
     i64 *nzi = alloc<i64>(n);
@@ -653,8 +655,8 @@ void Sampler::build_lowrank(int lev) {
             lr.Bvalf = lv.Bvalf;
             lr.y = lv.y;
             lr.part = lv.part;
-            lr.counter = lv.counter;
-            k_bt_x_z<double, NOISE_NONE, false><<<dim3(m, lv.bt_split), 256, 0, stream>>>(xs, lr, nz);
+            k_bt_partial<double><<<dim3(m, lv.bt_split), 256, 0, stream>>>(xs, lr);
+            k_lr_solve<NOISE_NONE, false><<<1, 256, 0, stream>>>(lr, lv.bt_split, nz);
             CK(cudaMemcpyAsync(yh.data(), lv.y, m * sizeof(double), cudaMemcpyDeviceToHost, stream));
             CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), stream));
             k_nonzeros<<<nblk(n, 256), 256, 0, stream>>>(xs, lv.g, nzi, nzv, cnt);

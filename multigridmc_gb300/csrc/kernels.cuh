@@ -10,7 +10,8 @@
 //   k_sweep_c27_pass    one colour of the 8-colour SOR sweep of a 27-point level
 //   k_sweep_wavefront   lexicographic SOR sweep as a hyperplane wavefront
 //                       (one CTA; parity mode)
-//   k_bt_x_z            y = B^T x and the m x m low-rank solve
+//   k_bt_partial        partial sums of y = B^T x
+//   k_lr_solve          y and the m x m low-rank solve
 //   k_lr_scatter        x += C z over the rows of C = M^{-1} B
 //   k_resid_restrict_tiled  f_c = R (f - A_0 x)  (fused residual + restriction)
 //   k_sub_Bq            f_c -= B_c Sigma^{-1} y
@@ -192,20 +193,30 @@ __device__ __forceinline__ float4 fine_normals(const NoiseArgs &nz, const Grid3 
 }
 
 // One colour of a red-black sweep of an axis-only (7-point) level, one
-// thread per point of the colour; a CTA covers 2 * RBP_THREADS consecutive
-// x-positions of one row (b, c), so each warp load reads a contiguous span.
+// thread per point of the colour.  A CTA is blockDim.x points along x times
+// blockDim.y rows (b) of one plane c (sweep_block() picks the shape so that
+// no thread idles on short rows); each warp load reads a contiguous span.
 // `reverse` walks the planes from the top so that the second colour finds
 // the data the first colour touched last in L2.
-constexpr int RBP_THREADS = 128;
+constexpr int RBP_THREADS = 256;
+
+// CTA shape for `count` work items along x: the smallest power of two
+// >= count (at least 8, at most RBP_THREADS) along x, the rest along y.
+__host__ __forceinline__ dim3 sweep_block(int count) {
+    int tx = 8;
+    while (tx < count && tx < RBP_THREADS) tx *= 2;
+    return dim3(tx, RBP_THREADS / tx, 1);
+}
 
 template <typename T, bool EXACT, int NOISE>
 __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_pass(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
                                                                StencilArg<T> s, int colour, int reverse, NoiseArgs nz) {
     pdl_begin();
-    const int b = blockIdx.y;
+    const int b = blockIdx.y * blockDim.y + threadIdx.y;
     const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
+    if (b >= g.N1) return;
     const int p = (colour + b + c) & 1;
-    const int a = 2 * (blockIdx.x * RBP_THREADS + threadIdx.x) + p;
+    const int a = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + p;
     T xi = T(0);
     if (NOISE == NOISE_PHILOX) xi = (T)pick(fine_normals(nz, g, a + 1, b, c), ((a + 1) & 7) >> 1);
     if (a >= g.N0) return;
@@ -222,11 +233,11 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
                                                               Grid3 g, StencilArg<float> s, int colour, int reverse,
                                                               NoiseArgs nz) {
     pdl_begin();
-    const int b = blockIdx.y;
+    const int b = blockIdx.y * blockDim.y + threadIdx.y;
     const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
-    const int q = blockIdx.x * RBP_THREADS + threadIdx.x;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
     const int ngrp = (g.N0 + 8) >> 3;
-    if (q >= ngrp) return;
+    if (q >= ngrp || b >= g.N1) return;
     const int P0 = 8 * q;
     const i64 rb = (i64)(c + 1) * g.sz + (i64)(b + 1) * g.sy;
     const float4 *xr = reinterpret_cast<const float4 *>(x + rb + P0);
@@ -292,8 +303,8 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ 
                                                                 StencilArg<T> s, int colour, NoiseArgs nz) {
     pdl_begin();
     const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
-    const int a = 2 * (blockIdx.x * RBP_THREADS + threadIdx.x) + pa;
-    const int b = 2 * blockIdx.y + pb, c = 2 * blockIdx.z + pc;
+    const int a = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + pa;
+    const int b = 2 * (blockIdx.y * blockDim.y + threadIdx.y) + pb, c = 2 * blockIdx.z + pc;
     if (b >= g.N1 || c >= g.N2) return;
     T xi = T(0);
     if (NOISE == NOISE_PHILOX) xi = (T)pick(point_normals(nz, g, a, b, c), (a & 7) >> 1);
@@ -357,9 +368,42 @@ struct LowRankArg {
     double *z;          // m scratch: coefficients of C
     float *zf;          // the same coefficients rounded to FP32 (FP32 chain)
     const float *Bvalf; // B values rounded to FP32 (FP32 chain)
-    double *part;       // m x gridDim.y scratch: partial sums of B^T x
-    unsigned *counter;  // block-completion counter (self-resetting)
+    double *part;       // m x P scratch: partial sums of B^T x
 };
+
+// Partial sums of y_j = sum_i B_ij x_i: gridDim.y CTAs per column j, CTA p
+// writing part[j * P + p].  Each thread issues four index/value loads, then
+// the four gathers of x, before it accumulates them in entry order; the
+// per-thread sums are in the state's precision (FP32 products for the FP32
+// chain) and are combined across the CTA in FP64.
+template <typename T>
+__global__ void __launch_bounds__(256) k_bt_partial(const T *__restrict__ x, LowRankArg lr) {
+    pdl_begin();
+    __shared__ double sh[32];
+    const int j = blockIdx.x, p = blockIdx.y, P = gridDim.y;
+    const i64 e0 = lr.Bptr[j], e1 = lr.Bptr[j + 1];
+    const i64 len = (e1 - e0 + P - 1) / P;
+    const i64 lo = e0 + p * len, hi = min(e1, lo + len);
+    T tacc = T(0);
+    for (i64 e = lo + threadIdx.x; e < hi; e += 4 * 256) {
+        i64 idx[4];
+        T val[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const i64 ee = e + 256 * k;
+            idx[k] = ee < hi ? lr.Bidx[ee] : -1;
+            val[k] = ee < hi ? (sizeof(T) == 4 ? (T)lr.Bvalf[ee] : (T)lr.Bval[ee]) : T(0);
+        }
+        T xv[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) xv[k] = idx[k] >= 0 ? x[idx[k]] : T(0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (idx[k] >= 0) tacc += val[k] * xv[k];
+    }
+    const double acc = block_sum<256>((double)tacc, sh);
+    if (threadIdx.x == 0) lr.part[j * P + p] = acc;
+}
 
 // Warp sums of RW per-lane row partials; lane 0 writes rows
 // base + warp + NWARP r of z (and of its FP32 copy).
@@ -377,42 +421,17 @@ __device__ __forceinline__ void store_rows(double (&t)[RW], const LowRankArg &lr
     }
 }
 
-// y_j = sum_i B_ij x_i with gridDim.y blocks per column j (partial sums in
-// `part`, combined in a fixed order by the last block to finish, so the
-// result does not depend on block timing).  With SOLVE the same block then
-// forms the coefficients z of the correction x += C z,
+// One CTA of 256 threads: y_k = sum_p part[k * P + p] (fixed order, so the
+// result does not depend on block timing).  With SOLVE it then forms the
+// coefficients z of the correction x += C z,
 //   z = w - S^{-1} (y + G w) = S^{-1} (Sigma w - y) = S^{-1} (Sigma^{1/2} xi' - y)
 // with w = Sigma^{-1/2} xi' the low-rank noise of sor_sampler.cc:29-33,
 // G = B^T C and S = Sigma + G (so S - G = Sigma and a single m x m product
 // remains); with_noise == 0 gives z = -S^{-1} y, the smoother's correction
 // x -= Bbar B^T x of sor_smoother.cc:47-51, Bbar = C S^{-1}.
-template <typename T, int NOISE, bool SOLVE>
-__global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRankArg lr, NoiseArgs nz) {
+template <int NOISE, bool SOLVE>
+__global__ void __launch_bounds__(256) k_lr_solve(LowRankArg lr, int P, NoiseArgs nz) {
     pdl_begin();
-    __shared__ double sh[32];
-    __shared__ bool last;
-    const int j = blockIdx.x, p = blockIdx.y, P = gridDim.y;
-    const i64 e0 = lr.Bptr[j], e1 = lr.Bptr[j + 1];
-    const i64 len = (e1 - e0 + P - 1) / P;
-    const i64 lo = e0 + p * len, hi = min(e1, lo + len);
-    // per-thread sums in the state's precision (FP32 products for the FP32
-    // chain), combined across the block and the partial sums in FP64
-    T tacc = T(0);
-    if (sizeof(T) == 4) {
-        for (i64 e = lo + threadIdx.x; e < hi; e += blockDim.x) tacc += (T)lr.Bvalf[e] * x[lr.Bidx[e]];
-    } else {
-        for (i64 e = lo + threadIdx.x; e < hi; e += blockDim.x) tacc += (T)lr.Bval[e] * x[lr.Bidx[e]];
-    }
-    double acc = block_sum<256>((double)tacc, sh);
-    if (threadIdx.x == 0) lr.part[j * P + p] = acc;
-    __threadfence();
-    if (threadIdx.x == 0) {
-        unsigned done = atomicAdd(lr.counter, 1u);
-        last = (done == gridDim.x * gridDim.y - 1);
-    }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
     const int m = lr.m;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr int NWARP = 8, RW = 8, QC = 4;  // rows per warp and 32-column chunks per lane in one batch
@@ -420,7 +439,7 @@ __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRank
     double *u = dyn;
     // Rows warp + NWARP r (r < RW) of S^{-1}, columns lane + 32 c (c < QC):
     // for m <= 64 the whole matrix is loaded here, before the partial sums
-    // are combined, so that every load of the block is in flight at once.
+    // are combined, so that every load of the CTA is in flight at once.
     const bool onebatch = SOLVE && m <= NWARP * RW && m <= 32 * QC;
     double a[RW][QC];
     if (onebatch) {
@@ -432,9 +451,8 @@ __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRank
                 a[r][c] = (k < m && q < m) ? __ldg(lr.Sinv + (i64)k * m + q) : 0.0;
             }
     }
-    // y_k: warp per column, lanes over the P partial sums (P <= 32: one load
-    // per lane), eight columns in flight per warp; with SOLVE also
-    // u_k = Sigma_k^{1/2} xi'_k - y_k
+    // y_k: warp per column, lanes over the P partial sums, eight columns in
+    // flight per warp; with SOLVE also u_k = Sigma_k^{1/2} xi'_k - y_k
     for (int k0 = warp; k0 < m; k0 += 8 * NWARP) {
         double t[8];
 #pragma unroll
@@ -442,7 +460,7 @@ __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRank
             const int k = k0 + NWARP * r;
             t[r] = 0.0;
             if (k < m)
-                for (int q = lane; q < P; q += 32) t[r] += __ldcg(lr.part + (i64)k * P + q);
+                for (int q = lane; q < P; q += 32) t[r] += lr.part[(i64)k * P + q];
         }
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
@@ -469,7 +487,6 @@ __global__ void __launch_bounds__(256) k_bt_x_z(const T *__restrict__ x, LowRank
             }
         }
     }
-    if (threadIdx.x == 0) *lr.counter = 0u;
     if (!SOLVE) return;
     __syncthreads();
     // z = S^{-1} u: warp per row, RW rows per warp in flight
