@@ -82,7 +82,7 @@ struct Level {
     double *Bval = nullptr;
     RowCsr Br;          // B by rows (double values)
     RowCsr C[2];        // C = M^{-1} B, forward / backward (T values)
-    double *Sinv[2] = {nullptr, nullptr};
+    double *SinvT[2] = {nullptr, nullptr};  // S^{-1} transposed, per sweep direction
     double *y = nullptr, *z = nullptr, *part = nullptr;
     float *zf = nullptr, *Bvalf = nullptr;
     int bt_split = 1;  // blocks per column of the B^T x reduction
@@ -205,6 +205,8 @@ NoiseArgs Sampler::noise_args(int lev, i64 count) {
 // (pdl_begin), so no kernel touches memory before its predecessor has
 // completed and flushed.  This hides the launch latency between the short
 // dependent kernels of a multigrid step.
+constexpr i64 PDL_MAX_POINTS = i64(1) << 22;
+
 template <typename... KArgs, typename... Args>
 static void plaunch(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
                     Args &&...args) {
@@ -231,7 +233,7 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
     StencilArg<T> s = stencil_arg<T>(lv, S.P.omega);
     if (S.P.ordering == MGMC_ORDER_LEXICOGRAPHIC) {
         int hb = lv.ncol == 2 ? 1 : 2, hc = lv.ncol == 2 ? 1 : 4;
-        plaunch(S.pdl, k_sweep_wavefront<T, NPT, EXACT, NOISE>, 1, 1024, 0, S.stream, x, f, lv.g, s, forward ? 1 : 0, hb, hc, nz);
+        plaunch(S.pdl && lv.g.pdl, k_sweep_wavefront<T, NPT, EXACT, NOISE>, 1, 1024, 0, S.stream, x, f, lv.g, s, forward ? 1 : 0, hb, hc, nz);
         S.launches++;
         return;
     }
@@ -246,7 +248,7 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
                     const int ngrp = (lv.g.N0 + 8) / 8;
                     const dim3 blk = sweep_block(ngrp);
                     dim3 grid((ngrp + blk.x - 1) / blk.x, (lv.g.N1 + blk.y - 1) / blk.y, lv.g.N2);
-                    plaunch(S.pdl, k_sweep_rb_vec<NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
+                    plaunch(S.pdl && lv.g.pdl, k_sweep_rb_vec<NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
                     S.launches++;
                     continue;
                 }
@@ -255,7 +257,7 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
                 const int na = (lv.g.N0 + 1) / 2;
                 const dim3 blk = sweep_block(na);
                 dim3 grid((na + blk.x - 1) / blk.x, (lv.g.N1 + blk.y - 1) / blk.y, lv.g.N2);
-                plaunch(S.pdl, k_sweep_rb_pass<T, EXACT, NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
+                plaunch(S.pdl && lv.g.pdl, k_sweep_rb_pass<T, EXACT, NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
             }
             S.launches++;
         }
@@ -275,7 +277,7 @@ static void launch_colour_passes(Sampler &S, const Level &lv, bool forward, T *x
         if (na <= 0 || nb <= 0 || nc <= 0) continue;
         const dim3 blk = sweep_block(na);
         dim3 grid((na + blk.x - 1) / blk.x, (nb + blk.y - 1) / blk.y, nc);
-        plaunch(S.pdl, k_sweep_c27_pass<T, EXACT, NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, nz);
+        plaunch(S.pdl && lv.g.pdl, k_sweep_c27_pass<T, EXACT, NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, nz);
         S.launches++;
     }
 }
@@ -310,6 +312,9 @@ static void launch_sweep(Sampler &S, const Level &lv, bool forward, int noise, v
         launch_sweep_noise<double, false>(S, lv, forward, noise, (double *)x, (const double *)f, nz);
 }
 
+// threads of the one-CTA low-rank solve: one per row, up to 256
+static unsigned solve_block(int m) { return (unsigned)std::min(256, std::max(32, (m + 31) / 32 * 32)); }
+
 template <typename T>
 static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, const NoiseArgs &nz) {
     LowRankArg lr;
@@ -319,7 +324,7 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     lr.Bval = lv.Bval;
     lr.Bvalf = lv.Bvalf;
     lr.zf = lv.zf;
-    lr.Sinv = lv.Sinv[dir];
+    lr.SinvT = lv.SinvT[dir];
     lr.sigma_sqrt = S.d_sigma_sqrt;
     lr.y = lv.y;
     lr.z = lv.z;
@@ -327,11 +332,11 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     const size_t smem = sizeof(double) * S.m;
     plaunch(S.pdl, k_bt_partial<T>, dim3(S.m, lv.bt_split), 256, 0, S.stream, (const T *)x, lr);
     if (noise == NOISE_NONE)
-        plaunch(S.pdl, k_lr_solve<NOISE_NONE, true>, 1, 256, smem, S.stream, lr, lv.bt_split, nz);
+        plaunch(S.pdl, k_lr_solve<NOISE_NONE, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
     else if (noise == NOISE_PHILOX)
-        plaunch(S.pdl, k_lr_solve<NOISE_PHILOX, true>, 1, 256, smem, S.stream, lr, lv.bt_split, nz);
+        plaunch(S.pdl, k_lr_solve<NOISE_PHILOX, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
     else
-        plaunch(S.pdl, k_lr_solve<NOISE_INJECTED, true>, 1, 256, smem, S.stream, lr, lv.bt_split, nz);
+        plaunch(S.pdl, k_lr_solve<NOISE_INJECTED, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
     const RowCsr &C = lv.C[dir];
     if (C.nrows > 0) {
         if (sizeof(T) == 4)
@@ -375,10 +380,10 @@ static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void
         dim3 grid((lc.g.N0 + RR_TX - 1) / RR_TX, (lc.g.N1 + RR_TY - 1) / RR_TY, (lc.g.N2 + RR_TZ - 1) / RR_TZ);
         const size_t sm = rr_tma_smem_bytes<T>();
         if (lv.npt == 7)
-            plaunch(S.pdl, k_resid_restrict_tma<T, 7>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap, (T *)fc, lv.g, lc.g, s,
+            plaunch(S.pdl && lv.g.pdl, k_resid_restrict_tma<T, 7>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap, (T *)fc, lv.g, lc.g, s,
                     S.d_err);
         else
-            plaunch(S.pdl, k_resid_restrict_tma<T, 27>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap, (T *)fc, lv.g, lc.g,
+            plaunch(S.pdl && lv.g.pdl, k_resid_restrict_tma<T, 27>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap, (T *)fc, lv.g, lc.g,
                     s, S.d_err);
         S.launches++;
         return;
@@ -387,16 +392,16 @@ static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void
         dim3 grid((lc.g.N0 + RR_TX - 1) / RR_TX, (lc.g.N1 + RR_TY - 1) / RR_TY, (lc.g.N2 + RR_TZ - 1) / RR_TZ);
         const size_t sm = rr_smem_bytes<T>();
         if (lv.npt == 7)
-            plaunch(S.pdl, k_resid_restrict_tiled<T, 7>, grid, RR_THREADS, sm, S.stream, (const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s);
+            plaunch(S.pdl && lv.g.pdl, k_resid_restrict_tiled<T, 7>, grid, RR_THREADS, sm, S.stream, (const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s);
         else
-            plaunch(S.pdl, k_resid_restrict_tiled<T, 27>, grid, RR_THREADS, sm, S.stream, (const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s);
+            plaunch(S.pdl && lv.g.pdl, k_resid_restrict_tiled<T, 27>, grid, RR_THREADS, sm, S.stream, (const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s);
         S.launches++;
         return;
     }
     if (lv.npt == 7 && !zero_stencil)
-        plaunch(S.pdl, k_resid_restrict<T, 7>, nblk(nc, 256), 256, 0, S.stream, (const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, S.dim);
+        plaunch(S.pdl && lv.g.pdl, k_resid_restrict<T, 7>, nblk(nc, 256), 256, 0, S.stream, (const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, S.dim);
     else
-        plaunch(S.pdl, k_resid_restrict<T, 27>, nblk(nc, 256), 256, 0, S.stream, (const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, S.dim);
+        plaunch(S.pdl && lv.g.pdl, k_resid_restrict<T, 27>, nblk(nc, 256), 256, 0, S.stream, (const T *)x, (const T *)f, (T *)fc, lv.g, lc.g, s, S.dim);
     S.launches++;
 }
 
@@ -412,7 +417,7 @@ static void launch_bt_plain(Sampler &S, Level &lv, const void *x) {
     lr.part = lv.part;
     NoiseArgs nz{};
     plaunch(S.pdl, k_bt_partial<T>, dim3(S.m, lv.bt_split), 256, 0, S.stream, (const T *)x, lr);
-    plaunch(S.pdl, k_lr_solve<NOISE_NONE, false>, 1, 256, 0, S.stream, lr, lv.bt_split, nz);
+    plaunch(S.pdl, k_lr_solve<NOISE_NONE, false>, 1, solve_block(S.m), 0, S.stream, lr, lv.bt_split, nz);
     S.launches += 2;
 }
 
@@ -448,16 +453,16 @@ void Sampler::prolong(int lev, double alpha, void *xc, void *x) {
     Level &lv = L[lev], &lc = L[lev + 1];
     dim3 grid((lc.g.N0 + 1 + 127) / 128, dim > 1 ? lc.g.N1 + 1 : 1, dim > 2 ? lc.g.N2 + 1 : 1);
     if (fp32)
-        plaunch(pdl, k_prolong_add<float>, grid, 128, 0, stream, (float *)x, (const float *)xc, lv.g, lc.g, (float)alpha, dim);
+        plaunch(pdl && lv.g.pdl, k_prolong_add<float>, grid, 128, 0, stream, (float *)x, (const float *)xc, lv.g, lc.g, (float)alpha, dim);
     else
-        plaunch(pdl, k_prolong_add<double>, grid, 128, 0, stream, (double *)x, (const double *)xc, lv.g, lc.g, alpha, dim);
+        plaunch(pdl && lv.g.pdl, k_prolong_add<double>, grid, 128, 0, stream, (double *)x, (const double *)xc, lv.g, lc.g, alpha, dim);
     launches++;
 }
 
 template <typename T, int NOISE>
 static void launch_chol(Sampler &S, Level &lv, const NoiseArgs &nz) {
     if (S.exact) {
-        plaunch(S.pdl, k_chol_subst<T, NOISE>, 1, 1024, 0, S.stream, (const T *)lv.f, (T *)lv.x, lv.g, S.dL, S.dgv, nz);
+        plaunch(S.pdl && lv.g.pdl, k_chol_subst<T, NOISE>, 1, 1024, 0, S.stream, (const T *)lv.f, (T *)lv.x, lv.g, S.dL, S.dgv, nz);
         S.launches++;
     } else {
         // FP32 chain: FP32 factor products (the state itself is FP32);
@@ -465,10 +470,10 @@ static void launch_chol(Sampler &S, Level &lv, const NoiseArgs &nz) {
         typedef T MT;
         const i64 n = lv.geo.n;
         unsigned blocks = (unsigned)((n + 7) / 8);
-        plaunch(S.pdl, k_chol_gemv_lower<T, MT, NOISE>, blocks, 256, S.chol_smem, S.stream, (const T *)lv.f, lv.g,
+        plaunch(S.pdl && lv.g.pdl, k_chol_gemv_lower<T, MT, NOISE>, blocks, 256, S.chol_smem, S.stream, (const T *)lv.f, lv.g,
                                                                                 (const MT *)S.dLinv, S.chol_ld,
                                                                                 (MT *)S.dgv, nz);
-        plaunch(S.pdl, k_chol_gemv_upper<T, MT>, blocks, 256, S.chol_smem, S.stream, (const MT *)S.dgv, lv.g, (const MT *)S.dLinvT,
+        plaunch(S.pdl && lv.g.pdl, k_chol_gemv_upper<T, MT>, blocks, 256, S.chol_smem, S.stream, (const MT *)S.dgv, lv.g, (const MT *)S.dLinvT,
                                                                          S.chol_ld, (T *)lv.x);
         S.launches += 2;
     }
@@ -656,7 +661,7 @@ void Sampler::build_lowrank(int lev) {
             lr.y = lv.y;
             lr.part = lv.part;
             k_bt_partial<double><<<dim3(m, lv.bt_split), 256, 0, stream>>>(xs, lr);
-            k_lr_solve<NOISE_NONE, false><<<1, 256, 0, stream>>>(lr, lv.bt_split, nz);
+            k_lr_solve<NOISE_NONE, false><<<1, solve_block(m), 0, stream>>>(lr, lv.bt_split, nz);
             CK(cudaMemcpyAsync(yh.data(), lv.y, m * sizeof(double), cudaMemcpyDeviceToHost, stream));
             CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), stream));
             k_nonzeros<<<nblk(n, 256), 256, 0, stream>>>(xs, lv.g, nzi, nzv, cnt);
@@ -697,7 +702,13 @@ void Sampler::build_lowrank(int lev) {
         } else {
             C.val = upload(val);
         }
-        lv.Sinv[dir] = upload(small_inverse(Sh, m));
+        {
+            const std::vector<double> Si = small_inverse(Sh, m);
+            std::vector<double> SiT((size_t)m * m);
+            for (int a = 0; a < m; ++a)
+                for (int q = 0; q < m; ++q) SiT[(size_t)q * m + a] = Si[(size_t)a * m + q];
+            lv.SinvT[dir] = upload(SiT);
+        }
     }
     CK(cudaStreamSynchronize(stream));
 }
@@ -859,6 +870,10 @@ void Sampler::build(const mgmc_operator_desc &op) {
         lv.sd = std::sqrt(lv.diag * (2. - P.omega) / P.omega);
         lv.ncol = colour_count(dim, st);
         lv.npt = stencil_npt(lv.ncol, st);
+        // programmatic dependent launch pays off for the short kernels of
+        // the coarser levels; the many-CTA kernels of large levels run
+        // without its per-CTA wait
+        lv.g.pdl = geo.n <= PDL_MAX_POINTS ? 1 : 0;
         L.push_back(lv);
     }
     for (auto &lv : L) {
@@ -931,35 +946,60 @@ void Sampler::ensure_scratch(int lev) {
 }
 
 // host / device compact FP64 vector -> padded T array of level lev
+// Device address through which kernels can read or write a host array
+// directly: page-locked (cudaHostAlloc / cudaHostRegister) memory is mapped
+// into the device's address space, so the conversion kernels move the data
+// across the host link themselves (one pass, no staging copy); null for
+// pageable memory.
+static void *mapped_host(const void *p) {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return pa.type == cudaMemoryTypeHost ? pa.devicePointer : nullptr;
+}
+
+static dim3 pack_grid(const Level &lv) { return dim3((lv.g.N0 + 255) / 256, lv.g.N1, lv.g.N2); }
+
 static void put_vec(Sampler &S, int lev, const double *src, int on_device, void *dst) {
     Level &lv = S.L[lev];
     const i64 n = lv.geo.n;
     if (n > S.L[0].geo.n) fail(MGMC_ERR_INVALID_ARGUMENT, "level size");
     const double *d = src;
     if (!on_device) {
-        CK(cudaMemcpyAsync(S.d_cvec, src, n * sizeof(double), cudaMemcpyHostToDevice, S.stream));
-        d = S.d_cvec;
+        d = (const double *)mapped_host(src);
+        if (!d) {
+            CK(cudaMemcpyAsync(S.d_cvec, src, n * sizeof(double), cudaMemcpyHostToDevice, S.stream));
+            d = S.d_cvec;
+        }
     }
     if (S.fp32)
-        k_unpack<float><<<nblk(n, 256), 256, 0, S.stream>>>(d, (float *)dst, lv.g);
+        k_unpack<float><<<pack_grid(lv), 256, 0, S.stream>>>(d, (float *)dst, lv.g);
     else
-        k_unpack<double><<<nblk(n, 256), 256, 0, S.stream>>>(d, (double *)dst, lv.g);
+        k_unpack<double><<<pack_grid(lv), 256, 0, S.stream>>>(d, (double *)dst, lv.g);
     S.check_launch();
 }
 
 static void get_vec(Sampler &S, int lev, const void *src, double *dst, int on_device) {
     Level &lv = S.L[lev];
     const i64 n = lv.geo.n;
-    double *d = on_device ? dst : S.d_cvec;
-    if (S.fp32)
-        k_pack<float><<<nblk(n, 256), 256, 0, S.stream>>>((const float *)src, d, lv.g);
-    else
-        k_pack<double><<<nblk(n, 256), 256, 0, S.stream>>>((const double *)src, d, lv.g);
-    S.check_launch();
+    double *d = dst;
+    bool staged = false;
     if (!on_device) {
-        CK(cudaMemcpyAsync(dst, S.d_cvec, n * sizeof(double), cudaMemcpyDeviceToHost, S.stream));
-        CK(cudaStreamSynchronize(S.stream));
+        d = (double *)mapped_host(dst);
+        if (!d) {
+            d = S.d_cvec;
+            staged = true;
+        }
     }
+    if (S.fp32)
+        k_pack<float><<<pack_grid(lv), 256, 0, S.stream>>>((const float *)src, d, lv.g);
+    else
+        k_pack<double><<<pack_grid(lv), 256, 0, S.stream>>>((const double *)src, d, lv.g);
+    S.check_launch();
+    if (staged) CK(cudaMemcpyAsync(dst, S.d_cvec, n * sizeof(double), cudaMemcpyDeviceToHost, S.stream));
+    if (!on_device) CK(cudaStreamSynchronize(S.stream));
 }
 
 // Capture one step into a CUDA graph (Philox noise: the step's launches and

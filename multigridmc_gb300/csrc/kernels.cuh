@@ -41,6 +41,7 @@ __device__ __forceinline__ void pdl_begin() {
 struct Grid3 {
     int N0, N1, N2;  // interior vertices per direction
     i64 sy, sz;      // padded strides
+    int pdl = 0;     // kernels on this level take part in programmatic dependent launch
     __host__ __device__ i64 pad(int a, int b, int c) const { return (i64)(c + 1) * sz + (i64)(b + 1) * sy + (a + 1); }
     __host__ __device__ i64 compact(int a, int b, int c) const { return ((i64)c * N1 + b) * N0 + a; }
 };
@@ -211,7 +212,7 @@ __host__ __forceinline__ dim3 sweep_block(int count) {
 template <typename T, bool EXACT, int NOISE>
 __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_pass(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
                                                                StencilArg<T> s, int colour, int reverse, NoiseArgs nz) {
-    pdl_begin();
+    if (g.pdl) pdl_begin();
     const int b = blockIdx.y * blockDim.y + threadIdx.y;
     const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
     if (b >= g.N1) return;
@@ -232,7 +233,7 @@ template <int NOISE>
 __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict__ x, const float *__restrict__ f,
                                                               Grid3 g, StencilArg<float> s, int colour, int reverse,
                                                               NoiseArgs nz) {
-    pdl_begin();
+    if (g.pdl) pdl_begin();
     const int b = blockIdx.y * blockDim.y + threadIdx.y;
     const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -301,7 +302,7 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
 template <typename T, bool EXACT, int NOISE>
 __global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
                                                                 StencilArg<T> s, int colour, NoiseArgs nz) {
-    pdl_begin();
+    if (g.pdl) pdl_begin();
     const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
     const int a = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + pa;
     const int b = 2 * (blockIdx.y * blockDim.y + threadIdx.y) + pb, c = 2 * blockIdx.z + pc;
@@ -321,7 +322,7 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ 
 template <typename T, int NPT, bool EXACT, int NOISE>
 __global__ void __launch_bounds__(1024) k_sweep_wavefront(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
                                                            StencilArg<T> s, int forward, int hb, int hc, NoiseArgs nz) {
-    pdl_begin();
+    if (g.pdl) pdl_begin();
     const int tmax = (g.N0 - 1) + hb * (g.N1 - 1) + hc * (g.N2 - 1);
     const int npair = g.N1 * g.N2;
     for (int step = 0; step <= tmax; ++step) {
@@ -362,7 +363,7 @@ struct LowRankArg {
     const i64 *Bptr;    // m+1, CSC of B (padded indices)
     const i64 *Bidx;
     const double *Bval;
-    const double *Sinv; // m x m, S^{-1} = (Sigma + B^T M^{-1} B)^{-1}
+    const double *SinvT; // m x m, S^{-1} = (Sigma + B^T M^{-1} B)^{-1}, transposed (column q contiguous)
     const double *sigma_sqrt; // Sigma^{1/2}
     double *y;          // m scratch: B^T x
     double *z;          // m scratch: coefficients of C
@@ -405,127 +406,64 @@ __global__ void __launch_bounds__(256) k_bt_partial(const T *__restrict__ x, Low
     if (threadIdx.x == 0) lr.part[j * P + p] = acc;
 }
 
-// Warp sums of RW per-lane row partials; lane 0 writes rows
-// base + warp + NWARP r of z (and of its FP32 copy).
-template <int RW, int NWARP>
-__device__ __forceinline__ void store_rows(double (&t)[RW], const LowRankArg &lr, int m, int warp, int lane, int base) {
-#pragma unroll
-    for (int r = 0; r < RW; ++r) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t[r] += __shfl_xor_sync(0xffffffffu, t[r], o);
-        const int k = base + warp + NWARP * r;
-        if (lane == 0 && k < m) {
-            lr.z[k] = t[r];
-            if (lr.zf) lr.zf[k] = (float)t[r];
-        }
-    }
-}
-
-// One CTA of 256 threads: y_k = sum_p part[k * P + p] (fixed order, so the
-// result does not depend on block timing).  With SOLVE it then forms the
-// coefficients z of the correction x += C z,
+// One CTA: y_k = sum_p part[k * P + p] (fixed order, so the result does not
+// depend on block timing).  With SOLVE it then forms the coefficients z of
+// the correction x += C z,
 //   z = w - S^{-1} (y + G w) = S^{-1} (Sigma w - y) = S^{-1} (Sigma^{1/2} xi' - y)
 // with w = Sigma^{-1/2} xi' the low-rank noise of sor_sampler.cc:29-33,
 // G = B^T C and S = Sigma + G (so S - G = Sigma and a single m x m product
 // remains); with_noise == 0 gives z = -S^{-1} y, the smoother's correction
 // x -= Bbar B^T x of sor_smoother.cc:47-51, Bbar = C S^{-1}.
+// One thread per row k: FP64 arithmetic is scarce on this GPU, so every
+// FP64 instruction works on 32 different rows (no shuffle trees); S^{-1} is
+// stored transposed (SinvT[q * m + k]) so that a warp's loads of one column
+// q are contiguous.
 template <int NOISE, bool SOLVE>
 __global__ void __launch_bounds__(256) k_lr_solve(LowRankArg lr, int P, NoiseArgs nz) {
     pdl_begin();
     const int m = lr.m;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr int NWARP = 8, RW = 8, QC = 4;  // rows per warp and 32-column chunks per lane in one batch
     extern __shared__ double dyn[];
     double *u = dyn;
-    // Rows warp + NWARP r (r < RW) of S^{-1}, columns lane + 32 c (c < QC):
-    // for m <= 64 the whole matrix is loaded here, before the partial sums
-    // are combined, so that every load of the CTA is in flight at once.
-    const bool onebatch = SOLVE && m <= NWARP * RW && m <= 32 * QC;
-    double a[RW][QC];
-    if (onebatch) {
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        double pv[8];
+        double t = 0.0;
+        for (int q0 = 0; q0 < P; q0 += 8) {
 #pragma unroll
-        for (int r = 0; r < RW; ++r)
+            for (int r = 0; r < 8; ++r) pv[r] = q0 + r < P ? lr.part[(i64)k * P + q0 + r] : 0.0;
 #pragma unroll
-            for (int c = 0; c < QC; ++c) {
-                const int k = warp + NWARP * r, q = lane + 32 * c;
-                a[r][c] = (k < m && q < m) ? __ldg(lr.Sinv + (i64)k * m + q) : 0.0;
-            }
-    }
-    // y_k: warp per column, lanes over the P partial sums, eight columns in
-    // flight per warp; with SOLVE also u_k = Sigma_k^{1/2} xi'_k - y_k
-    for (int k0 = warp; k0 < m; k0 += 8 * NWARP) {
-        double t[8];
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            const int k = k0 + NWARP * r;
-            t[r] = 0.0;
-            if (k < m)
-                for (int q = lane; q < P; q += 32) t[r] += lr.part[(i64)k * P + q];
+            for (int r = 0; r < 8; ++r)
+                if (q0 + r < P) t += pv[r];
         }
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t[r] += __shfl_xor_sync(0xffffffffu, t[r], o);
-        }
-        if (lane < 8) {
-            const int k = k0 + NWARP * lane;
-            double tk = t[0];
-#pragma unroll
-            for (int r = 1; r < 8; ++r) tk = lane == r ? t[r] : tk;
-            if (k < m) {
-                lr.y[k] = tk;
-                if (SOLVE) {
-                    double xi = 0.0;
-                    if (NOISE == NOISE_PHILOX) {
-                        float4 rn = normals4(
-                            philox4x32_10(noise_ctr(nz, (unsigned)(k >> 2), PURPOSE_LOWRANK, 0), noise_key(nz)));
-                        xi = (double)pick(rn, k & 3);
-                    }
-                    if (NOISE == NOISE_INJECTED) xi = nz.buf[k];
-                    u[k] = lr.sigma_sqrt[k] * xi - tk;
-                }
+        lr.y[k] = t;
+        if (SOLVE) {
+            double xi = 0.0;
+            if (NOISE == NOISE_PHILOX) {
+                float4 rn = normals4(philox4x32_10(noise_ctr(nz, (unsigned)(k >> 2), PURPOSE_LOWRANK, 0), noise_key(nz)));
+                xi = (double)pick(rn, k & 3);
             }
+            if (NOISE == NOISE_INJECTED) xi = nz.buf[k];
+            u[k] = lr.sigma_sqrt[k] * xi - t;
         }
     }
     if (!SOLVE) return;
     __syncthreads();
-    // z = S^{-1} u: warp per row, RW rows per warp in flight
-    if (onebatch) {
-        double t[RW];
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        double t0 = 0.0, t1 = 0.0;
+        int q = 0;
+        for (; q + 16 <= m; q += 16) {
+            double sv[16];
 #pragma unroll
-        for (int r = 0; r < RW; ++r) {
-            t[r] = 0.0;
+            for (int r = 0; r < 16; ++r) sv[r] = __ldg(lr.SinvT + (i64)(q + r) * m + k);
 #pragma unroll
-            for (int c = 0; c < QC; ++c) {
-                const int q = lane + 32 * c;
-                if (q < m) t[r] += a[r][c] * u[q];
+            for (int r = 0; r < 16; r += 2) {
+                t0 = fma(sv[r], u[q + r], t0);
+                t1 = fma(sv[r + 1], u[q + r + 1], t1);
             }
         }
-        store_rows<RW, NWARP>(t, lr, m, warp, lane, 0);
-    } else {
-        for (int k0 = warp; k0 < m; k0 += RW * NWARP) {
-            double t[RW];
-#pragma unroll
-            for (int r = 0; r < RW; ++r) t[r] = 0.0;
-            for (int q0 = 0; q0 < m; q0 += 32 * QC) {
-                double b[RW][QC];
-#pragma unroll
-                for (int r = 0; r < RW; ++r)
-#pragma unroll
-                    for (int c = 0; c < QC; ++c) {
-                        const int k = k0 + NWARP * r, q = q0 + lane + 32 * c;
-                        b[r][c] = (k < m && q < m) ? __ldg(lr.Sinv + (i64)k * m + q) : 0.0;
-                    }
-#pragma unroll
-                for (int r = 0; r < RW; ++r)
-#pragma unroll
-                    for (int c = 0; c < QC; ++c) {
-                        const int q = q0 + lane + 32 * c;
-                        if (q < m) t[r] += b[r][c] * u[q];
-                    }
-            }
-            store_rows<RW, NWARP>(t, lr, m, warp, lane, k0 - warp);
-        }
+        for (; q < m; ++q) t0 = fma(__ldg(lr.SinvT + (i64)q * m + k), u[q], t0);
+        const double zk = t0 + t1;
+        lr.z[k] = zk;
+        if (lr.zf) lr.zf[k] = (float)zk;
     }
 }
 
@@ -565,7 +503,7 @@ template <typename T, int NPT>
 __global__ void __launch_bounds__(256) k_resid_restrict(const T *__restrict__ x, const T *__restrict__ f,
                                                          T *__restrict__ fc, Grid3 gf, Grid3 gc, StencilArg<T> s,
                                                          int dim) {
-    pdl_begin();
+    if (gf.pdl) pdl_begin();
     i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     i64 nc = (i64)gc.N0 * gc.N1 * gc.N2;
     if (t >= nc) return;
@@ -615,7 +553,7 @@ template <typename T, int NPT>
 __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tiled(const T *__restrict__ x, const T *__restrict__ f,
                                                                       T *__restrict__ fc, Grid3 gf, Grid3 gc,
                                                                       StencilArg<T> s) {
-    pdl_begin();
+    if (gf.pdl) pdl_begin();
     extern __shared__ __align__(16) unsigned char rr_smem[];
     T *xs = reinterpret_cast<T *>(rr_smem);             // [RR_XD][RR_XH][RR_XW]
     T *rs = xs + RR_XW * RR_XH * RR_XD;                  // [RR_FD][RR_FH][RR_FW]
@@ -747,7 +685,7 @@ __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tma(const __grid_
                                                                    const __grid_constant__ CUtensorMap fmap,
                                                                    T *__restrict__ fc, Grid3 gf, Grid3 gc,
                                                                    StencilArg<T> s, unsigned *__restrict__ err) {
-    pdl_begin();
+    if (gf.pdl) pdl_begin();
     extern __shared__ __align__(1024) unsigned char rr_tma_smem[];
     __shared__ unsigned long long bar;
     T *xs = reinterpret_cast<T *>(rr_tma_smem);                      // [RR_XD][RR_XH][RR_BW]
@@ -832,7 +770,7 @@ __global__ void __launch_bounds__(256) k_add_Bq(T *__restrict__ dst, i64 nrows, 
 template <typename T>
 __global__ void __launch_bounds__(128) k_prolong_add(T *__restrict__ x, const T *__restrict__ xc, Grid3 gf, Grid3 gc,
                                                       T alpha, int dim) {
-    pdl_begin();
+    if (gf.pdl) pdl_begin();
     // coarse cell (i, j, k), 0 <= i <= Nc0 etc., owns the fine vertices with
     // 1-based coordinates 2 i + {0, 1} (those inside the interior); its
     // corners are the coarse vertices i, i+1 (1-based, ghosts are zero)
@@ -896,7 +834,7 @@ __global__ void __launch_bounds__(128) k_prolong_add(T *__restrict__ x, const T 
 template <typename T>
 __global__ void __launch_bounds__(256) k_apply_stencil(const T *__restrict__ x, T *__restrict__ y, Grid3 g,
                                                         StencilArg<T> s) {
-    pdl_begin();
+    if (g.pdl) pdl_begin();
     i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     i64 n = (i64)g.N0 * g.N1 * g.N2;
     if (t >= n) return;
@@ -911,28 +849,24 @@ __global__ void __launch_bounds__(256) k_apply_stencil(const T *__restrict__ x, 
 
 // ---------------------------------------------------- layout conversion
 template <typename T>
-__global__ void k_unpack(const double *__restrict__ src, T *__restrict__ dst, Grid3 g) {
-    pdl_begin();
-    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    i64 n = (i64)g.N0 * g.N1 * g.N2;
-    if (t >= n) return;
-    int a = (int)(t % g.N0), b = (int)((t / g.N0) % g.N1), c = (int)(t / ((i64)g.N0 * g.N1));
-    dst[g.pad(a, b, c)] = (T)src[t];
+__global__ void __launch_bounds__(256) k_unpack(const double *__restrict__ src, T *__restrict__ dst, Grid3 g) {
+    if (g.pdl) pdl_begin();
+    const int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y, c = blockIdx.z;
+    if (a >= g.N0) return;
+    dst[g.pad(a, b, c)] = (T)src[((i64)c * g.N1 + b) * g.N0 + a];
 }
 
 template <typename T>
-__global__ void k_pack(const T *__restrict__ src, double *__restrict__ dst, Grid3 g) {
-    pdl_begin();
-    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    i64 n = (i64)g.N0 * g.N1 * g.N2;
-    if (t >= n) return;
-    int a = (int)(t % g.N0), b = (int)((t / g.N0) % g.N1), c = (int)(t / ((i64)g.N0 * g.N1));
-    dst[t] = (double)src[g.pad(a, b, c)];
+__global__ void __launch_bounds__(256) k_pack(const T *__restrict__ src, double *__restrict__ dst, Grid3 g) {
+    if (g.pdl) pdl_begin();
+    const int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y, c = blockIdx.z;
+    if (a >= g.N0) return;
+    dst[((i64)c * g.N1 + b) * g.N0 + a] = (double)src[g.pad(a, b, c)];
 }
 
 template <typename T>
 __global__ void k_zero_interior(T *__restrict__ x, Grid3 g) {
-    pdl_begin();
+    if (g.pdl) pdl_begin();
     i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     i64 n = (i64)g.N0 * g.N1 * g.N2;
     if (t >= n) return;
@@ -949,7 +883,7 @@ template <typename T, int NOISE>
 __global__ void __launch_bounds__(1024) k_chol_subst(const T *__restrict__ f, T *__restrict__ x, Grid3 g,
                                                       const double *__restrict__ L, double *__restrict__ gv,
                                                       NoiseArgs nz) {
-    pdl_begin();
+    if (g.pdl) pdl_begin();
     const i64 n = (i64)g.N0 * g.N1 * g.N2;
     for (i64 i = threadIdx.x; i < n; i += blockDim.x) {
         int a = (int)(i % g.N0), b = (int)((i / g.N0) % g.N1), c = (int)(i / ((i64)g.N0 * g.N1));
@@ -1043,7 +977,7 @@ __device__ __forceinline__ MT warp_row_dot(const MT *__restrict__ row, const MT 
 template <typename T, typename MT, int NOISE>
 __global__ void __launch_bounds__(256) k_chol_gemv_lower(const T *__restrict__ f, Grid3 g, const MT *__restrict__ Linv,
                                                           int ld, MT *__restrict__ v, NoiseArgs nz) {
-    pdl_begin();
+    if (g.pdl) pdl_begin();
     extern __shared__ __align__(16) unsigned char chol_sm[];
     MT *fs = reinterpret_cast<MT *>(chol_sm);
     const int n = g.N0 * g.N1 * g.N2;
@@ -1078,7 +1012,7 @@ __global__ void __launch_bounds__(256) k_chol_gemv_lower(const T *__restrict__ f
 template <typename T, typename MT>
 __global__ void __launch_bounds__(256) k_chol_gemv_upper(const MT *__restrict__ v, Grid3 g,
                                                           const MT *__restrict__ LinvT, int ld, T *__restrict__ x) {
-    pdl_begin();
+    if (g.pdl) pdl_begin();
     extern __shared__ __align__(16) unsigned char chol_sm[];
     MT *vs = reinterpret_cast<MT *>(chol_sm);
     const int n = g.N0 * g.N1 * g.N2;
