@@ -95,6 +95,7 @@ struct Sampler {
     int dim = 3, m = 0;
     bool fp32 = false, exact = false;
     bool pdl = true;  // programmatic dependent launch between step kernels (MGMC_NO_PDL=1 turns it off)
+    bool march = true;  // plane-marching FP32 fine sweep (MGMC_SWEEP_MARCH=0: one plane per CTA)
     int noise_mode = NOISE_PHILOX;
     std::vector<Level> L;
     std::vector<double> Sigma;
@@ -244,6 +245,17 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
         for (int pass = 0; pass < 2; ++pass) {
             const int colour = forward ? pass : 1 - pass;
             if constexpr (std::is_same<T, float>::value) {
+                if (vec && S.march) {
+                    const int ngrp = (lv.g.N0 + 8) / 8;
+                    const dim3 blk = sweep_block(ngrp);
+                    dim3 grid((ngrp + blk.x - 1) / blk.x, (lv.g.N1 + blk.y - 1) / blk.y, (lv.g.N2 + RB_CZ - 1) / RB_CZ);
+                    if (pass == 0)
+                        plaunch(S.pdl && lv.g.pdl, k_sweep_rb_march<NOISE, false>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, nz);
+                    else
+                        plaunch(S.pdl && lv.g.pdl, k_sweep_rb_march<NOISE, true>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, nz);
+                    S.launches++;
+                    continue;
+                }
                 if (vec) {
                     const int ngrp = (lv.g.N0 + 8) / 8;
                     const dim3 blk = sweep_block(ngrp);
@@ -313,7 +325,9 @@ static void launch_sweep(Sampler &S, const Level &lv, bool forward, int noise, v
 }
 
 // threads of the one-CTA low-rank solve: one per row, up to 256
-static unsigned solve_block(int m) { return (unsigned)std::min(256, std::max(32, (m + 31) / 32 * 32)); }
+static unsigned solve_block(int) { return 256u; }
+// its dynamic shared memory: u (m) and the partial products (256)
+static size_t solve_smem(int m) { return sizeof(double) * ((size_t)m + 256); }
 
 template <typename T>
 static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, const NoiseArgs &nz) {
@@ -329,7 +343,7 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     lr.y = lv.y;
     lr.z = lv.z;
     lr.part = lv.part;
-    const size_t smem = sizeof(double) * S.m;
+    const size_t smem = solve_smem(S.m);
     plaunch(S.pdl, k_bt_partial<T>, dim3(S.m, lv.bt_split), 256, 0, S.stream, (const T *)x, lr);
     if (noise == NOISE_NONE)
         plaunch(S.pdl, k_lr_solve<NOISE_NONE, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
@@ -826,6 +840,8 @@ void Sampler::build(const mgmc_operator_desc &op) {
     {
         const char *e = std::getenv("MGMC_NO_PDL");
         pdl = !(e && e[0] == '1');
+        const char *mch = std::getenv("MGMC_SWEEP_MARCH");
+        march = !(mch && mch[0] == '0');
     }
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaFuncSetAttribute(k_resid_restrict_tiled<double, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -29,13 +29,12 @@ namespace mgmc {
 typedef long long i64;
 typedef unsigned long long u64;
 
-// Programmatic dependent launch: let the next kernel on the stream be
-// scheduled now, then wait until the previous kernel has completed and its
-// writes are visible.  Without the launch attribute both are no-ops.
-__device__ __forceinline__ void pdl_begin() {
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-}
+// Programmatic dependent launch: wait until the previous kernel on the
+// stream has completed and its writes are visible (a kernel launched with
+// the programmatic-serialization attribute may start while its predecessor
+// drains; the predecessor triggers it implicitly as its CTAs exit).  Without
+// the attribute this is a no-op.
+__device__ __forceinline__ void pdl_begin() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // ------------------------------------------------------------- geometry
 struct Grid3 {
@@ -282,7 +281,7 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
         res = fmaf(s.w[22], zp[j], res);
         float cval = fv[j];
         if (NOISE != NOISE_NONE) cval = fmaf(s.sd, xi, cval);
-        x[rb + P0 + j] = v[j + 1] + s.omega_diag * (cval - res);
+        v[j + 1] = v[j + 1] + s.omega_diag * (cval - res);  // neighbours are of the other colour
     };
     if (j0 == 0) {
         upd(0, 0);
@@ -294,6 +293,127 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
         upd(3, 1);
         upd(5, 2);
         upd(7, 3);
+    }
+    // Whole 8-position spans go back as two float4 stores (full sectors
+    // instead of one partial sector per point); the other colour's values
+    // are rewritten unchanged -- no thread writes them in this pass.  A span
+    // that reaches past its row (short rows only) stores its second half
+    // point by point.
+    float4 *xo = reinterpret_cast<float4 *>(x + rb + P0);
+    xo[0] = make_float4(v[1], v[2], v[3], v[4]);
+    if (P0 + 8 <= g.sy) {
+        xo[1] = make_float4(v[5], v[6], v[7], v[8]);
+    } else {
+#pragma unroll
+        for (int j = 4; j < 8; ++j) {
+            const int a = P0 + j - 1;
+            if (((j - j0) & 1) == 0 && a >= 0 && a < g.N0) x[rb + P0 + j] = v[j + 1];
+        }
+    }
+}
+
+// Plane-marching FP32 variant: a thread owns the 8-position span [8q, 8q+8)
+// of row b and walks RB_CZ consecutive planes (upwards, or downwards with
+// REV), keeping the spans of the planes below, at and above the current one
+// in registers; per plane it loads the next plane's span, the two y-neighbour
+// spans (mostly L1 hits: they are other warps' own spans) and f, updates the
+// 4 points of the colour and stores the span as two float4.  Points of one
+// colour only have neighbours of the other colour, so the in-register spans
+// stay valid while the walk proceeds.
+constexpr int RB_CZ = 8;
+
+__device__ __forceinline__ void ld8(const float *p, float *r) {
+    const float4 a = reinterpret_cast<const float4 *>(p)[0], b = reinterpret_cast<const float4 *>(p)[1];
+    r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+    r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+}
+
+template <int NOISE, bool REV>
+__global__ void __launch_bounds__(RBP_THREADS, 3) k_sweep_rb_march(float *__restrict__ x, const float *__restrict__ f,
+                                                                Grid3 g, StencilArg<float> s, int colour, NoiseArgs nz) {
+    if (g.pdl) pdl_begin();
+    const int b = blockIdx.y * blockDim.y + threadIdx.y;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ngrp = (g.N0 + 8) >> 3;
+    if (q >= ngrp || b >= g.N1) return;
+    const int P0 = 8 * q;
+    const int chunk = REV ? (int)gridDim.z - 1 - (int)blockIdx.z : (int)blockIdx.z;
+    const int cA = chunk * RB_CZ, cB = min(g.N2, cA + RB_CZ);  // planes [cA, cB)
+    constexpr int d = REV ? -1 : 1;
+    const i64 rowoff = (i64)(b + 1) * g.sy + P0;
+    // span of plane cc (cc = -1 and cc = N2 are the zero ghost planes)
+    auto span = [&](int cc) { return x + (i64)(cc + 1) * g.sz + rowoff; };
+    float behind[8], v[10], ahead[8];  // planes c - d, c (with the x-halo), c + d
+    int c = REV ? cB - 1 : cA;
+    ld8(span(c - d), behind);
+    ld8(span(c), v + 1);
+    ld8(span(c + d), ahead);
+    const int cend = REV ? cA - 1 : cB;
+    for (; c != cend; c += d) {
+        const float *rc = span(c);
+        float ym[8], yp[8], fv[8];
+        ld8(rc - g.sy, ym);
+        ld8(rc + g.sy, yp);
+        ld8(f + (rc - x), fv);
+        v[0] = P0 > 0 ? rc[-1] : 0.f;
+        v[9] = rc[8];
+        const float(&zm)[8] = REV ? ahead : behind;  // plane c - 1
+        const float(&zp)[8] = REV ? behind : ahead;  // plane c + 1
+        const int j0 = (colour + b + c + 1) & 1;
+        float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (NOISE == NOISE_PHILOX) nrm = fine_normals(nz, g, P0 + j0, b, c);
+        auto upd = [&](int j, int k) {
+            const int a = P0 + j - 1;
+            if (a < 0 || a >= g.N0) return;
+            float xi = 0.f;
+            if (NOISE == NOISE_PHILOX) xi = pick(nrm, k);
+            if (NOISE == NOISE_INJECTED) xi = (float)nz.buf[g.compact(a, b, c)];
+            float res = s.w[4] * zm[j];
+            res = fmaf(s.w[10], ym[j], res);
+            res = fmaf(s.w[12], v[j], res);
+            res = fmaf(s.w[13], v[j + 1], res);
+            res = fmaf(s.w[14], v[j + 2], res);
+            res = fmaf(s.w[16], yp[j], res);
+            res = fmaf(s.w[22], zp[j], res);
+            float cval = fv[j];
+            if (NOISE != NOISE_NONE) cval = fmaf(s.sd, xi, cval);
+            v[j + 1] = v[j + 1] + s.omega_diag * (cval - res);
+        };
+        if (j0 == 0) {
+            upd(0, 0);
+            upd(2, 1);
+            upd(4, 2);
+            upd(6, 3);
+        } else {
+            upd(1, 0);
+            upd(3, 1);
+            upd(5, 2);
+            upd(7, 3);
+        }
+        float4 *xo = reinterpret_cast<float4 *>(const_cast<float *>(rc));
+        xo[0] = make_float4(v[1], v[2], v[3], v[4]);
+        if (P0 + 8 <= g.sy) {
+            xo[1] = make_float4(v[5], v[6], v[7], v[8]);
+        } else {
+#pragma unroll
+            for (int j = 4; j < 8; ++j) {
+                const int a = P0 + j - 1;
+                if (((j - j0) & 1) == 0 && a >= 0 && a < g.N0) x[(rc - x) + j] = v[j + 1];
+            }
+        }
+        // walk one plane: behind <- current, current <- ahead, ahead <- next
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            behind[j] = v[j + 1];
+            v[j + 1] = ahead[j];
+        }
+        const int cn = c + 2 * d;
+        if (cn >= -1 && cn <= g.N2) {
+            ld8(span(cn), ahead);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) ahead[j] = 0.f;
+        }
     }
 }
 
@@ -423,7 +543,11 @@ __global__ void __launch_bounds__(256) k_lr_solve(LowRankArg lr, int P, NoiseArg
     pdl_begin();
     const int m = lr.m;
     extern __shared__ double dyn[];
-    double *u = dyn;
+    double *u = dyn;                 // m
+    double *acc = dyn + m;           // [tpr][rows] partial products
+    // rows handled at once and threads per row (blockDim.x = 256)
+    const int rows = m < 256 ? m : 256;
+    const int tpr = 256 / rows;
     for (int k = threadIdx.x; k < m; k += blockDim.x) {
         double pv[8];
         double t = 0.0;
@@ -447,23 +571,36 @@ __global__ void __launch_bounds__(256) k_lr_solve(LowRankArg lr, int P, NoiseArg
     }
     if (!SOLVE) return;
     __syncthreads();
-    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    // z = S^{-1} u: thread (g, k) of g < tpr sums the columns q = g, g + tpr, ...
+    // of row k (loads of one column contiguous over k), in batches of 8
+    // loads issued together; the tpr partial sums are then added in order g.
+    const int g = threadIdx.x / rows, kk = threadIdx.x % rows;
+    for (int k0 = 0; k0 < m; k0 += rows) {
+        const int k = k0 + kk;
         double t0 = 0.0, t1 = 0.0;
-        int q = 0;
-        for (; q + 16 <= m; q += 16) {
-            double sv[16];
+        if (g < tpr && k < m) {
+            int q = g;
+            for (; q + 7 * tpr < m; q += 8 * tpr) {
+                double sv[8];
 #pragma unroll
-            for (int r = 0; r < 16; ++r) sv[r] = __ldg(lr.SinvT + (i64)(q + r) * m + k);
+                for (int r = 0; r < 8; ++r) sv[r] = __ldg(lr.SinvT + (i64)(q + r * tpr) * m + k);
 #pragma unroll
-            for (int r = 0; r < 16; r += 2) {
-                t0 = fma(sv[r], u[q + r], t0);
-                t1 = fma(sv[r + 1], u[q + r + 1], t1);
+                for (int r = 0; r < 8; r += 2) {
+                    t0 = fma(sv[r], u[q + r * tpr], t0);
+                    t1 = fma(sv[r + 1], u[q + (r + 1) * tpr], t1);
+                }
             }
+            for (; q < m; q += tpr) t0 = fma(__ldg(lr.SinvT + (i64)q * m + k), u[q], t0);
+            acc[g * rows + kk] = t0 + t1;
         }
-        for (; q < m; ++q) t0 = fma(__ldg(lr.SinvT + (i64)q * m + k), u[q], t0);
-        const double zk = t0 + t1;
-        lr.z[k] = zk;
-        if (lr.zf) lr.zf[k] = (float)zk;
+        __syncthreads();
+        if (threadIdx.x < rows && k0 + threadIdx.x < m) {
+            double zk = 0.0;
+            for (int h = 0; h < tpr; ++h) zk += acc[h * rows + threadIdx.x];
+            lr.z[k0 + threadIdx.x] = zk;
+            if (lr.zf) lr.zf[k0 + threadIdx.x] = (float)zk;
+        }
+        __syncthreads();
     }
 }
 
