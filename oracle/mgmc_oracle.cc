@@ -12,14 +12,18 @@
 // the library is compiled with -ffp-contract=off so that no FMA contraction
 // changes rounding.
 //
-// Parity status: the reference cannot be compiled here (Eigen >= 5.0,
-// libconfig++, LAPACKE, googletest absent, no network).  The oracle is
-// pinned by the reference's own known-answer and property tests
+// Parity status: the reference's sampling path cannot be compiled here
+// (Eigen >= 5.0, libconfig++, LAPACKE, googletest absent, no network).  The
+// oracle is pinned by the reference's own known-answer and property tests
 // (lattice index maps, quadrature, CLCG serial/leapfrog agreement,
 // Statistics on an AR(1) process, intergrid adjointness, smoother fixed
 // point, sampler mean/covariance against the exact covariance), restated in
-// tests/test_oracle_*.py.  Pathwise chain values of the reference itself are
-// unpinned: no reference binary can be run to produce them.
+// tests/test_oracle_*.py, and its random number generator is compared draw
+// by draw (integers, uniforms, normals; serial and leapfrog) with the
+// reference's own CLCGenerator compiled from its sources (oracle/
+// build_ref.py), the one part of the path that builds without Eigen.
+// Pathwise chain values of the reference itself are unpinned: no reference
+// binary of the sampler can be run to produce them.
 //
 // Deviations, both deliberate and documented:
 //  * the coarse-level Cholesky sampler factorises in natural order, which is

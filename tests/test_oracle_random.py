@@ -69,3 +69,44 @@ def test_polar_method_pairs():
                 break
         L = sqrt(-2 * log(s) / s)
         assert z[2 * p] == L * u1 and z[2 * p + 1] == L * u2
+
+
+def _reference_rng():
+    """The reference's own CLCGenerator, compiled from its sources by
+    oracle/build_ref.py (present only where the reference sources are)."""
+    import ctypes as C
+    import os
+    import pytest
+    from oracle import build_ref
+    path = build_ref.build()
+    if path is None or not os.path.exists(path):
+        pytest.skip("reference sources not available: reference RNG not built")
+    L = C.CDLL(path)
+    L.ref_clcg_create.restype = C.c_void_p
+    L.ref_clcg_destroy.argtypes = [C.c_void_p]
+    L.ref_clcg_draw_int.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_int32)]
+    L.ref_clcg_draw_uniform.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_double)]
+    L.ref_clcg_draw_normal.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_double)]
+    L.ref_clcg_leapfrog_ints.argtypes = [C.c_int, C.c_int64, C.POINTER(C.c_int32)]
+    L.ref_clcg_leapfrog_ints.restype = C.c_int
+    return L, C
+
+
+def test_oracle_rng_equals_reference_build():
+    """Draw-by-draw equality with the reference's own generator: integers,
+    uniforms and polar-method normals (bitwise), serial and leapfrog."""
+    L, C = _reference_rng()
+    n = 200000
+    for kind, ctype, dtype in (("int", C.c_int32, np.int32), ("uniform", C.c_double, np.float64),
+                               ("normal", C.c_double, np.float64)):
+        h = L.ref_clcg_create()
+        ref = np.zeros(n, dtype=dtype)
+        getattr(L, f"ref_clcg_draw_{kind}")(h, n, ref.ctypes.data_as(C.POINTER(ctype)))
+        L.ref_clcg_destroy(h)
+        mine = getattr(O.CLCG(), f"draw_{kind}")(n)
+        assert np.array_equal(np.asarray(mine), ref), kind
+    nthreads, m = 4, 1000
+    ref = np.zeros(nthreads * m, dtype=np.int32)
+    got = L.ref_clcg_leapfrog_ints(nthreads, m, ref.ctypes.data_as(C.POINTER(C.c_int32)))
+    for t in range(got):
+        assert np.array_equal(O.CLCG(got, t).draw_int(m), ref[t * m:(t + 1) * m]), f"thread {t} of {got}"
