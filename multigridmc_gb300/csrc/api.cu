@@ -240,6 +240,17 @@ static void plaunch(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, s
     CK(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
 }
 
+// Raise a kernel's dynamic shared memory limit to at least `bytes`.  The
+// limit belongs to the kernel and is shared by every sampler and level of
+// the process, so it is only ever raised.
+template <typename... KArgs>
+static void raise_smem_limit(void (*kernel)(KArgs...), size_t bytes) {
+    cudaFuncAttributes fa;
+    CK(cudaFuncGetAttributes(&fa, kernel));
+    if ((int)bytes > fa.maxDynamicSharedSizeBytes)
+        CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
 // ----------------------------------------------------------- sweep launch
 template <typename T, bool EXACT, int NOISE>
 static void launch_colour_passes(Sampler &S, const Level &lv, bool forward, T *x, const T *f, const StencilArg<T> &s,
@@ -646,7 +657,14 @@ void Sampler::smooth_cluster(int lev, int nsweep, unsigned dirs) {
 template <typename T, bool EXACT, int NOISE>
 static bool cluster_fits(int NC, size_t smem) {
     auto k = k_level_smooth_cluster<T, EXACT, NOISE>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+    // the attribute belongs to the kernel, shared by every level: only raise it
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, k) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    const int want = std::max(fa.maxDynamicSharedSizeBytes, (int)smem);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, want) != cudaSuccess ||
         cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
         cudaGetLastError();
         return false;
@@ -986,12 +1004,12 @@ void Sampler::build_coarse() {
         dLinvT = put(true);
         dLinv = put(false);
         if (chol_smem > 48 * 1024) {
-            CK(cudaFuncSetAttribute(k_chol_gemv_lower<float, float, NOISE_PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
-            CK(cudaFuncSetAttribute(k_chol_gemv_lower<double, double, NOISE_PHILOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
-            CK(cudaFuncSetAttribute(k_chol_gemv_lower<float, float, NOISE_INJECTED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
-            CK(cudaFuncSetAttribute(k_chol_gemv_lower<double, double, NOISE_INJECTED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
-            CK(cudaFuncSetAttribute(k_chol_gemv_upper<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
-            CK(cudaFuncSetAttribute(k_chol_gemv_upper<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chol_smem));
+            raise_smem_limit(k_chol_gemv_lower<float, float, NOISE_PHILOX>, chol_smem);
+            raise_smem_limit(k_chol_gemv_lower<double, double, NOISE_PHILOX>, chol_smem);
+            raise_smem_limit(k_chol_gemv_lower<float, float, NOISE_INJECTED>, chol_smem);
+            raise_smem_limit(k_chol_gemv_lower<double, double, NOISE_INJECTED>, chol_smem);
+            raise_smem_limit(k_chol_gemv_upper<float, float>, chol_smem);
+            raise_smem_limit(k_chol_gemv_upper<double, double>, chol_smem);
         }
     }
 }
@@ -1070,14 +1088,10 @@ void Sampler::build(const mgmc_operator_desc &op) {
         pdl = !(e && e[0] == '1');
     }
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-    CK(cudaFuncSetAttribute(k_resid_restrict_tiled<double, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)rr_smem_bytes<double>()));
-    CK(cudaFuncSetAttribute(k_resid_restrict_tiled<double, 27>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)rr_smem_bytes<double>()));
-    CK(cudaFuncSetAttribute(k_resid_restrict_tma<double, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)rr_tma_smem_bytes<double>()));
-    CK(cudaFuncSetAttribute(k_resid_restrict_tma<double, 27>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)rr_tma_smem_bytes<double>()));
+    raise_smem_limit(k_resid_restrict_tiled<double, 7>, rr_smem_bytes<double>());
+    raise_smem_limit(k_resid_restrict_tiled<double, 27>, rr_smem_bytes<double>());
+    raise_smem_limit(k_resid_restrict_tma<double, 7>, rr_tma_smem_bytes<double>());
+    raise_smem_limit(k_resid_restrict_tma<double, 27>, rr_tma_smem_bytes<double>());
     d_step = alloc<u64>(1);
     d_obs_count = alloc<u64>(1);
     d_err = alloc<unsigned>(1);
