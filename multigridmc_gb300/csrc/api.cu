@@ -223,6 +223,7 @@ NoiseArgs Sampler::noise_args(int lev, i64 count) {
 // completed and flushed.  This hides the launch latency between the short
 // dependent kernels of a multigrid step.
 constexpr i64 PDL_MAX_POINTS = i64(1) << 22;
+constexpr i64 CL_MAX_POINTS = i64(1) << 17;  // largest level smoothed inside one cluster
 
 template <typename... KArgs, typename... Args>
 static void plaunch(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
@@ -301,10 +302,10 @@ static void launch_colour_passes(Sampler &S, const Level &lv, bool forward, T *x
     for (int cc = 0; cc < lv.ncol; ++cc) {
         const int colour = forward ? cc : lv.ncol - 1 - cc;
         const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
-        const int na = (lv.g.N0 - pa + 1) / 2, nb = (lv.g.N1 - pb + 1) / 2, nc = (lv.g.N2 - pc + 1) / 2;
-        if (na <= 0 || nb <= 0 || nc <= 0) continue;
-        const dim3 blk = sweep_block(na);
-        dim3 grid((na + blk.x - 1) / blk.x, (nb + blk.y - 1) / blk.y, nc);
+        const int ngx = (lv.g.N0 - pa + 7) / 8, nb = (lv.g.N1 - pb + 1) / 2, nc = (lv.g.N2 - pc + 1) / 2;
+        if (ngx <= 0 || nb <= 0 || nc <= 0) continue;
+        const dim3 blk = sweep_block(ngx);
+        dim3 grid((ngx + blk.x - 1) / blk.x, (nb + blk.y - 1) / blk.y, nc);
         plaunch(S.pdl && lv.g.pdl, k_sweep_c27_pass<T, EXACT, NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, nz);
         S.launches++;
     }
@@ -702,6 +703,11 @@ void Sampler::build_cluster(int lev) {
     if (dim != 3 || lev == 0 || lev + 1 >= (int)L.size() || lv.npt != 27 || P.ordering != MGMC_ORDER_MULTICOLOUR ||
         m > CL_MAX_M || nsw > CL_MAX_SWEEPS)
         return;
+    // Larger levels have more work per colour than CL_MAX_NC SMs finish
+    // faster than the per-colour launches on the whole GPU.
+    i64 max_points = CL_MAX_POINTS;
+    if (const char *e = std::getenv("MGMC_CLUSTER_MAX_POINTS")) max_points = std::atoll(e);
+    if (lv.geo.n > max_points) return;
     const int NC = std::min(CL_MAX_NC, lv.g.N2);
     const size_t smem = fp32 ? cl_smem_bytes<float>(lv.g, NC) : cl_smem_bytes<double>(lv.g, NC);
     if (smem > 227 * 1024) return;
