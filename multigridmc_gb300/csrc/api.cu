@@ -302,10 +302,10 @@ static void launch_colour_passes(Sampler &S, const Level &lv, bool forward, T *x
     for (int cc = 0; cc < lv.ncol; ++cc) {
         const int colour = forward ? cc : lv.ncol - 1 - cc;
         const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
-        const int ngx = (lv.g.N0 - pa + 7) / 8, nb = (lv.g.N1 - pb + 1) / 2, nc = (lv.g.N2 - pc + 1) / 2;
-        if (ngx <= 0 || nb <= 0 || nc <= 0) continue;
-        const dim3 blk = sweep_block(ngx);
-        dim3 grid((ngx + blk.x - 1) / blk.x, (nb + blk.y - 1) / blk.y, nc);
+        const int na = (lv.g.N0 - pa + 1) / 2, nb = (lv.g.N1 - pb + 1) / 2, nc = (lv.g.N2 - pc + 1) / 2;
+        if (na <= 0 || nb <= 0 || nc <= 0) continue;
+        const dim3 blk = sweep_block(na);
+        dim3 grid((na + blk.x - 1) / blk.x, (nb + blk.y - 1) / blk.y, nc);
         plaunch(S.pdl && lv.g.pdl, k_sweep_c27_pass<T, EXACT, NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, nz);
         S.launches++;
     }
@@ -708,7 +708,9 @@ void Sampler::build_cluster(int lev) {
     i64 max_points = CL_MAX_POINTS;
     if (const char *e = std::getenv("MGMC_CLUSTER_MAX_POINTS")) max_points = std::atoll(e);
     if (lv.geo.n > max_points) return;
-    const int NC = std::min(CL_MAX_NC, lv.g.N2);
+    // about four planes per CTA: fewer CTAs read fewer remote planes and
+    // meet at cheaper cluster barriers
+    const int NC = std::min(CL_MAX_NC, std::max(1, lv.g.N2 / 4));
     const size_t smem = fp32 ? cl_smem_bytes<float>(lv.g, NC) : cl_smem_bytes<double>(lv.g, NC);
     if (smem > 227 * 1024) return;
     bool ok;

@@ -313,68 +313,21 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
     }
 }
 
-// The (up to) four points a0 + 2j (j < 4, a < N0) of one colour in the
-// 8-aligned x-group of row (b, c), a0 = 8 grp + (colour & 1): every row of
-// the 3x3x3 neighbourhood is read once as 9 consecutive values (padded
-// positions a0 .. a0 + 8) and serves all four points, and one Philox block
-// gives their four normals.  pl[dz] is the base of plane c + dz - 1 (null: a
-// zero ghost plane that is not stored); the row of b + dy - 1 starts at
-// pl[dz] + (b + dy) sy.  Per point the arithmetic and its order are those of
-// sor_point<T, 27, EXACT>.
-template <typename T, bool EXACT, int NOISE>
-__device__ __forceinline__ void c27_update4(const T *const (&pl)[3], const T *__restrict__ f, const Grid3 &g,
-                                            const StencilArg<T> &s, int a0, int b, int c, const NoiseArgs &nz) {
-    typedef Ar<EXACT> Ops;
-    T res[4] = {T(0), T(0), T(0), T(0)};
-#pragma unroll
-    for (int dz = 0; dz < 3; ++dz) {
-        if (pl[dz] == nullptr) continue;  // zero ghost plane: its terms add nothing
-#pragma unroll
-        for (int dy = 0; dy < 3; ++dy) {
-            const T *row = pl[dz] + (i64)(b + dy) * g.sy + a0;
-            T v[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) v[k] = row[k];
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-#pragma unroll
-                for (int dx = 0; dx < 3; ++dx) res[j] = Ops::add(res[j], Ops::mul(s.w[dz * 9 + dy * 3 + dx], v[2 * j + dx]));
-        }
-    }
-    float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (NOISE == NOISE_PHILOX) nrm = point_normals(nz, g, a0, b, c);
-    T *xrow = const_cast<T *>(pl[1]) + (i64)(b + 1) * g.sy + a0 + 1;
-    const T *frow = f + g.pad(a0, b, c);
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int a = a0 + 2 * j;
-        if (a >= g.N0) break;
-        T xi = T(0);
-        if (NOISE == NOISE_PHILOX) xi = (T)pick(nrm, j);
-        if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
-        T cval = frow[2 * j];
-        if (NOISE != NOISE_NONE) cval = Ops::add(Ops::mul(s.sd, xi), cval);
-        const T xo = xrow[2 * j];
-        if (EXACT)
-            xrow[2 * j] = Ops::add(xo, Ops::mul(s.omega, Ops::sub(cval, res[j])) / s.diag);
-        else
-            xrow[2 * j] = xo + s.omega_diag * (cval - res[j]);
-    }
-}
-
-// One colour of an 8-colour (27-point) sweep (colour index
-// (a & 1) | (b & 1) << 1 | (c & 1) << 2): a thread per x-group of four
-// points of the colour (c27_update4).
+// One colour of an 8-colour (27-point) sweep, one thread per point (colour
+// index (a & 1) | (b & 1) << 1 | (c & 1) << 2).
 template <typename T, bool EXACT, int NOISE>
 __global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
                                                                 StencilArg<T> s, int colour, NoiseArgs nz) {
     if (g.pdl) pdl_begin();
     const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
-    const int a0 = 8 * (blockIdx.x * blockDim.x + threadIdx.x) + pa;
+    const int a = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + pa;
     const int b = 2 * (blockIdx.y * blockDim.y + threadIdx.y) + pb, c = 2 * blockIdx.z + pc;
-    if (a0 >= g.N0 || b >= g.N1 || c >= g.N2) return;
-    const T *pl[3] = {x + (i64)c * g.sz, x + (i64)(c + 1) * g.sz, x + (i64)(c + 2) * g.sz};
-    c27_update4<T, EXACT, NOISE>(pl, f, g, s, a0, b, c, nz);
+    if (b >= g.N1 || c >= g.N2) return;
+    T xi = T(0);
+    if (NOISE == NOISE_PHILOX) xi = (T)pick(point_normals(nz, g, a, b, c), (a & 7) >> 1);
+    if (a >= g.N0) return;
+    if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
+    sor_point<T, 27, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
 }
 
 // ------------------------------------------------ cluster-resident level
@@ -447,7 +400,7 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_level_smooth_cluster(const __
     cg::cluster_group cl = cg::this_cluster();
     const int r = (int)cl.block_rank(), NC = (int)cl.num_blocks();
     const Grid3 g = A.g;
-    const i64 sz = g.sz;
+    const i64 sz = g.sz, sy = g.sy;
     int zlo, zhi;
     cl_slab(r, NC, g.N2, zlo, zhi);
     const int nzl = zhi - zlo;
@@ -472,17 +425,41 @@ __global__ void __launch_bounds__(CL_THREADS, 1) k_level_smooth_cluster(const __
         for (int kc = 0; kc < 8; ++kc) {
             const int colour = fwd ? kc : 7 - kc;
             const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
-            const int ngx = (g.N0 - pa + 7) >> 3, nb = (g.N1 - pb + 1) >> 1;
+            const int na = (g.N0 - pa + 1) >> 1, nb = (g.N1 - pb + 1) >> 1;
             const int c0 = zlo + ((pc - zlo) & 1);
             const int ncz = c0 < zhi ? (zhi - c0 + 1) >> 1 : 0;
-            const int cnt = ngx * nb * ncz;
+            const int cnt = na * nb * ncz;
             for (int t = threadIdx.x; t < cnt; t += CL_THREADS) {
-                const int ia = t % ngx, tt = t / ngx, ib = tt % nb, ic = tt / nb;
-                const int a0 = 8 * ia + pa, b = pb + 2 * ib, c = c0 + 2 * ic;
+                const int ia = t % na, tt = t / na, ib = tt % nb, ic = tt / nb;
+                const int a = pa + 2 * ia, b = pb + 2 * ib, c = c0 + 2 * ic;
+                T xi = T(0);
+                if (NOISE == NOISE_PHILOX) xi = (T)pick(point_normals(nz, g, a, b, c), (a & 7) >> 1);
+                if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
                 const int lz = c - zlo;
-                const T *pl[3] = {lz > 0 ? xs + (i64)(lz - 1) * sz : xprev, xs + (i64)lz * sz,
-                                  lz + 1 < nzl ? xs + (i64)(lz + 1) * sz : xnext};
-                c27_update4<T, EXACT, NOISE>(pl, A.f, g, A.s, a0, b, c, nz);
+                const i64 in = (i64)(b + 1) * sy + (a + 1);
+                const T *pl[3];
+                pl[0] = lz > 0 ? xs + (i64)(lz - 1) * sz : xprev;  // null: the ghost plane below the level
+                pl[1] = xs + (i64)lz * sz;
+                pl[2] = lz + 1 < nzl ? xs + (i64)(lz + 1) * sz : xnext;
+                T res = T(0);
+#pragma unroll
+                for (int dz = 0; dz < 3; ++dz) {
+                    const T *p = pl[dz];
+                    if (p == nullptr) continue;  // zero ghost plane: its terms add nothing
+#pragma unroll
+                    for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+                        for (int dx = -1; dx <= 1; ++dx)
+                            res = Ops::add(res, Ops::mul(A.s.w[dz * 9 + (dy + 1) * 3 + (dx + 1)], p[in + dy * sy + dx]));
+                }
+                T cval = A.f[g.pad(a, b, c)];
+                if (NOISE != NOISE_NONE) cval = Ops::add(Ops::mul(A.s.sd, xi), cval);
+                T *pt = xs + (i64)lz * sz + in;
+                const T xo = *pt;
+                if (EXACT)
+                    *pt = Ops::add(xo, Ops::mul(A.s.omega, Ops::sub(cval, res)) / A.s.diag);
+                else
+                    *pt = xo + A.s.omega_diag * (cval - res);
             }
             cl.sync();
         }
