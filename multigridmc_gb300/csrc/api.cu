@@ -109,6 +109,7 @@ struct Sampler {
     mgmc_sampler_params P;
     int dim = 3, m = 0;
     bool fp32 = false, exact = false;
+    int nsm = 152;    // SMs of the device
     bool pdl = true;  // programmatic dependent launch between step kernels (MGMC_NO_PDL=1 turns it off)
     int noise_mode = NOISE_PHILOX;
     std::vector<Level> L;
@@ -360,22 +361,30 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     lr.y = lv.y;
     lr.z = lv.z;
     lr.part = lv.part;
-    const size_t smem = solve_smem(S.m);
     plaunch(S.pdl, k_bt_partial<T>, dim3(S.m, lv.bt_split), 256, 0, S.stream, (const T *)x, lr);
-    if (noise == NOISE_NONE)
-        plaunch(S.pdl, k_lr_solve<NOISE_NONE, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
-    else if (noise == NOISE_PHILOX)
-        plaunch(S.pdl, k_lr_solve<NOISE_PHILOX, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
-    else
-        plaunch(S.pdl, k_lr_solve<NOISE_INJECTED, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
     const RowCsr &C = lv.C[dir];
     if (C.nrows > 0) {
-        if (sizeof(T) == 4)
-            plaunch(S.pdl, k_lr_scatter_f<T>, nblk(C.nrows, 256), 256, 0, S.stream, x, C.nrows, C.rows, C.ptr, C.col, (const T *)C.val,
-                                                                         lv.zf);
+        // solve and correction in one launch; every CTA repeats the (FP64)
+        // m x m solve, so the grid stays at two CTAs per SM at most
+        const unsigned blocks = (unsigned)std::min<i64>(nblk(C.nrows, 256), 2 * S.nsm);
+        const size_t sm = sizeof(double) * (2 * (size_t)S.m + 256);
+        if (noise == NOISE_NONE)
+            plaunch(S.pdl, k_lr_apply<T, NOISE_NONE>, blocks, 256, sm, S.stream, x, lr, lv.bt_split, nz, C.nrows, C.rows,
+                    C.ptr, C.col, (const T *)C.val);
+        else if (noise == NOISE_PHILOX)
+            plaunch(S.pdl, k_lr_apply<T, NOISE_PHILOX>, blocks, 256, sm, S.stream, x, lr, lv.bt_split, nz, C.nrows, C.rows,
+                    C.ptr, C.col, (const T *)C.val);
         else
-            plaunch(S.pdl, k_lr_scatter<T>, nblk(C.nrows, 256), 256, 0, S.stream, x, C.nrows, C.rows, C.ptr, C.col, (const T *)C.val, lv.z);
-        S.launches++;
+            plaunch(S.pdl, k_lr_apply<T, NOISE_INJECTED>, blocks, 256, sm, S.stream, x, lr, lv.bt_split, nz, C.nrows,
+                    C.rows, C.ptr, C.col, (const T *)C.val);
+    } else {
+        const size_t smem = solve_smem(S.m);
+        if (noise == NOISE_NONE)
+            plaunch(S.pdl, k_lr_solve<NOISE_NONE, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
+        else if (noise == NOISE_PHILOX)
+            plaunch(S.pdl, k_lr_solve<NOISE_PHILOX, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
+        else
+            plaunch(S.pdl, k_lr_solve<NOISE_INJECTED, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
     }
     S.launches += 2;
 }
@@ -1091,6 +1100,7 @@ void Sampler::build(const mgmc_operator_desc &op) {
     chol = P.coarse_solver == MGMC_COARSE_CHOLESKY;
     m = op.m;
     CK(cudaSetDevice(P.device));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, P.device));
     {
         const char *e = std::getenv("MGMC_NO_PDL");
         pdl = !(e && e[0] == '1');
@@ -1171,6 +1181,15 @@ void Sampler::build(const mgmc_operator_desc &op) {
         }
         d_sigma_inv = upload(si);
         d_sigma_sqrt = upload(ss);
+        const size_t lr_smem = sizeof(double) * (2 * (size_t)m + 256);
+        if (lr_smem > 48 * 1024) {
+            raise_smem_limit(k_lr_apply<float, NOISE_NONE>, lr_smem);
+            raise_smem_limit(k_lr_apply<float, NOISE_PHILOX>, lr_smem);
+            raise_smem_limit(k_lr_apply<float, NOISE_INJECTED>, lr_smem);
+            raise_smem_limit(k_lr_apply<double, NOISE_NONE>, lr_smem);
+            raise_smem_limit(k_lr_apply<double, NOISE_PHILOX>, lr_smem);
+            raise_smem_limit(k_lr_apply<double, NOISE_INJECTED>, lr_smem);
+        }
         for (size_t lev = 0; lev < L.size(); ++lev) build_lowrank((int)lev);
     }
     if (chol) build_coarse();

@@ -12,7 +12,7 @@
 //                       (one CTA; parity mode)
 //   k_bt_partial        partial sums of y = B^T x
 //   k_lr_solve          y and the m x m low-rank solve
-//   k_lr_scatter        x += C z over the rows of C = M^{-1} B
+//   k_lr_apply          the solve and x += C z over the rows of C = M^{-1} B
 //   k_resid_restrict_tiled  f_c = R (f - A_0 x)  (fused residual + restriction)
 //   k_sub_Bq            f_c -= B_c Sigma^{-1} y
 //   k_prolong_add       x += alpha P x_c
@@ -625,13 +625,14 @@ __global__ void __launch_bounds__(256) k_bt_partial(const T *__restrict__ x, Low
 // FP64 instruction works on 32 different rows (no shuffle trees); S^{-1} is
 // stored transposed (SinvT[q * m + k]) so that a warp's loads of one column
 // q are contiguous.
+// The low-rank solve of one CTA of 256 threads (see k_lr_solve); with
+// SOLVE the coefficients z end up in zs (shared, m doubles) and, if
+// `publish`, in lr.z / lr.zf.  u and acc are shared scratch of m and 256
+// doubles.
 template <int NOISE, bool SOLVE>
-__global__ void __launch_bounds__(256) k_lr_solve(LowRankArg lr, int P, NoiseArgs nz) {
-    pdl_begin();
+__device__ __forceinline__ void lr_solve_cta(const LowRankArg &lr, int P, const NoiseArgs &nz, double *u, double *acc,
+                                             double *zs, bool publish) {
     const int m = lr.m;
-    extern __shared__ double dyn[];
-    double *u = dyn;                 // m
-    double *acc = dyn + m;           // [tpr][rows] partial products
     // rows handled at once and threads per row (blockDim.x = 256)
     const int rows = m < 256 ? m : 256;
     const int tpr = 256 / rows;
@@ -645,7 +646,7 @@ __global__ void __launch_bounds__(256) k_lr_solve(LowRankArg lr, int P, NoiseArg
             for (int r = 0; r < 8; ++r)
                 if (q0 + r < P) t += pv[r];
         }
-        lr.y[k] = t;
+        if (publish) lr.y[k] = t;
         if (SOLVE) {
             double xi = 0.0;
             if (NOISE == NOISE_PHILOX) {
@@ -684,37 +685,60 @@ __global__ void __launch_bounds__(256) k_lr_solve(LowRankArg lr, int P, NoiseArg
         if (threadIdx.x < rows && k0 + threadIdx.x < m) {
             double zk = 0.0;
             for (int h = 0; h < tpr; ++h) zk += acc[h * rows + threadIdx.x];
-            lr.z[k0 + threadIdx.x] = zk;
-            if (lr.zf) lr.zf[k0 + threadIdx.x] = (float)zk;
+            if (zs) zs[k0 + threadIdx.x] = zk;
+            if (publish) {
+                lr.z[k0 + threadIdx.x] = zk;
+                if (lr.zf) lr.zf[k0 + threadIdx.x] = (float)zk;
+            }
         }
         __syncthreads();
     }
 }
 
-// x[row] += sum_e C_e z_{col_e} over the support rows of C = M^{-1} B
-// (FP32 chain: FP32 coefficients, no FP64 conversion in the loop).
-template <typename T>
-__global__ void __launch_bounds__(256) k_lr_scatter_f(T *__restrict__ x, i64 nrows, const i64 *__restrict__ rows,
-                                                       const i64 *__restrict__ ptr, const int *__restrict__ col,
-                                                       const T *__restrict__ val, const float *__restrict__ z) {
+template <int NOISE, bool SOLVE>
+__global__ void __launch_bounds__(256) k_lr_solve(LowRankArg lr, int P, NoiseArgs nz) {
     pdl_begin();
-    for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += (i64)gridDim.x * blockDim.x) {
-        T acc = T(0);
-        for (i64 e = ptr[r]; e < ptr[r + 1]; ++e) acc += val[e] * (T)z[col[e]];
-        x[rows[r]] += acc;
-    }
+    extern __shared__ double dyn[];
+    lr_solve_cta<NOISE, SOLVE>(lr, P, nz, dyn, dyn + lr.m, nullptr, true);
 }
 
-// x[row] += sum_e C_e z_{col_e} over the support rows of C = M^{-1} B.
-template <typename T>
-__global__ void __launch_bounds__(256) k_lr_scatter(T *__restrict__ x, i64 nrows, const i64 *__restrict__ rows,
-                                                     const i64 *__restrict__ ptr, const int *__restrict__ col,
-                                                     const T *__restrict__ val, const double *__restrict__ z) {
+// Low-rank solve and correction in one launch: every CTA forms z itself
+// (the same arithmetic in the same order in every CTA, so all agree) and
+// adds C z on its share of the support rows of C = M^{-1} B, four rows per
+// thread and iteration with their loads issued together.
+template <typename T, int NOISE>
+__global__ void __launch_bounds__(256) k_lr_apply(T *__restrict__ x, LowRankArg lr, int P, NoiseArgs nz, i64 nrows,
+                                                  const i64 *__restrict__ rows, const i64 *__restrict__ ptr,
+                                                  const int *__restrict__ col, const T *__restrict__ val) {
     pdl_begin();
-    for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += (i64)gridDim.x * blockDim.x) {
-        T acc = T(0);
-        for (i64 e = ptr[r]; e < ptr[r + 1]; ++e) acc += val[e] * (T)z[col[e]];
-        x[rows[r]] += acc;
+    extern __shared__ double dyn[];
+    const int m = lr.m;
+    double *zs = dyn, *u = dyn + m, *acc = dyn + 2 * m;
+    lr_solve_cta<NOISE, true>(lr, P, nz, u, acc, zs, blockIdx.x == 0);
+    // zs is complete after the last __syncthreads of lr_solve_cta
+    const i64 stride = (i64)gridDim.x * blockDim.x;
+    for (i64 r0 = (i64)blockIdx.x * blockDim.x + threadIdx.x; r0 < nrows; r0 += 4 * stride) {
+        i64 rr[4], e0[4], e1[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const i64 r = r0 + j * stride;
+            const bool ok = r < nrows;
+            rr[j] = ok ? rows[r] : -1;
+            e0[j] = ok ? ptr[r] : 0;
+            e1[j] = ok ? ptr[r + 1] : 0;
+        }
+        T accv[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            accv[j] = T(0);
+            for (i64 e = e0[j]; e < e1[j]; ++e) accv[j] += val[e] * (T)zs[col[e]];
+        }
+        T xv[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) xv[j] = rr[j] >= 0 ? x[rr[j]] : T(0);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (rr[j] >= 0) x[rr[j]] = xv[j] + accv[j];
     }
 }
 
