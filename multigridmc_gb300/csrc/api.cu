@@ -88,21 +88,6 @@ struct Level {
     int bt_split = 1;  // blocks per column of the B^T x reduction
     CUtensorMap xmap{}, fmap{};  // 3D tile maps of x and f for the residual-restriction
     bool tma = false;            // maps valid (3D, rows of a multiple of 16 bytes)
-    // C = M^{-1} B on the host (levels >= 1), for the cluster lists
-    std::vector<i64> hCrows[2], hCptr[2];
-    std::vector<int> hCcol[2];
-    std::vector<double> hCval[2];
-    // cluster-resident smoothing (k_level_smooth_cluster); NC == 0: not used
-    struct {
-        int NC = 0;
-        size_t smem = 0;
-        int *bptr = nullptr, *bidx = nullptr;
-        double *bval = nullptr;
-        float *bvalf = nullptr;
-        int *crange[2] = {nullptr, nullptr}, *cidx[2] = {nullptr, nullptr};
-        int *cptr[2] = {nullptr, nullptr}, *ccol[2] = {nullptr, nullptr};
-        void *cval[2] = {nullptr, nullptr};
-    } cl;
 };
 
 struct Sampler {
@@ -172,8 +157,6 @@ struct Sampler {
     void build(const mgmc_operator_desc &op);
     void build_lowrank(int lev);
     void make_tile_maps(Level &lv);
-    void build_cluster(int lev);
-    void smooth_cluster(int lev, int nsweep, unsigned dirs);
     void build_coarse();
     void launch_step();
     void sor(int lev, bool forward, bool noisy, void *x, void *f);
@@ -224,7 +207,6 @@ NoiseArgs Sampler::noise_args(int lev, i64 count) {
 // completed and flushed.  This hides the launch latency between the short
 // dependent kernels of a multigrid step.
 constexpr i64 PDL_MAX_POINTS = i64(1) << 22;
-constexpr i64 CL_MAX_POINTS = i64(1) << 17;  // largest level smoothed inside one cluster
 
 template <typename... KArgs, typename... Args>
 static void plaunch(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
@@ -556,10 +538,7 @@ void Sampler::sample(int lev) {
     const int cyc = lev > 0 ? P.cycle : 1;
     const bool ssor = P.smoother == MGMC_SMOOTHER_SSOR;
     for (int j = 0; j < cyc; ++j) {
-        if (lv.cl.NC > 0) {
-            if (P.npresmooth > 0)
-                smooth_cluster(lev, ssor ? 2 * P.npresmooth : P.npresmooth, ssor ? 0x55555555u : 0xffffffffu);
-        } else if (ssor) {
+        if (ssor) {
             for (int k = 0; k < P.npresmooth; ++k) {
                 sor(lev, true, true, lv.x, lv.f);
                 sor(lev, false, true, lv.x, lv.f);
@@ -570,10 +549,7 @@ void Sampler::sample(int lev) {
         resid_restrict(lev);  // also zeroes the coarse state
         sample(lev + 1);
         prolong(lev, P.coarse_scaling, lc.x, lv.x);
-        if (lv.cl.NC > 0) {
-            if (P.npostsmooth > 0)
-                smooth_cluster(lev, ssor ? 2 * P.npostsmooth : P.npostsmooth, ssor ? 0x55555555u : 0u);
-        } else if (ssor) {
+        if (ssor) {
             for (int k = 0; k < P.npostsmooth; ++k) {
                 sor(lev, true, true, lv.x, lv.f);
                 sor(lev, false, true, lv.x, lv.f);
@@ -582,231 +558,6 @@ void Sampler::sample(int lev) {
             for (int k = 0; k < P.npostsmooth; ++k) sor(lev, false, true, lv.x, lv.f);
         }
     }
-}
-
-template <typename T, bool EXACT, int NOISE>
-static void launch_cluster_t(Sampler &S, Level &lv, const ClusterArg<T> &A) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(lv.cl.NC);
-    cfg.blockDim = dim3(CL_THREADS);
-    cfg.dynamicSmemBytes = lv.cl.smem;
-    cfg.stream = S.stream;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = lv.cl.NC;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    CK(cudaLaunchKernelEx(&cfg, k_level_smooth_cluster<T, EXACT, NOISE>, A));
-}
-
-template <typename T>
-static ClusterArg<T> cluster_arg(Sampler &S, Level &lv) {
-    ClusterArg<T> A = {};
-    A.x = (T *)lv.x;
-    A.f = (const T *)lv.f;
-    A.g = lv.g;
-    A.s = stencil_arg<T>(lv, S.P.omega);
-    A.m = S.m;
-    A.bptr = lv.cl.bptr;
-    A.bidx = lv.cl.bidx;
-    A.bval = lv.cl.bval;
-    A.bvalf = lv.cl.bvalf;
-    for (int d = 0; d < 2; ++d) {
-        A.crange[d] = lv.cl.crange[d];
-        A.cidx[d] = lv.cl.cidx[d];
-        A.cptr[d] = lv.cl.cptr[d];
-        A.ccol[d] = lv.cl.ccol[d];
-        A.cval[d] = (const T *)lv.cl.cval[d];
-        A.SinvT[d] = lv.SinvT[d];
-    }
-    A.sigma_sqrt = S.d_sigma_sqrt;
-    return A;
-}
-
-// `nsweep` sweeps of level `lev` in one cluster launch; sweep i runs forward
-// when bit i of `dirs` is set.  Noise offsets and invocation numbers advance
-// exactly as nsweep calls of sor() would advance them.
-void Sampler::smooth_cluster(int lev, int nsweep, unsigned dirs) {
-    Level &lv = L[lev];
-    NoiseArgs nzp[CL_MAX_SWEEPS], nzl[CL_MAX_SWEEPS];
-    for (int i = 0; i < nsweep; ++i) {
-        nzp[i] = noise_args(lev, lv.geo.n);
-        nzl[i] = m > 0 ? noise_args(lev, m) : nzp[i];
-        inv++;
-    }
-    auto fill = [&](auto &A) {
-        A.nsweep = nsweep;
-        A.dirs = dirs;
-        for (int i = 0; i < nsweep; ++i) {
-            A.nzp[i] = nzp[i];
-            A.nzl[i] = nzl[i];
-        }
-    };
-    if (fp32) {
-        ClusterArg<float> A = cluster_arg<float>(*this, lv);
-        fill(A);
-        if (noise_mode == NOISE_PHILOX)
-            launch_cluster_t<float, false, NOISE_PHILOX>(*this, lv, A);
-        else
-            launch_cluster_t<float, false, NOISE_INJECTED>(*this, lv, A);
-    } else {
-        ClusterArg<double> A = cluster_arg<double>(*this, lv);
-        fill(A);
-        if (noise_mode == NOISE_PHILOX)
-            launch_cluster_t<double, false, NOISE_PHILOX>(*this, lv, A);
-        else if (exact)
-            launch_cluster_t<double, true, NOISE_INJECTED>(*this, lv, A);
-        else
-            launch_cluster_t<double, false, NOISE_INJECTED>(*this, lv, A);
-    }
-    launches++;
-}
-
-template <typename T, bool EXACT, int NOISE>
-static bool cluster_fits(int NC, size_t smem) {
-    auto k = k_level_smooth_cluster<T, EXACT, NOISE>;
-    // the attribute belongs to the kernel, shared by every level: only raise it
-    cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, k) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
-    }
-    const int want = std::max(fa.maxDynamicSharedSizeBytes, (int)smem);
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, want) != cudaSuccess ||
-        cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(NC);
-    cfg.blockDim = dim3(CL_THREADS);
-    cfg.dynamicSmemBytes = smem;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = NC;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    int ncl = 0;
-    if (cudaOccupancyMaxActiveClusters(&ncl, k, &cfg) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
-    }
-    return ncl >= 1;
-}
-
-// Cluster-resident smoothing for an intermediate 27-point level whose x
-// fits in the shared memory of one cluster (at most CL_MAX_NC CTAs): the
-// per-CTA lists of B entries and C rows in slab-local indices.
-void Sampler::build_cluster(int lev) {
-    Level &lv = L[lev];
-    {
-        const char *e = std::getenv("MGMC_NO_CLUSTER");
-        if (e && e[0] == '1') return;
-    }
-    const bool ssor = P.smoother == MGMC_SMOOTHER_SSOR;
-    const int nsw = (ssor ? 2 : 1) * std::max(P.npresmooth, P.npostsmooth);
-    if (dim != 3 || lev == 0 || lev + 1 >= (int)L.size() || lv.npt != 27 || P.ordering != MGMC_ORDER_MULTICOLOUR ||
-        m > CL_MAX_M || nsw > CL_MAX_SWEEPS)
-        return;
-    // Larger levels have more work per colour than CL_MAX_NC SMs finish
-    // faster than the per-colour launches on the whole GPU.
-    i64 max_points = CL_MAX_POINTS;
-    if (const char *e = std::getenv("MGMC_CLUSTER_MAX_POINTS")) max_points = std::atoll(e);
-    if (lv.geo.n > max_points) return;
-    // about four planes per CTA: fewer CTAs read fewer remote planes and
-    // meet at cheaper cluster barriers
-    const int NC = std::min(CL_MAX_NC, std::max(1, lv.g.N2 / 4));
-    const size_t smem = fp32 ? cl_smem_bytes<float>(lv.g, NC) : cl_smem_bytes<double>(lv.g, NC);
-    if (smem > 227 * 1024) return;
-    bool ok;
-    if (fp32)
-        ok = noise_mode == NOISE_PHILOX ? cluster_fits<float, false, NOISE_PHILOX>(NC, smem)
-                                        : cluster_fits<float, false, NOISE_INJECTED>(NC, smem);
-    else if (noise_mode == NOISE_PHILOX)
-        ok = cluster_fits<double, false, NOISE_PHILOX>(NC, smem);
-    else
-        ok = exact ? cluster_fits<double, true, NOISE_INJECTED>(NC, smem) : cluster_fits<double, false, NOISE_INJECTED>(NC, smem);
-    if (!ok) return;
-    const i64 sz = lv.g.sz;
-    std::vector<int> zlo(NC + 1);
-    for (int r = 0; r < NC; ++r) {
-        int a0, a1;
-        cl_slab(r, NC, lv.g.N2, a0, a1);
-        zlo[r] = a0;
-        zlo[r + 1] = a1;
-    }
-    auto rank_of = [&](int c) {
-        int r = 0;
-        while (r + 1 < NC && c >= zlo[r + 1]) ++r;
-        return r;
-    };
-    if (m > 0) {
-        // B entries per CTA and column (ascending compact index inside a column)
-        std::vector<std::vector<std::vector<std::pair<int, double>>>> be(NC, std::vector<std::vector<std::pair<int, double>>>(m));
-        const int N0 = lv.g.N0, N1 = lv.g.N1;
-        for (int k = 0; k < m; ++k)
-            for (i64 e = lv.Bh.ptr[k]; e < lv.Bh.ptr[k + 1]; ++e) {
-                const i64 i = lv.Bh.row[e];
-                const int a = (int)(i % N0), b = (int)((i / N0) % N1), c = (int)(i / ((i64)N0 * N1));
-                const int r = rank_of(c);
-                be[r][k].emplace_back((int)(lv.g.pad(a, b, c) - (i64)(zlo[r] + 1) * sz), lv.Bh.val[e]);
-            }
-        std::vector<int> bptr, bidx;
-        std::vector<double> bval;
-        for (int r = 0; r < NC; ++r)
-            for (int k = 0; k <= m; ++k) {
-                bptr.push_back((int)bidx.size());
-                if (k == m) break;
-                for (auto &pv : be[r][k]) {
-                    bidx.push_back(pv.first);
-                    bval.push_back(pv.second);
-                }
-            }
-        if (bidx.empty()) {
-            bidx.push_back(0);
-            bval.push_back(0.0);
-        }
-        std::vector<float> bvf(bval.begin(), bval.end());
-        lv.cl.bptr = upload(bptr);
-        lv.cl.bidx = upload(bidx);
-        lv.cl.bval = upload(bval);
-        lv.cl.bvalf = upload(bvf);
-        for (int d = 0; d < 2; ++d) {
-            const std::vector<i64> &rows = lv.hCrows[d], &ptr = lv.hCptr[d];
-            std::vector<int> crange(NC + 1, 0), cidx, cptr{0}, ccol(lv.hCcol[d]);
-            for (size_t i = 0; i < rows.size(); ++i) {
-                const int c = (int)(rows[i] / sz) - 1;
-                const int r = rank_of(c);
-                crange[r + 1] = (int)i + 1;
-                cidx.push_back((int)(rows[i] - (i64)(zlo[r] + 1) * sz));
-                cptr.push_back((int)ptr[i + 1]);
-            }
-            for (int r = 1; r <= NC; ++r) crange[r] = std::max(crange[r], crange[r - 1]);
-            if (cidx.empty()) {
-                cidx.push_back(0);
-                ccol.push_back(0);
-            }
-            lv.cl.crange[d] = upload(crange);
-            lv.cl.cidx[d] = upload(cidx);
-            lv.cl.cptr[d] = upload(cptr);
-            lv.cl.ccol[d] = upload(ccol);
-            if (fp32) {
-                std::vector<float> vf(lv.hCval[d].begin(), lv.hCval[d].end());
-                if (vf.empty()) vf.push_back(0.f);
-                lv.cl.cval[d] = upload(vf);
-            } else {
-                std::vector<double> vd(lv.hCval[d]);
-                if (vd.empty()) vd.push_back(0.0);
-                lv.cl.cval[d] = upload(vd);
-            }
-        }
-    }
-    lv.cl.NC = NC;
-    lv.cl.smem = smem;
 }
 
 void Sampler::step_end() {
@@ -962,12 +713,6 @@ void Sampler::build_lowrank(int lev) {
             val.push_back(std::get<2>(trip[e]));
         }
         if (!trip.empty()) ptr.push_back((i64)col.size());
-        if (lev >= 1) {
-            lv.hCrows[dir] = rows;
-            lv.hCptr[dir] = ptr;
-            lv.hCcol[dir] = col;
-            lv.hCval[dir] = val;
-        }
         RowCsr &C = lv.C[dir];
         C.nrows = (i64)rows.size();
         C.rows = upload(rows);
@@ -1193,7 +938,6 @@ void Sampler::build(const mgmc_operator_desc &op) {
         for (size_t lev = 0; lev < L.size(); ++lev) build_lowrank((int)lev);
     }
     if (chol) build_coarse();
-    for (size_t lev = 1; lev + 1 < L.size(); ++lev) build_cluster((int)lev);
     // noise per step (dry count)
     noise_per_step = 0;
     {

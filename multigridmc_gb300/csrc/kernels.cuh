@@ -22,7 +22,6 @@
 
 #include <cstdint>
 #include <cuda.h>  // CUtensorMap (type only; the driver entry point is resolved at run time)
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 namespace mgmc {
@@ -328,197 +327,6 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ 
     if (a >= g.N0) return;
     if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
     sor_point<T, 27, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
-}
-
-// ------------------------------------------------ cluster-resident level
-// A whole smoothing sequence (up to CL_MAX_SWEEPS 8-colour sweeps of a
-// 27-point level, each followed by its low-rank correction) in one thread
-// block cluster: CTA r of the NC CTAs keeps the planes [zlo_r, zhi_r) of x
-// in its shared memory (padded plane layout, ghosts zero) and reads the
-// neighbouring slabs' boundary planes through distributed shared memory; a
-// cluster barrier separates the colours.  Per point the arithmetic, its
-// order and the Philox counters are those of k_sweep_c27_pass, so the chain
-// is the one the per-colour launches produce.  The low-rank correction
-// gathers per-CTA partial sums of B^T x (fixed order) in CTA 0, which forms
-// z = S^{-1} (Sigma^{1/2} xi' - y) and broadcasts it; each CTA then adds C z
-// on its own rows.  This replaces 8 launches per sweep (plus 3 per low-rank
-// correction) on levels whose x fits in the cluster's shared memory.
-constexpr int CL_MAX_SWEEPS = 8;
-constexpr int CL_THREADS = 1024;
-constexpr int CL_MAX_M = 128;
-constexpr int CL_MAX_NC = 16;
-
-template <typename T>
-struct ClusterArg {
-    T *x;
-    const T *f;
-    Grid3 g;
-    StencilArg<T> s;
-    int nsweep;
-    unsigned dirs;  // bit i set: sweep i runs forward (colours ascending)
-    NoiseArgs nzp[CL_MAX_SWEEPS], nzl[CL_MAX_SWEEPS];  // point and low-rank noise of each sweep
-    int m;
-    const int *bptr;  // [NC][m + 1]: CTA r's entries of column k are bptr[r (m+1) + k] .. + 1
-    const int *bidx;  // slab-local index of the entry's point
-    const double *bval;
-    const float *bvalf;
-    const int *crange[2];  // [NC + 1]: CTA r's rows of C (per sweep direction)
-    const int *cidx[2];    // slab-local index of the row
-    const int *cptr[2];
-    const int *ccol[2];
-    const T *cval[2];
-    const double *SinvT[2];
-    const double *sigma_sqrt;
-};
-
-// planes [zlo, zhi) of CTA r out of NC (balanced split of N2 planes)
-__host__ __device__ __forceinline__ void cl_slab(int r, int NC, int N2, int &zlo, int &zhi) {
-    zlo = (int)((i64)r * N2 / NC);
-    zhi = (int)((i64)(r + 1) * N2 / NC);
-}
-
-// Slab of the largest CTA plus CL_TAIL(g) zeros: the neighbourhood rows of
-// the last row of the last plane reach up to sy + 7 elements past the plane
-// (the next plane's ghost row in the global layout).
-__host__ __device__ __forceinline__ i64 cl_tail(const Grid3 &g) { return g.sy + 16; }
-
-template <typename T>
-__host__ __device__ __forceinline__ size_t cl_slab_bytes(const Grid3 &g, int NC) {
-    const int nzmax = (g.N2 + NC - 1) / NC;
-    return (((size_t)nzmax * (size_t)g.sz + (size_t)cl_tail(g)) * sizeof(T) + 15) / 16 * 16;
-}
-
-template <typename T>
-__host__ __device__ __forceinline__ size_t cl_smem_bytes(const Grid3 &g, int NC) {
-    return cl_slab_bytes<T>(g, NC) + sizeof(double) * ((size_t)CL_MAX_M * (2 + CL_MAX_NC) + CL_THREADS);
-}
-
-template <typename T, bool EXACT, int NOISE>
-__global__ void __launch_bounds__(CL_THREADS, 1) k_level_smooth_cluster(const __grid_constant__ ClusterArg<T> A) {
-    namespace cg = cooperative_groups;
-    typedef Ar<EXACT> Ops;
-    cg::cluster_group cl = cg::this_cluster();
-    const int r = (int)cl.block_rank(), NC = (int)cl.num_blocks();
-    const Grid3 g = A.g;
-    const i64 sz = g.sz, sy = g.sy;
-    int zlo, zhi;
-    cl_slab(r, NC, g.N2, zlo, zhi);
-    const int nzl = zhi - zlo;
-    int zlo_p = 0, zhi_p = 0;
-    if (r > 0) cl_slab(r - 1, NC, g.N2, zlo_p, zhi_p);
-    extern __shared__ __align__(16) unsigned char cl_smem[];
-    T *xs = reinterpret_cast<T *>(cl_smem);
-    double *zc = reinterpret_cast<double *>(cl_smem + cl_slab_bytes<T>(g, NC));  // [CL_MAX_M] coefficients z
-    double *u = zc + CL_MAX_M;                                                  // [CL_MAX_M] (CTA 0)
-    double *part = u + CL_MAX_M;                                                // [CL_MAX_NC][CL_MAX_M] (CTA 0)
-    double *acc = part + CL_MAX_NC * CL_MAX_M;                                  // [CL_THREADS] (CTA 0)
-    const T *xprev = r > 0 ? cl.map_shared_rank(xs, r - 1) + (i64)(zhi_p - zlo_p - 1) * sz : nullptr;
-    const T *xnext = r + 1 < NC ? cl.map_shared_rank(xs, r + 1) : nullptr;
-    const T *xg = A.x + (i64)(zlo + 1) * sz;
-    for (i64 i = threadIdx.x; i < (i64)nzl * sz; i += CL_THREADS) xs[i] = xg[i];
-    for (i64 i = threadIdx.x; i < cl_tail(g); i += CL_THREADS) xs[(i64)nzl * sz + i] = T(0);
-    cl.sync();
-    const int m = A.m;
-    for (int sw = 0; sw < A.nsweep; ++sw) {
-        const bool fwd = (A.dirs >> sw) & 1u;
-        const NoiseArgs nz = A.nzp[sw];
-        for (int kc = 0; kc < 8; ++kc) {
-            const int colour = fwd ? kc : 7 - kc;
-            const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
-            const int na = (g.N0 - pa + 1) >> 1, nb = (g.N1 - pb + 1) >> 1;
-            const int c0 = zlo + ((pc - zlo) & 1);
-            const int ncz = c0 < zhi ? (zhi - c0 + 1) >> 1 : 0;
-            const int cnt = na * nb * ncz;
-            for (int t = threadIdx.x; t < cnt; t += CL_THREADS) {
-                const int ia = t % na, tt = t / na, ib = tt % nb, ic = tt / nb;
-                const int a = pa + 2 * ia, b = pb + 2 * ib, c = c0 + 2 * ic;
-                T xi = T(0);
-                if (NOISE == NOISE_PHILOX) xi = (T)pick(point_normals(nz, g, a, b, c), (a & 7) >> 1);
-                if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
-                const int lz = c - zlo;
-                const i64 in = (i64)(b + 1) * sy + (a + 1);
-                const T *pl[3];
-                pl[0] = lz > 0 ? xs + (i64)(lz - 1) * sz : xprev;  // null: the ghost plane below the level
-                pl[1] = xs + (i64)lz * sz;
-                pl[2] = lz + 1 < nzl ? xs + (i64)(lz + 1) * sz : xnext;
-                T res = T(0);
-#pragma unroll
-                for (int dz = 0; dz < 3; ++dz) {
-                    const T *p = pl[dz];
-                    if (p == nullptr) continue;  // zero ghost plane: its terms add nothing
-#pragma unroll
-                    for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-                        for (int dx = -1; dx <= 1; ++dx)
-                            res = Ops::add(res, Ops::mul(A.s.w[dz * 9 + (dy + 1) * 3 + (dx + 1)], p[in + dy * sy + dx]));
-                }
-                T cval = A.f[g.pad(a, b, c)];
-                if (NOISE != NOISE_NONE) cval = Ops::add(Ops::mul(A.s.sd, xi), cval);
-                T *pt = xs + (i64)lz * sz + in;
-                const T xo = *pt;
-                if (EXACT)
-                    *pt = Ops::add(xo, Ops::mul(A.s.omega, Ops::sub(cval, res)) / A.s.diag);
-                else
-                    *pt = xo + A.s.omega_diag * (cval - res);
-            }
-            cl.sync();
-        }
-        if (m == 0) continue;
-        // low-rank correction of this sweep
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        double *part0 = cl.map_shared_rank(part, 0);
-        for (int k = warp; k < m; k += CL_THREADS / 32) {
-            const int e0 = A.bptr[r * (m + 1) + k], e1 = A.bptr[r * (m + 1) + k + 1];
-            T tacc = T(0);
-            for (int e = e0 + lane; e < e1; e += 32)
-                tacc += (sizeof(T) == 4 ? (T)A.bvalf[e] : (T)A.bval[e]) * xs[A.bidx[e]];
-            double sum = (double)tacc;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-            if (lane == 0) part0[r * CL_MAX_M + k] = sum;
-        }
-        cl.sync();
-        if (r == 0) {
-            const NoiseArgs nl = A.nzl[sw];
-            for (int k = threadIdx.x; k < m; k += CL_THREADS) {
-                double y = 0.0;
-                for (int q = 0; q < NC; ++q) y += part[q * CL_MAX_M + k];
-                double xi = 0.0;
-                if (NOISE == NOISE_PHILOX) {
-                    float4 rn = normals4(philox4x32_10(noise_ctr(nl, (unsigned)(k >> 2), PURPOSE_LOWRANK, 0), noise_key(nl)));
-                    xi = (double)pick(rn, k & 3);
-                }
-                if (NOISE == NOISE_INJECTED) xi = nl.buf[k];
-                u[k] = A.sigma_sqrt[k] * xi - y;
-            }
-            __syncthreads();
-            const double *SiT = A.SinvT[fwd ? 0 : 1];
-            const int tpr = CL_THREADS / m, gq = threadIdx.x / m, kk = threadIdx.x % m;
-            if (gq < tpr) {
-                double t = 0.0;
-                for (int q = gq; q < m; q += tpr) t = fma(SiT[(i64)q * m + kk], u[q], t);
-                acc[gq * m + kk] = t;
-            }
-            __syncthreads();
-            if (threadIdx.x < m) {
-                double zk = 0.0;
-                for (int h = 0; h < tpr; ++h) zk += acc[h * m + threadIdx.x];
-                for (int q = 0; q < NC; ++q) cl.map_shared_rank(zc, q)[threadIdx.x] = zk;
-            }
-        }
-        cl.sync();
-        const int dir = fwd ? 0 : 1;
-        const int r0 = A.crange[dir][r], r1 = A.crange[dir][r + 1];
-        for (int i = r0 + threadIdx.x; i < r1; i += CL_THREADS) {
-            T accv = T(0);
-            for (int e = A.cptr[dir][i]; e < A.cptr[dir][i + 1]; ++e) accv += A.cval[dir][e] * (T)zc[A.ccol[dir][e]];
-            xs[A.cidx[dir][i]] += accv;
-        }
-        cl.sync();
-    }
-    T *xw = A.x + (i64)(zlo + 1) * sz;
-    for (i64 i = threadIdx.x; i < (i64)nzl * sz; i += CL_THREADS) xw[i] = xs[i];
-    cl.sync();
 }
 
 // ------------------------------------------------ lexicographic wavefront

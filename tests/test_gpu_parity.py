@@ -140,23 +140,3 @@ def test_errors_are_status_codes():
     with pytest.raises(M.MGMCError) as e:
         M.MultigridMCSampler(op_bad, _mg(2))
     assert e.value.status == 3
-
-
-@pytest.mark.parametrize("precision,tol", [(M.FP64, 1e-11), (M.FP32_MIXED, 1e-4)], ids=["fp64", "fp32"])
-def test_cluster_smoother_matches_colour_passes(monkeypatch, precision, tol):
-    """Intermediate 27-point levels smoothed inside one thread block cluster
-    (shared-memory resident) give the chain of the per-colour launches: same
-    Philox counters and point arithmetic; only the summation order of B^T x
-    and of the m x m product differs."""
-    _, op_p = posterior((64, 64, 64), m=16)
-    f = np.random.default_rng(5).standard_normal(op_p.n)
-    states = []
-    for off in ("0", "1"):
-        monkeypatch.setenv("MGMC_NO_CLUSTER", off)
-        s = M.MultigridMCSampler(op_p, _mg(5), ordering=M.MULTICOLOUR, precision=precision, seed=11)
-        s.fix_rhs(f)
-        s.step(4)
-        states.append(s.get_state())
-        s.close()
-    err = np.linalg.norm(states[0] - states[1]) / np.linalg.norm(states[1])
-    assert err < tol, f"cluster vs colour passes: {err:.3e}"
