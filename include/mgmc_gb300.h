@@ -170,6 +170,15 @@ mgmc_status mgmc_sampler_nlevel(mgmc_sampler *s, int *nlevel);
 mgmc_status mgmc_sampler_level_size(mgmc_sampler *s, int level, int64_t *n);
 /* Number of kernel launches one step issues (measurement bookkeeping). */
 mgmc_status mgmc_sampler_launches_per_step(mgmc_sampler *s, int64_t *count);
+/* Adjoint of one step with its noise held fixed (no counterpart in the
+ * reference; pathwise differentiation of chain functionals).  A step is
+ * affine in the state and the right hand side, x' = Phi x + K f + noise
+ * terms; on entry xbar (n values) holds the adjoint of x', on return the
+ * adjoint of x, Phi^T xbar, and K^T xbar has been added to fbar (n values).
+ * Vectors in the reference's vertex order, host (on_device = 0) or device
+ * pointers.  Gradients with respect to the measurement values y follow
+ * through f = B Sigma^{-1} y. */
+mgmc_status mgmc_sampler_adjoint_step(mgmc_sampler *s, double *xbar, double *fbar, int on_device);
 
 /* -------------------------------------------- level building blocks */
 mgmc_status mgmc_level_stencil(mgmc_sampler *s, int level, double stencil[27]);

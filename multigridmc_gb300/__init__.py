@@ -101,6 +101,7 @@ SIGNATURES = {
     "mgmc_sampler_nlevel": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "mgmc_sampler_level_size": (C.c_int, [_P, C.c_int, _I64]),
     "mgmc_sampler_launches_per_step": (C.c_int, [_P, _I64]),
+    "mgmc_sampler_adjoint_step": (C.c_int, [_P, _D, _D, C.c_int]),
     "mgmc_level_stencil": (C.c_int, [_P, C.c_int, _D]),
     "mgmc_level_apply": (C.c_int, [_P, C.c_int, _D, _D]),
     "mgmc_level_restrict": (C.c_int, [_P, C.c_int, _D, _D]),
@@ -354,6 +355,16 @@ class MultigridMCSampler:
         x = np.zeros(self.n)
         _check(self._L.mgmc_sampler_get_state(self._h, _dp(x), 0))
         return x
+
+    def adjoint_step(self, xbar, fbar):
+        """Adjoint of one step with its noise held fixed: xbar (the adjoint of
+        the step's output state) becomes the adjoint of its input state, in
+        place, and the adjoint with respect to the right hand side f is added
+        to fbar.  No counterpart in the reference."""
+        assert xbar.dtype == np.float64 and xbar.flags.c_contiguous and xbar.size == self.n
+        assert fbar.dtype == np.float64 and fbar.flags.c_contiguous and fbar.size == self.n
+        _check(self._L.mgmc_sampler_adjoint_step(self._h, _dp(xbar), _dp(fbar), 0))
+        return xbar
 
     def step(self, nsteps=1):
         _check(self._L.mgmc_sampler_step(self._h, int(nsteps)))

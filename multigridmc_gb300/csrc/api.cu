@@ -86,6 +86,7 @@ struct Level {
     double *y = nullptr, *z = nullptr, *part = nullptr;
     float *zf = nullptr, *Bvalf = nullptr;
     int bt_split = 1;  // blocks per column of the B^T x reduction
+    void *adj[4] = {nullptr, nullptr, nullptr, nullptr};  // adjoint: x-bar, f-bar, two work vectors (T, padded)
     CUtensorMap xmap{}, fmap{};  // 3D tile maps of x and f for the residual-restriction
     bool tma = false;            // maps valid (3D, rows of a multiple of 16 bytes)
 };
@@ -157,6 +158,10 @@ struct Sampler {
     void build(const mgmc_operator_desc &op);
     void build_lowrank(int lev);
     void make_tile_maps(Level &lv);
+    double *adj_m = nullptr;  // m-vector for the adjoint's transposed low-rank solve
+    void ensure_adjoint();
+    template <typename T>
+    void adjoint_sample(int lev);
     void build_coarse();
     void launch_step();
     void sor(int lev, bool forward, bool noisy, void *x, void *f);
@@ -743,9 +748,9 @@ void Sampler::build_coarse() {
     if (!dense_cholesky(Q, n)) fail(MGMC_ERR_NOT_SPD, "coarse precision matrix is not positive definite");
     dgv = alloc<double>(n);
     chol_smem = (size_t)n * sizeof(double);
-    if (exact) {
-        dL = upload(Q);
-    } else {
+    if (exact) dL = upload(Q);  // parity path: substitution in the oracle's order
+    {
+        // throughput path and adjoint: explicit inverse factors
         std::vector<double> T = inverse_factor_transposed(Q, n);  // (L^{-1})^T
         const size_t esz = fp32 ? sizeof(float) : sizeof(double);
         const i64 ld = (i64)((n * esz + 15) / 16 * 16 / esz);
@@ -1071,6 +1076,139 @@ static void run_steps(Sampler &S, i64 nsteps) {
     }
     ensure_graph(S);
     for (i64 k = 0; k < nsteps; ++k) CK(cudaGraphLaunch(S.gexec, S.stream));
+}
+
+// ------------------------------------------------------------- adjoint
+// Transpose of the linear part of one MGMC step with its noise held fixed.
+// With fixed noise a step is affine: x' = Phi x + K f + (noise terms); the
+// adjoint maps x-bar' to Phi^T x-bar' and adds K^T x-bar' to f-bar.  It is
+// assembled from the forward kernels: a sweep of direction d is
+// x <- x + M_d^{-1}(c - A_0 x), M_d = D / omega + (A_0's part before the
+// point in the sweep order), and for symmetric A_0, M_d^T is the splitting
+// of the opposite direction, so M_d^{-T} v is a noise-free sweep of the
+// opposite direction from x = 0 with right hand side v.  The low-rank
+// correction x <- (I - C S^{-1} B^T) x (C = M_d^{-1} B) has transpose
+// I - B S^{-T} B^T M_d^{-T}; R = P^T; the coarse Cholesky sample
+// L^{-T}(xi + L^{-1} f) has the symmetric linear part Q_c^{-1}.  No
+// counterpart in the reference.
+void Sampler::ensure_adjoint() {
+    for (auto &lv : L)
+        for (int k = 0; k < 4; ++k)
+            if (!lv.adj[k]) lv.adj[k] = talloc(lv.geo.nalloc);
+    if (!adj_m) adj_m = alloc<double>((size_t)std::max(m, 1));
+}
+
+template <typename T>
+static void adj_zero(Sampler &S, const Level &lv, void *v) {
+    CK(cudaMemsetAsync(v, 0, (size_t)lv.geo.nalloc * sizeof(T), S.stream));
+}
+
+template <typename T>
+static void adj_axpy(Sampler &S, const Level &lv, void *y, const void *x, double alpha) {
+    const unsigned blocks = (unsigned)std::min<i64>(nblk(lv.geo.nalloc, 256), 8 * S.nsm);
+    plaunch(false, k_axpy<T>, blocks, 256, 0, S.stream, (T *)y, (const T *)x, (T)alpha, (i64)lv.geo.nalloc);
+}
+
+// out = M^{-T} v for the sweep of direction `forward` on level lev
+template <typename T>
+static void adj_msolve(Sampler &S, int lev, bool forward, const void *v, void *out) {
+    Level &lv = S.L[lev];
+    adj_zero<T>(S, lv, out);
+    NoiseArgs nz{};
+    nz.d_step = S.d_step;
+    launch_sweep(S, lv, !forward, NOISE_NONE, out, v, nz, S.fp32, false);
+}
+
+template <typename T>
+static void adj_apply_a0(Sampler &S, Level &lv, const void *x, void *y) {
+    plaunch(false, k_apply_stencil<T>, nblk(lv.geo.n, 256), 256, 0, S.stream, (const T *)x, (T *)y, lv.g,
+            stencil_arg<T>(lv, S.P.omega));
+}
+
+// adjoint of one SOR sweep of direction `forward` with its low-rank
+// correction: a = x-bar (in/out), b = f-bar (accumulated)
+template <typename T>
+static void adjoint_sor(Sampler &S, int lev, bool forward) {
+    Level &lv = S.L[lev];
+    void *a = lv.adj[0], *b = lv.adj[1], *w = lv.adj[2], *u = lv.adj[3];
+    if (S.m > 0) {
+        adj_msolve<T>(S, lev, forward, a, w);  // w = M^{-T} a
+        launch_bt_plain<T>(S, lv, w);          // y = B^T w
+        k_sinvt_q<<<(S.m + 255) / 256, 256, 0, S.stream>>>(lv.SinvT[forward ? 0 : 1], lv.y, S.d_sigma_sqrt, S.adj_m, S.m);
+        launch_add_Bq<T>(S, lv, a, S.adj_m, -1.0);  // a -= B S^{-T} y
+    }
+    adj_msolve<T>(S, lev, forward, a, u);  // u = M^{-T} a
+    adj_axpy<T>(S, lv, b, u, 1.0);        // f-bar += u
+    adj_apply_a0<T>(S, lv, u, w);
+    adj_axpy<T>(S, lv, a, w, -1.0);       // a -= A_0 u
+}
+
+// MultigridMCSampler::sample in reverse: on entry L[lev].adj[0] is the
+// adjoint of the level's output state, on return the adjoint of its input
+// state, and L[lev].adj[1] has accumulated the adjoint of its right hand side.
+template <typename T>
+void Sampler::adjoint_sample(int lev) {
+    const int nlev = (int)L.size();
+    Level &lv = L[lev];
+    if (lev == nlev - 1) {
+        if (chol) {
+            // f-bar += Q_c^{-1} x-bar; the coarse sample does not read its input state
+            const i64 n = lv.geo.n;
+            const unsigned blocks = (unsigned)((n + 7) / 8);
+            NoiseArgs nz{};
+            plaunch(false, k_chol_gemv_lower<T, T, NOISE_NONE>, blocks, 256, chol_smem, stream, (const T *)lv.adj[0], lv.g,
+                    (const T *)dLinv, chol_ld, (T *)dgv, nz);
+            adj_zero<T>(*this, lv, lv.adj[2]);
+            plaunch(false, k_chol_gemv_upper<T, T>, blocks, 256, chol_smem, stream, (const T *)dgv, lv.g, (const T *)dLinvT,
+                    chol_ld, (T *)lv.adj[2]);
+            adj_axpy<T>(*this, lv, lv.adj[1], lv.adj[2], 1.0);
+        } else {
+            for (int k = P.ncoarsesmooth - 1; k >= 0; --k) {
+                adjoint_sor<T>(*this, lev, false);
+                adjoint_sor<T>(*this, lev, true);
+            }
+        }
+        adj_zero<T>(*this, lv, lv.adj[0]);  // the coarse level starts from zero
+        return;
+    }
+    Level &lc = L[lev + 1];
+    const int cyc = lev > 0 ? P.cycle : 1;
+    const bool ssor = P.smoother == MGMC_SMOOTHER_SSOR;
+    for (int j = cyc - 1; j >= 0; --j) {
+        for (int k = P.npostsmooth - 1; k >= 0; --k) {
+            if (ssor) {
+                adjoint_sor<T>(*this, lev, false);
+                adjoint_sor<T>(*this, lev, true);
+            } else {
+                adjoint_sor<T>(*this, lev, false);
+            }
+        }
+        // x += alpha P x_c  ->  x_c-bar = alpha R x-bar
+        launch_resid_restrict<T>(*this, lev, lv.adj[0], lv.adj[0], lc.adj[2], nullptr, true);
+        adj_zero<T>(*this, lc, lc.adj[0]);
+        adj_axpy<T>(*this, lc, lc.adj[0], lc.adj[2], P.coarse_scaling);
+        adj_zero<T>(*this, lc, lc.adj[1]);
+        adjoint_sample<T>(lev + 1);
+        // f_c = R (f - A x)  ->  t = P f_c-bar; f-bar += t; x-bar -= A t
+        void *t = lv.adj[2], *u = lv.adj[3];
+        adj_zero<T>(*this, lv, t);
+        prolong(lev, 1.0, lc.adj[1], t);
+        adj_axpy<T>(*this, lv, lv.adj[1], t, 1.0);
+        adj_apply_a0<T>(*this, lv, t, u);
+        if (m > 0) {
+            launch_bt_plain<T>(*this, lv, t);
+            launch_add_Bq<T>(*this, lv, u, lv.y, 1.0);
+        }
+        adj_axpy<T>(*this, lv, lv.adj[0], u, -1.0);
+        for (int k = P.npresmooth - 1; k >= 0; --k) {
+            if (ssor) {
+                adjoint_sor<T>(*this, lev, false);
+                adjoint_sor<T>(*this, lev, true);
+            } else {
+                adjoint_sor<T>(*this, lev, true);
+            }
+        }
+    }
 }
 
 }  // namespace mgmc
@@ -1597,3 +1735,45 @@ mgmc_status mgmc_batch_destroy(mgmc_batch *b) {
 }
 
 }  // extern "C"
+
+mgmc_status mgmc_sampler_adjoint_step(mgmc_sampler *s, double *xbar, double *fbar, int on_device) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!xbar || !fbar) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    CK(cudaStreamSynchronize(S.stream));
+    S.ensure_adjoint();
+    Level &l0 = S.L[0];
+    put_vec(S, 0, xbar, on_device, l0.adj[0]);
+    if (S.fp32) {
+        adj_zero<float>(S, l0, l0.adj[1]);
+        S.adjoint_sample<float>(0);
+    } else {
+        adj_zero<double>(S, l0, l0.adj[1]);
+        S.adjoint_sample<double>(0);
+    }
+    S.check_launch();
+    // f-bar is accumulated: add this step's part through a device compact copy
+    get_vec(S, 0, l0.adj[0], xbar, on_device);
+    {
+        const i64 n = l0.geo.n;
+        double *d = S.d_cvec;
+        if (S.fp32)
+            k_pack<float><<<pack_grid(l0), 256, 0, S.stream>>>((const float *)l0.adj[1], d, l0.g);
+        else
+            k_pack<double><<<pack_grid(l0), 256, 0, S.stream>>>((const double *)l0.adj[1], d, l0.g);
+        S.check_launch();
+        std::vector<double> h;
+        if (on_device) {
+            const unsigned blocks = (unsigned)std::min<i64>(nblk(n, 256), 8 * S.nsm);
+            k_axpy<double><<<blocks, 256, 0, S.stream>>>(fbar, d, 1.0, n);
+            S.check_launch();
+        } else {
+            h.resize(n);
+            CK(cudaMemcpyAsync(h.data(), d, n * sizeof(double), cudaMemcpyDeviceToHost, S.stream));
+            CK(cudaStreamSynchronize(S.stream));
+            for (i64 i = 0; i < n; ++i) fbar[i] += h[i];
+        }
+    }
+    CK(cudaStreamSynchronize(S.stream));
+    API_END
+}

@@ -1104,6 +1104,26 @@ __global__ void __launch_bounds__(256) k_chol_gemv_upper(const MT *__restrict__ 
     }
 }
 
+// ------------------------------------------------------------- adjoint
+// y += alpha x over whole padded arrays (ghosts are zero in both).
+template <typename T>
+__global__ void __launch_bounds__(256) k_axpy(T *__restrict__ y, const T *__restrict__ x, T alpha, i64 n) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) y[i] += alpha * x[i];
+}
+
+// out_k = Sigma_k sum_j (S^{-1})_{jk} q_j: the transposed m x m solve of the
+// low-rank correction, scaled by Sigma so that k_add_Bq (which divides by
+// Sigma) applies B S^{-T} q.  One thread per k; SinvT row k is column k of
+// S^{-1}.
+__global__ void __launch_bounds__(256) k_sinvt_q(const double *__restrict__ SinvT, const double *__restrict__ q,
+                                                 const double *__restrict__ sigma_sqrt, double *__restrict__ out, int m) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    double t = 0.0;
+    for (int j = 0; j < m; ++j) t = fma(SinvT[(i64)k * m + j], q[j], t);
+    out[k] = sigma_sqrt[k] * sigma_sqrt[k] * t;
+}
+
 // ------------------------------------------------------------ step end
 // Observables z_p = b_p^T x of measure_sampling_time (sampling_time.cc:40),
 // one CTA per probe p (probe p's entries are bptr[p]..bptr[p+1]), stored at
