@@ -36,6 +36,10 @@ RADIUS = 0.05
 VARIANCE = 1e-4
 NLEVEL = 5
 IACT_WINDOW = 50
+# DRAM bytes (read + write) of one k_sweep_rb_vec launch at 256^3, from an
+# ncu capture of `python bench.py --profile-steps 1` (summary in
+# profiles/k_sweep_rb_vec_256cubed.md): 133.97 MB read + 24.84 MB written
+RB_VEC_DRAM_BYTES = 158.81e6
 METRIC = "indep. samples/s (rate/IACT), 3D 256³ posterior: mixed vs FP64 plain, 1 GB300"
 UNIT = "indep_samples/s"
 PUBLISHED_MGMC_IACT = 1.28  # python/plot_summary.py:28-29, MGMC at 64^3
@@ -344,7 +348,7 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--iact-samples", type=int, default=6000)
+    ap.add_argument("--iact-samples", type=int, default=12000)
     ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
@@ -415,7 +419,10 @@ def main():
     ach, bpl, tl = sweep_roofline(M, torch, s32, M.FP32_MIXED, peak)
     s32.close()
     # FP64 chain
-    s64, ms64, z64 = time_chain(M, torch, op, f, obs, M.FP64, args.steps, args.warmup, extra, dist, 2000 + rank)
+    # same seed: the FP64 chain draws the FP32 chain's normals (coupled
+    # chains), so the two IACT estimates share their Monte Carlo noise and
+    # the ratio of the two values is the cost ratio of equal-quality samples
+    s64, ms64, z64 = time_chain(M, torch, op, f, obs, M.FP64, args.steps, args.warmup, extra, dist, 1000 + rank)
     iact64 = M.statistics.tau_int(z64, IACT_WINDOW)
     ach64, bpl64, tl64 = sweep_roofline(M, torch, s64, M.FP64, peak)
     s64.close()
@@ -467,7 +474,7 @@ def main():
         "gpu_launches": int(launches * args.steps),
         "launches_per_step": int(launches),
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                     "traffic": None, "kernel": "k_sweep_rb_vec<float> (one colour pass of the fine-level red-black SOR sweep, Philox noise)",
+                     "traffic": RB_VEC_DRAM_BYTES, "traffic_unit": "bytes per launch (ncu dram__bytes_read+write)", "kernel": "k_sweep_rb_vec<float> (one colour pass of the fine-level red-black SOR sweep, Philox noise)",
                      "algorithmic_bytes_per_launch": bpl, "launch_s": tl, "peak_kind": peak_kind},
         "cpu_baseline": cpu,
     }

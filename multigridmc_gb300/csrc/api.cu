@@ -212,6 +212,8 @@ NoiseArgs Sampler::noise_args(int lev, i64 count) {
 // completed and flushed.  This hides the launch latency between the short
 // dependent kernels of a multigrid step.
 constexpr i64 PDL_MAX_POINTS = i64(1) << 22;
+// supports of C up to this many rows take the fused solve + correction
+constexpr i64 LR_FUSE_MAX_ROWS = i64(1) << 16;
 
 template <typename... KArgs, typename... Args>
 static void plaunch(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
@@ -350,7 +352,24 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     lr.part = lv.part;
     plaunch(S.pdl, k_bt_partial<T>, dim3(S.m, lv.bt_split), 256, 0, S.stream, (const T *)x, lr);
     const RowCsr &C = lv.C[dir];
-    if (C.nrows > 0) {
+    if (C.nrows > LR_FUSE_MAX_ROWS) {
+        // large support: one solve, then the correction on the whole GPU
+        const size_t smem = solve_smem(S.m);
+        if (noise == NOISE_NONE)
+            plaunch(S.pdl, k_lr_solve<NOISE_NONE, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
+        else if (noise == NOISE_PHILOX)
+            plaunch(S.pdl, k_lr_solve<NOISE_PHILOX, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
+        else
+            plaunch(S.pdl, k_lr_solve<NOISE_INJECTED, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
+        const unsigned blocks = (unsigned)std::min<i64>(nblk(C.nrows, 4 * 256), 8 * S.nsm);
+        if (sizeof(T) == 4)
+            plaunch(S.pdl, k_lr_scatter<T, float>, blocks, 256, 0, S.stream, x, C.nrows, C.rows, C.ptr, C.col,
+                    (const T *)C.val, (const float *)lv.zf);
+        else
+            plaunch(S.pdl, k_lr_scatter<T, double>, blocks, 256, 0, S.stream, x, C.nrows, C.rows, C.ptr, C.col,
+                    (const T *)C.val, (const double *)lv.z);
+        S.launches++;
+    } else if (C.nrows > 0) {
         // solve and correction in one launch; every CTA repeats the (FP64)
         // m x m solve, so the grid stays at two CTAs per SM at most
         const unsigned blocks = (unsigned)std::min<i64>(nblk(C.nrows, 256), 2 * S.nsm);

@@ -13,6 +13,7 @@
 //   k_bt_partial        partial sums of y = B^T x
 //   k_lr_solve          y and the m x m low-rank solve
 //   k_lr_apply          the solve and x += C z over the rows of C = M^{-1} B
+//   k_lr_scatter        x += C z (large supports, after k_lr_solve)
 //   k_resid_restrict_tiled  f_c = R (f - A_0 x)  (fused residual + restriction)
 //   k_sub_Bq            f_c -= B_c Sigma^{-1} y
 //   k_prolong_add       x += alpha P x_c
@@ -540,6 +541,40 @@ __global__ void __launch_bounds__(256) k_lr_apply(T *__restrict__ x, LowRankArg 
         for (int j = 0; j < 4; ++j) {
             accv[j] = T(0);
             for (i64 e = e0[j]; e < e1[j]; ++e) accv[j] += val[e] * (T)zs[col[e]];
+        }
+        T xv[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) xv[j] = rr[j] >= 0 ? x[rr[j]] : T(0);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (rr[j] >= 0) x[rr[j]] = xv[j] + accv[j];
+    }
+}
+
+// x[row] += sum_e C_e z_{col_e} over the support rows of C = M^{-1} B, with
+// the coefficients z of k_lr_solve (ZT = float: the FP32 chain's rounded
+// copy), four rows per thread and iteration with their loads issued together.
+template <typename T, typename ZT>
+__global__ void __launch_bounds__(256) k_lr_scatter(T *__restrict__ x, i64 nrows, const i64 *__restrict__ rows,
+                                                     const i64 *__restrict__ ptr, const int *__restrict__ col,
+                                                     const T *__restrict__ val, const ZT *__restrict__ z) {
+    pdl_begin();
+    const i64 stride = (i64)gridDim.x * blockDim.x;
+    for (i64 r0 = (i64)blockIdx.x * blockDim.x + threadIdx.x; r0 < nrows; r0 += 4 * stride) {
+        i64 rr[4], e0[4], e1[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const i64 r = r0 + j * stride;
+            const bool ok = r < nrows;
+            rr[j] = ok ? rows[r] : -1;
+            e0[j] = ok ? ptr[r] : 0;
+            e1[j] = ok ? ptr[r + 1] : 0;
+        }
+        T accv[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            accv[j] = T(0);
+            for (i64 e = e0[j]; e < e1[j]; ++e) accv[j] += val[e] * (T)z[col[e]];
         }
         T xv[4];
 #pragma unroll
