@@ -113,6 +113,22 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def replica_max(values, dist, device):
+    """Max over the ranks of per-rank times (the slowest replica sets the
+    job's time); `dist` is torch.distributed or None for one process."""
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def replica_rate(world, seconds_per_step, iact):
+    """Whole-job independent samples/s of `world` replica chains, each taking
+    `seconds_per_step` (the max over ranks) per step."""
+    return world / seconds_per_step / iact
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -427,18 +443,13 @@ def main():
     ach64, bpl64, tl64 = sweep_roofline(M, torch, s64, M.FP64, peak)
     s64.close()
 
-    ms_t = torch.tensor([ms32, ms64], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms32, ms64 = ms_t.tolist()
-    value = world * 1000.0 / ms32 / iact32
-    value64 = world * 1000.0 / ms64 / iact64
+    ms32, ms64 = replica_max([ms32, ms64], dist, "cuda")
+    value = replica_rate(world, ms32 / 1000.0, iact32)
+    value64 = replica_rate(world, ms64 / 1000.0, iact64)
 
     e2e_val, e2e_dt, h2d, d2h = time_e2e(M, torch, op, f, M.FP32_MIXED, args.e2e_steps, 1000 + rank, iact32)
-    e2e_t = torch.tensor([e2e_dt], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_val = world / e2e_t.item() / iact32
+    (e2e_dt,) = replica_max([e2e_dt], dist, "cuda")
+    e2e_val = replica_rate(world, e2e_dt, iact32)
 
     if rank != 0:
         return
