@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_pass(T *__restrict__ x
 // the matching spans of the four neighbouring rows and f as float4, draws
 // one Philox block for its 4 points of the colour and stores those 4 points.
 template <int NOISE>
-__global__ void __launch_bounds__(RBP_THREADS, 4) k_sweep_rb_vec(float *__restrict__ x, const float *__restrict__ f,
+__global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict__ x, const float *__restrict__ f,
                                                               Grid3 g, StencilArg<float> s, int colour, int reverse,
                                                               NoiseArgs nz) {
     if (g.pdl) pdl_begin();
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(RBP_THREADS, 4) k_sweep_rb_vec(float *__restri
     const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     const int ngrp = (g.N0 + 8) >> 3;
-    const bool active = q < ngrp && b < g.N1;
+    if (q >= ngrp || b >= g.N1) return;
     const int P0 = 8 * q;
     const i64 rb = (i64)(c + 1) * g.sz + (i64)(b + 1) * g.sy;
     const float4 *xr = reinterpret_cast<const float4 *>(x + rb + P0);
@@ -249,19 +249,11 @@ __global__ void __launch_bounds__(RBP_THREADS, 4) k_sweep_rb_vec(float *__restri
     const float4 *fr = reinterpret_cast<const float4 *>(f + rb + P0);
     float v[10], ym[8], yp[8], zm[8], zp[8], fv[8];
     {
-        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 a0 = active ? xr[0] : z4, a1 = active ? xr[1] : z4;
+        const float4 a0 = xr[0], a1 = xr[1];
+        v[0] = P0 > 0 ? x[rb + P0 - 1] : 0.f;  // P0 - 1 is a ghost column for q = 0 (read 0 directly)
         v[1] = a0.x; v[2] = a0.y; v[3] = a0.z; v[4] = a0.w;
         v[5] = a1.x; v[6] = a1.y; v[7] = a1.z; v[8] = a1.w;
-        // x-halo of the span from the neighbouring lanes of the same row
-        // (every lane of the warp takes part in the shuffles); the lanes at a
-        // warp or row end read it (position P0 - 1 is the zero ghost for q = 0)
-        const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
-        const float left = __shfl_up_sync(0xffffffffu, v[8], 1);
-        const float right = __shfl_down_sync(0xffffffffu, v[1], 1);
-        if (!active) return;
-        v[0] = (lane > 0 && threadIdx.x > 0) ? left : (P0 > 0 ? x[rb + P0 - 1] : 0.f);
-        v[9] = (lane < 31 && threadIdx.x + 1 < blockDim.x && q + 1 < ngrp) ? right : x[rb + P0 + 8];
+        v[9] = x[rb + P0 + 8];
         const float4 n0 = xn[0], n1 = xn[1], s0 = xs_[0], s1 = xs_[1], d0 = xd[0], d1 = xd[1], u0 = xu[0], u1 = xu[1];
         const float4 f0 = fr[0], f1 = fr[1];
         ym[0] = n0.x; ym[1] = n0.y; ym[2] = n0.z; ym[3] = n0.w; ym[4] = n1.x; ym[5] = n1.y; ym[6] = n1.z; ym[7] = n1.w;
