@@ -842,6 +842,125 @@ __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tma(const __grid_
     if (xc) xc[gc.pad(ca, cb, cc)] = T(0);  // the coarse sample starts from zero
 }
 
+// TMA variant of the FP32 red-black colour pass for rows of at most 256
+// floats that are a multiple of 16 bytes: a CTA of 32 x 8 threads owns 8
+// rows of one plane; thread 0 copies the 10 x 3 rows around them (planes
+// c - 1 .. c + 1, rows b0 - 1 .. b0 + 8) and the 8 rows of f into shared
+// memory with two bulk tensor copies, so the five neighbour spans of a
+// thread are shared-memory loads instead of L1 requests.  The update of a
+// span and its two float4 stores are those of k_sweep_rb_vec.  Rows beyond
+// the plane read as zero, like the ghost row they stand for.
+constexpr int RBT_ROWS = 8;
+
+__host__ __device__ __forceinline__ size_t rbt_xtile_bytes(i64 W) {
+    return ((size_t)3 * (RBT_ROWS + 2) * (size_t)W * sizeof(float) + 127) / 128 * 128;
+}
+__host__ __device__ __forceinline__ size_t rbt_smem_bytes(i64 W) {
+    return rbt_xtile_bytes(W) + (size_t)RBT_ROWS * (size_t)W * sizeof(float);
+}
+
+template <int NOISE>
+__global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_tma(const __grid_constant__ CUtensorMap xmap,
+                                                              const __grid_constant__ CUtensorMap fmap,
+                                                              float *__restrict__ x, Grid3 g, StencilArg<float> s,
+                                                              int colour, int reverse, NoiseArgs nz,
+                                                              unsigned *__restrict__ err) {
+    if (g.pdl) pdl_begin();
+    extern __shared__ __align__(1024) unsigned char rbt_smem[];
+    __shared__ unsigned long long bar;
+    const int W = (int)g.sy;
+    float *xt = reinterpret_cast<float *>(rbt_smem);                        // [3][RBT_ROWS + 2][W]
+    float *ft = reinterpret_cast<float *>(rbt_smem + rbt_xtile_bytes(W));  // [RBT_ROWS][W]
+    const int b0 = blockIdx.y * RBT_ROWS;
+    const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if (tid == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (tid == 0) {
+        mbar_expect_tx(&bar, (unsigned)(sizeof(float) * W * (3 * (RBT_ROWS + 2) + RBT_ROWS)));
+        tma_load_3d(xt, &xmap, 0, b0, c, &bar);         // padded rows b0.., planes c.. (fine b0 - 1, c - 1)
+        tma_load_3d(ft, &fmap, 0, b0 + 1, c + 1, &bar);  // fine rows b0.., plane c
+    }
+    const bool ok = mbar_wait_bounded(&bar, 0, TILE_WAIT_NS);
+    if (__syncthreads_or(!ok)) {
+        if (tid == 0) atomicOr(err, ERR_TILE_TIMEOUT);
+        mbar_wait_bounded(&bar, 0, TILE_WAIT_NS);
+        return;
+    }
+    const int q = threadIdx.x, r = threadIdx.y, b = b0 + r;
+    const int ngrp = (g.N0 + 8) >> 3;
+    if (q >= ngrp || b >= g.N1) return;
+    const int P0 = 8 * q;
+    const float *rowc = xt + (i64)((RBT_ROWS + 2) + r + 1) * W;  // plane c, row b
+    const float *rowd = rowc - (i64)(RBT_ROWS + 2) * W;           // plane c - 1
+    const float *rowu = rowc + (i64)(RBT_ROWS + 2) * W;           // plane c + 1
+    const float *rowf = ft + (i64)r * W;
+    float v[10], ym[8], yp[8], zm[8], zp[8], fv[8];
+    {
+        const float4 *pc = reinterpret_cast<const float4 *>(rowc + P0);
+        const float4 *pn = reinterpret_cast<const float4 *>(rowc - W + P0);
+        const float4 *ps = reinterpret_cast<const float4 *>(rowc + W + P0);
+        const float4 *pd = reinterpret_cast<const float4 *>(rowd + P0);
+        const float4 *pu = reinterpret_cast<const float4 *>(rowu + P0);
+        const float4 *pf = reinterpret_cast<const float4 *>(rowf + P0);
+        const float4 a0 = pc[0], a1 = pc[1];
+        v[0] = P0 > 0 ? rowc[P0 - 1] : 0.f;
+        v[1] = a0.x; v[2] = a0.y; v[3] = a0.z; v[4] = a0.w;
+        v[5] = a1.x; v[6] = a1.y; v[7] = a1.z; v[8] = a1.w;
+        v[9] = P0 + 8 < W ? rowc[P0 + 8] : 0.f;  // position sy is the next row's zero ghost
+        const float4 n0 = pn[0], n1 = pn[1], s0 = ps[0], s1 = ps[1], d0 = pd[0], d1 = pd[1], u0 = pu[0], u1 = pu[1];
+        const float4 f0 = pf[0], f1 = pf[1];
+        ym[0] = n0.x; ym[1] = n0.y; ym[2] = n0.z; ym[3] = n0.w; ym[4] = n1.x; ym[5] = n1.y; ym[6] = n1.z; ym[7] = n1.w;
+        yp[0] = s0.x; yp[1] = s0.y; yp[2] = s0.z; yp[3] = s0.w; yp[4] = s1.x; yp[5] = s1.y; yp[6] = s1.z; yp[7] = s1.w;
+        zm[0] = d0.x; zm[1] = d0.y; zm[2] = d0.z; zm[3] = d0.w; zm[4] = d1.x; zm[5] = d1.y; zm[6] = d1.z; zm[7] = d1.w;
+        zp[0] = u0.x; zp[1] = u0.y; zp[2] = u0.z; zp[3] = u0.w; zp[4] = u1.x; zp[5] = u1.y; zp[6] = u1.z; zp[7] = u1.w;
+        fv[0] = f0.x; fv[1] = f0.y; fv[2] = f0.z; fv[3] = f0.w; fv[4] = f1.x; fv[5] = f1.y; fv[6] = f1.z; fv[7] = f1.w;
+    }
+    const int j0 = (colour + b + c + 1) & 1;
+    float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (NOISE == NOISE_PHILOX) nrm = fine_normals(nz, g, P0 + j0, b, c);
+    auto upd = [&](int j, int k) {
+        const int a = P0 + j - 1;
+        if (a < 0 || a >= g.N0) return;
+        float xi = 0.f;
+        if (NOISE == NOISE_PHILOX) xi = pick(nrm, k);
+        if (NOISE == NOISE_INJECTED) xi = (float)nz.buf[g.compact(a, b, c)];
+        float res = s.w[4] * zm[j];
+        res = fmaf(s.w[10], ym[j], res);
+        res = fmaf(s.w[12], v[j], res);
+        res = fmaf(s.w[13], v[j + 1], res);
+        res = fmaf(s.w[14], v[j + 2], res);
+        res = fmaf(s.w[16], yp[j], res);
+        res = fmaf(s.w[22], zp[j], res);
+        float cval = fv[j];
+        if (NOISE != NOISE_NONE) cval = fmaf(s.sd, xi, cval);
+        v[j + 1] = v[j + 1] + s.omega_diag * (cval - res);
+    };
+    if (j0 == 0) {
+        upd(0, 0);
+        upd(2, 1);
+        upd(4, 2);
+        upd(6, 3);
+    } else {
+        upd(1, 0);
+        upd(3, 1);
+        upd(5, 2);
+        upd(7, 3);
+    }
+    const i64 rb = (i64)(c + 1) * g.sz + (i64)(b + 1) * g.sy;
+    float4 *xo = reinterpret_cast<float4 *>(x + rb + P0);
+    xo[0] = make_float4(v[1], v[2], v[3], v[4]);
+    if (P0 + 8 <= g.sy) {
+        xo[1] = make_float4(v[5], v[6], v[7], v[8]);
+    } else {
+#pragma unroll
+        for (int j = 4; j < 8; ++j) {
+            const int a = P0 + j - 1;
+            if (((j - j0) & 1) == 0 && a >= 0 && a < g.N0) x[rb + P0 + j] = v[j + 1];
+        }
+    }
+}
+
 // dst[row] += sign * sum_e B_e y_{col_e} / Sigma_{col_e} over the rows of B
 // (row-compressed): the B Sigma^{-1} B^T x part of A x.
 template <typename T>
