@@ -91,6 +91,7 @@ struct Level {
     bool tma = false;            // maps valid (3D, rows of a multiple of 16 bytes)
     CUtensorMap sxmap{}, sfmap{};  // FP32 sweep tiles (k_sweep_rb_tma): 3 planes x 10 rows of x, 8 rows of f
     bool sweep_tma = false;
+    int sweep_ctas_per_sm = 1;  // resident CTAs of k_sweep_rb_pipe per SM
 };
 
 struct Sampler {
@@ -267,9 +268,14 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
             const int colour = forward ? pass : 1 - pass;
             if constexpr (std::is_same<T, float>::value) {
                 if (vec && lv.sweep_tma && S.sweep_tma && x == lv.x && f == lv.f) {
-                    dim3 grid(1, (lv.g.N1 + RBT_ROWS - 1) / RBT_ROWS, lv.g.N2);
-                    plaunch(S.pdl && lv.g.pdl, k_sweep_rb_tma<NOISE>, grid, dim3(32, RBT_ROWS), rbt_smem_bytes(lv.g.sy),
-                            S.stream, lv.sxmap, lv.sfmap, x, lv.g, s, colour, pass, nz, S.d_err);
+                    // row blocks x plane chunks: one wave of resident CTAs
+                    const int rowblocks = (lv.g.N1 + RBQ_R - 1) / RBQ_R;
+                    const int want = std::max(1, std::min(lv.g.N2, lv.sweep_ctas_per_sm * S.nsm / rowblocks));
+                    const int cz = (lv.g.N2 + want - 1) / want;
+                    const int nchunk = (lv.g.N2 + cz - 1) / cz;
+                    plaunch(S.pdl && lv.g.pdl, k_sweep_rb_pipe<NOISE>, dim3(rowblocks, nchunk), dim3(32, RBQ_R),
+                            rbq_smem_bytes(lv.g.sy), S.stream, lv.sxmap, lv.sfmap, x, lv.g, s, colour, pass, cz, nz,
+                            S.d_err);
                     S.launches++;
                     continue;
                 }
@@ -855,12 +861,23 @@ void Sampler::make_tile_maps(Level &lv) {
     lv.tma = true;
     // tiles of the TMA colour pass: whole rows (at most 256 floats)
     if (fp32 && lv.g.sy <= 256) {
-        const cuuint32_t sxbox[3] = {(cuuint32_t)lv.g.sy, RBT_ROWS + 2, 3}, sfbox[3] = {(cuuint32_t)lv.g.sy, RBT_ROWS, 1};
+        const cuuint32_t sxbox[3] = {(cuuint32_t)lv.g.sy, RBQ_R + 2, 1}, sfbox[3] = {(cuuint32_t)lv.g.sy, RBQ_R, 1};
         if (enc(&lv.sxmap, dt, 3, lv.x, dims, strides, sxbox, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS &&
             enc(&lv.sfmap, dt, 3, lv.f, dims, strides, sfbox, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
             lv.sweep_tma = true;
+    }
+    if (lv.sweep_tma) {
+        // all of the SM's unified L1/shared storage as shared memory: four CTAs' slab rings per SM
+        for (auto k : {k_sweep_rb_pipe<NOISE_NONE>, k_sweep_rb_pipe<NOISE_PHILOX>, k_sweep_rb_pipe<NOISE_INJECTED>}) {
+            CK(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+            raise_smem_limit(k, rbq_smem_bytes(lv.g.sy));
+        }
+        int nb = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_sweep_rb_pipe<NOISE_PHILOX>, 32 * RBQ_R,
+                                                         rbq_smem_bytes(lv.g.sy)));
+        lv.sweep_ctas_per_sm = std::max(1, nb);
     }
 }
 
