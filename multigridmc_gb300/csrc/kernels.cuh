@@ -862,9 +862,12 @@ __device__ __forceinline__ void ld8(const float *p, float *r) {
     r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
 }
 
-__host__ __device__ __forceinline__ size_t rbq_xslab_floats(i64 W) { return (size_t)(RBQ_R + 2) * (size_t)W; }
+// Slab strides rounded up to 128 bytes: every bulk tensor copy lands on a
+// 128-byte aligned shared-memory address whatever the row width.
+__host__ __device__ __forceinline__ size_t rbq_xslab_floats(i64 W) { return ((size_t)(RBQ_R + 2) * (size_t)W + 31) / 32 * 32; }
+__host__ __device__ __forceinline__ size_t rbq_fslab_floats(i64 W) { return ((size_t)RBQ_R * (size_t)W + 31) / 32 * 32; }
 __host__ __device__ __forceinline__ size_t rbq_smem_bytes(i64 W) {
-    return sizeof(float) * (RBQ_NX * rbq_xslab_floats(W) + RBQ_NF * (size_t)RBQ_R * (size_t)W);
+    return sizeof(float) * (RBQ_NX * rbq_xslab_floats(W) + RBQ_NF * rbq_fslab_floats(W));
 }
 
 template <int NOISE>
@@ -877,7 +880,7 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_pipe(const __grid_cons
     extern __shared__ __align__(1024) unsigned char rbq_smem[];
     __shared__ unsigned long long xbar[RBQ_NX], fbar[RBQ_NF];
     const int W = (int)g.sy;
-    const size_t XS = rbq_xslab_floats(W), FS = (size_t)RBQ_R * W;
+    const size_t XS = rbq_xslab_floats(W), FS = rbq_fslab_floats(W);
     float *xsl = reinterpret_cast<float *>(rbq_smem);  // [RBQ_NX][RBQ_R + 2][W]
     float *fsl = xsl + RBQ_NX * XS;                      // [RBQ_NF][RBQ_R][W]
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
@@ -891,7 +894,7 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_pipe(const __grid_cons
     // f of plane p is the j-th f copy, j = d (p - cs)
     auto xk = [&](int p) { return d * (p - (cs - d)); };
     auto fj = [&](int p) { return d * (p - cs); };
-    const unsigned xbytes = (unsigned)(sizeof(float) * XS), fbytes = (unsigned)(sizeof(float) * FS);
+    const unsigned xbytes = (unsigned)(sizeof(float) * (RBQ_R + 2) * W), fbytes = (unsigned)(sizeof(float) * RBQ_R * W);
     auto load_x = [&](int p) {  // p in [-1, N2]: padded plane p + 1
         const int k = xk(p), sl = k % RBQ_NX;
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
