@@ -89,9 +89,6 @@ struct Level {
     void *adj[4] = {nullptr, nullptr, nullptr, nullptr};  // adjoint: x-bar, f-bar, two work vectors (T, padded)
     CUtensorMap xmap{}, fmap{};  // 3D tile maps of x and f for the residual-restriction
     bool tma = false;            // maps valid (3D, rows of a multiple of 16 bytes)
-    CUtensorMap sxmap{}, sfmap{};  // FP32 sweep tiles (k_sweep_rb_tma): 3 planes x 10 rows of x, 8 rows of f
-    bool sweep_tma = false;
-    int sweep_ctas_per_sm = 1;  // resident CTAs of k_sweep_rb_pipe per SM
 };
 
 struct Sampler {
@@ -99,7 +96,6 @@ struct Sampler {
     int dim = 3, m = 0;
     bool fp32 = false, exact = false;
     int nsm = 152;    // SMs of the device
-    bool sweep_tma = true;  // TMA tiles for the FP32 fine colour pass (MGMC_SWEEP_TMA=0: plain loads)
     bool pdl = true;  // programmatic dependent launch between step kernels (MGMC_NO_PDL=1 turns it off)
     int noise_mode = NOISE_PHILOX;
     std::vector<Level> L;
@@ -267,18 +263,6 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
         for (int pass = 0; pass < 2; ++pass) {
             const int colour = forward ? pass : 1 - pass;
             if constexpr (std::is_same<T, float>::value) {
-                if (vec && lv.sweep_tma && S.sweep_tma && x == lv.x && f == lv.f) {
-                    // row blocks x plane chunks: one wave of resident CTAs
-                    const int rowblocks = (lv.g.N1 + RBQ_R - 1) / RBQ_R;
-                    const int want = std::max(1, std::min(lv.g.N2, lv.sweep_ctas_per_sm * S.nsm / rowblocks));
-                    const int cz = (lv.g.N2 + want - 1) / want;
-                    const int nchunk = (lv.g.N2 + cz - 1) / cz;
-                    plaunch(S.pdl && lv.g.pdl, k_sweep_rb_pipe<NOISE>, dim3(rowblocks, nchunk), dim3(32, RBQ_R),
-                            rbq_smem_bytes(lv.g.sy), S.stream, lv.sxmap, lv.sfmap, x, lv.g, s, colour, pass, cz, nz,
-                            S.d_err);
-                    S.launches++;
-                    continue;
-                }
                 if (vec) {
                     const int ngrp = (lv.g.N0 + 8) / 8;
                     const dim3 blk = sweep_block(ngrp);
@@ -859,26 +843,6 @@ void Sampler::make_tile_maps(Level &lv) {
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return;
     lv.tma = true;
-    // tiles of the TMA colour pass: whole rows (at most 256 floats)
-    if (fp32 && lv.g.sy <= 256) {
-        const cuuint32_t sxbox[3] = {(cuuint32_t)lv.g.sy, RBQ_R + 2, 1}, sfbox[3] = {(cuuint32_t)lv.g.sy, RBQ_R, 1};
-        if (enc(&lv.sxmap, dt, 3, lv.x, dims, strides, sxbox, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS &&
-            enc(&lv.sfmap, dt, 3, lv.f, dims, strides, sfbox, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
-            lv.sweep_tma = true;
-    }
-    if (lv.sweep_tma) {
-        // all of the SM's unified L1/shared storage as shared memory: four CTAs' slab rings per SM
-        for (auto k : {k_sweep_rb_pipe<NOISE_NONE>, k_sweep_rb_pipe<NOISE_PHILOX>, k_sweep_rb_pipe<NOISE_INJECTED>}) {
-            CK(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-            raise_smem_limit(k, rbq_smem_bytes(lv.g.sy));
-        }
-        int nb = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_sweep_rb_pipe<NOISE_PHILOX>, 32 * RBQ_R,
-                                                         rbq_smem_bytes(lv.g.sy)));
-        lv.sweep_ctas_per_sm = std::max(1, nb);
-    }
 }
 
 void Sampler::build(const mgmc_operator_desc &op) {
@@ -909,8 +873,6 @@ void Sampler::build(const mgmc_operator_desc &op) {
     {
         const char *e = std::getenv("MGMC_NO_PDL");
         pdl = !(e && e[0] == '1');
-        const char *st = std::getenv("MGMC_SWEEP_TMA");
-        sweep_tma = !(st && st[0] == '0');
     }
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     raise_smem_limit(k_resid_restrict_tiled<double, 7>, rr_smem_bytes<double>());

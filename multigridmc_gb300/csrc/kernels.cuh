@@ -842,179 +842,6 @@ __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tma(const __grid_
     if (xc) xc[gc.pad(ca, cb, cc)] = T(0);  // the coarse sample starts from zero
 }
 
-// Pipelined TMA variant of the FP32 red-black colour pass (rows of at most
-// 256 floats, a multiple of 16 bytes).  A CTA of 32 x RBQ_R threads owns
-// RBQ_R rows and walks the planes of one chunk (upwards, or downwards for the
-// second colour).  Thread 0 keeps a ring of RBQ_NX shared-memory slabs of
-// RBQ_R + 2 rows (the CTA's rows and their y-neighbours) filled by bulk
-// tensor copies three planes ahead, plus RBQ_NF slabs of f; every other
-// thread reads its five neighbour spans from shared memory, so x and f come
-// from DRAM once and the L1 load pipeline only carries shared-memory loads.
-// Points of one colour only have neighbours of the other colour, which this
-// pass does not change, so slabs copied while neighbouring CTAs write their
-// own points stay valid.  Waits are bounded (TILE_WAIT_NS); a timeout sets
-// the error bit and drains the copies in flight before the CTA exits.
-constexpr int RBQ_R = 8, RBQ_NX = 4, RBQ_NF = 2;
-
-__device__ __forceinline__ void ld8(const float *p, float *r) {
-    const float4 a = reinterpret_cast<const float4 *>(p)[0], b = reinterpret_cast<const float4 *>(p)[1];
-    r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
-    r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
-}
-
-// Slab strides rounded up to 128 bytes: every bulk tensor copy lands on a
-// 128-byte aligned shared-memory address whatever the row width.
-__host__ __device__ __forceinline__ size_t rbq_xslab_floats(i64 W) { return ((size_t)(RBQ_R + 2) * (size_t)W + 31) / 32 * 32; }
-__host__ __device__ __forceinline__ size_t rbq_fslab_floats(i64 W) { return ((size_t)RBQ_R * (size_t)W + 31) / 32 * 32; }
-__host__ __device__ __forceinline__ size_t rbq_smem_bytes(i64 W) {
-    return sizeof(float) * (RBQ_NX * rbq_xslab_floats(W) + RBQ_NF * rbq_fslab_floats(W));
-}
-
-template <int NOISE>
-__global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_pipe(const __grid_constant__ CUtensorMap xmap,
-                                                               const __grid_constant__ CUtensorMap fmap,
-                                                               float *__restrict__ x, Grid3 g, StencilArg<float> s,
-                                                               int colour, int reverse, int cz, NoiseArgs nz,
-                                                               unsigned *__restrict__ err) {
-    if (g.pdl) pdl_begin();
-    extern __shared__ __align__(1024) unsigned char rbq_smem[];
-    __shared__ unsigned long long xbar[RBQ_NX], fbar[RBQ_NF];
-    const int W = (int)g.sy;
-    const size_t XS = rbq_xslab_floats(W), FS = rbq_fslab_floats(W);
-    float *xsl = reinterpret_cast<float *>(rbq_smem);  // [RBQ_NX][RBQ_R + 2][W]
-    float *fsl = xsl + RBQ_NX * XS;                      // [RBQ_NF][RBQ_R][W]
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int b0 = blockIdx.x * RBQ_R;
-    const int chunk = reverse ? (int)gridDim.y - 1 - (int)blockIdx.y : (int)blockIdx.y;
-    const int cA = chunk * cz, cB = min(g.N2, cA + cz);
-    const int d = reverse ? -1 : 1;
-    const int cs = reverse ? cB - 1 : cA;  // first plane of the walk
-    const int n = cB - cA;                  // planes walked
-    // plane p is the k-th slab copy, k = d (p - (cs - d)); slot k % RBQ_NX, phase parity (k / RBQ_NX) & 1;
-    // f of plane p is the j-th f copy, j = d (p - cs)
-    auto xk = [&](int p) { return d * (p - (cs - d)); };
-    auto fj = [&](int p) { return d * (p - cs); };
-    const unsigned xbytes = (unsigned)(sizeof(float) * (RBQ_R + 2) * W), fbytes = (unsigned)(sizeof(float) * RBQ_R * W);
-    auto load_x = [&](int p) {  // p in [-1, N2]: padded plane p + 1
-        const int k = xk(p), sl = k % RBQ_NX;
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect_tx(&xbar[sl], xbytes);
-        tma_load_3d(xsl + sl * XS, &xmap, 0, b0, p + 1, &xbar[sl]);
-    };
-    auto load_f = [&](int p) {
-        const int j = fj(p), sl = j % RBQ_NF;
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect_tx(&fbar[sl], fbytes);
-        tma_load_3d(fsl + sl * FS, &fmap, 0, b0 + 1, p + 1, &fbar[sl]);
-    };
-    if (tid == 0) {
-        for (int i = 0; i < RBQ_NX; ++i) mbar_init(&xbar[i], 1);
-        for (int i = 0; i < RBQ_NF; ++i) mbar_init(&fbar[i], 1);
-    }
-    __syncthreads();
-    if (tid == 0 && n > 0) {
-        for (int i = 0; i < 4; ++i) {  // planes cs - d .. cs + 2d
-            const int p = cs + (i - 1) * d;
-            if (p >= -1 && p <= g.N2 && i <= n + 1) load_x(p);
-        }
-        load_f(cs);
-        if (n > 1) load_f(cs + d);
-    }
-    const int q = threadIdx.x, r = threadIdx.y, b = b0 + r;
-    const int ngrp = (g.N0 + 8) >> 3;
-    const bool active = q < ngrp && b < g.N1;
-    const int P0 = 8 * q;
-    bool failed = false;
-    for (int it = 0; it < n; ++it) {
-        const int c = cs + it * d;
-        // slabs of planes c - 1, c, c + 1 and f of plane c
-        bool ok = true;
-        for (int dz = -1; dz <= 1; ++dz) {
-            const int k = xk(c + dz);
-            ok = ok && mbar_wait_bounded(&xbar[k % RBQ_NX], (unsigned)((k / RBQ_NX) & 1), TILE_WAIT_NS);
-        }
-        {
-            const int j = fj(c);
-            ok = ok && mbar_wait_bounded(&fbar[j % RBQ_NF], (unsigned)((j / RBQ_NF) & 1), TILE_WAIT_NS);
-        }
-        if (__syncthreads_or(!ok)) {
-            failed = true;
-            break;
-        }
-        if (active) {
-            const float *rowc = xsl + (xk(c) % RBQ_NX) * XS + (size_t)(r + 1) * W;
-            const float *rowd = xsl + (xk(c - 1) % RBQ_NX) * XS + (size_t)(r + 1) * W;
-            const float *rowu = xsl + (xk(c + 1) % RBQ_NX) * XS + (size_t)(r + 1) * W;
-            const float *rowf = fsl + (fj(c) % RBQ_NF) * FS + (size_t)r * W;
-            float v[10], ym[8], yp[8], zm[8], zp[8], fv[8];
-            ld8(rowc + P0, v + 1);
-            v[0] = P0 > 0 ? rowc[P0 - 1] : 0.f;
-            v[9] = P0 + 8 < W ? rowc[P0 + 8] : 0.f;  // position sy is the next row's zero ghost
-            ld8(rowc - W + P0, ym);
-            ld8(rowc + W + P0, yp);
-            ld8(rowd + P0, zm);
-            ld8(rowu + P0, zp);
-            ld8(rowf + P0, fv);
-            const int j0 = (colour + b + c + 1) & 1;
-            float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (NOISE == NOISE_PHILOX) nrm = fine_normals(nz, g, P0 + j0, b, c);
-            auto upd = [&](int j, int k) {
-                const int a = P0 + j - 1;
-                if (a < 0 || a >= g.N0) return;
-                float xi = 0.f;
-                if (NOISE == NOISE_PHILOX) xi = pick(nrm, k);
-                if (NOISE == NOISE_INJECTED) xi = (float)nz.buf[g.compact(a, b, c)];
-                float res = s.w[4] * zm[j];
-                res = fmaf(s.w[10], ym[j], res);
-                res = fmaf(s.w[12], v[j], res);
-                res = fmaf(s.w[13], v[j + 1], res);
-                res = fmaf(s.w[14], v[j + 2], res);
-                res = fmaf(s.w[16], yp[j], res);
-                res = fmaf(s.w[22], zp[j], res);
-                float cval = fv[j];
-                if (NOISE != NOISE_NONE) cval = fmaf(s.sd, xi, cval);
-                v[j + 1] = v[j + 1] + s.omega_diag * (cval - res);
-            };
-            if (j0 == 0) {
-                upd(0, 0);
-                upd(2, 1);
-                upd(4, 2);
-                upd(6, 3);
-            } else {
-                upd(1, 0);
-                upd(3, 1);
-                upd(5, 2);
-                upd(7, 3);
-            }
-            const i64 rb = (i64)(c + 1) * g.sz + (i64)(b + 1) * g.sy;
-            float4 *xo = reinterpret_cast<float4 *>(x + rb + P0);
-            xo[0] = make_float4(v[1], v[2], v[3], v[4]);
-            if (P0 + 8 <= g.sy) {
-                xo[1] = make_float4(v[5], v[6], v[7], v[8]);
-            } else {
-#pragma unroll
-                for (int j = 4; j < 8; ++j) {
-                    const int a = P0 + j - 1;
-                    if (((j - j0) & 1) == 0 && a >= 0 && a < g.N0) x[rb + P0 + j] = v[j + 1];
-                }
-            }
-        }
-        __syncthreads();  // every thread is done with the slab of plane c - d and f of plane c
-        if (tid == 0) {
-            if (it + 3 <= n && c + 3 * d >= -1 && c + 3 * d <= g.N2) load_x(c + 3 * d);  // z-neighbour of plane c + 2d
-            if (it + 2 < n) load_f(c + 2 * d);
-        }
-    }
-    if (failed) {
-        if (tid == 0) {
-            atomicOr(err, ERR_TILE_TIMEOUT);
-            // let every copy in flight land before the CTA's shared memory is released
-            for (int i = 0; i < RBQ_NX; ++i) mbar_wait_bounded(&xbar[i], 0, TILE_WAIT_NS), mbar_wait_bounded(&xbar[i], 1, TILE_WAIT_NS);
-            for (int i = 0; i < RBQ_NF; ++i) mbar_wait_bounded(&fbar[i], 0, TILE_WAIT_NS), mbar_wait_bounded(&fbar[i], 1, TILE_WAIT_NS);
-        }
-    }
-}
-
 // dst[row] += sign * sum_e B_e y_{col_e} / Sigma_{col_e} over the rows of B
 // (row-compressed): the B Sigma^{-1} B^T x part of A x.
 template <typename T>
