@@ -86,6 +86,7 @@ struct Level {
     double *y = nullptr, *z = nullptr, *part = nullptr;
     float *zf = nullptr, *Bvalf = nullptr;
     int bt_split = 1;  // blocks per column of the B^T x reduction
+    unsigned *counter = nullptr;  // CTA counter of k_bt_solve
     void *adj[4] = {nullptr, nullptr, nullptr, nullptr};  // adjoint: x-bar, f-bar, two work vectors (T, padded)
     CUtensorMap xmap{}, fmap{};  // 3D tile maps of x and f for the residual-restriction
     bool tma = false;            // maps valid (3D, rows of a multiple of 16 bytes)
@@ -350,17 +351,19 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     lr.y = lv.y;
     lr.z = lv.z;
     lr.part = lv.part;
-    plaunch(S.pdl, k_bt_partial<T>, dim3(S.m, lv.bt_split), 256, 0, S.stream, (const T *)x, lr);
+    lr.counter = lv.counter;
     const RowCsr &C = lv.C[dir];
+    const dim3 bgrid(S.m, lv.bt_split);
     if (C.nrows > LR_FUSE_MAX_ROWS) {
-        // large support: one solve, then the correction on the whole GPU
+        // large support: partial sums with the solve in their last CTA, then
+        // the correction on the whole GPU
         const size_t smem = solve_smem(S.m);
         if (noise == NOISE_NONE)
-            plaunch(S.pdl, k_lr_solve<NOISE_NONE, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
+            plaunch(S.pdl, k_bt_solve<T, NOISE_NONE, true>, bgrid, 256, smem, S.stream, (const T *)x, lr, nz);
         else if (noise == NOISE_PHILOX)
-            plaunch(S.pdl, k_lr_solve<NOISE_PHILOX, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
+            plaunch(S.pdl, k_bt_solve<T, NOISE_PHILOX, true>, bgrid, 256, smem, S.stream, (const T *)x, lr, nz);
         else
-            plaunch(S.pdl, k_lr_solve<NOISE_INJECTED, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
+            plaunch(S.pdl, k_bt_solve<T, NOISE_INJECTED, true>, bgrid, 256, smem, S.stream, (const T *)x, lr, nz);
         const unsigned blocks = (unsigned)std::min<i64>(nblk(C.nrows, 4 * 256), 8 * S.nsm);
         if (sizeof(T) == 4)
             plaunch(S.pdl, k_lr_scatter<T, float>, blocks, 256, 0, S.stream, x, C.nrows, C.rows, C.ptr, C.col,
@@ -370,6 +373,8 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
                     (const T *)C.val, (const double *)lv.z);
         S.launches++;
     } else if (C.nrows > 0) {
+        plaunch(S.pdl, k_bt_partial<T>, bgrid, 256, 0, S.stream, (const T *)x, lr);
+        S.launches++;
         // solve and correction in one launch; every CTA repeats the (FP64)
         // m x m solve, so the grid stays at two CTAs per SM at most
         const unsigned blocks = (unsigned)std::min<i64>(nblk(C.nrows, 256), 2 * S.nsm);
@@ -384,6 +389,8 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
             plaunch(S.pdl, k_lr_apply<T, NOISE_INJECTED>, blocks, 256, sm, S.stream, x, lr, lv.bt_split, nz, C.nrows,
                     C.rows, C.ptr, C.col, (const T *)C.val);
     } else {
+        plaunch(S.pdl, k_bt_partial<T>, bgrid, 256, 0, S.stream, (const T *)x, lr);
+        S.launches++;
         const size_t smem = solve_smem(S.m);
         if (noise == NOISE_NONE)
             plaunch(S.pdl, k_lr_solve<NOISE_NONE, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
@@ -392,7 +399,7 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
         else
             plaunch(S.pdl, k_lr_solve<NOISE_INJECTED, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
     }
-    S.launches += 2;
+    S.launches += 1;
 }
 
 // SORSampler::apply (sor_sampler.cc:37-59) / SORSmoother::apply
@@ -461,10 +468,11 @@ static void launch_bt_plain(Sampler &S, Level &lv, const void *x) {
     lr.Bvalf = lv.Bvalf;
     lr.y = lv.y;
     lr.part = lv.part;
+    lr.counter = lv.counter;
     NoiseArgs nz{};
-    plaunch(S.pdl, k_bt_partial<T>, dim3(S.m, lv.bt_split), 256, 0, S.stream, (const T *)x, lr);
-    plaunch(S.pdl, k_lr_solve<NOISE_NONE, false>, 1, solve_block(S.m), 0, S.stream, lr, lv.bt_split, nz);
-    S.launches += 2;
+    plaunch(S.pdl, k_bt_solve<T, NOISE_NONE, false>, dim3(S.m, lv.bt_split), 256, solve_smem(S.m), S.stream,
+            (const T *)x, lr, nz);
+    S.launches += 1;
 }
 
 template <typename T>
@@ -680,6 +688,8 @@ void Sampler::build_lowrank(int lev) {
         lv.bt_split = (int)std::min<i64>(32, std::max<i64>(1, (maxcol + 511) / 512));
     }
     lv.part = alloc<double>((size_t)m * lv.bt_split);
+    lv.counter = alloc<unsigned>(1);
+    CK(cudaMemsetAsync(lv.counter, 0, sizeof(unsigned), stream));
     // FP64 work arrays
     double *xs = alloc<double>(geo.nalloc), *fs = alloc<double>(geo.nalloc);
     i64 *nzi = alloc<i64>(n);

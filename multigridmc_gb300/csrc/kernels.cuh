@@ -11,6 +11,7 @@
 //   k_sweep_wavefront   lexicographic SOR sweep as a hyperplane wavefront
 //                       (one CTA; parity mode)
 //   k_bt_partial        partial sums of y = B^T x
+//   k_bt_solve          the partial sums and, in the last CTA, the solve
 //   k_lr_solve          y and the m x m low-rank solve
 //   k_lr_apply          the solve and x += C z over the rows of C = M^{-1} B
 //   k_lr_scatter        x += C z (large supports, after k_lr_solve)
@@ -386,6 +387,7 @@ struct LowRankArg {
     float *zf;          // the same coefficients rounded to FP32 (FP32 chain)
     const float *Bvalf; // B values rounded to FP32 (FP32 chain)
     double *part;       // m x P scratch: partial sums of B^T x
+    unsigned *counter;  // CTA counter of k_bt_solve (reset by its last CTA)
 };
 
 // Partial sums of y_j = sum_i B_ij x_i: gridDim.y CTAs per column j, CTA p
@@ -394,9 +396,7 @@ struct LowRankArg {
 // per-thread sums are in the state's precision (FP32 products for the FP32
 // chain) and are combined across the CTA in FP64.
 template <typename T>
-__global__ void __launch_bounds__(256) k_bt_partial(const T *__restrict__ x, LowRankArg lr) {
-    pdl_begin();
-    __shared__ double sh[32];
+__device__ __forceinline__ void bt_partial_cta(const T *__restrict__ x, const LowRankArg &lr, double *sh) {
     const int j = blockIdx.x, p = blockIdx.y, P = gridDim.y;
     const i64 e0 = lr.Bptr[j], e1 = lr.Bptr[j + 1];
     const i64 len = (e1 - e0 + P - 1) / P;
@@ -420,6 +420,13 @@ __global__ void __launch_bounds__(256) k_bt_partial(const T *__restrict__ x, Low
     }
     const double acc = block_sum<256>((double)tacc, sh);
     if (threadIdx.x == 0) lr.part[j * P + p] = acc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_bt_partial(const T *__restrict__ x, LowRankArg lr) {
+    pdl_begin();
+    __shared__ double sh[32];
+    bt_partial_cta<T>(x, lr, sh);
 }
 
 // One CTA: y_k = sum_p part[k * P + p] (fixed order, so the result does not
@@ -450,7 +457,7 @@ __device__ __forceinline__ void lr_solve_cta(const LowRankArg &lr, int P, const 
         double t = 0.0;
         for (int q0 = 0; q0 < P; q0 += 8) {
 #pragma unroll
-            for (int r = 0; r < 8; ++r) pv[r] = q0 + r < P ? lr.part[(i64)k * P + q0 + r] : 0.0;
+            for (int r = 0; r < 8; ++r) pv[r] = q0 + r < P ? __ldcg(lr.part + (i64)k * P + q0 + r) : 0.0;
 #pragma unroll
             for (int r = 0; r < 8; ++r)
                 if (q0 + r < P) t += pv[r];
@@ -509,6 +516,26 @@ __global__ void __launch_bounds__(256) k_lr_solve(LowRankArg lr, int P, NoiseArg
     pdl_begin();
     extern __shared__ double dyn[];
     lr_solve_cta<NOISE, SOLVE>(lr, P, nz, dyn, dyn + lr.m, nullptr, true);
+}
+
+// Partial sums and the solve in one launch: the last CTA to finish (block
+// counter, reset by that CTA) forms y -- and with SOLVE z -- from the
+// partial sums in the same fixed order as k_lr_solve, so the result does
+// not depend on block timing.
+template <typename T, int NOISE, bool SOLVE>
+__global__ void __launch_bounds__(256) k_bt_solve(const T *__restrict__ x, LowRankArg lr, NoiseArgs nz) {
+    pdl_begin();
+    __shared__ double sh[32];
+    __shared__ bool last;
+    bt_partial_cta<T>(x, lr, sh);
+    __threadfence();
+    if (threadIdx.x == 0) last = atomicAdd(lr.counter, 1u) == gridDim.x * gridDim.y - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x == 0) *lr.counter = 0u;
+    extern __shared__ double dyn[];
+    lr_solve_cta<NOISE, SOLVE>(lr, gridDim.y, nz, dyn, dyn + lr.m, nullptr, true);
 }
 
 // Low-rank solve and correction in one launch: every CTA forms z itself
