@@ -87,6 +87,7 @@ struct Level {
     float *zf = nullptr, *Bvalf = nullptr;
     int bt_split = 1;  // blocks per column of the B^T x reduction
     unsigned *counter = nullptr;  // CTA counter of k_bt_solve
+    int sweep_tx = 0;             // CTA width of the colour passes chosen by the autotuner (0: sweep_block())
     void *adj[4] = {nullptr, nullptr, nullptr, nullptr};  // adjoint: x-bar, f-bar, two work vectors (T, padded)
     CUtensorMap xmap{}, fmap{};  // 3D tile maps of x and f for the residual-restriction
     bool tma = false;            // maps valid (3D, rows of a multiple of 16 bytes)
@@ -161,6 +162,7 @@ struct Sampler {
     void make_tile_maps(Level &lv);
     double *adj_m = nullptr;  // m-vector for the adjoint's transposed low-rank solve
     void ensure_adjoint();
+    void autotune_sweeps();
     template <typename T>
     void adjoint_sample(int lev);
     void build_coarse();
@@ -244,6 +246,13 @@ static void raise_smem_limit(void (*kernel)(KArgs...), size_t bytes) {
 }
 
 // ----------------------------------------------------------- sweep launch
+// CTA shape of a level's colour passes: the autotuned width, or the
+// smallest power of two covering the `count` work items of a row.
+static dim3 level_block(const Level &lv, int count) {
+    if (lv.sweep_tx > 0) return dim3(lv.sweep_tx, RBP_THREADS / lv.sweep_tx, 1);
+    return sweep_block(count);
+}
+
 template <typename T, bool EXACT, int NOISE>
 static void launch_colour_passes(Sampler &S, const Level &lv, bool forward, T *x, const T *f, const StencilArg<T> &s,
                                  const NoiseArgs &nz);
@@ -266,7 +275,7 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
             if constexpr (std::is_same<T, float>::value) {
                 if (vec) {
                     const int ngrp = (lv.g.N0 + 8) / 8;
-                    const dim3 blk = sweep_block(ngrp);
+                    const dim3 blk = level_block(lv, ngrp);
                     dim3 grid((ngrp + blk.x - 1) / blk.x, (lv.g.N1 + blk.y - 1) / blk.y, lv.g.N2);
                     plaunch(S.pdl && lv.g.pdl, k_sweep_rb_vec<NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
                     S.launches++;
@@ -275,7 +284,7 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
             }
             {
                 const int na = (lv.g.N0 + 1) / 2;
-                const dim3 blk = sweep_block(na);
+                const dim3 blk = level_block(lv, na);
                 dim3 grid((na + blk.x - 1) / blk.x, (lv.g.N1 + blk.y - 1) / blk.y, lv.g.N2);
                 plaunch(S.pdl && lv.g.pdl, k_sweep_rb_pass<T, EXACT, NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
             }
@@ -295,7 +304,7 @@ static void launch_colour_passes(Sampler &S, const Level &lv, bool forward, T *x
         const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
         const int na = (lv.g.N0 - pa + 1) / 2, nb = (lv.g.N1 - pb + 1) / 2, nc = (lv.g.N2 - pc + 1) / 2;
         if (na <= 0 || nb <= 0 || nc <= 0) continue;
-        const dim3 blk = sweep_block(na);
+        const dim3 blk = level_block(lv, na);
         dim3 grid((na + blk.x - 1) / blk.x, (nb + blk.y - 1) / blk.y, nc);
         plaunch(S.pdl && lv.g.pdl, k_sweep_c27_pass<T, EXACT, NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, nz);
         S.launches++;
@@ -997,7 +1006,56 @@ void Sampler::build(const mgmc_operator_desc &op) {
         noise_off = off0;
         counting = false;
     }
+    autotune_sweeps();
     CK(cudaStreamSynchronize(stream));
+    check_launch();
+}
+
+// Autotuner of the colour passes' CTA shape: for every level that sweeps,
+// time a few noise-free sweeps on scratch vectors for each CTA width that
+// fits the level's rows (the block shape does not change any result: every
+// thread owns whole points or spans) and keep the fastest.  MGMC_AUTOTUNE=0
+// keeps the heuristic shapes.
+void Sampler::autotune_sweeps() {
+    if (const char *e = std::getenv("MGMC_AUTOTUNE"))
+        if (e[0] == '0') return;
+    if (P.ordering != MGMC_ORDER_MULTICOLOUR) return;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const int nlev = (int)L.size();
+    for (int lev = 0; lev < nlev; ++lev) {
+        if (lev == nlev - 1 && chol) break;
+        Level &lv = L[lev];
+        ensure_scratch(lev);
+        const bool vec = fp32 && !exact && lv.npt == 7 && (lv.g.sy % 4) == 0 && (lv.g.sz % 4) == 0;
+        const int count = vec ? (lv.g.N0 + 8) / 8 : (lv.g.N0 + 1) / 2;
+        int cap = 8;
+        while (cap < count && cap < RBP_THREADS) cap *= 2;
+        NoiseArgs nz{};
+        nz.d_step = d_step;
+        const int noise = noise_mode == NOISE_PHILOX ? NOISE_PHILOX : NOISE_NONE;
+        float best = 1e30f;
+        int best_tx = 0;
+        for (int tx = 8; tx <= std::min(RBP_THREADS, 2 * cap); tx *= 2) {
+            lv.sweep_tx = tx;
+            for (int r = 0; r < 2; ++r) launch_sweep(*this, lv, true, noise, lv.s1, lv.s2, nz, fp32, exact);
+            CK(cudaEventRecord(e0, stream));
+            for (int r = 0; r < 4; ++r) launch_sweep(*this, lv, r % 2 == 0, noise, lv.s1, lv.s2, nz, fp32, exact);
+            CK(cudaEventRecord(e1, stream));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                best_tx = tx;
+            }
+        }
+        lv.sweep_tx = best_tx;
+        CK(cudaMemsetAsync(lv.s1, 0, (size_t)lv.geo.nalloc * tsize(), stream));
+    }
+    CK(cudaEventDestroy(e0));
+    CK(cudaEventDestroy(e1));
     check_launch();
 }
 

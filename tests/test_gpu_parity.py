@@ -140,3 +140,19 @@ def test_errors_are_status_codes():
     with pytest.raises(M.MGMCError) as e:
         M.MultigridMCSampler(op_bad, _mg(2))
     assert e.value.status == 3
+
+
+def test_autotuned_shapes_do_not_change_the_chain(monkeypatch):
+    """The colour passes' CTA shapes chosen by the autotuner leave every
+    value of the chain unchanged (FP32-mixed, Philox noise, bitwise)."""
+    _, op_p = posterior((32, 32, 32), m=8)
+    f = np.random.default_rng(4).standard_normal(op_p.n)
+    states = []
+    for tune in ("0", "1"):
+        monkeypatch.setenv("MGMC_AUTOTUNE", tune)
+        s = M.MultigridMCSampler(op_p, _mg(4), ordering=M.MULTICOLOUR, precision=M.FP32_MIXED, seed=5)
+        s.fix_rhs(f)
+        s.step(5)
+        states.append(s.get_state())
+        s.close()
+    assert np.array_equal(states[0], states[1])
