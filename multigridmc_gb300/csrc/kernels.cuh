@@ -6,7 +6,9 @@
 // zero, so stencil loads need no boundary tests.
 //
 // Kernels (one V-cycle at level l uses them in this order):
-//   k_sweep_rb_pass     one colour of the red-black SOR sweep of a 7-point level
+//   k_sweep_rb_vec      one colour of the red-black SOR sweep of the 7-point
+//                       level, FP32, 8-point spans with float4 loads/stores
+//   k_sweep_rb_pass     the same, one point per thread (FP64, parity)
 //   k_sweep_c27_pass    one colour of the 8-colour SOR sweep of a 27-point level
 //   k_sweep_wavefront   lexicographic SOR sweep as a hyperplane wavefront
 //                       (one CTA; parity mode)
@@ -14,12 +16,15 @@
 //   k_bt_solve          the partial sums and, in the last CTA, the solve
 //   k_lr_solve          y and the m x m low-rank solve
 //   k_lr_apply          the solve and x += C z over the rows of C = M^{-1} B
-//   k_lr_scatter        x += C z (large supports, after k_lr_solve)
-//   k_resid_restrict_tiled  f_c = R (f - A_0 x)  (fused residual + restriction)
-//   k_sub_Bq            f_c -= B_c Sigma^{-1} y
+//   k_lr_scatter        x += C z (large supports, after k_bt_solve)
+//   k_resid_restrict_tma    f_c = R (f - A_0 x), TMA tiles (fused residual
+//                           + restriction; _tiled / plain variants otherwise)
+//   k_add_Bq            f_c -= B_c Sigma^{-1} y
 //   k_prolong_add       x += alpha P x_c
-//   k_chol_*            coarse-level FP64 Cholesky sample
-//   k_step_end          observable z = b^T x, step counter
+//   k_chol_gemv_*       coarse-level Cholesky sample (k_chol_subst: parity)
+//   k_step_end          observables z = b^T x, step counter
+// Host conversions: k_unpack / k_unpack2 / k_pack; adjoint helpers: k_axpy,
+// k_sinvt_q; building blocks: k_apply_stencil.
 #pragma once
 
 #include <cstdint>
@@ -997,16 +1002,6 @@ __global__ void __launch_bounds__(256) k_pack(const T *__restrict__ src, double 
     const int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y, c = blockIdx.z;
     if (a >= g.N0) return;
     dst[((i64)c * g.N1 + b) * g.N0 + a] = (double)src[g.pad(a, b, c)];
-}
-
-template <typename T>
-__global__ void k_zero_interior(T *__restrict__ x, Grid3 g) {
-    if (g.pdl) pdl_begin();
-    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    i64 n = (i64)g.N0 * g.N1 * g.N2;
-    if (t >= n) return;
-    int a = (int)(t % g.N0), b = (int)((t / g.N0) % g.N1), c = (int)(t / ((i64)g.N0 * g.N1));
-    x[g.pad(a, b, c)] = T(0);
 }
 
 // ------------------------------------------------- coarse Cholesky sample
