@@ -338,6 +338,34 @@ def batch_study(nchain, steps, warmup=5, seed=3):
             "iact_p90": float(np.percentile(taus, 90)) if taus else None, "iact_window": 20, "steps": steps}
 
 
+def convergence_study(nchain, nsteps, seed=5000):
+    """measure_convergence (convergence.cc:4-161) as batched GPU chains: a
+    32^3 posterior (kappa^2 = 10, 8 measurements r = 0.1 Sigma = 1e-4),
+    FP32-mixed, nchain chains from x = 0; per step |E[z^k] - E[z]| and
+    |Var[z^k] - Var[z]| with their statistical errors, against the exact
+    moments of z = b^T x (CG on the assembled operator, FP64)."""
+    import multigridmc_gb300 as M
+    from multigridmc_gb300.measurements import exact_observable_moments, measure_convergence
+    shape = (32, 32, 32)
+    rng = np.random.default_rng(seed)
+    m = 8
+    op = M.LinearOperator.shifted_laplace_fd(shape, KAPPA_SQ).with_measurements(
+        rng.uniform(0.1, 0.9, size=(m, 3)), np.ones(m), VARIANCE, 0.1)
+    y = rng.standard_normal(m)
+    f = op.B_dense() @ (y / op.Sigma)
+    bidx, bval = M.measurement_vector(shape, [0.5, 0.5, 0.5], RADIUS)
+    mu, var = exact_observable_moments(op, f, bidx, bval)
+    t0 = time.perf_counter()
+    res = measure_convergence(op, M.MultigridParameters(nlevel=4), f, bidx, bval, nchain, nsteps, seed=seed,
+                              precision=M.FP32_MIXED)
+    dt = time.perf_counter() - t0
+    dm = np.abs(res["mean"] - mu)
+    dv = np.abs(res["variance"] - var)
+    return {"nchain": nchain, "nsteps": nsteps, "exact_mean": mu, "exact_variance": var,
+            "mean_diff": dm.tolist(), "mean_err": res["err_mean"].tolist(),
+            "variance_diff": dv.tolist(), "variance_err": res["err_variance"].tolist(), "wall_s": dt}
+
+
 def profile_steps(nsteps, warmup, precision):
     """The benchmark chain for a profiler: warm-up steps, then `nsteps` steps
     inside the NVTX range "timed"."""
@@ -372,6 +400,8 @@ def main():
                     help="run the coupled FP32/FP64 covariance comparison instead of the benchmark")
     ap.add_argument("--batch-chains", type=int, default=0, metavar="N",
                     help="run the batched-chains study (N chains of mixed sizes) instead of the benchmark")
+    ap.add_argument("--convergence-study", type=int, default=0, metavar="NCHAIN",
+                    help="run measure_convergence over NCHAIN batched chains (--steps steps) instead of the benchmark")
     ap.add_argument("--profile-steps", type=int, default=0, metavar="K",
                     help="profiling mode: K steps of the benchmark chain inside an NVTX range 'timed' "
                          "(after --warmup steps), for ncu --nvtx-include timed/; prints no JSON")
@@ -382,6 +412,9 @@ def main():
         return
     if args.batch_chains > 0:
         print(json.dumps({"batch_study": batch_study(args.batch_chains, args.steps)}), flush=True)
+        return
+    if args.convergence_study > 0:
+        print(json.dumps({"convergence_study": convergence_study(args.convergence_study, args.steps)}), flush=True)
         return
     if args.covariance_study > 0:
         print(json.dumps({"covariance_study": covariance_study(args.covariance_study)}), flush=True)

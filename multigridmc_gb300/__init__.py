@@ -259,6 +259,32 @@ class LinearOperator:
             sigma.append(variance_global)
         return self.with_lowrank(cols, sigma)
 
+    def to_scipy(self):
+        """A = A_0 + B Sigma^{-1} B^T as a scipy.sparse CSR matrix in the
+        vertex order (the matrix LinearOperator::get_sparse of the reference
+        assembles; host-side, for exact comparators at moderate sizes)."""
+        import scipy.sparse as sp
+        N = [c - 1 for c in self.shape] + [1] * (3 - self.dim)
+        n = self.n
+        idx = np.arange(n).reshape(N[2], N[1], N[0])
+        rows, cols, vals = [], [], []
+        for dz in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dx in (-1, 0, 1):
+                    w = float(self.stencil[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)])
+                    if w == 0.0:
+                        continue
+                    src = idx[max(0, -dz):N[2] - max(0, dz), max(0, -dy):N[1] - max(0, dy), max(0, -dx):N[0] - max(0, dx)]
+                    dst = idx[max(0, dz):N[2] + min(0, dz), max(0, dy):N[1] + min(0, dy), max(0, dx):N[0] + min(0, dx)]
+                    rows.append(src.ravel())
+                    cols.append(dst.ravel())
+                    vals.append(np.full(src.size, w))
+        A = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
+        if self.m > 0:
+            Bs = sp.csc_matrix((self.B_val, self.B_idx, self.B_ptr), shape=(n, self.m))
+            A = (A + Bs @ sp.diags(1.0 / self.Sigma) @ Bs.T).tocsr()
+        return A
+
     def B_dense(self):
         B = np.zeros((self.n, self.m))
         for j in range(self.m):

@@ -153,3 +153,21 @@ def test_fixed_point_256cubed(precision, tol):
     for direction in (M.FORWARD, M.BACKWARD):
         y = s.sor(0, direction, b, x.copy(), with_noise=False)
         assert np.linalg.norm(y - x) / np.linalg.norm(x) < tol
+
+
+def test_convergence_of_observable_moments():
+    """measure_convergence (convergence.cc:4-161) over 400 batched FP64
+    chains from x = 0: after a few MGMC steps the mean and variance of the
+    observable z = b^T x agree with the exact ones within 5 standard errors."""
+    from multigridmc_gb300.measurements import exact_observable_moments, measure_convergence
+    from problems import posterior, rhs
+    shape = (16, 16, 16)
+    _, op = posterior(shape, m=4, radius=0.1)
+    f = rhs(op)
+    bidx, bval = M.measurement_vector(shape, [0.5, 0.5, 0.5], 0.1)
+    mu, var = exact_observable_moments(op, f, bidx, bval)
+    res = measure_convergence(op, M.MultigridParameters(nlevel=3), f, bidx, bval, nchain=400, nsteps=10,
+                              seed=900, precision=M.FP64)
+    for k in range(4, 11):
+        assert abs(res["mean"][k] - mu) <= 5 * res["err_mean"][k], (k, res["mean"][k], mu)
+        assert abs(res["variance"][k] - var) <= 5 * res["err_variance"][k], (k, res["variance"][k], var)

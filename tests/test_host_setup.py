@@ -69,3 +69,26 @@ def test_operator_description():
     oo.add_measurements(loc, [1.0, 2.0], variance_scaling=1e-4, radius=0.1)
     Bd, sig = oo.B_dense()
     assert np.array_equal(Bd, op.B_dense()) and np.array_equal(sig, op.Sigma)
+
+
+def test_sparse_operator_and_exact_observable_moments():
+    """LinearOperator.to_scipy assembles A_0 + B Sigma^{-1} B^T (A_0 equal to
+    the oracle's CSR operator), and the exact moments of z = b^T x used by the
+    convergence measurement agree with a dense solve."""
+    from multigridmc_gb300.measurements import exact_observable_moments
+    from problems import posterior, rhs
+    for shape, m in [((16, 16, 16), 4), ((12, 10), 2), ((9,), 0)]:
+        op_o, op_p = posterior(shape, m=m, radius=0.1)
+        A = op_p.to_scipy().toarray()
+        B = op_p.B_dense()
+        A0 = A - (B / op_p.Sigma) @ B.T if m else A
+        assert np.abs(A0 - op_o.dense()).max() <= 1e-12 * np.abs(A0).max()
+    _, op = posterior((12, 12), m=3, radius=0.1)
+    f = rhs(op)
+    bidx, bval = M.measurement_vector((12, 12), [0.5, 0.5], 0.1)
+    mu, var = exact_observable_moments(op, f, bidx, bval)
+    A = op.to_scipy().toarray()
+    b = np.zeros(op.n)
+    b[bidx] = bval
+    assert abs(mu - b @ np.linalg.solve(A, f)) <= 1e-9 * abs(mu)
+    assert abs(var - b @ np.linalg.solve(A, b)) <= 1e-9 * var
