@@ -900,8 +900,11 @@ __global__ void __launch_bounds__(128) k_prolong_add(T *__restrict__ x, const T 
     // coarse cell (i, j, k), 0 <= i <= Nc0 etc., owns the fine vertices with
     // 1-based coordinates 2 i + {0, 1} (those inside the interior); its
     // corners are the coarse vertices i, i+1 (1-based, ghosts are zero)
+    // planes from the top: the residual-restriction before ends there, and
+    // the sweep after starts at the bottom, which this kernel writes last
+    // (both find their first planes in L2)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = dim > 1 ? (int)blockIdx.y : 0, k = dim > 2 ? (int)blockIdx.z : 0;
+    const int j = dim > 1 ? (int)blockIdx.y : 0, k = dim > 2 ? (int)(gridDim.z - 1 - blockIdx.z) : 0;
     if (i > gc.N0) return;
     const int ny = dim > 1 ? 2 : 1, nz = dim > 2 ? 2 : 1;
     T cv[2][2][2];
