@@ -1,0 +1,73 @@
+"""Driver configurations in libconfig syntax (src/auxilliary/parameters.cc)
+become the operator, right hand side and multigrid parameters of the GPU
+sampler."""
+import numpy as np
+import pytest
+
+import multigridmc_gb300 as M
+from multigridmc_gb300.config import load_run, parse_libconfig
+
+PARAMS = """
+// a driver configuration
+general = {
+    dim = 2;
+    do_cholesky = false;  do_ssor = true;  do_multigridmc = true;
+    measure_time_per_sample = true;
+    operator = "posterior";
+}
+lattice = { nx = 32; ny = 16; nz = 8; }
+smoother = { nsmooth = 1; omega = 1.0; }
+multigrid = {
+    smoother = "SSOR"; coarse_solver = "Cholesky";
+    npresmooth = 1; npostsmooth = 2; ncoarsesmooth = 1;
+    omega = 1.2; nlevel = 3; cycle = 2; coarse_scaling = 1.0; verbose = 2;
+}
+sampling = { timeseries = { nsamples = 100; nwarmup = 10; }
+             convergence = { nthreads = 2; nsteps = 4; nsamples = 8; } }
+prior = { pdemodel = "shiftedlaplace_fd"; correlationlengthmodel = "constant"; }
+constantcorrelationlengthmodel = { Lambda = 0.25; }
+/* measurements */
+measurements = {
+    radius = 0.1;
+    sample_location = [0.5, 0.5];
+    variance_scaling = 1.E-2;
+    measure_global = true;
+    mean_global = 1.5;
+    variance_global = 0.01;
+    filename = "meas.cfg";
+}
+"""
+
+MEAS = """
+dim = 2;
+n = 3;
+measurement_locations = [0.25, 0.3, 0.6, 0.7, 0.8, 0.2];
+mean = [1.0, -2.0, 0.5];
+variance = [1e-4, 2e-4, 1.5e-4];
+"""
+
+
+def test_parse_libconfig_syntax():
+    r = parse_libconfig('a = 1; b = -2.5e-3; c = "x\\ty"; d = true; g = { h = [1, 2.0]; i = (3, "s"); }; # c\n')
+    assert r == {"a": 1, "b": -2.5e-3, "c": "x\ty", "d": True, "g": {"h": [1, 2.0], "i": [3, "s"]}}
+
+
+def test_run_config_builds_the_posterior(tmp_path):
+    (tmp_path / "params.cfg").write_text(PARAMS)
+    (tmp_path / "meas.cfg").write_text(MEAS)
+    cfg = load_run(str(tmp_path / "params.cfg"))
+    assert cfg.shape == (32, 16) and cfg.operator == "posterior"
+    assert cfg.kappa_sq == pytest.approx(16.0)
+    prm = cfg.multigrid_parameters()
+    assert (prm.nlevel, prm.npostsmooth, prm.cycle, prm.omega) == (3, 2, 2, 1.2)
+    op = cfg.linear_operator()
+    assert op.m == 4  # three balls and the global average
+    np.testing.assert_allclose(op.Sigma, [1e-6, 2e-6, 1.5e-6, 0.01])
+    ref = M.LinearOperator.shifted_laplace_fd((32, 16), 16.0).with_measurements(
+        [[0.25, 0.3], [0.6, 0.7], [0.8, 0.2]], [1e-4, 2e-4, 1.5e-4], variance_scaling=1e-2, radius=0.1,
+        measure_global=True, variance_global=0.01)
+    assert np.array_equal(op.B_idx, ref.B_idx) and np.allclose(op.B_val, ref.B_val)
+    f = cfg.rhs(op)
+    y = np.array([1.0, -2.0, 0.5, 1.5])
+    np.testing.assert_allclose(f, op.B_dense() @ (y / op.Sigma), rtol=1e-12)
+    assert cfg.sample_location() == [0.5, 0.5]
