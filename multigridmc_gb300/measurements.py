@@ -4,9 +4,12 @@ GPU chains.
 ``measure_convergence`` follows src/measurements/convergence.cc:4-161: many
 chains of one sampler start from x = 0 with the same right hand side, the
 observable z = b^T x is recorded at every step, and the sample moments of
-z^k across chains are compared with the exact mean and variance of z; the
-reference runs the chains on OpenMP threads, here they advance together in
-one CUDA graph (``MultigridMCBatch``).
+z^k across chains are compared with the exact mean and variance of z.
+``measure_mean_squared_error`` follows mean_squared_error.cc:4-65: the
+squared error of each chain's running average of z against the exact mean,
+averaged over chains.  The reference runs the chains one after another or on
+OpenMP threads; here they advance together in one CUDA graph
+(``MultigridMCBatch``).
 """
 import numpy as np
 
@@ -31,11 +34,10 @@ def exact_observable_moments(op, f, bidx, bval):
     return float(b @ mu), float(b @ w)
 
 
-def measure_convergence(op, params, f, bidx, bval, nchain, nsteps, seed=0, **sampler_kw):
-    """Moments of z^k = b^T x^k over `nchain` chains started at x^0 = 0, for
-    k = 0 .. nsteps (convergence.cc:44-64).  Returns a dict of per-step
-    arrays: mean, variance (biased, as the reference's x2_avg - x_avg^2),
-    and the statistical errors of both (convergence.cc:96-99)."""
+def batched_observations(op, params, f, bidx, bval, nchain, nsteps, seed=0, **sampler_kw):
+    """z^k = b^T x^k for k = 0 .. nsteps of `nchain` chains (seeds seed ..
+    seed + nchain - 1) started at x^0 = 0 and advanced together; returns an
+    (nchain, nsteps + 1) array."""
     chains = []
     for i in range(nchain):
         s = MultigridMCSampler(op, params, seed=seed + i, **sampler_kw)
@@ -51,6 +53,15 @@ def measure_convergence(op, params, f, bidx, bval, nchain, nsteps, seed=0, **sam
     batch.close()
     for s in chains:
         s.close()
+    return Z
+
+
+def measure_convergence(op, params, f, bidx, bval, nchain, nsteps, seed=0, **sampler_kw):
+    """Moments of z^k = b^T x^k over `nchain` chains started at x^0 = 0, for
+    k = 0 .. nsteps (convergence.cc:44-64).  Returns a dict of per-step
+    arrays: mean, variance (biased, as the reference's x2_avg - x_avg^2),
+    and the statistical errors of both (convergence.cc:96-99)."""
+    Z = batched_observations(op, params, f, bidx, bval, nchain, nsteps, seed, **sampler_kw)
     m1 = Z.mean(0)
     m2 = (Z ** 2).mean(0)
     m3 = (Z ** 3).mean(0)
@@ -62,3 +73,16 @@ def measure_convergence(op, params, f, bidx, bval, nchain, nsteps, seed=0, **sam
     err_var = np.sqrt(np.maximum(mu4 - (nchain - 3.0) / (nchain - 1.0) * sigma_sq ** 2, 0.0) / nchain)
     return {"mean": m1, "variance": var, "err_mean": err_mean, "err_variance": err_var, "nchain": nchain,
             "nsteps": nsteps}
+
+
+def measure_mean_squared_error(op, params, f, bidx, bval, mean_exact, nchain, nsteps, seed=0, **sampler_kw):
+    """Mean squared error of the running average of z over steps 0 .. j
+    (including the start x^0 = 0) against the exact mean, averaged over
+    `nchain` chains, for j = 0 .. nsteps - 1, with the reference's error
+    estimate (mean_squared_error.cc:44-64)."""
+    Z = batched_observations(op, params, f, bidx, bval, nchain, max(nsteps - 1, 0), seed, **sampler_kw)
+    running = np.cumsum(Z, axis=1) / np.arange(1, Z.shape[1] + 1)
+    se = (running - mean_exact) ** 2
+    mse = se.mean(0)
+    mse_error = ((se ** 2).mean(0) - mse ** 2) / (nchain - 1.0)
+    return {"mse": mse, "mse_error": mse_error, "nchain": nchain, "nsteps": nsteps}

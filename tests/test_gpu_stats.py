@@ -171,3 +171,24 @@ def test_convergence_of_observable_moments():
     for k in range(4, 11):
         assert abs(res["mean"][k] - mu) <= 5 * res["err_mean"][k], (k, res["mean"][k], mu)
         assert abs(res["variance"][k] - var) <= 5 * res["err_variance"][k], (k, res["variance"][k], var)
+
+
+def test_mean_squared_error_of_running_average():
+    """measure_mean_squared_error (mean_squared_error.cc:4-65) over 400
+    batched FP64 chains: the squared error of the running average falls like
+    the bias (mean / (j + 1))^2 plus tau Var / (j + 1) predicts."""
+    from multigridmc_gb300.measurements import exact_observable_moments, measure_mean_squared_error
+    from problems import posterior, rhs
+    shape = (16, 16, 16)
+    _, op = posterior(shape, m=4, radius=0.1)
+    f = rhs(op)
+    bidx, bval = M.measurement_vector(shape, [0.5, 0.5, 0.5], 0.1)
+    mu, var = exact_observable_moments(op, f, bidx, bval)
+    res = measure_mean_squared_error(op, M.MultigridParameters(nlevel=3), f, bidx, bval, mu, nchain=400, nsteps=12,
+                                     seed=1900, precision=M.FP64)
+    mse = res["mse"]
+    assert mse[0] == pytest.approx(mu * mu)  # the running average starts at z^0 = 0
+    for j in (6, 11):
+        model = (mu / (j + 1)) ** 2 + 2.0 * var / (j + 1)
+        assert mse[j] < model, (j, mse[j], model)
+        assert mse[j] > 0.25 * var / (j + 1), (j, mse[j])
