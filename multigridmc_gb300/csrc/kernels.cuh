@@ -400,12 +400,21 @@ __global__ void __launch_bounds__(CP_THREADS) k_sweep_c27_pair(const T *__restri
     extern __shared__ __align__(16) unsigned char cp_smem[];
     T *S = reinterpret_cast<T *>(cp_smem);  // [CP_SC][CP_SB][CP_SA], tile origin at (a0 - 2, b0 - 2, c0 - 2)
     const int a0 = blockIdx.x * CP_TA, b0 = blockIdx.y * CP_TB, c0 = blockIdx.z * CP_TC;
-    for (int i = threadIdx.x; i < CP_SA * CP_SB * CP_SC; i += CP_THREADS) {
+    // all of a thread's tile loads are issued before any is stored
+    constexpr int NT = CP_SA * CP_SB * CP_SC, NR = (NT + CP_THREADS - 1) / CP_THREADS;
+    T v[NR];
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+        const int i = threadIdx.x + r * CP_THREADS;
         const int la = i % CP_SA, t = i / CP_SA, lb = t % CP_SB, lc = t / CP_SB;
         const int a = a0 - 2 + la, b = b0 - 2 + lb, c = c0 - 2 + lc;
-        T v = T(0);  // outside the interior: the zero ghost
-        if (a >= 0 && a < g.N0 && b >= 0 && b < g.N1 && c >= 0 && c < g.N2) v = xin[g.pad(a, b, c)];
-        S[i] = v;
+        v[r] = T(0);  // outside the interior: the zero ghost
+        if (i < NT && a >= 0 && a < g.N0 && b >= 0 && b < g.N1 && c >= 0 && c < g.N2) v[r] = xin[g.pad(a, b, c)];
+    }
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+        const int i = threadIdx.x + r * CP_THREADS;
+        if (i < NT) S[i] = v[r];
     }
     __syncthreads();
     cp_colour<T, EXACT, NOISE>(S, f, g, s, col0, 1, a0, b0, c0, nz);
