@@ -76,7 +76,6 @@ struct Level {
     int ncol = 2, npt = 7;
     double diag = 0, sd = 0;
     void *x = nullptr, *f = nullptr;    // state and right hand side (T, padded)
-    void *x2 = nullptr;                 // second state buffer of the paired colour passes (27-point 3D levels)
     void *s1 = nullptr, *s2 = nullptr;  // scratch for the building-block calls
     SparseCols Bh;                      // B on this level (compact indices)
     i64 *Bptr = nullptr, *Bidx = nullptr;
@@ -296,25 +295,10 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
     }
 }
 
-// 2^dim colours, one launch per colour; on the chain's own state of a 3D
-// level, two colours per launch (k_sweep_c27_pair) alternating between the
-// state and its second buffer -- after the four launches the sweep's result
-// is back in lv.x
+// 2^dim colours, one launch per colour
 template <typename T, bool EXACT, int NOISE>
 static void launch_colour_passes(Sampler &S, const Level &lv, bool forward, T *x, const T *f, const StencilArg<T> &s,
                                  const NoiseArgs &nz) {
-    if (lv.x2 && x == lv.x && lv.ncol == 8) {
-        dim3 grid((lv.g.N0 + CP_TA - 1) / CP_TA, (lv.g.N1 + CP_TB - 1) / CP_TB, (lv.g.N2 + CP_TC - 1) / CP_TC);
-        for (int p = 0; p < 4; ++p) {
-            const int col0 = forward ? 2 * p : 7 - 2 * p, col1 = forward ? 2 * p + 1 : 6 - 2 * p;
-            const T *src = (const T *)((p & 1) ? lv.x2 : lv.x);
-            T *dst = (T *)((p & 1) ? lv.x : lv.x2);
-            plaunch(S.pdl && lv.g.pdl, k_sweep_c27_pair<T, EXACT, NOISE>, grid, CP_THREADS, cp_smem_bytes<T>(), S.stream,
-                    src, dst, f, lv.g, s, col0, col1, nz);
-            S.launches++;
-        }
-        return;
-    }
     for (int cc = 0; cc < lv.ncol; ++cc) {
         const int colour = forward ? cc : lv.ncol - 1 - cc;
         const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
@@ -954,13 +938,9 @@ void Sampler::build(const mgmc_operator_desc &op) {
         lv.g.pdl = geo.n <= PDL_MAX_POINTS ? 1 : 0;
         L.push_back(lv);
     }
-    bool pairs = dim == 3 && P.ordering == MGMC_ORDER_MULTICOLOUR;
-    if (const char *e = std::getenv("MGMC_NO_PAIR"))
-        if (e[0] == '1') pairs = false;
     for (auto &lv : L) {
         lv.x = talloc(lv.geo.nalloc);
         lv.f = talloc(lv.geo.nalloc);
-        if (pairs && lv.npt == 27 && lv.ncol == 8) lv.x2 = talloc(lv.geo.nalloc);
     }
     for (size_t lev = 0; lev + 1 < L.size(); ++lev) make_tile_maps(L[lev]);
     d_cvec = alloc<double>(L[0].geo.n);

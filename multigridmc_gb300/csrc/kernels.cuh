@@ -336,98 +336,6 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ 
     sor_point<T, 27, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
 }
 
-// Two consecutive colours of an 8-colour sweep in one launch, reading the
-// state from `xin` and writing the whole state to `xout` (ping-pong: no CTA
-// ever reads a value another CTA of the same launch writes).  A CTA stages
-// its CP_TA x CP_TB x CP_TC tile of xin with a two-point halo in shared
-// memory, updates the first colour on the tile plus a one-point halo (the
-// halo points are recomputed identically by the neighbouring CTAs: same
-// inputs, same Philox counters, same arithmetic), then the second colour on
-// the tile, and writes the tile out.  Per point the arithmetic and its order
-// are those of sor_point<T, 27, EXACT>, so the chain equals the one of the
-// per-colour launches value for value, with half the launches.
-constexpr int CP_TA = 16, CP_TB = 16, CP_TC = 8;
-constexpr int CP_SA = CP_TA + 4, CP_SB = CP_TB + 4, CP_SC = CP_TC + 4;
-constexpr int CP_THREADS = 256;
-
-template <typename T>
-__host__ __device__ __forceinline__ size_t cp_smem_bytes() {
-    return sizeof(T) * CP_SA * CP_SB * CP_SC;
-}
-
-template <typename T, bool EXACT, int NOISE>
-__device__ __forceinline__ void cp_colour(T *S, const T *__restrict__ f, const Grid3 &g, const StencilArg<T> &s,
-                                          int colour, int h, int a0, int b0, int c0, const NoiseArgs &nz) {
-    typedef Ar<EXACT> Ops;
-    const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
-    const int alo = a0 - h, blo = b0 - h, clo = c0 - h;
-    const int qa = (pa - alo) & 1, qb = (pb - blo) & 1, qc = (pc - clo) & 1;
-    const int na = (CP_TA + 2 * h - qa + 1) >> 1, nb = (CP_TB + 2 * h - qb + 1) >> 1, nc = (CP_TC + 2 * h - qc + 1) >> 1;
-    const int cnt = na * nb * nc;
-    for (int t = threadIdx.x; t < cnt; t += CP_THREADS) {
-        const int ia = t % na, tt = t / na, ib = tt % nb, ic = tt / nb;
-        const int a = alo + qa + 2 * ia, b = blo + qb + 2 * ib, c = clo + qc + 2 * ic;
-        if (a < 0 || a >= g.N0 || b < 0 || b >= g.N1 || c < 0 || c >= g.N2) continue;
-        T xi = T(0);
-        if (NOISE == NOISE_PHILOX) xi = (T)pick(point_normals(nz, g, a, b, c), (a & 7) >> 1);
-        if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
-        const int la = a - a0 + 2, lb = b - b0 + 2, lc = c - c0 + 2;
-        T res = T(0);
-#pragma unroll
-        for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-            for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-                for (int dx = -1; dx <= 1; ++dx)
-                    res = Ops::add(res, Ops::mul(s.w[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)],
-                                                 S[((lc + dz) * CP_SB + (lb + dy)) * CP_SA + (la + dx)]));
-        T cval = f[g.pad(a, b, c)];
-        if (NOISE != NOISE_NONE) cval = Ops::add(Ops::mul(s.sd, xi), cval);
-        T *pt = S + (lc * CP_SB + lb) * CP_SA + la;
-        const T xo = *pt;
-        if (EXACT)
-            *pt = Ops::add(xo, Ops::mul(s.omega, Ops::sub(cval, res)) / s.diag);
-        else
-            *pt = xo + s.omega_diag * (cval - res);
-    }
-}
-
-template <typename T, bool EXACT, int NOISE>
-__global__ void __launch_bounds__(CP_THREADS) k_sweep_c27_pair(const T *__restrict__ xin, T *__restrict__ xout,
-                                                               const T *__restrict__ f, Grid3 g, StencilArg<T> s,
-                                                               int col0, int col1, NoiseArgs nz) {
-    if (g.pdl) pdl_begin();
-    extern __shared__ __align__(16) unsigned char cp_smem[];
-    T *S = reinterpret_cast<T *>(cp_smem);  // [CP_SC][CP_SB][CP_SA], tile origin at (a0 - 2, b0 - 2, c0 - 2)
-    const int a0 = blockIdx.x * CP_TA, b0 = blockIdx.y * CP_TB, c0 = blockIdx.z * CP_TC;
-    // all of a thread's tile loads are issued before any is stored
-    constexpr int NT = CP_SA * CP_SB * CP_SC, NR = (NT + CP_THREADS - 1) / CP_THREADS;
-    T v[NR];
-#pragma unroll
-    for (int r = 0; r < NR; ++r) {
-        const int i = threadIdx.x + r * CP_THREADS;
-        const int la = i % CP_SA, t = i / CP_SA, lb = t % CP_SB, lc = t / CP_SB;
-        const int a = a0 - 2 + la, b = b0 - 2 + lb, c = c0 - 2 + lc;
-        v[r] = T(0);  // outside the interior: the zero ghost
-        if (i < NT && a >= 0 && a < g.N0 && b >= 0 && b < g.N1 && c >= 0 && c < g.N2) v[r] = xin[g.pad(a, b, c)];
-    }
-#pragma unroll
-    for (int r = 0; r < NR; ++r) {
-        const int i = threadIdx.x + r * CP_THREADS;
-        if (i < NT) S[i] = v[r];
-    }
-    __syncthreads();
-    cp_colour<T, EXACT, NOISE>(S, f, g, s, col0, 1, a0, b0, c0, nz);
-    __syncthreads();
-    cp_colour<T, EXACT, NOISE>(S, f, g, s, col1, 0, a0, b0, c0, nz);
-    __syncthreads();
-    for (int i = threadIdx.x; i < CP_TA * CP_TB * CP_TC; i += CP_THREADS) {
-        const int la = i % CP_TA, t = i / CP_TA, lb = t % CP_TB, lc = t / CP_TB;
-        const int a = a0 + la, b = b0 + lb, c = c0 + lc;
-        if (a < g.N0 && b < g.N1 && c < g.N2) xout[g.pad(a, b, c)] = S[((lc + 2) * CP_SB + (lb + 2)) * CP_SA + (la + 2)];
-    }
-}
-
 // ------------------------------------------------ lexicographic wavefront
 // Lexicographic order as hyperplanes t = a + hb b + hc c: every neighbour
 // that precedes a point lexicographically lies on an earlier hyperplane

@@ -156,20 +156,3 @@ def test_autotuned_shapes_do_not_change_the_chain(monkeypatch):
         states.append(s.get_state())
         s.close()
     assert np.array_equal(states[0], states[1])
-
-
-@pytest.mark.parametrize("precision", [M.FP32_MIXED, M.FP64], ids=["fp32", "fp64"])
-def test_paired_colour_passes_equal_single_passes(monkeypatch, precision):
-    """Two colours per launch on the 27-point levels (tile + one-point halo,
-    ping-pong buffers) give the chain of one launch per colour, bit for bit."""
-    _, op_p = posterior((64, 64, 64), m=8)
-    f = np.random.default_rng(6).standard_normal(op_p.n)
-    states = []
-    for off in ("1", "0"):
-        monkeypatch.setenv("MGMC_NO_PAIR", off)
-        s = M.MultigridMCSampler(op_p, _mg(5), ordering=M.MULTICOLOUR, precision=precision, seed=21)
-        s.fix_rhs(f)
-        s.step(4)
-        states.append(s.get_state())
-        s.close()
-    assert np.array_equal(states[0], states[1])
