@@ -180,6 +180,26 @@ mgmc_status mgmc_sampler_launches_per_step(mgmc_sampler *s, int64_t *count);
  * through f = B Sigma^{-1} y. */
 mgmc_status mgmc_sampler_adjoint_step(mgmc_sampler *s, double *xbar, double *fbar, int on_device);
 
+/* ------------------------------------------------ deterministic solver */
+/* MultigridPreconditioner::apply (src/preconditioner/multigrid_preconditioner.cc:102-108):
+ * x = P b, one cycle of the sampler's hierarchy with the noise switched off,
+ * from x = 0 on every level (:76), with the SOR/SSOR smoothers of
+ * multigrid_preconditioner.cc:17-35 and a Cholesky coarse solve whatever
+ * the sampler's coarse_solver (:41-46).  Computed in the sampler's
+ * precision.  The chain's state and right hand side are left unchanged. */
+mgmc_status mgmc_sampler_precondition(mgmc_sampler *s, const double *b, double *x, int on_device);
+/* LoopSolver::apply (src/solver/loop_solver.cc:9-53) with that
+ * preconditioner: x = 0; for k < maxiter: r = A x - b, stop when
+ * |r| / |b| < rtol and |r| < atol, else x -= P r.  The iterate and the
+ * residual are FP64 whatever the sampler's precision (an FP32-mixed
+ * sampler gives mixed-precision iterative refinement).  On return *niter is
+ * the iteration at which the test passed (maxiter when it never did),
+ * *rnorm the last residual norm (-1 when maxiter = 0) and *converged 0 or
+ * 1; not converging is not an error (the reference only reports it).  The
+ * chain's state and right hand side are left unchanged. */
+mgmc_status mgmc_sampler_solve(mgmc_sampler *s, const double *b, double *x, double rtol, double atol, int maxiter,
+                               int on_device, int *niter, double *rnorm, int *converged);
+
 /* -------------------------------------------- level building blocks */
 mgmc_status mgmc_level_stencil(mgmc_sampler *s, int level, double stencil[27]);
 /* y = A x on level `level` (including B Sigma^{-1} B^T x). */

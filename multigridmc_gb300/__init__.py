@@ -13,6 +13,9 @@ this module              reference (eikehmueller/MultigridMC)
 ``MultigridMCSampler``   MultigridMCSampler (sampler/multigridmc_sampler.cc:8-145)
 ``SSORSampler``          SSORSampler (sampler/ssor_sampler.{hh,cc})
 ``CholeskySampler``      DenseCholeskySampler (sampler/cholesky_sampler.cc:25-37)
+``MultigridPreconditioner``  MultigridPreconditioner (preconditioner/multigrid_preconditioner.cc:8-108)
+``LoopSolver``           LoopSolver (solver/loop_solver.cc:9-53) with IterativeSolverParameters
+                         (auxilliary/parameters.hh:130-147)
 =======================  ==========================================================
 
 Every call goes through the C ABI of ``libmgmc_gb300.so``
@@ -33,6 +36,7 @@ from . import build as _build
 __all__ = [
     "MGMCError", "load", "fd_stencil", "galerkin_stencil", "measurement_vector", "LinearOperator",
     "MultigridParameters", "MultigridMCSampler", "MultigridMCBatch", "SSORSampler", "CholeskySampler",
+    "IterativeSolverParameters", "MultigridPreconditioner", "LoopSolver",
     "FP64", "FP32_MIXED", "LEXICOGRAPHIC", "MULTICOLOUR", "PHILOX", "INJECTED", "FORWARD", "BACKWARD",
 ]
 
@@ -102,6 +106,9 @@ SIGNATURES = {
     "mgmc_sampler_level_size": (C.c_int, [_P, C.c_int, _I64]),
     "mgmc_sampler_launches_per_step": (C.c_int, [_P, _I64]),
     "mgmc_sampler_adjoint_step": (C.c_int, [_P, _D, _D, C.c_int]),
+    "mgmc_sampler_precondition": (C.c_int, [_P, _D, _D, C.c_int]),
+    "mgmc_sampler_solve": (C.c_int, [_P, _D, _D, C.c_double, C.c_double, C.c_int, C.c_int,
+                                     C.POINTER(C.c_int), _D, C.POINTER(C.c_int)]),
     "mgmc_level_stencil": (C.c_int, [_P, C.c_int, _D]),
     "mgmc_level_apply": (C.c_int, [_P, C.c_int, _D, _D]),
     "mgmc_level_restrict": (C.c_int, [_P, C.c_int, _D, _D]),
@@ -392,6 +399,25 @@ class MultigridMCSampler:
         _check(self._L.mgmc_sampler_adjoint_step(self._h, _dp(xbar), _dp(fbar), 0))
         return xbar
 
+    def precondition(self, b):
+        """x = P b: one noise-free cycle of this hierarchy from zero
+        (MultigridPreconditioner::apply); the chain is left unchanged."""
+        b = _f64(b)
+        x = np.zeros(self.n)
+        _check(self._L.mgmc_sampler_precondition(self._h, _dp(b), _dp(x), 0))
+        return x
+
+    def solve(self, b, rtol=1e-10, atol=1e-10, maxiter=100):
+        """LoopSolver::apply with this hierarchy as the multigrid
+        preconditioner: returns (x, niter, residual norm, converged); the
+        chain is left unchanged."""
+        b = _f64(b)
+        x = np.zeros(self.n)
+        it, rn, cv = C.c_int(0), C.c_double(0.0), C.c_int(0)
+        _check(self._L.mgmc_sampler_solve(self._h, _dp(b), _dp(x), float(rtol), float(atol), int(maxiter), 0,
+                                          C.byref(it), C.byref(rn), C.byref(cv)))
+        return x, it.value, rn.value, bool(cv.value)
+
     def step(self, nsteps=1):
         _check(self._L.mgmc_sampler_step(self._h, int(nsteps)))
 
@@ -544,3 +570,62 @@ def CholeskySampler(linear_operator, **kw):
     (DenseCholeskySampler, cholesky_sampler.cc:25-37)."""
     p = MultigridParameters(nlevel=1, coarse_solver="Cholesky")
     return MultigridMCSampler(linear_operator, p, **kw)
+
+
+# ------------------------------------------------------ deterministic solver
+@dataclass
+class IterativeSolverParameters:
+    """IterativeSolverParameters (auxilliary/parameters.hh:130-147)."""
+    rtol: float = 1.0e-10
+    atol: float = 1.0e-10
+    maxiter: int = 100
+    verbose: int = 0
+
+
+class MultigridPreconditioner:
+    """MultigridPreconditioner (multigrid_preconditioner.cc:8-108) on the GPU:
+    a noise-free cycle of the sampler hierarchy for ``linear_operator`` with
+    the smoothers of ``params`` and a Cholesky coarse solve."""
+
+    def __init__(self, linear_operator, params=None, ordering=MULTICOLOUR, precision=FP64, device=0):
+        self.linear_operator = linear_operator
+        self._s = MultigridMCSampler(linear_operator, params, ordering=ordering, precision=precision, device=device)
+
+    def apply(self, b, x=None):
+        """x = P b (x is filled in place when given)."""
+        y = self._s.precondition(b)
+        if x is None:
+            return y
+        x[:] = y
+        return x
+
+    def close(self):
+        self._s.close()
+
+
+class LoopSolver:
+    """LoopSolver (loop_solver.cc:9-53): x = 0, then x -= P (A x - b) until
+    |r| / |b| < rtol and |r| < atol or maxiter iterations."""
+
+    def __init__(self, linear_operator, preconditioner, params=None):
+        if not isinstance(preconditioner, MultigridPreconditioner):
+            raise TypeError("the GPU loop solver runs with a MultigridPreconditioner")
+        if preconditioner.linear_operator is not linear_operator:
+            raise ValueError("preconditioner built for another operator")
+        self.linear_operator = linear_operator
+        self.preconditioner = preconditioner
+        self.params = params or IterativeSolverParameters()
+        self.niter, self.rnorm, self.converged = 0, -1.0, False
+
+    def apply(self, b, x=None):
+        p = self.params
+        y, self.niter, self.rnorm, self.converged = self.preconditioner._s.solve(b, p.rtol, p.atol, p.maxiter)
+        if p.verbose >= 1:
+            if self.converged:
+                print(f"Solver converged after {self.niter:5d} iterations\n||r|| = {self.rnorm:8.3e}")
+            else:
+                print(f"Solver failed to converge after {p.maxiter:5d} iterations")
+        if x is None:
+            return y
+        x[:] = y
+        return x

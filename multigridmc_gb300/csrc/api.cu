@@ -130,6 +130,14 @@ struct Sampler {
     bool counting = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    // deterministic solver: LoopSolver around MultigridPreconditioner
+    bool noisy = true;  // false while the preconditioner's noise-free cycle is recorded
+    double *sv_x = nullptr, *sv_b = nullptr, *sv_r = nullptr;  // FP64 iterate, rhs, residual (padded level 0)
+    double *sv_part = nullptr, *sv_norm = nullptr;             // |r|^2 partial sums and total
+    int sv_np = 0;
+    void *sv_keep_x = nullptr, *sv_keep_f = nullptr;  // the chain's x_0 and f_0 while a solve borrows them
+    cudaGraph_t rgraph = nullptr, pgraph = nullptr;   // residual + norm; preconditioner cycle
+    cudaGraphExec_t rexec = nullptr, pexec = nullptr;
     std::vector<void *> owned;  // every device allocation
 
     template <typename P_>
@@ -153,6 +161,10 @@ struct Sampler {
     ~Sampler() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
+        if (rexec) cudaGraphExecDestroy(rexec);
+        if (rgraph) cudaGraphDestroy(rgraph);
+        if (pexec) cudaGraphExecDestroy(pexec);
+        if (pgraph) cudaGraphDestroy(pgraph);
         for (void *p : owned) cudaFree(p);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -167,8 +179,10 @@ struct Sampler {
     void adjoint_sample(int lev);
     void build_coarse();
     void launch_step();
-    void sor(int lev, bool forward, bool noisy, void *x, void *f);
+    void sor(int lev, bool forward, bool noisy, void *x, void *f, int nsparse = 1);
+    void smooth(int lev, bool forward, int nsmooth);
     void sample(int lev);
+    void ensure_solver();
     void coarse_sample(int lev);
     void resid_restrict(int lev);
     void prolong(int lev, double alpha, void *xc, void *x);
@@ -414,12 +428,15 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
 // SORSampler::apply (sor_sampler.cc:37-59) / SORSmoother::apply
 // (sor_smoother.cc:40-54) on level `lev`: noise draw order n point normals,
 // then m low-rank normals.
-void Sampler::sor(int lev, bool forward, bool noisy, void *x, void *f) {
+// nsparse > 1 (noise-free only): that many sweeps of the sparse part before
+// the one low-rank correction, as SORSmoother::apply does with nsmooth > 1
+// (sor_smoother.cc:43-53 around the nsmooth sweeps of :64-76).
+void Sampler::sor(int lev, bool forward, bool noisy, void *x, void *f, int nsparse) {
     Level &lv = L[lev];
     int noise = noisy ? noise_mode : NOISE_NONE;
     NoiseArgs nz = noisy ? noise_args(lev, lv.geo.n) : noise_args(lev, 0);
     if (!noisy) nz.buf = nullptr;
-    launch_sweep(*this, lv, forward, noise, x, f, nz, fp32, exact);
+    for (int k = 0; k < (noisy ? 1 : nsparse); ++k) launch_sweep(*this, lv, forward, noise, x, f, nz, fp32, exact);
     if (m > 0) {
         NoiseArgs nzl = noisy ? noise_args(lev, m) : noise_args(lev, 0);
         if (!noisy) nzl.buf = nullptr;
@@ -546,6 +563,17 @@ static void launch_chol(Sampler &S, Level &lv, const NoiseArgs &nz) {
 // (multigridmc_sampler.cc:54-79, 112-116)
 void Sampler::coarse_sample(int lev) {
     Level &lv = L[lev];
+    if (!noisy) {
+        // the preconditioner's coarse solver is always Cholesky
+        // (multigrid_preconditioner.cc:41-46): x = Q^{-1} f
+        NoiseArgs nz = noise_args(lev, 0);
+        nz.buf = nullptr;
+        if (fp32)
+            launch_chol<float, NOISE_NONE>(*this, lv, nz);
+        else
+            launch_chol<double, NOISE_NONE>(*this, lv, nz);
+        return;
+    }
     if (chol) {
         NoiseArgs nz = noise_args(lev, lv.geo.n);
         if (fp32) {
@@ -581,24 +609,34 @@ void Sampler::sample(int lev) {
     for (int j = 0; j < cyc; ++j) {
         if (ssor) {
             for (int k = 0; k < P.npresmooth; ++k) {
-                sor(lev, true, true, lv.x, lv.f);
-                sor(lev, false, true, lv.x, lv.f);
+                sor(lev, true, noisy, lv.x, lv.f);
+                sor(lev, false, noisy, lv.x, lv.f);
             }
         } else {
-            for (int k = 0; k < P.npresmooth; ++k) sor(lev, true, true, lv.x, lv.f);
+            smooth(lev, true, P.npresmooth);
         }
         resid_restrict(lev);  // also zeroes the coarse state
         sample(lev + 1);
         prolong(lev, P.coarse_scaling, lc.x, lv.x);
         if (ssor) {
             for (int k = 0; k < P.npostsmooth; ++k) {
-                sor(lev, true, true, lv.x, lv.f);
-                sor(lev, false, true, lv.x, lv.f);
+                sor(lev, true, noisy, lv.x, lv.f);
+                sor(lev, false, noisy, lv.x, lv.f);
             }
         } else {
-            for (int k = 0; k < P.npostsmooth; ++k) sor(lev, false, true, lv.x, lv.f);
+            smooth(lev, false, P.npostsmooth);
         }
     }
+}
+
+// SOR smoothing with nsmooth passes in one direction: the sampler's
+// SORSampler draws fresh noise for each sweep (sor_sampler.cc:37-59); the
+// preconditioner's SORSmoother repeats nsmooth times nsmooth sparse sweeps
+// and one low-rank correction (sor_smoother.cc:40-78), which is the same
+// for nsmooth = 1.
+void Sampler::smooth(int lev, bool forward, int nsmooth) {
+    Level &lv = L[lev];
+    for (int k = 0; k < nsmooth; ++k) sor(lev, forward, noisy, lv.x, lv.f, nsmooth);
 }
 
 void Sampler::step_end() {
@@ -813,6 +851,8 @@ void Sampler::build_coarse() {
             raise_smem_limit(k_chol_gemv_lower<double, double, NOISE_PHILOX>, chol_smem);
             raise_smem_limit(k_chol_gemv_lower<float, float, NOISE_INJECTED>, chol_smem);
             raise_smem_limit(k_chol_gemv_lower<double, double, NOISE_INJECTED>, chol_smem);
+            raise_smem_limit(k_chol_gemv_lower<float, float, NOISE_NONE>, chol_smem);
+            raise_smem_limit(k_chol_gemv_lower<double, double, NOISE_NONE>, chol_smem);
             raise_smem_limit(k_chol_gemv_upper<float, float>, chol_smem);
             raise_smem_limit(k_chol_gemv_upper<double, double>, chol_smem);
         }
@@ -1082,7 +1122,8 @@ static void *mapped_host(const void *p) {
 
 static dim3 pack_grid(const Level &lv) { return dim3((lv.g.N0 + 255) / 256, lv.g.N1, lv.g.N2); }
 
-static void put_vec(Sampler &S, int lev, const double *src, int on_device, void *dst) {
+// as_f64: dst is an FP64 array whatever the chain's precision
+static void put_vec(Sampler &S, int lev, const double *src, int on_device, void *dst, bool as_f64 = false) {
     Level &lv = S.L[lev];
     const i64 n = lv.geo.n;
     if (n > S.L[0].geo.n) fail(MGMC_ERR_INVALID_ARGUMENT, "level size");
@@ -1094,14 +1135,14 @@ static void put_vec(Sampler &S, int lev, const double *src, int on_device, void 
             d = S.d_cvec;
         }
     }
-    if (S.fp32)
+    if (S.fp32 && !as_f64)
         k_unpack<float><<<pack_grid(lv), 256, 0, S.stream>>>(d, (float *)dst, lv.g);
     else
         k_unpack<double><<<pack_grid(lv), 256, 0, S.stream>>>(d, (double *)dst, lv.g);
     S.check_launch();
 }
 
-static void get_vec(Sampler &S, int lev, const void *src, double *dst, int on_device) {
+static void get_vec(Sampler &S, int lev, const void *src, double *dst, int on_device, bool as_f64 = false) {
     Level &lv = S.L[lev];
     const i64 n = lv.geo.n;
     double *d = dst;
@@ -1113,7 +1154,7 @@ static void get_vec(Sampler &S, int lev, const void *src, double *dst, int on_de
             staged = true;
         }
     }
-    if (S.fp32)
+    if (S.fp32 && !as_f64)
         k_pack<float><<<pack_grid(lv), 256, 0, S.stream>>>((const float *)src, d, lv.g);
     else
         k_pack<double><<<pack_grid(lv), 256, 0, S.stream>>>((const double *)src, d, lv.g);
@@ -1164,6 +1205,93 @@ static void run_steps(Sampler &S, i64 nsteps) {
     ensure_graph(S);
     for (i64 k = 0; k < nsteps; ++k) CK(cudaGraphLaunch(S.gexec, S.stream));
 }
+
+// ------------------------------------------------- deterministic solver
+// LoopSolver (loop_solver.cc:9-53) around MultigridPreconditioner
+// (multigrid_preconditioner.cc:8-108) on this hierarchy.  The
+// preconditioner is the sampler's cycle with the noise switched off: the
+// same sweeps with their low-rank corrections, residual-restriction,
+// prolongation and coarse scaling, from a zero state, with the Cholesky
+// coarse solve.  Two graphs: the FP64 residual r = b - A x with |r|^2 (and
+// the preconditioner's input f_0 = r, x_0 = 0), and the cycle followed by
+// x += P r.
+void Sampler::ensure_solver() {
+    if (rexec && pexec) return;
+    if (!dLinv) build_coarse();
+    Level &l0 = L[0];
+    const i64 na = l0.geo.nalloc;
+    if (!sv_x) {
+        sv_x = alloc<double>(na);
+        sv_b = alloc<double>(na);
+        sv_r = alloc<double>(na);
+        for (double *p : {sv_x, sv_b, sv_r}) CK(cudaMemsetAsync(p, 0, (size_t)na * sizeof(double), stream));
+        const i64 nrows = (i64)l0.g.N1 * l0.g.N2;
+        sv_np = (int)((nrows + SOLVE_ROWS - 1) / SOLVE_ROWS);
+        sv_part = alloc<double>(sv_np);
+        sv_norm = alloc<double>(1);
+        sv_keep_x = talloc(na);
+        sv_keep_f = talloc(na);
+    }
+    auto capture = [&](cudaGraph_t &g, cudaGraphExec_t &ge, const std::function<void()> &body) {
+        CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            body();
+            check_launch();
+        } catch (...) {
+            noisy = true;
+            cudaGraph_t gg = nullptr;
+            cudaStreamEndCapture(stream, &gg);
+            if (gg) cudaGraphDestroy(gg);
+            throw;
+        }
+        CK(cudaStreamEndCapture(stream, &g));
+        CK(cudaGraphInstantiate(&ge, g, 0));
+    };
+    if (!rexec)
+        capture(rgraph, rexec, [&]() {
+            const StencilArg<double> st = stencil_arg<double>(l0, P.omega);
+            if (l0.npt == 7)
+                k_solve_resid<7><<<pack_grid(l0), 256, 0, stream>>>(sv_x, sv_b, sv_r, l0.g, st);
+            else
+                k_solve_resid<27><<<pack_grid(l0), 256, 0, stream>>>(sv_x, sv_b, sv_r, l0.g, st);
+            if (m > 0) {
+                launch_bt_plain<double>(*this, l0, sv_x);
+                launch_add_Bq<double>(*this, l0, sv_r, l0.y, -1.0);
+            }
+            if (fp32)
+                k_solve_rhs<float><<<sv_np, 256, 0, stream>>>(sv_r, (float *)l0.f, (float *)l0.x, l0.g, sv_part);
+            else
+                k_solve_rhs<double><<<sv_np, 256, 0, stream>>>(sv_r, (double *)l0.f, (double *)l0.x, l0.g, sv_part);
+            k_solve_norm<<<1, 256, 0, stream>>>(sv_part, sv_np, sv_norm);
+        });
+    if (!pexec)
+        capture(pgraph, pexec, [&]() {
+            noisy = false;
+            sample(0);
+            noisy = true;
+            const unsigned blocks = (unsigned)std::min<i64>(nblk(na, 256), 8 * nsm);
+            if (fp32)
+                k_solve_update<float><<<blocks, 256, 0, stream>>>(sv_x, (const float *)l0.x, na);
+            else
+                k_solve_update<double><<<blocks, 256, 0, stream>>>(sv_x, (const double *)l0.x, na);
+        });
+}
+
+// The chain's x_0 and f_0 are borrowed by a solve and put back afterwards.
+struct BorrowLevel0 {
+    Sampler &S;
+    explicit BorrowLevel0(Sampler &s) : S(s) {
+        const size_t bytes = (size_t)S.L[0].geo.nalloc * S.tsize();
+        CK(cudaMemcpyAsync(S.sv_keep_x, S.L[0].x, bytes, cudaMemcpyDeviceToDevice, S.stream));
+        CK(cudaMemcpyAsync(S.sv_keep_f, S.L[0].f, bytes, cudaMemcpyDeviceToDevice, S.stream));
+    }
+    ~BorrowLevel0() {
+        const size_t bytes = (size_t)S.L[0].geo.nalloc * S.tsize();
+        cudaMemcpyAsync(S.L[0].x, S.sv_keep_x, bytes, cudaMemcpyDeviceToDevice, S.stream);
+        cudaMemcpyAsync(S.L[0].f, S.sv_keep_f, bytes, cudaMemcpyDeviceToDevice, S.stream);
+        cudaStreamSynchronize(S.stream);
+    }
+};
 
 // ------------------------------------------------------------- adjoint
 // Transpose of the linear part of one MGMC step with its noise held fixed.
@@ -1822,6 +1950,62 @@ mgmc_status mgmc_batch_destroy(mgmc_batch *b) {
 }
 
 }  // extern "C"
+
+mgmc_status mgmc_sampler_precondition(mgmc_sampler *s, const double *b, double *x, int on_device) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!b || !x) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    CK(cudaStreamSynchronize(S.stream));
+    S.ensure_solver();
+    Level &l0 = S.L[0];
+    BorrowLevel0 borrow(S);
+    put_vec(S, 0, b, on_device, l0.f);
+    CK(cudaMemsetAsync(l0.x, 0, (size_t)l0.geo.nalloc * S.tsize(), S.stream));
+    CK(cudaGraphLaunch(S.pexec, S.stream));
+    get_vec(S, 0, l0.x, x, on_device);
+    CK(cudaStreamSynchronize(S.stream));
+    check_device_errors(S);
+    API_END
+}
+
+mgmc_status mgmc_sampler_solve(mgmc_sampler *s, const double *b, double *x, double rtol, double atol, int maxiter,
+                               int on_device, int *niter, double *rnorm, int *converged) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!b || !x || !niter || !rnorm || !converged) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    if (maxiter < 0) fail(MGMC_ERR_INVALID_ARGUMENT, "maxiter < 0");
+    CK(cudaStreamSynchronize(S.stream));
+    S.ensure_solver();
+    Level &l0 = S.L[0];
+    int k = 0;
+    double r0 = 0.0, rn = -1.0;
+    bool conv = false;
+    {
+        BorrowLevel0 borrow(S);
+        put_vec(S, 0, b, on_device, S.sv_b, true);
+        CK(cudaMemsetAsync(S.sv_x, 0, (size_t)l0.geo.nalloc * sizeof(double), S.stream));  // loop_solver.cc:17
+        for (k = 0; k < maxiter; ++k) {
+            CK(cudaGraphLaunch(S.rexec, S.stream));
+            double r2 = 0.0;
+            CK(cudaMemcpyAsync(&r2, S.sv_norm, sizeof(double), cudaMemcpyDeviceToHost, S.stream));
+            CK(cudaStreamSynchronize(S.stream));
+            rn = std::sqrt(r2);
+            if (!std::isfinite(rn)) fail(MGMC_ERR_NONFINITE, "non-finite residual in the solver");
+            if (k == 0) r0 = rn;  // |A 0 - b| = |b| (loop_solver.cc:11)
+            if (rn / r0 < rtol && rn < atol) {
+                conv = true;
+                break;
+            }
+            CK(cudaGraphLaunch(S.pexec, S.stream));
+        }
+        get_vec(S, 0, S.sv_x, x, on_device, true);
+    }
+    check_device_errors(S);
+    *niter = k;
+    *rnorm = rn;
+    *converged = conv ? 1 : 0;
+    API_END
+}
 
 mgmc_status mgmc_sampler_adjoint_step(mgmc_sampler *s, double *xbar, double *fbar, int on_device) {
     API_BEGIN

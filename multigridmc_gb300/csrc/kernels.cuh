@@ -24,7 +24,9 @@
 //   k_chol_gemv_*       coarse-level Cholesky sample (k_chol_subst: parity)
 //   k_step_end          observables z = b^T x, step counter
 // Host conversions: k_unpack / k_unpack2 / k_pack; adjoint helpers: k_axpy,
-// k_sinvt_q; building blocks: k_apply_stencil.
+// k_sinvt_q; deterministic solver (FP64 loop around the noise-free cycle):
+// k_solve_resid, k_solve_rhs, k_solve_norm, k_solve_update; building
+// blocks: k_apply_stencil.
 #pragma once
 
 #include <cstdint>
@@ -161,9 +163,9 @@ struct Ar<false> {
 // side of sor_sampler.cc:42-46):
 //   c = sd * xi + f;  res = sum_k w_k x_k (ascending index, diagonal
 //   included);  x += omega * (c - res) / diag.
+// Row P of A_0 x: sum_k w_k x_k in ascending index order, diagonal included.
 template <typename T, int NPT, bool EXACT>
-__device__ __forceinline__ void sor_point(T *__restrict__ x, const T *__restrict__ f, const Grid3 &g,
-                                          const StencilArg<T> &s, i64 P, bool noisy, T xi) {
+__device__ __forceinline__ T stencil_row(const T *__restrict__ x, const Grid3 &g, const StencilArg<T> &s, i64 P) {
     typedef Ar<EXACT> A;
     T res = T(0);
     if (NPT == 7) {
@@ -180,6 +182,14 @@ __device__ __forceinline__ void sor_point(T *__restrict__ x, const T *__restrict
                 for (int dx = -1; dx <= 1; ++dx)
                     res = A::add(res, A::mul(s.w[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)], x[P + dz * g.sz + dy * g.sy + dx]));
     }
+    return res;
+}
+
+template <typename T, int NPT, bool EXACT>
+__device__ __forceinline__ void sor_point(T *__restrict__ x, const T *__restrict__ f, const Grid3 &g,
+                                          const StencilArg<T> &s, i64 P, bool noisy, T xi) {
+    typedef Ar<EXACT> A;
+    const T res = stencil_row<T, NPT, EXACT>(x, g, s, P);
     T cval = f[P];
     if (noisy) cval = A::add(A::mul(s.sd, xi), cval);
     T xo = x[P];
@@ -1182,6 +1192,67 @@ __global__ void __launch_bounds__(256) k_sinvt_q(const double *__restrict__ Sinv
     double t = 0.0;
     for (int j = 0; j < m; ++j) t = fma(SinvT[(i64)k * m + j], q[j], t);
     out[k] = sigma_sqrt[k] * sigma_sqrt[k] * t;
+}
+
+// ------------------------------------------------- deterministic solver
+// One iteration of LoopSolver::apply (loop_solver.cc:24-42) keeps the
+// iterate x, the right hand side b and the residual r in FP64 on level 0,
+// whatever the type T of the hierarchy that applies the multigrid
+// preconditioner: with an FP32 hierarchy the loop is iterative refinement
+// and still converges to FP64 accuracy.
+//
+// r = b - A_0 x over the interior (the low-rank term is added afterwards by
+// k_add_Bq with sign -1).
+template <int NPT>
+__global__ void __launch_bounds__(256) k_solve_resid(const double *__restrict__ x, const double *__restrict__ b,
+                                                     double *__restrict__ r, Grid3 g, StencilArg<double> s) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x, bb = blockIdx.y, c = blockIdx.z;
+    if (a >= g.N0) return;
+    const i64 P = g.pad(a, bb, c);
+    r[P] = b[P] - stencil_row<double, NPT, false>(x, g, s, P);
+}
+
+// Per CTA: SOLVE_ROWS rows (b, c) of the interior.  The partial sums of
+// |r|^2 go to part[blockIdx.x] (a fixed grid, so the norm is
+// reproducible); the preconditioner gets f = (T) r and the zero initial
+// state of MultigridPreconditioner::solve (multigrid_preconditioner.cc:76).
+constexpr int SOLVE_ROWS = 8;
+template <typename T>
+__global__ void __launch_bounds__(256) k_solve_rhs(const double *__restrict__ r, T *__restrict__ f,
+                                                   T *__restrict__ x, Grid3 g, double *__restrict__ part) {
+    __shared__ double sh[32];
+    const i64 nrows = (i64)g.N1 * g.N2;
+    double acc = 0.0;
+    for (int q = 0; q < SOLVE_ROWS; ++q) {
+        const i64 row = (i64)blockIdx.x * SOLVE_ROWS + q;
+        if (row >= nrows) break;
+        const int bb = (int)(row % g.N1), c = (int)(row / g.N1);
+        for (int a = threadIdx.x; a < g.N0; a += blockDim.x) {
+            const i64 P = g.pad(a, bb, c);
+            const double v = r[P];
+            acc += v * v;
+            f[P] = (T)v;
+            x[P] = T(0);
+        }
+    }
+    acc = block_sum<256>(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// |r|^2 = the sum of the partial sums, in one CTA.
+__global__ void __launch_bounds__(256) k_solve_norm(const double *__restrict__ part, int np, double *__restrict__ out) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) acc += part[i];
+    acc = block_sum<256>(acc, sh);
+    if (threadIdx.x == 0) *out = acc;
+}
+
+// x += P r: the preconditioner's result (type T) added to the FP64 iterate
+// over whole padded arrays (ghosts are zero in both).
+template <typename T>
+__global__ void __launch_bounds__(256) k_solve_update(double *__restrict__ x, const T *__restrict__ dx, i64 n) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) x[i] += (double)dx[i];
 }
 
 // ------------------------------------------------------------ step end

@@ -84,6 +84,12 @@ def lib():
         "orc_sampler_mean_cov": (C.c_int, [_P, C.c_int64, _D, _D, C.c_int64, C.c_int64, _D, _D]),
         "orc_ssor_smoother_apply": (None, [_P, C.c_double, C.c_int, C.c_int, _D, _D]),
         "orc_dense_cholesky": (C.c_int, [_D, C.c_int64]),
+        "orc_mg_create": (_P, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int,
+                               C.c_int]),
+        "orc_mg_destroy": (None, [_P]),
+        "orc_mg_apply": (None, [_P, _D, _D]),
+        "orc_loop_solve": (C.c_int, [_P, _D, _D, C.c_double, C.c_double, C.c_int, _D, _INT]),
+        "orc_cholesky_solve": (C.c_int, [_P, _D, _D]),
         "orc_stats_create": (_P, [C.c_int, C.c_uint]),
         "orc_stats_destroy": (None, [_P]),
         "orc_stats_record": (None, [_P, _D, C.c_int64]),
@@ -405,6 +411,49 @@ def mgmc_sampler(op, source, nlevel, smoother="SSOR", coarse_solver="Cholesky", 
 def ssor_smoother_apply(op, omega, b, x, nsmooth=1, ordering=0):
     b = np.ascontiguousarray(b, dtype=np.float64)
     lib().orc_ssor_smoother_apply(op.h, omega, nsmooth, ordering, _dp(b), _dp(x))
+
+
+class MGPreconditioner:
+    """MultigridPreconditioner (multigrid_preconditioner.cc:8-108); coarse
+    solve by the Woodbury CholeskySolver (woodbury=True) or the dense
+    natural-order factor of the full coarse precision."""
+
+    def __init__(self, op, nlevel, smoother="SSOR", npresmooth=1, npostsmooth=1, omega=1.0, cycle=1,
+                 coarse_scaling=1.0, ordering=0, woodbury=True):
+        self.op = op
+        self.h = lib().orc_mg_create(op.h, nlevel, 1 if smoother == "SSOR" else 0, npresmooth, npostsmooth,
+                                     omega, cycle, coarse_scaling, ordering, int(woodbury))
+        if not self.h:
+            raise RuntimeError("multigrid preconditioner set-up failed")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_mg_destroy(self.h)
+            self.h = None
+
+    def apply(self, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(self.op.n)
+        lib().orc_mg_apply(self.h, _dp(b), _dp(x))
+        return x
+
+    def loop_solve(self, b, rtol, atol, maxiter):
+        """LoopSolver::apply (loop_solver.cc:9-53): (x, niter, rnorm, converged)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(self.op.n)
+        rn = C.c_double(0.0)
+        cv = C.c_int(0)
+        it = lib().orc_loop_solve(self.h, _dp(b), _dp(x), rtol, atol, maxiter, C.byref(rn), C.byref(cv))
+        return x, it, rn.value, bool(cv.value)
+
+
+def cholesky_solve(op, b):
+    """CholeskySolver::apply (cholesky_solver.cc:9-43, Woodbury form)."""
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(op.n)
+    if lib().orc_cholesky_solve(op.h, _dp(b), _dp(x)):
+        raise np.linalg.LinAlgError("not SPD")
+    return x
 
 
 def dense_cholesky(A):

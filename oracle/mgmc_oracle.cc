@@ -1064,6 +1064,225 @@ struct MGMCSampler : Sampler {
 };
 
 // ---------------------------------------------------------------------------
+// Deterministic solvers: cholesky_solver.cc:9-43, multigrid_preconditioner.cc
+// :8-108, loop_solver.cc:9-53.
+// ---------------------------------------------------------------------------
+// CholeskySolver: factor the sparse part A_0 and apply the low-rank term by
+// the Woodbury identity, x = y - Bbar B^T y with y = A_0^{-1} b and
+// Bbar = A_0^{-1} B (Sigma + B^T A_0^{-1} B)^{-1} (cholesky_solver.cc:9-43).
+// The factor is the dense natural-order one (the reference: Eigen's
+// SimplicialLLT with AMD ordering; the solution agrees to rounding).
+struct CholeskySolver {
+    std::shared_ptr<LinOp> op;
+    int64_t n;
+    std::vector<double> L, Bbar;  // Bbar n x m row-major
+    bool ok;
+    explicit CholeskySolver(std::shared_ptr<LinOp> op_) : op(op_) {
+        n = op->n();
+        L.assign(n * n, 0.0);
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t k = op->A.ptr[i]; k < op->A.ptr[i + 1]; ++k) L[i * n + op->A.col[k]] = op->A.val[k];
+        ok = dense_cholesky(L, n);
+        const int m = op->m();
+        if (!ok || m == 0) return;
+        std::vector<double> AinvB((size_t)n * m), col(n), y(n);
+        for (int j = 0; j < m; ++j) {
+            std::fill(col.begin(), col.end(), 0.0);
+            for (int64_t e = op->B.ptr[j]; e < op->B.ptr[j + 1]; ++e) col[op->B.row[e]] = op->B.val[e];
+            solve_A0(col.data(), y.data());
+            for (int64_t i = 0; i < n; ++i) AinvB[(size_t)i * m + j] = y[i];
+        }
+        std::vector<double> S((size_t)m * m, 0.0);  // Sigma + B^T A_0^{-1} B
+        for (int a = 0; a < m; ++a) {
+            for (int b = 0; b < m; ++b) {
+                double acc = 0.0;
+                for (int64_t e = op->B.ptr[a]; e < op->B.ptr[a + 1]; ++e) acc += op->B.val[e] * AinvB[(size_t)op->B.row[e] * m + b];
+                S[a * m + b] = acc;
+            }
+            S[a * m + a] += op->Sigma[a];
+        }
+        std::vector<double> Sinv = dense_inverse(S, m);
+        Bbar.assign((size_t)n * m, 0.0);
+        for (int64_t i = 0; i < n; ++i)
+            for (int b = 0; b < m; ++b) {
+                double acc = 0.0;
+                for (int a = 0; a < m; ++a) acc += AinvB[(size_t)i * m + a] * Sinv[a * m + b];
+                Bbar[(size_t)i * m + b] = acc;
+            }
+    }
+    void solve_A0(const double *b, double *x) const {  // L L^T x = b
+        std::vector<double> g(n);
+        for (int64_t i = 0; i < n; ++i) {
+            double s = b[i];
+            for (int64_t k = 0; k < i; ++k) s -= L[i * n + k] * g[k];
+            g[i] = s / L[i * n + i];
+        }
+        for (int64_t i = n - 1; i >= 0; --i) {
+            double s = g[i];
+            for (int64_t k = n - 1; k > i; --k) s -= L[k * n + i] * x[k];
+            x[i] = s / L[i * n + i];
+        }
+    }
+    void apply(const double *b, double *x) const {  // cholesky_solver.cc:29-43
+        const int m = op->m();
+        if (m == 0) {
+            solve_A0(b, x);
+            return;
+        }
+        std::vector<double> y(n), BTy(m, 0.0);
+        solve_A0(b, y.data());
+        for (int j = 0; j < m; ++j) {
+            double acc = 0.0;
+            for (int64_t e = op->B.ptr[j]; e < op->B.ptr[j + 1]; ++e) acc += op->B.val[e] * y[op->B.row[e]];
+            BTy[j] = acc;
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            double acc = 0.0;
+            for (int j = 0; j < m; ++j) acc += Bbar[(size_t)i * m + j] * BTy[j];
+            x[i] = y[i] - acc;
+        }
+    }
+};
+
+// MultigridPreconditioner (multigrid_preconditioner.cc:8-108).  The coarse
+// solve is the CholeskySolver above (woodbury = true) or the noise-free
+// dense natural-order Cholesky sample of the full coarse precision
+// (woodbury = false), the form the GPU computes; both give Q_c^{-1} b to
+// rounding.
+struct MGPreconditioner {
+    MGParams p;
+    bool woodbury;
+    std::vector<std::shared_ptr<LinOp>> ops;
+    std::vector<std::unique_ptr<SORSmoother>> fwd, bwd;
+    std::vector<std::unique_ptr<Intergrid>> ig;
+    std::unique_ptr<CholeskySolver> coarse_w;
+    std::unique_ptr<CholeskySampler> coarse_d;
+    BufferSource zeros;  // the noise of the dense coarse sample: zero
+    std::vector<std::vector<double>> x_ell, b_ell, r_ell;
+    BbarCache cache;
+    bool ok = true;
+    MGPreconditioner(std::shared_ptr<LinOp> op, const MGParams &p_, bool woodbury_) : p(p_), woodbury(woodbury_) {
+        std::shared_ptr<LinOp> lin_op = op;
+        for (int level = 0; level < p.nlevel; ++level) {
+            int64_t n = lin_op->n();
+            x_ell.emplace_back(n, 0.0);
+            b_ell.emplace_back(n, 0.0);
+            r_ell.emplace_back(n, 0.0);
+            ops.push_back(lin_op);
+            fwd.emplace_back(new SORSmoother(lin_op, p.omega, true, p.ordering, &cache));
+            bwd.emplace_back(new SORSmoother(lin_op, p.omega, false, p.ordering, &cache));
+            if (level < p.nlevel - 1) {
+                if (!lin_op->lat.coarsenable()) throw std::runtime_error("cannot coarsen lattice");
+                ig.emplace_back(new Intergrid(lin_op->lat));
+                lin_op = coarsen(*lin_op, *ig.back());
+            }
+        }
+        if (woodbury) {
+            coarse_w.reset(new CholeskySolver(lin_op));
+            ok = coarse_w->ok;
+        } else {
+            zeros.data.assign((size_t)lin_op->n(), 0.0);
+            coarse_d.reset(new CholeskySampler(lin_op, &zeros));
+            ok = coarse_d->ok;
+        }
+    }
+    // SORSmoother::apply with nsmooth passes (sor_smoother.cc:40-78): nsmooth
+    // times nsmooth sparse sweeps and one low-rank correction
+    void sor_smooth(const SORSmoother &s, int nsmooth, const double *b, double *x) {
+        for (int k = 0; k < nsmooth; ++k) {
+            for (int j = 0; j < nsmooth; ++j) s.apply_sparse(b, x);
+            if (s.op->m() > 0) {
+                // the low-rank part of SORSmoother::apply alone: x -= Bbar B^T x
+                const int m = s.op->m();
+                std::vector<double> y(m, 0.0);
+                for (int jj = 0; jj < m; ++jj) {
+                    double acc = 0.0;
+                    for (int64_t e = s.op->B.ptr[jj]; e < s.op->B.ptr[jj + 1]; ++e) acc += s.op->B.val[e] * x[s.op->B.row[e]];
+                    y[jj] = acc;
+                }
+                const double *Bb = s.Bbar->data();
+                for (int64_t i = 0; i < s.op->n(); ++i) {
+                    double acc = 0.0;
+                    for (int jj = 0; jj < m; ++jj) acc += Bb[(size_t)i * m + jj] * y[jj];
+                    x[i] -= acc;
+                }
+            }
+        }
+    }
+    void smooth(int level, bool pre, const double *b, double *x) {
+        const int ns = pre ? p.npresmooth : p.npostsmooth;
+        if (p.smoother == 1) {  // SSORSmoother (ssor_smoother.cc:9-16)
+            for (int k = 0; k < ns; ++k) {
+                fwd[level]->apply(b, x);
+                bwd[level]->apply(b, x);
+            }
+        } else {  // SOR: forward before, backward after the coarse correction
+            sor_smooth(pre ? *fwd[level] : *bwd[level], ns, b, x);
+        }
+    }
+    void solve(int level) {  // multigrid_preconditioner.cc:73-100
+        std::fill(x_ell[level].begin(), x_ell[level].end(), 0.0);
+        if (level == p.nlevel - 1) {
+            if (woodbury) {
+                coarse_w->apply(b_ell[level].data(), x_ell[level].data());
+            } else {
+                zeros.pos = 0;
+                coarse_d->apply(b_ell[level].data(), x_ell[level].data());
+            }
+            return;
+        }
+        int cyc = (level > 0) ? p.cycle : 1;
+        for (int j = 0; j < cyc; ++j) {
+            smooth(level, true, b_ell[level].data(), x_ell[level].data());
+            ops[level]->apply(x_ell[level].data(), r_ell[level].data());
+            int64_t n = ops[level]->n();
+            for (int64_t i = 0; i < n; ++i) r_ell[level][i] = b_ell[level][i] - r_ell[level][i];
+            ig[level]->restrict_(r_ell[level].data(), b_ell[level + 1].data());
+            solve(level + 1);
+            ig[level]->prolongate_add(p.coarse_scaling, x_ell[level + 1].data(), x_ell[level].data());
+            smooth(level, false, b_ell[level].data(), x_ell[level].data());
+        }
+    }
+    void apply(const double *b, double *x) {  // :103-108
+        std::copy(b, b + ops[0]->n(), b_ell[0].begin());
+        solve(0);
+        std::copy(x_ell[0].begin(), x_ell[0].end(), x);
+    }
+};
+
+static double vec_norm(const std::vector<double> &v) {
+    double s = 0.0;
+    for (double a : v) s += a * a;
+    return sqrt(s);
+}
+
+// LoopSolver::apply (loop_solver.cc:9-53); returns the iteration count at
+// convergence, or maxiter.
+static int loop_solve(const LinOp &op, MGPreconditioner &P, const double *b, double *x, double rtol, double atol,
+                      int maxiter, double *rnorm, int *converged) {
+    const int64_t n = op.n();
+    double r0_nrm = vec_norm(std::vector<double>(b, b + n));
+    std::fill(x, x + n, 0.0);
+    std::vector<double> r(n), Pr(n);
+    *converged = 0;
+    *rnorm = -1.0;
+    int k = 0;
+    for (k = 0; k < maxiter; ++k) {
+        op.apply(x, r.data());
+        for (int64_t i = 0; i < n; ++i) r[i] -= b[i];
+        const double r_nrm = vec_norm(r);
+        *rnorm = r_nrm;
+        if ((r_nrm / r0_nrm < rtol) && (r_nrm < atol)) {
+            *converged = 1;
+            break;
+        }
+        P.apply(r.data(), Pr.data());
+        for (int64_t i = 0; i < n; ++i) x[i] -= Pr[i];
+    }
+    return k;
+}
+
+// ---------------------------------------------------------------------------
 // Statistics: statistics.{hh,cc}
 // ---------------------------------------------------------------------------
 struct Statistics {
@@ -1430,6 +1649,39 @@ int orc_dense_cholesky(double *A, int64_t n) {
     std::vector<double> M(A, A + n * n);
     if (!dense_cholesky(M, n)) return 1;
     std::copy(M.begin(), M.end(), A);
+    return 0;
+}
+
+// ---- deterministic solvers ----
+struct orc_mg {
+    std::unique_ptr<MGPreconditioner> P;
+    std::shared_ptr<LinOp> op;
+};
+orc_mg *orc_mg_create(orc_op *o, int nlevel, int smoother, int npresmooth, int npostsmooth, double omega, int cycle,
+                      double coarse_scaling, int ordering, int woodbury) {
+    MGParams p{nlevel, smoother, 0, npresmooth, npostsmooth, 1, omega, cycle, coarse_scaling, ordering};
+    try {
+        auto *h = new orc_mg{std::unique_ptr<MGPreconditioner>(new MGPreconditioner(o->op, p, woodbury != 0)), o->op};
+        if (!h->P->ok) {
+            delete h;
+            return nullptr;
+        }
+        return h;
+    } catch (...) {
+        return nullptr;
+    }
+}
+void orc_mg_destroy(orc_mg *h) { delete h; }
+void orc_mg_apply(orc_mg *h, const double *b, double *x) { h->P->apply(b, x); }
+int orc_loop_solve(orc_mg *h, const double *b, double *x, double rtol, double atol, int maxiter, double *rnorm,
+                   int *converged) {
+    return loop_solve(*h->op, *h->P, b, x, rtol, atol, maxiter, rnorm, converged);
+}
+// CholeskySolver::apply (Woodbury); returns 1 if A_0 is not SPD
+int orc_cholesky_solve(orc_op *o, const double *b, double *x) {
+    CholeskySolver s(o->op);
+    if (!s.ok) return 1;
+    s.apply(b, x);
     return 0;
 }
 
