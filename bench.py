@@ -274,6 +274,25 @@ def covariance_study(nsamples, nprobe=256, warmup=50, seed=1000):
     C32 = np.cov(Z["fp32"][:, :nprobe].T)
     C64 = np.cov(Z["fp64"][:, :nprobe].T)
     res["cov_rel_frobenius"] = float(np.linalg.norm(C32 - C64) / np.linalg.norm(C64))
+    # each chain against the exact posterior: mean Q^{-1} f and the probe
+    # covariances e_p^T Q^{-1} e_q, by multigrid solves on the GPU
+    Cx, mu, solve_s = exact_probe_moments(op, f, pts)
+    for name in ("fp32", "fp64"):
+        Zp = Z[name][:, :nprobe]
+        C = np.cov(Zp.T)
+        tau = res[name]["iact"]
+        # Monte Carlo standard errors for nsamples draws with integrated
+        # autocorrelation time tau: Var(C^_pq) ~ tau (C_pq^2 + C_pp C_qq) / N,
+        # Var(mean_p) ~ tau C_pp / N
+        cov_se = np.sqrt(tau * np.sum(Cx ** 2 + np.outer(np.diag(Cx), np.diag(Cx))) / nsamples)
+        mean_se = np.sqrt(tau * np.sum(np.diag(Cx)) / nsamples)
+        res[name]["cov_vs_exact_rel_frobenius"] = float(np.linalg.norm(C - Cx) / np.linalg.norm(Cx))
+        res[name]["cov_vs_exact_mc_expected"] = float(cov_se / np.linalg.norm(Cx))
+        res[name]["mean_vs_exact_rel"] = float(np.linalg.norm(Zp.mean(0) - mu) / np.linalg.norm(mu))
+        res[name]["mean_vs_exact_mc_expected"] = float(mean_se / np.linalg.norm(mu))
+    res["exact_moments"] = {"method": "MG-preconditioned loop solves on the GPU (FP32-mixed cycle, FP64 "
+                                      "refinement, rtol 1e-10), one per probe plus one for the mean",
+                            "seconds": solve_s}
     res["mean_rel_diff"] = float(np.linalg.norm(Z["fp32"][:, :nprobe].mean(0) - Z["fp64"][:, :nprobe].mean(0))
                                  / np.linalg.norm(Z["fp64"][:, :nprobe].mean(0)))
     res["pathwise_rel_diff_last"] = float(np.linalg.norm(Z["fp32"][-1, :nprobe] - Z["fp64"][-1, :nprobe])
@@ -281,6 +300,74 @@ def covariance_study(nsamples, nprobe=256, warmup=50, seed=1000):
     res["nsamples"] = nsamples
     res["nprobe"] = nprobe
     return res
+
+
+def exact_probe_moments(op, f, pts, rtol=1e-10):
+    """Exact posterior mean at the probe points, (Q^{-1} f)[pts], and the
+    probe covariance matrix (Q^{-1})[pts, pts], by LoopSolver solves with the
+    multigrid preconditioner on the GPU (the reference's Woodbury + loop
+    solve comparator of cholesky_solver.cc / loop_solver.cc at sizes where a
+    factorisation does not fit)."""
+    import torch
+    import multigridmc_gb300 as M
+    s = M.MultigridMCSampler(op, M.MultigridParameters(nlevel=NLEVEL), precision=M.FP32_MIXED)
+    b = torch.zeros(op.n, dtype=torch.float64, device="cuda")
+    x = torch.zeros_like(b)
+    idx = torch.as_tensor(np.asarray(pts, np.int64), device="cuda")
+    t0 = time.perf_counter()
+    C = np.zeros((len(pts), len(pts)))
+    for k, p in enumerate(pts):
+        b.zero_()
+        b[int(p)] = 1.0
+        torch.cuda.synchronize()
+        _, _, conv = s.solve_device(b.data_ptr(), x.data_ptr(), rtol, 1e30, 100)
+        if not conv:
+            raise RuntimeError("probe solve did not converge")
+        C[:, k] = x[idx].cpu().numpy()
+    b.copy_(torch.from_numpy(np.asarray(f, np.float64)))
+    torch.cuda.synchronize()
+    _, _, conv = s.solve_device(b.data_ptr(), x.data_ptr(), rtol, 1e30, 100)
+    if not conv:
+        raise RuntimeError("mean solve did not converge")
+    mu = x[idx].cpu().numpy()
+    dt = time.perf_counter() - t0
+    s.close()
+    return 0.5 * (C + C.T), mu, dt
+
+
+def solve_study(rtol=1e-10, repeats=3):
+    """The reference's deterministic multigrid solve (driver_mg: LoopSolver
+    with MultigridPreconditioner) of Q x = f on the 256^3 posterior: FP64
+    cycle and FP32-mixed cycle with FP64 refinement; device-resident
+    vectors, host clock around the whole solve (it synchronises once per
+    iteration for the convergence test)."""
+    import torch
+    import multigridmc_gb300 as M
+    op, f, _, _, _ = problem()
+    b = torch.from_numpy(np.asarray(f, np.float64)).cuda()
+    x = torch.zeros_like(b)
+    out = {}
+    for name, prec in (("fp32_mixed", M.FP32_MIXED), ("fp64", M.FP64)):
+        s = M.MultigridMCSampler(op, M.MultigridParameters(nlevel=NLEVEL), precision=prec)
+        s.solve_device(b.data_ptr(), x.data_ptr(), rtol, 1e30, 100)  # graphs and solver buffers
+        best = None
+        for _ in range(repeats):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            it, rn, conv = s.solve_device(b.data_ptr(), x.data_ptr(), rtol, 1e30, 100)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        # residual of the returned x, checked through the FP64 operator apply
+        xh = x.cpu().numpy()
+        r = f - s.level_apply(0, xh) if prec == M.FP64 else None
+        s.close()
+        out[name] = {"iterations": it, "converged": conv, "ms": best * 1e3, "ms_per_iteration": best * 1e3 / max(it, 1),
+                     "rel_residual": rn / float(np.linalg.norm(f))}
+        if r is not None:
+            out[name]["rel_residual_host_check"] = float(np.linalg.norm(r) / np.linalg.norm(f))
+    out["rtol"] = rtol
+    out["problem"] = "3D 256^3 posterior, 64 measurements, V(1,1) SSOR, 5 levels, coarse Cholesky 16^3"
+    return out
 
 
 def batch_study(nchain, steps, warmup=5, seed=3):
@@ -402,6 +489,8 @@ def main():
                     help="run the batched-chains study (N chains of mixed sizes) instead of the benchmark")
     ap.add_argument("--convergence-study", type=int, default=0, metavar="NCHAIN",
                     help="run measure_convergence over NCHAIN batched chains (--steps steps) instead of the benchmark")
+    ap.add_argument("--solve-study", action="store_true",
+                    help="time the deterministic multigrid solve of Q x = f instead of the benchmark")
     ap.add_argument("--profile-steps", type=int, default=0, metavar="K",
                     help="profiling mode: K steps of the benchmark chain inside an NVTX range 'timed' "
                          "(after --warmup steps), for ncu --nvtx-include timed/; prints no JSON")
@@ -415,6 +504,9 @@ def main():
         return
     if args.convergence_study > 0:
         print(json.dumps({"convergence_study": convergence_study(args.convergence_study, args.steps)}), flush=True)
+        return
+    if args.solve_study:
+        print(json.dumps({"solve_study": solve_study()}), flush=True)
         return
     if args.covariance_study > 0:
         print(json.dumps({"covariance_study": covariance_study(args.covariance_study)}), flush=True)

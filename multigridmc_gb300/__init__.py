@@ -418,6 +418,16 @@ class MultigridMCSampler:
                                           C.byref(it), C.byref(rn), C.byref(cv)))
         return x, it.value, rn.value, bool(cv.value)
 
+    def solve_device(self, b_ptr, x_ptr, rtol=1e-10, atol=1e-10, maxiter=100):
+        """solve() on device vectors given as addresses of n float64 values
+        (the solution is written to x_ptr); returns (niter, residual norm,
+        converged)."""
+        it, rn, cv = C.c_int(0), C.c_double(0.0), C.c_int(0)
+        _check(self._L.mgmc_sampler_solve(self._h, C.cast(C.c_void_p(b_ptr), _D), C.cast(C.c_void_p(x_ptr), _D),
+                                          float(rtol), float(atol), int(maxiter), 1, C.byref(it), C.byref(rn),
+                                          C.byref(cv)))
+        return it.value, rn.value, bool(cv.value)
+
     def step(self, nsteps=1):
         _check(self._L.mgmc_sampler_step(self._h, int(nsteps)))
 
