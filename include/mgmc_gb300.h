@@ -27,6 +27,8 @@
  *   mgmc_measurement_vector  MeasuredOperator::measurement_vector
  *                                                     src/linear_operator/measured_operator.cc:69-171
  *   mgmc_galerkin_stencil    LinearOperator::coarsen  src/linear_operator/linear_operator.cc:10-23
+ *   mgmc_sampler_precondition MultigridPreconditioner::apply src/preconditioner/multigrid_preconditioner.cc:102-108
+ *   mgmc_sampler_solve       LoopSolver::apply        src/solver/loop_solver.cc:9-53
  *
  * Conventions
  *  - Every entry point returns an mgmc_status; none exits, throws or traps
@@ -179,6 +181,24 @@ mgmc_status mgmc_sampler_launches_per_step(mgmc_sampler *s, int64_t *count);
  * pointers.  Gradients with respect to the measurement values y follow
  * through f = B Sigma^{-1} y. */
 mgmc_status mgmc_sampler_adjoint_step(mgmc_sampler *s, double *xbar, double *fbar, int on_device);
+/* Adjoint of one step with respect to the parameters as well (no
+ * counterpart in the reference).  Replays the step from x_in (n values)
+ * with the sampler's fixed right hand side and the step's noise -- the
+ * next mgmc_sampler_noise_per_step() injected values, which it consumes
+ * like a step, or with Philox noise the noise of the step taken when the
+ * step counter was step_index (0 for the first step after creation) --
+ * records its intermediate states, and then, as mgmc_sampler_adjoint_step,
+ * turns xbar into the adjoint of x_in and adds K^T xbar to fbar.  It also
+ * adds to *g_centre the derivative of xbar^T x_out with respect to the
+ * fine stencil's centre weight (the FD prior's centre weight is
+ * h^d kappa^2 + const, so d/dkappa^2 = h^d d/dcentre; coarse stencils
+ * follow by Galerkin coarsening) and to g_logsigma[k] (m values) the
+ * derivative with respect to log Sigma_k, both with the right hand side
+ * held fixed (f = B Sigma^{-1} y adds -(B^T fbar)_k y_k / Sigma_k).
+ * g_centre and g_logsigma are host pointers; x_in, xbar and fbar follow
+ * on_device.  The chain's state is left unchanged. */
+mgmc_status mgmc_sampler_adjoint_params(mgmc_sampler *s, const double *x_in, int64_t step_index, double *xbar,
+                                        double *fbar, double *g_centre, double *g_logsigma, int on_device);
 
 /* ------------------------------------------------ deterministic solver */
 /* MultigridPreconditioner::apply (src/preconditioner/multigrid_preconditioner.cc:102-108):

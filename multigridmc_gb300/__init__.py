@@ -106,6 +106,7 @@ SIGNATURES = {
     "mgmc_sampler_level_size": (C.c_int, [_P, C.c_int, _I64]),
     "mgmc_sampler_launches_per_step": (C.c_int, [_P, _I64]),
     "mgmc_sampler_adjoint_step": (C.c_int, [_P, _D, _D, C.c_int]),
+    "mgmc_sampler_adjoint_params": (C.c_int, [_P, _D, C.c_int64, _D, _D, _D, _D, C.c_int]),
     "mgmc_sampler_precondition": (C.c_int, [_P, _D, _D, C.c_int]),
     "mgmc_sampler_solve": (C.c_int, [_P, _D, _D, C.c_double, C.c_double, C.c_int, C.c_int,
                                      C.POINTER(C.c_int), _D, C.POINTER(C.c_int)]),
@@ -398,6 +399,22 @@ class MultigridMCSampler:
         assert fbar.dtype == np.float64 and fbar.flags.c_contiguous and fbar.size == self.n
         _check(self._L.mgmc_sampler_adjoint_step(self._h, _dp(xbar), _dp(fbar), 0))
         return xbar
+
+    def adjoint_params(self, x_in, xbar, fbar, step_index=0):
+        """adjoint_step with the parameters: replays the step from x_in (with
+        the step's noise: the next injected values, or the Philox noise of
+        step `step_index`), turns xbar into the adjoint of x_in in place, adds
+        K^T xbar to fbar and returns (d/dcentre, d/dlog Sigma) of xbar^T x_out
+        with the right hand side held fixed.  No counterpart in the
+        reference."""
+        x_in = _f64(x_in)
+        assert xbar.dtype == np.float64 and xbar.flags.c_contiguous and xbar.size == self.n
+        assert fbar.dtype == np.float64 and fbar.flags.c_contiguous and fbar.size == self.n
+        gc = C.c_double(0.0)
+        gs = np.zeros(max(self.op.m, 1))
+        _check(self._L.mgmc_sampler_adjoint_params(self._h, _dp(x_in), int(step_index), _dp(xbar), _dp(fbar),
+                                                   C.byref(gc), _dp(gs), 0))
+        return gc.value, gs[:self.op.m].copy()
 
     def precondition(self, b):
         """x = P b: one noise-free cycle of this hierarchy from zero

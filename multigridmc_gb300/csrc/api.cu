@@ -7,6 +7,7 @@
 // kernel launches on the sampler's stream, captured once into a CUDA graph
 // when the noise comes from the in-kernel Philox generator.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -174,6 +175,39 @@ struct Sampler {
     void make_tile_maps(Level &lv);
     double *adj_m = nullptr;  // m-vector for the adjoint's transposed low-rank solve
     void ensure_adjoint();
+    // parameter adjoint: a replay of one step records the input and output
+    // state of every sweep, the state entering each residual and every
+    // level's right hand side (the tape); the reverse pass then adds each
+    // event's derivative with respect to the fine centre weight and log Sigma
+    enum { EV_SWEEP = 0, EV_RESID = 1, EV_COARSE = 2 };
+    struct TapeEvent {
+        int kind, lev;
+        bool forward;
+        void *xin, *xout, *f;
+        NoiseArgs nzp, nzl;  // point (coarse) and low-rank noise of the event
+    };
+    bool taping = false, param_adj = false;
+    std::vector<TapeEvent> tape;
+    std::vector<std::vector<void *>> tape_pool;  // snapshot buffers per level
+    std::vector<int> tape_next;
+    std::vector<void *> tape_last;  // latest snapshot of the level's state (null once it changed)
+    std::vector<void *> tape_f;     // snapshot of the level's current right hand side
+    std::vector<std::array<double, 27>> pa_E;  // dA_0/ds on every level
+    double *pa_gs = nullptr, *pa_gsig = nullptr;  // gradient accumulators
+    double *pa_part = nullptr;
+    int pa_part_cap = 0;
+    double *pa_Bu = nullptr, *pa_Bv = nullptr, *pa_xi = nullptr, *pa_xic = nullptr, *pa_U = nullptr;
+    void *pa_phi = nullptr, *pa_cv = nullptr, *pa_mu = nullptr;
+    void ensure_param_adjoint();
+    void *tape_snap(int lev, const void *src);
+    void *tape_state(int lev);
+    TapeEvent tape_pop(int kind, int lev, bool forward);
+    template <typename T>
+    void pgrad_sweep(const TapeEvent &ev, const void *u);
+    template <typename T>
+    void pgrad_minus_udav(int lev, const void *u, const void *v);
+    template <typename T>
+    void pgrad_coarse(const TapeEvent &ev);
     void autotune_sweeps();
     template <typename T>
     void adjoint_sample(int lev);
@@ -183,6 +217,7 @@ struct Sampler {
     void smooth(int lev, bool forward, int nsmooth);
     void sample(int lev);
     void ensure_solver();
+    void ensure_solver_buffers();
     void coarse_sample(int lev);
     void resid_restrict(int lev);
     void prolong(int lev, double alpha, void *xc, void *x);
@@ -436,14 +471,21 @@ void Sampler::sor(int lev, bool forward, bool noisy, void *x, void *f, int nspar
     int noise = noisy ? noise_mode : NOISE_NONE;
     NoiseArgs nz = noisy ? noise_args(lev, lv.geo.n) : noise_args(lev, 0);
     if (!noisy) nz.buf = nullptr;
+    void *xin = taping ? tape_state(lev) : nullptr;
     for (int k = 0; k < (noisy ? 1 : nsparse); ++k) launch_sweep(*this, lv, forward, noise, x, f, nz, fp32, exact);
+    NoiseArgs nzl{};
     if (m > 0) {
-        NoiseArgs nzl = noisy ? noise_args(lev, m) : noise_args(lev, 0);
+        nzl = noisy ? noise_args(lev, m) : noise_args(lev, 0);
         if (!noisy) nzl.buf = nullptr;
         if (fp32)
             launch_lowrank<float>(*this, lv, forward ? 0 : 1, noise, (float *)x, nzl);
         else
             launch_lowrank<double>(*this, lv, forward ? 0 : 1, noise, (double *)x, nzl);
+    }
+    if (taping) {
+        void *xout = tape_snap(lev, x);
+        tape_last[lev] = xout;
+        tape.push_back(TapeEvent{EV_SWEEP, lev, forward, xin, xout, tape_f[lev], nz, nzl});
     }
     if (noisy) inv++;
 }
@@ -484,15 +526,16 @@ static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void
     S.launches++;
 }
 
+// y = B^T x on the level (into the level's y unless `y` is given)
 template <typename T>
-static void launch_bt_plain(Sampler &S, Level &lv, const void *x) {
+static void launch_bt_plain(Sampler &S, Level &lv, const void *x, double *y = nullptr) {
     LowRankArg lr{};
     lr.m = S.m;
     lr.Bptr = lv.Bptr;
     lr.Bidx = lv.Bidx;
     lr.Bval = lv.Bval;
     lr.Bvalf = lv.Bvalf;
-    lr.y = lv.y;
+    lr.y = y ? y : lv.y;
     lr.part = lv.part;
     lr.counter = lv.counter;
     NoiseArgs nz{};
@@ -514,6 +557,7 @@ static void launch_add_Bq(Sampler &S, Level &lv, void *dst, const double *y, dou
 // next level (:126): R (f - A_0 x) - B_c Sigma^{-1} B^T x.
 void Sampler::resid_restrict(int lev) {
     Level &lv = L[lev], &lc = L[lev + 1];
+    if (taping) tape.push_back(TapeEvent{EV_RESID, lev, true, tape_state(lev), nullptr, nullptr, NoiseArgs{}, NoiseArgs{}});
     if (fp32) {
         launch_resid_restrict<float>(*this, lev, lv.x, lv.f, lc.f, lc.x, false);
         if (m > 0) {
@@ -527,10 +571,15 @@ void Sampler::resid_restrict(int lev) {
             launch_add_Bq<double>(*this, lc, lc.f, lv.y, -1.0);
         }
     }
+    if (taping) {
+        tape_last[lev + 1] = nullptr;  // the coarse state starts from zero
+        tape_f[lev + 1] = tape_snap(lev + 1, lc.f);
+    }
 }
 
 void Sampler::prolong(int lev, double alpha, void *xc, void *x) {
     Level &lv = L[lev], &lc = L[lev + 1];
+    if (taping) tape_last[lev] = nullptr;
     dim3 grid((lc.g.N0 + 1 + 127) / 128, dim > 1 ? lc.g.N1 + 1 : 1, dim > 2 ? lc.g.N2 + 1 : 1);
     if (fp32)
         plaunch(pdl && lv.g.pdl, k_prolong_add<float>, grid, 128, 0, stream, (float *)x, (const float *)xc, lv.g, lc.g, (float)alpha, dim);
@@ -576,6 +625,10 @@ void Sampler::coarse_sample(int lev) {
     }
     if (chol) {
         NoiseArgs nz = noise_args(lev, lv.geo.n);
+        if (taping) {
+            tape.push_back(TapeEvent{EV_COARSE, lev, true, nullptr, nullptr, tape_f[lev], nz, NoiseArgs{}});
+            tape_last[lev] = nullptr;
+        }
         if (fp32) {
             if (noise_mode == NOISE_PHILOX)
                 launch_chol<float, NOISE_PHILOX>(*this, lv, nz);
@@ -1215,9 +1268,7 @@ static void run_steps(Sampler &S, i64 nsteps) {
 // coarse solve.  Two graphs: the FP64 residual r = b - A x with |r|^2 (and
 // the preconditioner's input f_0 = r, x_0 = 0), and the cycle followed by
 // x += P r.
-void Sampler::ensure_solver() {
-    if (rexec && pexec) return;
-    if (!dLinv) build_coarse();
+void Sampler::ensure_solver_buffers() {
     Level &l0 = L[0];
     const i64 na = l0.geo.nalloc;
     if (!sv_x) {
@@ -1232,6 +1283,14 @@ void Sampler::ensure_solver() {
         sv_keep_x = talloc(na);
         sv_keep_f = talloc(na);
     }
+}
+
+void Sampler::ensure_solver() {
+    if (rexec && pexec) return;
+    if (!dLinv) build_coarse();
+    ensure_solver_buffers();
+    Level &l0 = L[0];
+    const i64 na = l0.geo.nalloc;
     auto capture = [&](cudaGraph_t &g, cudaGraphExec_t &ge, const std::function<void()> &body) {
         CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         try {
@@ -1353,6 +1412,7 @@ static void adjoint_sor(Sampler &S, int lev, bool forward) {
         launch_add_Bq<T>(S, lv, a, S.adj_m, -1.0);  // a -= B S^{-T} y
     }
     adj_msolve<T>(S, lev, forward, a, u);  // u = M^{-T} a
+    if (S.param_adj) S.pgrad_sweep<T>(S.tape_pop(Sampler::EV_SWEEP, lev, forward), u);
     adj_axpy<T>(S, lv, b, u, 1.0);        // f-bar += u
     adj_apply_a0<T>(S, lv, u, w);
     adj_axpy<T>(S, lv, a, w, -1.0);       // a -= A_0 u
@@ -1376,6 +1436,7 @@ void Sampler::adjoint_sample(int lev) {
             adj_zero<T>(*this, lv, lv.adj[2]);
             plaunch(false, k_chol_gemv_upper<T, T>, blocks, 256, chol_smem, stream, (const T *)dgv, lv.g, (const T *)dLinvT,
                     chol_ld, (T *)lv.adj[2]);
+            if (param_adj) pgrad_coarse<T>(tape_pop(EV_COARSE, lev, true));
             adj_axpy<T>(*this, lv, lv.adj[1], lv.adj[2], 1.0);
         } else {
             for (int k = P.ncoarsesmooth - 1; k >= 0; --k) {
@@ -1408,6 +1469,7 @@ void Sampler::adjoint_sample(int lev) {
         void *t = lv.adj[2], *u = lv.adj[3];
         adj_zero<T>(*this, lv, t);
         prolong(lev, 1.0, lc.adj[1], t);
+        if (param_adj) pgrad_minus_udav<T>(lev, t, tape_pop(EV_RESID, lev, true).xin);
         adj_axpy<T>(*this, lv, lv.adj[1], t, 1.0);
         adj_apply_a0<T>(*this, lv, t, u);
         if (m > 0) {
@@ -1426,6 +1488,164 @@ void Sampler::adjoint_sample(int lev) {
     }
 }
 
+
+// ------------------------------------------------------ parameter adjoint
+void *Sampler::tape_snap(int lev, const void *src) {
+    auto &pool = tape_pool[lev];
+    int &k = tape_next[lev];
+    if (k == (int)pool.size()) pool.push_back(talloc(L[lev].geo.nalloc));
+    void *dst = pool[k++];
+    CK(cudaMemcpyAsync(dst, src, (size_t)L[lev].geo.nalloc * tsize(), cudaMemcpyDeviceToDevice, stream));
+    return dst;
+}
+
+void *Sampler::tape_state(int lev) {
+    if (!tape_last[lev]) tape_last[lev] = tape_snap(lev, L[lev].x);
+    return tape_last[lev];
+}
+
+Sampler::TapeEvent Sampler::tape_pop(int kind, int lev, bool forward) {
+    if (tape.empty()) fail(MGMC_ERR_INVALID_ARGUMENT, "parameter adjoint: tape exhausted");
+    TapeEvent ev = tape.back();
+    if (ev.kind != kind || ev.lev != lev || (kind == EV_SWEEP && ev.forward != forward))
+        fail(MGMC_ERR_INVALID_ARGUMENT, "parameter adjoint: tape out of order");
+    tape.pop_back();
+    return ev;
+}
+
+// dA_0/ds per level (the Galerkin stencils of the unit centre weight), the
+// gradient accumulators, and for the Cholesky coarse level
+// Phi(L^{-1} E_c L^{-T}) and L^{-1} B_c.
+void Sampler::ensure_param_adjoint() {
+    ensure_adjoint();
+    if (pa_gs) return;
+    const int nl = (int)L.size();
+    pa_E.assign(nl, std::array<double, 27>{});
+    pa_E[0][13] = 1.0;
+    for (int l = 1; l < nl; ++l) galerkin_stencil(dim, pa_E[l - 1].data(), pa_E[l].data());
+    tape_pool.assign(nl, {});
+    tape_next.assign(nl, 0);
+    tape_last.assign(nl, nullptr);
+    tape_f.assign(nl, nullptr);
+    const i64 np0 = ((i64)L[0].g.N1 * L[0].g.N2 + SOLVE_ROWS - 1) / SOLVE_ROWS;
+    i64 cap = 8 * np0;
+    const int mm = std::max(m, 1);
+    pa_Bu = alloc<double>(mm);
+    pa_Bv = alloc<double>(mm);
+    pa_xi = alloc<double>(mm);
+    for (double *p : {pa_Bu, pa_Bv, pa_xi}) CK(cudaMemsetAsync(p, 0, mm * sizeof(double), stream));
+    if (chol) {
+        Level &lv = L.back();
+        const i64 n = lv.geo.n, ld = chol_ld;
+        cap = std::max<i64>(cap, (n + 7) / 8);
+        std::vector<double> Q = dense_precision(lv.geo, lv.st, lv.Bh, Sigma);
+        if (!dense_cholesky(Q, n)) fail(MGMC_ERR_NOT_SPD, "coarse precision matrix is not positive definite");
+        const std::vector<double> Tt = inverse_factor_transposed(Q, n);
+        const std::vector<double> phi = cholesky_phi_sandwich(Tt, lv.geo, pa_E.back().data());
+        if (fp32) {
+            std::vector<float> M((size_t)n * ld, 0.0f);
+            for (i64 i = 0; i < n; ++i)
+                for (i64 j = 0; j <= i; ++j) M[(size_t)i * ld + j] = (float)phi[(size_t)i * n + j];
+            pa_phi = upload(M);
+        } else {
+            std::vector<double> M((size_t)n * ld, 0.0);
+            for (i64 i = 0; i < n; ++i)
+                for (i64 j = 0; j <= i; ++j) M[(size_t)i * ld + j] = phi[(size_t)i * n + j];
+            pa_phi = upload(M);
+        }
+        if (m > 0) pa_U = upload(inverse_factor_times(Tt, n, lv.Bh));
+        pa_xic = alloc<double>(n);
+        pa_cv = alloc<char>((size_t)ld * tsize());
+        pa_mu = talloc(lv.geo.nalloc);
+        if (chol_smem > 48 * 1024) {
+            raise_smem_limit(k_pgrad_coarse_phi<float>, chol_smem);
+            raise_smem_limit(k_pgrad_coarse_phi<double>, chol_smem);
+        }
+    }
+    pa_part = alloc<double>(cap);
+    pa_part_cap = (int)cap;
+    pa_gs = alloc<double>(1);
+    pa_gsig = alloc<double>(mm);
+    CK(cudaStreamSynchronize(stream));
+}
+
+// One sweep's contribution: u = M_f^{-T} x-bar'' of the sweep, its input
+// and output states and right hand side from the tape.
+template <typename T>
+void Sampler::pgrad_sweep(const TapeEvent &ev, const void *u) {
+    Level &lv = L[ev.lev];
+    PgradStencils st;
+    for (int k = 0; k < 27; ++k) {
+        st.a[k] = lv.st[k];
+        st.e[k] = pa_E[ev.lev][k];
+    }
+    const int ncol = P.ordering == MGMC_ORDER_LEXICOGRAPHIC ? 0 : lv.ncol;
+    const int np = (int)(((i64)lv.g.N1 * lv.g.N2 + SOLVE_ROWS - 1) / SOLVE_ROWS);
+    k_pgrad_stencil<T><<<np, 256, 0, stream>>>((const T *)u, (const T *)ev.xout, (const T *)ev.xin, (const T *)ev.f, lv.g,
+                                               st, ncol, ev.forward ? 1 : 0, pa_part);
+    if (m > 0) {
+        launch_bt_plain<T>(*this, lv, u, pa_Bu);
+        launch_bt_plain<T>(*this, lv, ev.xout, pa_Bv);
+        if (noise_mode == NOISE_PHILOX)
+            k_lowrank_normals<NOISE_PHILOX><<<nblk(m, 256), 256, 0, stream>>>(ev.nzl, m, pa_xi);
+        else
+            k_lowrank_normals<NOISE_INJECTED><<<nblk(m, 256), 256, 0, stream>>>(ev.nzl, m, pa_xi);
+    }
+    const double ac = lv.diag, ec = pa_E[ev.lev][13];
+    const PgradCoef cf{ec / (2.0 * ac), P.omega, ac, ec, 0};
+    k_pgrad_combine<<<1, 256, 0, stream>>>(pa_part, np, pa_Bu, pa_Bv, pa_xi, d_sigma_inv, d_sigma_sqrt, m, cf, pa_gs,
+                                           pa_gsig);
+    check_launch();
+}
+
+// -u^T dA v on level lev: the residual f - A x (u = P f_c-bar, v = the
+// state entering the residual) and the coarse mean Q^{-1} f (u = Q^{-1}
+// x-bar, v = Q^{-1} f).
+template <typename T>
+void Sampler::pgrad_minus_udav(int lev, const void *u, const void *v) {
+    Level &lv = L[lev];
+    PgradStencils st;
+    for (int k = 0; k < 27; ++k) {
+        st.a[k] = lv.st[k];
+        st.e[k] = pa_E[lev][k];
+    }
+    const int np = (int)(((i64)lv.g.N1 * lv.g.N2 + SOLVE_ROWS - 1) / SOLVE_ROWS);
+    k_pgrad_stencil<T><<<np, 256, 0, stream>>>((const T *)u, (const T *)v, (const T *)v, (const T *)v, lv.g, st, 0, 1,
+                                               pa_part);
+    if (m > 0) {
+        launch_bt_plain<T>(*this, lv, u, pa_Bu);
+        launch_bt_plain<T>(*this, lv, v, pa_Bv);
+    }
+    const PgradCoef cf{0.0, P.omega, lv.diag, pa_E[lev][13], 1};
+    k_pgrad_combine<<<1, 256, 0, stream>>>(pa_part, np, pa_Bu, pa_Bv, pa_xi, d_sigma_inv, d_sigma_sqrt, m, cf, pa_gs,
+                                           pa_gsig);
+    check_launch();
+}
+
+// The coarse Cholesky sample's contribution; on entry the level's adj[2]
+// holds w1 = Q^{-1} x-bar and dgv holds w2 = L^{-1} x-bar.
+template <typename T>
+void Sampler::pgrad_coarse(const TapeEvent &ev) {
+    typedef T MT;
+    Level &lv = L[ev.lev];
+    const i64 n = lv.geo.n;
+    const unsigned blocks = (unsigned)((n + 7) / 8);
+    if (noise_mode == NOISE_PHILOX)
+        k_coarse_normals<NOISE_PHILOX><<<nblk(n, 256), 256, 0, stream>>>(ev.nzp, (int)n, pa_xic);
+    else
+        k_coarse_normals<NOISE_INJECTED><<<nblk(n, 256), 256, 0, stream>>>(ev.nzp, (int)n, pa_xic);
+    k_pgrad_coarse_phi<MT><<<blocks, 256, chol_smem, stream>>>((const MT *)pa_phi, chol_ld, (const MT *)dgv, pa_xic, (int)n,
+                                                               pa_part);
+    k_accum_sum<<<1, 256, 0, stream>>>(pa_part, (int)blocks, -1.0, pa_gs);
+    if (m > 0)
+        k_pgrad_coarse_sigma<MT><<<m, 256, 0, stream>>>(pa_U, (const MT *)dgv, pa_xic, d_sigma_inv, pa_gsig, (int)n);
+    NoiseArgs nz{};
+    plaunch(false, k_chol_gemv_lower<T, MT, NOISE_NONE>, blocks, 256, chol_smem, stream, (const T *)ev.f, lv.g,
+            (const MT *)dLinv, chol_ld, (MT *)pa_cv, nz);
+    plaunch(false, k_chol_gemv_upper<T, MT>, blocks, 256, chol_smem, stream, (const MT *)pa_cv, lv.g, (const MT *)dLinvT,
+            chol_ld, (T *)pa_mu);
+    pgrad_minus_udav<T>(ev.lev, lv.adj[2], pa_mu);
+}
 }  // namespace mgmc
 
 // ===================================================================== ABI
@@ -2007,6 +2227,30 @@ mgmc_status mgmc_sampler_solve(mgmc_sampler *s, const double *b, double *x, doub
     API_END
 }
 
+// x-bar out of level 0's adj[0], and f-bar += level 0's adj[1]
+static void adjoint_outputs(Sampler &S, double *xbar, double *fbar, int on_device) {
+    Level &l0 = S.L[0];
+    get_vec(S, 0, l0.adj[0], xbar, on_device);
+    const i64 n = l0.geo.n;
+    double *d = S.d_cvec;
+    if (S.fp32)
+        k_pack<float><<<pack_grid(l0), 256, 0, S.stream>>>((const float *)l0.adj[1], d, l0.g);
+    else
+        k_pack<double><<<pack_grid(l0), 256, 0, S.stream>>>((const double *)l0.adj[1], d, l0.g);
+    S.check_launch();
+    if (on_device) {
+        const unsigned blocks = (unsigned)std::min<i64>(nblk(n, 256), 8 * S.nsm);
+        k_axpy<double><<<blocks, 256, 0, S.stream>>>(fbar, d, 1.0, n);
+        S.check_launch();
+    } else {
+        std::vector<double> h(n);
+        CK(cudaMemcpyAsync(h.data(), d, n * sizeof(double), cudaMemcpyDeviceToHost, S.stream));
+        CK(cudaStreamSynchronize(S.stream));
+        for (i64 i = 0; i < n; ++i) fbar[i] += h[i];
+    }
+    CK(cudaStreamSynchronize(S.stream));
+}
+
 mgmc_status mgmc_sampler_adjoint_step(mgmc_sampler *s, double *xbar, double *fbar, int on_device) {
     API_BEGIN
     Sampler &S = impl(s);
@@ -2023,28 +2267,81 @@ mgmc_status mgmc_sampler_adjoint_step(mgmc_sampler *s, double *xbar, double *fba
         S.adjoint_sample<double>(0);
     }
     S.check_launch();
-    // f-bar is accumulated: add this step's part through a device compact copy
-    get_vec(S, 0, l0.adj[0], xbar, on_device);
-    {
-        const i64 n = l0.geo.n;
-        double *d = S.d_cvec;
-        if (S.fp32)
-            k_pack<float><<<pack_grid(l0), 256, 0, S.stream>>>((const float *)l0.adj[1], d, l0.g);
-        else
-            k_pack<double><<<pack_grid(l0), 256, 0, S.stream>>>((const double *)l0.adj[1], d, l0.g);
-        S.check_launch();
-        std::vector<double> h;
-        if (on_device) {
-            const unsigned blocks = (unsigned)std::min<i64>(nblk(n, 256), 8 * S.nsm);
-            k_axpy<double><<<blocks, 256, 0, S.stream>>>(fbar, d, 1.0, n);
-            S.check_launch();
-        } else {
-            h.resize(n);
-            CK(cudaMemcpyAsync(h.data(), d, n * sizeof(double), cudaMemcpyDeviceToHost, S.stream));
-            CK(cudaStreamSynchronize(S.stream));
-            for (i64 i = 0; i < n; ++i) fbar[i] += h[i];
-        }
-    }
+    adjoint_outputs(S, xbar, fbar, on_device);
+    API_END
+}
+
+mgmc_status mgmc_sampler_adjoint_params(mgmc_sampler *s, const double *x_in, int64_t step_index, double *xbar,
+                                        double *fbar, double *g_centre, double *g_logsigma, int on_device) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!x_in || !xbar || !fbar || !g_centre || (S.m > 0 && !g_logsigma)) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    if (step_index < 0) fail(MGMC_ERR_INVALID_ARGUMENT, "step_index < 0");
     CK(cudaStreamSynchronize(S.stream));
+    if (S.noise_mode == NOISE_INJECTED && S.noise_len - S.noise_pos < S.noise_per_step)
+        fail(MGMC_ERR_NOISE_EXHAUSTED, "injected noise exhausted: " + std::to_string(S.noise_len - S.noise_pos) + " queued, " +
+                                           std::to_string(S.noise_per_step) + " needed per step");
+    S.ensure_solver_buffers();
+    S.ensure_param_adjoint();
+    Level &l0 = S.L[0];
+    const int mm = std::max(S.m, 1);
+    double gs = 0.0;
+    std::vector<double> gsig(mm, 0.0);
+    u64 saved_step = 0;
+    CK(cudaMemcpy(&saved_step, S.d_step, sizeof(u64), cudaMemcpyDeviceToHost));
+    struct Restore {
+        Sampler &S;
+        u64 step;
+        ~Restore() {
+            S.taping = false;
+            S.param_adj = false;
+            S.noisy = true;
+            S.tape.clear();
+            cudaMemcpyAsync(S.d_step, &step, sizeof(u64), cudaMemcpyHostToDevice, S.stream);
+            cudaStreamSynchronize(S.stream);
+        }
+    };
+    {
+        BorrowLevel0 borrow(S);
+        Restore restore{S, saved_step};
+        put_vec(S, 0, x_in, on_device, l0.x);
+        const u64 k = (u64)step_index;
+        CK(cudaMemcpyAsync(S.d_step, &k, sizeof(u64), cudaMemcpyHostToDevice, S.stream));
+        // replay the step, recording the tape (the noise of step step_index,
+        // or the next injected noise)
+        S.tape.clear();
+        std::fill(S.tape_next.begin(), S.tape_next.end(), 0);
+        std::fill(S.tape_last.begin(), S.tape_last.end(), nullptr);
+        std::fill(S.tape_f.begin(), S.tape_f.end(), nullptr);
+        S.tape_f[0] = l0.f;
+        S.inv = 0;
+        S.noise_off = S.noise_pos;
+        S.taping = true;
+        S.sample(0);
+        S.taping = false;
+        S.check_launch();
+        // reverse pass
+        put_vec(S, 0, xbar, on_device, l0.adj[0]);
+        CK(cudaMemsetAsync(S.pa_gs, 0, sizeof(double), S.stream));
+        CK(cudaMemsetAsync(S.pa_gsig, 0, mm * sizeof(double), S.stream));
+        S.param_adj = true;
+        if (S.fp32) {
+            adj_zero<float>(S, l0, l0.adj[1]);
+            S.adjoint_sample<float>(0);
+        } else {
+            adj_zero<double>(S, l0, l0.adj[1]);
+            S.adjoint_sample<double>(0);
+        }
+        S.param_adj = false;
+        S.check_launch();
+        if (!S.tape.empty()) fail(MGMC_ERR_INVALID_ARGUMENT, "parameter adjoint: tape not consumed");
+        adjoint_outputs(S, xbar, fbar, on_device);
+        CK(cudaMemcpy(&gs, S.pa_gs, sizeof(double), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(gsig.data(), S.pa_gsig, mm * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    if (S.noise_mode == NOISE_INJECTED) S.noise_pos += S.noise_per_step;
+    check_device_errors(S);
+    *g_centre += gs;
+    for (int k = 0; k < S.m; ++k) g_logsigma[k] += gsig[k];
     API_END
 }

@@ -25,8 +25,10 @@
 //   k_step_end          observables z = b^T x, step counter
 // Host conversions: k_unpack / k_unpack2 / k_pack; adjoint helpers: k_axpy,
 // k_sinvt_q; deterministic solver (FP64 loop around the noise-free cycle):
-// k_solve_resid, k_solve_rhs, k_solve_norm, k_solve_update; building
-// blocks: k_apply_stencil.
+// k_solve_resid, k_solve_rhs, k_solve_norm, k_solve_update; parameter
+// adjoint: k_pgrad_stencil, k_pgrad_combine, k_lowrank_normals,
+// k_coarse_normals, k_pgrad_coarse_phi, k_pgrad_coarse_sigma, k_accum_sum;
+// building blocks: k_apply_stencil.
 #pragma once
 
 #include <cstdint>
@@ -1253,6 +1255,264 @@ __global__ void __launch_bounds__(256) k_solve_norm(const double *__restrict__ p
 template <typename T>
 __global__ void __launch_bounds__(256) k_solve_update(double *__restrict__ x, const T *__restrict__ dx, i64 n) {
     for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) x[i] += (double)dx[i];
+}
+
+// ------------------------------------------------ parameter adjoint
+// Derivatives of one step (noise fixed) with respect to the fine stencil's
+// centre weight s (for the FD prior, s = h^d kappa^2 + const, so
+// d/dkappa^2 = h^d d/ds) and to log Sigma_k.  A sweep is
+// x'' = x + M_f^{-1}(c - A x) with M_f = M + B Sigma^{-1} B^T,
+// M = D / omega + (A_0's part before the point in the sweep order) and
+// c = f + sd xi + B Sigma^{-1/2} xi'; with u = M_f^{-T} x-bar'' it adds
+//   u^T dc - u^T dN x - u^T dM_f x''   (N = A_0 - M)
+// to the gradient.  dA_0/ds on level l is the Galerkin stencil E_l of the
+// unit centre weight; the noise part c - f = M x'' + N x + B Sigma^{-1} B^T x''
+// - f is rebuilt from the sweep's input and output states, so the point
+// normals need not be stored.
+struct PgradStencils {
+    double a[27];  // the level's A_0
+    double e[27];  // E_l = dA_0 / ds
+};
+
+// Colour of interior point (a, b, c) in the multicolour order (2 colours:
+// parity of a + b + c; 2^dim colours: one parity bit per direction).
+__device__ __forceinline__ int point_colour(int ncol, int a, int b, int c) {
+    return ncol == 2 ? ((a + b + c) & 1) : ((a & 1) | ((b & 1) << 1) | ((c & 1) << 2));
+}
+
+// Per CTA of SOLVE_ROWS rows, the eight sums over the level's points p
+// (part[8 * blockIdx.x + j]):
+//   0: u_p sum_{q before p} A_pq v_q    1: u_p sum_{q after p} A_pq w_q
+//   2: u_p sum_{q before p} E_pq v_q    3: u_p sum_{q before p} E_pq w_q
+//   4: u_p sum_{q after p} E_pq w_q     5: u_p v_p   6: u_p w_p   7: u_p f_p
+// (v = the sweep's output, w = its input; off-diagonal neighbours only).
+// "Before" is the order of the sweep of direction `forward`: by linear
+// index for the lexicographic order (ncol = 0), by colour otherwise.
+template <typename T>
+__global__ void __launch_bounds__(256) k_pgrad_stencil(const T *__restrict__ u, const T *__restrict__ v,
+                                                       const T *__restrict__ w, const T *__restrict__ f, Grid3 g,
+                                                       PgradStencils st, int ncol, int forward,
+                                                       double *__restrict__ part) {
+    __shared__ double sh[32];
+    const i64 nrows = (i64)g.N1 * g.N2;
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int q = 0; q < SOLVE_ROWS; ++q) {
+        const i64 row = (i64)blockIdx.x * SOLVE_ROWS + q;
+        if (row >= nrows) break;
+        const int bb = (int)(row % g.N1), c = (int)(row / g.N1);
+        for (int a = threadIdx.x; a < g.N0; a += blockDim.x) {
+            const i64 P = g.pad(a, bb, c);
+            const double up = (double)u[P];
+            if (up == 0.0) continue;
+            const int cp = ncol ? point_colour(ncol, a, bb, c) : 0;
+            double lav = 0, uaw = 0, lev = 0, lew = 0, uew = 0;
+            for (int dz = -1; dz <= 1; ++dz)
+                for (int dy = -1; dy <= 1; ++dy)
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        const int k = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1);
+                        if (k == 13) continue;
+                        const double wa = st.a[k], we = st.e[k];
+                        if (wa == 0.0 && we == 0.0) continue;
+                        bool before;
+                        if (ncol == 0) {
+                            const bool lower = dz < 0 || (dz == 0 && (dy < 0 || (dy == 0 && dx < 0)));
+                            before = forward ? lower : !lower;
+                        } else {
+                            const int cq = point_colour(ncol, a + dx, bb + dy, c + dz);
+                            before = forward ? cq < cp : cq > cp;
+                        }
+                        const i64 Q = P + dz * g.sz + dy * g.sy + dx;
+                        if (before) {
+                            const double vq = (double)v[Q], wq = (double)w[Q];
+                            lav += wa * vq;
+                            lev += we * vq;
+                            lew += we * wq;
+                        } else {
+                            const double wq = (double)w[Q];
+                            uaw += wa * wq;
+                            uew += we * wq;
+                        }
+                    }
+            acc[0] += up * lav;
+            acc[1] += up * uaw;
+            acc[2] += up * lev;
+            acc[3] += up * lew;
+            acc[4] += up * uew;
+            acc[5] += up * (double)v[P];
+            acc[6] += up * (double)w[P];
+            acc[7] += up * (double)f[P];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const double t = block_sum<256>(acc[j], sh);
+        if (threadIdx.x == 0) part[8 * (i64)blockIdx.x + j] = t;
+        __syncthreads();
+    }
+}
+
+// Adds one event's contribution to the gradients (one CTA).  Sums the eight
+// partial streams of k_pgrad_stencil into S0..S7 and, with Bu = B^T u,
+// Bv = B^T v and the low-rank normals xi' of the sweep:
+// sweep (mode 0), kd = dsd/ds / sd = E_c / (2 A_c):
+//   g_s += kd [S0 + A_c/omega S5 + S1 + A_c (1 - 1/omega) S6 - S7
+//              + sum_k Bu_k Bv_k / Sigma_k - sum_k Bu_k xi'_k / Sigma_k^{1/2}]
+//          - [S2 + S4 + E_c S6 + E_c/omega (S5 - S6)]
+//   g_k += Bu_k (Bv_k / Sigma_k - xi'_k / (2 Sigma_k^{1/2}))
+// -u^T dA v with v = w (mode 1: the residual f - A x with u = P f_c-bar,
+// and the coarse mean Q^{-1} f with u = Q^{-1} x-bar):
+//   g_s -= S3 + S4 + E_c S6;   g_k += Bu_k Bv_k / Sigma_k
+struct PgradCoef {
+    double kd, omega, ac, ec;
+    int mode;
+};
+__global__ void __launch_bounds__(256) k_pgrad_combine(const double *__restrict__ part, int np,
+                                                       const double *__restrict__ Bu, const double *__restrict__ Bv,
+                                                       const double *__restrict__ xi,
+                                                       const double *__restrict__ sigma_inv,
+                                                       const double *__restrict__ sigma_sqrt, int m, PgradCoef cf,
+                                                       double *__restrict__ g_s, double *__restrict__ g_sig) {
+    __shared__ double sh[32];
+    double S[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        double a = 0.0;
+        for (int i = threadIdx.x; i < np; i += blockDim.x) a += part[8 * (i64)i + j];
+        S[j] = block_sum<256>(a, sh);
+        __syncthreads();
+    }
+    double q1 = 0.0, q2 = 0.0;
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        q1 += Bu[k] * Bv[k] * sigma_inv[k];
+        if (cf.mode == 0) q2 += Bu[k] * xi[k] / sigma_sqrt[k];
+        g_sig[k] += cf.mode == 0 ? Bu[k] * (Bv[k] * sigma_inv[k] - 0.5 * xi[k] / sigma_sqrt[k])
+                                 : Bu[k] * Bv[k] * sigma_inv[k];
+    }
+    q1 = block_sum<256>(q1, sh);
+    __syncthreads();
+    q2 = block_sum<256>(q2, sh);
+    if (threadIdx.x == 0) {
+        double c;
+        if (cf.mode == 0)
+            c = cf.kd * (S[0] + cf.ac / cf.omega * S[5] + S[1] + cf.ac * (1.0 - 1.0 / cf.omega) * S[6] - S[7] + q1 - q2) -
+                (S[2] + S[4] + cf.ec * S[6] + cf.ec / cf.omega * (S[5] - S[6]));
+        else
+            c = -(S[3] + S[4] + cf.ec * S[6]);
+        *g_s += c;
+    }
+}
+
+// The low-rank normals xi'_k of one sweep (as the low-rank kernels draw
+// them), and the n coarse normals of the Cholesky sample, compact.
+template <int NOISE>
+__global__ void __launch_bounds__(256) k_lowrank_normals(NoiseArgs nz, int m, double *__restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    double xi = 0.0;
+    if (NOISE == NOISE_PHILOX) {
+        float4 rn = normals4(philox4x32_10(noise_ctr(nz, (unsigned)(k >> 2), PURPOSE_LOWRANK, 0), noise_key(nz)));
+        xi = (double)pick(rn, k & 3);
+    }
+    if (NOISE == NOISE_INJECTED) xi = nz.buf[k];
+    out[k] = xi;
+}
+
+template <int NOISE>
+__global__ void __launch_bounds__(256) k_coarse_normals(NoiseArgs nz, int n, double *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double xi = 0.0;
+    if (NOISE == NOISE_PHILOX) {
+        float4 r = normals4(philox4x32_10(noise_ctr(nz, (unsigned)(i >> 2), PURPOSE_COARSE, 0), noise_key(nz)));
+        xi = (double)pick(r, i & 3);
+    }
+    if (NOISE == NOISE_INJECTED) xi = nz.buf[i];
+    out[i] = xi;
+}
+
+// The coarse Cholesky sample x = Q^{-1} f + L^{-T} xi, Q = L L^T: with
+// dL = L Phi(L^{-1} dQ L^{-T}), Phi(X) = strict lower part + half the
+// diagonal, x-bar^T dx = -w1^T dQ mu - xi^T Phi(L^{-1} dQ L^{-T}) w2
+// (mu = Q^{-1} f, w1 = Q^{-1} x-bar, w2 = L^{-1} x-bar).
+//
+// s-term: part[blockIdx.x] = sum over its rows i of xi_i (Phi(X_E) w2)_i,
+// X_E = L^{-1} E_c L^{-T} stored like the inverse factor (row-major, ld a
+// multiple of 16 bytes, zeros above the diagonal); one warp per row.
+template <typename MT>
+__global__ void __launch_bounds__(256) k_pgrad_coarse_phi(const MT *__restrict__ Phi, int ld,
+                                                          const MT *__restrict__ w2, const double *__restrict__ xi,
+                                                          int n, double *__restrict__ part) {
+    extern __shared__ __align__(16) unsigned char chol_sm[];
+    __shared__ double sh[32];
+    MT *ws = reinterpret_cast<MT *>(chol_sm);
+    for (int i = threadIdx.x; i < ld; i += blockDim.x) ws[i] = i < n ? w2[i] : MT(0);
+    __syncthreads();
+    constexpr int NV = Vec16<MT>::N;
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    double acc = 0.0;
+    for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+        const MT r = warp_row_dot<MT>(Phi + (i64)i * ld, ws, 0, i / NV + 1, lane);
+        if (lane == 0) acc += xi[i] * (double)r;
+    }
+    acc = block_sum<256>(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// *target += scale * sum(part[0 .. np))
+__global__ void __launch_bounds__(256) k_accum_sum(const double *__restrict__ part, int np, double scale,
+                                                   double *__restrict__ target) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) acc += part[i];
+    acc = block_sum<256>(acc, sh);
+    if (threadIdx.x == 0) *target += scale * acc;
+}
+
+// log Sigma_k term of the coarse sample's L^{-T} xi part (dQ = -b_k b_k^T /
+// Sigma_k, u = L^{-1} b_k, column k of U):
+//   g_k += (1 / Sigma_k) sum_j u_j w2_j (sum_{i > j} u_i xi_i + u_j xi_j / 2).
+// One CTA per k; the suffix sums run over chunks of 256 indices from the
+// end, a block scan inside each chunk.
+template <typename MT>
+__global__ void __launch_bounds__(256) k_pgrad_coarse_sigma(const double *__restrict__ U, const MT *__restrict__ w2,
+                                                            const double *__restrict__ xi,
+                                                            const double *__restrict__ sigma_inv,
+                                                            double *__restrict__ g_sig, int n) {
+    __shared__ double wsum[8];
+    __shared__ double sh[32];
+    __shared__ double carry;
+    const int k = blockIdx.x;
+    const double *u = U + (i64)k * n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0.0;
+    __syncthreads();
+    double acc = 0.0;
+    for (int base = ((n - 1) / 256) * 256; base >= 0; base -= 256) {
+        const int j = base + threadIdx.x;
+        const double uj = j < n ? u[j] : 0.0, xj = j < n ? xi[j] : 0.0, wj = j < n ? (double)w2[j] : 0.0;
+        const double v = uj * xj;
+        double incl = v;  // sum over the lanes at or above this one
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double t = __shfl_down_sync(0xffffffffu, incl, o);
+            if (lane + o < 32) incl += t;
+        }
+        if (lane == 0) wsum[warp] = incl;
+        __syncthreads();
+        double above = 0.0;
+        for (int q = warp + 1; q < 8; ++q) above += wsum[q];
+        acc += wj * uj * (carry + above + (incl - v) + 0.5 * v);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tot = 0.0;
+            for (int q = 0; q < 8; ++q) tot += wsum[q];
+            carry += tot;
+        }
+        __syncthreads();
+    }
+    acc = block_sum<256>(acc, sh);
+    if (threadIdx.x == 0) g_sig[k] += sigma_inv[k] * acc;
 }
 
 // ------------------------------------------------------------ step end

@@ -358,6 +358,56 @@ std::vector<double> inverse_factor_transposed(const std::vector<double> &L, int6
     return T;
 }
 
+std::vector<double> cholesky_phi_sandwich(const std::vector<double> &T, const Geometry &g, const double E[27]) {
+    const int64_t n = g.n;
+    // Y = E L^{-T}: row p of Y sums the rows q of L^{-T} (= rows of T) over
+    // the stencil neighbours q of p
+    std::vector<double> Y((size_t)(n * n), 0.0);
+#pragma omp parallel for schedule(static) if (n > 256)
+    for (int64_t p = 0; p < n; ++p) {
+        const int a = (int)(p % g.N[0]), b = (int)((p / g.N[0]) % g.N[1]), c = (int)(p / ((int64_t)g.N[0] * g.N[1]));
+        double *y = &Y[(size_t)p * n];
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const double w = E[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)];
+                    const int qa = a + dx, qb = b + dy, qc = c + dz;
+                    if (w == 0.0 || qa < 0 || qb < 0 || qc < 0 || qa >= g.N[0] || qb >= g.N[1] || qc >= g.N[2]) continue;
+                    const int64_t q = ((int64_t)qc * g.N[1] + qb) * g.N[0] + qa;
+                    const double *t = &T[(size_t)q * n];
+                    for (int64_t j = q; j < n; ++j) y[j] += w * t[j];  // T row q is zero before column q
+                }
+    }
+    // X = L^{-1} Y on and below the diagonal: X[i][j] = sum_{k <= i} L^{-1}[i][k] Y[k][j]
+    std::vector<double> Phi((size_t)(n * n), 0.0);
+#pragma omp parallel for schedule(dynamic, 8) if (n > 256)
+    for (int64_t i = 0; i < n; ++i) {
+        double *x = &Phi[(size_t)i * n];
+        for (int64_t k = 0; k <= i; ++k) {
+            const double l = T[(size_t)k * n + i];  // L^{-1}[i][k]
+            if (l == 0.0) continue;
+            const double *y = &Y[(size_t)k * n];
+            for (int64_t j = 0; j <= i; ++j) x[j] += l * y[j];
+        }
+        x[i] *= 0.5;
+    }
+    return Phi;
+}
+
+std::vector<double> inverse_factor_times(const std::vector<double> &T, int64_t n, const SparseCols &B) {
+    std::vector<double> U((size_t)n * B.m, 0.0);
+    for (int k = 0; k < B.m; ++k) {
+        double *u = &U[(size_t)k * n];
+        for (int64_t e = B.ptr[k]; e < B.ptr[k + 1]; ++e) {
+            const int64_t l = B.row[e];
+            const double v = B.val[e];
+            const double *t = &T[(size_t)l * n];
+            for (int64_t i = l; i < n; ++i) u[i] += v * t[i];  // L^{-1}[i][l] = T[l][i], zero for i < l
+        }
+    }
+    return U;
+}
+
 std::vector<double> small_inverse(const std::vector<double> &S, int m) {
     std::vector<double> LU = S, inv((size_t)m * m, 0.0);
     std::vector<int> piv(m);

@@ -66,6 +66,14 @@ std::vector<double> dense_precision(const Geometry &g, const double st[27], cons
 bool dense_cholesky(std::vector<double> &Q, int64_t n);
 // L^{-1} of a lower-triangular row-major factor; returns (L^{-1})^T row-major
 std::vector<double> inverse_factor_transposed(const std::vector<double> &L, int64_t n);
+// Phi(L^{-1} E L^{-T}) for the constant-stencil matrix E on geometry g
+// (Dirichlet: neighbours outside omitted), from T = (L^{-1})^T row-major:
+// the strict lower part and half the diagonal, row-major n x n, zeros
+// above the diagonal (the derivative of the Cholesky factor in direction E
+// is L Phi(L^{-1} E L^{-T}))
+std::vector<double> cholesky_phi_sandwich(const std::vector<double> &T, const Geometry &g, const double E[27]);
+// L^{-1} B from T = (L^{-1})^T: column k (n values) stored at k * n
+std::vector<double> inverse_factor_times(const std::vector<double> &T, int64_t n, const SparseCols &B);
 // inverse of a small dense matrix by LU with partial pivoting
 std::vector<double> small_inverse(const std::vector<double> &S, int m);
 

@@ -161,3 +161,174 @@ def test_checkpointed_autograd_function():
     assert abs(J.item() - ch.J(y.detach().numpy())) <= 1e-12 * abs(J.item())
     ref = ch.grad(y.detach().numpy())
     assert np.allclose(gy.numpy(), ref, rtol=1e-10, atol=1e-14 * np.abs(ref).max())
+
+
+# ------------------------------------------------- parameter derivatives
+class ParamChain:
+    """J(kappa^2, log Sigma, y) = (1/T) sum_t ||x_t on the sub-cube||^2 over
+    T steps from x_0 = 0 with f = B Sigma^{-1} y, for the FD prior with the
+    measurement columns of `locs` (fixed B), injected noise fixed by seed or
+    Philox noise fixed by the sampler seed."""
+
+    def __init__(self, shape, locs, prm, nsteps, kappa_sq=10.0, variance=1e-3, radius=0.1, ordering=M.MULTICOLOUR,
+                 precision=M.FP64, noise=M.INJECTED, seed=11):
+        self.shape, self.prm, self.T = tuple(shape), prm, nsteps
+        self.ordering, self.precision, self.noise, self.seed = ordering, precision, noise, seed
+        self.cols = [M.measurement_vector(self.shape, x0, radius) for x0 in locs]
+        self.m = len(self.cols)
+        self.theta0 = (kappa_sq, np.full(self.m, np.log(variance)))
+        self.y = np.random.default_rng(seed + 1).standard_normal(self.m)
+        op = self.op(*self.theta0)
+        self.n = op.n
+        self.B = op.B_dense()
+        self.mask = _subcube_mask(self.shape)
+        self.hd = float(np.prod([1.0 / c for c in self.shape]))
+        s = self.sampler(op)
+        self.nps = s.noise_per_step
+        s.close()
+        self.normals = np.random.default_rng(seed).standard_normal(nsteps * self.nps)
+
+    def op(self, kappa_sq, logsig):
+        return M.LinearOperator.shifted_laplace_fd(self.shape, kappa_sq).with_lowrank(self.cols, np.exp(logsig))
+
+    def sampler(self, op):
+        return M.MultigridMCSampler(op, self.prm, ordering=self.ordering, precision=self.precision, noise=self.noise,
+                                    seed=self.seed)
+
+    def f_of(self, logsig):
+        return self.B @ (self.y / np.exp(logsig))
+
+    def run(self, kappa_sq, logsig):
+        s = self.sampler(self.op(kappa_sq, logsig))
+        f = self.f_of(logsig)
+        x = np.zeros(self.n)
+        xs = [x.copy()]
+        for t in range(self.T):
+            if self.noise == M.INJECTED:
+                s.inject_noise(self.normals[t * self.nps:(t + 1) * self.nps])
+            s.apply(f, x)
+            xs.append(x.copy())
+        return s, f, xs
+
+    def J(self, kappa_sq, logsig):
+        s, _, xs = self.run(kappa_sq, logsig)
+        s.close()
+        return sum(float((self.mask * xt) @ xt) for xt in xs[1:]) / self.T
+
+    def grad(self, kappa_sq, logsig):
+        """(dJ/dkappa^2, dJ/dlog Sigma, dJ/dy) by the parameter adjoint."""
+        s, f, xs = self.run(kappa_sq, logsig)
+        lam = (2.0 / self.T) * self.mask * xs[-1]
+        fbar = np.zeros(self.n)
+        gc, gsig = 0.0, np.zeros(self.m)
+        for t in range(self.T - 1, -1, -1):  # lam = adjoint of x_{t+1}
+            if self.noise == M.INJECTED:
+                s.inject_noise(self.normals[t * self.nps:(t + 1) * self.nps])
+            c, g = s.adjoint_params(xs[t], lam, fbar, step_index=t)
+            gc += c
+            gsig += g
+            if t >= 1:
+                lam += (2.0 / self.T) * self.mask * xs[t]
+        s.close()
+        sig = np.exp(logsig)
+        Btf = self.B.T @ fbar
+        return self.hd * gc, gsig - Btf * self.y / sig, Btf / sig
+
+
+def _check_fd(ch, gk, gs, rel=1e-5, h=1e-6):
+    k2, ls = ch.theta0
+    scale = max(abs(gk), np.abs(gs).max())
+    dk = h * k2
+    fd = (ch.J(k2 + dk, ls) - ch.J(k2 - dk, ls)) / (2 * dk)
+    assert abs(gk - fd) <= rel * max(abs(fd), 1e-3 * abs(gk)), f"d/dkappa^2: adjoint {gk} vs FD {fd}"
+    for k in range(ch.m):
+        e = np.zeros(ch.m)
+        e[k] = h
+        fd = (ch.J(k2, ls + e) - ch.J(k2, ls - e)) / (2 * h)
+        assert abs(gs[k] - fd) <= rel * max(abs(fd), 1e-3 * scale), f"d/dlog Sigma[{k}]: adjoint {gs[k]} vs FD {fd}"
+
+
+_LOCS3 = [(0.3, 0.4, 0.5), (0.6, 0.55, 0.4), (0.45, 0.7, 0.65), (0.5, 0.3, 0.35)]
+PARAM_CASES = [
+    ("3d-16-ssor", (16, 16, 16), _LOCS3, _mg(3), M.MULTICOLOUR),
+    ("3d-16-ssor-lex", (16, 16, 16), _LOCS3[:3], _mg(3), M.LEXICOGRAPHIC),
+    ("3d-16-coarse-ssor", (16, 16, 16), _LOCS3[:2], _mg(3, coarse="SSOR"), M.MULTICOLOUR),
+    ("2d-32-sor-w", (32, 32), [(0.3, 0.6), (0.7, 0.4), (0.5, 0.5)], _mg(3, omega=1.2, cycle=2, smoother="SOR"),
+     M.MULTICOLOUR),
+    ("2d-32-ssor-w-lex", (32, 32), [(0.3, 0.6), (0.7, 0.4)], _mg(3, omega=0.9, cycle=2), M.LEXICOGRAPHIC),
+]
+
+
+@pytest.mark.parametrize("name,shape,locs,prm,ordering", PARAM_CASES, ids=[c[0] for c in PARAM_CASES])
+def test_parameter_gradients_match_finite_differences(name, shape, locs, prm, ordering):
+    """dJ/dkappa^2 and dJ/dlog Sigma_k (with f = B Sigma^{-1} y following
+    Sigma) by the parameter adjoint against central finite differences of
+    the FP64 chain with the same injected noise (step 1e-6 relative),
+    within 1e-5 relative."""
+    ch = ParamChain(shape, locs, prm, nsteps=8, ordering=ordering)
+    gk, gs, _ = ch.grad(*ch.theta0)
+    _check_fd(ch, gk, gs)
+
+
+def test_parameter_gradients_philox_noise():
+    """The same with in-kernel Philox noise: the adjoint replays each step
+    with the noise of its step counter, and the finite differences rebuild
+    the sampler with the same seed."""
+    ch = ParamChain((16, 16, 16), _LOCS3, _mg(3), nsteps=6, noise=M.PHILOX, seed=21)
+    gk, gs, _ = ch.grad(*ch.theta0)
+    _check_fd(ch, gk, gs)
+
+
+def test_measurement_value_gradient_of_parameter_adjoint():
+    """The y-gradient of the parameter adjoint equals the plain adjoint's
+    (the linear part is the same computation)."""
+    ch = ParamChain((16, 16, 16), _LOCS3, _mg(3), nsteps=5)
+    _, _, gy = ch.grad(*ch.theta0)
+    s, f, xs = ch.run(*ch.theta0)
+    lam = (2.0 / ch.T) * ch.mask * xs[-1]
+    fbar = np.zeros(ch.n)
+    for t in range(ch.T - 1, -1, -1):
+        s.adjoint_step(lam, fbar)
+        if t >= 1:
+            lam += (2.0 / ch.T) * ch.mask * xs[t]
+    s.close()
+    ref = (ch.B.T @ fbar) / np.exp(ch.theta0[1])
+    assert np.allclose(gy, ref, rtol=1e-12, atol=1e-14 * np.abs(ref).max())
+
+
+def test_fp32_parameter_gradients_against_fp64():
+    """FP32-mixed parameter gradients against the FP64 ones of the coupled
+    chain (Philox noise, same seed), within 1e-3 relative."""
+    kw = dict(shape=(16, 16, 16), locs=_LOCS3, prm=_mg(3), nsteps=6, noise=M.PHILOX, seed=31)
+    g64 = ParamChain(precision=M.FP64, **kw).grad(*ParamChain(**kw).theta0)
+    c32 = ParamChain(precision=M.FP32_MIXED, **kw)
+    g32 = c32.grad(*c32.theta0)
+    for a, b in zip(g32, g64):
+        a, b = np.atleast_1d(a), np.atleast_1d(b)
+        assert np.linalg.norm(a - b) <= 1e-3 * np.linalg.norm(b)
+
+
+def test_parameter_gradient_against_oracle_chain():
+    """dJ/dkappa^2 against central differences of the oracle's CPU chain (the
+    reference algorithm, lexicographic order) with the same injected noise."""
+    import oracle as O
+    ch = ParamChain((16, 16, 16), _LOCS3[:2], _mg(3), nsteps=6, ordering=M.LEXICOGRAPHIC)
+    gk, _, _ = ch.grad(*ch.theta0)
+    k2, ls = ch.theta0
+
+    def J_oracle(kappa_sq):
+        op = O.Operator.fd(list(ch.shape), kappa_sq)
+        op.set_lowrank(ch.B, np.exp(ls))
+        src = O.Source(ch.normals)
+        s = O.mgmc_sampler(op, src, 3, "SSOR", "Cholesky", ordering=0)
+        f = ch.f_of(ls)
+        x = np.zeros(ch.n)
+        J = 0.0
+        for _ in range(ch.T):
+            s.apply(f, x)
+            J += float((ch.mask * x) @ x)
+        return J / ch.T
+
+    dk = 1e-6 * k2
+    fd = (J_oracle(k2 + dk) - J_oracle(k2 - dk)) / (2 * dk)
+    assert abs(gk - fd) <= 1e-5 * abs(fd)
