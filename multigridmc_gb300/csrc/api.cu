@@ -1444,7 +1444,10 @@ void Sampler::adjoint_sample(int lev) {
                 adjoint_sor<T>(*this, lev, true);
             }
         }
-        adj_zero<T>(*this, lv, lv.adj[0]);  // the coarse level starts from zero
+        // a coarse level starts from zero, and the Cholesky sample does not
+        // read its input; a one-level SSOR sampler's input is the chain's
+        // state, whose adjoint the sweeps above have formed
+        if (chol || lev > 0) adj_zero<T>(*this, lv, lv.adj[0]);
         return;
     }
     Level &lc = L[lev + 1];

@@ -22,6 +22,7 @@ def _sampler(op, prm, ordering=M.MULTICOLOUR, precision=M.FP64):
 
 CASES = [
     ("1d-lowrank", lambda: operator_1d(True)[1], _mg(3)),
+    ("2d-post-16-one-level-ssor", lambda: posterior((16, 16), m=3, radius=0.1)[1], _mg(1, coarse="SSOR")),
     ("1d-lowrank-sor-w", lambda: operator_1d(True)[1], _mg(3, omega=0.8, cycle=2, smoother="SOR")),
     ("2d-post-32", lambda: posterior((32, 32), m=4, radius=0.1)[1], _mg(4, omega=1.2)),
     ("3d-post-16", lambda: posterior((16, 16, 16), m=8)[1], _mg(3)),
@@ -235,17 +236,32 @@ class ParamChain:
         return self.hd * gc, gsig - Btf * self.y / sig, Btf / sig
 
 
-def _check_fd(ch, gk, gs, rel=1e-5, h=1e-6):
+def _check_fd(ch, gk, gs):
+    """Two checks per parameter: central differences with step 1e-6
+    (relative for kappa^2, absolute for log Sigma) within 1e-5 relative, the
+    error judged against the larger of |FD| and a tenth of the largest
+    gradient entry (the chain's rounding, ~1e-13 relative, divided by the
+    step is ~1e-7 of the gradient's scale); and the fourth-order central
+    difference with step 1e-4, whose truncation (~1e-16) and rounding
+    (~1e-9) errors are both small, within 1e-7 of the gradient's scale."""
     k2, ls = ch.theta0
     scale = max(abs(gk), np.abs(gs).max())
-    dk = h * k2
-    fd = (ch.J(k2 + dk, ls) - ch.J(k2 - dk, ls)) / (2 * dk)
-    assert abs(gk - fd) <= rel * max(abs(fd), 1e-3 * abs(gk)), f"d/dkappa^2: adjoint {gk} vs FD {fd}"
-    for k in range(ch.m):
+
+    def J_at(i, t):
+        if i < 0:
+            return ch.J(k2 * (1.0 + t), ls)
         e = np.zeros(ch.m)
-        e[k] = h
-        fd = (ch.J(k2, ls + e) - ch.J(k2, ls - e)) / (2 * h)
-        assert abs(gs[k] - fd) <= rel * max(abs(fd), 1e-3 * scale), f"d/dlog Sigma[{k}]: adjoint {gs[k]} vs FD {fd}"
+        e[i] = t
+        return ch.J(k2, ls + e)
+
+    for i, g in [(-1, gk)] + list(enumerate(gs)):
+        unit = k2 if i < 0 else 1.0
+        h = 1e-6
+        fd2 = (J_at(i, h) - J_at(i, -h)) / (2 * h * unit)
+        assert abs(g - fd2) <= 1e-5 * max(abs(fd2), 0.1 * scale), f"parameter {i}: adjoint {g} vs FD {fd2}"
+        h = 1e-4
+        fd4 = (8 * (J_at(i, h) - J_at(i, -h)) - (J_at(i, 2 * h) - J_at(i, -2 * h))) / (12 * h * unit)
+        assert abs(g - fd4) <= 1e-7 * scale, f"parameter {i}: adjoint {g} vs fourth-order FD {fd4}"
 
 
 _LOCS3 = [(0.3, 0.4, 0.5), (0.6, 0.55, 0.4), (0.45, 0.7, 0.65), (0.5, 0.3, 0.35)]
@@ -256,15 +272,15 @@ PARAM_CASES = [
     ("2d-32-sor-w", (32, 32), [(0.3, 0.6), (0.7, 0.4), (0.5, 0.5)], _mg(3, omega=1.2, cycle=2, smoother="SOR"),
      M.MULTICOLOUR),
     ("2d-32-ssor-w-lex", (32, 32), [(0.3, 0.6), (0.7, 0.4)], _mg(3, omega=0.9, cycle=2), M.LEXICOGRAPHIC),
+    ("2d-16-one-level-ssor", (16, 16), [(0.3, 0.6), (0.7, 0.4)], _mg(1, coarse="SSOR"), M.MULTICOLOUR),
 ]
 
 
 @pytest.mark.parametrize("name,shape,locs,prm,ordering", PARAM_CASES, ids=[c[0] for c in PARAM_CASES])
 def test_parameter_gradients_match_finite_differences(name, shape, locs, prm, ordering):
     """dJ/dkappa^2 and dJ/dlog Sigma_k (with f = B Sigma^{-1} y following
-    Sigma) by the parameter adjoint against central finite differences of
-    the FP64 chain with the same injected noise (step 1e-6 relative),
-    within 1e-5 relative."""
+    Sigma) by the parameter adjoint against finite differences of the FP64
+    chain with the same injected noise."""
     ch = ParamChain(shape, locs, prm, nsteps=8, ordering=ordering)
     gk, gs, _ = ch.grad(*ch.theta0)
     _check_fd(ch, gk, gs)
