@@ -335,6 +335,157 @@ def exact_probe_moments(op, f, pts, rtol=1e-10):
     return 0.5 * (C + C.T), mu, dt
 
 
+def adjoint_study(nsteps=200, every=10, nfd=4, seed=7):
+    """Differentiation: 3D 128^3 posterior (kappa^2 = 10, 32 measurements,
+    centres U[0.1, 0.9]^3, radius 0.05, Sigma = 1e-4, values N(0, 1)),
+    J = mean over 200 MGMC steps from x = 0 of ||x on the sub-cube
+    [0.25, 0.75]^3||^2 with the Philox noise fixed by the seed; gradients
+    with respect to kappa^2, the measurement values y and log Sigma by the
+    parameter adjoint with a checkpoint every 10 steps (each segment
+    recomputed from its checkpoint), FP64 and FP32-mixed; the FP64 gradient
+    against central differences (step 1e-6 relative) for kappa^2 and the
+    first nfd entries of y and log Sigma."""
+    import torch
+    import scipy.sparse as sp
+    import multigridmc_gb300 as M
+    shape, m = (128, 128, 128), 32
+    rng = np.random.default_rng(1)
+    loc = rng.uniform(0.1, 0.9, size=(m, 3))
+    y0 = rng.standard_normal(m)
+    cols = [M.measurement_vector(shape, x0, RADIUS) for x0 in loc]
+    k20, ls0 = KAPPA_SQ, np.full(m, np.log(VARIANCE))
+
+    def make_op(k2, ls):
+        return M.LinearOperator.shifted_laplace_fd(shape, k2).with_lowrank(cols, np.exp(ls))
+
+    op0 = make_op(k20, ls0)
+    n = op0.n
+    B = sp.csc_matrix((op0.B_val, op0.B_idx, op0.B_ptr), shape=(n, m))
+    hd = 1.0 / float(np.prod(shape))
+    N = [c - 1 for c in shape]
+    ax = [(np.arange(k) + 1.0) / c for k, c in zip(N, shape)]
+    inside = ((ax[2][:, None, None] >= 0.25) & (ax[2][:, None, None] <= 0.75) &
+              (ax[1][None, :, None] >= 0.25) & (ax[1][None, :, None] <= 0.75) &
+              (ax[0][None, None, :] >= 0.25) & (ax[0][None, None, :] <= 0.75))
+    mask = torch.from_numpy(inside.reshape(-1).astype(np.float64)).cuda()
+    prm = M.MultigridParameters(nlevel=5)
+
+    def sampler(op, prec):
+        return M.MultigridMCSampler(op, prm, precision=prec, noise=M.PHILOX, seed=seed)
+
+    def forward(s, ls, yv, keep=False):
+        s.fix_rhs(B @ (yv / np.exp(ls)))
+        x = torch.zeros(n, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        s.set_state_device(x.data_ptr())
+        s.step_counter = 0
+        J = torch.zeros((), dtype=torch.float64, device="cuda")
+        cps = {0: x.clone()}
+        for t in range(nsteps):
+            s.step(1)
+            s.get_state_device(x.data_ptr())
+            J += (mask * x * x).sum()
+            if keep and (t + 1) % every == 0 and t + 1 < nsteps:
+                cps[t + 1] = x.clone()
+        return float(J) / nsteps, cps
+
+    def gradient(prec):
+        s = sampler(op0, prec)
+        for _ in range(2):  # warm-up: graphs, tape buffers, lazy allocations
+            x = torch.zeros(n, dtype=torch.float64, device="cuda")
+            lam = torch.ones_like(x)
+            fb = torch.zeros_like(x)
+            torch.cuda.synchronize()
+            s.set_state_device(x.data_ptr())
+            s.step(3)
+            s.adjoint_params_device(x.data_ptr(), lam.data_ptr(), fb.data_ptr(), step_index=0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        J, cps = forward(s, ls0, y0, keep=True)
+        torch.cuda.synchronize()
+        t_fwd = time.perf_counter() - t0
+        lam = torch.zeros(n, dtype=torch.float64, device="cuda")
+        fbar = torch.zeros_like(lam)
+        gc, gs = 0.0, np.zeros(m)
+        t0 = time.perf_counter()
+        for a in reversed(range(0, nsteps, every)):
+            b = min(nsteps, a + every)
+            x = cps[a].clone()
+            torch.cuda.synchronize()
+            s.set_state_device(x.data_ptr())
+            s.step_counter = a
+            xs = [cps[a]]
+            for _ in range(a, b):
+                s.step(1)
+                xt = torch.empty_like(x)
+                s.get_state_device(xt.data_ptr())
+                xs.append(xt)
+            for t in range(b - 1, a - 1, -1):  # lam: adjoint of x_{t+1}
+                lam += (2.0 / nsteps) * mask * xs[t + 1 - a]
+                torch.cuda.synchronize()
+                c, g = s.adjoint_params_device(xs[t - a].data_ptr(), lam.data_ptr(), fbar.data_ptr(), step_index=t)
+                gc += c
+                gs += g
+        torch.cuda.synchronize()
+        t_rev = time.perf_counter() - t0
+        Btf = B.T @ fbar.cpu().numpy()
+        sig = np.exp(ls0)
+        grads = {"kappa_sq": hd * gc, "y": Btf / sig, "log_sigma": gs - Btf * y0 / sig}
+        return s, J, grads, {"forward_ms_per_step": t_fwd * 1e3 / nsteps, "reverse_ms_per_step": t_rev * 1e3 / nsteps}
+
+    out = {}
+    s64, J64, g64, tm64 = gradient(M.FP64)
+    s32, J32, g32, tm32 = gradient(M.FP32_MIXED)
+    s32.close()
+    out["fp64"] = {"J": J64, **tm64}
+    out["fp32_mixed"] = {"J": J32, **tm32}
+    out["fp32_vs_fp64_rel"] = {k: float(np.linalg.norm(np.atleast_1d(g32[k]) - np.atleast_1d(g64[k])) /
+                                        np.linalg.norm(np.atleast_1d(g64[k]))) for k in g64}
+    # finite differences of the FP64 chain: central, step 1e-6 (relative for
+    # kappa^2 and y, absolute for log Sigma), and fourth order with step 1e-4
+    # (J ~ 1e7 here, so the two-point difference carries eps J / h ~ 1e-3 of
+    # rounding; the fourth-order one, with its larger step, ~1e-5)
+    checks = []
+
+    def J_with(k2=k20, ls=ls0, yv=y0, reuse=None):
+        s = reuse or sampler(make_op(k2, ls), M.FP64)
+        J, _ = forward(s, ls, yv)
+        if reuse is None:
+            s.close()
+        return J
+
+    def J_dir(kind, k, t):
+        if kind == "kappa_sq":
+            return J_with(k2=k20 * (1.0 + t))
+        e = np.zeros(m)
+        if kind == "log_sigma":
+            e[k] = t
+            return J_with(ls=ls0 + e)
+        e[k] = t * max(1.0, abs(y0[k]))
+        return J_with(yv=y0 + e, reuse=s64)
+
+    params = [("kappa_sq", 0, g64["kappa_sq"], k20, abs(g64["kappa_sq"]))]
+    for k in range(nfd):
+        params.append(("log_sigma", k, float(g64["log_sigma"][k]), 1.0, np.abs(g64["log_sigma"]).max()))
+        params.append(("y", k, float(g64["y"][k]), max(1.0, abs(y0[k])), np.abs(g64["y"]).max()))
+    for kind, k, g, unit, scale in params:
+        h = 1e-6
+        fd2 = (J_dir(kind, k, h) - J_dir(kind, k, -h)) / (2 * h * unit)
+        h = 1e-4
+        fd4 = (8 * (J_dir(kind, k, h) - J_dir(kind, k, -h)) - (J_dir(kind, k, 2 * h) - J_dir(kind, k, -2 * h))) / (12 * h * unit)
+        name = kind if kind == "kappa_sq" else f"{kind}[{k}]"
+        checks.append({"param": name, "adjoint": g, "fd2": fd2, "fd4": fd4,
+                       "rel_err_fd2": abs(g - fd2) / max(abs(fd2), 0.1 * scale),
+                       "rel_err_fd4": abs(g - fd4) / max(abs(fd4), 0.1 * scale)})
+    s64.close()
+    out["fd_checks_fp64"] = checks
+    out["max_rel_err_fd2"] = max(c["rel_err_fd2"] for c in checks)
+    out["max_rel_err_fd4"] = max(c["rel_err_fd4"] for c in checks)
+    out["problem"] = ("3D 128^3 posterior, 32 measurements, V(1,1) SSOR, 5 levels, coarse Cholesky 8^3, Philox noise, "
+                      f"{nsteps} steps, checkpoints every {every}")
+    return out
+
+
 def solve_study(rtol=1e-10, repeats=3):
     """The reference's deterministic multigrid solve (driver_mg: LoopSolver
     with MultigridPreconditioner) of Q x = f on the 256^3 posterior: FP64
@@ -489,6 +640,8 @@ def main():
                     help="run the batched-chains study (N chains of mixed sizes) instead of the benchmark")
     ap.add_argument("--convergence-study", type=int, default=0, metavar="NCHAIN",
                     help="run measure_convergence over NCHAIN batched chains (--steps steps) instead of the benchmark")
+    ap.add_argument("--adjoint-study", action="store_true",
+                    help="run the 128^3 differentiation study (parameter adjoint with checkpoints, FD checks)")
     ap.add_argument("--solve-study", action="store_true",
                     help="time the deterministic multigrid solve of Q x = f instead of the benchmark")
     ap.add_argument("--profile-steps", type=int, default=0, metavar="K",
@@ -504,6 +657,9 @@ def main():
         return
     if args.convergence_study > 0:
         print(json.dumps({"convergence_study": convergence_study(args.convergence_study, args.steps)}), flush=True)
+        return
+    if args.adjoint_study:
+        print(json.dumps({"adjoint_study": adjoint_study()}), flush=True)
         return
     if args.solve_study:
         print(json.dumps({"solve_study": solve_study()}), flush=True)

@@ -170,6 +170,11 @@ mgmc_status mgmc_sampler_synchronize(mgmc_sampler *s);
 mgmc_status mgmc_sampler_stream(mgmc_sampler *s, void **cuda_stream);
 mgmc_status mgmc_sampler_nlevel(mgmc_sampler *s, int *nlevel);
 mgmc_status mgmc_sampler_level_size(mgmc_sampler *s, int level, int64_t *n);
+/* The step counter that keys the Philox noise (the number of steps taken
+ * since creation); setting it lets a chain segment be recomputed from a
+ * checkpoint with its original noise.  No counterpart in the reference. */
+mgmc_status mgmc_sampler_set_step_counter(mgmc_sampler *s, int64_t step);
+mgmc_status mgmc_sampler_get_step_counter(mgmc_sampler *s, int64_t *step);
 /* Number of kernel launches one step issues (measurement bookkeeping). */
 mgmc_status mgmc_sampler_launches_per_step(mgmc_sampler *s, int64_t *count);
 /* Adjoint of one step with its noise held fixed (no counterpart in the

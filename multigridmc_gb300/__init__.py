@@ -95,6 +95,8 @@ SIGNATURES = {
     "mgmc_sampler_set_state": (C.c_int, [_P, _D, C.c_int]),
     "mgmc_sampler_get_state": (C.c_int, [_P, _D, C.c_int]),
     "mgmc_sampler_step": (C.c_int, [_P, C.c_int64]),
+    "mgmc_sampler_set_step_counter": (C.c_int, [_P, C.c_int64]),
+    "mgmc_sampler_get_step_counter": (C.c_int, [_P, _I64]),
     "mgmc_sampler_set_observable": (C.c_int, [_P, C.c_int64, _I64, _D, C.c_int64]),
     "mgmc_sampler_read_observations": (C.c_int, [_P, _D, C.c_int64, _I64]),
     "mgmc_sampler_set_probes": (C.c_int, [_P, C.c_int, _I64, _I64, _D, C.c_int64]),
@@ -447,6 +449,35 @@ class MultigridMCSampler:
 
     def step(self, nsteps=1):
         _check(self._L.mgmc_sampler_step(self._h, int(nsteps)))
+
+    @property
+    def step_counter(self):
+        """The Philox step counter (steps taken since creation)."""
+        c = C.c_int64(0)
+        _check(self._L.mgmc_sampler_get_step_counter(self._h, C.byref(c)))
+        return c.value
+
+    @step_counter.setter
+    def step_counter(self, k):
+        _check(self._L.mgmc_sampler_set_step_counter(self._h, int(k)))
+
+    # --- device-resident vectors (addresses of n float64 values)
+    def set_state_device(self, x_ptr):
+        _check(self._L.mgmc_sampler_set_state(self._h, C.cast(C.c_void_p(x_ptr), _D), 1))
+
+    def get_state_device(self, x_ptr):
+        """Writes the state to x_ptr and waits for it."""
+        _check(self._L.mgmc_sampler_get_state(self._h, C.cast(C.c_void_p(x_ptr), _D), 1))
+        self.synchronize()
+
+    def adjoint_params_device(self, x_ptr, xbar_ptr, fbar_ptr, step_index=0):
+        """adjoint_params on device vectors; returns (d/dcentre, d/dlog Sigma)."""
+        gc = C.c_double(0.0)
+        gs = np.zeros(max(self.op.m, 1))
+        cast = lambda p: C.cast(C.c_void_p(p), _D)
+        _check(self._L.mgmc_sampler_adjoint_params(self._h, cast(x_ptr), int(step_index), cast(xbar_ptr),
+                                                   cast(fbar_ptr), C.byref(gc), _dp(gs), 1))
+        return gc.value, gs[:self.op.m].copy()
 
     def synchronize(self):
         _check(self._L.mgmc_sampler_synchronize(self._h))

@@ -1785,6 +1785,27 @@ mgmc_status mgmc_sampler_get_state(mgmc_sampler *s, double *x, int on_device) {
     API_END
 }
 
+mgmc_status mgmc_sampler_set_step_counter(mgmc_sampler *s, int64_t step) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (step < 0) fail(MGMC_ERR_INVALID_ARGUMENT, "step < 0");
+    const u64 k = (u64)step;
+    CK(cudaMemcpyAsync(S.d_step, &k, sizeof(u64), cudaMemcpyHostToDevice, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    API_END
+}
+
+mgmc_status mgmc_sampler_get_step_counter(mgmc_sampler *s, int64_t *step) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!step) fail(MGMC_ERR_INVALID_ARGUMENT, "null step");
+    u64 k = 0;
+    CK(cudaMemcpyAsync(&k, S.d_step, sizeof(u64), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    *step = (int64_t)k;
+    API_END
+}
+
 mgmc_status mgmc_sampler_step(mgmc_sampler *s, int64_t nsteps) {
     API_BEGIN
     Sampler &S = impl(s);
