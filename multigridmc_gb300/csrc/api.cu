@@ -127,7 +127,8 @@ struct Sampler {
     // step construction
     unsigned inv = 0;
     i64 noise_off = 0;
-    i64 launches = 0;
+    i64 launches = 0;       // kernel launches counted while a sequence is issued
+    i64 step_launches = 0;  // ... of the last step issued by launch_step
     bool counting = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -708,6 +709,7 @@ void Sampler::launch_step() {
     launches = 0;
     sample(0);
     step_end();
+    step_launches = launches;
 }
 
 // ------------------------------------------------------------- set-up
@@ -1984,7 +1986,7 @@ mgmc_status mgmc_sampler_launches_per_step(mgmc_sampler *s, int64_t *count) {
     Sampler &S = impl(s);
     if (!count) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
     if (S.noise_mode == NOISE_PHILOX) ensure_graph(S);
-    *count = S.launches;
+    *count = S.step_launches;
     API_END
 }
 
