@@ -167,6 +167,8 @@ struct Sampler {
         if (rgraph) cudaGraphDestroy(rgraph);
         if (pexec) cudaGraphExecDestroy(pexec);
         if (pgraph) cudaGraphDestroy(pgraph);
+        if (pa_exec) cudaGraphExecDestroy(pa_exec);
+        if (pa_graph) cudaGraphDestroy(pa_graph);
         for (void *p : owned) cudaFree(p);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -199,7 +201,15 @@ struct Sampler {
     int pa_part_cap = 0;
     double *pa_Bu = nullptr, *pa_Bv = nullptr, *pa_xi = nullptr, *pa_xic = nullptr, *pa_U = nullptr;
     void *pa_phi = nullptr, *pa_cv = nullptr, *pa_mu = nullptr;
+    // with Philox noise every launch of the replay and the reverse pass has
+    // the same arguments at every call (the tape's buffers are reused, the
+    // step enters through the device step counter): after one direct call
+    // the sequence runs as one CUDA graph
+    cudaGraph_t pa_graph = nullptr;
+    cudaGraphExec_t pa_exec = nullptr;
+    int pa_calls = 0;
     void ensure_param_adjoint();
+    void param_adjoint_pass();
     void *tape_snap(int lev, const void *src);
     void *tape_state(int lev);
     TapeEvent tape_pop(int kind, int lev, bool forward);
@@ -1574,20 +1584,46 @@ void Sampler::ensure_param_adjoint() {
     CK(cudaStreamSynchronize(stream));
 }
 
+static PgradStencils pgrad_stencils(const Level &lv, const std::array<double, 27> &E) {
+    PgradStencils st;
+    for (int k = 0; k < 27; ++k) {
+        st.a[k] = lv.st[k];
+        st.e[k] = E[k];
+        st.af[k] = (float)lv.st[k];
+        st.ef[k] = (float)E[k];
+    }
+    return st;
+}
+
+template <typename T>
+static void launch_pgrad_stencil(Sampler &S, const Level &lv, const std::array<double, 27> &E, const void *u,
+                                 const void *v, const void *w, const void *f, int ncol, bool forward, int np) {
+    const PgradStencils st = pgrad_stencils(lv, E);
+    bool has_e = false;
+    for (int k = 0; k < 27; ++k) has_e |= (k != 13 && E[k] != 0.0);
+    const T *U = (const T *)u, *V = (const T *)v, *W = (const T *)w, *F = (const T *)f;
+    const int fw = forward ? 1 : 0;
+    if (lv.npt == 7) {
+        if (has_e)
+            k_pgrad_stencil<T, 7, true><<<np, 256, 0, S.stream>>>(U, V, W, F, lv.g, st, ncol, fw, S.pa_part);
+        else
+            k_pgrad_stencil<T, 7, false><<<np, 256, 0, S.stream>>>(U, V, W, F, lv.g, st, ncol, fw, S.pa_part);
+    } else {
+        if (has_e)
+            k_pgrad_stencil<T, 27, true><<<np, 256, 0, S.stream>>>(U, V, W, F, lv.g, st, ncol, fw, S.pa_part);
+        else
+            k_pgrad_stencil<T, 27, false><<<np, 256, 0, S.stream>>>(U, V, W, F, lv.g, st, ncol, fw, S.pa_part);
+    }
+}
+
 // One sweep's contribution: u = M_f^{-T} x-bar'' of the sweep, its input
 // and output states and right hand side from the tape.
 template <typename T>
 void Sampler::pgrad_sweep(const TapeEvent &ev, const void *u) {
     Level &lv = L[ev.lev];
-    PgradStencils st;
-    for (int k = 0; k < 27; ++k) {
-        st.a[k] = lv.st[k];
-        st.e[k] = pa_E[ev.lev][k];
-    }
     const int ncol = P.ordering == MGMC_ORDER_LEXICOGRAPHIC ? 0 : lv.ncol;
     const int np = (int)(((i64)lv.g.N1 * lv.g.N2 + SOLVE_ROWS - 1) / SOLVE_ROWS);
-    k_pgrad_stencil<T><<<np, 256, 0, stream>>>((const T *)u, (const T *)ev.xout, (const T *)ev.xin, (const T *)ev.f, lv.g,
-                                               st, ncol, ev.forward ? 1 : 0, pa_part);
+    launch_pgrad_stencil<T>(*this, lv, pa_E[ev.lev], u, ev.xout, ev.xin, ev.f, ncol, ev.forward, np);
     if (m > 0) {
         launch_bt_plain<T>(*this, lv, u, pa_Bu);
         launch_bt_plain<T>(*this, lv, ev.xout, pa_Bv);
@@ -1609,14 +1645,8 @@ void Sampler::pgrad_sweep(const TapeEvent &ev, const void *u) {
 template <typename T>
 void Sampler::pgrad_minus_udav(int lev, const void *u, const void *v) {
     Level &lv = L[lev];
-    PgradStencils st;
-    for (int k = 0; k < 27; ++k) {
-        st.a[k] = lv.st[k];
-        st.e[k] = pa_E[lev][k];
-    }
     const int np = (int)(((i64)lv.g.N1 * lv.g.N2 + SOLVE_ROWS - 1) / SOLVE_ROWS);
-    k_pgrad_stencil<T><<<np, 256, 0, stream>>>((const T *)u, (const T *)v, (const T *)v, (const T *)v, lv.g, st, 0, 1,
-                                               pa_part);
+    launch_pgrad_stencil<T>(*this, lv, pa_E[lev], u, v, v, v, 0, true, np);
     if (m > 0) {
         launch_bt_plain<T>(*this, lv, u, pa_Bu);
         launch_bt_plain<T>(*this, lv, v, pa_Bv);
@@ -1651,6 +1681,38 @@ void Sampler::pgrad_coarse(const TapeEvent &ev) {
             chol_ld, (T *)pa_mu);
     pgrad_minus_udav<T>(ev.lev, lv.adj[2], pa_mu);
 }
+// The replay of one step from level 0's state, recording the tape, and the
+// reverse pass from level 0's adj[0], accumulating the parameter gradients
+// (device work only, so that it can be captured).
+void Sampler::param_adjoint_pass() {
+    Level &l0 = L[0];
+    const int mm = std::max(m, 1);
+    tape.clear();
+    std::fill(tape_next.begin(), tape_next.end(), 0);
+    std::fill(tape_last.begin(), tape_last.end(), nullptr);
+    std::fill(tape_f.begin(), tape_f.end(), nullptr);
+    tape_f[0] = l0.f;
+    inv = 0;
+    noise_off = noise_pos;
+    taping = true;
+    sample(0);
+    taping = false;
+    check_launch();
+    CK(cudaMemsetAsync(pa_gs, 0, sizeof(double), stream));
+    CK(cudaMemsetAsync(pa_gsig, 0, mm * sizeof(double), stream));
+    param_adj = true;
+    if (fp32) {
+        adj_zero<float>(*this, l0, l0.adj[1]);
+        adjoint_sample<float>(0);
+    } else {
+        adj_zero<double>(*this, l0, l0.adj[1]);
+        adjoint_sample<double>(0);
+    }
+    param_adj = false;
+    check_launch();
+    if (!tape.empty()) fail(MGMC_ERR_INVALID_ARGUMENT, "parameter adjoint: tape not consumed");
+}
+
 }  // namespace mgmc
 
 // ===================================================================== ABI
@@ -2333,34 +2395,26 @@ mgmc_status mgmc_sampler_adjoint_params(mgmc_sampler *s, const double *x_in, int
         put_vec(S, 0, x_in, on_device, l0.x);
         const u64 k = (u64)step_index;
         CK(cudaMemcpyAsync(S.d_step, &k, sizeof(u64), cudaMemcpyHostToDevice, S.stream));
-        // replay the step, recording the tape (the noise of step step_index,
-        // or the next injected noise)
-        S.tape.clear();
-        std::fill(S.tape_next.begin(), S.tape_next.end(), 0);
-        std::fill(S.tape_last.begin(), S.tape_last.end(), nullptr);
-        std::fill(S.tape_f.begin(), S.tape_f.end(), nullptr);
-        S.tape_f[0] = l0.f;
-        S.inv = 0;
-        S.noise_off = S.noise_pos;
-        S.taping = true;
-        S.sample(0);
-        S.taping = false;
-        S.check_launch();
-        // reverse pass
         put_vec(S, 0, xbar, on_device, l0.adj[0]);
-        CK(cudaMemsetAsync(S.pa_gs, 0, sizeof(double), S.stream));
-        CK(cudaMemsetAsync(S.pa_gsig, 0, mm * sizeof(double), S.stream));
-        S.param_adj = true;
-        if (S.fp32) {
-            adj_zero<float>(S, l0, l0.adj[1]);
-            S.adjoint_sample<float>(0);
+        if (S.noise_mode == NOISE_PHILOX && S.pa_calls > 0) {
+            if (!S.pa_exec) {
+                CK(cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal));
+                try {
+                    S.param_adjoint_pass();
+                } catch (...) {
+                    cudaGraph_t g = nullptr;
+                    cudaStreamEndCapture(S.stream, &g);
+                    if (g) cudaGraphDestroy(g);
+                    throw;
+                }
+                CK(cudaStreamEndCapture(S.stream, &S.pa_graph));
+                CK(cudaGraphInstantiate(&S.pa_exec, S.pa_graph, 0));
+            }
+            CK(cudaGraphLaunch(S.pa_exec, S.stream));
         } else {
-            adj_zero<double>(S, l0, l0.adj[1]);
-            S.adjoint_sample<double>(0);
+            S.param_adjoint_pass();
         }
-        S.param_adj = false;
-        S.check_launch();
-        if (!S.tape.empty()) fail(MGMC_ERR_INVALID_ARGUMENT, "parameter adjoint: tape not consumed");
+        S.pa_calls++;
         adjoint_outputs(S, xbar, fbar, on_device);
         CK(cudaMemcpy(&gs, S.pa_gs, sizeof(double), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(gsig.data(), S.pa_gsig, mm * sizeof(double), cudaMemcpyDeviceToHost));

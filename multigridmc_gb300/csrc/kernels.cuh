@@ -1272,7 +1272,21 @@ __global__ void __launch_bounds__(256) k_solve_update(double *__restrict__ x, co
 struct PgradStencils {
     double a[27];  // the level's A_0
     double e[27];  // E_l = dA_0 / ds
+    float af[27], ef[27];  // the same rounded to FP32 (neighbour sums of FP32 chains)
 };
+
+template <typename T>
+__device__ __forceinline__ T pg_a(const PgradStencils &st, int k);
+template <>
+__device__ __forceinline__ float pg_a<float>(const PgradStencils &st, int k) { return st.af[k]; }
+template <>
+__device__ __forceinline__ double pg_a<double>(const PgradStencils &st, int k) { return st.a[k]; }
+template <typename T>
+__device__ __forceinline__ T pg_e(const PgradStencils &st, int k);
+template <>
+__device__ __forceinline__ float pg_e<float>(const PgradStencils &st, int k) { return st.ef[k]; }
+template <>
+__device__ __forceinline__ double pg_e<double>(const PgradStencils &st, int k) { return st.e[k]; }
 
 // Colour of interior point (a, b, c) in the multicolour order (2 colours:
 // parity of a + b + c; 2^dim colours: one parity bit per direction).
@@ -1281,14 +1295,18 @@ __device__ __forceinline__ int point_colour(int ncol, int a, int b, int c) {
 }
 
 // Per CTA of SOLVE_ROWS rows, the eight sums over the level's points p
-// (part[8 * blockIdx.x + j]):
+// (part[j * gridDim.x + blockIdx.x]):
 //   0: u_p sum_{q before p} A_pq v_q    1: u_p sum_{q after p} A_pq w_q
 //   2: u_p sum_{q before p} E_pq v_q    3: u_p sum_{q before p} E_pq w_q
 //   4: u_p sum_{q after p} E_pq w_q     5: u_p v_p   6: u_p w_p   7: u_p f_p
-// (v = the sweep's output, w = its input; off-diagonal neighbours only).
-// "Before" is the order of the sweep of direction `forward`: by linear
-// index for the lexicographic order (ncol = 0), by colour otherwise.
-template <typename T>
+// (v = the sweep's output, w = its input; off-diagonal neighbours only, the
+// 6 axis neighbours of a 7-point level or all 26).  "Before" is the order
+// of the sweep of direction `forward`: by linear index for the
+// lexicographic order (ncol = 0), by colour otherwise.  The neighbour sums
+// run in the chain's type T, the u_p-weighted sums in FP64.  Without
+// off-diagonal entries in E (HAS_E false: the fine level's E is the unit
+// centre weight) sums 2 to 4 are zero and skipped.
+template <typename T, int NPT, bool HAS_E>
 __global__ void __launch_bounds__(256) k_pgrad_stencil(const T *__restrict__ u, const T *__restrict__ v,
                                                        const T *__restrict__ w, const T *__restrict__ f, Grid3 g,
                                                        PgradStencils st, int ncol, int forward,
@@ -1302,17 +1320,20 @@ __global__ void __launch_bounds__(256) k_pgrad_stencil(const T *__restrict__ u, 
         const int bb = (int)(row % g.N1), c = (int)(row / g.N1);
         for (int a = threadIdx.x; a < g.N0; a += blockDim.x) {
             const i64 P = g.pad(a, bb, c);
-            const double up = (double)u[P];
-            if (up == 0.0) continue;
+            const T up = u[P];
+            if (up == T(0)) continue;
             const int cp = ncol ? point_colour(ncol, a, bb, c) : 0;
-            double lav = 0, uaw = 0, lev = 0, lew = 0, uew = 0;
+            T lav = 0, uaw = 0, lev = 0, lew = 0, uew = 0;
+#pragma unroll
             for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
                 for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
                     for (int dx = -1; dx <= 1; ++dx) {
+                        const int nzo = (dx != 0) + (dy != 0) + (dz != 0);
+                        if (nzo == 0 || (NPT == 7 && nzo > 1)) continue;
                         const int k = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1);
-                        if (k == 13) continue;
-                        const double wa = st.a[k], we = st.e[k];
-                        if (wa == 0.0 && we == 0.0) continue;
+                        const T wa = pg_a<T>(st, k), we = pg_e<T>(st, k);
                         bool before;
                         if (ncol == 0) {
                             const bool lower = dz < 0 || (dz == 0 && (dy < 0 || (dy == 0 && dx < 0)));
@@ -1322,37 +1343,42 @@ __global__ void __launch_bounds__(256) k_pgrad_stencil(const T *__restrict__ u, 
                             before = forward ? cq < cp : cq > cp;
                         }
                         const i64 Q = P + dz * g.sz + dy * g.sy + dx;
+                        const T wq = w[Q];
                         if (before) {
-                            const double vq = (double)v[Q], wq = (double)w[Q];
+                            const T vq = v[Q];
                             lav += wa * vq;
-                            lev += we * vq;
-                            lew += we * wq;
+                            if (HAS_E) {
+                                lev += we * vq;
+                                lew += we * wq;
+                            }
                         } else {
-                            const double wq = (double)w[Q];
                             uaw += wa * wq;
-                            uew += we * wq;
+                            if (HAS_E) uew += we * wq;
                         }
                     }
-            acc[0] += up * lav;
-            acc[1] += up * uaw;
-            acc[2] += up * lev;
-            acc[3] += up * lew;
-            acc[4] += up * uew;
-            acc[5] += up * (double)v[P];
-            acc[6] += up * (double)w[P];
-            acc[7] += up * (double)f[P];
+            const double ud = (double)up;
+            acc[0] += ud * (double)lav;
+            acc[1] += ud * (double)uaw;
+            if (HAS_E) {
+                acc[2] += ud * (double)lev;
+                acc[3] += ud * (double)lew;
+                acc[4] += ud * (double)uew;
+            }
+            acc[5] += ud * (double)v[P];
+            acc[6] += ud * (double)w[P];
+            acc[7] += ud * (double)f[P];
         }
     }
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         const double t = block_sum<256>(acc[j], sh);
-        if (threadIdx.x == 0) part[8 * (i64)blockIdx.x + j] = t;
+        if (threadIdx.x == 0) part[(i64)j * gridDim.x + blockIdx.x] = t;
         __syncthreads();
     }
 }
 
 // Adds one event's contribution to the gradients (one CTA).  Sums the eight
-// partial streams of k_pgrad_stencil into S0..S7 and, with Bu = B^T u,
+// partial streams of k_pgrad_stencil (np values each) into S0..S7 and, with Bu = B^T u,
 // Bv = B^T v and the low-rank normals xi' of the sweep:
 // sweep (mode 0), kd = dsd/ds / sd = E_c / (2 A_c):
 //   g_s += kd [S0 + A_c/omega S5 + S1 + A_c (1 - 1/omega) S6 - S7
@@ -1377,7 +1403,7 @@ __global__ void __launch_bounds__(256) k_pgrad_combine(const double *__restrict_
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         double a = 0.0;
-        for (int i = threadIdx.x; i < np; i += blockDim.x) a += part[8 * (i64)i + j];
+        for (int i = threadIdx.x; i < np; i += blockDim.x) a += part[(i64)j * np + i];
         S[j] = block_sum<256>(a, sh);
         __syncthreads();
     }
