@@ -224,6 +224,20 @@ mgmc_status mgmc_sampler_precondition(mgmc_sampler *s, const double *b, double *
  * chain's state and right hand side are left unchanged. */
 mgmc_status mgmc_sampler_solve(mgmc_sampler *s, const double *b, double *x, double rtol, double atol, int maxiter,
                                int on_device, int *niter, double *rnorm, int *converged);
+/* Exact sampler, the comparator of SparseCholeskySampler / DenseCholeskySampler
+ * (src/sampler/cholesky_sampler.cc:9-37) at sizes a factorisation does not
+ * reach: x = Q^{-1}(f + eta) with eta ~ N(0, Q), Q = A_0 + B Sigma^{-1} B^T,
+ * is an exact draw from N(Q^{-1} f, Q^{-1}).  eta is drawn in-kernel (Philox
+ * keyed by the sampler's seed and step counter, which the call advances by
+ * one) from an edge decomposition of A_0 -- which needs a symmetric stencil
+ * with non-positive off-diagonal weights and weak diagonal dominance (the
+ * FD prior has it; otherwise MGMC_ERR_UNSUPPORTED) -- plus B Sigma^{-1/2} xi;
+ * the system is solved by mgmc_sampler_solve's loop to relative residual
+ * rtol (MGMC_ERR_NONFINITE if maxiter iterations do not reach it).  The
+ * sample does not depend on the chain's state, which is left unchanged.
+ * *niter (may be NULL) receives the iteration count. */
+mgmc_status mgmc_sampler_exact_sample(mgmc_sampler *s, const double *f, double *x, double rtol, int maxiter,
+                                      int on_device, int *niter);
 
 /* -------------------------------------------- level building blocks */
 mgmc_status mgmc_level_stencil(mgmc_sampler *s, int level, double stencil[27]);

@@ -14,6 +14,8 @@ this module              reference (eikehmueller/MultigridMC)
 ``SSORSampler``          SSORSampler (sampler/ssor_sampler.{hh,cc})
 ``CholeskySampler``      DenseCholeskySampler (sampler/cholesky_sampler.cc:25-37)
 ``MultigridPreconditioner``  MultigridPreconditioner (preconditioner/multigrid_preconditioner.cc:8-108)
+``ExactSampler``         exact draws x = Q^{-1}(f + eta), the comparator role of SparseCholeskySampler
+                         (sampler/cholesky_sampler.cc:9-23)
 ``LoopSolver``           LoopSolver (solver/loop_solver.cc:9-53) with IterativeSolverParameters
                          (auxilliary/parameters.hh:130-147)
 =======================  ==========================================================
@@ -36,7 +38,7 @@ from . import build as _build
 __all__ = [
     "MGMCError", "load", "fd_stencil", "galerkin_stencil", "measurement_vector", "LinearOperator",
     "MultigridParameters", "MultigridMCSampler", "MultigridMCBatch", "SSORSampler", "CholeskySampler",
-    "IterativeSolverParameters", "MultigridPreconditioner", "LoopSolver",
+    "IterativeSolverParameters", "MultigridPreconditioner", "LoopSolver", "ExactSampler",
     "FP64", "FP32_MIXED", "LEXICOGRAPHIC", "MULTICOLOUR", "PHILOX", "INJECTED", "FORWARD", "BACKWARD",
 ]
 
@@ -110,6 +112,7 @@ SIGNATURES = {
     "mgmc_sampler_adjoint_step": (C.c_int, [_P, _D, _D, C.c_int]),
     "mgmc_sampler_adjoint_params": (C.c_int, [_P, _D, C.c_int64, _D, _D, _D, _D, C.c_int]),
     "mgmc_sampler_precondition": (C.c_int, [_P, _D, _D, C.c_int]),
+    "mgmc_sampler_exact_sample": (C.c_int, [_P, _D, _D, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "mgmc_sampler_solve": (C.c_int, [_P, _D, _D, C.c_double, C.c_double, C.c_int, C.c_int,
                                      C.POINTER(C.c_int), _D, C.POINTER(C.c_int)]),
     "mgmc_level_stencil": (C.c_int, [_P, C.c_int, _D]),
@@ -437,6 +440,23 @@ class MultigridMCSampler:
                                           C.byref(it), C.byref(rn), C.byref(cv)))
         return x, it.value, rn.value, bool(cv.value)
 
+    def exact_sample(self, f, rtol=1e-10, maxiter=100):
+        """An exact draw from N(Q^{-1} f, Q^{-1}): x = Q^{-1}(f + eta) with
+        eta ~ N(0, Q) drawn in-kernel, solved by the multigrid loop solver;
+        advances the step counter.  Returns (x, iterations)."""
+        f = _f64(f)
+        x = np.zeros(self.n)
+        it = C.c_int(0)
+        _check(self._L.mgmc_sampler_exact_sample(self._h, _dp(f), _dp(x), float(rtol), int(maxiter), 0, C.byref(it)))
+        return x, it.value
+
+    def exact_sample_device(self, f_ptr, x_ptr, rtol=1e-10, maxiter=100):
+        it = C.c_int(0)
+        cast = lambda p: C.cast(C.c_void_p(p), _D)
+        _check(self._L.mgmc_sampler_exact_sample(self._h, cast(f_ptr), cast(x_ptr), float(rtol), int(maxiter), 1,
+                                                 C.byref(it)))
+        return it.value
+
     def solve_device(self, b_ptr, x_ptr, rtol=1e-10, atol=1e-10, maxiter=100):
         """solve() on device vectors given as addresses of n float64 values
         (the solution is written to x_ptr); returns (niter, residual norm,
@@ -621,6 +641,26 @@ def SSORSampler(linear_operator, omega=1.0, nsmooth=1, **kw):
     coarse solver is SSOR with `nsmooth` forward/backward pairs."""
     p = MultigridParameters(nlevel=1, coarse_solver="SSOR", ncoarsesmooth=nsmooth, omega=omega)
     return MultigridMCSampler(linear_operator, p, **kw)
+
+
+class ExactSampler:
+    """Exact sampler (the role of SparseCholeskySampler, cholesky_sampler.cc:9-23,
+    at any lattice size): every apply(f, x) overwrites x with an independent
+    draw x = Q^{-1}(f + eta), eta ~ N(0, Q), by a multigrid solve to relative
+    residual `rtol` on the hierarchy of `params`."""
+
+    def __init__(self, linear_operator, params=None, precision=FP32_MIXED, seed=0, rtol=1e-10, device=0):
+        self.op = linear_operator
+        self.rtol = rtol
+        self._s = MultigridMCSampler(linear_operator, params, precision=precision, seed=seed, device=device)
+
+    def apply(self, f, x):
+        y, _ = self._s.exact_sample(f, self.rtol)
+        x[:] = y
+        return x
+
+    def close(self):
+        self._s.close()
 
 
 def CholeskySampler(linear_operator, **kw):

@@ -229,6 +229,11 @@ struct Sampler {
     void sample(int lev);
     void ensure_solver();
     void ensure_solver_buffers();
+    // exact sampler: x = Q^{-1}(f + eta), eta ~ N(0, Q), by the loop solver
+    EdgeWeights ew{};
+    bool ew_ready = false;
+    double *ex_y = nullptr;
+    void ensure_exact();
     void coarse_sample(int lev);
     void resid_restrict(int lev);
     void prolong(int lev, double alpha, void *xc, void *x);
@@ -1348,6 +1353,32 @@ void Sampler::ensure_solver() {
         });
 }
 
+// Edge weights of the fine stencil for the exact sampler's perturbation
+// (k_prior_perturbation): symmetric, non-positive off-diagonal weights and
+// a non-negative diagonal surplus.
+void Sampler::ensure_exact() {
+    if (ew_ready) return;
+    const double *w = L[0].st;
+    double off = 0.0;
+    for (int k = 0; k < 27; ++k) {
+        if (k == 13) continue;
+        if (w[k] > 0.0 || w[k] != w[26 - k])
+            fail(MGMC_ERR_UNSUPPORTED, "the exact sampler needs a symmetric stencil with non-positive off-diagonal weights");
+        off -= w[k];
+    }
+    double c0 = w[13] - off;
+    if (c0 < -1e-12 * w[13]) fail(MGMC_ERR_UNSUPPORTED, "the exact sampler needs a weakly diagonally dominant stencil");
+    ew.c0 = std::sqrt(std::max(c0, 0.0));
+    for (int k = 14; k < 27; ++k) {
+        ew.ck[k - 14] = std::sqrt(-w[k]);
+        ew.off[k - 14][0] = k % 3 - 1;
+        ew.off[k - 14][1] = (k / 3) % 3 - 1;
+        ew.off[k - 14][2] = k / 9 - 1;
+    }
+    ex_y = alloc<double>((size_t)std::max(m, 1));
+    ew_ready = true;
+}
+
 // The chain's x_0 and f_0 are borrowed by a solve and put back afterwards.
 struct BorrowLevel0 {
     Sampler &S;
@@ -2276,6 +2307,35 @@ mgmc_status mgmc_sampler_precondition(mgmc_sampler *s, const double *b, double *
     API_END
 }
 
+// LoopSolver::apply on the solver's FP64 vectors: b in sv_b, x from zero
+// (loop_solver.cc:17) into sv_x; returns the iteration at which the test
+// passed (maxiter when it never did), the last residual norm (-1 when
+// maxiter = 0) and whether it passed.
+static int loop_solve(Sampler &S, double rtol, double atol, int maxiter, double *rnorm, bool *converged) {
+    Level &l0 = S.L[0];
+    CK(cudaMemsetAsync(S.sv_x, 0, (size_t)l0.geo.nalloc * sizeof(double), S.stream));
+    int k = 0;
+    double r0 = 0.0, rn = -1.0;
+    bool conv = false;
+    for (k = 0; k < maxiter; ++k) {
+        CK(cudaGraphLaunch(S.rexec, S.stream));
+        double r2 = 0.0;
+        CK(cudaMemcpyAsync(&r2, S.sv_norm, sizeof(double), cudaMemcpyDeviceToHost, S.stream));
+        CK(cudaStreamSynchronize(S.stream));
+        rn = std::sqrt(r2);
+        if (!std::isfinite(rn)) fail(MGMC_ERR_NONFINITE, "non-finite residual in the solver");
+        if (k == 0) r0 = rn;  // |A 0 - b| = |b| (loop_solver.cc:11)
+        if (rn / r0 < rtol && rn < atol) {
+            conv = true;
+            break;
+        }
+        CK(cudaGraphLaunch(S.pexec, S.stream));
+    }
+    *rnorm = rn;
+    *converged = conv;
+    return k;
+}
+
 mgmc_status mgmc_sampler_solve(mgmc_sampler *s, const double *b, double *x, double rtol, double atol, int maxiter,
                                int on_device, int *niter, double *rnorm, int *converged) {
     API_BEGIN
@@ -2284,34 +2344,62 @@ mgmc_status mgmc_sampler_solve(mgmc_sampler *s, const double *b, double *x, doub
     if (maxiter < 0) fail(MGMC_ERR_INVALID_ARGUMENT, "maxiter < 0");
     CK(cudaStreamSynchronize(S.stream));
     S.ensure_solver();
-    Level &l0 = S.L[0];
     int k = 0;
-    double r0 = 0.0, rn = -1.0;
+    double rn = -1.0;
     bool conv = false;
     {
         BorrowLevel0 borrow(S);
         put_vec(S, 0, b, on_device, S.sv_b, true);
-        CK(cudaMemsetAsync(S.sv_x, 0, (size_t)l0.geo.nalloc * sizeof(double), S.stream));  // loop_solver.cc:17
-        for (k = 0; k < maxiter; ++k) {
-            CK(cudaGraphLaunch(S.rexec, S.stream));
-            double r2 = 0.0;
-            CK(cudaMemcpyAsync(&r2, S.sv_norm, sizeof(double), cudaMemcpyDeviceToHost, S.stream));
-            CK(cudaStreamSynchronize(S.stream));
-            rn = std::sqrt(r2);
-            if (!std::isfinite(rn)) fail(MGMC_ERR_NONFINITE, "non-finite residual in the solver");
-            if (k == 0) r0 = rn;  // |A 0 - b| = |b| (loop_solver.cc:11)
-            if (rn / r0 < rtol && rn < atol) {
-                conv = true;
-                break;
-            }
-            CK(cudaGraphLaunch(S.pexec, S.stream));
-        }
+        k = loop_solve(S, rtol, atol, maxiter, &rn, &conv);
         get_vec(S, 0, S.sv_x, x, on_device, true);
     }
     check_device_errors(S);
     *niter = k;
     *rnorm = rn;
     *converged = conv ? 1 : 0;
+    API_END
+}
+
+mgmc_status mgmc_sampler_exact_sample(mgmc_sampler *s, const double *f, double *x, double rtol, int maxiter,
+                                      int on_device, int *niter) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    if (!f || !x) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    if (maxiter < 1 || !(rtol > 0.0)) fail(MGMC_ERR_INVALID_ARGUMENT, "maxiter >= 1 and rtol > 0 required");
+    CK(cudaStreamSynchronize(S.stream));
+    S.ensure_solver();
+    S.ensure_exact();
+    Level &l0 = S.L[0];
+    int k = 0;
+    double rn = -1.0;
+    bool conv = false;
+    {
+        BorrowLevel0 borrow(S);
+        put_vec(S, 0, f, on_device, S.sv_b, true);
+        NoiseArgs nz{};
+        nz.seed = S.P.seed;
+        nz.d_step = S.d_step;
+        if (l0.npt == 7)
+            k_prior_perturbation<7><<<pack_grid(l0), 256, 0, S.stream>>>(S.sv_b, l0.g, S.ew, nz);
+        else
+            k_prior_perturbation<27><<<pack_grid(l0), 256, 0, S.stream>>>(S.sv_b, l0.g, S.ew, nz);
+        if (S.m > 0) {
+            k_lowrank_perturbation<<<nblk(S.m, 256), 256, 0, S.stream>>>(nz, S.d_sigma_sqrt, S.m, S.ex_y);
+            launch_add_Bq<double>(S, l0, S.sv_b, S.ex_y, 1.0);
+        }
+        S.check_launch();
+        k = loop_solve(S, rtol, HUGE_VAL, maxiter, &rn, &conv);
+        if (!conv) fail(MGMC_ERR_NONFINITE, "exact sample: the solve did not reach the tolerance");
+        get_vec(S, 0, S.sv_x, x, on_device, true);
+        u64 step = 0;
+        CK(cudaMemcpyAsync(&step, S.d_step, sizeof(u64), cudaMemcpyDeviceToHost, S.stream));
+        CK(cudaStreamSynchronize(S.stream));
+        step += 1;  // the next sample draws new noise
+        CK(cudaMemcpyAsync(S.d_step, &step, sizeof(u64), cudaMemcpyHostToDevice, S.stream));
+        CK(cudaStreamSynchronize(S.stream));
+    }
+    check_device_errors(S);
+    if (niter) *niter = k;
     API_END
 }
 

@@ -67,7 +67,7 @@ struct StencilArg {
 
 // ---------------------------------------------------------------- noise
 enum { NOISE_NONE = 0, NOISE_PHILOX = 1, NOISE_INJECTED = 2 };
-enum { PURPOSE_POINT = 0, PURPOSE_LOWRANK = 1, PURPOSE_COARSE = 2 };
+enum { PURPOSE_POINT = 0, PURPOSE_LOWRANK = 1, PURPOSE_COARSE = 2, PURPOSE_EXACT = 3 };
 
 struct NoiseArgs {
     const double *buf;   // injected: normals for this consumer, index = vertex / column
@@ -1255,6 +1255,60 @@ __global__ void __launch_bounds__(256) k_solve_norm(const double *__restrict__ p
 template <typename T>
 __global__ void __launch_bounds__(256) k_solve_update(double *__restrict__ x, const T *__restrict__ dx, i64 n) {
     for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) x[i] += (double)dx[i];
+}
+
+// ------------------------------------------------------ exact sampler
+// A draw eta ~ N(0, A_0) for a symmetric stencil with non-positive
+// off-diagonal weights and a non-negative diagonal surplus
+// c_0 = w_c - sum_k |w_k|:  x^T A_0 x = c_0 |x|^2 + sum over edges (p, q) of
+// c_k (x_q - x_p)^2, one edge per pair of stencil neighbours in each of the
+// 13 directions k of positive linear offset, c_k = -w_k, and one boundary
+// edge (outside value zero) wherever a neighbour lies outside the lattice
+// (which keeps the diagonal of the Dirichlet operator).  So
+//   eta_p = sqrt(c_0) xi_p + sum_k sqrt(c_k) (xi_{k, p - o_k} - xi_{k, p}),
+// with independent normals xi on the points and on the edges (edge (r, r +
+// o_k) keyed by its lower end r, which may be a ghost position).  Philox
+// keys: the sampler's seed; counter (edge or point id, purpose EXACT,
+// direction k in the level byte, the step counter).  b += eta.
+struct EdgeWeights {
+    double c0;        // sqrt(c_0)
+    double ck[13];    // sqrt(c_k) for the directions of positive offset
+    int off[13][3];   // (dx, dy, dz) of direction k
+};
+
+__device__ __forceinline__ double exact_normal(const NoiseArgs &nz, int k, unsigned id) {
+    NoiseArgs a = nz;
+    a.level = (unsigned)k;
+    return (double)normals4(philox4x32_10(noise_ctr(a, id, PURPOSE_EXACT, 0), noise_key(a))).x;
+}
+
+template <int NPT>
+__global__ void __launch_bounds__(256) k_prior_perturbation(double *__restrict__ b, Grid3 g, EdgeWeights ew,
+                                                            NoiseArgs nz) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x, bb = blockIdx.y, c = blockIdx.z;
+    if (a >= g.N0) return;
+    // ids over positions (-1 .. N) in every direction
+    const unsigned X = (unsigned)g.N0 + 2u, Y = (unsigned)g.N1 + 2u;
+    auto id = [&](int pa, int pb, int pc) { return ((unsigned)(pc + 1) * Y + (unsigned)(pb + 1)) * X + (unsigned)(pa + 1); };
+    double eta = ew.c0 * exact_normal(nz, 0, id(a, bb, c));
+#pragma unroll
+    for (int k = 0; k < 13; ++k) {
+        const int dx = ew.off[k][0], dy = ew.off[k][1], dz = ew.off[k][2];
+        if (NPT == 7 && (dx != 0) + (dy != 0) + (dz != 0) > 1) continue;
+        if (ew.ck[k] == 0.0) continue;
+        eta += ew.ck[k] * (exact_normal(nz, k + 1, id(a - dx, bb - dy, c - dz)) - exact_normal(nz, k + 1, id(a, bb, c)));
+    }
+    b[g.pad(a, bb, c)] += eta;
+}
+
+// y_j = Sigma_j^{1/2} xi_j with m more normals (direction byte 14), so that
+// k_add_Bq (which divides by Sigma) adds B Sigma^{-1/2} xi: the low-rank
+// part of eta ~ N(0, A_0 + B Sigma^{-1} B^T).
+__global__ void __launch_bounds__(256) k_lowrank_perturbation(NoiseArgs nz, const double *__restrict__ sigma_sqrt, int m,
+                                                              double *__restrict__ y) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    y[j] = sigma_sqrt[j] * exact_normal(nz, 14, (unsigned)j);
 }
 
 // ------------------------------------------------ parameter adjoint
