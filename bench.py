@@ -492,6 +492,84 @@ def adjoint_study(nsteps=200, every=10, nfd=4, seed=7):
     return out
 
 
+def summary_study(sizes=(16, 32, 48, 64, 128), m=32, seed=1):
+    """The reference's published comparison (python/plot_summary.py:23-33:
+    IACT and time per independent sample of the Cholesky, Gibbs and MGMC
+    samplers on a 3D posterior at 16^3 .. 64^3 cells) on the GPU, plus
+    128^3: posterior kappa^2 = 10 with m ball measurements (centres
+    U[0.1, 0.9]^3, radius 0.05, Sigma = 1e-4, values N(0, 1)), observable
+    b^T x with b the measurement vector at the centre (sampling_time.cc:22-40).
+    MGMC: V(1,1) SSOR down to 8^3 cells (6^3 at 48^3); Gibbs: the one-level
+    SSOR sampler; exact: x = Q^{-1}(f + eta), one multigrid solve to 1e-10
+    per independent draw (the role of the Cholesky sampler, whose dense or
+    sparse factor does not reach these sizes here).  Time per independent
+    sample = ms per step x IACT; IACT windows grow to 10 IACT."""
+    import multigridmc_gb300 as M
+    levels = {16: 2, 32: 3, 48: 4, 64: 4, 96: 4, 128: 5}
+    rows = []
+    for N in sizes:
+        shape = (N, N, N)
+        rng = np.random.default_rng(seed)
+        loc = rng.uniform(0.1, 0.9, size=(m, 3))
+        y = rng.standard_normal(m)
+        op = M.LinearOperator.shifted_laplace_fd(shape, KAPPA_SQ).with_measurements(
+            loc, np.ones(m), variance_scaling=VARIANCE, radius=RADIUS)
+        f = np.zeros(op.n)
+        for j in range(op.m):
+            sl = slice(op.B_ptr[j], op.B_ptr[j + 1])
+            f[op.B_idx[sl]] += op.B_val[sl] * (y[j] / op.Sigma[j])
+        bidx, bval = M.measurement_vector(shape, [0.5, 0.5, 0.5], RADIUS)
+        row = {"cells": N, "unknowns": op.n}
+
+        def chain(params, prec, nsteps, warm):
+            s = M.MultigridMCSampler(op, params, precision=prec, seed=seed + 100)
+            s.fix_rhs(f)
+            s.step(warm)
+            s.set_observable(bidx, bval, nsteps + 8)
+            s.synchronize()
+            t0 = time.perf_counter()
+            s.step(nsteps)
+            s.synchronize()
+            dt = (time.perf_counter() - t0) / nsteps
+            z = s.read_observations(nsteps + 8)[:nsteps]
+            s.close()
+            K = 50
+            tau = M.statistics.tau_int(z, K)
+            while K < 10 * tau and 10 * tau < len(z) / 20:
+                K = int(10 * tau) + 1
+                tau = M.statistics.tau_int(z, K)
+            return {"ms_per_step": dt * 1e3, "iact": tau, "window": K, "steps": nsteps,
+                    "ms_per_indep": dt * 1e3 * max(tau, 1.0)}
+
+        mg = M.MultigridParameters(nlevel=levels[N])
+        gibbs = M.MultigridParameters(nlevel=1, coarse_solver="SSOR", ncoarsesmooth=1)
+        row["mgmc_fp64"] = chain(mg, M.FP64, 4000, 100)
+        row["mgmc_fp32"] = chain(mg, M.FP32_MIXED, 4000, 100)
+        gsteps = 100000 if N >= 128 else 50000
+        row["gibbs_fp64"] = chain(gibbs, M.FP64, gsteps, 2000)
+        if N < 128:
+            row["gibbs_fp32"] = chain(gibbs, M.FP32_MIXED, gsteps, 2000)
+        import torch
+        fd = torch.from_numpy(np.asarray(f, np.float64)).cuda()
+        xd = torch.empty_like(fd)
+        torch.cuda.synchronize()
+        for name, prec in (("exact_fp32", M.FP32_MIXED), ("exact_fp64", M.FP64)):
+            s = M.MultigridMCSampler(op, mg, precision=prec, seed=seed + 200)
+            for _ in range(3):
+                s.exact_sample_device(fd.data_ptr(), xd.data_ptr())
+            ns = 40
+            its = 0
+            t0 = time.perf_counter()
+            for _ in range(ns):
+                its += s.exact_sample_device(fd.data_ptr(), xd.data_ptr())
+            dt = (time.perf_counter() - t0) / ns
+            s.close()
+            row[name] = {"ms_per_sample": dt * 1e3, "iterations": its / ns, "ms_per_indep": dt * 1e3}
+        rows.append(row)
+        print(json.dumps({"summary_row": row}), flush=True)
+    return rows
+
+
 def solve_study(rtol=1e-10, repeats=3):
     """The reference's deterministic multigrid solve (driver_mg: LoopSolver
     with MultigridPreconditioner) of Q x = f on the 256^3 posterior: FP64
@@ -648,6 +726,8 @@ def main():
                     help="run measure_convergence over NCHAIN batched chains (--steps steps) instead of the benchmark")
     ap.add_argument("--adjoint-study", action="store_true",
                     help="run the 128^3 differentiation study (parameter adjoint with checkpoints, FD checks)")
+    ap.add_argument("--summary-study", action="store_true",
+                    help="MGMC vs Gibbs vs exact sampler at 16^3 .. 128^3 (the reference's summary comparison)")
     ap.add_argument("--solve-study", action="store_true",
                     help="time the deterministic multigrid solve of Q x = f instead of the benchmark")
     ap.add_argument("--profile-steps", type=int, default=0, metavar="K",
@@ -666,6 +746,9 @@ def main():
         return
     if args.adjoint_study:
         print(json.dumps({"adjoint_study": adjoint_study()}), flush=True)
+        return
+    if args.summary_study:
+        print(json.dumps({"summary_study": summary_study()}), flush=True)
         return
     if args.solve_study:
         print(json.dumps({"solve_study": solve_study()}), flush=True)
