@@ -52,7 +52,7 @@
 extern "C" {
 #endif
 
-#define MGMC_ABI_VERSION 1
+#define MGMC_ABI_VERSION 2
 
 typedef enum mgmc_status {
     MGMC_OK = 0,
@@ -96,6 +96,13 @@ typedef struct mgmc_operator_desc {
     const int64_t *B_rowidx; /* vertex indices in the reference's order */
     const double *B_val;
     const double *Sigma;     /* m diagonal entries of the measurement covariance */
+    /* Optional per-vertex centre weight of the fine stencil (n values in the
+     * reference's vertex order), replacing stencil[13]: the FD prior with a
+     * variable correlation length, diagonal h^d kappa^2(x) + sum_d 2 h^d / h_d^2
+     * (shiftedlaplace_fd_operator.cc:33-52, correlationlength_model.hh:83-112).
+     * The coarse levels then carry per-point 27-point Galerkin stencils.
+     * Needs dim >= 2 and MGMC_ORDER_MULTICOLOUR; NULL for a constant stencil. */
+    const double *centre;
 } mgmc_operator_desc;
 
 /* Sampler parameters: MultigridParameters plus the GB300 execution choices. */

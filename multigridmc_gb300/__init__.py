@@ -65,7 +65,8 @@ class _OpDesc(C.Structure):
     _fields_ = [("dim", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
                 ("stencil", C.c_double * 27), ("m", C.c_int),
                 ("B_colptr", C.POINTER(C.c_int64)), ("B_rowidx", C.POINTER(C.c_int64)),
-                ("B_val", C.POINTER(C.c_double)), ("Sigma", C.POINTER(C.c_double))]
+                ("B_val", C.POINTER(C.c_double)), ("Sigma", C.POINTER(C.c_double)),
+                ("centre", C.POINTER(C.c_double))]
 
 
 class _Params(C.Structure):
@@ -224,6 +225,7 @@ class LinearOperator:
     B_idx: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
     B_val: np.ndarray = field(default_factory=lambda: np.zeros(0))
     Sigma: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    centre: np.ndarray = None  # per-vertex centre weight of the stencil (variable coefficients), or None
 
     @property
     def dim(self):
@@ -244,6 +246,37 @@ class LinearOperator:
             kappa_sq = 1.0 / Lambda ** 2
         return cls(tuple(int(s) for s in shape), fd_stencil(shape, kappa_sq))
 
+    @staticmethod
+    def periodic_kappa_sq(shape, Lambda_min, Lambda_max):
+        """kappa^2(x) = 1 / Lambda(x)^2 at the vertices, Lambda(x) = Lambda_1 +
+        Lambda_2 prod_d cos(pi x_d), Lambda_1,2 = (Lambda_max +- Lambda_min) / 2
+        (PeriodicCorrelationLengthModel, correlationlength_model.hh:83-112);
+        vertex i (0-based) of a direction with n cells at x = (i + 1) / n."""
+        L1, L2 = 0.5 * (Lambda_max + Lambda_min), 0.5 * (Lambda_max - Lambda_min)
+        axes = [np.cos(np.pi * (np.arange(c - 1) + 1.0) / c) for c in shape]
+        lam = np.full([c - 1 for c in shape[::-1]], L2)
+        for d, a in enumerate(axes):  # x fastest: the last array axis
+            sh = [1] * len(shape)
+            sh[len(shape) - 1 - d] = a.size
+            lam = lam * a.reshape(sh)
+        lam = lam + L1
+        return (1.0 / (lam * lam)).reshape(-1)
+
+    @classmethod
+    def shifted_laplace_fd_periodic(cls, shape, Lambda_min, Lambda_max):
+        """ShiftedLaplaceFDOperator with the periodic correlation length: the
+        neighbour weights -h^d / h_d^2 and the per-vertex diagonal
+        h^d kappa^2(x) + sum_d 2 h^d / h_d^2 (shiftedlaplace_fd_operator.cc:33-52)."""
+        shape = tuple(int(s) for s in shape)
+        st = fd_stencil(shape, 0.0)
+        hd = 1.0
+        for c in shape:
+            hd *= 1.0 / c
+        diag = hd * cls.periodic_kappa_sq(shape, Lambda_min, Lambda_max)
+        for c in shape:
+            diag = diag + 2.0 * hd * (c * c)
+        return cls(shape, st, centre=diag)
+
     def with_lowrank(self, Bdense_or_cols, Sigma):
         """Attach B (dense n x m array, or list of (idx, val) columns) and Sigma."""
         cols = Bdense_or_cols
@@ -256,7 +289,7 @@ class LinearOperator:
             val.extend(np.asarray(v, np.float64)[order].tolist())
             ptr.append(len(idx))
         return LinearOperator(self.shape, self.stencil, np.array(ptr, np.int64), np.array(idx, np.int64),
-                              np.array(val, np.float64), _f64(Sigma))
+                              np.array(val, np.float64), _f64(Sigma), self.centre)
 
     def with_measurements(self, locations, variance, variance_scaling=1.0, radius=0.05, measure_global=False,
                           variance_global=0.0):
@@ -293,6 +326,8 @@ class LinearOperator:
                     cols.append(dst.ravel())
                     vals.append(np.full(src.size, w))
         A = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
+        if self.centre is not None:
+            A = (A + sp.diags(np.asarray(self.centre, np.float64) - float(self.stencil[13]))).tocsr()
         if self.m > 0:
             Bs = sp.csc_matrix((self.B_val, self.B_idx, self.B_ptr), shape=(n, self.m))
             A = (A + Bs @ sp.diags(1.0 / self.Sigma) @ Bs.T).tocsr()
@@ -317,6 +352,12 @@ class LinearOperator:
         d.B_rowidx = self._keep[1].ctypes.data_as(_I64)
         d.B_val = self._keep[2].ctypes.data_as(_D)
         d.Sigma = self._keep[3].ctypes.data_as(_D)
+        if self.centre is not None:
+            c = _f64(self.centre)
+            if c.size != self.n:
+                raise ValueError("centre needs one weight per vertex")
+            self._keep = self._keep + (c,)
+            d.centre = c.ctypes.data_as(_D)
         return d
 
 

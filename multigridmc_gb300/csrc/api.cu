@@ -92,7 +92,19 @@ struct Level {
     void *adj[4] = {nullptr, nullptr, nullptr, nullptr};  // adjoint: x-bar, f-bar, two work vectors (T, padded)
     CUtensorMap xmap{}, fmap{};  // 3D tile maps of x and f for the residual-restriction
     bool tma = false;            // maps valid (3D, rows of a multiple of 16 bytes)
+    // variable coefficients: 0 the constant stencil st; 1 a per-point centre
+    // weight (the fine level of a variable-coefficient prior); 2 a per-point
+    // 27-point stencil (its Galerkin coarse levels), weight-major with stride nalloc
+    int var = 0;
+    void *vw = nullptr;        // the field in the level's type (padded, ghosts zero)
+    double *vw64 = nullptr;    // FP64 copy of a level-0 centre field (solver, exact sampler)
+    std::vector<double> vh;    // host field, compact: n centre weights or 27 x n weights
 };
+
+template <typename T>
+static VarField<T> var_field(const Level &lv) {
+    return VarField<T>{(const T *)lv.vw, lv.geo.nalloc};
+}
 
 struct Sampler {
     mgmc_sampler_params P;
@@ -210,6 +222,7 @@ struct Sampler {
     int pa_calls = 0;
     void ensure_param_adjoint();
     void param_adjoint_pass();
+    void upload_field(Level &lv);
     void *tape_snap(int lev, const void *src);
     void *tape_state(int lev);
     TapeEvent tape_pop(int kind, int lev, bool forward);
@@ -223,6 +236,7 @@ struct Sampler {
     template <typename T>
     void adjoint_sample(int lev);
     void build_coarse();
+    std::vector<double> level_precision(const Level &lv) const;
     void launch_step();
     void sor(int lev, bool forward, bool noisy, void *x, void *f, int nsparse = 1);
     void smooth(int lev, bool forward, int nsmooth);
@@ -231,6 +245,7 @@ struct Sampler {
     void ensure_solver_buffers();
     // exact sampler: x = Q^{-1}(f + eta), eta ~ N(0, Q), by the loop solver
     EdgeWeights ew{};
+    double ex_offsum = 0.0;  // sum of |off-diagonal weights| of the fine stencil
     bool ew_ready = false;
     double *ex_y = nullptr;
     void ensure_exact();
@@ -251,6 +266,7 @@ static StencilArg<T> stencil_arg(const Level &lv, double omega) {
     s.omega = (T)omega;
     s.sd = (T)lv.sd;
     s.omega_diag = (T)(omega / lv.diag);
+    s.tmo = (T)(2. - omega);
     return s;
 }
 
@@ -342,7 +358,12 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
                     const int ngrp = (lv.g.N0 + 8) / 8;
                     const dim3 blk = level_block(lv, ngrp);
                     dim3 grid((ngrp + blk.x - 1) / blk.x, (lv.g.N1 + blk.y - 1) / blk.y, lv.g.N2);
-                    plaunch(S.pdl && lv.g.pdl, k_sweep_rb_vec<NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
+                    if (lv.var == 1)
+                        plaunch(S.pdl && lv.g.pdl, k_sweep_rb_vec<NOISE, true>, grid, blk, 0, S.stream, x, f, lv.g, s, colour,
+                                pass, nz, (const float *)lv.vw);
+                    else
+                        plaunch(S.pdl && lv.g.pdl, k_sweep_rb_vec<NOISE, false>, grid, blk, 0, S.stream, x, f, lv.g, s, colour,
+                                pass, nz, (const float *)nullptr);
                     S.launches++;
                     continue;
                 }
@@ -351,7 +372,16 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
                 const int na = (lv.g.N0 + 1) / 2;
                 const dim3 blk = level_block(lv, na);
                 dim3 grid((na + blk.x - 1) / blk.x, (lv.g.N1 + blk.y - 1) / blk.y, lv.g.N2);
-                plaunch(S.pdl && lv.g.pdl, k_sweep_rb_pass<T, EXACT, NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz);
+                const VarField<T> vf = var_field<T>(lv);
+                if (lv.var == 1)
+                    plaunch(S.pdl && lv.g.pdl, k_sweep_rb_pass<T, EXACT, NOISE, 1>, grid, blk, 0, S.stream, x, f, lv.g, s, colour,
+                            pass, nz, vf);
+                else if (lv.var == 2)
+                    plaunch(S.pdl && lv.g.pdl, k_sweep_rb_pass<T, EXACT, NOISE, 2>, grid, blk, 0, S.stream, x, f, lv.g, s, colour,
+                            pass, nz, vf);
+                else
+                    plaunch(S.pdl && lv.g.pdl, k_sweep_rb_pass<T, EXACT, NOISE, 0>, grid, blk, 0, S.stream, x, f, lv.g, s, colour,
+                            pass, nz, vf);
             }
             S.launches++;
         }
@@ -371,7 +401,13 @@ static void launch_colour_passes(Sampler &S, const Level &lv, bool forward, T *x
         if (na <= 0 || nb <= 0 || nc <= 0) continue;
         const dim3 blk = level_block(lv, na);
         dim3 grid((na + blk.x - 1) / blk.x, (nb + blk.y - 1) / blk.y, nc);
-        plaunch(S.pdl && lv.g.pdl, k_sweep_c27_pass<T, EXACT, NOISE>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, nz);
+        const VarField<T> vf = var_field<T>(lv);
+        if (lv.var == 2)
+            plaunch(S.pdl && lv.g.pdl, k_sweep_c27_pass<T, EXACT, NOISE, 2>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, nz, vf);
+        else if (lv.var == 1)
+            plaunch(S.pdl && lv.g.pdl, k_sweep_c27_pass<T, EXACT, NOISE, 1>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, nz, vf);
+        else
+            plaunch(S.pdl && lv.g.pdl, k_sweep_c27_pass<T, EXACT, NOISE, 0>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, nz, vf);
         S.launches++;
     }
 }
@@ -513,6 +549,21 @@ static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void
     if (zero_stencil)
         for (int k = 0; k < 27; ++k) s.w[k] = T(0);
     const i64 nc = lc.geo.n;
+    if (lv.var && !zero_stencil) {  // variable coefficients: the plain fused kernel
+        const VarField<T> vf = var_field<T>(lv);
+        const bool pdl = S.pdl && lv.g.pdl;
+        if (lv.npt == 7 && lv.var == 1)
+            plaunch(pdl, k_resid_restrict<T, 7, 1>, nblk(nc, 256), 256, 0, S.stream, (const T *)x, (const T *)f, (T *)fc, (T *)xc,
+                    lv.g, lc.g, s, S.dim, vf);
+        else if (lv.var == 1)
+            plaunch(pdl, k_resid_restrict<T, 27, 1>, nblk(nc, 256), 256, 0, S.stream, (const T *)x, (const T *)f, (T *)fc, (T *)xc,
+                    lv.g, lc.g, s, S.dim, vf);
+        else
+            plaunch(pdl, k_resid_restrict<T, 27, 2>, nblk(nc, 256), 256, 0, S.stream, (const T *)x, (const T *)f, (T *)fc, (T *)xc,
+                    lv.g, lc.g, s, S.dim, vf);
+        S.launches++;
+        return;
+    }
     if (S.dim == 3 && !zero_stencil && lv.tma && x == lv.x && f == lv.f) {
         dim3 grid((lc.g.N0 + RR_TX - 1) / RR_TX, (lc.g.N1 + RR_TY - 1) / RR_TY, (lc.g.N2 + RR_TZ - 1) / RR_TZ);
         const size_t sm = rr_tma_smem_bytes<T>();
@@ -535,10 +586,11 @@ static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void
         S.launches++;
         return;
     }
+    const VarField<T> vf0{nullptr, 0};
     if (lv.npt == 7 && !zero_stencil)
-        plaunch(S.pdl && lv.g.pdl, k_resid_restrict<T, 7>, nblk(nc, 256), 256, 0, S.stream, (const T *)x, (const T *)f, (T *)fc, (T *)xc, lv.g, lc.g, s, S.dim);
+        plaunch(S.pdl && lv.g.pdl, k_resid_restrict<T, 7, 0>, nblk(nc, 256), 256, 0, S.stream, (const T *)x, (const T *)f, (T *)fc, (T *)xc, lv.g, lc.g, s, S.dim, vf0);
     else
-        plaunch(S.pdl && lv.g.pdl, k_resid_restrict<T, 27>, nblk(nc, 256), 256, 0, S.stream, (const T *)x, (const T *)f, (T *)fc, (T *)xc, lv.g, lc.g, s, S.dim);
+        plaunch(S.pdl && lv.g.pdl, k_resid_restrict<T, 27, 0>, nblk(nc, 256), 256, 0, S.stream, (const T *)x, (const T *)f, (T *)fc, (T *)xc, lv.g, lc.g, s, S.dim, vf0);
     S.launches++;
 }
 
@@ -886,11 +938,21 @@ void Sampler::build_lowrank(int lev) {
     CK(cudaStreamSynchronize(stream));
 }
 
+// dense A_0 + B Sigma^{-1} B^T of a level (constant stencil or field)
+std::vector<double> Sampler::level_precision(const Level &lv) const {
+    if (!lv.var) return dense_precision(lv.geo, lv.st, lv.Bh, Sigma);
+    if (lv.var == 2) return dense_precision_field(lv.geo, lv.vh, lv.Bh, Sigma);
+    std::vector<double> full((size_t)27 * lv.geo.n);
+    for (int k = 0; k < 27; ++k)
+        for (i64 i = 0; i < lv.geo.n; ++i) full[(size_t)k * lv.geo.n + i] = k == 13 ? lv.vh[i] : lv.st[k];
+    return dense_precision_field(lv.geo, full, lv.Bh, Sigma);
+}
+
 void Sampler::build_coarse() {
     Level &lv = L.back();
     const i64 n = lv.geo.n;
     if (n > 12000) fail(MGMC_ERR_UNSUPPORTED, "coarse level has " + std::to_string(n) + " unknowns; the dense Cholesky sampler takes at most 12000");
-    std::vector<double> Q = dense_precision(lv.geo, lv.st, lv.Bh, Sigma);
+    std::vector<double> Q = level_precision(lv);
     if (!dense_cholesky(Q, n)) fail(MGMC_ERR_NOT_SPD, "coarse precision matrix is not positive definite");
     dgv = alloc<double>(n);
     chol_smem = (size_t)n * sizeof(double);
@@ -992,6 +1054,9 @@ void Sampler::build(const mgmc_operator_desc &op) {
     if (op.m < 0 || (op.m > 0 && (!op.B_colptr || !op.B_rowidx || !op.B_val || !op.Sigma)))
         fail(MGMC_ERR_INVALID_ARGUMENT, "low-rank term needs B and Sigma");
     if (op.m > 3072) fail(MGMC_ERR_UNSUPPORTED, "at most 3072 measurement columns");
+    if (op.centre && op.dim < 2) fail(MGMC_ERR_UNSUPPORTED, "a per-vertex centre weight needs dim >= 2");
+    if (op.centre && P.ordering != MGMC_ORDER_MULTICOLOUR)
+        fail(MGMC_ERR_UNSUPPORTED, "a per-vertex centre weight needs the multicolour ordering");
     fp32 = P.precision == MGMC_FP32_MIXED;
     noise_mode = P.noise == MGMC_NOISE_INJECTED ? NOISE_INJECTED : NOISE_PHILOX;
     exact = !fp32 && noise_mode == NOISE_INJECTED;
@@ -1038,6 +1103,29 @@ void Sampler::build(const mgmc_operator_desc &op) {
         lv.g.sz = geo.sz;
         std::memcpy(lv.st, st, sizeof(st));
         lv.diag = st[13];
+        if (op.centre) {
+            // variable coefficients: level 0 keeps the centre weights, every
+            // coarser level the Galerkin product of the level above
+            if (lev == 0) {
+                lv.var = 1;
+                lv.vh.assign(op.centre, op.centre + geo.n);
+            } else {
+                Level &lf = L[lev - 1];
+                lv.var = 2;
+                lv.vh = galerkin_field(lf.geo, lf.st, lf.var == 1 ? lf.vh.data() : nullptr,
+                                       lf.var == 2 ? lf.vh.data() : nullptr);
+                if (lev > 1) std::vector<double>().swap(lf.vh);  // only the fine centre and the coarsest field stay
+            }
+            double dmin = HUGE_VAL, dsum = 0.0;
+            const double *dp = lv.var == 1 ? lv.vh.data() : lv.vh.data() + (size_t)13 * geo.n;
+            for (i64 i = 0; i < geo.n; ++i) {
+                dmin = std::min(dmin, dp[i]);
+                dsum += dp[i];
+            }
+            if (!(dmin > 0.0)) fail(MGMC_ERR_NOT_SPD, "stencil diagonal must be positive");
+            lv.diag = dsum / (double)geo.n;  // a representative value; the kernels read the field
+            upload_field(lv);
+        }
         if (!(lv.diag > 0.0)) fail(MGMC_ERR_NOT_SPD, "stencil diagonal must be positive");
         lv.sd = std::sqrt(lv.diag * (2. - P.omega) / P.omega);
         lv.ncol = colour_count(dim, st);
@@ -1046,7 +1134,7 @@ void Sampler::build(const mgmc_operator_desc &op) {
         // the coarser levels; the many-CTA kernels of large levels run
         // without its per-CTA wait
         lv.g.pdl = geo.n <= PDL_MAX_POINTS ? 1 : 0;
-        L.push_back(lv);
+        L.push_back(std::move(lv));
     }
     for (auto &lv : L) {
         lv.x = talloc(lv.geo.nalloc);
@@ -1119,6 +1207,23 @@ void Sampler::build(const mgmc_operator_desc &op) {
     autotune_sweeps();
     CK(cudaStreamSynchronize(stream));
     check_launch();
+}
+
+// A level's host field to the device: padded, the level's type (and for a
+// level-0 centre field an FP64 copy as well); ghosts stay zero.
+void Sampler::upload_field(Level &lv) {
+    const i64 n = lv.geo.n, na = lv.geo.nalloc;
+    const int planes = lv.var == 1 ? 1 : 27;
+    std::vector<double> pad((size_t)planes * na, 0.0);
+    for (int k = 0; k < planes; ++k)
+        for (i64 i = 0; i < n; ++i) pad[(size_t)k * na + lv.geo.pad(i)] = lv.vh[(size_t)k * n + i];
+    if (fp32) {
+        std::vector<float> pf(pad.begin(), pad.end());
+        lv.vw = upload(pf);
+    } else {
+        lv.vw = upload(pad);
+    }
+    if (lv.var == 1) lv.vw64 = fp32 ? upload(pad) : (double *)lv.vw;
 }
 
 // Autotuner of the colour passes' CTA shape: for every level that sweeps,
@@ -1326,10 +1431,17 @@ void Sampler::ensure_solver() {
     if (!rexec)
         capture(rgraph, rexec, [&]() {
             const StencilArg<double> st = stencil_arg<double>(l0, P.omega);
-            if (l0.npt == 7)
-                k_solve_resid<7><<<pack_grid(l0), 256, 0, stream>>>(sv_x, sv_b, sv_r, l0.g, st);
-            else
-                k_solve_resid<27><<<pack_grid(l0), 256, 0, stream>>>(sv_x, sv_b, sv_r, l0.g, st);
+            const VarField<double> vf{l0.vw64, l0.geo.nalloc};
+            if (l0.var == 1) {
+                if (l0.npt == 7)
+                    k_solve_resid<7, 1><<<pack_grid(l0), 256, 0, stream>>>(sv_x, sv_b, sv_r, l0.g, st, vf);
+                else
+                    k_solve_resid<27, 1><<<pack_grid(l0), 256, 0, stream>>>(sv_x, sv_b, sv_r, l0.g, st, vf);
+            } else if (l0.npt == 7) {
+                k_solve_resid<7, 0><<<pack_grid(l0), 256, 0, stream>>>(sv_x, sv_b, sv_r, l0.g, st, vf);
+            } else {
+                k_solve_resid<27, 0><<<pack_grid(l0), 256, 0, stream>>>(sv_x, sv_b, sv_r, l0.g, st, vf);
+            }
             if (m > 0) {
                 launch_bt_plain<double>(*this, l0, sv_x);
                 launch_add_Bq<double>(*this, l0, sv_r, l0.y, -1.0);
@@ -1366,9 +1478,14 @@ void Sampler::ensure_exact() {
             fail(MGMC_ERR_UNSUPPORTED, "the exact sampler needs a symmetric stencil with non-positive off-diagonal weights");
         off -= w[k];
     }
-    double c0 = w[13] - off;
-    if (c0 < -1e-12 * w[13]) fail(MGMC_ERR_UNSUPPORTED, "the exact sampler needs a weakly diagonally dominant stencil");
-    ew.c0 = std::sqrt(std::max(c0, 0.0));
+    double cmin = w[13];
+    if (L[0].var == 1)
+        for (double d : L[0].vh) cmin = std::min(cmin, d);
+    else if (L[0].var == 2)
+        fail(MGMC_ERR_UNSUPPORTED, "the exact sampler needs constant off-diagonal weights");
+    if (cmin - off < -1e-12 * cmin) fail(MGMC_ERR_UNSUPPORTED, "the exact sampler needs a weakly diagonally dominant stencil");
+    ew.c0 = std::sqrt(std::max(w[13] - off, 0.0));
+    ex_offsum = off;
     for (int k = 14; k < 27; ++k) {
         ew.ck[k - 14] = std::sqrt(-w[k]);
         ew.off[k - 14][0] = k % 3 - 1;
@@ -1426,6 +1543,20 @@ static void adj_axpy(Sampler &S, const Level &lv, void *y, const void *x, double
     plaunch(false, k_axpy<T>, blocks, 256, 0, S.stream, (T *)y, (const T *)x, (T)alpha, (i64)lv.geo.nalloc);
 }
 
+// y = A_0 x on a level (constant or variable stencil)
+template <typename T>
+static void launch_apply_stencil(Sampler &S, const Level &lv, const void *x, void *y) {
+    const StencilArg<T> s = stencil_arg<T>(lv, S.P.omega);
+    const VarField<T> vf = var_field<T>(lv);
+    const unsigned nb = nblk(lv.geo.n, 256);
+    if (lv.var == 1)
+        plaunch(false, k_apply_stencil<T, 1>, nb, 256, 0, S.stream, (const T *)x, (T *)y, lv.g, s, vf);
+    else if (lv.var == 2)
+        plaunch(false, k_apply_stencil<T, 2>, nb, 256, 0, S.stream, (const T *)x, (T *)y, lv.g, s, vf);
+    else
+        plaunch(false, k_apply_stencil<T, 0>, nb, 256, 0, S.stream, (const T *)x, (T *)y, lv.g, s, vf);
+}
+
 // out = M^{-T} v for the sweep of direction `forward` on level lev
 template <typename T>
 static void adj_msolve(Sampler &S, int lev, bool forward, const void *v, void *out) {
@@ -1438,8 +1569,7 @@ static void adj_msolve(Sampler &S, int lev, bool forward, const void *v, void *o
 
 template <typename T>
 static void adj_apply_a0(Sampler &S, Level &lv, const void *x, void *y) {
-    plaunch(false, k_apply_stencil<T>, nblk(lv.geo.n, 256), 256, 0, S.stream, (const T *)x, (T *)y, lv.g,
-            stencil_arg<T>(lv, S.P.omega));
+    launch_apply_stencil<T>(S, lv, x, y);
 }
 
 // adjoint of one SOR sweep of direction `forward` with its low-rank
@@ -1565,6 +1695,8 @@ Sampler::TapeEvent Sampler::tape_pop(int kind, int lev, bool forward) {
 void Sampler::ensure_param_adjoint() {
     ensure_adjoint();
     if (pa_gs) return;
+    for (const auto &lv : L)
+        if (lv.var) fail(MGMC_ERR_UNSUPPORTED, "parameter derivatives need a constant stencil");
     const int nl = (int)L.size();
     pa_E.assign(nl, std::array<double, 27>{});
     pa_E[0][13] = 1.0;
@@ -2101,13 +2233,13 @@ mgmc_status mgmc_level_apply(mgmc_sampler *s, int level, const double *x, double
     Level &lv = S.L[level];
     put_vec(S, level, x, 0, lv.s1);
     if (S.fp32) {
-        k_apply_stencil<float><<<nblk(lv.geo.n, 256), 256, 0, S.stream>>>((const float *)lv.s1, (float *)lv.s2, lv.g, stencil_arg<float>(lv, S.P.omega));
+        launch_apply_stencil<float>(S, lv, lv.s1, lv.s2);
         if (S.m > 0 && lv.Bptr) {
             launch_bt_plain<float>(S, lv, lv.s1);
             launch_add_Bq<float>(S, lv, lv.s2, lv.y, 1.0);
         }
     } else {
-        k_apply_stencil<double><<<nblk(lv.geo.n, 256), 256, 0, S.stream>>>((const double *)lv.s1, (double *)lv.s2, lv.g, stencil_arg<double>(lv, S.P.omega));
+        launch_apply_stencil<double>(S, lv, lv.s1, lv.s2);
         if (S.m > 0 && lv.Bptr) {
             launch_bt_plain<double>(S, lv, lv.s1);
             launch_add_Bq<double>(S, lv, lv.s2, lv.y, 1.0);
@@ -2379,10 +2511,11 @@ mgmc_status mgmc_sampler_exact_sample(mgmc_sampler *s, const double *f, double *
         NoiseArgs nz{};
         nz.seed = S.P.seed;
         nz.d_step = S.d_step;
+        const double *cdiag = l0.var == 1 ? l0.vw64 : nullptr;
         if (l0.npt == 7)
-            k_prior_perturbation<7><<<pack_grid(l0), 256, 0, S.stream>>>(S.sv_b, l0.g, S.ew, nz);
+            k_prior_perturbation<7><<<pack_grid(l0), 256, 0, S.stream>>>(S.sv_b, l0.g, S.ew, nz, cdiag, S.ex_offsum);
         else
-            k_prior_perturbation<27><<<pack_grid(l0), 256, 0, S.stream>>>(S.sv_b, l0.g, S.ew, nz);
+            k_prior_perturbation<27><<<pack_grid(l0), 256, 0, S.stream>>>(S.sv_b, l0.g, S.ew, nz, cdiag, S.ex_offsum);
         if (S.m > 0) {
             k_lowrank_perturbation<<<nblk(S.m, 256), 256, 0, S.stream>>>(nz, S.d_sigma_sqrt, S.m, S.ex_y);
             launch_add_Bq<double>(S, l0, S.sv_b, S.ex_y, 1.0);

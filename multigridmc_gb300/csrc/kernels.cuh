@@ -63,7 +63,25 @@ struct StencilArg {
     T omega;
     T sd;         // sqrt(diag (2 - omega) / omega): noise scale (sor_sampler.cc:20-27)
     T omega_diag; // omega / diag
+    T tmo;        // 2 - omega (per-point noise scales of variable stencils)
 };
+
+// Per-point stencil of a level with variable coefficients.  VAR == 1: w[P]
+// (padded index) is the centre weight, the other weights are the constant
+// ones of StencilArg; VAR == 2: w[k * stride + P] is weight k.  VAR == 0:
+// the constant StencilArg alone.
+template <typename T>
+struct VarField {
+    const T *w;
+    i64 stride;
+};
+
+template <typename T, int VAR>
+__device__ __forceinline__ T vweight(const StencilArg<T> &s, const VarField<T> &vf, i64 P, int k) {
+    if (VAR == 2) return vf.w[(i64)k * vf.stride + P];
+    if (VAR == 1 && k == 13) return vf.w[P];
+    return s.w[k];
+}
 
 // ---------------------------------------------------------------- noise
 enum { NOISE_NONE = 0, NOISE_PHILOX = 1, NOISE_INJECTED = 2 };
@@ -166,15 +184,16 @@ struct Ar<false> {
 //   c = sd * xi + f;  res = sum_k w_k x_k (ascending index, diagonal
 //   included);  x += omega * (c - res) / diag.
 // Row P of A_0 x: sum_k w_k x_k in ascending index order, diagonal included.
-template <typename T, int NPT, bool EXACT>
-__device__ __forceinline__ T stencil_row(const T *__restrict__ x, const Grid3 &g, const StencilArg<T> &s, i64 P) {
+template <typename T, int NPT, bool EXACT, int VAR = 0>
+__device__ __forceinline__ T stencil_row(const T *__restrict__ x, const Grid3 &g, const StencilArg<T> &s, i64 P,
+                                         const VarField<T> &vf = VarField<T>{nullptr, 0}) {
     typedef Ar<EXACT> A;
     T res = T(0);
     if (NPT == 7) {
         const int ks[7] = {4, 10, 12, 13, 14, 16, 22};
         const i64 os[7] = {-g.sz, -g.sy, -1, 0, 1, g.sy, g.sz};
 #pragma unroll
-        for (int q = 0; q < 7; ++q) res = A::add(res, A::mul(s.w[ks[q]], x[P + os[q]]));
+        for (int q = 0; q < 7; ++q) res = A::add(res, A::mul(vweight<T, VAR>(s, vf, P, ks[q]), x[P + os[q]]));
     } else {
 #pragma unroll
         for (int dz = -1; dz <= 1; ++dz)
@@ -182,23 +201,40 @@ __device__ __forceinline__ T stencil_row(const T *__restrict__ x, const Grid3 &g
             for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
                 for (int dx = -1; dx <= 1; ++dx)
-                    res = A::add(res, A::mul(s.w[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)], x[P + dz * g.sz + dy * g.sy + dx]));
+                    res = A::add(res, A::mul(vweight<T, VAR>(s, vf, P, (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)),
+                                             x[P + dz * g.sz + dy * g.sy + dx]));
     }
     return res;
 }
 
-template <typename T, int NPT, bool EXACT>
+// With a variable stencil (VAR != 0) the diagonal, the noise scale
+// sqrt(d (2 - omega) / omega) and omega / d are formed per point, in the
+// oracle's operation order on the parity path.
+template <typename T, int NPT, bool EXACT, int VAR = 0>
 __device__ __forceinline__ void sor_point(T *__restrict__ x, const T *__restrict__ f, const Grid3 &g,
-                                          const StencilArg<T> &s, i64 P, bool noisy, T xi) {
+                                          const StencilArg<T> &s, i64 P, bool noisy, T xi,
+                                          const VarField<T> &vf = VarField<T>{nullptr, 0}) {
     typedef Ar<EXACT> A;
-    const T res = stencil_row<T, NPT, EXACT>(x, g, s, P);
+    const T res = stencil_row<T, NPT, EXACT, VAR>(x, g, s, P, vf);
     T cval = f[P];
-    if (noisy) cval = A::add(A::mul(s.sd, xi), cval);
     T xo = x[P];
-    if (EXACT)
-        x[P] = A::add(xo, A::mul(s.omega, A::sub(cval, res)) / s.diag);
-    else
-        x[P] = xo + s.omega_diag * (cval - res);
+    if (VAR == 0) {
+        if (noisy) cval = A::add(A::mul(s.sd, xi), cval);
+        if (EXACT)
+            x[P] = A::add(xo, A::mul(s.omega, A::sub(cval, res)) / s.diag);
+        else
+            x[P] = xo + s.omega_diag * (cval - res);
+    } else {
+        const T d = vweight<T, VAR>(s, vf, P, 13);
+        if (noisy) {
+            const T sd = sqrt(A::mul(d, s.tmo) / s.omega);
+            cval = A::add(A::mul(sd, xi), cval);
+        }
+        if (EXACT)
+            x[P] = A::add(xo, A::mul(s.omega, A::sub(cval, res)) / d);
+        else
+            x[P] = xo + (s.omega / d) * (cval - res);
+    }
 }
 
 // ------------------------------------------------- red-black SOR sweep
@@ -227,9 +263,10 @@ __host__ __forceinline__ dim3 sweep_block(int count) {
     return dim3(tx, RBP_THREADS / tx, 1);
 }
 
-template <typename T, bool EXACT, int NOISE>
+template <typename T, bool EXACT, int NOISE, int VAR = 0>
 __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_pass(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
-                                                               StencilArg<T> s, int colour, int reverse, NoiseArgs nz) {
+                                                               StencilArg<T> s, int colour, int reverse, NoiseArgs nz,
+                                                               VarField<T> vf) {
     if (g.pdl) pdl_begin();
     const int b = blockIdx.y * blockDim.y + threadIdx.y;
     const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
@@ -240,17 +277,19 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_pass(T *__restrict__ x
     if (NOISE == NOISE_PHILOX) xi = (T)pick(fine_normals(nz, g, a + 1, b, c), ((a + 1) & 7) >> 1);
     if (a >= g.N0) return;
     if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
-    sor_point<T, 7, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
+    sor_point<T, 7, EXACT, VAR>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi, vf);
 }
 
 // FP32 variant with vector loads (rows padded to a multiple of 4 floats): a
 // thread owns the 8 padded positions [8q, 8q + 8) of a row, loads them and
 // the matching spans of the four neighbouring rows and f as float4, draws
 // one Philox block for its 4 points of the colour and stores those 4 points.
-template <int NOISE>
+// VD: a per-point centre weight field vd (same padded layout), loaded as a
+// fifth pair of float4 spans.
+template <int NOISE, bool VD = false>
 __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict__ x, const float *__restrict__ f,
                                                               Grid3 g, StencilArg<float> s, int colour, int reverse,
-                                                              NoiseArgs nz) {
+                                                              NoiseArgs nz, const float *__restrict__ vd) {
     if (g.pdl) pdl_begin();
     const int b = blockIdx.y * blockDim.y + threadIdx.y;
     const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
@@ -265,7 +304,12 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
     const float4 *xd = reinterpret_cast<const float4 *>(x + rb - g.sz + P0);
     const float4 *xu = reinterpret_cast<const float4 *>(x + rb + g.sz + P0);
     const float4 *fr = reinterpret_cast<const float4 *>(f + rb + P0);
-    float v[10], ym[8], yp[8], zm[8], zp[8], fv[8];
+    float v[10], ym[8], yp[8], zm[8], zp[8], fv[8], dv[8];
+    if (VD) {
+        const float4 *dr = reinterpret_cast<const float4 *>(vd + rb + P0);
+        const float4 d0 = dr[0], d1 = dr[1];
+        dv[0] = d0.x; dv[1] = d0.y; dv[2] = d0.z; dv[3] = d0.w; dv[4] = d1.x; dv[5] = d1.y; dv[6] = d1.z; dv[7] = d1.w;
+    }
     {
         const float4 a0 = xr[0], a1 = xr[1];
         v[0] = P0 > 0 ? x[rb + P0 - 1] : 0.f;  // P0 - 1 is a ghost column for q = 0 (read 0 directly)
@@ -291,16 +335,19 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
         float xi = 0.f;
         if (NOISE == NOISE_PHILOX) xi = pick(nrm, k);
         if (NOISE == NOISE_INJECTED) xi = (float)nz.buf[g.compact(a, b, c)];
+        const float dg = VD ? dv[j] : s.w[13];
         float res = s.w[4] * zm[j];
         res = fmaf(s.w[10], ym[j], res);
         res = fmaf(s.w[12], v[j], res);
-        res = fmaf(s.w[13], v[j + 1], res);
+        res = fmaf(dg, v[j + 1], res);
         res = fmaf(s.w[14], v[j + 2], res);
         res = fmaf(s.w[16], yp[j], res);
         res = fmaf(s.w[22], zp[j], res);
         float cval = fv[j];
-        if (NOISE != NOISE_NONE) cval = fmaf(s.sd, xi, cval);
-        v[j + 1] = v[j + 1] + s.omega_diag * (cval - res);  // neighbours are of the other colour
+        const float sd = VD ? sqrtf(dg * s.tmo / s.omega) : s.sd;
+        if (NOISE != NOISE_NONE) cval = fmaf(sd, xi, cval);
+        const float od = VD ? s.omega / dg : s.omega_diag;
+        v[j + 1] = v[j + 1] + od * (cval - res);  // neighbours are of the other colour
     };
     if (j0 == 0) {
         upd(0, 0);
@@ -333,9 +380,10 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
 
 // One colour of an 8-colour (27-point) sweep, one thread per point (colour
 // index (a & 1) | (b & 1) << 1 | (c & 1) << 2).
-template <typename T, bool EXACT, int NOISE>
+template <typename T, bool EXACT, int NOISE, int VAR = 0>
 __global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
-                                                                StencilArg<T> s, int colour, NoiseArgs nz) {
+                                                                StencilArg<T> s, int colour, NoiseArgs nz,
+                                                                VarField<T> vf) {
     if (g.pdl) pdl_begin();
     const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
     const int a = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + pa;
@@ -345,7 +393,7 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ 
     if (NOISE == NOISE_PHILOX) xi = (T)pick(point_normals(nz, g, a, b, c), (a & 7) >> 1);
     if (a >= g.N0) return;
     if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
-    sor_point<T, 27, EXACT>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi);
+    sor_point<T, 27, EXACT, VAR>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi, vf);
 }
 
 // ------------------------------------------------ lexicographic wavefront
@@ -634,10 +682,10 @@ __global__ void __launch_bounds__(256) k_lr_scatter(T *__restrict__ x, i64 nrows
 // r(a) = prod {1/2, 1, 1/2}: IntergridOperator::restrict
 // (intergrid_operator.hh:74-88) of the residual f - A_0 x
 // (multigridmc_sampler.cc:124-126), with the stencil part of A.
-template <typename T, int NPT>
+template <typename T, int NPT, int VAR = 0>
 __global__ void __launch_bounds__(256) k_resid_restrict(const T *__restrict__ x, const T *__restrict__ f,
                                                          T *__restrict__ fc, T *__restrict__ xc, Grid3 gf, Grid3 gc, StencilArg<T> s,
-                                                         int dim) {
+                                                         int dim, VarField<T> vf) {
     if (gf.pdl) pdl_begin();
     i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     i64 nc = (i64)gc.N0 * gc.N1 * gc.N2;
@@ -653,7 +701,9 @@ __global__ void __launch_bounds__(256) k_resid_restrict(const T *__restrict__ x,
                 T wr = T((ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0));
                 i64 P = gf.pad(fa + ax, fb + ay, fc_ + az);
                 T res = T(0);
-                if (NPT == 7) {
+                if (VAR) {
+                    res = stencil_row<T, NPT, false, VAR>(x, gf, s, P, vf);
+                } else if (NPT == 7) {
                     res = s.w[4] * x[P - gf.sz] + s.w[10] * x[P - gf.sy] + s.w[12] * x[P - 1] + s.w[13] * x[P] +
                           s.w[14] * x[P + 1] + s.w[16] * x[P + gf.sy] + s.w[22] * x[P + gf.sz];
                 } else {
@@ -972,9 +1022,9 @@ __global__ void __launch_bounds__(128) k_prolong_add(T *__restrict__ x, const T 
 
 // ----------------------------------------------------- stencil apply
 // y = A_0 x (LinearOperator::apply without the low-rank term).
-template <typename T>
+template <typename T, int VAR = 0>
 __global__ void __launch_bounds__(256) k_apply_stencil(const T *__restrict__ x, T *__restrict__ y, Grid3 g,
-                                                        StencilArg<T> s) {
+                                                        StencilArg<T> s, VarField<T> vf) {
     if (g.pdl) pdl_begin();
     i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     i64 n = (i64)g.N0 * g.N1 * g.N2;
@@ -984,7 +1034,8 @@ __global__ void __launch_bounds__(256) k_apply_stencil(const T *__restrict__ x, 
     T res = T(0);
     for (int dz = -1; dz <= 1; ++dz)
         for (int dy = -1; dy <= 1; ++dy)
-            for (int dx = -1; dx <= 1; ++dx) res += s.w[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)] * x[P + dz * g.sz + dy * g.sy + dx];
+            for (int dx = -1; dx <= 1; ++dx)
+                res += vweight<T, VAR>(s, vf, P, (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)) * x[P + dz * g.sz + dy * g.sy + dx];
     y[P] = res;
 }
 
@@ -1205,13 +1256,14 @@ __global__ void __launch_bounds__(256) k_sinvt_q(const double *__restrict__ Sinv
 //
 // r = b - A_0 x over the interior (the low-rank term is added afterwards by
 // k_add_Bq with sign -1).
-template <int NPT>
+template <int NPT, int VAR = 0>
 __global__ void __launch_bounds__(256) k_solve_resid(const double *__restrict__ x, const double *__restrict__ b,
-                                                     double *__restrict__ r, Grid3 g, StencilArg<double> s) {
+                                                     double *__restrict__ r, Grid3 g, StencilArg<double> s,
+                                                     VarField<double> vf) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x, bb = blockIdx.y, c = blockIdx.z;
     if (a >= g.N0) return;
     const i64 P = g.pad(a, bb, c);
-    r[P] = b[P] - stencil_row<double, NPT, false>(x, g, s, P);
+    r[P] = b[P] - stencil_row<double, NPT, false, VAR>(x, g, s, P, vf);
 }
 
 // Per CTA: SOLVE_ROWS rows (b, c) of the interior.  The partial sums of
@@ -1282,15 +1334,18 @@ __device__ __forceinline__ double exact_normal(const NoiseArgs &nz, int k, unsig
     return (double)normals4(philox4x32_10(noise_ctr(a, id, PURPOSE_EXACT, 0), noise_key(a))).x;
 }
 
+// cdiag (may be null): per-point centre weights, c_0 = cdiag[P] - offsum.
 template <int NPT>
 __global__ void __launch_bounds__(256) k_prior_perturbation(double *__restrict__ b, Grid3 g, EdgeWeights ew,
-                                                            NoiseArgs nz) {
+                                                            NoiseArgs nz, const double *__restrict__ cdiag,
+                                                            double offsum) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x, bb = blockIdx.y, c = blockIdx.z;
     if (a >= g.N0) return;
     // ids over positions (-1 .. N) in every direction
     const unsigned X = (unsigned)g.N0 + 2u, Y = (unsigned)g.N1 + 2u;
     auto id = [&](int pa, int pb, int pc) { return ((unsigned)(pc + 1) * Y + (unsigned)(pb + 1)) * X + (unsigned)(pa + 1); };
-    double eta = ew.c0 * exact_normal(nz, 0, id(a, bb, c));
+    const double c0 = cdiag ? sqrt(fmax(cdiag[g.pad(a, bb, c)] - offsum, 0.0)) : ew.c0;
+    double eta = c0 * exact_normal(nz, 0, id(a, bb, c));
 #pragma unroll
     for (int k = 0; k < 13; ++k) {
         const int dx = ew.off[k][0], dy = ew.off[k][1], dz = ew.off[k][2];

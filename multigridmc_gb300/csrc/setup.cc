@@ -358,6 +358,111 @@ std::vector<double> inverse_factor_transposed(const std::vector<double> &L, int6
     return T;
 }
 
+std::vector<double> galerkin_field(const Geometry &fine, const double stencil[27], const double *centre,
+                                   const double *full) {
+    const Geometry crs = fine.coarse();
+    const int64_t n = fine.n, nc = crs.n;
+    const int *N = fine.N, *Nc = crs.N;
+    const bool act[3] = {fine.dim > 0, fine.dim > 1, fine.dim > 2};
+    std::vector<double> out((size_t)27 * nc, 0.0);
+    auto wgt = [&](int64_t f, int k) -> double {
+        if (full) return full[(size_t)k * n + f];
+        return k == 13 && centre ? centre[f] : stencil[k];
+    };
+#pragma omp parallel for schedule(static) if (nc > 4096)
+    for (int64_t pc = 0; pc < nc; ++pc) {
+        int c[3] = {(int)(pc % Nc[0]), (int)((pc / Nc[0]) % Nc[1]), (int)(pc / ((int64_t)Nc[0] * Nc[1]))};
+        double acc[27] = {0};
+        int lo[3], hi[3];
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = act[d] ? -1 : 0;
+            hi[d] = act[d] ? 1 : 0;
+        }
+        for (int rz = lo[2]; rz <= hi[2]; ++rz)
+            for (int ry = lo[1]; ry <= hi[1]; ++ry)
+                for (int rx = lo[0]; rx <= hi[0]; ++rx) {
+                    const int r[3] = {rx, ry, rz};
+                    int fp[3];
+                    double wr = 1.0;
+                    bool in = true;
+                    for (int d = 0; d < 3; ++d) {
+                        fp[d] = act[d] ? 2 * c[d] + 1 + r[d] : 0;
+                        if (r[d]) wr *= 0.5;
+                        in = in && fp[d] >= 0 && fp[d] < N[d];
+                    }
+                    if (!in) continue;
+                    const int64_t f = ((int64_t)fp[2] * N[1] + fp[1]) * N[0] + fp[0];
+                    for (int k = 0; k < 27; ++k) {
+                        const int o[3] = {k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1};
+                        bool ok = true;
+                        int gq[3];
+                        for (int d = 0; d < 3; ++d) {
+                            if (!act[d] && o[d]) ok = false;
+                            gq[d] = fp[d] + o[d];
+                            ok = ok && gq[d] >= 0 && gq[d] < N[d];
+                        }
+                        if (!ok) continue;
+                        const double a = wgt(f, k);
+                        if (a == 0.0) continue;
+                        // coarse parents q of the fine neighbour gq: gq = 2 q + 1 + s, s in {-1, 0, 1}
+                        int pq[3][2], np_[3];
+                        double pw[3][2];
+                        for (int d = 0; d < 3; ++d) {
+                            if (!act[d]) {
+                                np_[d] = 1;
+                                pq[d][0] = 0;
+                                pw[d][0] = 1.0;
+                            } else if (gq[d] % 2 == 1) {
+                                np_[d] = 1;
+                                pq[d][0] = (gq[d] - 1) / 2;
+                                pw[d][0] = 1.0;
+                            } else {
+                                np_[d] = 2;
+                                pq[d][0] = gq[d] / 2 - 1;
+                                pq[d][1] = gq[d] / 2;
+                                pw[d][0] = pw[d][1] = 0.5;
+                            }
+                        }
+                        for (int iz = 0; iz < np_[2]; ++iz)
+                            for (int iy = 0; iy < np_[1]; ++iy)
+                                for (int ix = 0; ix < np_[0]; ++ix) {
+                                    const int q[3] = {pq[0][ix], pq[1][iy], pq[2][iz]};
+                                    bool qin = true;
+                                    for (int d = 0; d < 3; ++d) qin = qin && q[d] >= 0 && q[d] < Nc[d];
+                                    if (!qin) continue;
+                                    const int kc = (q[2] - c[2] + 1) * 9 + (q[1] - c[1] + 1) * 3 + (q[0] - c[0] + 1);
+                                    acc[kc] += wr * a * pw[0][ix] * pw[1][iy] * pw[2][iz];
+                                }
+                    }
+                }
+        for (int k = 0; k < 27; ++k) out[(size_t)k * nc + pc] = acc[k];
+    }
+    return out;
+}
+
+std::vector<double> dense_precision_field(const Geometry &g, const std::vector<double> &field, const SparseCols &B,
+                                          const std::vector<double> &Sigma) {
+    const int64_t n = g.n;
+    std::vector<double> Q((size_t)(n * n), 0.0);
+    for (int64_t p = 0; p < n; ++p) {
+        const int a = (int)(p % g.N[0]), b = (int)((p / g.N[0]) % g.N[1]), c = (int)(p / ((int64_t)g.N[0] * g.N[1]));
+        for (int k = 0; k < 27; ++k) {
+            const double w = field[(size_t)k * n + p];
+            if (w == 0.0) continue;
+            const int qa = a + k % 3 - 1, qb = b + (k / 3) % 3 - 1, qc = c + k / 9 - 1;
+            if (qa < 0 || qb < 0 || qc < 0 || qa >= g.N[0] || qb >= g.N[1] || qc >= g.N[2]) continue;
+            Q[(size_t)p * n + ((int64_t)qc * g.N[1] + qb) * g.N[0] + qa] = w;
+        }
+    }
+    for (int j = 0; j < B.m; ++j) {
+        const double sinv = 1.0 / Sigma[j];
+        for (int64_t e = B.ptr[j]; e < B.ptr[j + 1]; ++e)
+            for (int64_t f = B.ptr[j]; f < B.ptr[j + 1]; ++f)
+                Q[(size_t)B.row[e] * n + B.row[f]] += B.val[e] * sinv * B.val[f];
+    }
+    return Q;
+}
+
 std::vector<double> cholesky_phi_sandwich(const std::vector<double> &T, const Geometry &g, const double E[27]) {
     const int64_t n = g.n;
     // Y = E L^{-T}: row p of Y sums the rows q of L^{-T} (= rows of T) over

@@ -61,6 +61,18 @@ SparseCols restrict_columns(const Geometry &fine, const SparseCols &B);
 // dense row-major precision matrix A_0 + B Sigma^{-1} B^T of one level
 std::vector<double> dense_precision(const Geometry &g, const double st[27], const SparseCols &B,
                                     const std::vector<double> &Sigma);
+// Galerkin product R A R^T (linear_operator.cc:10-23) of a per-point stencil
+// field: A's weight k at fine point f (compact index) is full[k * n + f] when
+// `full` is given, else the constant stencil[k] with the centre replaced by
+// centre[f].  Returns the coarse field, weight-major (k * n_c + p_c);
+// neighbours outside the lattice are omitted (Dirichlet), as in the sparse
+// triple product.
+std::vector<double> galerkin_field(const Geometry &fine, const double stencil[27], const double *centre,
+                                   const double *full);
+// dense row-major A_0 + B Sigma^{-1} B^T of a level with a weight-major
+// per-point stencil field (27 x n)
+std::vector<double> dense_precision_field(const Geometry &g, const std::vector<double> &field, const SparseCols &B,
+                                          const std::vector<double> &Sigma);
 // natural-order Cholesky Q = L L^T in place (lower triangle, zeros above);
 // false if a pivot is not positive
 bool dense_cholesky(std::vector<double> &Q, int64_t n);

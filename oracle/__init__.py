@@ -84,6 +84,7 @@ def lib():
         "orc_sampler_mean_cov": (C.c_int, [_P, C.c_int64, _D, _D, C.c_int64, C.c_int64, _D, _D]),
         "orc_ssor_smoother_apply": (None, [_P, C.c_double, C.c_int, C.c_int, _D, _D]),
         "orc_dense_cholesky": (C.c_int, [_D, C.c_int64]),
+        "orc_op_set_diagonal": (None, [_P, _D]),
         "orc_mg_create": (_P, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int,
                                C.c_int]),
         "orc_mg_destroy": (None, [_P]),
@@ -256,6 +257,12 @@ class Operator:
         for j in range(self.m):
             Bd[row[ptr[j]:ptr[j + 1]], j] = val[ptr[j]:ptr[j + 1]]
         return Bd, sig
+
+    def set_diagonal(self, diag):
+        """Per-vertex diagonal of A_0 (variable-coefficient FD prior)."""
+        self._diag = np.ascontiguousarray(diag, dtype=np.float64)
+        lib().orc_op_set_diagonal(self.h, _dp(self._diag))
+        return self
 
     def set_lowrank(self, Bdense, Sigma):
         Bdense = np.asarray(Bdense, dtype=np.float64)

@@ -1473,6 +1473,16 @@ void orc_op_set_lowrank(orc_op *o, int m, const int64_t *ptr, const int64_t *row
     B.val.assign(val, val + ptr[m]);
     o->op->Sigma.assign(Sigma, Sigma + m);
 }
+// Per-vertex diagonal (the FD prior with a variable correlation length,
+// shiftedlaplace_fd_operator.cc:33-52): the diagonal entry of every row of
+// A_0 is replaced by diag[row].
+void orc_op_set_diagonal(orc_op *o, const double *diag) {
+    Csr &A = o->op->A;
+    for (int64_t i = 0; i < A.n; ++i)
+        for (int64_t k = A.ptr[i]; k < A.ptr[i + 1]; ++k)
+            if (A.col[k] == i) A.val[k] = diag[i];
+    A.finish_diag();
+}
 // MeasuredOperator (measured_operator.cc:9-47): locations[k*dim+d],
 // Sigma_kk = variance_scaling * variance[k]; optional global mean column.
 void orc_op_add_measurements(orc_op *o, int n_meas, const double *locations, const double *variance,

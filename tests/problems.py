@@ -48,3 +48,21 @@ def rhs(op_p, seed=7):
         y = rng.standard_normal(op_p.m)
         f += op_p.B_dense() @ (y / op_p.Sigma)
     return f
+
+
+def periodic_posterior(shape, Lambda_min=0.12, Lambda_max=0.23, m=0, radius=0.05, variance=1e-4, seed=1, lo=0.1,
+                       hi=0.9):
+    """Shifted-Laplace FD prior with the periodic correlation length
+    (correlationlength_model.hh:83-112: a per-vertex diagonal) and m ball
+    measurements, for the oracle and the GB300 library."""
+    dim = len(shape)
+    op_p = M.LinearOperator.shifted_laplace_fd_periodic(shape, Lambda_min, Lambda_max)
+    op_o = O.Operator.from_stencil(list(shape), op_p.stencil)
+    op_o.set_diagonal(op_p.centre)
+    if m > 0:
+        rng = np.random.default_rng(seed)
+        loc = rng.uniform(lo, hi, size=(m, dim))
+        var = np.ones(m)
+        op_o.add_measurements(loc, var, variance_scaling=variance, radius=radius)
+        op_p = op_p.with_measurements(loc, var, variance_scaling=variance, radius=radius)
+    return op_o, op_p

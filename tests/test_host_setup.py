@@ -21,7 +21,7 @@ def test_library_exports_every_declared_symbol():
     for n in sorted(names):
         assert hasattr(lib, n), n
     assert names == set(M.SIGNATURES), "binding table and header differ"
-    assert lib.mgmc_abi_version() == 1
+    assert lib.mgmc_abi_version() == 2
 
 
 @pytest.mark.parametrize("shape", [(8,), (64, 64), (16, 16, 16), (6, 10, 4), (256, 256, 256)])
@@ -92,3 +92,25 @@ def test_sparse_operator_and_exact_observable_moments():
     b[bidx] = bval
     assert abs(mu - b @ np.linalg.solve(A, f)) <= 1e-9 * abs(mu)
     assert abs(var - b @ np.linalg.solve(A, b)) <= 1e-9 * var
+
+
+def test_periodic_correlation_length_model():
+    """kappa^2(x) of PeriodicCorrelationLengthModel (correlationlength_model.hh:83-112)
+    at the vertex coordinates, and the variable FD diagonal in to_scipy."""
+    shape = (6, 5, 4)
+    k = M.LinearOperator.periodic_kappa_sq(shape, 0.1, 0.3)
+    ref = []
+    for c in range(3):
+        for b in range(4):
+            for a in range(5):
+                lam = 0.1
+                for xd in ((a + 1) / 6, (b + 1) / 5, (c + 1) / 4):
+                    lam *= np.cos(np.pi * xd)
+                ref.append(1.0 / (lam + 0.2) ** 2)
+    assert np.allclose(k, ref, rtol=1e-14)
+    op = M.LinearOperator.shifted_laplace_fd_periodic(shape, 0.1, 0.3)
+    hd = 1.0 / (6 * 5 * 4)
+    assert np.allclose(op.centre, hd * k + 2 * hd * (36 + 25 + 16), rtol=1e-14)
+    A = op.to_scipy()
+    assert np.allclose(A.diagonal(), op.centre)
+    assert np.allclose(A[0, 1], -hd * 36)
