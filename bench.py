@@ -570,6 +570,50 @@ def summary_study(sizes=(16, 32, 48, 64, 128), m=32, seed=1):
     return rows
 
 
+def variable_study(N=256, nsteps=4000, Lambda_min=0.12, Lambda_max=0.23, seed=1):
+    """Variable coefficients at the benchmark's size: the 256^3 posterior
+    (64 measurements, radius 0.05, Sigma = 1e-4) with the periodic
+    correlation length (correlationlength_model.hh:83-112) instead of the
+    constant kappa^2 = 10; per-vertex centre weights on the fine level,
+    per-point Galerkin 27-point stencils below.  ms per step (graph, host
+    clock over nsteps), IACT of b^T x, independent samples/s, FP32-mixed and
+    FP64, and the constant-coefficient chain of the same run."""
+    import multigridmc_gb300 as M
+    shape = (N, N, N)
+    rng = np.random.default_rng(seed)
+    loc = rng.uniform(0.1, 0.9, size=(M_MEAS, 3))
+    y = rng.standard_normal(M_MEAS)
+    bidx, bval = M.measurement_vector(shape, [0.5, 0.5, 0.5], RADIUS)
+    out = {}
+    for label, base in (("periodic", M.LinearOperator.shifted_laplace_fd_periodic(shape, Lambda_min, Lambda_max)),
+                        ("constant", M.LinearOperator.shifted_laplace_fd(shape, KAPPA_SQ))):
+        op = base.with_measurements(loc, np.ones(M_MEAS), variance_scaling=VARIANCE, radius=RADIUS)
+        f = np.zeros(op.n)
+        for j in range(op.m):
+            sl = slice(op.B_ptr[j], op.B_ptr[j + 1])
+            f[op.B_idx[sl]] += op.B_val[sl] * (y[j] / op.Sigma[j])
+        for pname, prec in (("fp32", M.FP32_MIXED), ("fp64", M.FP64)):
+            t0 = time.perf_counter()
+            s = M.MultigridMCSampler(op, M.MultigridParameters(nlevel=NLEVEL), precision=prec, seed=seed + 10)
+            setup = time.perf_counter() - t0
+            s.fix_rhs(f)
+            s.step(50)
+            s.set_observable(bidx, bval, nsteps + 8)
+            s.synchronize()
+            t0 = time.perf_counter()
+            s.step(nsteps)
+            s.synchronize()
+            dt = (time.perf_counter() - t0) / nsteps
+            z = s.read_observations(nsteps + 8)[:nsteps]
+            s.close()
+            tau = M.statistics.tau_int(z, IACT_WINDOW)
+            out[f"{label}_{pname}"] = {"ms_per_step": dt * 1e3, "iact": tau, "indep_per_s": 1.0 / (dt * tau),
+                                       "setup_s": setup}
+    out["problem"] = (f"3D {N}^3 posterior, {M_MEAS} measurements; periodic Lambda in [{Lambda_min}, {Lambda_max}] "
+                      f"vs constant kappa^2 = {KAPPA_SQ}; V(1,1) SSOR, {NLEVEL} levels")
+    return out
+
+
 def solve_study(rtol=1e-10, repeats=3):
     """The reference's deterministic multigrid solve (driver_mg: LoopSolver
     with MultigridPreconditioner) of Q x = f on the 256^3 posterior: FP64
@@ -728,6 +772,8 @@ def main():
                     help="run the 128^3 differentiation study (parameter adjoint with checkpoints, FD checks)")
     ap.add_argument("--summary-study", action="store_true",
                     help="MGMC vs Gibbs vs exact sampler at 16^3 .. 128^3 (the reference's summary comparison)")
+    ap.add_argument("--variable-study", action="store_true",
+                    help="the 256^3 posterior with the periodic correlation length (variable coefficients)")
     ap.add_argument("--solve-study", action="store_true",
                     help="time the deterministic multigrid solve of Q x = f instead of the benchmark")
     ap.add_argument("--profile-steps", type=int, default=0, metavar="K",
@@ -749,6 +795,9 @@ def main():
         return
     if args.summary_study:
         print(json.dumps({"summary_study": summary_study()}), flush=True)
+        return
+    if args.variable_study:
+        print(json.dumps({"variable_study": variable_study()}), flush=True)
         return
     if args.solve_study:
         print(json.dumps({"solve_study": solve_study()}), flush=True)

@@ -2,8 +2,8 @@
 
 ``load_run(parameters_file)`` reads a parameters file of the reference's
 driver (the groups that src/auxilliary/parameters.cc reads: general, lattice,
-smoother, multigrid, sampling, prior, constantcorrelationlengthmodel,
-measurements) and the measurement file it names (dim, n,
+smoother, multigrid, sampling, prior, constantcorrelationlengthmodel or
+periodiccorrelationlengthmodel, measurements) and the measurement file it names (dim, n,
 measurement_locations, mean, variance), and builds the linear operator, the
 right hand side and the multigrid parameters of the sampling path, so that a
 ``driver_mgmc`` configuration runs unchanged on the GPU sampler.
@@ -123,10 +123,16 @@ class RunConfig:
     sampling: dict
     measurements: dict = field(default_factory=dict)
     measurement_data: dict = field(default_factory=dict)
+    correlation: str = "constant"  # or "periodic": Lambda_min, Lambda_max below
+    Lambda_min: float = 0.0
+    Lambda_max: float = 0.0
 
     @property
     def kappa_sq(self):
-        """kappa^2 = 1 / Lambda^2 (correlationlength_model.hh:52)."""
+        """kappa^2 = 1 / Lambda^2 (correlationlength_model.hh:52) of the
+        constant correlation-length model."""
+        if self.correlation != "constant":
+            raise ValueError("kappa^2 varies in space for the periodic model")
         return 1.0 / self.Lambda ** 2
 
     def multigrid_parameters(self):
@@ -142,7 +148,10 @@ class RunConfig:
         """The prior (ShiftedLaplaceFDOperator) or the posterior
         (MeasuredOperator) of the configuration (driver_mgmc.cc:120-160)."""
         from . import LinearOperator
-        op = LinearOperator.shifted_laplace_fd(self.shape, self.kappa_sq)
+        if self.correlation == "periodic":
+            op = LinearOperator.shifted_laplace_fd_periodic(self.shape, self.Lambda_min, self.Lambda_max)
+        else:
+            op = LinearOperator.shifted_laplace_fd(self.shape, self.kappa_sq)
         if self.operator == "prior":
             return op
         ms, md = self.measurements, self.measurement_data
@@ -187,13 +196,19 @@ def load_run(parameters_file, measurements_file=None):
     if operator not in ("prior", "posterior"):
         raise ValueError("operator has to be 'prior' or 'posterior'")
     prior = root.get("prior", {"pdemodel": "shiftedlaplace_fd", "correlationlengthmodel": "constant"})
-    if prior.get("pdemodel") != "shiftedlaplace_fd" or prior.get("correlationlengthmodel") != "constant":
-        raise NotImplementedError("only the shifted-Laplace FD prior with a constant correlation length is on the "
-                                  "GPU sampling path")
-    cfg = RunConfig(dim=dim, shape=shape, operator=operator,
-                    Lambda=float(root["constantcorrelationlengthmodel"]["Lambda"]), multigrid=root["multigrid"],
+    model = prior.get("correlationlengthmodel")
+    if prior.get("pdemodel") != "shiftedlaplace_fd" or model not in ("constant", "periodic"):
+        raise NotImplementedError("only the shifted-Laplace FD prior (constant or periodic correlation length) is on "
+                                  "the GPU sampling path")
+    Lambda = float(root["constantcorrelationlengthmodel"]["Lambda"]) if model == "constant" else 0.0
+    cfg = RunConfig(dim=dim, shape=shape, operator=operator, Lambda=Lambda, multigrid=root["multigrid"],
                     smoother=root.get("smoother", {}), sampling=root.get("sampling", {}),
-                    measurements=root.get("measurements", {}))
+                    measurements=root.get("measurements", {}), correlation=model)
+    if model == "periodic":  # parameters.cc:236-256
+        per = root["periodiccorrelationlengthmodel"]
+        cfg.Lambda_min, cfg.Lambda_max = float(per["Lambda_min"]), float(per["Lambda_max"])
+        if not (cfg.Lambda_max >= cfg.Lambda_min and cfg.Lambda_min > 0):
+            raise ValueError("periodic correlation length needs 0 < Lambda_min <= Lambda_max")
     if operator == "posterior":
         path = measurements_file or cfg.measurements["filename"]
         if not os.path.exists(path):

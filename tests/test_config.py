@@ -71,3 +71,19 @@ def test_run_config_builds_the_posterior(tmp_path):
     y = np.array([1.0, -2.0, 0.5, 1.5])
     np.testing.assert_allclose(f, op.B_dense() @ (y / op.Sigma), rtol=1e-12)
     assert cfg.sample_location() == [0.5, 0.5]
+
+
+def test_periodic_correlation_length(tmp_path):
+    """prior.correlationlengthmodel = "periodic" (parameters.cc:236-256)
+    gives the FD prior with the per-vertex diagonal of the periodic model."""
+    text = PARAMS.replace('correlationlengthmodel = "constant"', 'correlationlengthmodel = "periodic"').replace(
+        'operator = "posterior"', 'operator = "prior"') + \
+        "periodiccorrelationlengthmodel = { Lambda_min = 0.12; Lambda_max = 0.23; };\n"
+    (tmp_path / "params.cfg").write_text(text)
+    cfg = load_run(str(tmp_path / "params.cfg"))
+    assert cfg.correlation == "periodic" and (cfg.Lambda_min, cfg.Lambda_max) == (0.12, 0.23)
+    op = cfg.linear_operator()
+    ref = M.LinearOperator.shifted_laplace_fd_periodic((32, 16), 0.12, 0.23)
+    assert np.array_equal(op.centre, ref.centre) and np.array_equal(op.stencil, ref.stencil)
+    with pytest.raises(ValueError):
+        cfg.kappa_sq
