@@ -97,13 +97,16 @@ struct Level {
     // 27-point stencil (its Galerkin coarse levels), weight-major with stride nalloc
     int var = 0;
     void *vw = nullptr;        // the field in the level's type (padded, ghosts zero)
-    double *vw64 = nullptr;    // FP64 copy of a level-0 centre field (solver, exact sampler)
+    double *vw64 = nullptr;    // the field in FP64 (vw itself for FP64 chains): FP64 kernels of FP32
+                               // chains (set-up sweeps, solver residual, exact sampler) read it
     std::vector<double> vh;    // host field, compact: n centre weights or 27 x n weights
 };
 
+// the level's field in the kernel's type T
 template <typename T>
 static VarField<T> var_field(const Level &lv) {
-    return VarField<T>{(const T *)lv.vw, lv.geo.nalloc};
+    const void *w = sizeof(T) == sizeof(double) ? (const void *)lv.vw64 : lv.vw;
+    return VarField<T>{(const T *)w, lv.geo.nalloc};
 }
 
 struct Sampler {
@@ -1209,21 +1212,21 @@ void Sampler::build(const mgmc_operator_desc &op) {
     check_launch();
 }
 
-// A level's host field to the device: padded, the level's type (and for a
-// level-0 centre field an FP64 copy as well); ghosts stay zero.
+// A level's host field to the device: padded, in FP64 and (FP32 chains) in
+// FP32 as well; ghosts stay zero.
 void Sampler::upload_field(Level &lv) {
     const i64 n = lv.geo.n, na = lv.geo.nalloc;
     const int planes = lv.var == 1 ? 1 : 27;
     std::vector<double> pad((size_t)planes * na, 0.0);
     for (int k = 0; k < planes; ++k)
         for (i64 i = 0; i < n; ++i) pad[(size_t)k * na + lv.geo.pad(i)] = lv.vh[(size_t)k * n + i];
+    lv.vw64 = upload(pad);
     if (fp32) {
         std::vector<float> pf(pad.begin(), pad.end());
         lv.vw = upload(pf);
     } else {
-        lv.vw = upload(pad);
+        lv.vw = lv.vw64;
     }
-    if (lv.var == 1) lv.vw64 = fp32 ? upload(pad) : (double *)lv.vw;
 }
 
 // Autotuner of the colour passes' CTA shape: for every level that sweeps,

@@ -35,7 +35,15 @@ def test_chain_parity_fp64(name, mk, prm):
     assert worst < 1e-12, f"{name}: max relative deviation {worst:.3e}"
 
 
-@pytest.mark.parametrize("name,mk,prm", CASES[1:3], ids=[c[0] for c in CASES[1:3]])
+FP32_CASES = CASES[1:3] + [
+    # weak measurements: the low-rank correction depends on the scale of
+    # C = M^{-1} B (with Sigma = 1e-4 it nearly does not), so this case
+    # checks the FP64 set-up sweeps of an FP32 chain on the variable field
+    ("3d-post-16-weak", lambda: periodic_posterior((16, 16, 16), m=4, variance=1e-1), _mg(3)),
+]
+
+
+@pytest.mark.parametrize("name,mk,prm", FP32_CASES, ids=[c[0] for c in FP32_CASES])
 def test_chain_parity_fp32(name, mk, prm):
     """FP32-mixed chain (the fine sweep with the centre field in float4
     spans) against the FP64 oracle: FP32 rounding only."""
