@@ -147,6 +147,11 @@ struct Sampler {
     bool counting = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    // level 0's f split by colour for the FP32 fine sweep (k_split_colours):
+    // colour k at fsplit + k * fhalf; refreshed wherever level 0's f changes
+    float *fsplit = nullptr;
+    i64 fhalf = 0;
+    void refresh_fsplit();
     // deterministic solver: LoopSolver around MultigridPreconditioner
     bool noisy = true;  // false while the preconditioner's noise-free cycle is recorded
     double *sv_x = nullptr, *sv_b = nullptr, *sv_r = nullptr;  // FP64 iterate, rhs, residual (padded level 0)
@@ -361,12 +366,24 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
                     const int ngrp = (lv.g.N0 + 8) / 8;
                     const dim3 blk = level_block(lv, ngrp);
                     dim3 grid((ngrp + blk.x - 1) / blk.x, (lv.g.N1 + blk.y - 1) / blk.y, lv.g.N2);
-                    if (lv.var == 1)
-                        plaunch(S.pdl && lv.g.pdl, k_sweep_rb_vec<NOISE, true>, grid, blk, 0, S.stream, x, f, lv.g, s, colour,
-                                pass, nz, (const float *)lv.vw);
+                    const bool v8 = (lv.g.sy % 8) == 0 && (lv.g.sz % 8) == 0;
+                    const float *vd = lv.var == 1 ? (const float *)lv.vw : nullptr;
+                    const bool pd = S.pdl && lv.g.pdl;
+                    // the colour-split f exists for level 0's own f only
+                    const bool fs = v8 && S.fsplit && f == S.L[0].f && &lv == &S.L[0];
+                    const float *fsc = fs ? S.fsplit + colour * S.fhalf : nullptr;
+                    if (lv.var == 1 && fs)
+                        plaunch(pd, k_sweep_rb_vec<NOISE, true, true, true>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz, vd, fsc);
+                    else if (lv.var == 1 && v8)
+                        plaunch(pd, k_sweep_rb_vec<NOISE, true, true, false>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz, vd, fsc);
+                    else if (lv.var == 1)
+                        plaunch(pd, k_sweep_rb_vec<NOISE, true, false, false>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz, vd, fsc);
+                    else if (fs)
+                        plaunch(pd, k_sweep_rb_vec<NOISE, false, true, true>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz, vd, fsc);
+                    else if (v8)
+                        plaunch(pd, k_sweep_rb_vec<NOISE, false, true, false>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz, vd, fsc);
                     else
-                        plaunch(S.pdl && lv.g.pdl, k_sweep_rb_vec<NOISE, false>, grid, blk, 0, S.stream, x, f, lv.g, s, colour,
-                                pass, nz, (const float *)nullptr);
+                        plaunch(pd, k_sweep_rb_vec<NOISE, false, false, false>, grid, blk, 0, S.stream, x, f, lv.g, s, colour, pass, nz, vd, fsc);
                     S.launches++;
                     continue;
                 }
@@ -1145,6 +1162,11 @@ void Sampler::build(const mgmc_operator_desc &op) {
     }
     for (size_t lev = 0; lev + 1 < L.size(); ++lev) make_tile_maps(L[lev]);
     d_cvec = alloc<double>(L[0].geo.n);
+    if (fp32 && P.ordering == MGMC_ORDER_MULTICOLOUR && L[0].npt == 7 && L[0].g.sy % 8 == 0 && L[0].g.sz % 8 == 0) {
+        fhalf = (L[0].geo.nalloc / 2 + 64) / 64 * 64;
+        fsplit = alloc<float>((size_t)2 * fhalf);
+        CK(cudaMemsetAsync(fsplit, 0, (size_t)2 * fhalf * sizeof(float), stream));
+    }
     // low-rank term on every level: B_{l+1} = R B_l
     if (m > 0) {
         SparseCols B;
@@ -1300,6 +1322,13 @@ static void *mapped_host(const void *p) {
 
 static dim3 pack_grid(const Level &lv) { return dim3((lv.g.N0 + 255) / 256, lv.g.N1, lv.g.N2); }
 
+void Sampler::refresh_fsplit() {
+    if (!fsplit) return;
+    const Level &l0 = L[0];
+    k_split_colours<<<pack_grid(l0), 256, 0, stream>>>((const float *)l0.f, fsplit, fhalf, l0.g);
+    check_launch();
+}
+
 // as_f64: dst is an FP64 array whatever the chain's precision
 static void put_vec(Sampler &S, int lev, const double *src, int on_device, void *dst, bool as_f64 = false) {
     Level &lv = S.L[lev];
@@ -1454,6 +1483,7 @@ void Sampler::ensure_solver() {
             else
                 k_solve_rhs<double><<<sv_np, 256, 0, stream>>>(sv_r, (double *)l0.f, (double *)l0.x, l0.g, sv_part);
             k_solve_norm<<<1, 256, 0, stream>>>(sv_part, sv_np, sv_norm);
+            refresh_fsplit();  // the cycle's fine sweeps read f = r through the colour split
         });
     if (!pexec)
         capture(pgraph, pexec, [&]() {
@@ -1511,6 +1541,9 @@ struct BorrowLevel0 {
         const size_t bytes = (size_t)S.L[0].geo.nalloc * S.tsize();
         cudaMemcpyAsync(S.L[0].x, S.sv_keep_x, bytes, cudaMemcpyDeviceToDevice, S.stream);
         cudaMemcpyAsync(S.L[0].f, S.sv_keep_f, bytes, cudaMemcpyDeviceToDevice, S.stream);
+        if (S.fsplit)
+            k_split_colours<<<dim3((S.L[0].g.N0 + 255) / 256, S.L[0].g.N1, S.L[0].g.N2), 256, 0, S.stream>>>(
+                (const float *)S.L[0].f, S.fsplit, S.fhalf, S.L[0].g);
         cudaStreamSynchronize(S.stream);
     }
 };
@@ -1996,6 +2029,7 @@ mgmc_status mgmc_sampler_fix_rhs(mgmc_sampler *s, const double *f, int on_device
     Sampler &S = impl(s);
     if (!f) fail(MGMC_ERR_INVALID_ARGUMENT, "null f");
     put_vec(S, 0, f, on_device, S.L[0].f);
+    S.refresh_fsplit();
     API_END
 }
 
@@ -2061,6 +2095,7 @@ mgmc_status mgmc_sampler_apply(mgmc_sampler *s, const double *f, double *x, int 
         put_vec(S, 0, f, on_device, S.L[0].f);
         put_vec(S, 0, x, on_device, S.L[0].x);
     }
+    S.refresh_fsplit();
     run_steps(S, 1);
     get_vec(S, 0, S.L[0].x, x, on_device);
     CK(cudaStreamSynchronize(S.stream));
@@ -2434,6 +2469,7 @@ mgmc_status mgmc_sampler_precondition(mgmc_sampler *s, const double *b, double *
     Level &l0 = S.L[0];
     BorrowLevel0 borrow(S);
     put_vec(S, 0, b, on_device, l0.f);
+    S.refresh_fsplit();
     CK(cudaMemsetAsync(l0.x, 0, (size_t)l0.geo.nalloc * S.tsize(), S.stream));
     CK(cudaGraphLaunch(S.pexec, S.stream));
     get_vec(S, 0, l0.x, x, on_device);

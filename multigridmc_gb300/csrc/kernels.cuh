@@ -280,16 +280,42 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_pass(T *__restrict__ x
     sor_point<T, 7, EXACT, VAR>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi, vf);
 }
 
+// 256-bit vector access (sm_100 and later): 8 floats at a 32-byte aligned
+// address in one instruction.  ld8 reads through L1 (x is written in the
+// same pass), ld8nc through the read-only path (f, fields).
+__device__ __forceinline__ void ld8(const float *p, float *v) {
+    asm volatile("ld.global.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+                 : "l"(p)
+                 : "memory");
+}
+__device__ __forceinline__ void ld8nc(const float *p, float *v) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+        : "l"(p));
+}
+__device__ __forceinline__ void st8(float *p, const float *v) {
+    asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]),
+                 "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
+                 : "memory");
+}
+
 // FP32 variant with vector loads (rows padded to a multiple of 4 floats): a
 // thread owns the 8 padded positions [8q, 8q + 8) of a row, loads them and
 // the matching spans of the four neighbouring rows and f as float4, draws
 // one Philox block for its 4 points of the colour and stores those 4 points.
 // VD: a per-point centre weight field vd (same padded layout), loaded as a
-// fifth pair of float4 spans.
-template <int NOISE, bool VD = false>
+// fifth pair of float4 spans.  V8 (rows a multiple of 8 floats): every span
+// is one 256-bit access instead of two float4 ones, which halves the L1
+// wavefronts of the loads (a warp's 32-byte spans are contiguous).  FS (with
+// V8): f comes from fsc, the colour's half of f split by colour
+// (k_split_colours), so the pass reads one float4 of f per span -- only the
+// values it uses -- instead of the whole span.
+template <int NOISE, bool VD = false, bool V8 = false, bool FS = false>
 __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict__ x, const float *__restrict__ f,
                                                               Grid3 g, StencilArg<float> s, int colour, int reverse,
-                                                              NoiseArgs nz, const float *__restrict__ vd) {
+                                                              NoiseArgs nz, const float *__restrict__ vd,
+                                                              const float *__restrict__ fsc) {
     if (g.pdl) pdl_begin();
     const int b = blockIdx.y * blockDim.y + threadIdx.y;
     const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
@@ -306,11 +332,36 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
     const float4 *fr = reinterpret_cast<const float4 *>(f + rb + P0);
     float v[10], ym[8], yp[8], zm[8], zp[8], fv[8], dv[8];
     if (VD) {
-        const float4 *dr = reinterpret_cast<const float4 *>(vd + rb + P0);
-        const float4 d0 = dr[0], d1 = dr[1];
-        dv[0] = d0.x; dv[1] = d0.y; dv[2] = d0.z; dv[3] = d0.w; dv[4] = d1.x; dv[5] = d1.y; dv[6] = d1.z; dv[7] = d1.w;
+        if (V8) {
+            ld8nc(vd + rb + P0, dv);
+        } else {
+            const float4 *dr = reinterpret_cast<const float4 *>(vd + rb + P0);
+            const float4 d0 = dr[0], d1 = dr[1];
+            dv[0] = d0.x; dv[1] = d0.y; dv[2] = d0.z; dv[3] = d0.w; dv[4] = d1.x; dv[5] = d1.y; dv[6] = d1.z; dv[7] = d1.w;
+        }
     }
-    {
+    // points of the colour: padded P with (P - 1 + b + c) & 1 == colour; the
+    // two parities get separate code so that every register index is static
+    const int j0 = (colour + b + c + 1) & 1;  // first local index j (P = P0 + j) of the colour
+    if (V8) {
+        v[0] = P0 > 0 ? x[rb + P0 - 1] : 0.f;
+        ld8(x + rb + P0, v + 1);
+        v[9] = x[rb + P0 + 8];
+        ld8(x + rb - g.sy + P0, ym);
+        ld8(x + rb + g.sy + P0, yp);
+        ld8(x + rb - g.sz + P0, zm);
+        ld8(x + rb + g.sz + P0, zp);
+        if (FS) {
+            const float4 fq = __ldg(reinterpret_cast<const float4 *>(fsc + ((rb + P0) >> 1)));
+            if (j0 == 0) {
+                fv[0] = fq.x; fv[2] = fq.y; fv[4] = fq.z; fv[6] = fq.w;
+            } else {
+                fv[1] = fq.x; fv[3] = fq.y; fv[5] = fq.z; fv[7] = fq.w;
+            }
+        } else {
+            ld8nc(f + rb + P0, fv);
+        }
+    } else {
         const float4 a0 = xr[0], a1 = xr[1];
         v[0] = P0 > 0 ? x[rb + P0 - 1] : 0.f;  // P0 - 1 is a ghost column for q = 0 (read 0 directly)
         v[1] = a0.x; v[2] = a0.y; v[3] = a0.z; v[4] = a0.w;
@@ -324,9 +375,6 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
         zp[0] = u0.x; zp[1] = u0.y; zp[2] = u0.z; zp[3] = u0.w; zp[4] = u1.x; zp[5] = u1.y; zp[6] = u1.z; zp[7] = u1.w;
         fv[0] = f0.x; fv[1] = f0.y; fv[2] = f0.z; fv[3] = f0.w; fv[4] = f1.x; fv[5] = f1.y; fv[6] = f1.z; fv[7] = f1.w;
     }
-    // points of the colour: padded P with (P - 1 + b + c) & 1 == colour; the
-    // two parities get separate code so that every register index is static
-    const int j0 = (colour + b + c + 1) & 1;  // first local index j (P = P0 + j) of the colour
     float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f);
     if (NOISE == NOISE_PHILOX) nrm = fine_normals(nz, g, P0 + j0, b, c);
     auto upd = [&](int j, int k) {
@@ -365,6 +413,10 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
     // are rewritten unchanged -- no thread writes them in this pass.  A span
     // that reaches past its row (short rows only) stores its second half
     // point by point.
+    if (V8 && P0 + 8 <= g.sy) {
+        st8(x + rb + P0, v + 1);
+        return;
+    }
     float4 *xo = reinterpret_cast<float4 *>(x + rb + P0);
     xo[0] = make_float4(v[1], v[2], v[3], v[4]);
     if (P0 + 8 <= g.sy) {
@@ -376,6 +428,19 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
             if (((j - j0) & 1) == 0 && a >= 0 && a < g.N0) x[rb + P0 + j] = v[j + 1];
         }
     }
+}
+
+// Level 0's f split by colour for the FP32 fine sweep: the value of point
+// (a, b, c) of colour k = (a + b + c) & 1 at fs[k * half + (P >> 1)], P its
+// padded index.  With even row and plane pitches, the two points P = 2i,
+// 2i + 1 of a row have different colours, so each colour's half holds one
+// value per pair, and a span [8q, 8q + 8) of a row maps to one float4.
+__global__ void __launch_bounds__(256) k_split_colours(const float *__restrict__ f, float *__restrict__ fs, i64 half,
+                                                       Grid3 g) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y, c = blockIdx.z;
+    if (a >= g.N0) return;
+    const i64 P = g.pad(a, b, c);
+    fs[(i64)((a + b + c) & 1) * half + (P >> 1)] = f[P];
 }
 
 // One colour of an 8-colour (27-point) sweep, one thread per point (colour
