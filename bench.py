@@ -38,8 +38,8 @@ NLEVEL = 5
 IACT_WINDOW = 50
 # DRAM bytes (read + write) of one k_sweep_rb_vec launch at 256^3, from an
 # ncu capture of `python bench.py --profile-steps 1` (summary in
-# profiles/k_sweep_rb_vec_256cubed.md): 133.97 MB read + 24.84 MB written
-RB_VEC_DRAM_BYTES = 158.81e6
+# profiles/k_sweep_rb_vec_256cubed.md): 100.68 MB read + 14.34 MB written
+RB_VEC_DRAM_BYTES = 115.01e6
 METRIC = "indep. samples/s (rate/IACT), 3D 256³ posterior: mixed vs FP64 plain, 1 GB300"
 UNIT = "indep_samples/s"
 PUBLISHED_MGMC_IACT = 1.28  # python/plot_summary.py:28-29, MGMC at 64^3
@@ -904,7 +904,7 @@ def main():
         "gpu_launches": int(launches * args.steps),
         "launches_per_step": int(launches),
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                     "traffic": RB_VEC_DRAM_BYTES, "traffic_unit": "bytes per launch (ncu dram__bytes_read+write)", "kernel": "k_sweep_rb_vec<float> (one colour pass of the fine-level red-black SOR sweep, Philox noise)",
+                     "traffic": RB_VEC_DRAM_BYTES, "traffic_unit": "bytes per launch (ncu dram__bytes_read+write)", "kernel": "k_sweep_rb_vec<1, 0, 1, 1> (one colour pass of the fine-level red-black SOR sweep: FP32, Philox noise, 256-bit spans, colour-split f)",
                      "algorithmic_bytes_per_launch": bpl, "launch_s": tl, "peak_kind": peak_kind},
         "cpu_baseline": cpu,
     }
