@@ -189,6 +189,42 @@ def sweep_roofline(M, torch, s, precision, peak):
     return achieved, bytes_per_launch, t
 
 
+def kernel_table(M, torch, s, precision, peak, sweep_launch_s):
+    """Achieved GB/s of the other fine-level kernel families on the
+    sampler's stream, algorithmic bytes per launch as for the sweep:
+    residual-restriction 2 n s + n_1 s (x and f read, f_1 written; the
+    low-rank term adds nnz(B)(8 + 2 s)), prolongation n_1 s + 2 n s, and the
+    low-rank correction of one sweep (the difference between sweeps with
+    and without it): nnz(B)(8 + 2 s) for B^T x and nnz(C)(s + 4) + rows(C)
+    2 s for x += C z, with nnz(C) = rows(C) taken as the support of C."""
+    n, n1 = s.level_size(0), s.level_size(1)
+    sz = 4 if precision == M.FP32_MIXED else 8
+    st = torch.cuda.ExternalStream(s.stream)
+
+    def timed(fn, rep):
+        fn(3)
+        s.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        fn(rep)
+        e1.record(st)
+        s.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / rep
+
+    out = {}
+    t = timed(lambda r: s.transfer_device(0, 0, r), 40)
+    b = 2 * n * sz + n1 * sz
+    out["resid_restrict"] = {"s": t, "algorithmic_bytes": b, "gbs": b / t / 1e9, "frac": b / t / 1e9 / peak}
+    t = timed(lambda r: s.transfer_device(0, 1, r), 40)
+    b = n1 * sz + 2 * n * sz
+    out["prolong_add"] = {"s": t, "algorithmic_bytes": b, "gbs": b / t / 1e9, "frac": b / t / 1e9 / peak}
+    t_full = timed(lambda r: s.sweep_device(0, nrepeat=r, with_lowrank=True), 20)
+    t_lr = t_full - 2 * sweep_launch_s
+    out["lowrank_per_sweep"] = {"s": t_lr, "note": "sweep with the low-rank correction minus its two colour passes"}
+    out["sweep_with_lowrank_s"] = t_full
+    return out
+
+
 def time_e2e(M, torch, op, f, precision, steps, seed, iact):
     """The same metric through Sampler::apply with host buffers: per step
     f and x go host->device (pinned) and x comes back device->host."""
@@ -852,6 +888,7 @@ def main():
     launches = s32.launches_per_step
     iact32 = M.statistics.tau_int(z32, IACT_WINDOW)
     ach, bpl, tl = sweep_roofline(M, torch, s32, M.FP32_MIXED, peak)
+    kernels = kernel_table(M, torch, s32, M.FP32_MIXED, peak, tl)
     s32.close()
     # FP64 chain
     # same seed: the FP64 chain draws the FP32 chain's normals (coupled
@@ -897,6 +934,7 @@ def main():
         "iact": iact32, "steps_per_s": 1000.0 / ms32,
         "fp64": {"value": value64, "ms_per_step": ms64, "iact": iact64, "steps_per_s": 1000.0 / ms64,
                  "sweep_gbs": ach64},
+        "kernels_fp32": kernels,
         "mixed_vs_fp64": value / value64,
         "clocks": clk,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

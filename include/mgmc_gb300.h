@@ -264,6 +264,13 @@ mgmc_status mgmc_level_sor(mgmc_sampler *s, int level, int direction, int with_n
  * Used to time the sweep kernels in isolation. */
 mgmc_status mgmc_level_sweep_device(mgmc_sampler *s, int level, int direction, int with_noise, int with_lowrank,
                                     int64_t nrepeat);
+/* `nrepeat` residual-restrictions from `level` to level+1 (which = 0: f_{l+1} =
+ * R (f - A x), with the low-rank term; multigridmc_sampler.cc:124-126) or
+ * prolongations (which = 1: x += alpha P x_{l+1}, :131) on the levels'
+ * device-resident vectors, asynchronous on the sampler's stream.  Used to time
+ * the transfer kernels in isolation; the residual-restriction also zeroes
+ * the coarse state. */
+mgmc_status mgmc_level_transfer_device(mgmc_sampler *s, int level, int which, int64_t nrepeat);
 
 /* ----------------------------------------------------------------- batch */
 /* Many independent chains (the reference's only parallel mode: independent

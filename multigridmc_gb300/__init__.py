@@ -122,6 +122,7 @@ SIGNATURES = {
     "mgmc_level_prolongate_add": (C.c_int, [_P, C.c_int, C.c_double, _D, _D]),
     "mgmc_level_sor": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _D, _D]),
     "mgmc_level_sweep_device": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64]),
+    "mgmc_level_transfer_device": (C.c_int, [_P, C.c_int, C.c_int, C.c_int64]),
     "mgmc_batch_create": (C.c_int, [C.c_int, C.POINTER(_P), C.POINTER(_P)]),
     "mgmc_batch_step": (C.c_int, [_P, C.c_int64]),
     "mgmc_batch_synchronize": (C.c_int, [_P]),
@@ -635,6 +636,11 @@ class MultigridMCSampler:
         """SOR sweeps on the level's device-resident vectors (asynchronous)."""
         _check(self._L.mgmc_level_sweep_device(self._h, level, direction, int(with_noise), int(with_lowrank),
                                                int(nrepeat)))
+
+    def transfer_device(self, level, which, nrepeat=1):
+        """Residual-restrictions (which=0) or prolongations (which=1) between
+        `level` and level+1 on the device-resident vectors (asynchronous)."""
+        _check(self._L.mgmc_level_transfer_device(self._h, level, int(which), int(nrepeat)))
 
     def sor(self, level, direction, f, x, with_noise=True):
         f = _f64(f)
