@@ -168,6 +168,14 @@ struct Sampler {
         owned.push_back(p);
         return p;
     }
+    // free an allocation of this sampler before the sampler ends
+    void release(void *p) {
+        auto it = std::find(owned.begin(), owned.end(), p);
+        if (it != owned.end()) {
+            cudaFree(p);
+            owned.erase(it);
+        }
+    }
     template <typename P_>
     P_ *upload(const std::vector<P_> &v) {
         P_ *p = dupload(v, stream);
@@ -879,11 +887,19 @@ void Sampler::build_lowrank(int lev) {
     lv.part = alloc<double>((size_t)m * lv.bt_split);
     lv.counter = alloc<unsigned>(1);
     CK(cudaMemsetAsync(lv.counter, 0, sizeof(unsigned), stream));
-    // FP64 work arrays
+    // FP64 work arrays, released at the end of the set-up
     double *xs = alloc<double>(geo.nalloc), *fs = alloc<double>(geo.nalloc);
     i64 *nzi = alloc<i64>(n);
     double *nzv = alloc<double>(n);
     unsigned long long *cnt = alloc<unsigned long long>(1);
+    struct Release {
+        Sampler &S;
+        std::vector<void *> ptrs;
+        ~Release() {
+            cudaStreamSynchronize(S.stream);
+            for (void *p : ptrs) S.release(p);
+        }
+    } work{*this, {xs, fs, nzi, nzv, cnt}};
     std::vector<double> yh(m);
     for (int dir = 0; dir < 2; ++dir) {
         std::vector<std::tuple<i64, int, double>> trip;
@@ -2359,6 +2375,23 @@ mgmc_status mgmc_level_sweep_device(mgmc_sampler *s, int level, int direction, i
         if (!with_lowrank) S.m = 0;
         S.sor(level, direction == MGMC_FORWARD, with_noise != 0, lv.x, lv.f);
         S.m = saved_m;
+    }
+    S.check_launch();
+    API_END
+}
+
+mgmc_status mgmc_level_transfer_device(mgmc_sampler *s, int level, int which, int64_t nrepeat) {
+    API_BEGIN
+    Sampler &S = impl(s);
+    check_level(S, level, true);
+    if (which != 0 && which != 1) fail(MGMC_ERR_INVALID_ARGUMENT, "which must be 0 (residual-restriction) or 1 (prolongation)");
+    if (nrepeat < 0) fail(MGMC_ERR_INVALID_ARGUMENT, "nrepeat < 0");
+    Level &lv = S.L[level], &lc = S.L[level + 1];
+    for (int64_t r = 0; r < nrepeat; ++r) {
+        if (which == 0)
+            S.resid_restrict(level);
+        else
+            S.prolong(level, S.P.coarse_scaling, lc.x, lv.x);
     }
     S.check_launch();
     API_END
