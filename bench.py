@@ -19,6 +19,7 @@ Under torchrun every rank runs an independent chain on its own GPU
 import argparse
 import json
 import os
+import platform
 import subprocess
 import sys
 import threading
@@ -278,7 +279,21 @@ def cpu_reference(seconds_budget=25.0, nsteps=None):
             break
     per_step = float(np.mean(times))
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"per_step_s": per_step, "steps": len(times), "setup_s": setup, "threads": threads}
+    return {"per_step_s": per_step, "steps": len(times), "setup_s": setup, "threads": threads, "host": host_cpu()}
+
+
+def host_cpu():
+    """CPU model and core count of this host (as lscpu reports them)."""
+    model = platform.machine()
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip() + f" ({platform.machine()})"
+                break
+    except Exception:
+        pass
+    return f"{model}, {os.cpu_count()} cores"
 
 
 def covariance_study(nsamples, nprobe=256, warmup=50, seed=1000):
@@ -856,7 +871,7 @@ def main():
         sample = (f"{r['steps']} MGMC steps of the oracle's reference restatement at 256^3, m=64 (lexicographic "
                   f"SOR, dense B-bar, CLCG), one chain, {r['threads']} OpenMP threads in the dense products; "
                   f"IACT {PUBLISHED_MGMC_IACT} = the reference's published MGMC IACT (python/plot_summary.py:28); "
-                  f"setup {r['setup_s']:.1f} s untimed")
+                  f"setup {r['setup_s']:.1f} s untimed; host {r['host']}")
         line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
                 "steps": r["steps"], "warmup": 1, "ms_per_step": r["per_step_s"] * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -917,7 +932,7 @@ def main():
             cpu = {"value": cv, "unit": UNIT, "cores": r["threads"], "kind": "port",
                    "sample": (f"{r['steps']} oracle MGMC steps at 256^3 m=64 (reference algorithm: lexicographic "
                               f"SOR, dense B-bar, CLCG), {r['per_step_s']:.2f} s/step, IACT "
-                              f"{PUBLISHED_MGMC_IACT} (published, python/plot_summary.py:28)")}
+                              f"{PUBLISHED_MGMC_IACT} (published, python/plot_summary.py:28); host {r['host']}")}
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
 

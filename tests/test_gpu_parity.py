@@ -72,6 +72,14 @@ def test_chain_parity_64cubed():
     assert worst < TOL_FP64
 
 
+def test_chain_parity_128cubed():
+    """The 128^3 posterior with 32 measurements (five levels down to 8^3
+    cells): FP64 chain against the oracle, 6 steps."""
+    op_o, op_p = posterior((128, 128, 128), m=32)
+    worst = _run_parity(op_o, op_p, _mg(5), M.MULTICOLOUR, 6)
+    assert worst < TOL_FP64
+
+
 @pytest.mark.parametrize("name,mk,prm", CASES[3:6], ids=[c[0] for c in CASES[3:6]])
 def test_chain_parity_fp32(name, mk, prm):
     """FP32-mixed chain against the FP64 oracle on the same noise: the
