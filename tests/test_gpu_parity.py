@@ -74,9 +74,9 @@ def test_chain_parity_64cubed():
 
 def test_chain_parity_128cubed():
     """The 128^3 posterior with 32 measurements (five levels down to 8^3
-    cells): FP64 chain against the oracle, 6 steps."""
+    cells): FP64 chain against the oracle, 20 steps."""
     op_o, op_p = posterior((128, 128, 128), m=32)
-    worst = _run_parity(op_o, op_p, _mg(5), M.MULTICOLOUR, 6)
+    worst = _run_parity(op_o, op_p, _mg(5), M.MULTICOLOUR, 20)
     assert worst < TOL_FP64
 
 
