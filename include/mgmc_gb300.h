@@ -103,6 +103,13 @@ typedef struct mgmc_operator_desc {
      * The coarse levels then carry per-point 27-point Galerkin stencils.
      * Needs dim >= 2 and MGMC_ORDER_MULTICOLOUR; NULL for a constant stencil. */
     const double *centre;
+    /* Optional per-vertex 27-point stencil of the fine level, weight-major
+     * (weight k of vertex p at field[k * n + p], k as in `stencil`): the FEM
+     * prior with a variable correlation length (mgmc_fem_field).  Takes
+     * precedence over stencil and centre; `stencil` should still hold a
+     * representative stencil (it sets the colouring).  Needs dim >= 2 and
+     * MGMC_ORDER_MULTICOLOUR; NULL otherwise. */
+    const double *field;
 } mgmc_operator_desc;
 
 /* Sampler parameters: MultigridParameters plus the GB300 execution choices. */
@@ -138,6 +145,12 @@ mgmc_status mgmc_fd_stencil(int dim, int nx, int ny, int nz, double kappa_sq, do
  * vertex.  Writes at most `capacity` entries and sets *nnz to the count. */
 mgmc_status mgmc_measurement_vector(int dim, int nx, int ny, int nz, const double *x0, double radius,
                                     int64_t *idx, double *val, int64_t capacity, int64_t *nnz);
+/* ShiftedLaplaceFEMOperator (shiftedlaplace_fem_operator.cc:9-152): Q1
+ * elements, 2-point Gauss-Legendre quadrature per direction; kappa^2
+ * constant (model 0, p0 = kappa^2) or from the periodic correlation length
+ * (model 1, p0 = Lambda_min, p1 = Lambda_max).  Writes the weight-major
+ * per-vertex stencils (27 x n values) to field. */
+mgmc_status mgmc_fem_field(int dim, int nx, int ny, int nz, int model, double p0, double p1, double *field);
 /* Galerkin triple product R A R^T of a constant stencil with the linear
  * intergrid operator (linear_operator.cc:10-23, intergrid_operator_linear.cc:8-31). */
 mgmc_status mgmc_galerkin_stencil(int dim, const double fine[27], double coarse[27]);

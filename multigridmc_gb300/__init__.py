@@ -66,7 +66,7 @@ class _OpDesc(C.Structure):
                 ("stencil", C.c_double * 27), ("m", C.c_int),
                 ("B_colptr", C.POINTER(C.c_int64)), ("B_rowidx", C.POINTER(C.c_int64)),
                 ("B_val", C.POINTER(C.c_double)), ("Sigma", C.POINTER(C.c_double)),
-                ("centre", C.POINTER(C.c_double))]
+                ("centre", C.POINTER(C.c_double)), ("field", C.POINTER(C.c_double))]
 
 
 class _Params(C.Structure):
@@ -91,6 +91,7 @@ SIGNATURES = {
     "mgmc_measurement_vector": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _D, C.c_double, _I64, _D,
                                           C.c_int64, _I64]),
     "mgmc_galerkin_stencil": (C.c_int, [C.c_int, _D, _D]),
+    "mgmc_fem_field": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _D]),
     "mgmc_sampler_create": (C.c_int, [C.POINTER(_OpDesc), C.POINTER(_Params), C.POINTER(_P)]),
     "mgmc_sampler_destroy": (C.c_int, [_P]),
     "mgmc_sampler_apply": (C.c_int, [_P, _D, _D, C.c_int]),
@@ -183,6 +184,15 @@ def fd_stencil(shape, kappa_sq):
     return st
 
 
+def fem_field(shape, model, p0, p1=0.0):
+    """Per-vertex stencils of ShiftedLaplaceFEMOperator (27 x n, weight-major):
+    model 0 constant kappa^2 = p0, model 1 periodic (Lambda_min, Lambda_max)."""
+    n = int(np.prod([s - 1 for s in shape]))
+    out = np.zeros((27, n))
+    _check(load().mgmc_fem_field(len(shape), *_shape3(shape), int(model), float(p0), float(p1), _dp(out)))
+    return out
+
+
 def galerkin_stencil(dim, fine):
     fine = _f64(fine)
     out = np.zeros(27)
@@ -227,6 +237,7 @@ class LinearOperator:
     B_val: np.ndarray = field(default_factory=lambda: np.zeros(0))
     Sigma: np.ndarray = field(default_factory=lambda: np.zeros(0))
     centre: np.ndarray = None  # per-vertex centre weight of the stencil (variable coefficients), or None
+    field: np.ndarray = None   # per-vertex 27-point stencils, weight-major (27 x n), or None
 
     @property
     def dim(self):
@@ -246,6 +257,26 @@ class LinearOperator:
         if kappa_sq is None:
             kappa_sq = 1.0 / Lambda ** 2
         return cls(tuple(int(s) for s in shape), fd_stencil(shape, kappa_sq))
+
+    @classmethod
+    def shifted_laplace_fem(cls, shape, kappa_sq=None, Lambda=None):
+        """ShiftedLaplaceFEMOperator (shiftedlaplace_fem_operator.cc:9-152) with a
+        constant correlation length: a constant 3^d-point stencil."""
+        if kappa_sq is None:
+            kappa_sq = 1.0 / Lambda ** 2
+        shape = tuple(int(s) for s in shape)
+        fld = fem_field(shape, 0, kappa_sq, 0.0)
+        n = fld.shape[1]
+        return cls(shape, fld[:, n // 2].copy())
+
+    @classmethod
+    def shifted_laplace_fem_periodic(cls, shape, Lambda_min, Lambda_max):
+        """ShiftedLaplaceFEMOperator with the periodic correlation length: a
+        per-vertex 3^d-point stencil field (the mass term follows kappa^2(x))."""
+        shape = tuple(int(s) for s in shape)
+        fld = fem_field(shape, 1, Lambda_min, Lambda_max)
+        n = fld.shape[1]
+        return cls(shape, fld[:, n // 2].copy(), field=fld)
 
     @staticmethod
     def periodic_kappa_sq(shape, Lambda_min, Lambda_max):
@@ -290,7 +321,7 @@ class LinearOperator:
             val.extend(np.asarray(v, np.float64)[order].tolist())
             ptr.append(len(idx))
         return LinearOperator(self.shape, self.stencil, np.array(ptr, np.int64), np.array(idx, np.int64),
-                              np.array(val, np.float64), _f64(Sigma), self.centre)
+                              np.array(val, np.float64), _f64(Sigma), self.centre, self.field)
 
     def with_measurements(self, locations, variance, variance_scaling=1.0, radius=0.05, measure_global=False,
                           variance_global=0.0):
@@ -318,16 +349,17 @@ class LinearOperator:
         for dz in (-1, 0, 1):
             for dy in (-1, 0, 1):
                 for dx in (-1, 0, 1):
-                    w = float(self.stencil[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)])
-                    if w == 0.0:
+                    k = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)
+                    w = float(self.stencil[k])
+                    if w == 0.0 and (self.field is None or not self.field[k].any()):
                         continue
                     src = idx[max(0, -dz):N[2] - max(0, dz), max(0, -dy):N[1] - max(0, dy), max(0, -dx):N[0] - max(0, dx)]
                     dst = idx[max(0, dz):N[2] + min(0, dz), max(0, dy):N[1] + min(0, dy), max(0, dx):N[0] + min(0, dx)]
                     rows.append(src.ravel())
                     cols.append(dst.ravel())
-                    vals.append(np.full(src.size, w))
+                    vals.append(np.asarray(self.field[k])[src.ravel()] if self.field is not None else np.full(src.size, w))
         A = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
-        if self.centre is not None:
+        if self.centre is not None and self.field is None:
             A = (A + sp.diags(np.asarray(self.centre, np.float64) - float(self.stencil[13]))).tocsr()
         if self.m > 0:
             Bs = sp.csc_matrix((self.B_val, self.B_idx, self.B_ptr), shape=(n, self.m))
@@ -359,6 +391,12 @@ class LinearOperator:
                 raise ValueError("centre needs one weight per vertex")
             self._keep = self._keep + (c,)
             d.centre = c.ctypes.data_as(_D)
+        if self.field is not None:
+            fl = _f64(self.field)
+            if fl.shape != (27, self.n):
+                raise ValueError("field needs 27 weights per vertex")
+            self._keep = self._keep + (fl,)
+            d.field = fl.ctypes.data_as(_D)
         return d
 
 

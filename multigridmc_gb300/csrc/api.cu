@@ -366,7 +366,7 @@ static void launch_sweep_t(Sampler &S, const Level &lv, bool forward, T *x, cons
     if (NPT == 7) {
         // red-black: two passes, the second walking the planes downwards;
         // FP32 rows padded to a multiple of 4 floats use the vector pass
-        const bool vec = sizeof(T) == 4 && !EXACT && (lv.g.sy % 4) == 0 && (lv.g.sz % 4) == 0;
+        const bool vec = sizeof(T) == 4 && !EXACT && (lv.g.sy % 4) == 0 && (lv.g.sz % 4) == 0 && lv.var != 2;
         for (int pass = 0; pass < 2; ++pass) {
             const int colour = forward ? pass : 1 - pass;
             if constexpr (std::is_same<T, float>::value) {
@@ -1090,9 +1090,9 @@ void Sampler::build(const mgmc_operator_desc &op) {
     if (op.m < 0 || (op.m > 0 && (!op.B_colptr || !op.B_rowidx || !op.B_val || !op.Sigma)))
         fail(MGMC_ERR_INVALID_ARGUMENT, "low-rank term needs B and Sigma");
     if (op.m > 3072) fail(MGMC_ERR_UNSUPPORTED, "at most 3072 measurement columns");
-    if (op.centre && op.dim < 2) fail(MGMC_ERR_UNSUPPORTED, "a per-vertex centre weight needs dim >= 2");
-    if (op.centre && P.ordering != MGMC_ORDER_MULTICOLOUR)
-        fail(MGMC_ERR_UNSUPPORTED, "a per-vertex centre weight needs the multicolour ordering");
+    if ((op.centre || op.field) && op.dim < 2) fail(MGMC_ERR_UNSUPPORTED, "a per-vertex stencil needs dim >= 2");
+    if ((op.centre || op.field) && P.ordering != MGMC_ORDER_MULTICOLOUR)
+        fail(MGMC_ERR_UNSUPPORTED, "a per-vertex stencil needs the multicolour ordering");
     fp32 = P.precision == MGMC_FP32_MIXED;
     noise_mode = P.noise == MGMC_NOISE_INJECTED ? NOISE_INJECTED : NOISE_PHILOX;
     exact = !fp32 && noise_mode == NOISE_INJECTED;
@@ -1139,10 +1139,21 @@ void Sampler::build(const mgmc_operator_desc &op) {
         lv.g.sz = geo.sz;
         std::memcpy(lv.st, st, sizeof(st));
         lv.diag = st[13];
-        if (op.centre) {
-            // variable coefficients: level 0 keeps the centre weights, every
-            // coarser level the Galerkin product of the level above
-            if (lev == 0) {
+        if (op.centre || op.field) {
+            // variable coefficients: level 0 keeps the centre weights (or
+            // the whole per-vertex stencils), every coarser level the
+            // Galerkin product of the level above
+            if (lev == 0 && op.field) {
+                lv.var = 2;
+                lv.vh.assign(op.field, op.field + (size_t)27 * geo.n);
+                // the colouring follows the couplings present anywhere in the field
+                for (int k = 0; k < 27; ++k) {
+                    double mx = 0.0;
+                    for (i64 i = 0; i < geo.n; ++i) mx = std::max(mx, std::fabs(lv.vh[(size_t)k * geo.n + i]));
+                    if (k != 13 && mx > 0.0 && st[k] == 0.0) st[k] = -mx;
+                }
+                std::memcpy(lv.st, st, sizeof(st));
+            } else if (lev == 0) {
                 lv.var = 1;
                 lv.vh.assign(op.centre, op.centre + geo.n);
             } else {
@@ -1284,7 +1295,7 @@ void Sampler::autotune_sweeps() {
         if (lev == nlev - 1 && chol) break;
         Level &lv = L[lev];
         ensure_scratch(lev);
-        const bool vec = fp32 && !exact && lv.npt == 7 && (lv.g.sy % 4) == 0 && (lv.g.sz % 4) == 0;
+        const bool vec = fp32 && !exact && lv.npt == 7 && (lv.g.sy % 4) == 0 && (lv.g.sz % 4) == 0 && lv.var != 2;
         const int count = vec ? (lv.g.N0 + 8) / 8 : (lv.g.N0 + 1) / 2;
         int cap = 8;
         while (cap < count && cap < RBP_THREADS) cap *= 2;
@@ -1480,7 +1491,9 @@ void Sampler::ensure_solver() {
         capture(rgraph, rexec, [&]() {
             const StencilArg<double> st = stencil_arg<double>(l0, P.omega);
             const VarField<double> vf{l0.vw64, l0.geo.nalloc};
-            if (l0.var == 1) {
+            if (l0.var == 2) {
+                k_solve_resid<27, 2><<<pack_grid(l0), 256, 0, stream>>>(sv_x, sv_b, sv_r, l0.g, st, vf);
+            } else if (l0.var == 1) {
                 if (l0.npt == 7)
                     k_solve_resid<7, 1><<<pack_grid(l0), 256, 0, stream>>>(sv_x, sv_b, sv_r, l0.g, st, vf);
                 else
@@ -1994,6 +2007,17 @@ mgmc_status mgmc_measurement_vector(int dim, int nx, int ny, int nz, const doubl
         ++k;
     }
     *nnz = k;
+    API_END
+}
+
+mgmc_status mgmc_fem_field(int dim, int nx, int ny, int nz, int model, double p0, double p1, double *field) {
+    API_BEGIN
+    if (dim < 1 || dim > 3 || !field) fail(MGMC_ERR_INVALID_ARGUMENT, "dim must be 1, 2 or 3");
+    if (model != 0 && model != 1) fail(MGMC_ERR_INVALID_ARGUMENT, "model must be 0 (constant) or 1 (periodic)");
+    if (model == 1 && !(p0 > 0.0 && p1 >= p0)) fail(MGMC_ERR_INVALID_ARGUMENT, "periodic model needs 0 < Lambda_min <= Lambda_max");
+    Geometry g(dim, nx, ny, nz);
+    const std::vector<double> f = fem_field(g, model, p0, p1);
+    std::copy(f.begin(), f.end(), field);
     API_END
 }
 

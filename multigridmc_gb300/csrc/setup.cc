@@ -440,6 +440,89 @@ std::vector<double> galerkin_field(const Geometry &fine, const double stencil[27
     return out;
 }
 
+std::vector<double> fem_field(const Geometry &g, int model, double p0, double p1) {
+    const int dim = g.dim;
+    const int64_t n = g.n;
+    double h[3] = {1, 1, 1}, hinv2[3] = {0, 0, 0};
+    double cell_volume = 1.0;
+    for (int d = 0; d < dim; ++d) {
+        h[d] = 1. / double(g.c[d]);
+        hinv2[d] = 1. / (h[d] * h[d]);
+        cell_volume *= h[d];
+    }
+    // quadrature on [0,1]^d, first direction slowest (quadrature.cc:11-56)
+    const double q1[2] = {0.5 * (-1.0 / std::sqrt(3.0) + 1.0), 0.5 * (1.0 / std::sqrt(3.0) + 1.0)};
+    const int nq = 1 << dim, nb = 1 << dim;
+    std::vector<std::array<double, 3>> qp(nq);
+    std::vector<double> qw(nq);
+    for (int q = 0; q < nq; ++q) {
+        double w = 1.0;
+        for (int d = 0; d < dim; ++d) {
+            qp[q][d] = q1[(q >> (dim - 1 - d)) & 1];
+            w *= 0.5 * 1.0;
+        }
+        qw[q] = w;
+    }
+    // basis index alpha in {0,1}^d, first direction slowest
+    auto bit = [&](int a, int d) { return (a >> (dim - 1 - d)) & 1; };
+    auto phi = [&](int a, const std::array<double, 3> &x) {
+        double v = 1.0;
+        for (int j = 0; j < dim; ++j) v *= bit(a, j) == 0 ? (1.0 - x[j]) : x[j];
+        return v;
+    };
+    auto dphi = [&](int a, int k, const std::array<double, 3> &x) {
+        double v = 1.0;
+        for (int j = 0; j < dim; ++j)
+            v *= j == k ? (bit(a, j) == 0 ? -1.0 : 1.0) : (bit(a, j) == 0 ? (1.0 - x[j]) : x[j]);
+        return v;
+    };
+    std::vector<double> pp((size_t)nb * nb * nq), gg((size_t)nb * nb * nq);
+    for (int a = 0; a < nb; ++a)
+        for (int b = 0; b < nb; ++b)
+            for (int q = 0; q < nq; ++q) {
+                pp[((size_t)a * nb + b) * nq + q] = phi(a, qp[q]) * phi(b, qp[q]);
+                double s = 0.0;
+                for (int k = 0; k < dim; ++k) s += dphi(a, k, qp[q]) * (hinv2[k] * dphi(b, k, qp[q]));
+                gg[((size_t)a * nb + b) * nq + q] = s;
+            }
+    const double L1 = 0.5 * (p1 + p0), L2 = 0.5 * (p1 - p0);
+    auto kappa_sq = [&](const double *x) {
+        if (model == 0) return p0;
+        double lam = L2;
+        for (int d = 0; d < dim; ++d) lam *= std::cos(M_PI * x[d]);
+        lam += L1;
+        return 1. / (lam * lam);
+    };
+    std::vector<double> field((size_t)27 * n, 0.0);
+    const int nc[3] = {g.c[0], dim > 1 ? g.c[1] : 1, dim > 2 ? g.c[2] : 1};
+    for (int ck = 0; ck < nc[2]; ++ck)
+        for (int cj = 0; cj < nc[1]; ++cj)
+            for (int ci = 0; ci < nc[0]; ++ci) {  // cells in the reference's linear order
+                const int cell[3] = {ci, cj, ck};
+                for (int a = 0; a < nb; ++a)
+                    for (int b = 0; b < nb; ++b) {
+                        int va[3] = {1, 1, 1}, vb[3] = {1, 1, 1};
+                        bool inside = true;
+                        for (int d = 0; d < dim; ++d) {
+                            va[d] = cell[d] + bit(a, d);
+                            vb[d] = cell[d] + bit(b, d);
+                            inside = inside && va[d] > 0 && va[d] < g.c[d] && vb[d] > 0 && vb[d] < g.c[d];
+                        }
+                        if (!inside) continue;
+                        double local = 0.0;
+                        for (int q = 0; q < nq; ++q) {
+                            double x[3] = {0, 0, 0};
+                            for (int d = 0; d < dim; ++d) x[d] = h[d] * (qp[q][d] + double(cell[d]));
+                            local += (kappa_sq(x) * pp[((size_t)a * nb + b) * nq + q] + gg[((size_t)a * nb + b) * nq + q]) * qw[q];
+                        }
+                        const int64_t row = ((int64_t)(va[2] - 1) * g.N[1] + (va[1] - 1)) * g.N[0] + (va[0] - 1);
+                        const int k = (vb[2] - va[2] + 1) * 9 + (vb[1] - va[1] + 1) * 3 + (vb[0] - va[0] + 1);
+                        field[(size_t)k * n + row] += local * cell_volume;
+                    }
+            }
+    return field;
+}
+
 std::vector<double> dense_precision_field(const Geometry &g, const std::vector<double> &field, const SparseCols &B,
                                           const std::vector<double> &Sigma) {
     const int64_t n = g.n;

@@ -69,6 +69,14 @@ std::vector<double> dense_precision(const Geometry &g, const double st[27], cons
 // triple product.
 std::vector<double> galerkin_field(const Geometry &fine, const double stencil[27], const double *centre,
                                    const double *full);
+// ShiftedLaplaceFEMOperator (shiftedlaplace_fem_operator.cc:9-152): Q1
+// elements, the 2-point Gauss-Legendre rule per direction, local entries
+// (kappa^2(x_q) phi_a phi_b + sum_d h_d^{-2} dphi_a dphi_b) w_q times the
+// cell volume, between interior vertices only.  kappa^2 is constant
+// (model 0, p0 = kappa^2) or periodic (model 1, correlationlength_model.hh:
+// 83-112, p0 = Lambda_min, p1 = Lambda_max).  Returns the weight-major
+// per-point field (27 x n; inactive directions keep zero weights).
+std::vector<double> fem_field(const Geometry &g, int model, double p0, double p1);
 // dense row-major A_0 + B Sigma^{-1} B^T of a level with a weight-major
 // per-point stencil field (27 x n)
 std::vector<double> dense_precision_field(const Geometry &g, const std::vector<double> &field, const SparseCols &B,

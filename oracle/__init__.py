@@ -85,6 +85,7 @@ def lib():
         "orc_ssor_smoother_apply": (None, [_P, C.c_double, C.c_int, C.c_int, _D, _D]),
         "orc_dense_cholesky": (C.c_int, [_D, C.c_int64]),
         "orc_op_set_diagonal": (None, [_P, _D]),
+        "orc_fem_operator": (_P, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double]),
         "orc_mg_create": (_P, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int,
                                C.c_int]),
         "orc_mg_destroy": (None, [_P]),
@@ -208,6 +209,13 @@ class Operator:
     @classmethod
     def fd(cls, shape, kappa_sq):
         return cls(lib().orc_fd_operator(*_dims(len(shape), shape), kappa_sq), shape)
+
+    @classmethod
+    def fem(cls, shape, model, p0, p1=0.0):
+        """ShiftedLaplaceFEMOperator: model 0 constant kappa^2 = p0, model 1
+        periodic correlation length (Lambda_min, Lambda_max)."""
+        dim, nx, ny, nz = _dims(len(shape), shape)
+        return cls(lib().orc_fem_operator(dim, nx, ny, nz, int(model), float(p0), float(p1)), shape)
 
     @classmethod
     def from_stencil(cls, shape, stencil27):

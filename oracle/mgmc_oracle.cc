@@ -327,6 +327,104 @@ struct Quadrature {  // quadrature.cc:11-56
     }
 };
 
+// ShiftedLaplaceFEMOperator (shiftedlaplace_fem_operator.cc:9-152): Q1
+// elements with GaussLegendreQuadrature(dim, 1); every pair (alpha, beta) of
+// basis functions of every cell whose corners are interior vertices adds
+// sum_q (kappa^2(x_q) phi_a phi_b + grad phi_a . h^{-2} grad phi_b) w_q times
+// the cell volume (cells in linear order, alpha and beta in
+// cartesian-product order).  model 0: kappa^2 = p0; model 1: periodic
+// correlation length, Lambda_min = p0, Lambda_max = p1
+// (correlationlength_model.hh:83-112).
+static std::shared_ptr<LinOp> fem_operator(const Lattice &lat, int model, double p0, double p1) {
+    const int dim = lat.dim;
+    double h[3] = {1, 1, 1}, hinv2[3] = {0, 0, 0}, cell_volume = 1.0;
+    for (int d = 0; d < dim; ++d) {
+        h[d] = 1. / double(lat.n[d]);
+        hinv2[d] = 1. / (h[d] * h[d]);
+        cell_volume *= h[d];
+    }
+    Quadrature quad(dim, 1);
+    auto basis = cartesian_product(std::vector<int>{0, 1}, dim);
+    auto phi = [&](const std::vector<int> &a, const std::vector<double> &x) {
+        double v = 1.0;
+        for (int j = 0; j < dim; ++j) v *= a[j] == 0 ? (1.0 - x[j]) : x[j];
+        return v;
+    };
+    auto dphi = [&](const std::vector<int> &a, int k, const std::vector<double> &x) {
+        double v = 1.0;
+        for (int j = 0; j < dim; ++j) v *= j == k ? (a[j] == 0 ? -1.0 : 1.0) : (a[j] == 0 ? (1.0 - x[j]) : x[j]);
+        return v;
+    };
+    std::vector<double> pp, gg;
+    for (auto &a : basis)
+        for (auto &b : basis)
+            for (auto &x : quad.points) {
+                pp.push_back(phi(a, x) * phi(b, x));
+                double sg = 0.0;
+                for (int k = 0; k < dim; ++k) sg += dphi(a, k, x) * (hinv2[k] * dphi(b, k, x));
+                gg.push_back(sg);
+            }
+    const double L1 = 0.5 * (p1 + p0), L2 = 0.5 * (p1 - p0);
+    auto kappa_sq = [&](const double *x) {
+        if (model == 0) return p0;
+        double lam = L2;
+        for (int d = 0; d < dim; ++d) lam *= cos(M_PI * x[d]);
+        lam += L1;
+        return 1. / (lam * lam);
+    };
+    const int64_t n = lat.nvertex();
+    std::vector<std::map<int64_t, double>> rows(n);
+    int64_t ncell = 1;
+    for (int d = 0; d < dim; ++d) ncell *= lat.n[d];
+    for (int64_t cidx = 0; cidx < ncell; ++cidx) {
+        int cell[3] = {0, 0, 0};
+        int64_t t = cidx;
+        for (int d = 0; d < dim; ++d) {
+            cell[d] = (int)(t % lat.n[d]);
+            t /= lat.n[d];
+        }
+        size_t count = 0;
+        for (auto &a : basis)
+            for (auto &b : basis) {
+                int va[3] = {1, 1, 1}, vb[3] = {1, 1, 1};
+                bool inside = true;
+                for (int d = 0; d < dim; ++d) {
+                    va[d] = cell[d] + a[d];
+                    vb[d] = cell[d] + b[d];
+                    inside = inside && va[d] > 0 && va[d] < lat.n[d] && vb[d] > 0 && vb[d] < lat.n[d];
+                }
+                if (!inside) {
+                    count += quad.points.size();
+                    continue;
+                }
+                double local = 0.0;
+                for (size_t j = 0; j < quad.points.size(); ++j) {
+                    double x[3] = {0, 0, 0};
+                    for (int d = 0; d < dim; ++d) x[d] = h[d] * (quad.points[j][d] + double(cell[d]));
+                    local += (kappa_sq(x) * pp[count] + gg[count]) * quad.weights[j];
+                    count++;
+                }
+                rows[lat.vertex_linear(va)][lat.vertex_linear(vb)] += local * cell_volume;
+            }
+    }
+    auto op = std::make_shared<LinOp>(lat);
+    Csr &A = op->A;
+    A.n = n;
+    A.ptr.assign(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        for (auto &e : rows[i]) {
+            A.col.push_back(e.first);
+            A.val.push_back(e.second);
+        }
+        A.ptr[i + 1] = (int64_t)A.col.size();
+    }
+    A.finish_diag();
+    op->B.nrow = n;
+    op->B.m = 0;
+    op->B.ptr.assign(1, 0);
+    return op;
+}
+
 static double norm_diff(const double *a, const double *b, int dim) {
     double s = 0.0;
     for (int d = 0; d < dim; ++d) s += (a[d] - b[d]) * (a[d] - b[d]);
@@ -1438,6 +1536,9 @@ void orc_fd_stencil(int dim, int nx, int ny, int nz, double kappa_sq, double *st
 }
 orc_op *orc_stencil_operator(int dim, int nx, int ny, int nz, const double *st) {
     return new orc_op{stencil_operator(Lattice(dim, nx, ny, nz), st)};
+}
+orc_op *orc_fem_operator(int dim, int nx, int ny, int nz, int model, double p0, double p1) {
+    return new orc_op{fem_operator(Lattice(dim, nx, ny, nz), model, p0, p1)};
 }
 orc_op *orc_fd_operator(int dim, int nx, int ny, int nz, double kappa_sq) {
     Lattice lat(dim, nx, ny, nz);

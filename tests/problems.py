@@ -66,3 +66,23 @@ def periodic_posterior(shape, Lambda_min=0.12, Lambda_max=0.23, m=0, radius=0.05
         op_o.add_measurements(loc, var, variance_scaling=variance, radius=radius)
         op_p = op_p.with_measurements(loc, var, variance_scaling=variance, radius=radius)
     return op_o, op_p
+
+
+def fem_posterior(shape, periodic=True, kappa_sq=10.0, Lambda_min=0.12, Lambda_max=0.23, m=0, radius=0.05,
+                  variance=1e-4, seed=1, lo=0.1, hi=0.9):
+    """Shifted-Laplace FEM prior (constant kappa^2 or the periodic
+    correlation length) with m ball measurements."""
+    dim = len(shape)
+    if periodic:
+        op_p = M.LinearOperator.shifted_laplace_fem_periodic(shape, Lambda_min, Lambda_max)
+        op_o = O.Operator.fem(list(shape), 1, Lambda_min, Lambda_max)
+    else:
+        op_p = M.LinearOperator.shifted_laplace_fem(shape, kappa_sq)
+        op_o = O.Operator.fem(list(shape), 0, kappa_sq)
+    if m > 0:
+        rng = np.random.default_rng(seed)
+        loc = rng.uniform(lo, hi, size=(m, dim))
+        var = np.ones(m)
+        op_o.add_measurements(loc, var, variance_scaling=variance, radius=radius)
+        op_p = op_p.with_measurements(loc, var, variance_scaling=variance, radius=radius)
+    return op_o, op_p

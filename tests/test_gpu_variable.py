@@ -10,7 +10,7 @@ import pytest
 
 import multigridmc_gb300 as M
 import oracle as O
-from problems import periodic_posterior, rhs
+from problems import fem_posterior, periodic_posterior, rhs
 from test_gpu_parity import _mg, _run_parity
 
 pytestmark = pytest.mark.gpu
@@ -22,6 +22,10 @@ CASES = [
     ("3d-post-16-sor-w-coarse-ssor", lambda: periodic_posterior((16, 16, 16), m=4),
      _mg(3, omega=0.9, cycle=2, smoother="SOR", coarse="SSOR")),
     ("3d-post-32", lambda: periodic_posterior((32, 32, 32), m=8), _mg(4)),
+    # the FEM prior: a per-vertex 27-point (9-point in 2D) stencil on the fine level
+    ("2d-fem-periodic-32", lambda: fem_posterior((32, 32), m=3, radius=0.1), _mg(4)),
+    ("3d-fem-periodic-16", lambda: fem_posterior((16, 16, 16), m=4), _mg(3)),
+    ("3d-fem-constant-16", lambda: fem_posterior((16, 16, 16), periodic=False, m=4), _mg(3)),
 ]
 
 
@@ -118,3 +122,27 @@ def test_refused_combinations():
         s.adjoint_params(np.zeros(op.n), np.ones(op.n), np.zeros(op.n))
     assert e.value.name == "MGMC_ERR_UNSUPPORTED"
     s.close()
+
+
+@pytest.mark.parametrize("lowrank", [False, True], ids=["prior", "measured"])
+@pytest.mark.parametrize("precision", [M.FP64, M.FP32_MIXED], ids=["fp64", "fp32-mixed"])
+def test_reference_solver_tests_fem(lowrank, precision):
+    """TestMultigrid / TestMultigridLowRank of test_solver.hh:112-170 on their
+    operator: the FEM prior with the periodic correlation length (Lambda in
+    [0.12, 0.23]) on 256^2, 10 measurements with variance 1 + 2U scaled by
+    1e-6 for the low-rank case; 5 levels, SSOR V(1,1), rtol 1e-13, atol 1e-12
+    (1e-11), maxiter 100; relative error below 1e-10."""
+    rng = np.random.default_rng(1212417)
+    op = M.LinearOperator.shifted_laplace_fem_periodic((256, 256), 0.12, 0.23)
+    if lowrank:
+        loc = rng.uniform(size=(10, 2))
+        var = 1.0 + 2.0 * rng.uniform(size=10)
+        op = op.with_measurements(loc, var, variance_scaling=1e-6, radius=0.05)
+    x_exact = np.random.default_rng(3).standard_normal(op.n)
+    b = op.to_scipy() @ x_exact
+    P = M.MultigridPreconditioner(op, _mg(5), precision=precision)
+    S = M.LoopSolver(op, P, M.IterativeSolverParameters(rtol=1e-13, atol=1e-11 if lowrank else 1e-12, maxiter=100))
+    x = S.apply(b)
+    P.close()
+    assert S.converged
+    assert np.linalg.norm(x - x_exact) / np.linalg.norm(x_exact) < 1e-10

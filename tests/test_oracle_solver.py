@@ -1,9 +1,9 @@
 """Oracle pins for the deterministic solvers: the reference's
 src/solver/test_solver.hh (CholeskySolver, multigrid-preconditioned
-LoopSolver with and without measurements), restated on the shifted-Laplace
-FD operator (the FEM operator with the periodic correlation-length model of
-those tests is not part of this build) with numpy-seeded exact solutions,
-plus the oracle's two coarse-solve forms against each other."""
+LoopSolver with and without measurements) on its operator, the
+shifted-Laplace FEM operator with the periodic correlation length
+(Lambda in [0.12, 0.23]), with numpy-seeded exact solutions and measurement
+locations, plus the oracle's two coarse-solve forms against each other."""
 import numpy as np
 import pytest
 
@@ -11,10 +11,11 @@ import oracle as O
 
 
 def _measured(shape, n_meas=10, variance_scaling=1e-6, radius=0.05, seed=1212417):
-    """test_solver.hh:22-80: 10 ball measurements at uniform locations with
-    variance 1 + 2 U, scaled by 1e-6."""
+    """test_solver.hh:22-80: FEM operator, periodic correlation length, 10
+    ball measurements at uniform locations with variance 1 + 2 U, scaled by
+    1e-6."""
     rng = np.random.default_rng(seed)
-    op = O.Operator.fd(list(shape), 1.0 / 0.15 ** 2)
+    op = _prior(shape)
     loc = rng.uniform(size=(n_meas, len(shape)))
     var = 1.0 + 2.0 * rng.uniform(size=n_meas)
     op.add_measurements(loc, var, variance_scaling=variance_scaling, radius=radius)
@@ -22,7 +23,7 @@ def _measured(shape, n_meas=10, variance_scaling=1e-6, radius=0.05, seed=1212417
 
 
 def _prior(shape):
-    return O.Operator.fd(list(shape), 1.0 / 0.15 ** 2)
+    return O.Operator.fem(list(shape), 1, 0.12, 0.23)
 
 
 def _exact(op, seed=3):
