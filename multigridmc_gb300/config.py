@@ -124,6 +124,7 @@ class RunConfig:
     measurements: dict = field(default_factory=dict)
     measurement_data: dict = field(default_factory=dict)
     correlation: str = "constant"  # or "periodic": Lambda_min, Lambda_max below
+    pdemodel: str = "shiftedlaplace_fd"  # or "shiftedlaplace_fem"
     Lambda_min: float = 0.0
     Lambda_max: float = 0.0
 
@@ -145,13 +146,16 @@ class RunConfig:
                                    coarse_scaling=float(mg["coarse_scaling"]))
 
     def linear_operator(self):
-        """The prior (ShiftedLaplaceFDOperator) or the posterior
+        """The prior (ShiftedLaplaceFDOperator or ShiftedLaplaceFEMOperator) or the posterior
         (MeasuredOperator) of the configuration (driver_mgmc.cc:120-160)."""
         from . import LinearOperator
+        fem = self.pdemodel == "shiftedlaplace_fem"
         if self.correlation == "periodic":
-            op = LinearOperator.shifted_laplace_fd_periodic(self.shape, self.Lambda_min, self.Lambda_max)
+            build = LinearOperator.shifted_laplace_fem_periodic if fem else LinearOperator.shifted_laplace_fd_periodic
+            op = build(self.shape, self.Lambda_min, self.Lambda_max)
         else:
-            op = LinearOperator.shifted_laplace_fd(self.shape, self.kappa_sq)
+            op = (LinearOperator.shifted_laplace_fem if fem else LinearOperator.shifted_laplace_fd)(self.shape,
+                                                                                                  self.kappa_sq)
         if self.operator == "prior":
             return op
         ms, md = self.measurements, self.measurement_data
@@ -197,13 +201,15 @@ def load_run(parameters_file, measurements_file=None):
         raise ValueError("operator has to be 'prior' or 'posterior'")
     prior = root.get("prior", {"pdemodel": "shiftedlaplace_fd", "correlationlengthmodel": "constant"})
     model = prior.get("correlationlengthmodel")
-    if prior.get("pdemodel") != "shiftedlaplace_fd" or model not in ("constant", "periodic"):
-        raise NotImplementedError("only the shifted-Laplace FD prior (constant or periodic correlation length) is on "
-                                  "the GPU sampling path")
+    if prior.get("pdemodel") not in ("shiftedlaplace_fd", "shiftedlaplace_fem") or model not in ("constant",
+                                                                                                  "periodic"):
+        raise NotImplementedError("the GPU sampling path takes the shifted-Laplace FD or FEM prior with a constant "
+                                  "or periodic correlation length")
     Lambda = float(root["constantcorrelationlengthmodel"]["Lambda"]) if model == "constant" else 0.0
     cfg = RunConfig(dim=dim, shape=shape, operator=operator, Lambda=Lambda, multigrid=root["multigrid"],
                     smoother=root.get("smoother", {}), sampling=root.get("sampling", {}),
-                    measurements=root.get("measurements", {}), correlation=model)
+                    measurements=root.get("measurements", {}), correlation=model,
+                    pdemodel=prior.get("pdemodel", "shiftedlaplace_fd"))
     if model == "periodic":  # parameters.cc:236-256
         per = root["periodiccorrelationlengthmodel"]
         cfg.Lambda_min, cfg.Lambda_max = float(per["Lambda_min"]), float(per["Lambda_max"])

@@ -87,3 +87,20 @@ def test_periodic_correlation_length(tmp_path):
     assert np.array_equal(op.centre, ref.centre) and np.array_equal(op.stencil, ref.stencil)
     with pytest.raises(ValueError):
         cfg.kappa_sq
+
+
+def test_fem_prior(tmp_path):
+    """prior.pdemodel = "shiftedlaplace_fem" gives the FEM operator
+    (constant or periodic correlation length)."""
+    text = PARAMS.replace('pdemodel = "shiftedlaplace_fd"', 'pdemodel = "shiftedlaplace_fem"').replace(
+        'operator = "posterior"', 'operator = "prior"')
+    (tmp_path / "params.cfg").write_text(text)
+    op = load_run(str(tmp_path / "params.cfg")).linear_operator()
+    ref = M.LinearOperator.shifted_laplace_fem((32, 16), 16.0)
+    assert np.array_equal(op.stencil, ref.stencil) and op.field is None
+    text = text.replace('correlationlengthmodel = "constant"', 'correlationlengthmodel = "periodic"') + \
+        "periodiccorrelationlengthmodel = { Lambda_min = 0.12; Lambda_max = 0.23; };\n"
+    (tmp_path / "params.cfg").write_text(text)
+    op = load_run(str(tmp_path / "params.cfg")).linear_operator()
+    ref = M.LinearOperator.shifted_laplace_fem_periodic((32, 16), 0.12, 0.23)
+    assert np.array_equal(op.field, ref.field)
