@@ -43,6 +43,8 @@ IACT_WINDOW = 50
 RB_VEC_DRAM_BYTES = 115.01e6
 METRIC = "indep. samples/s (rate/IACT), 3D 256³ posterior: mixed vs FP64 plain, 1 GB300"
 UNIT = "indep_samples/s"
+WORKLOAD = ("3D 256^3 posterior MGMC V(1,1) SSOR omega=1, 5 levels, coarse dense Cholesky 16^3, "
+            "64 measurements r=0.05 Sigma=1e-4, kappa^2=10")
 PUBLISHED_MGMC_IACT = 1.28  # python/plot_summary.py:28-29, MGMC at 64^3
 
 
@@ -875,8 +877,8 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
                 "steps": r["steps"], "warmup": 1, "ms_per_step": r["per_step_s"] * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": "3D 256^3 posterior MGMC V(1,1) SSOR, 5 levels, m=64", "precision": "fp64",
-                           "ordering": "lexicographic"},
+                "config": {"workload": WORKLOAD, "unknowns": int(np.prod([n - 1 for n in SHAPE])),
+                           "precision": "fp64", "ordering": "lexicographic (the reference's sweep order)"},
                 "cpu_baseline": {"value": val, "unit": UNIT, "cores": r["threads"], "kind": "port", "sample": sample},
                 "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
@@ -940,8 +942,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (FP64 Cholesky factorisation and m x m low-rank system)", "data": "synthetic",
-        "config": {"workload": "3D 256^3 posterior MGMC V(1,1) SSOR omega=1, 5 levels, coarse dense Cholesky 16^3, "
-                               "64 measurements r=0.05 Sigma=1e-4, kappa^2=10",
+        "config": {"workload": WORKLOAD,
                    "unknowns": int(op.n), "ordering": "multicolour (red-black fine, 8-colour coarse)",
                    "noise": "in-kernel Philox4x32-10", "parallelism": f"replicas x{world}",
                    "l2": "per-step working set > L2 (x and f alone 134 MB FP32 / 268 MB FP64)",
