@@ -439,6 +439,7 @@ class MultigridMCSampler:
         p.ordering, p.precision, p.noise = ordering, precision, noise
         p.seed = seed
         p.device = device
+        self._args = dict(ordering=ordering, precision=precision, noise=noise, device=device)
         self._h = C.c_void_p()
         desc = linear_operator._desc()
         self._L = load()
@@ -463,8 +464,27 @@ class MultigridMCSampler:
         return x
 
     def fix_rhs(self, f):
+        """The right hand side ``step()`` samples with (Sampler::fix_rhs,
+        sampler.hh:64); ``apply(f, x)`` always uses its own f, as in the
+        reference, whose MultigridMCSampler inherits the no-op fix_rhs."""
         f = _f64(f)
         _check(self._L.mgmc_sampler_fix_rhs(self._h, _dp(f), 0))
+
+    def unfix_rhs(self):
+        """Sampler::unfix_rhs (sampler.hh:71): a no-op for this sampler --
+        ``apply(f, x)`` reads its f on every call either way."""
+
+    def get_linear_operator(self):
+        """Sampler::get_linear_operator (sampler.hh:51-54)."""
+        return self.op
+
+    def deep_copy(self, seed):
+        """Sampler::deep_copy (sampler.hh:40, multigridmc_sampler.hh:50-57):
+        a new sampler of the same operator and parameters that draws from its
+        own noise stream -- the Philox key ``seed`` in place of the
+        reference's RandomGenerator -- with its own chain state (zero) and
+        no fixed right hand side.  The copy shares nothing on the device."""
+        return MultigridMCSampler(self.op, self.params, seed=seed, **self._args)
 
     def set_state(self, x):
         x = _f64(x)
@@ -750,7 +770,10 @@ class ExactSampler:
 
 def CholeskySampler(linear_operator, **kw):
     """Exact sampler with the dense natural-order Cholesky factor
-    (DenseCholeskySampler, cholesky_sampler.cc:25-37)."""
+    (DenseCholeskySampler, cholesky_sampler.cc:25-37).  Its ``apply(f, x)``
+    reads f on every call; the reference's Cholesky samplers, after
+    ``fix_rhs(f0)``, sample with f0 whatever f ``apply`` is given
+    (cholesky_sampler.hh:52-66; its callers pass the same f)."""
     p = MultigridParameters(nlevel=1, coarse_solver="Cholesky")
     return MultigridMCSampler(linear_operator, p, **kw)
 

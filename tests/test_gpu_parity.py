@@ -164,3 +164,29 @@ def test_autotuned_shapes_do_not_change_the_chain(monkeypatch):
         states.append(s.get_state())
         s.close()
     assert np.array_equal(states[0], states[1])
+
+
+def test_sampler_surface_deep_copy():
+    """Sampler::deep_copy / get_linear_operator / unfix_rhs (sampler.hh:40-71):
+    a deep copy with the original's seed runs the original's chain bit for bit
+    from zero, whatever state the original is in; another seed gives another
+    chain; the copy shares the operator and nothing on the device."""
+    _, op = posterior((32, 32, 32), m=8)
+    f = rhs(op)
+    a = M.MultigridMCSampler(op, _mg(4), precision=M.FP32_MIXED, seed=11)
+    xa = np.zeros(op.n)
+    for _ in range(3):
+        a.apply(f, xa)
+    b, c = a.deep_copy(11), a.deep_copy(12)
+    assert b.get_linear_operator() is op and c.params is a.params
+    xb, xc = np.zeros(op.n), np.zeros(op.n)
+    for _ in range(3):
+        b.apply(f, xb)
+        c.apply(f, xc)
+    assert np.array_equal(xa, xb)
+    assert not np.array_equal(xa, xc)
+    a.unfix_rhs()
+    a.apply(f, xa)
+    assert np.array_equal(b.get_state(), xb)
+    for s in (a, b, c):
+        s.close()
