@@ -14,6 +14,8 @@ this module              reference (eikehmueller/MultigridMC)
 ``SSORSampler``          SSORSampler (sampler/ssor_sampler.{hh,cc})
 ``CholeskySampler``      DenseCholeskySampler (sampler/cholesky_sampler.cc:25-37)
 ``MultigridPreconditioner``  MultigridPreconditioner (preconditioner/multigrid_preconditioner.cc:8-108)
+``SORSmoother``          SORSmoother (smoother/sor_smoother.cc:9-78), nsmooth = 1
+``SSORSmoother``         SSORSmoother (smoother/ssor_smoother.cc:9-16)
 ``ExactSampler``         exact draws x = Q^{-1}(f + eta), the comparator role of SparseCholeskySampler
                          (sampler/cholesky_sampler.cc:9-23)
 ``LoopSolver``           LoopSolver (solver/loop_solver.cc:9-53) with IterativeSolverParameters
@@ -38,7 +40,8 @@ from . import build as _build
 __all__ = [
     "MGMCError", "load", "fd_stencil", "galerkin_stencil", "measurement_vector", "LinearOperator",
     "MultigridParameters", "MultigridMCSampler", "MultigridMCBatch", "SSORSampler", "CholeskySampler",
-    "IterativeSolverParameters", "MultigridPreconditioner", "LoopSolver", "ExactSampler",
+    "IterativeSolverParameters", "MultigridPreconditioner", "LoopSolver", "ExactSampler", "SORSmoother",
+    "SSORSmoother",
     "FP64", "FP32_MIXED", "LEXICOGRAPHIC", "MULTICOLOUR", "PHILOX", "INJECTED", "FORWARD", "BACKWARD",
 ]
 
@@ -704,6 +707,36 @@ class MultigridMCSampler:
         f = _f64(f)
         assert x.dtype == np.float64 and x.flags.c_contiguous
         _check(self._L.mgmc_level_sor(self._h, level, direction, int(with_noise), _dp(f), _dp(x)))
+        return x
+
+
+class SORSmoother:
+    """SORSmoother::apply (smoother/sor_smoother.cc:40-78) with nsmooth = 1,
+    the form every sampler and SSORSmoother builds: one noise-free SOR sweep
+    of level ``level`` of ``sampler``'s hierarchy (its operator and omega) in
+    ``direction``, then the low-rank correction x -= Bbar B^T x.  ``x`` is
+    updated in place."""
+
+    def __init__(self, sampler, level=0, direction=FORWARD):
+        self.sampler, self.level, self.direction = sampler, level, direction
+
+    def apply(self, b, x):
+        return self.sampler.sor(self.level, self.direction, b, x, with_noise=False)
+
+
+class SSORSmoother:
+    """SSORSmoother::apply (smoother/ssor_smoother.cc:9-16): ``nsmooth``
+    times a forward then a backward SORSmoother on one level."""
+
+    def __init__(self, sampler, level=0, nsmooth=1):
+        self.forward = SORSmoother(sampler, level, FORWARD)
+        self.backward = SORSmoother(sampler, level, BACKWARD)
+        self.nsmooth = nsmooth
+
+    def apply(self, b, x):
+        for _ in range(self.nsmooth):
+            self.forward.apply(b, x)
+            self.backward.apply(b, x)
         return x
 
 

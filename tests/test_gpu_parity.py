@@ -190,3 +190,25 @@ def test_sampler_surface_deep_copy():
     assert np.array_equal(b.get_state(), xb)
     for s in (a, b, c):
         s.close()
+
+
+@pytest.mark.parametrize("ordering", [M.LEXICOGRAPHIC, M.MULTICOLOUR], ids=["lex", "multicolour"])
+def test_ssor_smoother(ordering):
+    """SSORSmoother::apply (ssor_smoother.cc:9-16) with nsmooth = 2 on the
+    fine and the first coarse level of a 2D posterior against the oracle's
+    forward / backward SOR sweeps fed zero noise (the smoother), 1e-12."""
+    op_o, op_p = posterior((32, 32), m=4, radius=0.1)
+    gpu = M.MultigridMCSampler(op_p, _mg(3, omega=1.2), ordering=ordering, noise=M.INJECTED)
+    ops = [op_o, op_o.coarsen()]
+    rng = np.random.default_rng(5)
+    for lev, oo in enumerate(ops):
+        b = rng.standard_normal(oo.n)
+        x0 = rng.standard_normal(oo.n)
+        xo = x0.copy()
+        for _ in range(2):
+            for fwd in (True, False):
+                src = O.Source(np.zeros(oo.n + oo.m))
+                O.sor_sampler(oo, src, 1.2, forward=fwd, ordering=ordering).apply(b, xo)
+        xg = M.SSORSmoother(gpu, lev, nsmooth=2).apply(b, x0.copy())
+        assert np.linalg.norm(xg - xo) <= 1e-12 * np.linalg.norm(xo), lev
+    gpu.close()
