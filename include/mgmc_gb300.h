@@ -27,6 +27,8 @@
  *   mgmc_measurement_vector  MeasuredOperator::measurement_vector
  *                                                     src/linear_operator/measured_operator.cc:69-171
  *   mgmc_galerkin_stencil    LinearOperator::coarsen  src/linear_operator/linear_operator.cc:10-23
+ *   mgmc_operator_coarsen    LinearOperator::coarsen  src/linear_operator/linear_operator.cc:10-23
+ *                            (the whole operator: stencil or field, B_c = R B)
  *   mgmc_sampler_precondition MultigridPreconditioner::apply src/preconditioner/multigrid_preconditioner.cc:102-108
  *   mgmc_sampler_solve       LoopSolver::apply        src/solver/loop_solver.cc:9-53
  *
@@ -154,6 +156,17 @@ mgmc_status mgmc_fem_field(int dim, int nx, int ny, int nz, int model, double p0
 /* Galerkin triple product R A R^T of a constant stencil with the linear
  * intergrid operator (linear_operator.cc:10-23, intergrid_operator_linear.cc:8-31). */
 mgmc_status mgmc_galerkin_stencil(int dim, const double fine[27], double coarse[27]);
+/* LinearOperator::coarsen (linear_operator.cc:10-23) of a whole operator on
+ * the host: the coarse lattice has half the cells per direction; its
+ * stencil R A R^T goes to coarse_stencil, and for a per-vertex operator
+ * (op->centre or op->field set) its per-vertex Galerkin stencils, 27 x n_c
+ * weight-major, go to coarse_field (required then, ignored otherwise);
+ * B_c = R B (CSC, row indices ascending) goes to Bc_colptr (m+1 entries) and
+ * Bc_rowidx / Bc_val (cap entries each).  *nnz receives nnz(B_c); call with
+ * Bc_rowidx = Bc_val = NULL to size them.  Sigma is unchanged. */
+mgmc_status mgmc_operator_coarsen(const mgmc_operator_desc *op, double coarse_stencil[27], double *coarse_field,
+                                  int64_t *Bc_colptr, int64_t *Bc_rowidx, double *Bc_val, int64_t cap,
+                                  int64_t *nnz);
 
 /* ------------------------------------------------------------- sampler */
 mgmc_status mgmc_sampler_create(const mgmc_operator_desc *op, const mgmc_sampler_params *params,

@@ -94,6 +94,7 @@ SIGNATURES = {
     "mgmc_measurement_vector": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _D, C.c_double, _I64, _D,
                                           C.c_int64, _I64]),
     "mgmc_galerkin_stencil": (C.c_int, [C.c_int, _D, _D]),
+    "mgmc_operator_coarsen": (C.c_int, [C.POINTER(_OpDesc), _D, _D, _I64, _I64, _D, C.c_int64, _I64]),
     "mgmc_fem_field": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _D]),
     "mgmc_sampler_create": (C.c_int, [C.POINTER(_OpDesc), C.POINTER(_Params), C.POINTER(_P)]),
     "mgmc_sampler_destroy": (C.c_int, [_P]),
@@ -339,6 +340,29 @@ class LinearOperator:
             cols.append((np.arange(self.n, dtype=np.int64), np.full(self.n, cv)))
             sigma.append(variance_global)
         return self.with_lowrank(cols, sigma)
+
+    def coarsen(self):
+        """LinearOperator::coarsen (linear_operator.cc:10-23): the operator
+        R A R^T + (R B) Sigma^{-1} (R B)^T on the lattice with half the cells
+        per direction (mgmc_operator_coarsen), with the coarse stencil, the
+        coarse per-vertex stencils of a variable operator and B_c = R B."""
+        cshape = tuple(s // 2 for s in self.shape)
+        nc = int(np.prod([s - 1 for s in cshape]))
+        variable = self.centre is not None or self.field is not None
+        st = np.zeros(27)
+        cf = np.zeros((27, nc)) if variable else None
+        ptr = np.zeros(self.m + 1, np.int64)
+        nnz = C.c_int64(0)
+        desc = self._desc()
+        L = load()
+        cfp = _dp(cf) if variable else None
+        _check(L.mgmc_operator_coarsen(C.byref(desc), _dp(st), cfp, ptr.ctypes.data_as(_I64), None, None, 0,
+                                       C.byref(nnz)))
+        idx = np.zeros(nnz.value, np.int64)
+        val = np.zeros(nnz.value)
+        _check(L.mgmc_operator_coarsen(C.byref(desc), _dp(st), cfp, ptr.ctypes.data_as(_I64),
+                                       idx.ctypes.data_as(_I64), _dp(val), nnz.value, C.byref(nnz)))
+        return LinearOperator(cshape, st, ptr, idx, val, np.array(self.Sigma, dtype=float), field=cf)
 
     def to_scipy(self):
         """A = A_0 + B Sigma^{-1} B^T as a scipy.sparse CSR matrix in the

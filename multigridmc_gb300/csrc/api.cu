@@ -2036,6 +2036,49 @@ mgmc_status mgmc_galerkin_stencil(int dim, const double fine[27], double coarse[
     API_END
 }
 
+mgmc_status mgmc_operator_coarsen(const mgmc_operator_desc *op, double coarse_stencil[27], double *coarse_field,
+                                  int64_t *Bc_colptr, int64_t *Bc_rowidx, double *Bc_val, int64_t cap, int64_t *nnz) {
+    API_BEGIN
+    if (!op || !coarse_stencil || !nnz) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    if (op->dim < 1 || op->dim > 3) fail(MGMC_ERR_INVALID_ARGUMENT, "dim must be 1, 2 or 3");
+    const int cells[3] = {op->nx, op->dim > 1 ? op->ny : 2, op->dim > 2 ? op->nz : 2};
+    for (int d = 0; d < op->dim; ++d)
+        if (cells[d] < 2) fail(MGMC_ERR_LATTICE, "every active direction needs at least 2 cells");
+    const Geometry g(op->dim, cells[0], cells[1], cells[2]);
+    if (!g.coarsenable()) fail(MGMC_ERR_LATTICE, "cannot coarsen the lattice [odd extent or no interior vertices left]");
+    if (op->m < 0 || (op->m > 0 && (!op->B_colptr || !op->B_rowidx || !op->B_val)))
+        fail(MGMC_ERR_INVALID_ARGUMENT, "low-rank term needs B");
+    if ((op->centre || op->field) && !coarse_field)
+        fail(MGMC_ERR_INVALID_ARGUMENT, "a per-vertex operator needs coarse_field (27 x n_c doubles)");
+    galerkin_stencil(op->dim, op->stencil, coarse_stencil);
+    if (op->centre || op->field) {
+        const std::vector<double> cf = galerkin_field(g, op->stencil, op->field ? nullptr : op->centre, op->field);
+        std::copy(cf.begin(), cf.end(), coarse_field);
+    }
+    SparseCols B;
+    B.m = op->m;
+    if (op->m > 0) {
+        B.ptr.assign(op->B_colptr, op->B_colptr + op->m + 1);
+        for (int j = 0; j < op->m; ++j)
+            for (i64 e = op->B_colptr[j]; e < op->B_colptr[j + 1]; ++e) {
+                if (op->B_rowidx[e] < 0 || op->B_rowidx[e] >= g.n) fail(MGMC_ERR_INVALID_ARGUMENT, "B row index out of range");
+                if (e > op->B_colptr[j] && op->B_rowidx[e] <= op->B_rowidx[e - 1])
+                    fail(MGMC_ERR_INVALID_ARGUMENT, "B row indices must ascend within a column");
+            }
+        B.row.assign(op->B_rowidx, op->B_rowidx + op->B_colptr[op->m]);
+        B.val.assign(op->B_val, op->B_val + op->B_colptr[op->m]);
+    }
+    const SparseCols Bc = op->m > 0 ? restrict_columns(g, B) : B;
+    *nnz = Bc.ptr[op->m];
+    if (Bc_colptr) std::copy(Bc.ptr.begin(), Bc.ptr.end(), Bc_colptr);
+    if (Bc_rowidx || Bc_val) {
+        if (!Bc_rowidx || !Bc_val || cap < *nnz) fail(MGMC_ERR_INVALID_ARGUMENT, "Bc arrays missing or shorter than nnz");
+        std::copy(Bc.row.begin(), Bc.row.end(), Bc_rowidx);
+        std::copy(Bc.val.begin(), Bc.val.end(), Bc_val);
+    }
+    API_END
+}
+
 mgmc_status mgmc_sampler_create(const mgmc_operator_desc *op, const mgmc_sampler_params *params, mgmc_sampler **out) {
     Sampler *S = nullptr;
     API_BEGIN

@@ -129,3 +129,46 @@ def test_fem_operator_equals_oracle(shape, model):
     else:
         op = M.LinearOperator.shifted_laplace_fem_periodic(shape, p0, p1)
     assert np.array_equal(op.to_scipy().toarray(), A)
+
+
+@pytest.mark.parametrize("kind", ["fd-1d-lowrank", "fd-2d", "fd-3d", "fd-periodic-2d", "fem-periodic-3d"])
+def test_operator_coarsen_matches_oracle(kind):
+    """LinearOperator.coarsen (mgmc_operator_coarsen; linear_operator.cc:10-23)
+    twice: the coarse operators R A R^T + (R B) Sigma^{-1} (R B)^T equal the
+    oracle's sparse triple products on random vectors to 1e-13, for a
+    constant stencil, the per-vertex centre of the periodic FD prior and the
+    per-vertex stencils of the periodic FEM prior."""
+    from problems import fem_posterior, operator_1d, periodic_posterior, posterior
+    if kind == "fd-1d-lowrank":
+        op_o, op_p = operator_1d(True)
+        depth = 1
+    elif kind == "fd-2d":
+        op_o, op_p = posterior((32, 32), m=4, radius=0.1)
+        depth = 2
+    elif kind == "fd-3d":
+        op_o, op_p = posterior((16, 16, 16), m=6, radius=0.1)
+        depth = 2
+    elif kind == "fd-periodic-2d":
+        op_o, op_p = periodic_posterior((32, 32), m=3, radius=0.1)
+        depth = 2
+    else:
+        op_o, op_p = fem_posterior((16, 16, 16), m=3, radius=0.1)
+        depth = 2
+    rng = np.random.default_rng(11)
+    for _ in range(depth):
+        op_o, op_p = op_o.coarsen(), op_p.coarsen()
+        assert op_p.n == op_o.n and op_p.m == op_o.m
+        x = rng.standard_normal(op_p.n)
+        yo = op_o.apply(x)
+        yp = op_p.to_scipy() @ x
+        assert np.linalg.norm(yp - yo) <= 1e-13 * np.linalg.norm(yo), kind
+
+
+def test_operator_coarsen_errors():
+    """An odd lattice cannot be coarsened: a status code, not an exit."""
+    op = M.LinearOperator.shifted_laplace_fd((10, 10), 10.0)
+    op2 = op.coarsen()
+    assert op2.shape == (5, 5)
+    with pytest.raises(M.MGMCError) as e:
+        op2.coarsen()
+    assert e.value.status == 2
