@@ -38,7 +38,8 @@ from . import statistics  # noqa: F401  (tau_int for chain observables)
 from . import build as _build
 
 __all__ = [
-    "MGMCError", "load", "fd_stencil", "galerkin_stencil", "measurement_vector", "LinearOperator",
+    "MGMCError", "load", "fd_stencil", "galerkin_stencil", "measurement_vector", "intergrid_to_sparse",
+    "LinearOperator",
     "MultigridParameters", "MultigridMCSampler", "MultigridMCBatch", "SSORSampler", "CholeskySampler",
     "IterativeSolverParameters", "MultigridPreconditioner", "LoopSolver", "ExactSampler", "SORSmoother",
     "SSORSmoother",
@@ -202,6 +203,38 @@ def galerkin_stencil(dim, fine):
     out = np.zeros(27)
     _check(load().mgmc_galerkin_stencil(dim, _dp(fine), _dp(out)))
     return out
+
+
+def intergrid_to_sparse(shape):
+    """IntergridOperator::to_sparse (intergrid/intergrid_operator.hh:122-144)
+    of the linear intergrid operator (intergrid_operator_linear.cc:8-31):
+    the restriction R from the lattice of `shape` cells to the lattice of
+    shape // 2 cells as a scipy.sparse CSR matrix (n_coarse x n_fine); coarse
+    vertex a sits on fine vertex 2 a + 1 per direction, with weights
+    prod_d {1/2, 1, 1/2} on its 3^d footprint.  The prolongation is R^T.
+    Host-side (set-up and checks); the samplers apply R and P with their own
+    kernels."""
+    import scipy.sparse as sp
+    dim = len(shape)
+    Nf = [c - 1 for c in shape]
+    Nc = [c // 2 - 1 for c in shape]
+    cidx = np.indices(Nc[::-1]).reshape(dim, -1)[::-1]  # coarse (a, b, c), x fastest
+    ccol = np.arange(int(np.prod(Nc)))
+    rows, cols, vals = [], [], []
+    for off in np.ndindex(*([3] * dim)):
+        o = np.array(off) - 1
+        fpos = 2 * cidx + 1 + o[:, None]
+        ok = np.all((fpos >= 0) & (fpos < np.array(Nf)[:, None]), axis=0)
+        frow = np.zeros(ok.sum(), np.int64)
+        stride = 1
+        for d in range(dim):
+            frow += fpos[d, ok] * stride
+            stride *= Nf[d]
+        rows.append(frow)
+        cols.append(ccol[ok])
+        vals.append(np.full(ok.sum(), 0.5 ** int(np.abs(o).sum())))
+    n_f, n_c = int(np.prod(Nf)), int(np.prod(Nc))
+    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(cols), np.concatenate(rows))), shape=(n_c, n_f))
 
 
 def measured_apply_noalloc(op, B_colptr, B_rowidx, B_val, Sigma, x, y, stream=0):

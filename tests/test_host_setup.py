@@ -172,3 +172,17 @@ def test_operator_coarsen_errors():
     with pytest.raises(M.MGMCError) as e:
         op2.coarsen()
     assert e.value.status == 2
+
+
+@pytest.mark.parametrize("shape", [(16,), (16, 8), (8, 16, 32)])
+def test_intergrid_to_sparse(shape):
+    """IntergridOperator::to_sparse (intergrid_operator.hh:122-144): R x and
+    R^T x_c equal the oracle's restrict and prolongate_add."""
+    R = M.intergrid_to_sparse(shape)
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal(R.shape[1])
+    xc = rng.standard_normal(R.shape[0])
+    assert np.allclose(R @ x, O.restrict(shape, x), rtol=0, atol=1e-14)
+    xp = np.zeros(R.shape[1])
+    O.prolongate_add(shape, 1.0, xc, xp)
+    assert np.allclose(R.T @ xc, xp, rtol=0, atol=1e-14)
