@@ -156,3 +156,26 @@ def test_maxiter_zero_and_zero_rhs():
     x, it, rn, conv = s.solve(np.zeros(op.n), maxiter=3)
     assert not conv and it == 3 and rn == 0.0 and not x.any()
     s.close()
+
+
+def test_cholesky_wrapper_dense_solve():
+    """TestEigenDenseSolve / TestEigenDenseSolveLLT (test_cholesky_wrapper.hh:
+    14-42, 120-143) on the GPU's coarse Cholesky: the 16 x 16 (6, -1)
+    tridiagonal matrix, |x - x_exact| < 1e-12, through the one-level
+    preconditioner (the factor's two triangular solves, throughput kernels)
+    and through the Cholesky sampler fed zero noise (x = L^-T (0 + L^-1 b),
+    the parity kernels)."""
+    st = np.zeros(27)
+    st[12], st[13], st[14] = -1.0, 6.0, -1.0
+    op = M.LinearOperator((17,), st)
+    x_exact = np.random.default_rng(1212957).standard_normal(16)
+    s = M.CholeskySampler(op, noise=M.INJECTED)
+    b = s.level_apply(0, x_exact)
+    P = M.MultigridPreconditioner(op, M.MultigridParameters(nlevel=1, coarse_solver="Cholesky"))
+    assert np.linalg.norm(P.apply(b) - x_exact) < 1e-12
+    P.close()
+    s.inject_noise(np.zeros(s.noise_per_step))
+    x = np.zeros(16)
+    s.apply(b, x)
+    s.close()
+    assert np.linalg.norm(x - x_exact) < 1e-12

@@ -86,3 +86,23 @@ def test_preconditioner_symmetric():
     P = O.MGPreconditioner(op, 4, "SSOR", omega=1.2, woodbury=False)
     lhs, rhs = P.apply(u) @ v, u @ P.apply(v)
     assert abs(lhs - rhs) <= 1e-12 * np.linalg.norm(P.apply(u)) * np.linalg.norm(v)
+
+
+def _tridiagonal16():
+    """The matrix of CholeskyWrapperTest (test_cholesky_wrapper.hh:14-42):
+    16 x 16, 6 on the diagonal, -1 beside it, with x_exact ~ N(0, 1)
+    (numpy-seeded here) and b = A x_exact."""
+    st = np.zeros(27)
+    st[12], st[13], st[14] = -1.0, 6.0, -1.0
+    x_exact = np.random.default_rng(1212957).standard_normal(16)
+    return st, x_exact
+
+
+def test_cholesky_wrapper_dense_solve():
+    """TestEigenDenseSolve / TestEigenDenseSolveLLT (test_cholesky_wrapper.hh:
+    120-143): |x - x_exact| < 1e-12 for the oracle's dense factor."""
+    st, x_exact = _tridiagonal16()
+    op = O.Operator.from_stencil([17], st)
+    b = op.apply(x_exact)
+    x = O.cholesky_solve(op, b)
+    assert np.linalg.norm(x - x_exact) < 1e-12
