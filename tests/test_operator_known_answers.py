@@ -63,3 +63,25 @@ def test_shifted_laplace_fem_operator_oracle(shape, tol):
     u, rhs_exact = _exact(shape)
     rhs = op.apply(u)
     assert np.linalg.norm(rhs - rhs_exact) / np.linalg.norm(rhs) < tol
+
+
+def _csr(op_o):
+    import scipy.sparse as sp
+    ptr, col, val = op_o.csr()
+    return sp.csr_matrix((val, col, ptr), shape=(op_o.n, op_o.n))
+
+
+@pytest.mark.parametrize("shape", [(8, 8), (8, 8, 8)], ids=["2d", "3d"])
+def test_coarsen_fem_operator(shape):
+    """TestCoarsenOperator2d / 3d (test_intergrid.hh:179-207): the Galerkin
+    coarsening of the FEM operator with Lambda = 1 is the FEM operator of the
+    coarse lattice, |difference|_F < 1e-12 -- for the library's
+    LinearOperator.coarsen and for the oracle's sparse triple product."""
+    import scipy.sparse.linalg as spl
+    coarse = tuple(s // 2 for s in shape)
+    fine_p = M.LinearOperator.shifted_laplace_fem(shape, Lambda=1.0)
+    direct_p = M.LinearOperator.shifted_laplace_fem(coarse, Lambda=1.0)
+    assert spl.norm(fine_p.coarsen().to_scipy() - direct_p.to_scipy()) < 1e-12
+    fine_o = O.Operator.fem(list(shape), 0, 1.0)
+    direct_o = O.Operator.fem(list(coarse), 0, 1.0)
+    assert spl.norm(_csr(fine_o.coarsen()) - _csr(direct_o)) < 1e-12
