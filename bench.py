@@ -37,10 +37,14 @@ RADIUS = 0.05
 VARIANCE = 1e-4
 NLEVEL = 5
 IACT_WINDOW = 50
-# DRAM bytes (read + write) of one k_sweep_rb_vec launch at 256^3, from an
-# ncu capture of `python bench.py --profile-steps 1` (summary in
-# profiles/k_sweep_rb_vec_256cubed.md): 100.68 MB read + 14.34 MB written
+# DRAM bytes (read + write) of one fine colour-pass launch at 256^3 -- a
+# constant taken from one ncu capture, not measured in the run
 RB_VEC_DRAM_BYTES = 115.01e6
+RB_VEC_TRAFFIC_SOURCE = ("constant: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, capture of "
+                         "`python bench.py --profile-steps 1` (profiles/k_sweep_rb_vec_256cubed.md): "
+                         "100.68 MB read + 14.34 MB written")
+RB_VEC_KERNEL = ("k_sweep_rb_vec<1, 0, 1, 1> (one colour pass of the fine-level red-black SOR sweep: FP32, Philox "
+                 "noise, 256-bit spans, colour-split f)")
 METRIC = "indep. samples/s (rate/IACT), 3D 256³ posterior: mixed vs FP64 plain, 1 GB300"
 UNIT = "indep_samples/s"
 WORKLOAD = ("3D 256^3 posterior MGMC V(1,1) SSOR omega=1, 5 levels, coarse dense Cholesky 16^3, "
@@ -171,10 +175,10 @@ def time_chain(M, torch, op, f, obs, precision, steps, warmup, iact_extra, dist,
 def sweep_roofline(M, torch, s, precision, peak):
     """Fine-level red-black SOR colour pass (``k_sweep_rb_vec`` in FP32,
     ``k_sweep_rb_pass`` in FP64; Philox noise, no low-rank update) timed on
-    the sampler's stream.  One sweep is two launches, one per colour; the
-    algorithmic bytes of one launch are 2 n s: every x value is read as a
-    neighbour or centre, and f is read and x written at the n/2 points of
-    the colour."""
+    the sampler's stream.  One sweep is two launches, one per colour.  The
+    algorithmic bytes of a sweep are 3 n s (x read, f read, x written once
+    each; in-kernel noise costs none), so one colour launch is charged
+    1.5 n s."""
     n = s.level_size(0)
     sz = 4 if precision == M.FP32_MIXED else 8
     s.sweep_device(0, nrepeat=5, with_lowrank=False)
@@ -187,7 +191,7 @@ def sweep_roofline(M, torch, s, precision, peak):
     e1.record(st)
     s.synchronize()
     t = e0.elapsed_time(e1) / 1e3 / (2 * rep)   # seconds per colour-pass launch
-    bytes_per_launch = 2 * n * sz
+    bytes_per_launch = 1.5 * n * sz
     achieved = bytes_per_launch / t / 1e9
     return achieved, bytes_per_launch, t
 
@@ -249,10 +253,11 @@ def time_e2e(M, torch, op, f, precision, steps, seed, iact):
     return 1.0 / dt / iact, dt, 2 * op.n * 8, op.n * 8
 
 
-def cpu_reference(seconds_budget=25.0, nsteps=None):
+def cpu_reference(seconds_budget=25.0, nsteps=None, warmup=1):
     """The oracle's restatement of the reference MGMC (lexicographic SOR,
     dense B-bar, CLCG noise) on the host cores, one chain, OpenMP threads in
-    the dense products; a bounded number of steps."""
+    the dense products; `warmup` untimed steps, then `nsteps` timed steps
+    (or as many as fit in `seconds_budget` when nsteps is None)."""
     import oracle as O
     import multigridmc_gb300 as M
     rng = np.random.default_rng(1)
@@ -268,7 +273,7 @@ def cpu_reference(seconds_budget=25.0, nsteps=None):
     s = O.mgmc_sampler(op, O.Source(), NLEVEL, ordering=0)
     setup = time.perf_counter() - t0
     x = np.zeros(op.n)
-    s.apply(f, x, 1)  # first step (touches every array)
+    s.apply(f, x, max(1, warmup))  # untimed steps (the first touches every array)
     times = []
     t_start = time.perf_counter()
     while True:
@@ -296,6 +301,47 @@ def host_cpu():
     except Exception:
         pass
     return f"{model}, {os.cpu_count()} cores"
+
+
+def coupled_run(s, probes, nsamples):
+    """`nsamples` further steps of sampler `s` recording every probe b_p^T x
+    after each step; returns the (nsamples, nprobe) observations."""
+    s.set_probes(probes, nsamples + 8)
+    s.step(nsamples)
+    s.synchronize()
+    return s.read_observations(nsamples + 8)
+
+
+def covariance_figures(M, op, f, pts, Z32, Z64, iact32, iact64, exact=True):
+    """The precision target of the 256^3 posterior: relative Frobenius
+    difference of the probe-point sample covariances of the coupled
+    FP32-mixed and FP64 chains (identical Philox normals, so the difference
+    is the FP32 chain's rounding, not Monte Carlo noise), and each chain
+    against the exact probe covariance within its Monte Carlo error."""
+    nprobe = len(pts)
+    C32 = np.cov(Z32[:, :nprobe].T)
+    C64 = np.cov(Z64[:, :nprobe].T)
+    out = {"fp32_vs_fp64_cov_rel_frobenius": float(np.linalg.norm(C32 - C64) / np.linalg.norm(C64)),
+           "fp32_vs_fp64_mean_rel": float(np.linalg.norm(Z32[:, :nprobe].mean(0) - Z64[:, :nprobe].mean(0))
+                                          / np.linalg.norm(Z64[:, :nprobe].mean(0))),
+           "nprobe": nprobe, "nsamples": int(Z32.shape[0]), "target": 1e-3,
+           "probes": "256 interior vertices drawn uniformly without replacement (seed 2)"}
+    if not exact:
+        return out
+    Cx, mu, solve_s = exact_probe_moments(op, f, pts)
+    for name, Z, tau in (("fp32", Z32, iact32), ("fp64", Z64, iact64)):
+        Zp = Z[:, :nprobe]
+        N = Zp.shape[0]
+        C = np.cov(Zp.T)
+        cov_se = np.sqrt(tau * np.sum(Cx ** 2 + np.outer(np.diag(Cx), np.diag(Cx))) / N)
+        mean_se = np.sqrt(tau * np.sum(np.diag(Cx)) / N)
+        out[name + "_vs_exact"] = {"cov_rel_frobenius": float(np.linalg.norm(C - Cx) / np.linalg.norm(Cx)),
+                                   "cov_mc_expected": float(cov_se / np.linalg.norm(Cx)),
+                                   "mean_rel": float(np.linalg.norm(Zp.mean(0) - mu) / np.linalg.norm(mu)),
+                                   "mean_mc_expected": float(mean_se / np.linalg.norm(mu))}
+    out["exact"] = ("probe covariances e_p^T Q^-1 e_q and the mean Q^-1 f by multigrid-preconditioned loop "
+                    f"solves on the GPU to rtol 1e-10 ({solve_s:.1f} s)")
+    return out
 
 
 def covariance_study(nsamples, nprobe=256, warmup=50, seed=1000):
@@ -811,7 +857,10 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--iact-samples", type=int, default=12000)
+    ap.add_argument("--iact-samples", type=int, default=20000,
+                    help="samples of the coupled FP32-mixed / FP64 run after the timed steps: IACT and the "
+                         "probe covariances")
+    ap.add_argument("--cov-probes", type=int, default=256)
     ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
@@ -868,14 +917,16 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        r = cpu_reference(seconds_budget=max(5.0, args.cpu_seconds), nsteps=None)
+        r = cpu_reference(nsteps=args.steps, warmup=args.warmup)
         val = 1.0 / r["per_step_s"] / PUBLISHED_MGMC_IACT
-        sample = (f"{r['steps']} MGMC steps of the oracle's reference restatement at 256^3, m=64 (lexicographic "
-                  f"SOR, dense B-bar, CLCG), one chain, {r['threads']} OpenMP threads in the dense products; "
-                  f"IACT {PUBLISHED_MGMC_IACT} = the reference's published MGMC IACT (python/plot_summary.py:28); "
-                  f"setup {r['setup_s']:.1f} s untimed; host {r['host']}")
+        sample = (f"{r['steps']} MGMC steps (after {args.warmup} untimed) of the oracle's reference restatement at "
+                  f"256^3, m=64 (lexicographic SOR, dense B-bar, CLCG), one chain, {r['threads']} OpenMP threads "
+                  f"in the dense products; IACT {PUBLISHED_MGMC_IACT} = the reference's published MGMC IACT at "
+                  f"64^3 (python/plot_summary.py:28), not measured at 256^3 on the CPU; setup "
+                  f"{r['setup_s']:.1f} s untimed; host {r['host']}")
         line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
-                "steps": r["steps"], "warmup": 1, "ms_per_step": r["per_step_s"] * 1e3, "higher_is_better": True,
+                "steps": r["steps"], "warmup": args.warmup, "ms_per_step": r["per_step_s"] * 1e3,
+                "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "unknowns": int(np.prod([n - 1 for n in SHAPE])),
                            "precision": "fp64", "ordering": "lexicographic (the reference's sweep order)"},
@@ -896,33 +947,44 @@ def main():
     op, f, obs, _, _ = problem()
     peak, peak_kind = measured_peaks()
     clocks = ClockSampler(local)
-    extra = max(0, args.iact_samples - args.steps)
+    rng = np.random.default_rng(2)
+    probe_pts = rng.choice(op.n, size=args.cov_probes, replace=False)
+    probes = [(np.array([p], np.int64), np.array([1.0])) for p in probe_pts] + [obs]
 
-    # FP32-mixed headline chain (clocks sampled during its timed region)
+    # FP32-mixed headline chain (clocks sampled during its timed region),
+    # then the coupled covariance run on the same chain
     clocks.start()
-    s32, ms32, z32 = time_chain(M, torch, op, f, obs, M.FP32_MIXED, args.steps, args.warmup, extra, dist, 1000 + rank)
+    s32, ms32, _ = time_chain(M, torch, op, f, obs, M.FP32_MIXED, args.steps, args.warmup, 0, dist, 1000 + rank)
     clk = clocks.stop()
     launches = s32.launches_per_step
-    iact32 = M.statistics.tau_int(z32, IACT_WINDOW)
+    Z32 = coupled_run(s32, probes, args.iact_samples)
     ach, bpl, tl = sweep_roofline(M, torch, s32, M.FP32_MIXED, peak)
     kernels = kernel_table(M, torch, s32, M.FP32_MIXED, peak, tl)
     s32.close()
-    # FP64 chain
-    # same seed: the FP64 chain draws the FP32 chain's normals (coupled
-    # chains), so the two IACT estimates share their Monte Carlo noise and
-    # the ratio of the two values is the cost ratio of equal-quality samples
-    s64, ms64, z64 = time_chain(M, torch, op, f, obs, M.FP64, args.steps, args.warmup, extra, dist, 1000 + rank)
-    iact64 = M.statistics.tau_int(z64, IACT_WINDOW)
+    # FP64 chain: same seed, so it draws the FP32 chain's normals (coupled
+    # chains): the two IACT estimates share their Monte Carlo noise, the ratio
+    # of the two values is the cost ratio of equal-quality samples, and the
+    # sample covariances differ only by the FP32 chain's rounding
+    s64, ms64, _ = time_chain(M, torch, op, f, obs, M.FP64, args.steps, args.warmup, 0, dist, 1000 + rank)
+    Z64 = coupled_run(s64, probes, args.iact_samples)
     ach64, bpl64, tl64 = sweep_roofline(M, torch, s64, M.FP64, peak)
     s64.close()
+    iact32 = M.statistics.tau_int(Z32[:, -1], IACT_WINDOW)
+    iact64 = M.statistics.tau_int(Z64[:, -1], IACT_WINDOW)
+    cov = covariance_figures(M, op, f, probe_pts, Z32, Z64, iact32, iact64, exact=(rank == 0 and world == 1))
 
     ms32, ms64 = replica_max([ms32, ms64], dist, "cuda")
     value = replica_rate(world, ms32 / 1000.0, iact32)
     value64 = replica_rate(world, ms64 / 1000.0, iact64)
 
     e2e_val, e2e_dt, h2d, d2h = time_e2e(M, torch, op, f, M.FP32_MIXED, args.e2e_steps, 1000 + rank, iact32)
-    (e2e_dt,) = replica_max([e2e_dt], dist, "cuda")
+    e2e64_val, e2e64_dt, _, _ = time_e2e(M, torch, op, f, M.FP64, args.e2e_steps, 1000 + rank, iact64)
+    e2e_dt, e2e64_dt = replica_max([e2e_dt, e2e64_dt], dist, "cuda")
     e2e_val = replica_rate(world, e2e_dt, iact32)
+    e2e64_val = replica_rate(world, e2e64_dt, iact64)
+    fma = {"fp64_tflops": M.device_fma_rate(M.FP64), "fp32_tflops": M.device_fma_rate(M.FP32_MIXED),
+           "how": "mgmc_device_fma_rate: 8 independent FMA chains per thread, 8 CTAs x 256 threads per SM, "
+                  "~20 ms per launch, best of 3, CUDA events"}
 
     if rank != 0:
         return
@@ -933,33 +995,45 @@ def main():
             cv = 1.0 / r["per_step_s"] / PUBLISHED_MGMC_IACT
             cpu = {"value": cv, "unit": UNIT, "cores": r["threads"], "kind": "port",
                    "sample": (f"{r['steps']} oracle MGMC steps at 256^3 m=64 (reference algorithm: lexicographic "
-                              f"SOR, dense B-bar, CLCG), {r['per_step_s']:.2f} s/step, IACT "
-                              f"{PUBLISHED_MGMC_IACT} (published, python/plot_summary.py:28); host {r['host']}")}
+                              f"SOR, dense B-bar, CLCG), {r['per_step_s']:.2f} s/step; IACT {PUBLISHED_MGMC_IACT} "
+                              f"= the reference's published MGMC IACT at 64^3 (python/plot_summary.py:28), not "
+                              f"measured at 256^3 on the CPU; host {r['host']}")}
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
 
+    n = int(op.n)
+    sweep_bytes = 3 * n * 4
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (FP64 Cholesky factorisation and m x m low-rank system)", "data": "synthetic",
         "config": {"workload": WORKLOAD,
-                   "unknowns": int(op.n), "ordering": "multicolour (red-black fine, 8-colour coarse)",
+                   "unknowns": n, "ordering": "multicolour (red-black fine, 8-colour coarse)",
                    "noise": "in-kernel Philox4x32-10", "parallelism": f"replicas x{world}",
                    "l2": "per-step working set > L2 (x and f alone 134 MB FP32 / 268 MB FP64)",
-                   "iact_window": IACT_WINDOW, "iact_samples": int(len(z32))},
+                   "iact_window": IACT_WINDOW, "iact_samples": int(Z32.shape[0])},
         "iact": iact32, "steps_per_s": 1000.0 / ms32,
+        "covariance_rel_err": cov["fp32_vs_fp64_cov_rel_frobenius"],
+        "covariance": cov,
         "fp64": {"value": value64, "ms_per_step": ms64, "iact": iact64, "steps_per_s": 1000.0 / ms64,
-                 "sweep_gbs": ach64},
+                 "sweep_gbs": ach64, "sweep_launch_s": tl64,
+                 "e2e": {"value": e2e64_val, "unit": UNIT, "ms_per_step": e2e64_dt * 1e3,
+                         "api": "mgmc_sampler_apply (pinned host f, x)"}},
         "kernels_fp32": kernels,
         "mixed_vs_fp64": value / value64,
+        "fma_peaks": fma,
         "clocks": clk,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_dt * 1e3, "api": "mgmc_sampler_apply (pinned host f, x)"},
         "gpu_launches": int(launches * args.steps),
         "launches_per_step": int(launches),
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                     "traffic": RB_VEC_DRAM_BYTES, "traffic_unit": "bytes per launch (ncu dram__bytes_read+write)", "kernel": "k_sweep_rb_vec<1, 0, 1, 1> (one colour pass of the fine-level red-black SOR sweep: FP32, Philox noise, 256-bit spans, colour-split f)",
-                     "algorithmic_bytes_per_launch": bpl, "launch_s": tl, "peak_kind": peak_kind},
+                     "traffic": RB_VEC_DRAM_BYTES,
+                     "traffic_source": RB_VEC_TRAFFIC_SOURCE,
+                     "kernel": RB_VEC_KERNEL,
+                     "algorithmic_bytes": "3 n s per sweep (x read, f read, x written), 1.5 n s per colour launch",
+                     "algorithmic_bytes_per_launch": bpl, "launch_s": tl, "sweep_s": 2 * tl,
+                     "sweep_gbs": sweep_bytes / (2 * tl) / 1e9, "peak_kind": peak_kind},
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)

@@ -313,25 +313,40 @@ mgmc_status mgmc_batch_synchronize(mgmc_batch *b);
 mgmc_status mgmc_batch_stream(mgmc_batch *b, void **cuda_stream);
 mgmc_status mgmc_batch_destroy(mgmc_batch *b);
 
+/* ------------------------------------------------------------ diagnostics */
+/* No counterpart in the reference.  Measured FMA throughput of the current
+ * GPU in TFLOP/s (2 flop per FMA), FP64 (precision = MGMC_FP64) or FP32
+ * (MGMC_FP32_MIXED): full occupancy, eight independent FMA chains per
+ * thread, about 20 ms per timed launch, best of three, CUDA events.  It
+ * bounds the kernels whose flops per byte exceed the HBM roofline's; it
+ * changes no clock or other setting of the GPU. */
+mgmc_status mgmc_device_fma_rate(int precision, double *tflops);
+
 /* ------------------------------------------- no-allocation operator apply */
 /* No counterpart in the reference.  y = A x for A = A_0 + B Sigma^{-1} B^T
- * (the product LinearOperator::apply computes) without allocating device
- * memory, for callers that cannot call cudaMalloc: work captured into a
- * CUDA graph in global capture mode, applications whose device memory is
- * owned by their own pool and lent to the library buffer by buffer, and
- * latency-critical loops that cannot afford cudaMalloc's device-wide
- * synchronisation.  `stencil` is a host array; B_colptr/B_rowidx/B_val
- * (column-compressed, as in mgmc_operator_desc), Sigma, x and y are device
- * pointers of the current device, vectors in the reference's vertex order.
- * Work is queued on `cuda_stream` (NULL = default stream) and the call
- * returns without waiting for it.
+ * without allocating device memory, for callers that cannot call
+ * cudaMalloc: work captured into a CUDA graph in global capture mode,
+ * applications whose device memory is owned by their own pool and lent to
+ * the library buffer by buffer, and latency-critical loops that cannot
+ * afford cudaMalloc's device-wide synchronisation.
+ * A_0 must be one constant 27-point stencil for every vertex (`stencil`, a
+ * host array); operators with a per-vertex centre or a per-vertex stencil
+ * field are not handled here.  B_colptr/B_rowidx/B_val (column-compressed,
+ * as in mgmc_operator_desc), Sigma, x and y are device pointers of the
+ * current device, vectors in the reference's vertex order.  Work is queued
+ * on `cuda_stream` (NULL = default stream) and the call returns without
+ * waiting for it.  A_0 x is summed per row in ascending index order; the
+ * low-rank part is added with atomics, so its order, and the last bits of
+ * y, can change from run to run.  A CUDA error pending from earlier work is
+ * reported (MGMC_ERR_CUDA) and left in place.
  * The only scratch, B^T x, lives in a static device array of
  * MGMC_NOALLOC_MAX_M doubles (32 KiB) that every GPU loading the library
  * holds until the process exits; m > MGMC_NOALLOC_MAX_M is rejected with
  * MGMC_ERR_INVALID_ARGUMENT.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call
- * before any stream capture.  All calls on a device share the array: calls
- * that overlap on the GPU race and must be ordered by the caller. */
+ * array's device address (cudaGetSymbolAddress) and loads the entry point's
+ * kernels; make that first call before any stream capture.  All calls on a
+ * device share the array: calls that overlap on the GPU race and must be
+ * ordered by the caller. */
 #define MGMC_NOALLOC_MAX_M 4096
 mgmc_status mgmc_measured_apply_noalloc(int dim, int nx, int ny, int nz, const double stencil[27], int m,
                                         const int64_t *B_colptr, const int64_t *B_rowidx, const double *B_val,

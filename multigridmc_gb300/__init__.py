@@ -134,6 +134,7 @@ SIGNATURES = {
     "mgmc_batch_synchronize": (C.c_int, [_P]),
     "mgmc_batch_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "mgmc_batch_destroy": (C.c_int, [_P]),
+    "mgmc_device_fma_rate": (C.c_int, [C.c_int, _D]),
     "mgmc_measured_apply_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _D, C.c_int, _P, _P, _P, _P,
                                               _P, _P, _P]),
 }
@@ -240,10 +241,25 @@ def intergrid_to_sparse(shape):
 def measured_apply_noalloc(op, B_colptr, B_rowidx, B_val, Sigma, x, y, stream=0):
     """mgmc_measured_apply_noalloc: y = A x with device buffers given as raw
     addresses (integers); nothing is allocated by the library.  Asynchronous
-    on `stream` (a cudaStream_t address, 0 = default stream)."""
+    on `stream` (a cudaStream_t address, 0 = default stream).  A_0 must be
+    one constant stencil: an operator with a per-vertex centre or stencil
+    field (periodic correlation length, FEM with variable coefficients) is
+    refused with MGMC_ERR_INVALID_ARGUMENT rather than applied with the
+    wrong weights."""
+    if op.centre is not None or op.field is not None:
+        raise MGMCError(1, "mgmc_measured_apply_noalloc handles a constant stencil A_0 only; this operator "
+                           "has per-vertex coefficients")
     st = _f64(op.stencil)
     _check(load().mgmc_measured_apply_noalloc(op.dim, *_shape3(op.shape), _dp(st), op.m, B_colptr, B_rowidx,
                                               B_val, Sigma, x, y, stream))
+
+
+def device_fma_rate(precision):
+    """mgmc_device_fma_rate: the measured FMA throughput of the current GPU
+    in TFLOP/s, FP64 (precision FP64) or FP32 (precision FP32_MIXED)."""
+    out = C.c_double(0.0)
+    _check(load().mgmc_device_fma_rate(int(precision), C.byref(out)))
+    return out.value
 
 
 def measurement_vector(shape, x0, radius):

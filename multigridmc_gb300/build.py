@@ -20,6 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = {
     "api.o": ("api.cu", ["kernels.cuh", "setup.h"]),
     "noalloc.o": ("noalloc.cu", []),
+    "peaks.o": ("peaks.cu", []),
     "setup.o": ("setup.cc", ["setup.h"]),
 }
 

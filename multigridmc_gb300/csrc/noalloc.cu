@@ -87,7 +87,10 @@ __global__ void __launch_bounds__(256) k_noalloc_btx(const double *__restrict__ 
     }
 }
 
-// y += B (Sigma^{-1} btx): columns may share rows, so the adds are atomic.
+// y += B (Sigma^{-1} btx): columns may share rows, so the adds are atomic,
+// and the order in which the columns' terms reach a row depends on block
+// timing -- the last bits of y may differ from run to run (mgmc_level_apply
+// sums in a fixed order).
 __global__ void __launch_bounds__(256) k_noalloc_add_B(double *__restrict__ y, const int64_t *__restrict__ ptr,
                                                        const int64_t *__restrict__ idx, const double *__restrict__ val,
                                                        const double *__restrict__ Sigma, const double *__restrict__ btx) {
@@ -130,10 +133,29 @@ extern "C" mgmc_status mgmc_measured_apply_noalloc(int dim, int nx, int ny, int 
             e = cudaGetSymbolAddress(&p, g_noalloc_btx);
             if (e != cudaSuccess)
                 return fail(MGMC_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            // Load all three kernels now, whatever m is: with lazy module
+            // loading a kernel is otherwise loaded at its first launch, which
+            // may come inside a later captured call (a first call with m = 0
+            // never launches the two low-rank kernels).
+            cudaFuncAttributes fa;
+            const void *kernels[3] = {reinterpret_cast<const void *>(k_noalloc_stencil),
+                                      reinterpret_cast<const void *>(k_noalloc_btx),
+                                      reinterpret_cast<const void *>(k_noalloc_add_B)};
+            for (const void *k : kernels) {
+                e = cudaFuncGetAttributes(&fa, k);
+                if (e != cudaSuccess)
+                    return fail(MGMC_ERR_CUDA, std::string("cudaFuncGetAttributes: ") + cudaGetErrorString(e));
+            }
             g_btx_addr[dev] = static_cast<double *>(p);
         }
         btx = g_btx_addr[dev];
     }
+    // An error left by earlier work on this thread is reported, not cleared:
+    // it is not this call's, and clearing it would hide it from its owner.
+    e = cudaPeekAtLastError();
+    if (e != cudaSuccess)
+        return fail(MGMC_ERR_CUDA, std::string("a CUDA error from earlier work is pending (left in place): ") +
+                                       cudaGetErrorString(e));
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     Stencil27 w;
     for (int k = 0; k < 27; ++k) w.w[k] = stencil[k];

@@ -14,7 +14,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = os.environ.get("MGMC_REFERENCE_SRC", "/root/reference/src")
+# the reference checkout's src/ directory: MGMC_REFERENCE_SRC, else the
+# directory `reference` next to this repository
+REF_SRC = os.environ.get("MGMC_REFERENCE_SRC",
+                         os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference", "src"))
 OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libref_random.so")
 

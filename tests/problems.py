@@ -86,3 +86,54 @@ def fem_posterior(shape, periodic=True, kappa_sq=10.0, Lambda_min=0.12, Lambda_m
         op_o.add_measurements(loc, var, variance_scaling=variance, radius=radius)
         op_p = op_p.with_measurements(loc, var, variance_scaling=variance, radius=radius)
     return op_o, op_p
+
+
+# Config 1 of the benchmark suite: the 2D prior on 64^2 cells (63^2 = 3,969
+# unknowns), kappa^2 = 10, no measurements, V(1,1) SSOR (omega = 1) on 4
+# levels with the Cholesky sampler on the 8^2-cell coarse level; 10^4 samples
+# after 100 burn-in steps.
+CONFIG1_SHAPE = (64, 64)
+CONFIG1_NLEVEL = 4
+CONFIG1_BURNIN = 100
+CONFIG1_NSAMPLES = 10000
+
+
+def config1_mean():
+    """Exact mean of the config-1 run: mu uniform in [0, 1] per vertex, and
+    f = Q mu (the reference's test right hand side, test_sampler.hh:113-130)."""
+    n = int(np.prod([c - 1 for c in CONFIG1_SHAPE]))
+    return np.random.default_rng(1342517).uniform(0.0, 1.0, n)
+
+
+def config1_check(X, mu, C, z, tau_bound=1.5):
+    """Sample moments of the chain X (nsamples x n) against the exact mean mu
+    and covariance C within Monte Carlo error, and the IACT of the observable
+    series z; `tau_bound` bounds the integrated autocorrelation time of the
+    per-vertex series in the error model.  Returns a dict of the figures;
+    raises AssertionError when one is outside its bound:
+    - per-vertex variance z-scores (v - C_pp) / (C_pp sqrt(2 tau / N)):
+      maximum below 5, root mean square below 1.25;
+    - per-vertex mean z-scores (m - mu_p) / sqrt(tau C_pp / N): the same;
+    - relative Frobenius error of the sample covariance below 1.3 times its
+      expected Monte Carlo size sqrt(tau sum(C_pq^2 + C_pp C_qq) / N) / |C|;
+    - the observable's IACT (window 50) between 0.7 and 2.0 (the reference
+      publishes 1.2-1.3 for MGMC)."""
+    import multigridmc_gb300 as M
+    N = X.shape[0]
+    d = np.diag(C)
+    m, v = X.mean(0), X.var(0)
+    zm = (m - mu) / np.sqrt(tau_bound * d / N)
+    zv = (v - d) / (d * np.sqrt(2.0 * tau_bound / N))
+    Ch = np.cov(X.T, bias=True)
+    rel = np.linalg.norm(Ch - C) / np.linalg.norm(C)
+    expected = np.sqrt(tau_bound * np.sum(C ** 2 + np.outer(d, d)) / N) / np.linalg.norm(C)
+    tau = M.statistics.tau_int(z, 50)
+    out = {"mean_z_max": float(np.abs(zm).max()), "mean_z_rms": float(np.sqrt(np.mean(zm ** 2))),
+           "var_z_max": float(np.abs(zv).max()), "var_z_rms": float(np.sqrt(np.mean(zv ** 2))),
+           "cov_rel_frobenius": float(rel), "cov_rel_frobenius_expected": float(expected), "iact": float(tau),
+           "var_max_abs_err": float(np.abs(v - d).max())}
+    assert out["mean_z_max"] < 5.0 and out["mean_z_rms"] < 1.25, out
+    assert out["var_z_max"] < 5.0 and out["var_z_rms"] < 1.25, out
+    assert rel < 1.3 * expected, out
+    assert 0.7 < tau < 2.0, out
+    return out

@@ -1,10 +1,13 @@
 """Driver configurations in libconfig syntax (src/auxilliary/parameters.cc)
 become the operator, right hand side and multigrid parameters of the GPU
 sampler."""
+import os
+
 import numpy as np
 import pytest
 
 import multigridmc_gb300 as M
+import oracle as O
 from multigridmc_gb300.config import load_run, parse_libconfig
 
 PARAMS = """
@@ -104,3 +107,87 @@ def test_fem_prior(tmp_path):
     op = load_run(str(tmp_path / "params.cfg")).linear_operator()
     ref = M.LinearOperator.shifted_laplace_fem_periodic((32, 16), 0.12, 0.23)
     assert np.array_equal(op.field, ref.field)
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _template():
+    return load_run(os.path.join(GOLDEN, "parameters_template.cfg"))
+
+
+def test_reference_templates_parse():
+    """The reference's own parameters_template.cfg and the measurement file
+    it names (copies in tests/golden/, made by make_fixtures.py) give the run
+    the reference's driver would set up: 2D posterior on 32^2 cells,
+    Lambda = 0.2, eight point measurements (radius 0: nearest vertex), a
+    W-cycle with SOR smoother and SSOR coarse solver on 4 levels."""
+    cfg = _template()
+    assert cfg.dim == 2 and cfg.shape == (32, 32) and cfg.operator == "posterior"
+    assert cfg.pdemodel == "shiftedlaplace_fd" and cfg.correlation == "constant"
+    assert cfg.kappa_sq == pytest.approx(25.0)
+    prm = cfg.multigrid_parameters()
+    assert (prm.smoother, prm.coarse_solver, prm.nlevel, prm.cycle) == ("SOR", "SSOR", 4, 2)
+    assert (prm.npresmooth, prm.npostsmooth, prm.ncoarsesmooth, prm.omega, prm.coarse_scaling) == (1, 1, 1, 1.0, 1.0)
+    assert cfg.sampling["timeseries"] == {"nsamples": 10000, "nwarmup": 1000}
+    assert cfg.sampling["convergence"]["nthreads"] == 6
+    assert cfg.sample_location() == [0.5, 0.5]
+    md = cfg.measurement_data
+    assert md["n"] == 8 and len(md["measurement_locations"]) == 16 and len(md["mean"]) == 8
+
+
+def test_reference_template_operator_equals_oracle():
+    """The template's posterior (FD prior, kappa^2 = 25, nearest-vertex
+    measurements, Sigma = variance) equals the oracle's MeasuredOperator
+    built from the same numbers: B bit for bit, A x to 1e-14."""
+    cfg = _template()
+    op = cfg.linear_operator()
+    md = cfg.measurement_data
+    loc = np.asarray(md["measurement_locations"], np.float64).reshape(8, 2)
+    op_o = O.Operator.fd([32, 32], 25.0)
+    op_o.add_measurements(loc, np.asarray(md["variance"], np.float64), variance_scaling=1.0, radius=0.0)
+    assert op.m == 8 and op_o.m == 8
+    Bo, sig_o = op_o.B_dense()
+    assert np.array_equal(op.B_dense(), Bo) and np.array_equal(op.Sigma, sig_o)
+    np.testing.assert_array_equal(op.Sigma, np.asarray(md["variance"], np.float64))
+    x = np.random.default_rng(3).standard_normal(op.n)
+    B = op.B_dense()
+    y = M.LinearOperator(op.shape, op.stencil).to_scipy() @ x + B @ ((B.T @ x) / op.Sigma)
+    want = op_o.apply(x)
+    assert np.linalg.norm(y - want) <= 1e-14 * np.linalg.norm(want)
+    f = cfg.rhs(op)
+    np.testing.assert_allclose(f, B @ (np.asarray(md["mean"]) / op.Sigma), rtol=1e-14)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ordering", [M.LEXICOGRAPHIC, M.MULTICOLOUR], ids=["lex", "multicolour"])
+def test_reference_template_chain_equals_oracle(ordering):
+    """MGMC as the template configures it (SOR smoother, SSOR coarse solver,
+    W-cycle, 4 levels) on the template's posterior: the FP64 GPU chain
+    against the oracle's on the same injected noise, 100 steps, 1e-12."""
+    cfg = _template()
+    op = cfg.linear_operator()
+    prm = cfg.multigrid_parameters()
+    md = cfg.measurement_data
+    op_o = O.Operator.fd([32, 32], 25.0)
+    op_o.add_measurements(np.asarray(md["measurement_locations"], np.float64).reshape(8, 2),
+                          np.asarray(md["variance"], np.float64), variance_scaling=1.0, radius=0.0)
+    gpu = M.MultigridMCSampler(op, prm, ordering=ordering, precision=M.FP64, noise=M.INJECTED)
+    nps = gpu.noise_per_step
+    nsteps = 100
+    noise = O.CLCG().draw_normal(nps * nsteps)
+    src = O.Source(noise)
+    orc = O.mgmc_sampler(op_o, src, prm.nlevel, smoother=prm.smoother, coarse_solver=prm.coarse_solver,
+                         npresmooth=prm.npresmooth, npostsmooth=prm.npostsmooth, ncoarsesmooth=prm.ncoarsesmooth,
+                         omega=prm.omega, cycle=prm.cycle, coarse_scaling=prm.coarse_scaling, ordering=ordering)
+    f = cfg.rhs(op)
+    xo, xg = np.zeros(op.n), np.zeros(op.n)
+    gpu.inject_noise(noise)
+    worst = 0.0
+    for _ in range(nsteps):
+        orc.apply(f, xo)
+        gpu.apply(f, xg)
+        worst = max(worst, np.linalg.norm(xg - xo) / np.linalg.norm(xo))
+    assert src.position == nps * nsteps
+    assert worst < 1e-12, worst
+    gpu.close()

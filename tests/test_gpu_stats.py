@@ -192,3 +192,32 @@ def test_mean_squared_error_of_running_average():
         model = (mu / (j + 1)) ** 2 + 2.0 * var / (j + 1)
         assert mse[j] < model, (j, mse[j], model)
         assert mse[j] > 0.25 * var / (j + 1), (j, mse[j])
+
+
+@pytest.mark.parametrize("precision", [M.FP64, M.FP32_MIXED], ids=["fp64", "fp32-mixed"])
+def test_config1_2d_prior_variance(precision):
+    """Config 1 in full on the GPU: 2D prior on 64^2 cells, kappa^2 = 10,
+    V(1,1) SSOR on 4 levels, Cholesky sampler on the 8^2-cell coarse level,
+    Philox noise; 10^4 samples after 100 burn-in steps.  Sample mean,
+    per-vertex variance and covariance against the exact covariance (dense
+    inverse of the precision) within Monte Carlo error, as the reference's
+    measured 2D MGMC test checks them (test_sampler.hh:271-334), and the IACT
+    of the centre ball average."""
+    import oracle as O
+    from problems import (CONFIG1_BURNIN, CONFIG1_NLEVEL, CONFIG1_NSAMPLES, CONFIG1_SHAPE, config1_check,
+                          config1_mean)
+    _, op = posterior(CONFIG1_SHAPE, kappa_sq=10.0)
+    oo = O.Operator.fd(list(CONFIG1_SHAPE), 10.0)
+    C = oo.covariance()
+    mu = config1_mean()
+    s = M.MultigridMCSampler(op, M.MultigridParameters(nlevel=CONFIG1_NLEVEL), precision=precision, seed=31)
+    s.fix_rhs(oo.precision() @ mu)
+    s.set_state(np.zeros(op.n))
+    s.step(CONFIG1_BURNIN)
+    X = np.zeros((CONFIG1_NSAMPLES, op.n))
+    for k in range(CONFIG1_NSAMPLES):
+        s.step(1)
+        X[k] = s.get_state()
+    s.close()
+    bidx, bval = M.measurement_vector(CONFIG1_SHAPE, [0.5, 0.5], 0.05)
+    config1_check(X, mu, C, X[:, bidx] @ bval)

@@ -186,3 +186,17 @@ def test_intergrid_to_sparse(shape):
     xp = np.zeros(R.shape[1])
     O.prolongate_add(shape, 1.0, xc, xp)
     assert np.allclose(R.T @ xc, xp, rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("kind", ["fem-periodic", "fd-periodic"])
+def test_noalloc_apply_refuses_variable_coefficients(kind):
+    """mgmc_measured_apply_noalloc takes one constant stencil; the wrapper
+    refuses operators with a per-vertex centre or stencil field (the call
+    never reaches the library, so no GPU is needed)."""
+    if kind == "fem-periodic":
+        op = M.LinearOperator.shifted_laplace_fem_periodic((8, 8), 0.12, 0.23)
+    else:
+        op = M.LinearOperator.shifted_laplace_fd_periodic((8, 8), 0.12, 0.23)
+    with pytest.raises(M.MGMCError) as e:
+        M.measured_apply_noalloc(op, 0, 0, 0, 0, 0, 0, 0)
+    assert e.value.status == 1 and "constant stencil" in str(e.value)

@@ -140,3 +140,26 @@ def test_injected_noise_reproduces_clcg_chain():
     xb = np.zeros(op.n)
     b.apply(f, xb, 5)
     assert np.array_equal(xa, xb)
+
+
+def test_config1_2d_prior_variance():
+    """Config 1 on the oracle (the reference's algorithm: lexicographic SSOR,
+    dense Cholesky coarse sampler, CLCG noise): 10^4 samples after 100
+    burn-in steps; sample mean, per-vertex variance and covariance against
+    the exact Cholesky covariance within Monte Carlo error, and the IACT of
+    the ball average at the centre."""
+    from problems import (CONFIG1_BURNIN, CONFIG1_NLEVEL, CONFIG1_NSAMPLES, CONFIG1_SHAPE, config1_check,
+                          config1_mean)
+    op = O.Operator.fd(list(CONFIG1_SHAPE), 10.0)
+    C = op.covariance()
+    mu = config1_mean()
+    f = op.precision() @ mu
+    s = O.mgmc_sampler(op, O.Source(), CONFIG1_NLEVEL)
+    x = np.zeros(op.n)
+    s.apply(f, x, CONFIG1_BURNIN)
+    X = np.zeros((CONFIG1_NSAMPLES, op.n))
+    for k in range(CONFIG1_NSAMPLES):
+        s.apply(f, x, 1)
+        X[k] = x
+    bidx, bval = O.measurement_vector(list(CONFIG1_SHAPE), [0.5, 0.5], 0.05)
+    config1_check(X, mu, C, X[:, bidx] @ bval)

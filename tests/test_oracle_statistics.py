@@ -66,3 +66,34 @@ def test_tau_int(ar1):
         wk = A @ wk
         tau += 2.0 * (1.0 - k / window) * vv @ wk / (vv @ w)
     assert abs(st.tau_int(vv) - tau) < 2e-2
+
+
+@pytest.mark.parametrize("rho,n,mu,window", [(0.3, 20000, 0.5, 50), (0.9, 100000, -2.0, 200), (0.0, 1000, 0.0, 10),
+                                             (0.6, 5000, 3.0, 20)])
+def test_library_tau_int_equals_oracle_statistics(rho, n, mu, window):
+    """multigridmc_gb300.statistics.tau_int (the IACT estimator of the
+    benchmark) equals the oracle's Statistics::tau_int (statistics.cc:65-79,
+    pinned on AR(1) above) on the same scalar series, to 1e-12 relative."""
+    from scipy.signal import lfilter
+    import multigridmc_gb300 as M
+    q = lfilter([1.0], [1.0, -rho], np.random.default_rng(5).standard_normal(n)) + mu
+    st = O.Statistics(1, window)
+    st.record(q)
+    want = st.tau_int(np.array([1.0]))
+    got = M.statistics.tau_int(q, window)
+    assert abs(got - want) <= 1e-12 * abs(want)
+
+
+def test_library_tau_int_on_an_mgmc_chain():
+    """The same comparison on the observable b^T x of the oracle's MGMC chain
+    (2D 32^2 prior, 4 levels, CLCG noise) with the benchmark's window 50."""
+    import multigridmc_gb300 as M
+    op = O.Operator.fd([32, 32], 10.0)
+    s = O.mgmc_sampler(op, O.Source(), 4)
+    bidx, bval = O.measurement_vector([32, 32], [0.5, 0.5], 0.1)
+    x = np.zeros(op.n)
+    z = s.observe(np.zeros(op.n), x, 3000, bidx, bval)
+    st = O.Statistics(1, 50)
+    st.record(z)
+    want = st.tau_int(np.array([1.0]))
+    assert abs(M.statistics.tau_int(z, 50) - want) <= 1e-12 * abs(want)
