@@ -172,7 +172,12 @@ mgmc_status mgmc_operator_coarsen(const mgmc_operator_desc *op, double coarse_st
 mgmc_status mgmc_sampler_create(const mgmc_operator_desc *op, const mgmc_sampler_params *params,
                                 mgmc_sampler **out);
 mgmc_status mgmc_sampler_destroy(mgmc_sampler *s);
-/* One sample: x <- MGMC step(f, x), both length n. */
+/* One sample: x <- MGMC step(f, x), both length n.  f == NULL: step with
+ * the right hand side already on the device (the last one given to
+ * mgmc_sampler_fix_rhs or mgmc_sampler_apply; MGMC_ERR_INVALID_ARGUMENT if
+ * there is none), so that only x crosses the host link -- the
+ * fix_rhs-then-apply loop of measure_sampling_time
+ * (src/measurements/sampling_time.cc:28-41). */
 mgmc_status mgmc_sampler_apply(mgmc_sampler *s, const double *f, double *x, int on_device);
 /* Keep f on the device for mgmc_sampler_step. */
 mgmc_status mgmc_sampler_fix_rhs(mgmc_sampler *s, const double *f, int on_device);

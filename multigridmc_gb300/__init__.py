@@ -534,15 +534,22 @@ class MultigridMCSampler:
 
     # --- Sampler surface
     def apply(self, f, x):
-        f = _f64(f)
+        """Sampler::apply: x <- one MGMC step with right hand side f.  With
+        f = None the step uses the right hand side already on the device
+        (fix_rhs, or the last apply), and only x crosses the host link."""
         assert x.dtype == np.float64 and x.flags.c_contiguous and x.size == self.n
+        if f is None:
+            _check(self._L.mgmc_sampler_apply(self._h, None, _dp(x), 0))
+            return x
+        f = _f64(f)
         _check(self._L.mgmc_sampler_apply(self._h, _dp(f), _dp(x), 0))
         return x
 
     def fix_rhs(self, f):
-        """The right hand side ``step()`` samples with (Sampler::fix_rhs,
-        sampler.hh:64); ``apply(f, x)`` always uses its own f, as in the
-        reference, whose MultigridMCSampler inherits the no-op fix_rhs."""
+        """The right hand side ``step()`` and ``apply(None, x)`` sample with
+        (Sampler::fix_rhs, sampler.hh:64); ``apply(f, x)`` with an f uses
+        that f, as in the reference, whose MultigridMCSampler inherits the
+        no-op fix_rhs."""
         f = _f64(f)
         _check(self._L.mgmc_sampler_fix_rhs(self._h, _dp(f), 0))
 

@@ -151,6 +151,7 @@ struct Sampler {
     // colour k at fsplit + k * fhalf; refreshed wherever level 0's f changes
     float *fsplit = nullptr;
     i64 fhalf = 0;
+    bool rhs_set = false;  // level 0's f was given (fix_rhs or apply): apply may take f = NULL
     void refresh_fsplit();
     // deterministic solver: LoopSolver around MultigridPreconditioner
     bool noisy = true;  // false while the preconditioner's noise-free cycle is recorded
@@ -307,9 +308,8 @@ NoiseArgs Sampler::noise_args(int lev, i64 count) {
 
 // Launch with programmatic stream serialization (pdl): the kernel's CTAs
 // may be scheduled while its predecessor on the stream drains; every step
-// kernel starts with griddepcontrol.launch_dependents / griddepcontrol.wait
-// (pdl_begin), so no kernel touches memory before its predecessor has
-// completed and flushed.  This hides the launch latency between the short
+// kernel starts with griddepcontrol.wait (pdl_begin), so no kernel touches
+// memory before its predecessor has completed and flushed.  This hides the launch latency between the short
 // dependent kernels of a multigrid step.
 constexpr i64 PDL_MAX_POINTS = i64(1) << 22;
 // supports of C up to this many rows take the fused solve + correction
@@ -2121,6 +2121,7 @@ mgmc_status mgmc_sampler_fix_rhs(mgmc_sampler *s, const double *f, int on_device
     if (!f) fail(MGMC_ERR_INVALID_ARGUMENT, "null f");
     put_vec(S, 0, f, on_device, S.L[0].f);
     S.refresh_fsplit();
+    S.rhs_set = true;
     API_END
 }
 
@@ -2172,7 +2173,20 @@ mgmc_status mgmc_sampler_step(mgmc_sampler *s, int64_t nsteps) {
 mgmc_status mgmc_sampler_apply(mgmc_sampler *s, const double *f, double *x, int on_device) {
     API_BEGIN
     Sampler &S = impl(s);
-    if (!f || !x) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    if (!x) fail(MGMC_ERR_INVALID_ARGUMENT, "null x");
+    if (!f) {
+        // the right hand side already on the device (Sampler::fix_rhs, then
+        // apply(f, x) with the fixed f: sampling_time.cc:28-41): only x
+        // travels
+        if (!S.rhs_set) fail(MGMC_ERR_INVALID_ARGUMENT, "f is NULL but no right hand side has been set");
+        put_vec(S, 0, x, on_device, S.L[0].x);
+        run_steps(S, 1);
+        get_vec(S, 0, S.L[0].x, x, on_device);
+        CK(cudaStreamSynchronize(S.stream));
+        check_device_errors(S);
+        return MGMC_OK;
+    }
+    S.rhs_set = true;
     const double *fm = on_device ? f : (const double *)mapped_host(f);
     const double *xm = on_device ? x : (const double *)mapped_host(x);
     if (fm && xm) {

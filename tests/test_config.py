@@ -164,7 +164,17 @@ def test_reference_template_operator_equals_oracle():
 def test_reference_template_chain_equals_oracle(ordering):
     """MGMC as the template configures it (SOR smoother, SSOR coarse solver,
     W-cycle, 4 levels) on the template's posterior: the FP64 GPU chain
-    against the oracle's on the same injected noise, 100 steps, 1e-12."""
+    against the oracle's on the same injected noise, 100 steps.
+
+    The template's point measurements have Sigma ~ 1.2e-6, so f = B Sigma^-1 y
+    reaches 3.4e6 at the measured vertices against states of order 4: every
+    sweep's value there cancels from ~1e6 down to O(1), and a rounding
+    difference of one ulp anywhere in f moves the chain by ~3e-12 relative
+    (measured below on the oracle itself).  The GPU's solve-form low-rank
+    correction and the oracle's explicit Bbar = M^-1 B S^-1 round
+    differently, so the bound is 100 such one-ulp perturbations instead of
+    the 1e-12 of the well-conditioned configurations (Sigma = 1e-4,
+    ball averages)."""
     cfg = _template()
     op = cfg.linear_operator()
     prm = cfg.multigrid_parameters()
@@ -181,13 +191,22 @@ def test_reference_template_chain_equals_oracle(ordering):
                          npresmooth=prm.npresmooth, npostsmooth=prm.npostsmooth, ncoarsesmooth=prm.ncoarsesmooth,
                          omega=prm.omega, cycle=prm.cycle, coarse_scaling=prm.coarse_scaling, ordering=ordering)
     f = cfg.rhs(op)
-    xo, xg = np.zeros(op.n), np.zeros(op.n)
+    # sensitivity of the oracle's chain to a one-ulp change of f
+    orc2 = O.mgmc_sampler(op_o, O.Source(noise), prm.nlevel, smoother=prm.smoother,
+                          coarse_solver=prm.coarse_solver, npresmooth=prm.npresmooth, npostsmooth=prm.npostsmooth,
+                          ncoarsesmooth=prm.ncoarsesmooth, omega=prm.omega, cycle=prm.cycle,
+                          coarse_scaling=prm.coarse_scaling, ordering=ordering)
+    f_ulp = np.nextafter(f, np.inf)
+    xo, xg, xu = np.zeros(op.n), np.zeros(op.n), np.zeros(op.n)
     gpu.inject_noise(noise)
-    worst = 0.0
+    worst, ulp = 0.0, 0.0
     for _ in range(nsteps):
         orc.apply(f, xo)
+        orc2.apply(f_ulp, xu)
         gpu.apply(f, xg)
         worst = max(worst, np.linalg.norm(xg - xo) / np.linalg.norm(xo))
+        ulp = max(ulp, np.linalg.norm(xu - xo) / np.linalg.norm(xo))
     assert src.position == nps * nsteps
-    assert worst < 1e-12, worst
+    assert 0.0 < ulp < 1e-11, ulp
+    assert worst < 100.0 * ulp, (worst, ulp)
     gpu.close()
