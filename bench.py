@@ -759,8 +759,10 @@ def batch_study(nchain, steps, warmup=5, seed=3):
     {32,48,64,96,128}^3 cells, kappa^2 log-uniform in [1, 100], 0-64
     measurements (centres U[0.1,0.9]^3, radius 0.05, variance 1e-4, values
     N(0,1)), FP32-mixed precision, V(1,1) SSOR, 5 levels, all
-    stepped by one CUDA graph.  Reports aggregate samples/s and the per-chain
-    IACT distribution."""
+    stepped by one CUDA graph launch per step: the chains of each lattice
+    size through the batched kernels, and, for comparison, every chain as
+    its own child graph.  Reports aggregate samples/s and the per-chain IACT
+    distribution (steps >= 60 for the IACT)."""
     import torch
     import multigridmc_gb300 as M
     rng = np.random.default_rng(seed)
@@ -788,23 +790,38 @@ def batch_study(nchain, steps, warmup=5, seed=3):
         chains.append(s)
         unknowns += op.n
     setup = time.perf_counter() - t0
-    batch = M.MultigridMCBatch(chains)
-    batch.step(warmup)
-    batch.synchronize()
-    st = torch.cuda.ExternalStream(batch.stream)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(st)
-    batch.step(steps)
-    e1.record(st)
-    batch.synchronize()
-    ms_step = e0.elapsed_time(e1) / steps
-    taus = []
-    for s in chains:
-        z = s.read_observations(warmup + steps + 8)[warmup:]
-        if len(z) > 60 and np.std(z) > 0:
-            taus.append(M.statistics.tau_int(z, 20))
-    batch.close()
+
+    def timed_batch():
+        batch = M.MultigridMCBatch(chains)
+        groups = batch.groups
+        batch.step(warmup)
+        batch.synchronize()
+        st = torch.cuda.ExternalStream(batch.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        batch.step(steps)
+        e1.record(st)
+        batch.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        taus = []
+        for s in chains:
+            z = s.read_observations(warmup + steps + 8)[warmup:]
+            if len(z) > 60 and np.std(z) > 0:
+                taus.append(M.statistics.tau_int(z, 20))
+        batch.close()
+        return ms, groups, taus
+
+    # batched kernels: one launch per kernel of the step for all chains of a
+    # lattice size; then the same chains as one child graph per chain
+    ms_step, groups, taus = timed_batch()
+    os.environ["MGMC_BATCH_KERNELS"] = "0"
+    try:
+        ms_graphs, _, _ = timed_batch()
+    finally:
+        del os.environ["MGMC_BATCH_KERNELS"]
     return {"nchain": nchain, "ms_per_batched_step": ms_step, "samples_per_s": nchain * 1000.0 / ms_step,
+            "groups": groups[0], "chains_in_groups": groups[1],
+            "graph_of_graphs": {"ms_per_batched_step": ms_graphs, "samples_per_s": nchain * 1000.0 / ms_graphs},
             "unknowns_total": int(unknowns), "setup_s": setup, "iact_median": float(np.median(taus)) if taus else None,
             "iact_p90": float(np.percentile(taus, 90)) if taus else None, "iact_window": 20, "steps": steps}
 

@@ -306,14 +306,23 @@ mgmc_status mgmc_level_transfer_device(mgmc_sampler *s, int level, int which, in
 /* ----------------------------------------------------------------- batch */
 /* Many independent chains (the reference's only parallel mode: independent
  * chains per OpenMP thread, src/measurements/convergence.cc:29-78) stepped
- * together: one CUDA graph holds every chain's step as a child graph, so
- * the chains run concurrently.  Chains keep their own state, right hand
+ * together.  Chains that share a lattice geometry and a step structure
+ * (FP32-mixed, MGMC_NOISE_PHILOX, multicolour order, SSOR smoother,
+ * Cholesky coarse solver, constant stencils, 3D) form groups whose step is
+ * one sequence of batched launches -- every launch covers all chains of
+ * the group; every other chain runs its own step graph; all of it is one
+ * CUDA graph launch per step.  A chain follows bit for bit the chain it
+ * follows when stepped alone.  Chains keep their own state, right hand
  * side and observables; they must use MGMC_NOISE_PHILOX and one device.
- * The samplers must outlive the batch; while it exists, step them only
- * through mgmc_batch_step. */
+ * Set observables (mgmc_sampler_set_observable / _set_probes) before
+ * creating the batch.  The samplers must outlive the batch; while it
+ * exists, step them only through mgmc_batch_step. */
 typedef struct mgmc_batch mgmc_batch;
 mgmc_status mgmc_batch_create(int nchain, mgmc_sampler *const *samplers, mgmc_batch **out);
 mgmc_status mgmc_batch_step(mgmc_batch *b, int64_t nsteps);
+/* No counterpart in the reference: the number of batched groups and of the
+ * chains they hold (the rest step through their own graphs). */
+mgmc_status mgmc_batch_info(mgmc_batch *b, int *ngroups, int *ngrouped);
 mgmc_status mgmc_batch_synchronize(mgmc_batch *b);
 mgmc_status mgmc_batch_stream(mgmc_batch *b, void **cuda_stream);
 mgmc_status mgmc_batch_destroy(mgmc_batch *b);

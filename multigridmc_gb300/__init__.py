@@ -131,6 +131,7 @@ SIGNATURES = {
     "mgmc_level_transfer_device": (C.c_int, [_P, C.c_int, C.c_int, C.c_int64]),
     "mgmc_batch_create": (C.c_int, [C.c_int, C.POINTER(_P), C.POINTER(_P)]),
     "mgmc_batch_step": (C.c_int, [_P, C.c_int64]),
+    "mgmc_batch_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "mgmc_batch_synchronize": (C.c_int, [_P]),
     "mgmc_batch_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "mgmc_batch_destroy": (C.c_int, [_P]),
@@ -835,6 +836,14 @@ class MultigridMCBatch:
 
     def synchronize(self):
         _check(self._L.mgmc_batch_synchronize(self._h))
+
+    @property
+    def groups(self):
+        """(number of batched groups, chains in them): the chains that step
+        through the batched kernels rather than their own step graphs."""
+        g, n = C.c_int(0), C.c_int(0)
+        _check(self._L.mgmc_batch_info(self._h, C.byref(g), C.byref(n)))
+        return g.value, n.value
 
     @property
     def stream(self):

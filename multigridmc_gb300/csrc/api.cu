@@ -14,6 +14,7 @@
 #include <cstring>
 #include <functional>
 #include <map>
+#include <memory>
 #include <string>
 #include <tuple>
 #include <type_traits>
@@ -89,6 +90,7 @@ struct Level {
     int bt_split = 1;  // blocks per column of the B^T x reduction
     unsigned *counter = nullptr;  // CTA counter of k_bt_solve
     int sweep_tx = 0;             // CTA width of the colour passes chosen by the autotuner (0: sweep_block())
+    int sweep_threads = 0;        // and its thread count, 128 or 256 (0: RBP_THREADS)
     void *adj[4] = {nullptr, nullptr, nullptr, nullptr};  // adjoint: x-bar, f-bar, two work vectors (T, padded)
     CUtensorMap xmap{}, fmap{};  // 3D tile maps of x and f for the residual-restriction
     bool tma = false;            // maps valid (3D, rows of a multiple of 16 bytes)
@@ -346,7 +348,10 @@ static void raise_smem_limit(void (*kernel)(KArgs...), size_t bytes) {
 // CTA shape of a level's colour passes: the autotuned width, or the
 // smallest power of two covering the `count` work items of a row.
 static dim3 level_block(const Level &lv, int count) {
-    if (lv.sweep_tx > 0) return dim3(lv.sweep_tx, RBP_THREADS / lv.sweep_tx, 1);
+    if (lv.sweep_tx > 0) {
+        const int nt = lv.sweep_threads > 0 ? lv.sweep_threads : RBP_THREADS;
+        return dim3(lv.sweep_tx, nt / lv.sweep_tx, 1);
+    }
     return sweep_block(count);
 }
 
@@ -1283,10 +1288,10 @@ void Sampler::upload_field(Level &lv) {
 }
 
 // Autotuner of the colour passes' CTA shape: for every level that sweeps,
-// time a few noise-free sweeps on scratch vectors for each CTA width that
-// fits the level's rows (the block shape does not change any result: every
-// thread owns whole points or spans) and keep the fastest.  MGMC_AUTOTUNE=0
-// keeps the heuristic shapes.
+// time a few sweeps on scratch vectors for each CTA of 128 or 256 threads
+// whose width fits the level's rows (the block shape does not change any
+// result: every thread owns whole points or spans) and keep the fastest.
+// MGMC_AUTOTUNE=0 keeps the heuristic shapes.
 void Sampler::autotune_sweeps() {
     if (const char *e = std::getenv("MGMC_AUTOTUNE"))
         if (e[0] == '0') return;
@@ -1307,26 +1312,31 @@ void Sampler::autotune_sweeps() {
         nz.d_step = d_step;
         const int noise = noise_mode == NOISE_PHILOX ? NOISE_PHILOX : NOISE_NONE;
         float best = 1e30f;
-        int best_tx = 0;
+        int best_tx = 0, best_nt = RBP_THREADS;
         // the level's own f (still zero, only read): level 0 then runs the
         // kernel variant the chain runs (the colour-split f); best of three
-        for (int tx = 8; tx <= std::min(RBP_THREADS, 2 * cap); tx *= 2) {
-            lv.sweep_tx = tx;
-            for (int r = 0; r < 2; ++r) launch_sweep(*this, lv, true, noise, lv.s1, lv.f, nz, fp32, exact);
-            for (int trial = 0; trial < 3; ++trial) {
-                CK(cudaEventRecord(e0, stream));
-                for (int r = 0; r < 4; ++r) launch_sweep(*this, lv, r % 2 == 0, noise, lv.s1, lv.f, nz, fp32, exact);
-                CK(cudaEventRecord(e1, stream));
-                CK(cudaEventSynchronize(e1));
-                float ms = 0.f;
-                CK(cudaEventElapsedTime(&ms, e0, e1));
-                if (ms < best) {
-                    best = ms;
-                    best_tx = tx;
+        for (int nt : {RBP_THREADS, RBP_THREADS / 2})
+            for (int tx = 8; tx <= std::min(nt, 2 * cap); tx *= 2) {
+                lv.sweep_tx = tx;
+                lv.sweep_threads = nt;
+                for (int r = 0; r < 2; ++r) launch_sweep(*this, lv, true, noise, lv.s1, lv.f, nz, fp32, exact);
+                for (int trial = 0; trial < 3; ++trial) {
+                    CK(cudaEventRecord(e0, stream));
+                    for (int r = 0; r < 4; ++r)
+                        launch_sweep(*this, lv, r % 2 == 0, noise, lv.s1, lv.f, nz, fp32, exact);
+                    CK(cudaEventRecord(e1, stream));
+                    CK(cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    CK(cudaEventElapsedTime(&ms, e0, e1));
+                    if (ms < best) {
+                        best = ms;
+                        best_tx = tx;
+                        best_nt = nt;
+                    }
                 }
             }
-        }
         lv.sweep_tx = best_tx;
+        lv.sweep_threads = best_nt;
         CK(cudaMemsetAsync(lv.s1, 0, (size_t)lv.geo.nalloc * tsize(), stream));
     }
     CK(cudaEventDestroy(e0));
@@ -2486,9 +2496,317 @@ mgmc_status mgmc_level_transfer_device(mgmc_sampler *s, int level, int which, in
     API_END
 }
 
+}  // extern "C"
+
 // ------------------------------------------------------------------- batch
+// Chains that share a lattice geometry and a step structure advance
+// through the batched kernels (k_*_batch in kernels.cuh): one launch per
+// kernel of the step covers every chain of the group, instead of one launch
+// per chain.  Eligible: FP32-mixed, Philox noise, multicolour order, SSOR
+// smoother, coarse Cholesky sampler, constant stencils, 3D.  A chain stepped
+// this way runs the same arithmetic on the same normals as when it is
+// stepped alone (the kernels share their bodies with the one-chain ones).
+// MGMC_BATCH_KERNELS=0 turns the grouping off (every chain then runs its own
+// step graph inside the batch graph).
+static bool batchable(const Sampler &S) {
+    if (!S.fp32 || S.exact || S.noise_mode != NOISE_PHILOX || S.dim != 3) return false;
+    if (S.P.ordering != MGMC_ORDER_MULTICOLOUR || S.P.smoother != MGMC_SMOOTHER_SSOR || !S.chol) return false;
+    if (S.L.size() < 2 || !S.dLinv) return false;
+    for (const Level &lv : S.L) {
+        if (lv.var != 0) return false;
+        if (lv.npt == 7 && !((lv.g.sy % 4) == 0 && (lv.g.sz % 4) == 0)) return false;
+    }
+    return true;
+}
+
+// chains with equal keys step through the same launches
+static std::vector<long long> batch_key(const Sampler &S) {
+    std::vector<long long> k = {S.dim, (long long)S.L.size(), S.P.npresmooth, S.P.npostsmooth, S.P.cycle, S.chol_ld,
+                                (long long)S.chol_smem};
+    long long cs;
+    std::memcpy(&cs, &S.P.coarse_scaling, sizeof(cs));
+    k.push_back(cs);
+    for (const Level &lv : S.L) {
+        for (long long v : {(long long)lv.g.N0, (long long)lv.g.N1, (long long)lv.g.N2, lv.g.sy, lv.g.sz,
+                            (long long)lv.npt, (long long)lv.ncol})
+            k.push_back(v);
+    }
+    return k;
+}
+
+struct BatchGroup {
+    std::vector<Sampler *> ch;
+    int G = 0, nlev = 0, max_m = 0, max_probe = 1;
+    std::vector<BatchLevelArg *> la;          // per level: G entries
+    BatchChainArg *ca = nullptr;
+    std::vector<std::array<BatchLowRank *, 2>> lr;  // per level and sweep direction
+    std::vector<BatchLowRank *> lr_res;       // per level: the residual's y = B^T x
+    std::vector<BtJob *> bt_jobs;             // per level
+    std::vector<int> n_bt;
+    std::vector<std::array<RowJob *, 2>> sc_jobs;
+    std::vector<std::array<int, 2>> n_sc;
+    std::vector<BatchAddBq *> bq;             // per level: rows of the next level's B
+    std::vector<RowJob *> bq_jobs;
+    std::vector<int> n_bq;
+    unsigned inv = 0;
+    std::vector<void *> owned;
+    ~BatchGroup() {
+        for (void *p : owned) cudaFree(p);
+    }
+    template <typename P_>
+    P_ *put(const std::vector<P_> &v, cudaStream_t st) {
+        if (v.empty()) return nullptr;
+        P_ *p = dupload(v, st);
+        owned.push_back(p);
+        return p;
+    }
+    void build(cudaStream_t st);
+    void record(cudaStream_t st);
+    void sor(int lev, bool forward, cudaStream_t st);
+    void sample(int lev, cudaStream_t st);
+};
+
+// row ranges of `rows` rows per chain in jobs of at most 1024 rows
+static void row_jobs(std::vector<RowJob> &jobs, int chain, i64 rows) {
+    for (i64 r = 0; r < rows; r += 1024) jobs.push_back(RowJob{chain, r, std::min(rows, r + 1024)});
+}
+
+void BatchGroup::build(cudaStream_t st) {
+    G = (int)ch.size();
+    const Sampler &S0 = *ch[0];
+    nlev = (int)S0.L.size();
+    la.resize(nlev);
+    lr.resize(nlev);
+    lr_res.resize(nlev);
+    bt_jobs.resize(nlev);
+    n_bt.assign(nlev, 0);
+    sc_jobs.resize(nlev);
+    n_sc.resize(nlev);
+    bq.resize(nlev);
+    bq_jobs.resize(nlev);
+    n_bq.assign(nlev, 0);
+    for (Sampler *S : ch) {
+        max_m = std::max(max_m, S->m);
+        max_probe = std::max(max_probe, S->nprobe);
+    }
+    for (int lev = 0; lev < nlev; ++lev) {
+        std::vector<BatchLevelArg> a(G);
+        std::vector<BatchLowRank> l0(G), l1(G), lres(G);
+        std::vector<BtJob> jobs;
+        std::vector<RowJob> sj0, sj1, qj;
+        std::vector<BatchAddBq> q(G);
+        for (int c = 0; c < G; ++c) {
+            Sampler &S = *ch[c];
+            Level &lv = S.L[lev];
+            BatchLevelArg &A = a[c];
+            A.x = (float *)lv.x;
+            A.f = (float *)lv.f;
+            A.fsplit = lev == 0 ? S.fsplit : nullptr;
+            A.fhalf = S.fhalf;
+            A.xc = lev + 1 < nlev ? (float *)S.L[lev + 1].x : nullptr;
+            A.fc = lev + 1 < nlev ? (float *)S.L[lev + 1].f : nullptr;
+            A.s = stencil_arg<float>(lv, S.P.omega);
+            if (S.m == 0) continue;
+            for (int dir = 0; dir < 2; ++dir) {
+                BatchLowRank &b = dir == 0 ? l0[c] : l1[c];
+                LowRankArg &r = b.lr;
+                r.m = S.m;
+                r.Bptr = lv.Bptr;
+                r.Bidx = lv.Bidx;
+                r.Bval = lv.Bval;
+                r.Bvalf = lv.Bvalf;
+                r.zf = lv.zf;
+                r.SinvT = lv.SinvT[dir];
+                r.sigma_sqrt = S.d_sigma_sqrt;
+                r.y = lv.y;
+                r.z = lv.z;
+                r.part = lv.part;
+                r.counter = lv.counter;
+                const RowCsr &C = lv.C[dir];
+                b.nrows = C.nrows;
+                b.rows = C.rows;
+                b.ptr = C.ptr;
+                b.col = C.col;
+                b.val = (const float *)C.val;
+                row_jobs(dir == 0 ? sj0 : sj1, c, C.nrows);
+            }
+            LowRankArg &r = lres[c].lr;  // launch_bt_plain's arguments
+            r.m = S.m;
+            r.Bptr = lv.Bptr;
+            r.Bidx = lv.Bidx;
+            r.Bval = lv.Bval;
+            r.Bvalf = lv.Bvalf;
+            r.y = lv.y;
+            r.part = lv.part;
+            r.counter = lv.counter;
+            for (int j = 0; j < S.m; ++j)
+                for (int p = 0; p < lv.bt_split; ++p) jobs.push_back(BtJob{c, j, p, lv.bt_split});
+            if (lev + 1 < nlev) {
+                const Level &lc = S.L[lev + 1];
+                const RowCsr &B = lc.Br;
+                q[c] = BatchAddBq{B.nrows, B.rows, B.ptr, B.col, (const double *)B.val, lv.y, S.d_sigma_inv,
+                                  (float *)lc.f};
+                row_jobs(qj, c, B.nrows);
+            }
+        }
+        la[lev] = put(a, st);
+        lr[lev] = {put(l0, st), put(l1, st)};
+        lr_res[lev] = put(lres, st);
+        bt_jobs[lev] = put(jobs, st);
+        n_bt[lev] = (int)jobs.size();
+        sc_jobs[lev] = {put(sj0, st), put(sj1, st)};
+        n_sc[lev] = {(int)sj0.size(), (int)sj1.size()};
+        bq[lev] = put(q, st);
+        bq_jobs[lev] = put(qj, st);
+        n_bq[lev] = (int)qj.size();
+    }
+    std::vector<BatchChainArg> c(G);
+    for (int k = 0; k < G; ++k) {
+        Sampler &S = *ch[k];
+        BatchChainArg &A = c[k];
+        A.seed = S.P.seed;
+        A.d_step = S.d_step;
+        A.Linv = (const float *)S.dLinv;
+        A.LinvT = (const float *)S.dLinvT;
+        A.gv = (float *)S.dgv;
+        A.nprobe = S.nprobe;
+        A.bptr = S.d_bptr;
+        A.bidx = S.d_bidx;
+        A.bval = S.d_bval;
+        A.obs = S.d_obs;
+        A.capacity = S.obs_cap;
+        A.obs_count = S.d_obs_count;
+        A.err = S.d_err;
+        A.done = S.d_done;
+    }
+    ca = put(c, st);
+    CK(cudaStreamSynchronize(st));
+}
+
+template <typename Kern>
+static void batch_launch_check(Kern) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) fail(MGMC_ERR_CUDA, std::string("batched kernel launch: ") + cudaGetErrorString(e));
+}
+
+// Sampler::sor for the whole group: one sweep, its low-rank correction
+void BatchGroup::sor(int lev, bool forward, cudaStream_t st) {
+    const Sampler &S0 = *ch[0];
+    const Level &lv = S0.L[lev];
+    Grid3 g = lv.g;
+    g.pdl = 0;
+    if (lv.npt == 7) {
+        const int ngrp = (g.N0 + 8) / 8;
+        const dim3 blk = level_block(lv, ngrp);
+        const dim3 grid((ngrp + blk.x - 1) / blk.x, (g.N1 + blk.y - 1) / blk.y, g.N2 * G);
+        const bool v8 = (g.sy % 8) == 0 && (g.sz % 8) == 0;
+        bool fs = v8 && lev == 0;
+        for (Sampler *S : ch) fs = fs && S->fsplit;
+        for (int pass = 0; pass < 2; ++pass) {
+            const int colour = forward ? pass : 1 - pass;
+            if (fs)
+                k_sweep_rb_vec_batch<NOISE_PHILOX, true, true><<<grid, blk, 0, st>>>(la[lev], ca, g, colour, pass, inv,
+                                                                                    (unsigned)lev);
+            else if (v8)
+                k_sweep_rb_vec_batch<NOISE_PHILOX, true, false><<<grid, blk, 0, st>>>(la[lev], ca, g, colour, pass,
+                                                                                     inv, (unsigned)lev);
+            else
+                k_sweep_rb_vec_batch<NOISE_PHILOX, false, false><<<grid, blk, 0, st>>>(la[lev], ca, g, colour, pass,
+                                                                                      inv, (unsigned)lev);
+            batch_launch_check(0);
+        }
+    } else {
+        for (int cc = 0; cc < lv.ncol; ++cc) {
+            const int colour = forward ? cc : lv.ncol - 1 - cc;
+            const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
+            const int na = (g.N0 - pa + 1) / 2, nb = (g.N1 - pb + 1) / 2, nc = (g.N2 - pc + 1) / 2;
+            if (na <= 0 || nb <= 0 || nc <= 0) continue;
+            const dim3 blk = level_block(lv, na);
+            const dim3 grid((na + blk.x - 1) / blk.x, (nb + blk.y - 1) / blk.y, nc * G);
+            k_sweep_c27_batch<NOISE_PHILOX><<<grid, blk, 0, st>>>(la[lev], ca, g, colour, nc, inv, (unsigned)lev);
+            batch_launch_check(0);
+        }
+    }
+    if (n_bt[lev] > 0) {
+        const int dir = forward ? 0 : 1;
+        k_bt_solve_batch<NOISE_PHILOX, true><<<n_bt[lev], 256, solve_smem(max_m), st>>>(la[lev], lr[lev][dir], ca,
+                                                                                       bt_jobs[lev], inv, (unsigned)lev);
+        batch_launch_check(0);
+        if (n_sc[lev][dir] > 0) {
+            k_lr_scatter_batch<<<n_sc[lev][dir], 256, 0, st>>>(la[lev], lr[lev][dir], sc_jobs[lev][dir]);
+            batch_launch_check(0);
+        }
+    }
+    inv++;
+}
+
+// Sampler::sample for the whole group (multigridmc_sampler.cc:109-136)
+void BatchGroup::sample(int lev, cudaStream_t st) {
+    const Sampler &S0 = *ch[0];
+    if (lev == nlev - 1) {
+        const Level &lv = S0.L[lev];
+        Grid3 g = lv.g;
+        g.pdl = 0;
+        const unsigned blocks = (unsigned)((lv.geo.n + 7) / 8);
+        k_chol_lower_batch<NOISE_PHILOX><<<dim3(blocks, G), 256, S0.chol_smem, st>>>(la[lev], ca, g, S0.chol_ld, inv,
+                                                                                     (unsigned)lev);
+        batch_launch_check(0);
+        k_chol_upper_batch<<<dim3(blocks, G), 256, S0.chol_smem, st>>>(la[lev], ca, g, S0.chol_ld);
+        batch_launch_check(0);
+        inv++;
+        return;
+    }
+    const Level &lv = S0.L[lev], &lc = S0.L[lev + 1];
+    Grid3 gf = lv.g, gc = lc.g;
+    gf.pdl = gc.pdl = 0;
+    const int cyc = lev > 0 ? S0.P.cycle : 1;
+    for (int j = 0; j < cyc; ++j) {
+        for (int k = 0; k < S0.P.npresmooth; ++k) {
+            sor(lev, true, st);
+            sor(lev, false, st);
+        }
+        // residual-restriction (also zeroes the coarse state), then the
+        // low-rank term of the residual
+        const int tz = (gc.N2 + RR_TZ - 1) / RR_TZ;
+        const dim3 rgrid((gc.N0 + RR_TX - 1) / RR_TX, (gc.N1 + RR_TY - 1) / RR_TY, tz * G);
+        if (lv.npt == 7)
+            k_resid_restrict_batch<7><<<rgrid, RR_THREADS, rr_smem_bytes<float>(), st>>>(la[lev], gf, gc, tz);
+        else
+            k_resid_restrict_batch<27><<<rgrid, RR_THREADS, rr_smem_bytes<float>(), st>>>(la[lev], gf, gc, tz);
+        batch_launch_check(0);
+        if (n_bt[lev] > 0) {
+            k_bt_solve_batch<NOISE_NONE, false><<<n_bt[lev], 256, solve_smem(max_m), st>>>(la[lev], lr_res[lev], ca,
+                                                                                          bt_jobs[lev], 0u, 0u);
+            batch_launch_check(0);
+            if (n_bq[lev] > 0) {
+                k_add_Bq_batch<<<n_bq[lev], 256, 0, st>>>(bq[lev], bq_jobs[lev]);
+                batch_launch_check(0);
+            }
+        }
+        sample(lev + 1, st);
+        const dim3 pgrid((gc.N0 + 1 + 127) / 128, gc.N1 + 1, (gc.N2 + 1) * G);
+        k_prolong_batch<<<pgrid, 128, 0, st>>>(la[lev], gf, gc, (float)S0.P.coarse_scaling, 3, gc.N2 + 1);
+        batch_launch_check(0);
+        for (int k = 0; k < S0.P.npostsmooth; ++k) {
+            sor(lev, true, st);
+            sor(lev, false, st);
+        }
+    }
+}
+
+void BatchGroup::record(cudaStream_t st) {
+    inv = 0;
+    sample(0, st);
+    k_step_end_batch<<<dim3(max_probe, G), 256, 0, st>>>(la[0], ca);
+    batch_launch_check(0);
+}
+
+extern "C" {
+
 struct mgmc_batch {
     std::vector<Sampler *> chains;
+    std::vector<std::unique_ptr<BatchGroup>> groups;
+    std::vector<cudaGraph_t> group_graphs;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -2513,7 +2831,50 @@ mgmc_status mgmc_batch_create(int nchain, mgmc_sampler *const *samplers, mgmc_ba
     CK(cudaSetDevice(B->device));
     CK(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
     CK(cudaGraphCreate(&B->graph, 0));
-    for (Sampler *S : B->chains) {
+    // groups of chains that step through the batched kernels
+    std::vector<Sampler *> solo;
+    {
+        bool group = true;
+        if (const char *e = std::getenv("MGMC_BATCH_KERNELS"))
+            if (e[0] == '0') group = false;
+        std::map<std::vector<long long>, std::vector<Sampler *>> keyed;
+        for (Sampler *S : B->chains) {
+            if (group && batchable(*S))
+                keyed[batch_key(*S)].push_back(S);
+            else
+                solo.push_back(S);
+        }
+        for (auto &kv : keyed) {
+            std::vector<Sampler *> &v = kv.second;
+            if (v.size() < 2) {
+                solo.insert(solo.end(), v.begin(), v.end());
+                continue;
+            }
+            // grid.z carries chains x planes: at most 65535
+            const int zmax = std::max(1, 65535 / std::max(1, v[0]->L[0].g.N2 + 1));
+            for (size_t a = 0; a < v.size(); a += (size_t)zmax) {
+                auto grp = std::make_unique<BatchGroup>();
+                grp->ch.assign(v.begin() + a, v.begin() + std::min(v.size(), a + (size_t)zmax));
+                for (Sampler *S : grp->ch) CK(cudaStreamSynchronize(S->stream));
+                grp->build(B->stream);
+                cudaGraph_t gg = nullptr;
+                CK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+                try {
+                    grp->record(B->stream);
+                } catch (...) {
+                    cudaStreamEndCapture(B->stream, &gg);
+                    if (gg) cudaGraphDestroy(gg);
+                    throw;
+                }
+                CK(cudaStreamEndCapture(B->stream, &gg));
+                B->group_graphs.push_back(gg);
+                cudaGraphNode_t node;
+                CK(cudaGraphAddChildGraphNode(&node, B->graph, nullptr, 0, gg));
+                B->groups.push_back(std::move(grp));
+            }
+        }
+    }
+    for (Sampler *S : solo) {
         CK(cudaStreamSynchronize(S->stream));
         // a chain's step graph becomes a child graph: captured with plain
         // (non-programmatic) dependencies
@@ -2536,6 +2897,7 @@ mgmc_status mgmc_batch_create(int nchain, mgmc_sampler *const *samplers, mgmc_ba
         if (B) {
             if (B->gexec) cudaGraphExecDestroy(B->gexec);
             if (B->graph) cudaGraphDestroy(B->graph);
+            for (cudaGraph_t gg : B->group_graphs) cudaGraphDestroy(gg);
             if (B->stream) cudaStreamDestroy(B->stream);
             delete B;
         }
@@ -2550,6 +2912,16 @@ mgmc_status mgmc_batch_step(mgmc_batch *b, int64_t nsteps) {
     if (!b || nsteps < 0) fail(MGMC_ERR_INVALID_ARGUMENT, "bad arguments");
     CK(cudaSetDevice(b->device));
     for (int64_t k = 0; k < nsteps; ++k) CK(cudaGraphLaunch(b->gexec, b->stream));
+    API_END
+}
+
+mgmc_status mgmc_batch_info(mgmc_batch *b, int *ngroups, int *ngrouped) {
+    API_BEGIN
+    if (!b || !ngroups || !ngrouped) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    *ngroups = (int)b->groups.size();
+    int n = 0;
+    for (const auto &g : b->groups) n += g->G;
+    *ngrouped = n;
     API_END
 }
 
@@ -2575,6 +2947,7 @@ mgmc_status mgmc_batch_destroy(mgmc_batch *b) {
     cudaStreamSynchronize(b->stream);
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
     if (b->graph) cudaGraphDestroy(b->graph);
+    for (cudaGraph_t gg : b->group_graphs) cudaGraphDestroy(gg);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     API_END

@@ -285,17 +285,33 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_pass(T *__restrict__ x
 
 // 256-bit vector access (sm_100 and later): 8 floats at a 32-byte aligned
 // address in one instruction.  ld8 reads through L1 (x is written in the
-// same pass), ld8nc through the read-only path (f, fields).
+// same pass); read-once streams use ld8_stream below.
 __device__ __forceinline__ void ld8(const float *p, float *v) {
     asm volatile("ld.global.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
                  : "l"(p)
                  : "memory");
 }
-__device__ __forceinline__ void ld8nc(const float *p, float *v) {
-    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+// Read-once streams (f and the centre field of the fine sweep): no L1
+// allocation, and first in line for L2 eviction, so that the L2 keeps x --
+// which the next colour pass reads again -- rather than f, which it does
+// not.  (Measured at 256^3: 53.3 -> 49.7 us per two-pass sweep.)
+__device__ __forceinline__ unsigned long long l2_evict_first_policy() {
+    unsigned long long p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ float4 ld4_stream(const float *p, unsigned long long pol) {
+    float4 r;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
+        : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+        : "l"(p), "l"(pol));
+    return r;
+}
+__device__ __forceinline__ void ld8_stream(const float *p, float *v, unsigned long long pol) {
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
         : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
-        : "l"(p));
+        : "l"(p), "l"(pol));
 }
 __device__ __forceinline__ void st8(float *p, const float *v) {
     asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]),
@@ -314,15 +330,17 @@ __device__ __forceinline__ void st8(float *p, const float *v) {
 // V8): f comes from fsc, the colour's half of f split by colour
 // (k_split_colours), so the pass reads one float4 of f per span -- only the
 // values it uses -- instead of the whole span.
-template <int NOISE, bool VD = false, bool V8 = false, bool FS = false>
-__global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict__ x, const float *__restrict__ f,
-                                                              Grid3 g, StencilArg<float> s, int colour, int reverse,
-                                                              NoiseArgs nz, const float *__restrict__ vd,
-                                                              const float *__restrict__ fsc) {
-    if (g.pdl) pdl_begin();
-    const int b = blockIdx.y * blockDim.y + threadIdx.y;
-    const int c = reverse ? g.N2 - 1 - (int)blockIdx.z : (int)blockIdx.z;
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+// The body, with the CTA coordinates (bx, by, bz) passed in: the solo
+// kernel below and the batched kernel (k_sweep_rb_vec_batch) run the same
+// arithmetic.
+template <int NOISE, bool VD, bool V8, bool FS>
+__device__ __forceinline__ void sweep_rb_vec_body(float *__restrict__ x, const float *__restrict__ f, const Grid3 &g,
+                                                  const StencilArg<float> &s, int colour, int reverse,
+                                                  const NoiseArgs &nz, const float *__restrict__ vd,
+                                                  const float *__restrict__ fsc, int bx, int by, int bz) {
+    const int b = by * blockDim.y + threadIdx.y;
+    const int c = reverse ? g.N2 - 1 - bz : bz;
+    const int q = bx * blockDim.x + threadIdx.x;
     const int ngrp = (g.N0 + 8) >> 3;
     if (q >= ngrp || b >= g.N1) return;
     const int P0 = 8 * q;
@@ -334,9 +352,10 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
     const float4 *xu = reinterpret_cast<const float4 *>(x + rb + g.sz + P0);
     const float4 *fr = reinterpret_cast<const float4 *>(f + rb + P0);
     float v[10], ym[8], yp[8], zm[8], zp[8], fv[8], dv[8];
+    const unsigned long long pol_stream = V8 ? l2_evict_first_policy() : 0ull;
     if (VD) {
         if (V8) {
-            ld8nc(vd + rb + P0, dv);
+            ld8_stream(vd + rb + P0, dv, pol_stream);
         } else {
             const float4 *dr = reinterpret_cast<const float4 *>(vd + rb + P0);
             const float4 d0 = dr[0], d1 = dr[1];
@@ -355,14 +374,14 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
         ld8(x + rb - g.sz + P0, zm);
         ld8(x + rb + g.sz + P0, zp);
         if (FS) {
-            const float4 fq = __ldg(reinterpret_cast<const float4 *>(fsc + ((rb + P0) >> 1)));
+            const float4 fq = ld4_stream(fsc + ((rb + P0) >> 1), pol_stream);
             if (j0 == 0) {
                 fv[0] = fq.x; fv[2] = fq.y; fv[4] = fq.z; fv[6] = fq.w;
             } else {
                 fv[1] = fq.x; fv[3] = fq.y; fv[5] = fq.z; fv[7] = fq.w;
             }
         } else {
-            ld8nc(f + rb + P0, fv);
+            ld8_stream(f + rb + P0, fv, pol_stream);
         }
     } else {
         const float4 a0 = xr[0], a1 = xr[1];
@@ -433,6 +452,15 @@ __global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict_
     }
 }
 
+template <int NOISE, bool VD = false, bool V8 = false, bool FS = false>
+__global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec(float *__restrict__ x, const float *__restrict__ f,
+                                                              Grid3 g, StencilArg<float> s, int colour, int reverse,
+                                                              NoiseArgs nz, const float *__restrict__ vd,
+                                                              const float *__restrict__ fsc) {
+    if (g.pdl) pdl_begin();
+    sweep_rb_vec_body<NOISE, VD, V8, FS>(x, f, g, s, colour, reverse, nz, vd, fsc, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // Level 0's f split by colour for the FP32 fine sweep: the value of point
 // (a, b, c) of colour k = (a + b + c) & 1 at fs[k * half + (P >> 1)], P its
 // padded index.  With even row and plane pitches, the two points P = 2i,
@@ -448,20 +476,27 @@ __global__ void __launch_bounds__(256) k_split_colours(const float *__restrict__
 
 // One colour of an 8-colour (27-point) sweep, one thread per point (colour
 // index (a & 1) | (b & 1) << 1 | (c & 1) << 2).
-template <typename T, bool EXACT, int NOISE, int VAR = 0>
-__global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
-                                                                StencilArg<T> s, int colour, NoiseArgs nz,
-                                                                VarField<T> vf) {
-    if (g.pdl) pdl_begin();
+template <typename T, bool EXACT, int NOISE, int VAR>
+__device__ __forceinline__ void sweep_c27_body(T *__restrict__ x, const T *__restrict__ f, const Grid3 &g,
+                                               const StencilArg<T> &s, int colour, const NoiseArgs &nz,
+                                               const VarField<T> &vf, int bx, int by, int bz) {
     const int pa = colour & 1, pb = (colour >> 1) & 1, pc = (colour >> 2) & 1;
-    const int a = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + pa;
-    const int b = 2 * (blockIdx.y * blockDim.y + threadIdx.y) + pb, c = 2 * blockIdx.z + pc;
+    const int a = 2 * (bx * blockDim.x + threadIdx.x) + pa;
+    const int b = 2 * (by * blockDim.y + threadIdx.y) + pb, c = 2 * bz + pc;
     if (b >= g.N1 || c >= g.N2) return;
     T xi = T(0);
     if (NOISE == NOISE_PHILOX) xi = (T)pick(point_normals(nz, g, a, b, c), (a & 7) >> 1);
     if (a >= g.N0) return;
     if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
     sor_point<T, 27, EXACT, VAR>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi, vf);
+}
+
+template <typename T, bool EXACT, int NOISE, int VAR = 0>
+__global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_pass(T *__restrict__ x, const T *__restrict__ f, Grid3 g,
+                                                                StencilArg<T> s, int colour, NoiseArgs nz,
+                                                                VarField<T> vf) {
+    if (g.pdl) pdl_begin();
+    sweep_c27_body<T, EXACT, NOISE, VAR>(x, f, g, s, colour, nz, vf, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // ------------------------------------------------ lexicographic wavefront
@@ -529,8 +564,8 @@ struct LowRankArg {
 // per-thread sums are in the state's precision (FP32 products for the FP32
 // chain) and are combined across the CTA in FP64.
 template <typename T>
-__device__ __forceinline__ void bt_partial_cta(const T *__restrict__ x, const LowRankArg &lr, double *sh) {
-    const int j = blockIdx.x, p = blockIdx.y, P = gridDim.y;
+__device__ __forceinline__ void bt_partial_cta(const T *__restrict__ x, const LowRankArg &lr, double *sh, int j, int p,
+                                               int P) {
     const i64 e0 = lr.Bptr[j], e1 = lr.Bptr[j + 1];
     const i64 len = (e1 - e0 + P - 1) / P;
     const i64 lo = e0 + p * len, hi = min(e1, lo + len);
@@ -559,7 +594,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_bt_partial(const T *__restrict__ x, LowRankArg lr) {
     pdl_begin();
     __shared__ double sh[32];
-    bt_partial_cta<T>(x, lr, sh);
+    bt_partial_cta<T>(x, lr, sh, blockIdx.x, blockIdx.y, gridDim.y);
 }
 
 // One CTA: y_k = sum_p part[k * P + p] (fixed order, so the result does not
@@ -656,19 +691,25 @@ __global__ void __launch_bounds__(256) k_lr_solve(LowRankArg lr, int P, NoiseArg
 // partial sums in the same fixed order as k_lr_solve, so the result does
 // not depend on block timing.
 template <typename T, int NOISE, bool SOLVE>
-__global__ void __launch_bounds__(256) k_bt_solve(const T *__restrict__ x, LowRankArg lr, NoiseArgs nz) {
-    pdl_begin();
+__device__ __forceinline__ void bt_solve_body(const T *__restrict__ x, const LowRankArg &lr, const NoiseArgs &nz, int j,
+                                              int p, int P) {
     __shared__ double sh[32];
     __shared__ bool last;
-    bt_partial_cta<T>(x, lr, sh);
+    bt_partial_cta<T>(x, lr, sh, j, p, P);
     __threadfence();
-    if (threadIdx.x == 0) last = atomicAdd(lr.counter, 1u) == gridDim.x * gridDim.y - 1;
+    if (threadIdx.x == 0) last = atomicAdd(lr.counter, 1u) == (unsigned)(lr.m * P) - 1u;
     __syncthreads();
     if (!last) return;
     __threadfence();
     if (threadIdx.x == 0) *lr.counter = 0u;
     extern __shared__ double dyn[];
-    lr_solve_cta<NOISE, SOLVE>(lr, gridDim.y, nz, dyn, dyn + lr.m, nullptr, true);
+    lr_solve_cta<NOISE, SOLVE>(lr, P, nz, dyn, dyn + lr.m, nullptr, true);
+}
+
+template <typename T, int NOISE, bool SOLVE>
+__global__ void __launch_bounds__(256) k_bt_solve(const T *__restrict__ x, LowRankArg lr, NoiseArgs nz) {
+    pdl_begin();
+    bt_solve_body<T, NOISE, SOLVE>(x, lr, nz, blockIdx.x, blockIdx.y, gridDim.y);
 }
 
 // Low-rank solve and correction in one launch: every CTA forms z itself
@@ -804,14 +845,13 @@ constexpr size_t rr_smem_bytes() {
 }
 
 template <typename T, int NPT>
-__global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tiled(const T *__restrict__ x, const T *__restrict__ f,
-                                                                      T *__restrict__ fc, T *__restrict__ xc, Grid3 gf, Grid3 gc,
-                                                                      StencilArg<T> s) {
-    if (gf.pdl) pdl_begin();
-    extern __shared__ __align__(16) unsigned char rr_smem[];
-    T *xs = reinterpret_cast<T *>(rr_smem);             // [RR_XD][RR_XH][RR_XW]
+__device__ __forceinline__ void resid_restrict_tiled_body(const T *__restrict__ x, const T *__restrict__ f,
+                                                          T *__restrict__ fc, T *__restrict__ xc, const Grid3 &gf,
+                                                          const Grid3 &gc, const StencilArg<T> &s, unsigned char *smem,
+                                                          int bx, int by, int bz) {
+    T *xs = reinterpret_cast<T *>(smem);                 // [RR_XD][RR_XH][RR_XW]
     T *rs = xs + RR_XW * RR_XH * RR_XD;                  // [RR_FD][RR_FH][RR_FW]
-    const int ca0 = blockIdx.x * RR_TX, cb0 = blockIdx.y * RR_TY, cc0 = blockIdx.z * RR_TZ;
+    const int ca0 = bx * RR_TX, cb0 = by * RR_TY, cc0 = bz * RR_TZ;
     // fine 0-based origin of the footprint: the centre of coarse ca0 is fine
     // 2 ca0 + 1, its lower neighbour 2 ca0
     const int fa0 = 2 * ca0, fb0 = 2 * cb0, fz0 = 2 * cc0;
@@ -864,6 +904,15 @@ __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tiled(const T *__
             }
     fc[gc.pad(ca, cb, cc)] = acc;
     if (xc) xc[gc.pad(ca, cb, cc)] = T(0);  // the coarse sample starts from zero
+}
+
+template <typename T, int NPT>
+__global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tiled(const T *__restrict__ x, const T *__restrict__ f,
+                                                                      T *__restrict__ fc, T *__restrict__ xc, Grid3 gf, Grid3 gc,
+                                                                      StencilArg<T> s) {
+    if (gf.pdl) pdl_begin();
+    extern __shared__ __align__(16) unsigned char rr_smem[];
+    resid_restrict_tiled_body<T, NPT>(x, f, fc, xc, gf, gc, s, rr_smem, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // ---------------------------------------------- bulk tensor copies (TMA)
@@ -1024,17 +1073,16 @@ __global__ void __launch_bounds__(256) k_add_Bq(T *__restrict__ dst, i64 nrows, 
 // gathers its <= 2^d coarse parents, weight 1 (even coordinate) or 1/2 for
 // each of the two parents (odd coordinate).
 template <typename T>
-__global__ void __launch_bounds__(128) k_prolong_add(T *__restrict__ x, const T *__restrict__ xc, Grid3 gf, Grid3 gc,
-                                                      T alpha, int dim) {
-    if (gf.pdl) pdl_begin();
+__device__ __forceinline__ void prolong_add_body(T *__restrict__ x, const T *__restrict__ xc, const Grid3 &gf,
+                                                 const Grid3 &gc, T alpha, int dim, int bx, int by, int bz_from_top) {
     // coarse cell (i, j, k), 0 <= i <= Nc0 etc., owns the fine vertices with
     // 1-based coordinates 2 i + {0, 1} (those inside the interior); its
     // corners are the coarse vertices i, i+1 (1-based, ghosts are zero)
     // planes from the top: the residual-restriction before ends there, and
     // the sweep after starts at the bottom, which this kernel writes last
     // (both find their first planes in L2)
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = dim > 1 ? (int)blockIdx.y : 0, k = dim > 2 ? (int)(gridDim.z - 1 - blockIdx.z) : 0;
+    const int i = bx * blockDim.x + threadIdx.x;
+    const int j = dim > 1 ? by : 0, k = dim > 2 ? bz_from_top : 0;
     if (i > gc.N0) return;
     const int ny = dim > 1 ? 2 : 1, nz = dim > 2 ? 2 : 1;
     T cv[2][2][2];
@@ -1086,6 +1134,13 @@ __global__ void __launch_bounds__(128) k_prolong_add(T *__restrict__ x, const T 
             }
         }
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_prolong_add(T *__restrict__ x, const T *__restrict__ xc, Grid3 gf, Grid3 gc,
+                                                      T alpha, int dim) {
+    if (gf.pdl) pdl_begin();
+    prolong_add_body<T>(x, xc, gf, gc, alpha, dim, blockIdx.x, blockIdx.y, (int)(gridDim.z - 1 - blockIdx.z));
 }
 
 // ----------------------------------------------------- stencil apply
@@ -1239,10 +1294,9 @@ __device__ __forceinline__ MT warp_row_dot(const MT *__restrict__ row, const MT 
 
 // v = xi + Linv f (row i: vectors 0 .. i / NV)
 template <typename T, typename MT, int NOISE>
-__global__ void __launch_bounds__(256) k_chol_gemv_lower(const T *__restrict__ f, Grid3 g, const MT *__restrict__ Linv,
-                                                          int ld, MT *__restrict__ v, NoiseArgs nz) {
-    if (g.pdl) pdl_begin();
-    extern __shared__ __align__(16) unsigned char chol_sm[];
+__device__ __forceinline__ void chol_gemv_lower_body(const T *__restrict__ f, const Grid3 &g, const MT *__restrict__ Linv,
+                                                     int ld, MT *__restrict__ v, const NoiseArgs &nz,
+                                                     unsigned char *chol_sm, int bx, int nbx) {
     MT *fs = reinterpret_cast<MT *>(chol_sm);
     const int n = g.N0 * g.N1 * g.N2;
     for (int i = threadIdx.x; i < ld; i += blockDim.x) {
@@ -1256,8 +1310,8 @@ __global__ void __launch_bounds__(256) k_chol_gemv_lower(const T *__restrict__ f
     __syncthreads();
     constexpr int NV = Vec16<MT>::N;
     const int lane = threadIdx.x & 31;
-    const int warps = gridDim.x * (blockDim.x >> 5);
-    for (int ii = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ii < n; ii += warps) {
+    const int warps = nbx * (blockDim.x >> 5);
+    for (int ii = bx * (blockDim.x >> 5) + (threadIdx.x >> 5); ii < n; ii += warps) {
         const int i = (ii & 1) ? n - 1 - (ii >> 1) : (ii >> 1);
         const MT acc = warp_row_dot<MT>(Linv + (i64)i * ld, fs, 0, i / NV + 1, lane);
         if (lane == 0) {
@@ -1272,20 +1326,27 @@ __global__ void __launch_bounds__(256) k_chol_gemv_lower(const T *__restrict__ f
     }
 }
 
-// ... x = Linv^T v (row j of Linv^T: vectors j / NV .. ld / NV - 1).
-template <typename T, typename MT>
-__global__ void __launch_bounds__(256) k_chol_gemv_upper(const MT *__restrict__ v, Grid3 g,
-                                                          const MT *__restrict__ LinvT, int ld, T *__restrict__ x) {
+template <typename T, typename MT, int NOISE>
+__global__ void __launch_bounds__(256) k_chol_gemv_lower(const T *__restrict__ f, Grid3 g, const MT *__restrict__ Linv,
+                                                          int ld, MT *__restrict__ v, NoiseArgs nz) {
     if (g.pdl) pdl_begin();
     extern __shared__ __align__(16) unsigned char chol_sm[];
+    chol_gemv_lower_body<T, MT, NOISE>(f, g, Linv, ld, v, nz, chol_sm, blockIdx.x, gridDim.x);
+}
+
+// ... x = Linv^T v (row j of Linv^T: vectors j / NV .. ld / NV - 1).
+template <typename T, typename MT>
+__device__ __forceinline__ void chol_gemv_upper_body(const MT *__restrict__ v, const Grid3 &g,
+                                                     const MT *__restrict__ LinvT, int ld, T *__restrict__ x,
+                                                     unsigned char *chol_sm, int bx, int nbx) {
     MT *vs = reinterpret_cast<MT *>(chol_sm);
     const int n = g.N0 * g.N1 * g.N2;
     for (int i = threadIdx.x; i < ld; i += blockDim.x) vs[i] = i < n ? v[i] : MT(0);
     __syncthreads();
     constexpr int NV = Vec16<MT>::N;
     const int lane = threadIdx.x & 31;
-    const int warps = gridDim.x * (blockDim.x >> 5);
-    for (int jj = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); jj < n; jj += warps) {
+    const int warps = nbx * (blockDim.x >> 5);
+    for (int jj = bx * (blockDim.x >> 5) + (threadIdx.x >> 5); jj < n; jj += warps) {
         const int j = (jj & 1) ? n - 1 - (jj >> 1) : (jj >> 1);
         const MT acc = warp_row_dot<MT>(LinvT + (i64)j * ld, vs, j / NV, ld / NV, lane);
         if (lane == 0) {
@@ -1293,6 +1354,14 @@ __global__ void __launch_bounds__(256) k_chol_gemv_upper(const MT *__restrict__ 
             x[g.pad(a, t % g.N1, t / g.N1)] = (T)acc;
         }
     }
+}
+
+template <typename T, typename MT>
+__global__ void __launch_bounds__(256) k_chol_gemv_upper(const MT *__restrict__ v, Grid3 g,
+                                                          const MT *__restrict__ LinvT, int ld, T *__restrict__ x) {
+    if (g.pdl) pdl_begin();
+    extern __shared__ __align__(16) unsigned char chol_sm[];
+    chol_gemv_upper_body<T, MT>(v, g, LinvT, ld, x, chol_sm, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------- adjoint
@@ -1726,16 +1795,14 @@ __global__ void __launch_bounds__(256) k_pgrad_coarse_sigma(const double *__rest
 // count and the step counter that keys the Philox streams.  Runs after
 // every other kernel of the step.
 template <typename T>
-__global__ void __launch_bounds__(256) k_step_end(const T *__restrict__ x, int nprobe, const i64 *__restrict__ bptr,
-                                                   const i64 *__restrict__ bidx, const double *__restrict__ bval,
-                                                   double *__restrict__ obs, i64 capacity, u64 *__restrict__ obs_count,
-                                                   u64 *__restrict__ d_step, unsigned *__restrict__ err,
-                                                   unsigned *__restrict__ done) {
-    pdl_begin();
+__device__ __forceinline__ void step_end_body(const T *__restrict__ x, int nprobe, const i64 *__restrict__ bptr,
+                                              const i64 *__restrict__ bidx, const double *__restrict__ bval,
+                                              double *__restrict__ obs, i64 capacity, u64 *__restrict__ obs_count,
+                                              u64 *__restrict__ d_step, unsigned *__restrict__ err,
+                                              unsigned *__restrict__ done, int p, int nblocks) {
     __shared__ double sh[32];
     __shared__ bool last;
-    const int p = blockIdx.x;
-    if (nprobe > 0) {
+    if (nprobe > 0 && p < nprobe) {
         double acc = 0.0;
         for (i64 e = bptr[p] + threadIdx.x; e < bptr[p + 1]; e += blockDim.x) acc += bval[e] * (double)x[bidx[e]];
         acc = block_sum<256>(acc, sh);
@@ -1746,13 +1813,226 @@ __global__ void __launch_bounds__(256) k_step_end(const T *__restrict__ x, int n
         }
     }
     __threadfence();
-    if (threadIdx.x == 0) last = (atomicAdd(done, 1u) == gridDim.x - 1);
+    if (threadIdx.x == 0) last = (atomicAdd(done, 1u) == (unsigned)nblocks - 1u);
     __syncthreads();
     if (last && threadIdx.x == 0) {
         if (nprobe > 0) *obs_count += 1ull;
         *d_step += 1ull;
         *done = 0u;
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_step_end(const T *__restrict__ x, int nprobe, const i64 *__restrict__ bptr,
+                                                   const i64 *__restrict__ bidx, const double *__restrict__ bval,
+                                                   double *__restrict__ obs, i64 capacity, u64 *__restrict__ obs_count,
+                                                   u64 *__restrict__ d_step, unsigned *__restrict__ err,
+                                                   unsigned *__restrict__ done) {
+    pdl_begin();
+    step_end_body<T>(x, nprobe, bptr, bidx, bval, obs, capacity, obs_count, d_step, err, done, blockIdx.x, gridDim.x);
+}
+
+// ------------------------------------------------------- batched chains
+// Chains of one lattice geometry stepped together (FP32-mixed chains with
+// Philox noise): every launch of the step covers all chains of the group --
+// blockIdx.z (or blockIdx.y) picks the chain for the regular work, a job
+// table for the ragged low-rank work -- and each chain keeps its own arrays,
+// stencils, low-rank data, Philox key and step counter.  The kernels call
+// the one-chain kernels' bodies, so a chain stepped in a batch draws the
+// same normals and computes the same values, bit for bit, as when it is
+// stepped alone.
+
+// One chain on one level.
+struct BatchLevelArg {
+    float *x, *f;
+    const float *fsplit;  // level 0: the colour-split f (colour k at fsplit + k * fhalf), else null
+    i64 fhalf;
+    float *xc, *fc;       // the next level's state and right hand side (null on the coarsest level)
+    StencilArg<float> s;
+};
+static_assert(sizeof(StencilArg<float>) == 32 * sizeof(float), "stencil argument: 32 floats");
+
+// One chain: noise key, step counter, coarse Cholesky factors, observables.
+struct BatchChainArg {
+    u64 seed;
+    u64 *d_step;
+    const float *Linv, *LinvT;
+    float *gv;
+    int nprobe;
+    const i64 *bptr, *bidx;
+    const double *bval;
+    double *obs;
+    i64 capacity;
+    u64 *obs_count;
+    unsigned *err, *done;
+};
+
+// Low-rank data of one chain on one level and sweep direction: the B^T x
+// arguments and C = M^{-1} B by rows.
+struct BatchLowRank {
+    LowRankArg lr;
+    i64 nrows;
+    const i64 *rows, *ptr;
+    const int *col;
+    const float *val;
+};
+
+// B^T x work unit: chain, column j, part p of P.
+struct BtJob {
+    int chain, j, p, P;
+};
+// Row range [r0, r1) of one chain's sparse rows.
+struct RowJob {
+    int chain;
+    i64 r0, r1;
+};
+// B_c Sigma^{-1} y rows of one chain's coarse level (the residual's
+// low-rank term), destination its coarse f.
+struct BatchAddBq {
+    i64 nrows;
+    const i64 *rows, *ptr;
+    const int *col;
+    const double *val, *y, *sigma_inv;
+    float *dst;
+};
+
+__device__ __forceinline__ void load_stencil_shared(StencilArg<float> &dst, const StencilArg<float> &src) {
+    const int t = (threadIdx.z * blockDim.y + threadIdx.y) * blockDim.x + threadIdx.x;
+    if (t < 32) reinterpret_cast<float *>(&dst)[t] = reinterpret_cast<const float *>(&src)[t];
+    __syncthreads();
+}
+
+__device__ __forceinline__ NoiseArgs batch_noise(const BatchChainArg &c, unsigned invocation, unsigned level) {
+    NoiseArgs nz;
+    nz.buf = nullptr;
+    nz.seed = c.seed;
+    nz.d_step = c.d_step;
+    nz.invocation = invocation;
+    nz.level = level;
+    return nz;
+}
+
+// red-black colour pass of the 7-point level, grid.z = chains x planes
+template <int NOISE, bool V8, bool FS>
+__global__ void __launch_bounds__(RBP_THREADS) k_sweep_rb_vec_batch(const BatchLevelArg *__restrict__ la,
+                                                                    const BatchChainArg *__restrict__ ca, Grid3 g,
+                                                                    int colour, int reverse, unsigned invocation,
+                                                                    unsigned level) {
+    __shared__ StencilArg<float> ss;
+    const int chain = blockIdx.z / g.N2, bz = blockIdx.z - chain * g.N2;
+    const BatchLevelArg &a = la[chain];
+    load_stencil_shared(ss, a.s);
+    const NoiseArgs nz = batch_noise(ca[chain], invocation, level);
+    const float *fsc = FS ? a.fsplit + colour * a.fhalf : nullptr;
+    sweep_rb_vec_body<NOISE, false, V8, FS>(a.x, a.f, g, ss, colour, reverse, nz, nullptr, fsc, blockIdx.x, blockIdx.y,
+                                            bz);
+}
+
+// one colour of an 8-colour level, grid.z = chains x colour planes
+template <int NOISE>
+__global__ void __launch_bounds__(RBP_THREADS) k_sweep_c27_batch(const BatchLevelArg *__restrict__ la,
+                                                                 const BatchChainArg *__restrict__ ca, Grid3 g,
+                                                                 int colour, int ncz, unsigned invocation,
+                                                                 unsigned level) {
+    __shared__ StencilArg<float> ss;
+    const int chain = blockIdx.z / ncz, bz = blockIdx.z - chain * ncz;
+    const BatchLevelArg &a = la[chain];
+    load_stencil_shared(ss, a.s);
+    const NoiseArgs nz = batch_noise(ca[chain], invocation, level);
+    sweep_c27_body<float, false, NOISE, 0>(a.x, a.f, g, ss, colour, nz, VarField<float>{nullptr, 0}, blockIdx.x,
+                                           blockIdx.y, bz);
+}
+
+// B^T x partial sums with the per-chain solve in each chain's last CTA
+// (SOLVE: the low-rank correction's coefficients; otherwise y = B^T x of the
+// residual), one CTA per job
+template <int NOISE, bool SOLVE>
+__global__ void __launch_bounds__(256) k_bt_solve_batch(const BatchLevelArg *__restrict__ la,
+                                                        const BatchLowRank *__restrict__ lrs,
+                                                        const BatchChainArg *__restrict__ ca,
+                                                        const BtJob *__restrict__ jobs, unsigned invocation,
+                                                        unsigned level) {
+    const BtJob jb = jobs[blockIdx.x];
+    const LowRankArg lr = lrs[jb.chain].lr;
+    const NoiseArgs nz = batch_noise(ca[jb.chain], invocation, level);
+    bt_solve_body<float, NOISE, SOLVE>(la[jb.chain].x, lr, nz, jb.j, jb.p, jb.P);
+}
+
+// x += C z over a row range of one chain (the per-row arithmetic of
+// k_lr_scatter)
+__global__ void __launch_bounds__(256) k_lr_scatter_batch(const BatchLevelArg *__restrict__ la,
+                                                          const BatchLowRank *__restrict__ lrs,
+                                                          const RowJob *__restrict__ jobs) {
+    const RowJob jb = jobs[blockIdx.x];
+    const BatchLowRank &c = lrs[jb.chain];
+    float *x = la[jb.chain].x;
+    const float *z = c.lr.zf;
+    for (i64 r = jb.r0 + threadIdx.x; r < jb.r1; r += blockDim.x) {
+        const i64 row = c.rows[r], e0 = c.ptr[r], e1 = c.ptr[r + 1];
+        float acc = 0.f;
+        for (i64 e = e0; e < e1; ++e) acc += c.val[e] * (float)z[c.col[e]];
+        x[row] = x[row] + acc;
+    }
+}
+
+// f_c -= B_c Sigma^{-1} y over a row range of one chain (the per-row
+// arithmetic of k_add_Bq with sign -1)
+__global__ void __launch_bounds__(256) k_add_Bq_batch(const BatchAddBq *__restrict__ bq,
+                                                      const RowJob *__restrict__ jobs) {
+    const RowJob jb = jobs[blockIdx.x];
+    const BatchAddBq &a = bq[jb.chain];
+    for (i64 r = jb.r0 + threadIdx.x; r < jb.r1; r += blockDim.x) {
+        double acc = 0.0;
+        for (i64 e = a.ptr[r]; e < a.ptr[r + 1]; ++e) acc += a.val[e] * (a.y[a.col[e]] * a.sigma_inv[a.col[e]]);
+        a.dst[a.rows[r]] += (float)(-1.0 * acc);
+    }
+}
+
+// residual + restriction, grid.z = chains x coarse tiles in z
+template <int NPT>
+__global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_batch(const BatchLevelArg *__restrict__ la, Grid3 gf,
+                                                                      Grid3 gc, int tz) {
+    __shared__ StencilArg<float> ss;
+    extern __shared__ __align__(16) unsigned char rr_smem_b[];
+    const int chain = blockIdx.z / tz, bz = blockIdx.z - chain * tz;
+    const BatchLevelArg &a = la[chain];
+    load_stencil_shared(ss, a.s);
+    resid_restrict_tiled_body<float, NPT>(a.x, a.f, a.fc, a.xc, gf, gc, ss, rr_smem_b, blockIdx.x, blockIdx.y, bz);
+}
+
+// x += alpha P x_c, grid.z = chains x (coarse planes + 1)
+__global__ void __launch_bounds__(128) k_prolong_batch(const BatchLevelArg *__restrict__ la, Grid3 gf, Grid3 gc,
+                                                       float alpha, int dim, int nzc) {
+    const int chain = blockIdx.z / nzc, bz = blockIdx.z - chain * nzc;
+    const BatchLevelArg &a = la[chain];
+    prolong_add_body<float>(a.x, a.xc, gf, gc, alpha, dim, blockIdx.x, blockIdx.y, nzc - 1 - bz);
+}
+
+// coarse Cholesky sample, grid.y = chains
+template <int NOISE>
+__global__ void __launch_bounds__(256) k_chol_lower_batch(const BatchLevelArg *__restrict__ la,
+                                                          const BatchChainArg *__restrict__ ca, Grid3 g, int ld,
+                                                          unsigned invocation, unsigned level) {
+    extern __shared__ __align__(16) unsigned char chol_sm_b[];
+    const BatchChainArg &c = ca[blockIdx.y];
+    const NoiseArgs nz = batch_noise(c, invocation, level);
+    chol_gemv_lower_body<float, float, NOISE>(la[blockIdx.y].f, g, c.Linv, ld, c.gv, nz, chol_sm_b, blockIdx.x,
+                                              gridDim.x);
+}
+
+__global__ void __launch_bounds__(256) k_chol_upper_batch(const BatchLevelArg *__restrict__ la,
+                                                          const BatchChainArg *__restrict__ ca, Grid3 g, int ld) {
+    extern __shared__ __align__(16) unsigned char chol_sm_b[];
+    const BatchChainArg &c = ca[blockIdx.y];
+    chol_gemv_upper_body<float, float>(c.gv, g, c.LinvT, ld, la[blockIdx.y].x, chol_sm_b, blockIdx.x, gridDim.x);
+}
+
+// observables and step counters, grid.y = chains
+__global__ void __launch_bounds__(256) k_step_end_batch(const BatchLevelArg *__restrict__ la,
+                                                        const BatchChainArg *__restrict__ ca) {
+    const BatchChainArg &c = ca[blockIdx.y];
+    step_end_body<float>(la[blockIdx.y].x, c.nprobe, c.bptr, c.bidx, c.bval, c.obs, c.capacity, c.obs_count, c.d_step,
+                         c.err, c.done, blockIdx.x, gridDim.x);
 }
 
 }  // namespace mgmc

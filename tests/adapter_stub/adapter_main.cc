@@ -53,7 +53,7 @@ int main(int argc, char **argv) {
         f.setZero();
         x.setZero();
         for (int k = 0; k < m; ++k)
-            for (int e = outer[k]; e < outer[k + 1]; ++e) f[inner[e]] += val[e] * y[k] / Sigma[k];
+            for (int e = outer[k]; e < outer[k + 1]; ++e) f[inner[e]] += val[e] * (y[k] / Sigma[k]);
         MultigridParameters p;
         p.nlevel = 3;
         std::vector<double> stencil(st, st + 27);
