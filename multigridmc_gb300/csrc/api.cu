@@ -598,14 +598,24 @@ static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void
         return;
     }
     if (S.dim == 3 && !zero_stencil && lv.tma && x == lv.x && f == lv.f) {
-        dim3 grid((lc.g.N0 + RR_TX - 1) / RR_TX, (lc.g.N1 + RR_TY - 1) / RR_TY, (lc.g.N2 + RR_TZ - 1) / RR_TZ);
-        const size_t sm = rr_tma_smem_bytes<T>();
+        // persistent CTAs, tiles double-buffered: as many CTAs as fit on the
+        // GPU at once (at most one per tile)
+        const int ntx = (lc.g.N0 + RR_TX - 1) / RR_TX, nty = (lc.g.N1 + RR_TY - 1) / RR_TY,
+                  ntz = (lc.g.N2 + RR_TZ - 1) / RR_TZ;
+        const int ntiles = ntx * nty * ntz;
+        const size_t sm = 2 * rr_pipe_stage_bytes<T>();
+        int per_sm = 1;
         if (lv.npt == 7)
-            plaunch(S.pdl && lv.g.pdl, k_resid_restrict_tma<T, 7>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap, (T *)fc, (T *)xc, lv.g, lc.g, s,
-                    S.d_err);
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resid_restrict_tma_pipe<T, 7>, RR_THREADS, sm));
         else
-            plaunch(S.pdl && lv.g.pdl, k_resid_restrict_tma<T, 27>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap, (T *)fc, (T *)xc, lv.g, lc.g,
-                    s, S.d_err);
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resid_restrict_tma_pipe<T, 27>, RR_THREADS, sm));
+        const int grid = std::max(1, std::min(ntiles, S.nsm * std::max(per_sm, 1)));
+        if (lv.npt == 7)
+            plaunch(S.pdl && lv.g.pdl, k_resid_restrict_tma_pipe<T, 7>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap,
+                    (T *)fc, (T *)xc, lv.g, lc.g, s, S.d_err, ntx, nty, ntiles);
+        else
+            plaunch(S.pdl && lv.g.pdl, k_resid_restrict_tma_pipe<T, 27>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap,
+                    (T *)fc, (T *)xc, lv.g, lc.g, s, S.d_err, ntx, nty, ntiles);
         S.launches++;
         return;
     }
@@ -1118,6 +1128,10 @@ void Sampler::build(const mgmc_operator_desc &op) {
     raise_smem_limit(k_resid_restrict_tiled<double, 27>, rr_smem_bytes<double>());
     raise_smem_limit(k_resid_restrict_tma<double, 7>, rr_tma_smem_bytes<double>());
     raise_smem_limit(k_resid_restrict_tma<double, 27>, rr_tma_smem_bytes<double>());
+    raise_smem_limit(k_resid_restrict_tma_pipe<float, 7>, 2 * rr_pipe_stage_bytes<float>());
+    raise_smem_limit(k_resid_restrict_tma_pipe<float, 27>, 2 * rr_pipe_stage_bytes<float>());
+    raise_smem_limit(k_resid_restrict_tma_pipe<double, 7>, 2 * rr_pipe_stage_bytes<double>());
+    raise_smem_limit(k_resid_restrict_tma_pipe<double, 27>, 2 * rr_pipe_stage_bytes<double>());
     d_step = alloc<u64>(1);
     d_obs_count = alloc<u64>(1);
     d_err = alloc<unsigned>(1);

@@ -984,32 +984,13 @@ __host__ __device__ constexpr size_t rr_tma_smem_bytes() {
     return rr_tma_xbytes<T>() + sizeof(T) * RR_BW * RR_FH * RR_FD;
 }
 
+// The arithmetic of one tile once its x and f boxes are in shared memory:
+// the residual overwrites f, then each thread restricts to its coarse point.
 template <typename T, int NPT>
-__global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tma(const __grid_constant__ CUtensorMap xmap,
-                                                                   const __grid_constant__ CUtensorMap fmap,
-                                                                   T *__restrict__ fc, T *__restrict__ xc, Grid3 gf, Grid3 gc,
-                                                                   StencilArg<T> s, unsigned *__restrict__ err) {
-    if (gf.pdl) pdl_begin();
-    extern __shared__ __align__(1024) unsigned char rr_tma_smem[];
-    __shared__ unsigned long long bar;
-    T *xs = reinterpret_cast<T *>(rr_tma_smem);                      // [RR_XD][RR_XH][RR_BW]
-    T *fs = reinterpret_cast<T *>(rr_tma_smem + rr_tma_xbytes<T>()); // [RR_FD][RR_FH][RR_BW]
-    const int ca0 = blockIdx.x * RR_TX, cb0 = blockIdx.y * RR_TY, cc0 = blockIdx.z * RR_TZ;
+__device__ __forceinline__ void resid_restrict_tile(const T *xs, T *fs, T *__restrict__ fc, T *__restrict__ xc,
+                                                    const Grid3 &gf, const Grid3 &gc, const StencilArg<T> &s, int ca0,
+                                                    int cb0, int cc0) {
     const int fa0 = 2 * ca0, fb0 = 2 * cb0, fz0 = 2 * cc0;
-    if (threadIdx.x == 0) mbar_init(&bar, 1);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        mbar_expect_tx(&bar, (unsigned)(sizeof(T) * RR_BW * (RR_XH * RR_XD + RR_FH * RR_FD)));
-        // padded coordinates: fine vertex a sits at a + 1
-        tma_load_3d(xs, &xmap, fa0, fb0, fz0, &bar);         // fine (fa0-1, fb0-1, fz0-1) ...
-        tma_load_3d(fs, &fmap, fa0, fb0 + 1, fz0 + 1, &bar); // fine (fa0-1, fb0, fz0) ...
-    }
-    const bool ok = mbar_wait_bounded(&bar, 0, TILE_WAIT_NS);
-    if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) atomicOr(err, ERR_TILE_TIMEOUT);
-        mbar_wait_bounded(&bar, 0, TILE_WAIT_NS);  // let copies in flight land before the CTA exits
-        return;
-    }
     constexpr int SY = RR_BW, SZ = RR_BW * RR_XH;
     for (int i = threadIdx.x; i < RR_FW * RR_FH * RR_FD; i += RR_THREADS) {
         const int la = i % RR_FW, lb = (i / RR_FW) % RR_FH, lc = i / (RR_FW * RR_FH);
@@ -1051,6 +1032,101 @@ __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tma(const __grid_
             }
     fc[gc.pad(ca, cb, cc)] = acc;
     if (xc) xc[gc.pad(ca, cb, cc)] = T(0);  // the coarse sample starts from zero
+}
+
+template <typename T, int NPT>
+__global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tma(const __grid_constant__ CUtensorMap xmap,
+                                                                   const __grid_constant__ CUtensorMap fmap,
+                                                                   T *__restrict__ fc, T *__restrict__ xc, Grid3 gf, Grid3 gc,
+                                                                   StencilArg<T> s, unsigned *__restrict__ err) {
+    if (gf.pdl) pdl_begin();
+    extern __shared__ __align__(1024) unsigned char rr_tma_smem[];
+    __shared__ unsigned long long bar;
+    T *xs = reinterpret_cast<T *>(rr_tma_smem);                      // [RR_XD][RR_XH][RR_BW]
+    T *fs = reinterpret_cast<T *>(rr_tma_smem + rr_tma_xbytes<T>()); // [RR_FD][RR_FH][RR_BW]
+    const int ca0 = blockIdx.x * RR_TX, cb0 = blockIdx.y * RR_TY, cc0 = blockIdx.z * RR_TZ;
+    const int fa0 = 2 * ca0, fb0 = 2 * cb0, fz0 = 2 * cc0;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&bar, (unsigned)(sizeof(T) * RR_BW * (RR_XH * RR_XD + RR_FH * RR_FD)));
+        // padded coordinates: fine vertex a sits at a + 1
+        tma_load_3d(xs, &xmap, fa0, fb0, fz0, &bar);         // fine (fa0-1, fb0-1, fz0-1) ...
+        tma_load_3d(fs, &fmap, fa0, fb0 + 1, fz0 + 1, &bar); // fine (fa0-1, fb0, fz0) ...
+    }
+    const bool ok = mbar_wait_bounded(&bar, 0, TILE_WAIT_NS);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicOr(err, ERR_TILE_TIMEOUT);
+        mbar_wait_bounded(&bar, 0, TILE_WAIT_NS);  // let copies in flight land before the CTA exits
+        return;
+    }
+    resid_restrict_tile<T, NPT>(xs, fs, fc, xc, gf, gc, s, ca0, cb0, cc0);
+}
+
+// Persistent, double-buffered variant: a CTA walks the tiles
+// t = blockIdx.x, blockIdx.x + gridDim.x, ... (x fastest, as the one-shot
+// grid orders them); while it computes tile t from one pair of x / f
+// buffers, the bulk tensor copies of its next tile land in the other pair,
+// so the copy latency of every tile but the first is hidden.  Per tile the
+// arithmetic is k_resid_restrict_tma's (resid_restrict_tile).  Waits are
+// bounded as in k_resid_restrict_tma; on a timeout the CTA flags the error,
+// lets both buffers' copies land (bounded) and returns.
+template <typename T>
+__host__ __device__ constexpr size_t rr_pipe_stage_bytes() {
+    return (rr_tma_smem_bytes<T>() + 127) / 128 * 128;
+}
+
+template <typename T, int NPT>
+__global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tma_pipe(const __grid_constant__ CUtensorMap xmap,
+                                                                        const __grid_constant__ CUtensorMap fmap,
+                                                                        T *__restrict__ fc, T *__restrict__ xc,
+                                                                        Grid3 gf, Grid3 gc, StencilArg<T> s,
+                                                                        unsigned *__restrict__ err, int ntx, int nty,
+                                                                        int ntiles) {
+    if (gf.pdl) pdl_begin();
+    extern __shared__ __align__(1024) unsigned char rr_pipe_smem[];
+    __shared__ unsigned long long bar[2];
+    constexpr size_t SB = rr_pipe_stage_bytes<T>();
+    auto xs = [&](int st) { return reinterpret_cast<T *>(rr_pipe_smem + (size_t)st * SB); };
+    auto fs = [&](int st) { return reinterpret_cast<T *>(rr_pipe_smem + (size_t)st * SB + rr_tma_xbytes<T>()); };
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+    }
+    __syncthreads();
+    auto issue = [&](int t, int st) {
+        const int bx = t % ntx, by = (t / ntx) % nty, bz = t / (ntx * nty);
+        const int fa0 = 2 * bx * RR_TX, fb0 = 2 * by * RR_TY, fz0 = 2 * bz * RR_TZ;
+        mbar_expect_tx(&bar[st], (unsigned)(sizeof(T) * RR_BW * (RR_XH * RR_XD + RR_FH * RR_FD)));
+        tma_load_3d(xs(st), &xmap, fa0, fb0, fz0, &bar[st]);
+        tma_load_3d(fs(st), &fmap, fa0, fb0 + 1, fz0 + 1, &bar[st]);
+    };
+    if (threadIdx.x == 0 && (int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
+    int it = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
+        const int st = it & 1;
+        const int tn = t + gridDim.x;
+        if (threadIdx.x == 0 && tn < ntiles) {
+            // the other pair of buffers was last read and written by this CTA's
+            // threads (generic proxy) before the __syncthreads closing the
+            // previous iteration; order those accesses before the copies
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(tn, st ^ 1);
+        }
+        const bool ok = mbar_wait_bounded(&bar[st], (unsigned)((it >> 1) & 1), TILE_WAIT_NS);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                atomicOr(err, ERR_TILE_TIMEOUT);
+                mbar_wait_bounded(&bar[st], (unsigned)((it >> 1) & 1), TILE_WAIT_NS);
+                if (tn < ntiles) mbar_wait_bounded(&bar[st ^ 1], (unsigned)(((it + 1) >> 1) & 1), TILE_WAIT_NS);
+            }
+            __syncthreads();
+            return;
+        }
+        const int bx = t % ntx, by = (t / ntx) % nty, bz = t / (ntx * nty);
+        resid_restrict_tile<T, NPT>(xs(st), fs(st), fc, xc, gf, gc, s, bx * RR_TX, by * RR_TY, bz * RR_TZ);
+        __syncthreads();
+    }
 }
 
 // dst[row] += sign * sum_e B_e y_{col_e} / Sigma_{col_e} over the rows of B
