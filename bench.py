@@ -597,7 +597,7 @@ def adjoint_study(nsteps=200, every=10, nfd=4, seed=7):
     return out
 
 
-def summary_study(sizes=(16, 32, 48, 64, 128), m=32, seed=1):
+def summary_study(sizes=(16, 32, 48, 64, 128), m=32, seed=1, lrchol_max=48):
     """The reference's published comparison (python/plot_summary.py:23-33:
     IACT and time per independent sample of the Cholesky, Gibbs and MGMC
     samplers on a 3D posterior at 16^3 .. 64^3 cells) on the GPU, plus
@@ -606,9 +606,9 @@ def summary_study(sizes=(16, 32, 48, 64, 128), m=32, seed=1):
     b^T x with b the measurement vector at the centre (sampling_time.cc:22-40).
     MGMC: V(1,1) SSOR down to 8^3 cells (6^3 at 48^3); Gibbs: the one-level
     SSOR sampler; exact: x = Q^{-1}(f + eta), one multigrid solve to 1e-10
-    per independent draw (the role of the Cholesky sampler, whose dense or
-    sparse factor does not reach these sizes here).  Time per independent
-    sample = ms per step x IACT; IACT windows grow to 10 IACT."""
+    per independent draw; the reference's LowRankCholeskySampler (factor of
+    A_0 on the host, samples on the GPU) up to lrchol_max^3 cells.  Time per
+    independent sample = ms per step x IACT; IACT windows grow to 10 IACT."""
     import multigridmc_gb300 as M
     levels = {16: 2, 32: 3, 48: 4, 64: 4, 96: 4, 128: 5}
     rows = []
@@ -670,6 +670,24 @@ def summary_study(sizes=(16, 32, 48, 64, 128), m=32, seed=1):
             dt = (time.perf_counter() - t0) / ns
             s.close()
             row[name] = {"ms_per_sample": dt * 1e3, "iterations": its / ns, "ms_per_indep": dt * 1e3}
+        if N <= lrchol_max:
+            # the reference's LowRankCholeskySampler: factor of A_0 on the
+            # host (set-up timed apart), FP64 samples on the GPU
+            t0 = time.perf_counter()
+            s = M.LowRankCholeskySampler(op, seed=seed + 300)
+            setup = time.perf_counter() - t0
+            s.fix_rhs(f)
+            for _ in range(3):
+                s.apply_device(0, xd.data_ptr())
+            torch.cuda.synchronize()
+            ns = 40
+            t0 = time.perf_counter()
+            for _ in range(ns):
+                s.apply_device(0, xd.data_ptr())
+            torch.cuda.synchronize()
+            dt = (time.perf_counter() - t0) / ns
+            s.close()
+            row["lowrank_cholesky_fp64"] = {"ms_per_sample": dt * 1e3, "ms_per_indep": dt * 1e3, "setup_s": setup}
         rows.append(row)
         print(json.dumps({"summary_row": row}), flush=True)
     return rows

@@ -327,6 +327,31 @@ mgmc_status mgmc_batch_synchronize(mgmc_batch *b);
 mgmc_status mgmc_batch_stream(mgmc_batch *b, void **cuda_stream);
 mgmc_status mgmc_batch_destroy(mgmc_batch *b);
 
+/* ------------------------------------------- low-rank Cholesky sampler */
+/* LowRankCholeskySampler (src/sampler/cholesky_sampler.cc:41-129,
+ * cholesky_sampler.hh:173-267): the exact comparator of the reference's
+ * summary study.  Created from an operator with a constant stencil (a
+ * per-vertex centre or field: MGMC_ERR_UNSUPPORTED); the Cholesky factor
+ * of A_0 is computed once on the host in FP64, block by block along the
+ * last lattice direction (A_0 is block tridiagonal there: planes in 3D),
+ * with the reference's low-rank correction (V = L^{-1} B = Q R, the factor
+ * W of Id - R (Sigma + V^T V)^{-1} R^T); samples are drawn on the GPU in
+ * FP64: n normals (noise MGMC_NOISE_PHILOX, key `seed`, or
+ * MGMC_NOISE_INJECTED in the reference's draw order), g = L^{-1} f
+ * corrected by the low-rank factors, x = L^{-T}(xi + g) corrected likewise.
+ * The host set-up costs about 2 nb p^3 flops (nb blocks of p vertices) and
+ * the device holds 2 nb p^2 + 3 n m doubles.  apply: x <- a sample (x's
+ * input value is not used); f == NULL samples with the fixed f. */
+typedef struct mgmc_lrchol mgmc_lrchol;
+mgmc_status mgmc_lrchol_create(const mgmc_operator_desc *op, int noise, uint64_t seed, int device, mgmc_lrchol **out);
+mgmc_status mgmc_lrchol_destroy(mgmc_lrchol *s);
+/* LowRankCholeskySampler::fix_rhs (cholesky_sampler.cc:117-129) */
+mgmc_status mgmc_lrchol_fix_rhs(mgmc_lrchol *s, const double *f, int on_device);
+/* LowRankCholeskySampler::apply (cholesky_sampler.cc:86-115) */
+mgmc_status mgmc_lrchol_apply(mgmc_lrchol *s, const double *f, double *x, int on_device);
+mgmc_status mgmc_lrchol_inject_noise(mgmc_lrchol *s, const double *normals, int64_t count);
+mgmc_status mgmc_lrchol_stream(mgmc_lrchol *s, void **cuda_stream);
+
 /* ------------------------------------------------------------ diagnostics */
 /* No counterpart in the reference.  Measured FMA throughput of the current
  * GPU in TFLOP/s (2 flop per FMA), FP64 (precision = MGMC_FP64) or FP32

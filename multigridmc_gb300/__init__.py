@@ -13,6 +13,7 @@ this module              reference (eikehmueller/MultigridMC)
 ``MultigridMCSampler``   MultigridMCSampler (sampler/multigridmc_sampler.cc:8-145)
 ``SSORSampler``          SSORSampler (sampler/ssor_sampler.{hh,cc})
 ``CholeskySampler``      DenseCholeskySampler (sampler/cholesky_sampler.cc:25-37)
+``LowRankCholeskySampler``  LowRankCholeskySampler (sampler/cholesky_sampler.cc:41-129)
 ``MultigridPreconditioner``  MultigridPreconditioner (preconditioner/multigrid_preconditioner.cc:8-108)
 ``SORSmoother``          SORSmoother (smoother/sor_smoother.cc:9-78), nsmooth = 1
 ``SSORSmoother``         SSORSmoother (smoother/ssor_smoother.cc:9-16)
@@ -41,6 +42,7 @@ __all__ = [
     "MGMCError", "load", "fd_stencil", "galerkin_stencil", "measurement_vector", "intergrid_to_sparse",
     "LinearOperator",
     "MultigridParameters", "MultigridMCSampler", "MultigridMCBatch", "SSORSampler", "CholeskySampler",
+    "LowRankCholeskySampler",
     "IterativeSolverParameters", "MultigridPreconditioner", "LoopSolver", "ExactSampler", "SORSmoother",
     "SSORSmoother",
     "FP64", "FP32_MIXED", "LEXICOGRAPHIC", "MULTICOLOUR", "PHILOX", "INJECTED", "FORWARD", "BACKWARD",
@@ -135,6 +137,12 @@ SIGNATURES = {
     "mgmc_batch_synchronize": (C.c_int, [_P]),
     "mgmc_batch_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "mgmc_batch_destroy": (C.c_int, [_P]),
+    "mgmc_lrchol_create": (C.c_int, [C.POINTER(_OpDesc), C.c_int, C.c_uint64, C.c_int, C.POINTER(_P)]),
+    "mgmc_lrchol_destroy": (C.c_int, [_P]),
+    "mgmc_lrchol_fix_rhs": (C.c_int, [_P, _D, C.c_int]),
+    "mgmc_lrchol_apply": (C.c_int, [_P, _D, _D, C.c_int]),
+    "mgmc_lrchol_inject_noise": (C.c_int, [_P, _D, C.c_int64]),
+    "mgmc_lrchol_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "mgmc_device_fma_rate": (C.c_int, [C.c_int, _D]),
     "mgmc_measured_apply_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _D, C.c_int, _P, _P, _P, _P,
                                               _P, _P, _P]),
@@ -898,6 +906,64 @@ def CholeskySampler(linear_operator, **kw):
     (cholesky_sampler.hh:52-66; its callers pass the same f)."""
     p = MultigridParameters(nlevel=1, coarse_solver="Cholesky")
     return MultigridMCSampler(linear_operator, p, **kw)
+
+
+class LowRankCholeskySampler:
+    """LowRankCholeskySampler (cholesky_sampler.cc:41-129): A_0 factored once
+    on the host (FP64, block by block along the last lattice direction), the
+    low-rank term through the thin QR of L^{-1} B; samples drawn on the GPU
+    (mgmc_lrchol_*).  ``apply(f, x)`` writes a sample into x; f = None uses
+    the f given to ``fix_rhs``."""
+
+    def __init__(self, linear_operator, noise=PHILOX, seed=0, device=0):
+        if linear_operator.centre is not None or linear_operator.field is not None:
+            raise MGMCError(8, "the low-rank Cholesky sampler takes a constant stencil")
+        self.op = linear_operator
+        self.n = linear_operator.n
+        self._L = load()
+        self._h = C.c_void_p()
+        desc = linear_operator._desc()
+        _check(self._L.mgmc_lrchol_create(C.byref(desc), int(noise), C.c_uint64(seed), int(device),
+                                          C.byref(self._h)))
+
+    def fix_rhs(self, f):
+        f = _f64(f)
+        _check(self._L.mgmc_lrchol_fix_rhs(self._h, _dp(f), 0))
+
+    def apply(self, f, x):
+        assert x.dtype == np.float64 and x.flags.c_contiguous and x.size == self.n
+        if f is None:
+            _check(self._L.mgmc_lrchol_apply(self._h, None, _dp(x), 0))
+        else:
+            f = _f64(f)
+            _check(self._L.mgmc_lrchol_apply(self._h, _dp(f), _dp(x), 0))
+        return x
+
+    def apply_device(self, f_ptr, x_ptr):
+        """apply on device arrays (raw addresses; f_ptr = 0: the fixed f)."""
+        _check(self._L.mgmc_lrchol_apply(self._h, C.cast(C.c_void_p(f_ptr or None), _D),
+                                         C.cast(C.c_void_p(x_ptr), _D), 1))
+
+    def inject_noise(self, normals):
+        normals = _f64(normals)
+        _check(self._L.mgmc_lrchol_inject_noise(self._h, _dp(normals), len(normals)))
+
+    @property
+    def stream(self):
+        st = C.c_void_p()
+        _check(self._L.mgmc_lrchol_stream(self._h, C.byref(st)))
+        return st.value
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.mgmc_lrchol_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ------------------------------------------------------ deterministic solver

@@ -598,24 +598,14 @@ static void launch_resid_restrict(Sampler &S, int lev, const void *x, const void
         return;
     }
     if (S.dim == 3 && !zero_stencil && lv.tma && x == lv.x && f == lv.f) {
-        // persistent CTAs, tiles double-buffered: as many CTAs as fit on the
-        // GPU at once (at most one per tile)
-        const int ntx = (lc.g.N0 + RR_TX - 1) / RR_TX, nty = (lc.g.N1 + RR_TY - 1) / RR_TY,
-                  ntz = (lc.g.N2 + RR_TZ - 1) / RR_TZ;
-        const int ntiles = ntx * nty * ntz;
-        const size_t sm = 2 * rr_pipe_stage_bytes<T>();
-        int per_sm = 1;
+        dim3 grid((lc.g.N0 + RR_TX - 1) / RR_TX, (lc.g.N1 + RR_TY - 1) / RR_TY, (lc.g.N2 + RR_TZ - 1) / RR_TZ);
+        const size_t sm = rr_tma_smem_bytes<T>();
         if (lv.npt == 7)
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resid_restrict_tma_pipe<T, 7>, RR_THREADS, sm));
+            plaunch(S.pdl && lv.g.pdl, k_resid_restrict_tma<T, 7>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap, (T *)fc, (T *)xc, lv.g, lc.g, s,
+                    S.d_err);
         else
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resid_restrict_tma_pipe<T, 27>, RR_THREADS, sm));
-        const int grid = std::max(1, std::min(ntiles, S.nsm * std::max(per_sm, 1)));
-        if (lv.npt == 7)
-            plaunch(S.pdl && lv.g.pdl, k_resid_restrict_tma_pipe<T, 7>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap,
-                    (T *)fc, (T *)xc, lv.g, lc.g, s, S.d_err, ntx, nty, ntiles);
-        else
-            plaunch(S.pdl && lv.g.pdl, k_resid_restrict_tma_pipe<T, 27>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap,
-                    (T *)fc, (T *)xc, lv.g, lc.g, s, S.d_err, ntx, nty, ntiles);
+            plaunch(S.pdl && lv.g.pdl, k_resid_restrict_tma<T, 27>, grid, RR_THREADS, sm, S.stream, lv.xmap, lv.fmap, (T *)fc, (T *)xc, lv.g, lc.g,
+                    s, S.d_err);
         S.launches++;
         return;
     }
@@ -1128,10 +1118,6 @@ void Sampler::build(const mgmc_operator_desc &op) {
     raise_smem_limit(k_resid_restrict_tiled<double, 27>, rr_smem_bytes<double>());
     raise_smem_limit(k_resid_restrict_tma<double, 7>, rr_tma_smem_bytes<double>());
     raise_smem_limit(k_resid_restrict_tma<double, 27>, rr_tma_smem_bytes<double>());
-    raise_smem_limit(k_resid_restrict_tma_pipe<float, 7>, 2 * rr_pipe_stage_bytes<float>());
-    raise_smem_limit(k_resid_restrict_tma_pipe<float, 27>, 2 * rr_pipe_stage_bytes<float>());
-    raise_smem_limit(k_resid_restrict_tma_pipe<double, 7>, 2 * rr_pipe_stage_bytes<double>());
-    raise_smem_limit(k_resid_restrict_tma_pipe<double, 27>, 2 * rr_pipe_stage_bytes<double>());
     d_step = alloc<u64>(1);
     d_obs_count = alloc<u64>(1);
     d_err = alloc<unsigned>(1);
@@ -2964,6 +2950,307 @@ mgmc_status mgmc_batch_destroy(mgmc_batch *b) {
     for (cudaGraph_t gg : b->group_graphs) cudaGraphDestroy(gg);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
+    API_END
+}
+
+}  // extern "C"
+
+// --------------------------------------------- low-rank Cholesky sampler
+// LowRankCholeskySampler (cholesky_sampler.cc:41-129) on the GPU.  The
+// factors come from lowrank_cholesky_factors (setup.cc): D_k = L_kk^{-1}
+// and O_k = L_{k,k-1} of the block factor of A_0, and Q, QW, QWT.  A sample
+// is xi ~ N(0, 1) (n normals: Philox or injected), g = L^{-1} f block by
+// block (g_k = D_k (f_k - O_k g_{k-1})), g += QW (Q^T g), xi += g,
+// xi += QWT (Q^T xi), and x = L^{-T} xi block by block from the last
+// (x_k = D_k^T (xi_k - O_{k+1}^T x_{k+1})) -- dense FP64 matrix-vector
+// products (k_dgemv_rows, k_dgemv_cols_partial / _finish) captured into
+// one CUDA graph.
+struct LrChol {
+    int device = 0, nb = 0, m = 0, noise = NOISE_PHILOX;
+    i64 n = 0, p = 0;
+    u64 seed = 0;
+    cudaStream_t stream = nullptr;
+    double *D = nullptr, *O = nullptr, *Q = nullptr, *QW = nullptr, *QWT = nullptr;
+    double *f = nullptr, *x = nullptr, *xi = nullptr, *g = nullptr, *t = nullptr, *mt = nullptr, *part = nullptr;
+    double *noise_buf = nullptr;
+    i64 noise_cap = 0, noise_len = 0, noise_pos = 0;
+    u64 *d_step = nullptr;
+    bool rhs_set = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<void *> owned;
+    static constexpr int RCH = 64;  // rows per partial sum of a transposed product
+    ~LrChol() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        for (void *q : owned) cudaFree(q);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    template <typename P_>
+    P_ *alloc(size_t count) {
+        P_ *q = dalloc<P_>(count);
+        owned.push_back(q);
+        return q;
+    }
+    template <typename P_>
+    P_ *upload(const std::vector<P_> &v) {
+        P_ *q = dupload(v, stream);
+        owned.push_back(q);
+        return q;
+    }
+    // y = yadd + alpha A v, A rows x cols row-major
+    void rows(const double *A, i64 r, i64 c, i64 lda, const double *v, const double *yadd, double alpha, double *y,
+              bool lower) {
+        const unsigned blocks = (unsigned)((r * 32 + 255) / 256);
+        if (lower)
+            k_dgemv_rows<true><<<blocks, 256, 0, stream>>>(A, r, c, lda, v, yadd, alpha, y);
+        else
+            k_dgemv_rows<false><<<blocks, 256, 0, stream>>>(A, r, c, lda, v, yadd, alpha, y);
+    }
+    // y = yadd + alpha A^T v
+    void cols(const double *A, i64 r, i64 c, i64 lda, const double *v, const double *yadd, double alpha, double *y,
+              bool lower) {
+        const int nch = (int)((r + RCH - 1) / RCH);
+        const int bs = c >= 256 ? 256 : (int)((c + 31) / 32 * 32);
+        const dim3 grid((unsigned)((c + bs - 1) / bs), (unsigned)nch);
+        if (lower)
+            k_dgemv_cols_partial<true><<<grid, bs, 0, stream>>>(A, r, c, lda, v, RCH, part);
+        else
+            k_dgemv_cols_partial<false><<<grid, bs, 0, stream>>>(A, r, c, lda, v, RCH, part);
+        k_dgemv_cols_finish<<<(unsigned)((c + 255) / 256), 256, 0, stream>>>(part, nch, c, yadd, alpha, y);
+    }
+    void sample() {
+        NoiseArgs nz{};
+        nz.seed = seed;
+        nz.d_step = d_step;
+        nz.invocation = 0;
+        nz.level = 0;
+        if (noise == NOISE_INJECTED) {
+            nz.buf = noise_buf + noise_pos;
+            k_cholesky_normals<NOISE_INJECTED><<<nblk(n, 256), 256, 0, stream>>>(nz, n, xi);
+        } else {
+            k_cholesky_normals<NOISE_PHILOX><<<nblk(n, 256), 256, 0, stream>>>(nz, n, xi);
+        }
+        // g = L^{-1} f
+        for (int k = 0; k < nb; ++k) {
+            const double *Dk = D + (size_t)k * p * p;
+            const double *v = f + k * p;
+            if (k > 0) {
+                rows(O + (size_t)k * p * p, p, p, p, g + (k - 1) * p, f + k * p, -1.0, t, false);
+                v = t;
+            }
+            rows(Dk, p, p, p, v, nullptr, 1.0, g + k * p, true);
+        }
+        if (m > 0) {  // g += QW (Q^T g)
+            cols(Q, n, m, m, g, nullptr, 1.0, mt, false);
+            rows(QW, n, m, m, mt, g, 1.0, g, false);
+        }
+        k_axpy<double><<<nblk(n, 256), 256, 0, stream>>>(xi, g, 1.0, n);
+        if (m > 0) {  // xi += QWT (Q^T xi)
+            cols(Q, n, m, m, xi, nullptr, 1.0, mt, false);
+            rows(QWT, n, m, m, mt, xi, 1.0, xi, false);
+        }
+        // x = L^{-T} xi
+        for (int k = nb - 1; k >= 0; --k) {
+            const double *v = xi + k * p;
+            if (k + 1 < nb) {
+                cols(O + (size_t)(k + 1) * p * p, p, p, p, x + (k + 1) * p, xi + k * p, -1.0, t, false);
+                v = t;
+            }
+            cols(D + (size_t)k * p * p, p, p, p, v, nullptr, 1.0, x + k * p, true);
+        }
+        k_counter_advance<<<1, 1, 0, stream>>>(d_step);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) fail(MGMC_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    }
+    void run() {
+        if (noise == NOISE_INJECTED) {
+            if (noise_len - noise_pos < n)
+                fail(MGMC_ERR_NOISE_EXHAUSTED, "injected noise exhausted: " + std::to_string(noise_len - noise_pos) +
+                                                   " queued, " + std::to_string(n) + " needed per sample");
+            sample();
+            noise_pos += n;
+            return;
+        }
+        if (!gexec) {
+            CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            try {
+                sample();
+            } catch (...) {
+                cudaGraph_t gg = nullptr;
+                cudaStreamEndCapture(stream, &gg);
+                if (gg) cudaGraphDestroy(gg);
+                throw;
+            }
+            CK(cudaStreamEndCapture(stream, &graph));
+            CK(cudaGraphInstantiate(&gexec, graph, 0));
+        }
+        CK(cudaGraphLaunch(gexec, stream));
+    }
+};
+
+struct mgmc_lrchol {
+    std::unique_ptr<LrChol> impl;
+};
+
+static LrChol &lrimpl(mgmc_lrchol *s) {
+    if (!s || !s->impl) fail(MGMC_ERR_INVALID_ARGUMENT, "null sampler");
+    CK(cudaSetDevice(s->impl->device));
+    return *s->impl;
+}
+
+// n doubles host or device -> device buffer dst of the sampler
+static void lr_put(LrChol &S, const double *src, int on_device, double *dst) {
+    CK(cudaMemcpyAsync(dst, src, (size_t)S.n * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                       S.stream));
+}
+
+extern "C" {
+
+mgmc_status mgmc_lrchol_create(const mgmc_operator_desc *op, int noise, uint64_t seed, int device, mgmc_lrchol **out) {
+    mgmc_lrchol *h = nullptr;
+    API_BEGIN
+    if (!op || !out) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    if (op->dim < 1 || op->dim > 3) fail(MGMC_ERR_INVALID_ARGUMENT, "dim must be 1, 2 or 3");
+    if (op->centre || op->field) fail(MGMC_ERR_UNSUPPORTED, "the low-rank Cholesky sampler takes a constant stencil");
+    if (noise != MGMC_NOISE_PHILOX && noise != MGMC_NOISE_INJECTED) fail(MGMC_ERR_INVALID_ARGUMENT, "invalid noise source");
+    if (op->m < 0 || (op->m > 0 && (!op->B_colptr || !op->B_rowidx || !op->B_val || !op->Sigma)))
+        fail(MGMC_ERR_INVALID_ARGUMENT, "low-rank term needs B and Sigma");
+    const int cells[3] = {op->nx, op->dim > 1 ? op->ny : 2, op->dim > 2 ? op->nz : 2};
+    for (int d = 0; d < op->dim; ++d)
+        if (cells[d] < 2) fail(MGMC_ERR_LATTICE, "every active direction needs at least 2 cells");
+    Geometry geo(op->dim, cells[0], cells[1], cells[2]);
+    SparseCols B;
+    B.m = op->m;
+    std::vector<double> Sigma;
+    if (op->m > 0) {
+        B.ptr.assign(op->B_colptr, op->B_colptr + op->m + 1);
+        for (int j = 0; j < op->m; ++j)
+            for (i64 e = op->B_colptr[j]; e < op->B_colptr[j + 1]; ++e)
+                if (op->B_rowidx[e] < 0 || op->B_rowidx[e] >= geo.n) fail(MGMC_ERR_INVALID_ARGUMENT, "B row index out of range");
+        B.row.assign(op->B_rowidx, op->B_rowidx + op->B_colptr[op->m]);
+        B.val.assign(op->B_val, op->B_val + op->B_colptr[op->m]);
+        Sigma.assign(op->Sigma, op->Sigma + op->m);
+    }
+    LowRankCholeskyFactors F;
+    if (!lowrank_cholesky_factors(geo, op->stencil, B, Sigma, F))
+        fail(MGMC_ERR_NOT_SPD, "the prior or the low-rank system is not positive definite");
+    h = new mgmc_lrchol();
+    h->impl.reset(new LrChol());
+    LrChol &S = *h->impl;
+    S.device = device;
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
+    S.n = geo.n;
+    S.nb = F.nb;
+    S.p = F.p;
+    S.m = F.m;
+    S.noise = noise == MGMC_NOISE_INJECTED ? NOISE_INJECTED : NOISE_PHILOX;
+    S.seed = seed;
+    S.D = S.upload(F.D);
+    S.O = S.upload(F.O);
+    if (S.m > 0) {
+        S.Q = S.upload(F.Q);
+        S.QW = S.upload(F.QW);
+        S.QWT = S.upload(F.QWT);
+    }
+    S.f = S.alloc<double>(S.n);
+    S.x = S.alloc<double>(S.n);
+    S.xi = S.alloc<double>(S.n);
+    S.g = S.alloc<double>(S.n);
+    S.t = S.alloc<double>(S.p);
+    S.mt = S.alloc<double>(std::max(S.m, 1));
+    const i64 maxr = std::max<i64>(S.n, S.p), maxc = std::max<i64>(S.p, S.m);
+    S.part = S.alloc<double>((size_t)((maxr + LrChol::RCH - 1) / LrChol::RCH) * maxc);
+    S.d_step = S.alloc<u64>(1);
+    CK(cudaMemsetAsync(S.d_step, 0, sizeof(u64), S.stream));
+    for (double *q : {S.f, S.x, S.xi, S.g}) CK(cudaMemsetAsync(q, 0, (size_t)S.n * sizeof(double), S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    *out = h;
+    h = nullptr;
+    }
+    catch (const Error &e) {
+        delete h;
+        g_err = e.msg;
+        return e.st;
+    }
+    catch (const std::bad_alloc &) {
+        delete h;
+        g_err = "host allocation failed";
+        return MGMC_ERR_OUT_OF_MEMORY;
+    }
+    return MGMC_OK;
+}
+
+mgmc_status mgmc_lrchol_destroy(mgmc_lrchol *s) {
+    API_BEGIN
+    if (!s) return MGMC_OK;
+    if (s->impl) {
+        cudaSetDevice(s->impl->device);
+        cudaStreamSynchronize(s->impl->stream);
+    }
+    delete s;
+    API_END
+}
+
+mgmc_status mgmc_lrchol_fix_rhs(mgmc_lrchol *s, const double *f, int on_device) {
+    API_BEGIN
+    LrChol &S = lrimpl(s);
+    if (!f) fail(MGMC_ERR_INVALID_ARGUMENT, "null f");
+    lr_put(S, f, on_device, S.f);
+    CK(cudaStreamSynchronize(S.stream));
+    S.rhs_set = true;
+    API_END
+}
+
+mgmc_status mgmc_lrchol_apply(mgmc_lrchol *s, const double *f, double *x, int on_device) {
+    API_BEGIN
+    LrChol &S = lrimpl(s);
+    if (!x) fail(MGMC_ERR_INVALID_ARGUMENT, "null x");
+    if (f) {
+        lr_put(S, f, on_device, S.f);
+        S.rhs_set = true;
+    } else if (!S.rhs_set) {
+        fail(MGMC_ERR_INVALID_ARGUMENT, "f is NULL but no right hand side has been set");
+    }
+    S.run();
+    CK(cudaMemcpyAsync(x, S.x, (size_t)S.n * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                       S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    API_END
+}
+
+mgmc_status mgmc_lrchol_inject_noise(mgmc_lrchol *s, const double *normals, int64_t count) {
+    API_BEGIN
+    LrChol &S = lrimpl(s);
+    if (S.noise != NOISE_INJECTED) fail(MGMC_ERR_INVALID_ARGUMENT, "the sampler draws Philox noise");
+    if (count < 0 || (count > 0 && !normals)) fail(MGMC_ERR_INVALID_ARGUMENT, "bad noise buffer");
+    // keep the unread tail, append the new normals
+    const i64 tail = S.noise_len - S.noise_pos;
+    std::vector<double> keep((size_t)tail);
+    if (tail > 0) CK(cudaMemcpy(keep.data(), S.noise_buf + S.noise_pos, (size_t)tail * sizeof(double), cudaMemcpyDeviceToHost));
+    const i64 need = tail + count;
+    if (need > S.noise_cap) {
+        if (S.noise_buf) {
+            cudaFree(S.noise_buf);
+            S.owned.erase(std::find(S.owned.begin(), S.owned.end(), (void *)S.noise_buf));
+        }
+        S.noise_buf = S.alloc<double>((size_t)need);
+        S.noise_cap = need;
+    }
+    if (tail > 0) CK(cudaMemcpy(S.noise_buf, keep.data(), (size_t)tail * sizeof(double), cudaMemcpyHostToDevice));
+    if (count > 0) CK(cudaMemcpy(S.noise_buf + tail, normals, (size_t)count * sizeof(double), cudaMemcpyHostToDevice));
+    S.noise_pos = 0;
+    S.noise_len = need;
+    API_END
+}
+
+mgmc_status mgmc_lrchol_stream(mgmc_lrchol *s, void **cuda_stream) {
+    API_BEGIN
+    LrChol &S = lrimpl(s);
+    if (!cuda_stream) fail(MGMC_ERR_INVALID_ARGUMENT, "null argument");
+    *cuda_stream = (void *)S.stream;
     API_END
 }
 

@@ -88,7 +88,7 @@ __device__ __forceinline__ T vweight(const StencilArg<T> &s, const VarField<T> &
 
 // ---------------------------------------------------------------- noise
 enum { NOISE_NONE = 0, NOISE_PHILOX = 1, NOISE_INJECTED = 2 };
-enum { PURPOSE_POINT = 0, PURPOSE_LOWRANK = 1, PURPOSE_COARSE = 2, PURPOSE_EXACT = 3 };
+enum { PURPOSE_POINT = 0, PURPOSE_LOWRANK = 1, PURPOSE_COARSE = 2, PURPOSE_EXACT = 3, PURPOSE_CHOLESKY = 4 };
 
 struct NoiseArgs {
     const double *buf;   // injected: normals for this consumer, index = vertex / column
@@ -1063,72 +1063,6 @@ __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tma(const __grid_
     resid_restrict_tile<T, NPT>(xs, fs, fc, xc, gf, gc, s, ca0, cb0, cc0);
 }
 
-// Persistent, double-buffered variant: a CTA walks the tiles
-// t = blockIdx.x, blockIdx.x + gridDim.x, ... (x fastest, as the one-shot
-// grid orders them); while it computes tile t from one pair of x / f
-// buffers, the bulk tensor copies of its next tile land in the other pair,
-// so the copy latency of every tile but the first is hidden.  Per tile the
-// arithmetic is k_resid_restrict_tma's (resid_restrict_tile).  Waits are
-// bounded as in k_resid_restrict_tma; on a timeout the CTA flags the error,
-// lets both buffers' copies land (bounded) and returns.
-template <typename T>
-__host__ __device__ constexpr size_t rr_pipe_stage_bytes() {
-    return (rr_tma_smem_bytes<T>() + 127) / 128 * 128;
-}
-
-template <typename T, int NPT>
-__global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tma_pipe(const __grid_constant__ CUtensorMap xmap,
-                                                                        const __grid_constant__ CUtensorMap fmap,
-                                                                        T *__restrict__ fc, T *__restrict__ xc,
-                                                                        Grid3 gf, Grid3 gc, StencilArg<T> s,
-                                                                        unsigned *__restrict__ err, int ntx, int nty,
-                                                                        int ntiles) {
-    if (gf.pdl) pdl_begin();
-    extern __shared__ __align__(1024) unsigned char rr_pipe_smem[];
-    __shared__ unsigned long long bar[2];
-    constexpr size_t SB = rr_pipe_stage_bytes<T>();
-    auto xs = [&](int st) { return reinterpret_cast<T *>(rr_pipe_smem + (size_t)st * SB); };
-    auto fs = [&](int st) { return reinterpret_cast<T *>(rr_pipe_smem + (size_t)st * SB + rr_tma_xbytes<T>()); };
-    if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-    }
-    __syncthreads();
-    auto issue = [&](int t, int st) {
-        const int bx = t % ntx, by = (t / ntx) % nty, bz = t / (ntx * nty);
-        const int fa0 = 2 * bx * RR_TX, fb0 = 2 * by * RR_TY, fz0 = 2 * bz * RR_TZ;
-        mbar_expect_tx(&bar[st], (unsigned)(sizeof(T) * RR_BW * (RR_XH * RR_XD + RR_FH * RR_FD)));
-        tma_load_3d(xs(st), &xmap, fa0, fb0, fz0, &bar[st]);
-        tma_load_3d(fs(st), &fmap, fa0, fb0 + 1, fz0 + 1, &bar[st]);
-    };
-    if (threadIdx.x == 0 && (int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
-    int it = 0;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
-        const int st = it & 1;
-        const int tn = t + gridDim.x;
-        if (threadIdx.x == 0 && tn < ntiles) {
-            // the other pair of buffers was last read and written by this CTA's
-            // threads (generic proxy) before the __syncthreads closing the
-            // previous iteration; order those accesses before the copies
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(tn, st ^ 1);
-        }
-        const bool ok = mbar_wait_bounded(&bar[st], (unsigned)((it >> 1) & 1), TILE_WAIT_NS);
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) {
-                atomicOr(err, ERR_TILE_TIMEOUT);
-                mbar_wait_bounded(&bar[st], (unsigned)((it >> 1) & 1), TILE_WAIT_NS);
-                if (tn < ntiles) mbar_wait_bounded(&bar[st ^ 1], (unsigned)(((it + 1) >> 1) & 1), TILE_WAIT_NS);
-            }
-            __syncthreads();
-            return;
-        }
-        const int bx = t % ntx, by = (t / ntx) % nty, bz = t / (ntx * nty);
-        resid_restrict_tile<T, NPT>(xs(st), fs(st), fc, xc, gf, gc, s, bx * RR_TX, by * RR_TY, bz * RR_TZ);
-        __syncthreads();
-    }
-}
-
 // dst[row] += sign * sum_e B_e y_{col_e} / Sigma_{col_e} over the rows of B
 // (row-compressed): the B Sigma^{-1} B^T x part of A x.
 template <typename T>
@@ -1907,6 +1841,81 @@ __global__ void __launch_bounds__(256) k_step_end(const T *__restrict__ x, int n
     pdl_begin();
     step_end_body<T>(x, nprobe, bptr, bidx, bval, obs, capacity, obs_count, d_step, err, done, blockIdx.x, gridDim.x);
 }
+
+// ------------------------------------------- low-rank Cholesky sampler
+// The sampler's solves with the block factor of A_0 and its low-rank
+// products are dense FP64 matrix-vector products of three kinds.
+
+// y_i = yadd_i + alpha sum_j A_ij v_j over a row-major rows x cols block
+// (leading dimension lda): one warp per row, lanes over the columns, a
+// warp-shuffle sum.  LOWER: the block is lower triangular (columns j <= i).
+// y may alias yadd (each row reads its own entry before writing it).
+template <bool LOWER>
+__global__ void __launch_bounds__(256) k_dgemv_rows(const double *__restrict__ A, i64 rows, i64 cols, i64 lda,
+                                                    const double *__restrict__ v, const double *yadd, double alpha,
+                                                    double *y) {
+    const i64 i = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= rows) return;
+    const i64 jmax = LOWER ? min(i + 1, cols) : cols;
+    const double *Ai = A + i * lda;
+    double a0 = 0.0, a1 = 0.0;
+    i64 j = lane;
+    for (; j + 32 < jmax; j += 64) {
+        a0 = fma(Ai[j], v[j], a0);
+        a1 = fma(Ai[j + 32], v[j + 32], a1);
+    }
+    if (j < jmax) a0 = fma(Ai[j], v[j], a0);
+    double acc = a0 + a1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[i] = (yadd ? yadd[i] : 0.0) + alpha * acc;
+}
+
+// Partial sums of (A^T v)_j over row chunk blockIdx.y (rows [c rch,
+// (c + 1) rch)): part[c cols + j], one thread per column (coalesced row
+// reads).  LOWER: A is lower triangular, rows i >= j only.
+template <bool LOWER>
+__global__ void __launch_bounds__(256) k_dgemv_cols_partial(const double *__restrict__ A, i64 rows, i64 cols, i64 lda,
+                                                            const double *__restrict__ v, int rch,
+                                                            double *__restrict__ part) {
+    const i64 j = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (j >= cols) return;
+    i64 i0 = (i64)c * rch;
+    const i64 i1 = min(rows, i0 + rch);
+    if (LOWER && i0 < j) i0 = j;
+    double acc = 0.0;
+    for (i64 i = i0; i < i1; ++i) acc = fma(A[i * lda + j], v[i], acc);
+    part[(i64)c * cols + j] = acc;
+}
+
+// y_j = yadd_j + alpha sum_c part[c cols + j], chunks in order (the result
+// does not depend on block timing).  y may alias yadd.
+__global__ void __launch_bounds__(256) k_dgemv_cols_finish(const double *__restrict__ part, int nch, i64 cols,
+                                                           const double *yadd, double alpha, double *y) {
+    const i64 j = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= cols) return;
+    double acc = 0.0;
+    for (int c = 0; c < nch; ++c) acc += part[(i64)c * cols + j];
+    y[j] = (yadd ? yadd[j] : 0.0) + alpha * acc;
+}
+
+// xi_i ~ N(0, 1): Philox (counter: vertex group i / 4, purpose
+// PURPOSE_CHOLESKY, the sampler's step counter) or the injected normals
+template <int NOISE>
+__global__ void __launch_bounds__(256) k_cholesky_normals(NoiseArgs nz, i64 n, double *__restrict__ xi) {
+    const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (NOISE == NOISE_INJECTED) {
+        xi[i] = nz.buf[i];
+    } else {
+        const float4 r = normals4(philox4x32_10(noise_ctr(nz, (unsigned)(i >> 2), PURPOSE_CHOLESKY, 0), noise_key(nz)));
+        xi[i] = (double)pick(r, (int)(i & 3));
+    }
+}
+
+__global__ void k_counter_advance(u64 *__restrict__ step) { *step += 1ull; }
 
 // ------------------------------------------------------- batched chains
 // Chains of one lattice geometry stepped together (FP32-mixed chains with

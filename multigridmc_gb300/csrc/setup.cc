@@ -629,4 +629,180 @@ std::vector<double> small_inverse(const std::vector<double> &S, int m) {
     return inv;
 }
 
+// ----------------------------------------------------- low-rank Cholesky
+bool lowrank_cholesky_factors(const Geometry &g, const double st[27], const SparseCols &B,
+                              const std::vector<double> &Sigma, LowRankCholeskyFactors &F) {
+    const int dim = g.dim;
+    const int64_t n = g.n;
+    const int nb = g.N[dim - 1];
+    const int64_t p = n / nb;
+    F.nb = nb;
+    F.p = p;
+    F.m = B.m;
+    // in-block coordinates: (a, b) in 3D, (a) in 2D, none in 1D; the block
+    // offset runs along direction dim - 1
+    const int n0 = dim >= 2 ? g.N[0] : 1, n1 = dim == 3 ? g.N[1] : 1;
+    auto coupling = [&](int64_t i, int64_t j, int off) {
+        const int ai = (int)(i % n0), bi = (int)(i / n0), aj = (int)(j % n0), bj = (int)(j / n0);
+        const int da = aj - ai, db = bj - bi;
+        if (da < -1 || da > 1 || db < -1 || db > 1) return 0.0;
+        if (dim == 3) return st[sidx(da, db, off)];
+        if (dim == 2) return st[sidx(da, off, 0)];
+        return st[sidx(off, 0, 0)];
+    };
+    std::vector<double> Ain((size_t)(p * p), 0.0), Aoff((size_t)(p * p), 0.0);
+    for (int64_t i = 0; i < p; ++i)
+        for (int64_t j = 0; j < p; ++j) {
+            Ain[i * p + j] = coupling(i, j, 0);
+            Aoff[i * p + j] = coupling(i, j, -1);  // row in block k, column in block k - 1
+        }
+    (void)n1;
+    F.D.assign((size_t)(nb * p * p), 0.0);
+    F.O.assign((size_t)(nb * p * p), 0.0);
+    std::vector<double> S = Ain;
+    for (int k = 0; k < nb; ++k) {
+        std::vector<double> Lk = S;
+        if (!dense_cholesky(Lk, p)) return false;
+        const std::vector<double> T = inverse_factor_transposed(Lk, p);  // (L_kk^{-1})^T
+        double *Dk = &F.D[(size_t)k * p * p];
+#pragma omp parallel for schedule(static) if (p > 256)
+        for (int64_t i = 0; i < p; ++i)
+            for (int64_t j = 0; j <= i; ++j) Dk[i * p + j] = T[j * p + i];
+        if (k + 1 == nb) break;
+        double *Ok = &F.O[(size_t)(k + 1) * p * p];
+        // L_{k+1,k} = A_{k+1,k} L_kk^{-T}: row i gathers the (few) coupled rows of T
+#pragma omp parallel for schedule(static) if (p > 256)
+        for (int64_t i = 0; i < p; ++i)
+            for (int64_t l = 0; l < p; ++l) {
+                const double a = Aoff[i * p + l];
+                if (a == 0.0) continue;
+                const double *Tl = &T[l * p];
+                for (int64_t j = 0; j < p; ++j) Ok[i * p + j] += a * Tl[j];
+            }
+        // S_{k+1} = A_{k+1,k+1} - L_{k+1,k} L_{k+1,k}^T (lower half, mirrored)
+#pragma omp parallel for schedule(dynamic, 16) if (p > 256)
+        for (int64_t i = 0; i < p; ++i) {
+            const double *Oi = &Ok[i * p];
+            for (int64_t j = 0; j <= i; ++j) {
+                const double *Oj = &Ok[j * p];
+                double d = 0.0;
+                for (int64_t l = 0; l < p; ++l) d += Oi[l] * Oj[l];
+                S[i * p + j] = Ain[i * p + j] - d;
+            }
+        }
+        for (int64_t i = 0; i < p; ++i)
+            for (int64_t j = i + 1; j < p; ++j) S[i * p + j] = S[j * p + i];
+    }
+    const int m = B.m;
+    if (m == 0) return true;
+    // V = L^{-1} B block by block: Y_k = D_k (B_k - O_k Y_{k-1}), n x m row-major
+    std::vector<double> V((size_t)(n * m), 0.0), Bk((size_t)(p * m));
+    for (int j = 0; j < m; ++j)
+        for (int64_t e = B.ptr[j]; e < B.ptr[j + 1]; ++e) V[B.row[e] * m + j] = B.val[e];  // B first, in place
+    for (int k = 0; k < nb; ++k) {
+        double *Yk = &V[(size_t)k * p * m];
+        std::copy(Yk, Yk + p * m, Bk.begin());
+        if (k > 0) {
+            const double *Ok = &F.O[(size_t)k * p * p];
+            const double *Yp = &V[(size_t)(k - 1) * p * m];
+#pragma omp parallel for schedule(static) if (p > 256)
+            for (int64_t i = 0; i < p; ++i)
+                for (int64_t l = 0; l < p; ++l) {
+                    const double o = Ok[i * p + l];
+                    if (o == 0.0) continue;
+                    for (int c = 0; c < m; ++c) Bk[i * m + c] -= o * Yp[l * m + c];
+                }
+        }
+        const double *Dk = &F.D[(size_t)k * p * p];
+#pragma omp parallel for schedule(static) if (p > 256)
+        for (int64_t i = 0; i < p; ++i) {
+            for (int c = 0; c < m; ++c) {
+                double d = 0.0;
+                for (int64_t l = 0; l <= i; ++l) d += Dk[i * p + l] * Bk[l * m + c];
+                Yk[i * m + c] = d;
+            }
+        }
+    }
+    // Householder QR of V; Q explicit (n x m), R (m x m) with a positive diagonal
+    std::vector<double> A = V, tau(m, 0.0), R((size_t)m * m, 0.0);
+    std::vector<std::vector<double>> refl(m);
+    for (int k = 0; k < m; ++k) {
+        double nrm = 0.0;
+        for (int64_t i = k; i < n; ++i) nrm += A[i * m + k] * A[i * m + k];
+        nrm = std::sqrt(nrm);
+        const double a0 = A[(int64_t)k * m + k];
+        const double alpha = a0 >= 0.0 ? -nrm : nrm;
+        std::vector<double> v((size_t)n, 0.0);
+        for (int64_t i = k; i < n; ++i) v[i] = A[i * m + k];
+        v[k] = a0 - alpha;
+        double vv = 0.0;
+        for (int64_t i = k; i < n; ++i) vv += v[i] * v[i];
+        if (vv > 0.0) {
+            for (int c = k; c < m; ++c) {
+                double d = 0.0;
+                for (int64_t i = k; i < n; ++i) d += v[i] * A[i * m + c];
+                const double sc = 2.0 * d / vv;
+                for (int64_t i = k; i < n; ++i) A[i * m + c] -= sc * v[i];
+            }
+            tau[k] = 2.0 / vv;
+        }
+        refl[k] = std::move(v);
+    }
+    for (int i = 0; i < m; ++i)
+        for (int c = i; c < m; ++c) R[(size_t)i * m + c] = A[(int64_t)i * m + c];
+    F.Q.assign((size_t)(n * m), 0.0);
+    for (int c = 0; c < m; ++c) F.Q[(size_t)c * m + c] = 1.0;
+    for (int k = m - 1; k >= 0; --k) {
+        const std::vector<double> &v = refl[k];
+        for (int c = 0; c < m; ++c) {
+            double d = 0.0;
+            for (int64_t i = k; i < n; ++i) d += v[i] * F.Q[i * m + c];
+            const double sc = tau[k] * d;
+            for (int64_t i = k; i < n; ++i) F.Q[i * m + c] -= sc * v[i];
+        }
+    }
+    for (int c = 0; c < m; ++c)
+        if (R[(size_t)c * m + c] < 0.0) {
+            for (int cc = 0; cc < m; ++cc) R[(size_t)c * m + cc] = -R[(size_t)c * m + cc];
+            for (int64_t i = 0; i < n; ++i) F.Q[i * m + c] = -F.Q[i * m + c];
+        }
+    // Id - Lambda = Id - R (Sigma + V^T V)^{-1} R^T and its lower factor W
+    std::vector<double> Sm((size_t)m * m, 0.0);
+    for (int a = 0; a < m; ++a)
+        for (int c = 0; c < m; ++c) {
+            double d = 0.0;
+            for (int64_t i = 0; i < n; ++i) d += V[i * m + a] * V[i * m + c];
+            Sm[(size_t)a * m + c] = d + (a == c ? Sigma[a] : 0.0);
+        }
+    const std::vector<double> Si = small_inverse(Sm, m);
+    std::vector<double> RSi((size_t)m * m, 0.0), W((size_t)m * m, 0.0);
+    for (int a = 0; a < m; ++a)
+        for (int c = 0; c < m; ++c) {
+            double d = 0.0;
+            for (int k = 0; k < m; ++k) d += R[(size_t)a * m + k] * Si[(size_t)k * m + c];
+            RSi[(size_t)a * m + c] = d;
+        }
+    for (int a = 0; a < m; ++a)
+        for (int c = 0; c < m; ++c) {
+            double d = 0.0;
+            for (int k = 0; k < m; ++k) d += RSi[(size_t)a * m + k] * R[(size_t)c * m + k];
+            W[(size_t)a * m + c] = (a == c ? 1.0 : 0.0) - d;
+        }
+    if (!dense_cholesky(W, m)) return false;
+    F.QW.assign((size_t)(n * m), 0.0);
+    F.QWT.assign((size_t)(n * m), 0.0);
+#pragma omp parallel for schedule(static) if (n > 4096)
+    for (int64_t i = 0; i < n; ++i)
+        for (int c = 0; c < m; ++c) {
+            double u = 0.0, l = 0.0;
+            for (int k = 0; k < m; ++k) {
+                u += F.Q[i * m + k] * (W[(size_t)c * m + k] - (k == c ? 1.0 : 0.0));  // (W^T - Id)[k][c]
+                l += F.Q[i * m + k] * (W[(size_t)k * m + c] - (k == c ? 1.0 : 0.0));  // (W - Id)[k][c]
+            }
+            F.QW[i * m + c] = u;
+            F.QWT[i * m + c] = l;
+        }
+    return true;
+}
+
 }  // namespace mgmc

@@ -97,4 +97,25 @@ std::vector<double> inverse_factor_times(const std::vector<double> &T, int64_t n
 // inverse of a small dense matrix by LU with partial pivoting
 std::vector<double> small_inverse(const std::vector<double> &S, int m);
 
+// LowRankCholeskySampler (cholesky_sampler.cc:41-96) set-up.  A_0 (constant
+// stencil, Dirichlet) is block tridiagonal in the vertex order, with blocks
+// of p = n / nb vertices along the last lattice direction (planes in 3D, rows
+// in 2D, single vertices in 1D), so its Cholesky factor L has diagonal
+// blocks L_kk and sub-diagonal blocks L_{k,k-1}:
+//   S_0 = A_00,  L_kk L_kk^T = S_k,  L_{k+1,k} = A_{k+1,k} L_kk^{-T},
+//   S_{k+1} = A_{k+1,k+1} - L_{k+1,k} L_{k+1,k}^T.
+// D holds the blocks L_kk^{-1} and O the blocks L_{k,k-1} (block 0 zero),
+// row-major p x p each.  With measurements, V = L^{-1} B has the thin QR
+// V = Q R (R with a positive diagonal), W is the lower Cholesky factor of
+// Id - R (Sigma + V^T V)^{-1} R^T, and QW = Q (W^T - Id), QWT = Q (W - Id),
+// n x m row-major.
+struct LowRankCholeskyFactors {
+    int nb = 0, m = 0;
+    int64_t p = 0;
+    std::vector<double> D, O, Q, QW, QWT;
+};
+// false if A_0 or Id - Lambda is not positive definite
+bool lowrank_cholesky_factors(const Geometry &g, const double st[27], const SparseCols &B,
+                              const std::vector<double> &Sigma, LowRankCholeskyFactors &F);
+
 }  // namespace mgmc

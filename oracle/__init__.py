@@ -76,6 +76,7 @@ def lib():
         "orc_sor_sampler": (_P, [_P, _P, C.c_double, C.c_int, C.c_int, C.c_int]),
         "orc_ssor_sampler": (_P, [_P, _P, C.c_double, C.c_int, C.c_int]),
         "orc_cholesky_sampler": (_P, [_P, _P]),
+        "orc_lowrank_cholesky_sampler": (_P, [_P, _P]),
         "orc_mgmc_sampler": (_P, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                   C.c_double, C.c_int, C.c_double, C.c_int]),
         "orc_sampler_destroy": (None, [_P]),
@@ -413,6 +414,12 @@ def ssor_sampler(op, source, omega, nsmooth=1, ordering=0):
 
 def cholesky_sampler(op, source):
     return Sampler(lib().orc_cholesky_sampler(op.h, source.h), op, source)
+
+
+def lowrank_cholesky_sampler(op, source):
+    """LowRankCholeskySampler (cholesky_sampler.cc:41-129) with the dense
+    natural-order factor of the sparse part."""
+    return Sampler(lib().orc_lowrank_cholesky_sampler(op.h, source.h), op, source)
 
 
 def mgmc_sampler(op, source, nlevel, smoother="SSOR", coarse_solver="Cholesky", npresmooth=1,

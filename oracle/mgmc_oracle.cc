@@ -1087,6 +1087,162 @@ struct CholeskySampler : Sampler {
     }
 };
 
+// cholesky_sampler.cc:41-129 (LowRankCholeskySampler): the sparse part A_0 is
+// factored (here by the dense natural-order LL^T), the low-rank term enters
+// through V = L^{-1} B, its thin QR V = QR (Householder, R with a positive
+// diagonal: the sampler does not depend on the signs of Q's columns), the
+// m x m matrix Id - Lambda = Id - R (Sigma + V^T V)^{-1} R^T and its lower
+// Cholesky factor W, with Q_W = Q (W^T - Id), Q_W_T = Q (W - Id).  A sample
+// draws n normals xi, forms g = L^{-1} f, g += Q_W (Q^T g), xi += g,
+// xi += Q_W_T (Q^T xi) and solves L^T x = xi.
+struct LowRankCholeskySampler : Sampler {
+    std::shared_ptr<LinOp> op;
+    NormalSource *rng;
+    int64_t n;
+    int m;
+    std::vector<double> L, Q, QW, QWT, xi, g, t;  // L n x n row-major; Q, QW, QWT n x m row-major
+    bool ok = true;
+    LowRankCholeskySampler(std::shared_ptr<LinOp> op_, NormalSource *rng_) : op(op_), rng(rng_) {
+        n = op->n();
+        m = op->m();
+        L.assign(n * n, 0.0);
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t k = op->A.ptr[i]; k < op->A.ptr[i + 1]; ++k) L[i * n + op->A.col[k]] = op->A.val[k];
+        ok = dense_cholesky(L, n);
+        xi.resize(n);
+        g.resize(n);
+        t.resize(std::max(m, 1));
+        if (!ok || m == 0) return;
+        // V = L^{-1} B, column by column (forward substitution)
+        std::vector<double> V(n * m, 0.0), b(n);
+        for (int j = 0; j < m; ++j) {
+            std::fill(b.begin(), b.end(), 0.0);
+            for (int64_t e = op->B.ptr[j]; e < op->B.ptr[j + 1]; ++e) b[op->B.row[e]] = op->B.val[e];
+            for (int64_t i = 0; i < n; ++i) {
+                double s = b[i];
+                for (int64_t k = 0; k < i; ++k) s -= L[i * n + k] * V[k * m + j];
+                V[i * m + j] = s / L[i * n + i];
+            }
+        }
+        // Householder QR of V (n x m): reflectors applied to a copy, R from
+        // the reduced matrix, Q from the reflectors applied to Id(n x m)
+        std::vector<double> A = V, tau(m, 0.0), vk(n);
+        std::vector<std::vector<double>> refl(m);
+        for (int k = 0; k < m; ++k) {
+            double nrm = 0.0;
+            for (int64_t i = k; i < n; ++i) nrm += A[i * m + k] * A[i * m + k];
+            nrm = sqrt(nrm);
+            const double a0 = A[k * m + k];
+            const double alpha = a0 >= 0.0 ? -nrm : nrm;
+            std::vector<double> v(n, 0.0);
+            for (int64_t i = k; i < n; ++i) v[i] = A[i * m + k];
+            v[k] = a0 - alpha;
+            double vv = 0.0;
+            for (int64_t i = k; i < n; ++i) vv += v[i] * v[i];
+            if (vv > 0.0) {
+                for (int c = k; c < m; ++c) {
+                    double d = 0.0;
+                    for (int64_t i = k; i < n; ++i) d += v[i] * A[i * m + c];
+                    const double sc = 2.0 * d / vv;
+                    for (int64_t i = k; i < n; ++i) A[i * m + c] -= sc * v[i];
+                }
+                tau[k] = 2.0 / vv;
+            }
+            refl[k] = v;
+        }
+        std::vector<double> R(m * m, 0.0);
+        for (int i = 0; i < m; ++i)
+            for (int c = i; c < m; ++c) R[i * m + c] = A[i * m + c];
+        Q.assign(n * m, 0.0);
+        for (int c = 0; c < m; ++c) Q[c * m + c] = 1.0;
+        for (int k = m - 1; k >= 0; --k) {
+            const std::vector<double> &v = refl[k];
+            for (int c = 0; c < m; ++c) {
+                double d = 0.0;
+                for (int64_t i = k; i < n; ++i) d += v[i] * Q[i * m + c];
+                const double sc = tau[k] * d;
+                for (int64_t i = k; i < n; ++i) Q[i * m + c] -= sc * v[i];
+            }
+        }
+        // signs: a positive diagonal of R (column c of Q and row c of R flip together)
+        for (int c = 0; c < m; ++c)
+            if (R[c * m + c] < 0.0) {
+                for (int cc = 0; cc < m; ++cc) R[c * m + cc] = -R[c * m + cc];
+                for (int64_t i = 0; i < n; ++i) Q[i * m + c] = -Q[i * m + c];
+            }
+        // Id - Lambda = Id - R (Sigma + V^T V)^{-1} R^T
+        std::vector<double> S(m * m, 0.0);
+        for (int a = 0; a < m; ++a)
+            for (int c = 0; c < m; ++c) {
+                double d = 0.0;
+                for (int64_t i = 0; i < n; ++i) d += V[i * m + a] * V[i * m + c];
+                S[a * m + c] = d + (a == c ? op->Sigma[a] : 0.0);
+            }
+        const std::vector<double> Si = dense_inverse(S, m);
+        std::vector<double> RSi(m * m, 0.0), W(m * m, 0.0);
+        for (int a = 0; a < m; ++a)
+            for (int c = 0; c < m; ++c) {
+                double d = 0.0;
+                for (int k = 0; k < m; ++k) d += R[a * m + k] * Si[k * m + c];
+                RSi[a * m + c] = d;
+            }
+        for (int a = 0; a < m; ++a)
+            for (int c = 0; c < m; ++c) {
+                double d = 0.0;
+                for (int k = 0; k < m; ++k) d += RSi[a * m + k] * R[c * m + k];
+                W[a * m + c] = (a == c ? 1.0 : 0.0) - d;
+            }
+        if (!dense_cholesky(W, m)) {
+            ok = false;
+            return;
+        }
+        // Q_W = Q (W^T - Id), Q_W_T = Q (W - Id)
+        QW.assign(n * m, 0.0);
+        QWT.assign(n * m, 0.0);
+        for (int64_t i = 0; i < n; ++i)
+            for (int c = 0; c < m; ++c) {
+                double u = 0.0, l = 0.0;
+                for (int k = 0; k < m; ++k) {
+                    const double wt = W[c * m + k] - (k == c ? 1.0 : 0.0);  // (W^T - Id)[k][c] = W[c][k] - d
+                    const double w = W[k * m + c] - (k == c ? 1.0 : 0.0);   // (W - Id)[k][c]
+                    u += Q[i * m + k] * wt;
+                    l += Q[i * m + k] * w;
+                }
+                QW[i * m + c] = u;
+                QWT[i * m + c] = l;
+            }
+    }
+    // y += Qx (Q^T v)
+    void lowrank_update(const std::vector<double> &Qx, const std::vector<double> &v, std::vector<double> &y) {
+        for (int c = 0; c < m; ++c) {
+            double d = 0.0;
+            for (int64_t i = 0; i < n; ++i) d += Q[i * m + c] * v[i];
+            t[c] = d;
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            double d = 0.0;
+            for (int c = 0; c < m; ++c) d += Qx[i * m + c] * t[c];
+            y[i] += d;
+        }
+    }
+    void apply(const double *f, double *x) override {
+        for (int64_t ell = 0; ell < n; ++ell) xi[ell] = rng->draw_normal();
+        for (int64_t i = 0; i < n; ++i) {  // L g = f
+            double s = f[i];
+            for (int64_t k = 0; k < i; ++k) s -= L[i * n + k] * g[k];
+            g[i] = s / L[i * n + i];
+        }
+        if (m > 0) lowrank_update(QW, g, g);
+        for (int64_t i = 0; i < n; ++i) xi[i] += g[i];
+        if (m > 0) lowrank_update(QWT, xi, xi);
+        for (int64_t i = n - 1; i >= 0; --i) {  // L^T x = xi
+            double s = xi[i];
+            for (int64_t k = n - 1; k > i; --k) s -= L[k * n + i] * x[k];
+            x[i] = s / L[i * n + i];
+        }
+    }
+};
+
 struct MGParams {
     int nlevel;
     int smoother;       // 0 = SOR, 1 = SSOR
@@ -1685,6 +1841,14 @@ orc_sampler *orc_ssor_sampler(orc_op *o, NormalSource *src, double omega, int ns
 }
 orc_sampler *orc_cholesky_sampler(orc_op *o, NormalSource *src) {
     auto *c = new CholeskySampler(o->op, src);
+    if (!c->ok) {
+        delete c;
+        return nullptr;
+    }
+    return new orc_sampler{std::unique_ptr<Sampler>(c)};
+}
+orc_sampler *orc_lowrank_cholesky_sampler(orc_op *o, NormalSource *src) {
+    auto *c = new LowRankCholeskySampler(o->op, src);
     if (!c->ok) {
         delete c;
         return nullptr;
