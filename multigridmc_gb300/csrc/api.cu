@@ -315,7 +315,10 @@ NoiseArgs Sampler::noise_args(int lev, i64 count) {
 // dependent kernels of a multigrid step.
 constexpr i64 PDL_MAX_POINTS = i64(1) << 22;
 // supports of C up to this many rows take the fused solve + correction
-constexpr i64 LR_FUSE_MAX_ROWS = i64(1) << 16;
+#ifndef MGMC_LR_FUSE_MAX_ROWS
+#define MGMC_LR_FUSE_MAX_ROWS (1ll << 16)
+#endif
+constexpr i64 LR_FUSE_MAX_ROWS = MGMC_LR_FUSE_MAX_ROWS;
 
 template <typename... KArgs, typename... Args>
 static void plaunch(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,

@@ -570,20 +570,22 @@ __device__ __forceinline__ void bt_partial_cta(const T *__restrict__ x, const Lo
     const i64 len = (e1 - e0 + P - 1) / P;
     const i64 lo = e0 + p * len, hi = min(e1, lo + len);
     T tacc = T(0);
-    for (i64 e = lo + threadIdx.x; e < hi; e += 4 * 256) {
-        i64 idx[4];
-        T val[4];
+    // eight index/value loads, then the eight gathers, in flight at once;
+    // the products are added in entry order
+    for (i64 e = lo + threadIdx.x; e < hi; e += 8 * 256) {
+        i64 idx[8];
+        T val[8];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < 8; ++k) {
             const i64 ee = e + 256 * k;
             idx[k] = ee < hi ? lr.Bidx[ee] : -1;
             val[k] = ee < hi ? (sizeof(T) == 4 ? (T)lr.Bvalf[ee] : (T)lr.Bval[ee]) : T(0);
         }
-        T xv[4];
+        T xv[8];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) xv[k] = idx[k] >= 0 ? x[idx[k]] : T(0);
+        for (int k = 0; k < 8; ++k) xv[k] = idx[k] >= 0 ? x[idx[k]] : T(0);
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
+        for (int k = 0; k < 8; ++k)
             if (idx[k] >= 0) tacc += val[k] * xv[k];
     }
     const double acc = block_sum<256>((double)tacc, sh);
@@ -620,6 +622,16 @@ __device__ __forceinline__ void lr_solve_cta(const LowRankArg &lr, int P, const 
     // rows handled at once and threads per row (blockDim.x = 256)
     const int rows = m < 256 ? m : 256;
     const int tpr = 256 / rows;
+    const int g = threadIdx.x / rows, kk = threadIdx.x % rows;
+    // m <= 64: each thread's slice of S^{-1} (at most 16 values) is loaded
+    // here, while the partial sums below are read, instead of after them
+    const int cnt = g < tpr ? (m - g + tpr - 1) / tpr : 0;
+    const bool pre = SOLVE && m <= 64;
+    double pv[16];
+    if (pre) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) pv[i] = i < cnt ? __ldg(lr.SinvT + (i64)(g + i * tpr) * m + kk) : 0.0;
+    }
     for (int k = threadIdx.x; k < m; k += blockDim.x) {
         double pv[8];
         double t = 0.0;
@@ -646,7 +658,38 @@ __device__ __forceinline__ void lr_solve_cta(const LowRankArg &lr, int P, const 
     // z = S^{-1} u: thread (g, k) of g < tpr sums the columns q = g, g + tpr, ...
     // of row k (loads of one column contiguous over k), in batches of 8
     // loads issued together; the tpr partial sums are then added in order g.
-    const int g = threadIdx.x / rows, kk = threadIdx.x % rows;
+    if (pre) {  // the same sums from the preloaded slice (one batch of rows: m <= 64)
+        double t0 = 0.0, t1 = 0.0;
+        if (g < tpr) {
+#pragma unroll
+            for (int i0 = 0; i0 < 16; i0 += 8) {
+                if (i0 + 7 < cnt) {
+#pragma unroll
+                    for (int r = 0; r < 8; r += 2) {
+                        t0 = fma(pv[i0 + r], u[g + (i0 + r) * tpr], t0);
+                        t1 = fma(pv[i0 + r + 1], u[g + (i0 + r + 1) * tpr], t1);
+                    }
+                } else {
+#pragma unroll
+                    for (int r = 0; r < 8; ++r)
+                        if (i0 + r < cnt) t0 = fma(pv[i0 + r], u[g + (i0 + r) * tpr], t0);
+                }
+            }
+            acc[g * rows + kk] = t0 + t1;
+        }
+        __syncthreads();
+        if (threadIdx.x < rows) {
+            double zk = 0.0;
+            for (int h = 0; h < tpr; ++h) zk += acc[h * rows + threadIdx.x];
+            if (zs) zs[threadIdx.x] = zk;
+            if (publish) {
+                lr.z[threadIdx.x] = zk;
+                if (lr.zf) lr.zf[threadIdx.x] = (float)zk;
+            }
+        }
+        __syncthreads();
+        return;
+    }
     for (int k0 = 0; k0 < m; k0 += rows) {
         const int k = k0 + kk;
         double t0 = 0.0, t1 = 0.0;
@@ -720,49 +763,79 @@ template <typename T, int NOISE>
 __global__ void __launch_bounds__(256) k_lr_apply(T *__restrict__ x, LowRankArg lr, int P, NoiseArgs nz, i64 nrows,
                                                   const i64 *__restrict__ rows, const i64 *__restrict__ ptr,
                                                   const int *__restrict__ col, const T *__restrict__ val) {
+    // a thread's first four rows (indices, entry ranges, first entries and
+    // state) do not depend on the partial sums the kernel before writes:
+    // loaded before the wait, the state through L2 (see k_lr_scatter)
+    const i64 stride = (i64)gridDim.x * blockDim.x;
+    i64 r0 = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    i64 rr[4], e0[4], e1[4];
+    int c0[4];
+    T v0[4], xv[4];
+    auto load = [&](bool before_wait) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const i64 r = r0 + j * stride;
+            const bool ok = r < nrows;
+            rr[j] = ok ? rows[r] : -1;
+            e0[j] = ok ? ptr[r] : 0;
+            e1[j] = ok ? ptr[r + 1] : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const bool has = e0[j] < e1[j];
+            c0[j] = has ? col[e0[j]] : 0;
+            v0[j] = has ? val[e0[j]] : T(0);
+            xv[j] = rr[j] >= 0 ? (before_wait ? __ldcg(x + rr[j]) : x[rr[j]]) : T(0);
+        }
+    };
+    if (r0 < nrows) load(true);
     pdl_begin();
     extern __shared__ double dyn[];
     const int m = lr.m;
     double *zs = dyn, *u = dyn + m, *acc = dyn + 2 * m;
     lr_solve_cta<NOISE, true>(lr, P, nz, u, acc, zs, blockIdx.x == 0);
     // zs is complete after the last __syncthreads of lr_solve_cta
-    const i64 stride = (i64)gridDim.x * blockDim.x;
-    for (i64 r0 = (i64)blockIdx.x * blockDim.x + threadIdx.x; r0 < nrows; r0 += 4 * stride) {
-        i64 rr[4], e0[4], e1[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const i64 r = r0 + j * stride;
-            const bool ok = r < nrows;
-            rr[j] = ok ? rows[r] : -1;
-            e0[j] = ok ? ptr[r] : 0;
-            e1[j] = ok ? ptr[r + 1] : 0;
-        }
+    for (; r0 < nrows; r0 += 4 * stride) {
         T accv[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             accv[j] = T(0);
-            for (i64 e = e0[j]; e < e1[j]; ++e) accv[j] += val[e] * (T)zs[col[e]];
+            if (e0[j] < e1[j]) {
+                accv[j] += v0[j] * (T)zs[c0[j]];
+                for (i64 e = e0[j] + 1; e < e1[j]; ++e) accv[j] += val[e] * (T)zs[col[e]];
+            }
         }
-        T xv[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) xv[j] = rr[j] >= 0 ? x[rr[j]] : T(0);
 #pragma unroll
         for (int j = 0; j < 4; ++j)
             if (rr[j] >= 0) x[rr[j]] = xv[j] + accv[j];
+        if (r0 + 4 * stride < nrows) {
+            r0 += 4 * stride;
+            load(false);
+            r0 -= 4 * stride;
+        }
     }
 }
 
 // x[row] += sum_e C_e z_{col_e} over the support rows of C = M^{-1} B, with
 // the coefficients z of k_lr_solve (ZT = float: the FP32 chain's rounded
 // copy), four rows per thread and iteration with their loads issued together.
+// Only z comes from the kernel just before (k_bt_solve); the row indices,
+// entry ranges, first entries and the state of a thread's first four rows
+// do not, so they are loaded before the wait for that kernel.  The state was
+// written by a kernel before k_bt_solve, which had completed when every CTA
+// of k_bt_solve passed its own wait, i.e. before this grid started; it is
+// read through L2 (ld.global.cg), the level at which those writes are
+// visible.
 template <typename T, typename ZT>
 __global__ void __launch_bounds__(256) k_lr_scatter(T *__restrict__ x, i64 nrows, const i64 *__restrict__ rows,
                                                      const i64 *__restrict__ ptr, const int *__restrict__ col,
                                                      const T *__restrict__ val, const ZT *__restrict__ z) {
-    pdl_begin();
     const i64 stride = (i64)gridDim.x * blockDim.x;
-    for (i64 r0 = (i64)blockIdx.x * blockDim.x + threadIdx.x; r0 < nrows; r0 += 4 * stride) {
-        i64 rr[4], e0[4], e1[4];
+    i64 r0 = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    i64 rr[4], e0[4], e1[4];
+    int c0[4];
+    T v0[4], xv[4];
+    auto load = [&](bool before_wait) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const i64 r = r0 + j * stride;
@@ -771,18 +844,34 @@ __global__ void __launch_bounds__(256) k_lr_scatter(T *__restrict__ x, i64 nrows
             e0[j] = ok ? ptr[r] : 0;
             e1[j] = ok ? ptr[r + 1] : 0;
         }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const bool has = e0[j] < e1[j];
+            c0[j] = has ? col[e0[j]] : 0;
+            v0[j] = has ? val[e0[j]] : T(0);
+            xv[j] = rr[j] >= 0 ? (before_wait ? __ldcg(x + rr[j]) : x[rr[j]]) : T(0);
+        }
+    };
+    if (r0 < nrows) load(true);
+    pdl_begin();
+    for (; r0 < nrows; r0 += 4 * stride) {
         T accv[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             accv[j] = T(0);
-            for (i64 e = e0[j]; e < e1[j]; ++e) accv[j] += val[e] * (T)z[col[e]];
+            if (e0[j] < e1[j]) {
+                accv[j] += v0[j] * (T)z[c0[j]];
+                for (i64 e = e0[j] + 1; e < e1[j]; ++e) accv[j] += val[e] * (T)z[col[e]];
+            }
         }
-        T xv[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) xv[j] = rr[j] >= 0 ? x[rr[j]] : T(0);
 #pragma unroll
         for (int j = 0; j < 4; ++j)
             if (rr[j] >= 0) x[rr[j]] = xv[j] + accv[j];
+        if (r0 + 4 * stride < nrows) {
+            r0 += 4 * stride;
+            load(false);
+            r0 -= 4 * stride;
+        }
     }
 }
 
