@@ -440,7 +440,7 @@ def exact_probe_moments(op, f, pts, rtol=1e-10):
     return 0.5 * (C + C.T), mu, dt
 
 
-def adjoint_study(nsteps=200, every=10, nfd=4, seed=7):
+def adjoint_study(nsteps=200, every=10, nfd=4, seed=7, fd2=True):
     """Differentiation: 3D 128^3 posterior (kappa^2 = 10, 32 measurements,
     centres U[0.1, 0.9]^3, radius 0.05, Sigma = 1e-4, values N(0, 1)),
     J = mean over 200 MGMC steps from x = 0 of ||x on the sub-cube
@@ -580,24 +580,92 @@ def adjoint_study(nsteps=200, every=10, nfd=4, seed=7):
         params.append(("log_sigma", k, float(g64["log_sigma"][k]), 1.0, np.abs(g64["log_sigma"]).max()))
         params.append(("y", k, float(g64["y"][k]), max(1.0, abs(y0[k])), np.abs(g64["y"]).max()))
     for kind, k, g, unit, scale in params:
-        h = 1e-6
-        fd2 = (J_dir(kind, k, h) - J_dir(kind, k, -h)) / (2 * h * unit)
+        c = {"param": kind if kind == "kappa_sq" else f"{kind}[{k}]", "adjoint": g}
+        if fd2:
+            h = 1e-6
+            d2 = (J_dir(kind, k, h) - J_dir(kind, k, -h)) / (2 * h * unit)
+            c.update(fd2=d2, rel_err_fd2=abs(g - d2) / max(abs(d2), 0.1 * scale))
         h = 1e-4
         fd4 = (8 * (J_dir(kind, k, h) - J_dir(kind, k, -h)) - (J_dir(kind, k, 2 * h) - J_dir(kind, k, -2 * h))) / (12 * h * unit)
-        name = kind if kind == "kappa_sq" else f"{kind}[{k}]"
-        checks.append({"param": name, "adjoint": g, "fd2": fd2, "fd4": fd4,
-                       "rel_err_fd2": abs(g - fd2) / max(abs(fd2), 0.1 * scale),
-                       "rel_err_fd4": abs(g - fd4) / max(abs(fd4), 0.1 * scale)})
+        c.update(fd4=fd4, rel_err_fd4=abs(g - fd4) / max(abs(fd4), 0.1 * scale))
+        checks.append(c)
     s64.close()
     out["fd_checks_fp64"] = checks
-    out["max_rel_err_fd2"] = max(c["rel_err_fd2"] for c in checks)
+    if fd2:
+        out["max_rel_err_fd2"] = max(c["rel_err_fd2"] for c in checks)
     out["max_rel_err_fd4"] = max(c["rel_err_fd4"] for c in checks)
     out["problem"] = ("3D 128^3 posterior, 32 measurements, V(1,1) SSOR, 5 levels, coarse Cholesky 8^3, Philox noise, "
                       f"{nsteps} steps, checkpoints every {every}")
     return out
 
 
-def summary_study(sizes=(16, 32, 48, 64, 128), m=32, seed=1, lrchol_max=48):
+def config1_figures(nsamples=10000, burnin=100, seed=31):
+    """Config 1: 2D prior on 64^2 cells (63^2 = 3,969 unknowns), kappa^2 = 10,
+    V(1,1) SSOR omega = 1 on 4 levels, Cholesky sampler on the 8^2-cell coarse
+    level, FP64 chain with Philox noise; 10^4 samples after 100 burn-in steps.
+    IACT of the centre ball average (window 50) and every vertex's sample
+    mean and variance against the exact mean mu and covariance (dense inverse
+    of the precision the library assembles; f = Q mu with mu uniform in
+    [0, 1]): z-scores with an integrated autocorrelation time of 1.5 in the
+    error model, and the covariance's relative Frobenius error against its
+    Monte Carlo expectation."""
+    import multigridmc_gb300 as M
+    shape = (64, 64)
+    op = M.LinearOperator.shifted_laplace_fd(shape, KAPPA_SQ)
+    Q = op.to_scipy().toarray()
+    C = np.linalg.inv(Q)
+    mu = np.random.default_rng(1342517).uniform(0.0, 1.0, op.n)
+    s = M.MultigridMCSampler(op, M.MultigridParameters(nlevel=4), precision=M.FP64, seed=seed)
+    s.fix_rhs(Q @ mu)
+    s.step(burnin)
+    bidx, bval = M.measurement_vector(shape, [0.5, 0.5], RADIUS)
+    probes = [(np.array([p], np.int64), np.array([1.0])) for p in range(op.n)] + [(bidx, bval)]
+    s.set_probes(probes, nsamples + 8)
+    s.step(nsamples)
+    s.synchronize()
+    Z = s.read_observations(nsamples + 8)
+    s.close()
+    X = Z[:, :op.n]
+    N, tau_b = X.shape[0], 1.5
+    d = np.diag(C)
+    zm = (X.mean(0) - mu) / np.sqrt(tau_b * d / N)
+    zv = (X.var(0) - d) / (d * np.sqrt(2.0 * tau_b / N))
+    Ch = np.cov(X.T, bias=True)
+    expected = np.sqrt(tau_b * np.sum(C ** 2 + np.outer(d, d)) / N) / np.linalg.norm(C)
+    return {"workload": "2D prior 64^2 cells, kappa^2=10, V(1,1) SSOR, 4 levels, coarse Cholesky 8^2, FP64",
+            "samples": int(N), "burnin": burnin, "iact": M.statistics.tau_int(Z[:, -1], IACT_WINDOW),
+            "mean_z_max": float(np.abs(zm).max()), "mean_z_rms": float(np.sqrt(np.mean(zm ** 2))),
+            "var_z_max": float(np.abs(zv).max()), "var_z_rms": float(np.sqrt(np.mean(zv ** 2))),
+            "cov_rel_frobenius": float(np.linalg.norm(Ch - C) / np.linalg.norm(C)),
+            "cov_rel_frobenius_mc_expected": float(expected)}
+
+
+def configs_section():
+    """The other configurations of the benchmark suite, compactly, each
+    guarded so that a failure is recorded instead of losing the line:
+    config 1 (2D 64^2 prior: IACT, variances vs exact), config 2 (128^3 FP64
+    posterior, 32 measurements: MGMC against the one-level SSOR Gibbs sampler
+    and the exact sampler), config 4 (512 batched chains), config 5 (128^3
+    differentiation, 200 steps, checkpoints every 10: the FP64 gradient
+    against fourth-order differences for kappa^2, y_0 and log Sigma_0, and the
+    FP32-mixed gradient against the FP64 one)."""
+    out = {}
+    for name, fn in (("config1_2d_prior_64", lambda: config1_figures()),
+                     ("config2_posterior_128_fp64", lambda: summary_study(sizes=(128,), gibbs_steps=40000,
+                                                                          fp32=False, verbose=False)[0]),
+                     ("config4_batch_512", lambda: batch_study(512, 100, compare=False)),
+                     ("config5_adjoint_128", lambda: adjoint_study(nfd=1, fd2=False))):
+        t0 = time.perf_counter()
+        try:
+            out[name] = fn()
+        except Exception as e:  # recorded, never fatal to the benchmark line
+            out[name] = {"failed": f"{type(e).__name__}: {e}"}
+        out[name]["wall_s"] = time.perf_counter() - t0
+    return out
+
+
+def summary_study(sizes=(16, 32, 48, 64, 128), m=32, seed=1, lrchol_max=48, gibbs_steps=None, fp32=True,
+                  verbose=True):
     """The reference's published comparison (python/plot_summary.py:23-33:
     IACT and time per independent sample of the Cholesky, Gibbs and MGMC
     samplers on a 3D posterior at 16^3 .. 64^3 cells) on the GPU, plus
@@ -649,16 +717,17 @@ def summary_study(sizes=(16, 32, 48, 64, 128), m=32, seed=1, lrchol_max=48):
         mg = M.MultigridParameters(nlevel=levels[N])
         gibbs = M.MultigridParameters(nlevel=1, coarse_solver="SSOR", ncoarsesmooth=1)
         row["mgmc_fp64"] = chain(mg, M.FP64, 4000, 100)
-        row["mgmc_fp32"] = chain(mg, M.FP32_MIXED, 4000, 100)
-        gsteps = 100000 if N >= 128 else 50000
+        if fp32:
+            row["mgmc_fp32"] = chain(mg, M.FP32_MIXED, 4000, 100)
+        gsteps = gibbs_steps or (100000 if N >= 128 else 50000)
         row["gibbs_fp64"] = chain(gibbs, M.FP64, gsteps, 2000)
-        if N < 128:
+        if N < 128 and fp32:
             row["gibbs_fp32"] = chain(gibbs, M.FP32_MIXED, gsteps, 2000)
         import torch
         fd = torch.from_numpy(np.asarray(f, np.float64)).cuda()
         xd = torch.empty_like(fd)
         torch.cuda.synchronize()
-        for name, prec in (("exact_fp32", M.FP32_MIXED), ("exact_fp64", M.FP64)):
+        for name, prec in (("exact_fp32", M.FP32_MIXED), ("exact_fp64", M.FP64))[(0 if fp32 else 1):]:
             s = M.MultigridMCSampler(op, mg, precision=prec, seed=seed + 200)
             for _ in range(3):
                 s.exact_sample_device(fd.data_ptr(), xd.data_ptr())
@@ -689,7 +758,8 @@ def summary_study(sizes=(16, 32, 48, 64, 128), m=32, seed=1, lrchol_max=48):
             s.close()
             row["lowrank_cholesky_fp64"] = {"ms_per_sample": dt * 1e3, "ms_per_indep": dt * 1e3, "setup_s": setup}
         rows.append(row)
-        print(json.dumps({"summary_row": row}), flush=True)
+        if verbose:
+            print(json.dumps({"summary_row": row}), flush=True)
     return rows
 
 
@@ -772,7 +842,7 @@ def solve_study(rtol=1e-10, repeats=3):
     return out
 
 
-def batch_study(nchain, steps, warmup=5, seed=3):
+def batch_study(nchain, steps, warmup=5, seed=3, compare=True):
     """Batching: nchain independent chains, cubic lattices drawn from
     {32,48,64,96,128}^3 cells, kappa^2 log-uniform in [1, 100], 0-64
     measurements (centres U[0.1,0.9]^3, radius 0.05, variance 1e-4, values
@@ -832,14 +902,19 @@ def batch_study(nchain, steps, warmup=5, seed=3):
     # batched kernels: one launch per kernel of the step for all chains of a
     # lattice size; then the same chains as one child graph per chain
     ms_step, groups, taus = timed_batch()
-    os.environ["MGMC_BATCH_KERNELS"] = "0"
-    try:
-        ms_graphs, _, _ = timed_batch()
-    finally:
-        del os.environ["MGMC_BATCH_KERNELS"]
+    graphs = None
+    if compare:
+        os.environ["MGMC_BATCH_KERNELS"] = "0"
+        try:
+            ms_graphs, _, _ = timed_batch()
+        finally:
+            del os.environ["MGMC_BATCH_KERNELS"]
+        graphs = {"ms_per_batched_step": ms_graphs, "samples_per_s": nchain * 1000.0 / ms_graphs}
+    for ch in chains:
+        ch.close()
     return {"nchain": nchain, "ms_per_batched_step": ms_step, "samples_per_s": nchain * 1000.0 / ms_step,
             "groups": groups[0], "chains_in_groups": groups[1],
-            "graph_of_graphs": {"ms_per_batched_step": ms_graphs, "samples_per_s": nchain * 1000.0 / ms_graphs},
+            "graph_of_graphs": graphs,
             "unknowns_total": int(unknowns), "setup_s": setup, "iact_median": float(np.median(taus)) if taus else None,
             "iact_p90": float(np.percentile(taus, 90)) if taus else None, "iact_window": 20, "steps": steps}
 
@@ -904,6 +979,8 @@ def main():
     ap.add_argument("--cov-probes", type=int, default=256)
     ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the compact runs of configs 1, 2, 4 and 5 after the headline measurement")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--covariance-study", type=int, default=0, metavar="NSAMPLES",
                     help="run the coupled FP32/FP64 covariance comparison instead of the benchmark")
@@ -1044,6 +1121,8 @@ def main():
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
 
+    configs = configs_section() if (world == 1 and not args.no_configs) else None
+
     n = int(op.n)
     sweep_bytes = 3 * n * 4
     line = {
@@ -1082,6 +1161,7 @@ def main():
                      "algorithmic_bytes_per_launch": bpl, "launch_s": tl, "sweep_s": 2 * tl,
                      "sweep_gbs": sweep_bytes / (2 * tl) / 1e9, "peak_kind": peak_kind},
         "cpu_baseline": cpu,
+        "configs": configs,
     }
     print(json.dumps(line), flush=True)
 
