@@ -61,6 +61,17 @@ static P *dupload(const std::vector<P> &v, cudaStream_t s) {
     return p;
 }
 
+// v as float-float pairs hi + lo: hi = v rounded to FP32, lo = the
+// remainder rounded to FP32 (about 48 significant bits in all)
+static std::vector<float2> float_float(const std::vector<double> &v) {
+    std::vector<float2> r(v.size());
+    for (size_t i = 0; i < v.size(); ++i) {
+        const float hi = (float)v[i];
+        r[i] = make_float2(hi, (float)(v[i] - (double)hi));
+    }
+    return r;
+}
+
 static inline unsigned nblk(i64 n, int bs) { return (unsigned)std::max<i64>(1, (n + bs - 1) / bs); }
 
 // Row-compressed sparse n x m matrix over its support rows (padded indices).
@@ -80,11 +91,13 @@ struct Level {
     void *x = nullptr, *f = nullptr;    // state and right hand side (T, padded)
     void *s1 = nullptr, *s2 = nullptr;  // scratch for the building-block calls
     SparseCols Bh;                      // B on this level (compact indices)
-    i64 *Bptr = nullptr, *Bidx = nullptr;
+    i64 *Bptr = nullptr;
+    unsigned *Bidx = nullptr;  // padded indices of B's entries
     double *Bval = nullptr;
     RowCsr Br;          // B by rows (double values)
-    RowCsr C[2];        // C = M^{-1} B, forward / backward (T values)
+    CorrRows C[2];      // C = M^{-1} B, forward / backward (T values)
     double *SinvT[2] = {nullptr, nullptr};  // S^{-1} transposed, per sweep direction
+    float2 *SinvT_ff[2] = {nullptr, nullptr};  // the same as float-float pairs (FP32 chain)
     double *y = nullptr, *z = nullptr, *part = nullptr;
     float *zf = nullptr, *Bvalf = nullptr;
     int bt_split = 1;  // blocks per column of the B^T x reduction
@@ -121,6 +134,7 @@ struct Sampler {
     std::vector<Level> L;
     std::vector<double> Sigma;
     double *d_sigma_inv = nullptr, *d_sigma_sqrt = nullptr;
+    float2 *d_sigma_sqrt_ff = nullptr;  // Sigma^{1/2} as float-float pairs (FP32 chain)
     // coarse Cholesky
     bool chol = false;
     double *dL = nullptr, *dgv = nullptr;
@@ -316,9 +330,13 @@ NoiseArgs Sampler::noise_args(int lev, i64 count) {
 constexpr i64 PDL_MAX_POINTS = i64(1) << 22;
 // supports of C up to this many rows take the fused solve + correction
 #ifndef MGMC_LR_FUSE_MAX_ROWS
-#define MGMC_LR_FUSE_MAX_ROWS (1ll << 16)
+#define MGMC_LR_FUSE_MAX_ROWS 200000ll
 #endif
 constexpr i64 LR_FUSE_MAX_ROWS = MGMC_LR_FUSE_MAX_ROWS;
+// CTAs per SM of the fused solve + correction (each CTA repeats the solve)
+#ifndef MGMC_LR_APPLY_CTAS_PER_SM
+#define MGMC_LR_APPLY_CTAS_PER_SM 2
+#endif
 
 template <typename... KArgs, typename... Args>
 static void plaunch(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
@@ -494,13 +512,16 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
     lr.zf = lv.zf;
     lr.SinvT = lv.SinvT[dir];
     lr.sigma_sqrt = S.d_sigma_sqrt;
+    lr.SinvT_ff = lv.SinvT_ff[dir];
+    lr.sigma_sqrt_ff = S.d_sigma_sqrt_ff;
     lr.y = lv.y;
     lr.z = lv.z;
     lr.part = lv.part;
     lr.counter = lv.counter;
-    const RowCsr &C = lv.C[dir];
+    const CorrRows &C = lv.C[dir];
+    const i64 nrows = C.n1 + C.nm;
     const dim3 bgrid(S.m, lv.bt_split);
-    if (C.nrows > LR_FUSE_MAX_ROWS) {
+    if (nrows > LR_FUSE_MAX_ROWS) {
         // large support: partial sums with the solve in their last CTA, then
         // the correction on the whole GPU
         const size_t smem = solve_smem(S.m);
@@ -510,40 +531,35 @@ static void launch_lowrank(Sampler &S, Level &lv, int dir, int noise, T *x, cons
             plaunch(S.pdl, k_bt_solve<T, NOISE_PHILOX, true>, bgrid, 256, smem, S.stream, (const T *)x, lr, nz);
         else
             plaunch(S.pdl, k_bt_solve<T, NOISE_INJECTED, true>, bgrid, 256, smem, S.stream, (const T *)x, lr, nz);
-        const unsigned blocks = (unsigned)std::min<i64>(nblk(C.nrows, 4 * 256), 8 * S.nsm);
+        const unsigned blocks = (unsigned)std::min<i64>(nblk(nrows, 4 * 256), 8 * S.nsm);
         if (sizeof(T) == 4)
-            plaunch(S.pdl, k_lr_scatter<T, float>, blocks, 256, 0, S.stream, x, C.nrows, C.rows, C.ptr, C.col,
-                    (const T *)C.val, (const float *)lv.zf);
+            plaunch(S.pdl, k_lr_scatter<T, float>, blocks, 256, 0, S.stream, x, C, (const float *)lv.zf);
         else
-            plaunch(S.pdl, k_lr_scatter<T, double>, blocks, 256, 0, S.stream, x, C.nrows, C.rows, C.ptr, C.col,
-                    (const T *)C.val, (const double *)lv.z);
+            plaunch(S.pdl, k_lr_scatter<T, double>, blocks, 256, 0, S.stream, x, C, (const double *)lv.z);
         S.launches++;
-    } else if (C.nrows > 0) {
+    } else if (nrows > 0) {
         plaunch(S.pdl, k_bt_partial<T>, bgrid, 256, 0, S.stream, (const T *)x, lr);
         S.launches++;
-        // solve and correction in one launch; every CTA repeats the (FP64)
-        // m x m solve, so the grid stays at two CTAs per SM at most
-        const unsigned blocks = (unsigned)std::min<i64>(nblk(C.nrows, 256), 2 * S.nsm);
+        // solve and correction in one launch; every CTA repeats the m x m
+        // solve, so the grid stays at a few CTAs per SM
+        const unsigned blocks = (unsigned)std::min<i64>(nblk(nrows, 256), MGMC_LR_APPLY_CTAS_PER_SM * S.nsm);
         const size_t sm = sizeof(double) * (2 * (size_t)S.m + 256);
         if (noise == NOISE_NONE)
-            plaunch(S.pdl, k_lr_apply<T, NOISE_NONE>, blocks, 256, sm, S.stream, x, lr, lv.bt_split, nz, C.nrows, C.rows,
-                    C.ptr, C.col, (const T *)C.val);
+            plaunch(S.pdl, k_lr_apply<T, NOISE_NONE>, blocks, 256, sm, S.stream, x, lr, lv.bt_split, nz, C);
         else if (noise == NOISE_PHILOX)
-            plaunch(S.pdl, k_lr_apply<T, NOISE_PHILOX>, blocks, 256, sm, S.stream, x, lr, lv.bt_split, nz, C.nrows, C.rows,
-                    C.ptr, C.col, (const T *)C.val);
+            plaunch(S.pdl, k_lr_apply<T, NOISE_PHILOX>, blocks, 256, sm, S.stream, x, lr, lv.bt_split, nz, C);
         else
-            plaunch(S.pdl, k_lr_apply<T, NOISE_INJECTED>, blocks, 256, sm, S.stream, x, lr, lv.bt_split, nz, C.nrows,
-                    C.rows, C.ptr, C.col, (const T *)C.val);
+            plaunch(S.pdl, k_lr_apply<T, NOISE_INJECTED>, blocks, 256, sm, S.stream, x, lr, lv.bt_split, nz, C);
     } else {
         plaunch(S.pdl, k_bt_partial<T>, bgrid, 256, 0, S.stream, (const T *)x, lr);
         S.launches++;
         const size_t smem = solve_smem(S.m);
         if (noise == NOISE_NONE)
-            plaunch(S.pdl, k_lr_solve<NOISE_NONE, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
+            plaunch(S.pdl, k_lr_solve<T, NOISE_NONE, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
         else if (noise == NOISE_PHILOX)
-            plaunch(S.pdl, k_lr_solve<NOISE_PHILOX, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
+            plaunch(S.pdl, k_lr_solve<T, NOISE_PHILOX, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
         else
-            plaunch(S.pdl, k_lr_solve<NOISE_INJECTED, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
+            plaunch(S.pdl, k_lr_solve<T, NOISE_INJECTED, true>, 1, solve_block(S.m), smem, S.stream, lr, lv.bt_split, nz);
     }
     S.launches += 1;
 }
@@ -825,7 +841,7 @@ static int stencil_npt(int ncol, const double st[27]) {
     return 7;
 }
 
-__global__ void k_scatter(const i64 *__restrict__ idx, const double *__restrict__ val, i64 cnt, double *__restrict__ dst) {
+__global__ void k_scatter(const unsigned *__restrict__ idx, const double *__restrict__ val, i64 cnt, double *__restrict__ dst) {
     i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < cnt) dst[idx[t]] = val[t];
 }
@@ -854,8 +870,10 @@ void Sampler::build_lowrank(int lev) {
     const i64 n = geo.n;
     // B on this level: CSC with padded indices, and row-compressed form
     {
-        std::vector<i64> bidx(lv.Bh.row.size());
-        for (size_t e = 0; e < bidx.size(); ++e) bidx[e] = geo.pad(lv.Bh.row[e]);
+        if (geo.nalloc > (i64)UINT32_MAX)
+            fail(MGMC_ERR_UNSUPPORTED, "measurements on a level of 2^32 or more padded points (32-bit indices of B and C)");
+        std::vector<unsigned> bidx(lv.Bh.row.size());
+        for (size_t e = 0; e < bidx.size(); ++e) bidx[e] = (unsigned)geo.pad(lv.Bh.row[e]);
         std::vector<i64> bptr(lv.Bh.ptr.begin(), lv.Bh.ptr.end());
         lv.Bptr = upload(bptr);
         lv.Bidx = upload(bidx);
@@ -934,7 +952,7 @@ void Sampler::build_lowrank(int lev) {
             lr.y = lv.y;
             lr.part = lv.part;
             k_bt_partial<double><<<dim3(m, lv.bt_split), 256, 0, stream>>>(xs, lr);
-            k_lr_solve<NOISE_NONE, false><<<1, solve_block(m), 0, stream>>>(lr, lv.bt_split, nz);
+            k_lr_solve<double, NOISE_NONE, false><<<1, solve_block(m), 0, stream>>>(lr, lv.bt_split, nz);
             CK(cudaMemcpyAsync(yh.data(), lv.y, m * sizeof(double), cudaMemcpyDeviceToHost, stream));
             CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), stream));
             k_nonzeros<<<nblk(n, 256), 256, 0, stream>>>(xs, lv.g, nzi, nzv, cnt);
@@ -951,29 +969,44 @@ void Sampler::build_lowrank(int lev) {
             for (unsigned long long e = 0; e < hc; ++e) trip.emplace_back(ii[e], j, vv[e]);
             for (int a = 0; a < m; ++a) Sh[(size_t)a * m + j] = yh[a] + (a == j ? Sigma[a] : 0.0);
         }
+        // rows with one entry as triples, the others in CSR form (entries
+        // of a row in column order)
         std::sort(trip.begin(), trip.end());
-        std::vector<i64> rows, ptr{0};
-        std::vector<int> col;
-        std::vector<double> val;
-        for (size_t e = 0; e < trip.size(); ++e) {
-            if (e == 0 || std::get<0>(trip[e]) != std::get<0>(trip[e - 1])) {
-                if (e > 0) ptr.push_back((i64)col.size());
-                rows.push_back(geo.pad(std::get<0>(trip[e])));
+        std::vector<unsigned> r1, rm;
+        std::vector<int> c1, pm{0}, cm;
+        std::vector<double> v1, vm;
+        for (size_t e = 0; e < trip.size();) {
+            size_t e1 = e + 1;
+            while (e1 < trip.size() && std::get<0>(trip[e1]) == std::get<0>(trip[e])) ++e1;
+            const unsigned row = (unsigned)geo.pad(std::get<0>(trip[e]));
+            if (e1 == e + 1) {
+                r1.push_back(row);
+                c1.push_back(std::get<1>(trip[e]));
+                v1.push_back(std::get<2>(trip[e]));
+            } else {
+                rm.push_back(row);
+                for (size_t k = e; k < e1; ++k) {
+                    cm.push_back(std::get<1>(trip[k]));
+                    vm.push_back(std::get<2>(trip[k]));
+                }
+                pm.push_back((int)cm.size());
             }
-            col.push_back(std::get<1>(trip[e]));
-            val.push_back(std::get<2>(trip[e]));
+            e = e1;
         }
-        if (!trip.empty()) ptr.push_back((i64)col.size());
-        RowCsr &C = lv.C[dir];
-        C.nrows = (i64)rows.size();
-        C.rows = upload(rows);
-        C.ptr = upload(ptr);
-        C.col = upload(col);
+        CorrRows &C = lv.C[dir];
+        C.n1 = (i64)r1.size();
+        C.nm = (i64)rm.size();
+        C.r1 = upload(r1);
+        C.c1 = upload(c1);
+        C.rm = upload(rm);
+        C.pm = upload(pm);
+        C.cm = upload(cm);
         if (fp32) {
-            std::vector<float> vf(val.begin(), val.end());
-            C.val = upload(vf);
+            C.v1 = upload(std::vector<float>(v1.begin(), v1.end()));
+            C.vm = upload(std::vector<float>(vm.begin(), vm.end()));
         } else {
-            C.val = upload(val);
+            C.v1 = upload(v1);
+            C.vm = upload(vm);
         }
         {
             const std::vector<double> Si = small_inverse(Sh, m);
@@ -981,6 +1014,7 @@ void Sampler::build_lowrank(int lev) {
             for (int a = 0; a < m; ++a)
                 for (int q = 0; q < m; ++q) SiT[(size_t)q * m + a] = Si[(size_t)a * m + q];
             lv.SinvT[dir] = upload(SiT);
+            lv.SinvT_ff[dir] = upload(float_float(SiT));
         }
     }
     CK(cudaStreamSynchronize(stream));
@@ -1231,6 +1265,7 @@ void Sampler::build(const mgmc_operator_desc &op) {
         }
         d_sigma_inv = upload(si);
         d_sigma_sqrt = upload(ss);
+        d_sigma_sqrt_ff = upload(float_float(ss));
         const size_t lr_smem = sizeof(double) * (2 * (size_t)m + 256);
         if (lr_smem > 48 * 1024) {
             raise_smem_limit(k_lr_apply<float, NOISE_NONE>, lr_smem);
@@ -2621,17 +2656,15 @@ void BatchGroup::build(cudaStream_t st) {
                 r.zf = lv.zf;
                 r.SinvT = lv.SinvT[dir];
                 r.sigma_sqrt = S.d_sigma_sqrt;
+                r.SinvT_ff = lv.SinvT_ff[dir];
+                r.sigma_sqrt_ff = S.d_sigma_sqrt_ff;
                 r.y = lv.y;
                 r.z = lv.z;
                 r.part = lv.part;
                 r.counter = lv.counter;
-                const RowCsr &C = lv.C[dir];
-                b.nrows = C.nrows;
-                b.rows = C.rows;
-                b.ptr = C.ptr;
-                b.col = C.col;
-                b.val = (const float *)C.val;
-                row_jobs(dir == 0 ? sj0 : sj1, c, C.nrows);
+                const CorrRows &C = lv.C[dir];
+                b.C = C;
+                row_jobs(dir == 0 ? sj0 : sj1, c, C.n1 + C.nm);
             }
             LowRankArg &r = lres[c].lr;  // launch_bt_plain's arguments
             r.m = S.m;

@@ -49,6 +49,10 @@ typedef unsigned long long u64;
 // grid runs, made the 256^3 step 1.8 % slower: the waiting CTAs hold SM
 // slots the running grid needs.)
 __device__ __forceinline__ void pdl_begin() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Let the next kernel on the stream start its CTAs now (they still wait in
+// pdl_begin until this grid has completed).  Used where one CTA is left
+// working alone, so that the next kernel's independent loads overlap it.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // ------------------------------------------------------------- geometry
 struct Grid3 {
@@ -542,11 +546,75 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
     return v;  // valid in warp 0
 }
 
+// ------------------------------------------------ float-float arithmetic
+// An unevaluated sum hi + lo of two FP32 numbers carries about 48
+// significant bits.  GB300 issues about two FP64 FMAs per clock per SM
+// against 128 FP32 ones, so the FP32 chain forms the cross-thread sums of
+// B^T x and the low-rank m x m product in this arithmetic instead of FP64.
+// Error-free transformations: TwoSum (Knuth, TAOCP vol. 2, 4.2.2), Fast
+// TwoSum (Dekker 1971) and TwoProd with an FMA (Ogita, Rump, Oishi,
+// "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005).  The _rn
+// intrinsics keep the compiler from contracting a product and a sum into one
+// FMA, which would break the transformations.
+struct ff32 {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff32 two_sum(float a, float b) {  // s + e == a + b exactly
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ ff32 fast_two_sum(float a, float b) {  // exact when |a| >= |b| or a == 0
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+// (a.hi + a.lo) + (b.hi + b.lo): both parts summed with TwoSum, then
+// renormalised twice (accurate under cancellation).  Symmetric in a and b
+// bit for bit, since TwoSum's error term is the exact error.
+__device__ __forceinline__ ff32 ff_add(ff32 a, ff32 b) {
+    ff32 s = two_sum(a.hi, b.hi);
+    const ff32 t = two_sum(a.lo, b.lo);
+    s = fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, t.lo));
+}
+// (a.hi + a.lo) (b.hi + b.lo) without the a.lo b.lo term
+__device__ __forceinline__ ff32 ff_mul(ff32 a, ff32 b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ ff32 ff_neg(ff32 a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ ff32 ff_of(float2 v) { return {v.x, v.y}; }
+__device__ __forceinline__ double ff_to_double(ff32 a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ float ff_to_float(ff32 a) { return __fadd_rn(a.hi, a.lo); }
+
+// block_sum's shuffle tree in float-float; the result is valid in warp 0
+template <int NT>
+__device__ __forceinline__ ff32 block_sum_ff(ff32 v, float2 *sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = ff_add(v, ff32{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)});
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = make_float2(v.hi, v.lo);
+    __syncthreads();
+    v = (threadIdx.x < NT / 32) ? ff_of(sh[threadIdx.x]) : ff32{0.f, 0.f};
+    if (w == 0) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v = ff_add(v, ff32{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)});
+    }
+    __syncthreads();
+    return v;
+}
+
 // Low-rank arguments of one level and sweep direction.
 struct LowRankArg {
     int m;
-    const i64 *Bptr;    // m+1, CSC of B (padded indices)
-    const i64 *Bidx;
+    const i64 *Bptr;    // m+1, CSC of B
+    const unsigned *Bidx;  // padded indices (levels below 2^32 padded points)
     const double *Bval;
     const double *SinvT; // m x m, S^{-1} = (Sigma + B^T M^{-1} B)^{-1}, transposed (column q contiguous)
     const double *sigma_sqrt; // Sigma^{1/2}
@@ -554,49 +622,65 @@ struct LowRankArg {
     double *z;          // m scratch: coefficients of C
     float *zf;          // the same coefficients rounded to FP32 (FP32 chain)
     const float *Bvalf; // B values rounded to FP32 (FP32 chain)
-    double *part;       // m x P scratch: partial sums of B^T x
+    double *part;       // m x P scratch: partial sums of B^T x (the FP32 chain
+                        // stores float-float pairs, float2, in the same slots)
     unsigned *counter;  // CTA counter of k_bt_solve (reset by its last CTA)
+    const float2 *SinvT_ff;      // SinvT as float-float pairs (FP32 chain)
+    const float2 *sigma_sqrt_ff; // Sigma^{1/2} as float-float pairs (FP32 chain)
 };
 
 // Partial sums of y_j = sum_i B_ij x_i: gridDim.y CTAs per column j, CTA p
-// writing part[j * P + p].  Each thread issues four index/value loads, then
-// the four gathers of x, before it accumulates them in entry order; the
+// writing part[j * P + p].  Each thread issues eight index/value loads, then
+// the eight gathers of x, before it accumulates them in entry order; the
 // per-thread sums are in the state's precision (FP32 products for the FP32
-// chain) and are combined across the CTA in FP64.
+// chain) and are combined across the CTA in FP64, or in float-float for the
+// FP32 chain (stored as a float2 in the slot).  B does not change, so a
+// thread's first index/value loads are issued before the wait for the
+// kernel that wrote x (`wait`: the caller has not waited yet).
 template <typename T>
 __device__ __forceinline__ void bt_partial_cta(const T *__restrict__ x, const LowRankArg &lr, double *sh, int j, int p,
-                                               int P) {
+                                               int P, bool wait = false) {
     const i64 e0 = lr.Bptr[j], e1 = lr.Bptr[j + 1];
     const i64 len = (e1 - e0 + P - 1) / P;
     const i64 lo = e0 + p * len, hi = min(e1, lo + len);
     T tacc = T(0);
-    // eight index/value loads, then the eight gathers, in flight at once;
-    // the products are added in entry order
-    for (i64 e = lo + threadIdx.x; e < hi; e += 8 * 256) {
-        i64 idx[8];
-        T val[8];
+    i64 idx[8];
+    T val[8];
+    auto load = [&](i64 e) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const i64 ee = e + 256 * k;
-            idx[k] = ee < hi ? lr.Bidx[ee] : -1;
+            idx[k] = ee < hi ? (i64)lr.Bidx[ee] : -1;
             val[k] = ee < hi ? (sizeof(T) == 4 ? (T)lr.Bvalf[ee] : (T)lr.Bval[ee]) : T(0);
         }
+    };
+    i64 e = lo + threadIdx.x;
+    load(e);
+    if (wait) pdl_begin();
+    // eight index/value loads, then the eight gathers, in flight at once;
+    // the products are added in entry order
+    for (; e < hi; e += 8 * 256) {
         T xv[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) xv[k] = idx[k] >= 0 ? x[idx[k]] : T(0);
 #pragma unroll
         for (int k = 0; k < 8; ++k)
             if (idx[k] >= 0) tacc += val[k] * xv[k];
+        if (e + 8 * 256 < hi) load(e + 8 * 256);
     }
-    const double acc = block_sum<256>((double)tacc, sh);
-    if (threadIdx.x == 0) lr.part[j * P + p] = acc;
+    if (sizeof(T) == 4) {
+        const ff32 acc = block_sum_ff<256>(ff32{(float)tacc, 0.f}, reinterpret_cast<float2 *>(sh));
+        if (threadIdx.x == 0) reinterpret_cast<float2 *>(lr.part)[j * P + p] = make_float2(acc.hi, acc.lo);
+    } else {
+        const double acc = block_sum<256>((double)tacc, sh);
+        if (threadIdx.x == 0) lr.part[j * P + p] = acc;
+    }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_bt_partial(const T *__restrict__ x, LowRankArg lr) {
-    pdl_begin();
     __shared__ double sh[32];
-    bt_partial_cta<T>(x, lr, sh, blockIdx.x, blockIdx.y, gridDim.y);
+    bt_partial_cta<T>(x, lr, sh, blockIdx.x, blockIdx.y, gridDim.y, true);
 }
 
 // One CTA: y_k = sum_p part[k * P + p] (fixed order, so the result does not
@@ -722,97 +806,287 @@ __device__ __forceinline__ void lr_solve_cta(const LowRankArg &lr, int P, const 
     }
 }
 
+// lr_solve_cta for the FP32 chain: the same sums, in the same order and the
+// same thread layout, in float-float arithmetic (partial sums as float2
+// pairs, S^{-1} and Sigma^{1/2} from their float-float copies).  z goes to
+// zsf (shared, m floats, rounded to FP32) and, if `publish`, to lr.z (the
+// float-float value in FP64) and lr.zf.  u and acc are shared scratch of m
+// and 256 float2.
 template <int NOISE, bool SOLVE>
+__device__ __forceinline__ void lr_solve_cta_ff(const LowRankArg &lr, int P, const NoiseArgs &nz, float2 *u,
+                                                float2 *acc, float *zsf, bool publish) {
+    const int m = lr.m;
+    const int rows = m < 256 ? m : 256;
+    const int tpr = 256 / rows;
+    const int g = threadIdx.x / rows, kk = threadIdx.x % rows;
+    const int cnt = g < tpr ? (m - g + tpr - 1) / tpr : 0;
+    const bool pre = SOLVE && m <= 64;
+    const float2 *part = reinterpret_cast<const float2 *>(lr.part);
+    float2 pv[16];
+    if (pre) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+            pv[i] = i < cnt ? __ldg(lr.SinvT_ff + (i64)(g + i * tpr) * m + kk) : make_float2(0.f, 0.f);
+    }
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        float2 pp[8];
+        ff32 t{0.f, 0.f};
+        for (int q0 = 0; q0 < P; q0 += 8) {
+#pragma unroll
+            for (int r = 0; r < 8; ++r) pp[r] = q0 + r < P ? __ldcg(part + (i64)k * P + q0 + r) : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                if (q0 + r < P) t = ff_add(t, ff_of(pp[r]));
+        }
+        if (publish) lr.y[k] = ff_to_double(t);
+        if (SOLVE) {
+            float xi = 0.f;
+            if (NOISE == NOISE_PHILOX) {
+                float4 rn = normals4(philox4x32_10(noise_ctr(nz, (unsigned)(k >> 2), PURPOSE_LOWRANK, 0), noise_key(nz)));
+                xi = pick(rn, k & 3);
+            }
+            if (NOISE == NOISE_INJECTED) xi = (float)nz.buf[k];
+            const ff32 uk = ff_add(ff_mul(ff_of(lr.sigma_sqrt_ff[k]), ff32{xi, 0.f}), ff_neg(t));
+            u[k] = make_float2(uk.hi, uk.lo);
+        }
+    }
+    if (!SOLVE) return;
+    __syncthreads();
+    auto finish = [&](int k, ff32 zk) {
+        if (zsf) zsf[k] = ff_to_float(zk);
+        if (publish) {
+            lr.z[k] = ff_to_double(zk);
+            if (lr.zf) lr.zf[k] = ff_to_float(zk);
+        }
+    };
+    if (pre) {
+        ff32 t0{0.f, 0.f}, t1{0.f, 0.f};
+        if (g < tpr) {
+#pragma unroll
+            for (int i = 0; i < 16; i += 2) {
+                if (i < cnt) t0 = ff_add(t0, ff_mul(ff_of(pv[i]), ff_of(u[g + i * tpr])));
+                if (i + 1 < cnt) t1 = ff_add(t1, ff_mul(ff_of(pv[i + 1]), ff_of(u[g + (i + 1) * tpr])));
+            }
+            const ff32 s = ff_add(t0, t1);
+            acc[g * rows + kk] = make_float2(s.hi, s.lo);
+        }
+        __syncthreads();
+        if (threadIdx.x < rows) {
+            ff32 zk{0.f, 0.f};
+            for (int h = 0; h < tpr; ++h) zk = ff_add(zk, ff_of(acc[h * rows + threadIdx.x]));
+            finish(threadIdx.x, zk);
+        }
+        __syncthreads();
+        return;
+    }
+    for (int k0 = 0; k0 < m; k0 += rows) {
+        const int k = k0 + kk;
+        if (g < tpr && k < m) {
+            ff32 t0{0.f, 0.f}, t1{0.f, 0.f};
+            int q = g;
+            for (; q + 7 * tpr < m; q += 8 * tpr) {
+                float2 sv[8];
+#pragma unroll
+                for (int r = 0; r < 8; ++r) sv[r] = __ldg(lr.SinvT_ff + (i64)(q + r * tpr) * m + k);
+#pragma unroll
+                for (int r = 0; r < 8; r += 2) {
+                    t0 = ff_add(t0, ff_mul(ff_of(sv[r]), ff_of(u[q + r * tpr])));
+                    t1 = ff_add(t1, ff_mul(ff_of(sv[r + 1]), ff_of(u[q + (r + 1) * tpr])));
+                }
+            }
+            for (; q < m; q += tpr) t0 = ff_add(t0, ff_mul(ff_of(__ldg(lr.SinvT_ff + (i64)q * m + k)), ff_of(u[q])));
+            const ff32 s = ff_add(t0, t1);
+            acc[g * rows + kk] = make_float2(s.hi, s.lo);
+        }
+        __syncthreads();
+        if (threadIdx.x < rows && k0 + threadIdx.x < m) {
+            ff32 zk{0.f, 0.f};
+            for (int h = 0; h < tpr; ++h) zk = ff_add(zk, ff_of(acc[h * rows + threadIdx.x]));
+            finish(k0 + threadIdx.x, zk);
+        }
+        __syncthreads();
+    }
+}
+
+// The low-rank solve of a chain in precision T: FP64 for the FP64 chain,
+// float-float for the FP32 chain (its partial sums are float-float pairs).
+// u and acc: shared scratch of m and 256 doubles; z goes to zs (m doubles of
+// shared memory, holding m floats for the FP32 chain) unless it is null.
+template <typename T, int NOISE, bool SOLVE>
+__device__ __forceinline__ void lr_solve_chain(const LowRankArg &lr, int P, const NoiseArgs &nz, double *u,
+                                               double *acc, double *zs, bool publish) {
+    if (sizeof(T) == 4)
+        lr_solve_cta_ff<NOISE, SOLVE>(lr, P, nz, reinterpret_cast<float2 *>(u), reinterpret_cast<float2 *>(acc),
+                                      reinterpret_cast<float *>(zs), publish);
+    else
+        lr_solve_cta<NOISE, SOLVE>(lr, P, nz, u, acc, zs, publish);
+}
+
+template <typename T, int NOISE, bool SOLVE>
 __global__ void __launch_bounds__(256) k_lr_solve(LowRankArg lr, int P, NoiseArgs nz) {
     pdl_begin();
     extern __shared__ double dyn[];
-    lr_solve_cta<NOISE, SOLVE>(lr, P, nz, dyn, dyn + lr.m, nullptr, true);
+    lr_solve_chain<T, NOISE, SOLVE>(lr, P, nz, dyn, dyn + lr.m, nullptr, true);
 }
 
 // Partial sums and the solve in one launch: the last CTA to finish (block
 // counter, reset by that CTA) forms y -- and with SOLVE z -- from the
 // partial sums in the same fixed order as k_lr_solve, so the result does
-// not depend on block timing.
+// not depend on block timing.  Only the thread that wrote the CTA's partial
+// sum fences before counting it, and the last CTA's counting thread fences
+// before the barrier after which its threads read the others' sums.
 template <typename T, int NOISE, bool SOLVE>
 __device__ __forceinline__ void bt_solve_body(const T *__restrict__ x, const LowRankArg &lr, const NoiseArgs &nz, int j,
-                                              int p, int P) {
+                                              int p, int P, bool wait = false) {
     __shared__ double sh[32];
     __shared__ bool last;
-    bt_partial_cta<T>(x, lr, sh, j, p, P);
-    __threadfence();
-    if (threadIdx.x == 0) last = atomicAdd(lr.counter, 1u) == (unsigned)(lr.m * P) - 1u;
+    bt_partial_cta<T>(x, lr, sh, j, p, P, wait);
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(lr.counter, 1u) == (unsigned)(lr.m * P) - 1u;
+        if (last) {
+            __threadfence();
+            *lr.counter = 0u;
+        }
+    }
     __syncthreads();
     if (!last) return;
-    __threadfence();
-    if (threadIdx.x == 0) *lr.counter = 0u;
+#ifndef MGMC_LR_NO_EARLY_TRIGGER
+    // every other CTA has exited: the next kernel (the correction) can load
+    // its rows of C while this CTA forms z
+    pdl_trigger();
+#endif
     extern __shared__ double dyn[];
-    lr_solve_cta<NOISE, SOLVE>(lr, P, nz, dyn, dyn + lr.m, nullptr, true);
+    lr_solve_chain<T, NOISE, SOLVE>(lr, P, nz, dyn, dyn + lr.m, nullptr, true);
 }
 
 template <typename T, int NOISE, bool SOLVE>
 __global__ void __launch_bounds__(256) k_bt_solve(const T *__restrict__ x, LowRankArg lr, NoiseArgs nz) {
-    pdl_begin();
-    bt_solve_body<T, NOISE, SOLVE>(x, lr, nz, blockIdx.x, blockIdx.y, gridDim.y);
+    bt_solve_body<T, NOISE, SOLVE>(x, lr, nz, blockIdx.x, blockIdx.y, gridDim.y, true);
 }
+
+// Support rows of C = M^{-1} B as x += C z reads them: the rows with one
+// entry -- nearly all, since the measurement balls rarely overlap -- as
+// (row, column, value) triples, the others in CSR form.  Padded row indices
+// are 32-bit (levels of fewer than 2^32 padded points).
+struct CorrRows {
+    i64 n1 = 0, nm = 0;            // rows with one entry / with several
+    const unsigned *r1 = nullptr;  // n1 padded row indices
+    const int *c1 = nullptr;       // their columns
+    const void *v1 = nullptr;      // their values (type T)
+    const unsigned *rm = nullptr;  // nm padded row indices
+    const int *pm = nullptr;       // nm + 1 offsets into cm / vm
+    const int *cm = nullptr;
+    const void *vm = nullptr;
+};
+
+// x[row] += C z over the multi-entry row r: the products added to zero in
+// entry order, then to the state
+template <typename T, typename ZT>
+__device__ __forceinline__ void corr_multi_row(T *__restrict__ x, const CorrRows &C, i64 r, const ZT *z) {
+    const T *vm = static_cast<const T *>(C.vm);
+    T acc = T(0);
+    for (int e = C.pm[r]; e < C.pm[r + 1]; ++e) acc += vm[e] * (T)z[C.cm[e]];
+    const unsigned row = C.rm[r];
+    x[row] = x[row] + acc;
+}
+
+// Four single-entry rows of a thread, r0 + j stride (j < 4): row index,
+// column, value and state loaded together; the update is the multi-entry
+// arithmetic with one product.  The state of rows loaded before the wait
+// for the previous kernel is read through L2 (see k_lr_scatter).
+template <typename T>
+struct CorrQuad {
+    unsigned row[4];
+    int col[4];
+    T val[4], xv[4];
+    __device__ __forceinline__ void load(const T *__restrict__ x, const CorrRows &C, i64 r0, i64 stride,
+                                         bool before_wait) {
+        const T *v1 = static_cast<const T *>(C.v1);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const i64 r = r0 + j * stride;
+            const bool ok = r < C.n1;
+            row[j] = ok ? C.r1[r] : 0u;
+            col[j] = ok ? C.c1[r] : 0;
+            val[j] = ok ? v1[r] : T(0);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            xv[j] = r0 + j * stride < C.n1 ? (before_wait ? __ldcg(x + row[j]) : x[row[j]]) : T(0);
+    }
+    template <typename ZT>
+    __device__ __forceinline__ void apply(T *__restrict__ x, const CorrRows &C, i64 r0, i64 stride,
+                                          const ZT *z) const {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (r0 + j * stride >= C.n1) continue;
+            T acc = T(0);
+            acc += val[j] * (T)z[col[j]];
+            x[row[j]] = xv[j] + acc;
+        }
+    }
+};
+
+// One multi-entry row r (two entries at least) with its row index, entry
+// range, first two entries and state loaded together, before the wait for
+// the previous kernel where the caller says so; the update is
+// corr_multi_row's arithmetic.
+template <typename T>
+struct CorrMulti {
+    unsigned row;
+    int e0, e1, col0, col1;
+    T val0, val1, xv;
+    __device__ __forceinline__ void load(const T *__restrict__ x, const CorrRows &C, i64 r, bool before_wait) {
+        const T *vm = static_cast<const T *>(C.vm);
+        row = C.rm[r];
+        e0 = C.pm[r];
+        e1 = C.pm[r + 1];
+        col0 = C.cm[e0];
+        col1 = C.cm[e0 + 1];
+        val0 = vm[e0];
+        val1 = vm[e0 + 1];
+        xv = before_wait ? __ldcg(x + row) : x[row];
+    }
+    template <typename ZT>
+    __device__ __forceinline__ void apply(T *__restrict__ x, const CorrRows &C, const ZT *z) const {
+        const T *vm = static_cast<const T *>(C.vm);
+        T acc = T(0);
+        acc += val0 * (T)z[col0];
+        acc += val1 * (T)z[col1];
+        for (int e = e0 + 2; e < e1; ++e) acc += vm[e] * (T)z[C.cm[e]];
+        x[row] = xv + acc;
+    }
+};
 
 // Low-rank solve and correction in one launch: every CTA forms z itself
 // (the same arithmetic in the same order in every CTA, so all agree) and
 // adds C z on its share of the support rows of C = M^{-1} B, four rows per
-// thread and iteration with their loads issued together.
+// thread and iteration with their loads issued together.  A thread's first
+// four rows do not depend on the partial sums the kernel before writes, so
+// they are loaded before the wait.
 template <typename T, int NOISE>
-__global__ void __launch_bounds__(256) k_lr_apply(T *__restrict__ x, LowRankArg lr, int P, NoiseArgs nz, i64 nrows,
-                                                  const i64 *__restrict__ rows, const i64 *__restrict__ ptr,
-                                                  const int *__restrict__ col, const T *__restrict__ val) {
-    // a thread's first four rows (indices, entry ranges, first entries and
-    // state) do not depend on the partial sums the kernel before writes:
-    // loaded before the wait, the state through L2 (see k_lr_scatter)
+__global__ void __launch_bounds__(256) k_lr_apply(T *__restrict__ x, LowRankArg lr, int P, NoiseArgs nz, CorrRows C) {
     const i64 stride = (i64)gridDim.x * blockDim.x;
-    i64 r0 = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    i64 rr[4], e0[4], e1[4];
-    int c0[4];
-    T v0[4], xv[4];
-    auto load = [&](bool before_wait) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const i64 r = r0 + j * stride;
-            const bool ok = r < nrows;
-            rr[j] = ok ? rows[r] : -1;
-            e0[j] = ok ? ptr[r] : 0;
-            e1[j] = ok ? ptr[r + 1] : 0;
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const bool has = e0[j] < e1[j];
-            c0[j] = has ? col[e0[j]] : 0;
-            v0[j] = has ? val[e0[j]] : T(0);
-            xv[j] = rr[j] >= 0 ? (before_wait ? __ldcg(x + rr[j]) : x[rr[j]]) : T(0);
-        }
-    };
-    if (r0 < nrows) load(true);
+    const i64 t0 = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    CorrQuad<T> q;
+    CorrMulti<T> mr;
+    if (t0 < C.n1) q.load(x, C, t0, stride, true);
+    if (t0 < C.nm) mr.load(x, C, t0, true);
     pdl_begin();
     extern __shared__ double dyn[];
     const int m = lr.m;
-    double *zs = dyn, *u = dyn + m, *acc = dyn + 2 * m;
-    lr_solve_cta<NOISE, true>(lr, P, nz, u, acc, zs, blockIdx.x == 0);
-    // zs is complete after the last __syncthreads of lr_solve_cta
-    for (; r0 < nrows; r0 += 4 * stride) {
-        T accv[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            accv[j] = T(0);
-            if (e0[j] < e1[j]) {
-                accv[j] += v0[j] * (T)zs[c0[j]];
-                for (i64 e = e0[j] + 1; e < e1[j]; ++e) accv[j] += val[e] * (T)zs[col[e]];
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (rr[j] >= 0) x[rr[j]] = xv[j] + accv[j];
-        if (r0 + 4 * stride < nrows) {
-            r0 += 4 * stride;
-            load(false);
-            r0 -= 4 * stride;
-        }
+    lr_solve_chain<T, NOISE, true>(lr, P, nz, dyn + m, dyn + 2 * m, dyn, blockIdx.x == 0);
+    // z (m values of type T at the start of dyn) is complete after the last
+    // __syncthreads of the solve
+    const T *zs = reinterpret_cast<const T *>(dyn);
+    for (i64 r0 = t0; r0 < C.n1; r0 += 4 * stride) {
+        q.apply(x, C, r0, stride, zs);
+        if (r0 + 4 * stride < C.n1) q.load(x, C, r0 + 4 * stride, stride, false);
+    }
+    for (i64 r = t0; r < C.nm; r += stride) {
+        if (r != t0) mr.load(x, C, r, false);
+        mr.apply(x, C, zs);
     }
 }
 
@@ -820,58 +1094,27 @@ __global__ void __launch_bounds__(256) k_lr_apply(T *__restrict__ x, LowRankArg 
 // the coefficients z of k_lr_solve (ZT = float: the FP32 chain's rounded
 // copy), four rows per thread and iteration with their loads issued together.
 // Only z comes from the kernel just before (k_bt_solve); the row indices,
-// entry ranges, first entries and the state of a thread's first four rows
-// do not, so they are loaded before the wait for that kernel.  The state was
-// written by a kernel before k_bt_solve, which had completed when every CTA
-// of k_bt_solve passed its own wait, i.e. before this grid started; it is
-// read through L2 (ld.global.cg), the level at which those writes are
-// visible.
+// columns, values and the state of a thread's first four rows do not, so
+// they are loaded before the wait for that kernel.  The state was written by
+// a kernel before k_bt_solve, which had completed when every CTA of
+// k_bt_solve passed its own wait, i.e. before this grid started; it is read
+// through L2 (ld.global.cg), the level at which those writes are visible.
 template <typename T, typename ZT>
-__global__ void __launch_bounds__(256) k_lr_scatter(T *__restrict__ x, i64 nrows, const i64 *__restrict__ rows,
-                                                     const i64 *__restrict__ ptr, const int *__restrict__ col,
-                                                     const T *__restrict__ val, const ZT *__restrict__ z) {
+__global__ void __launch_bounds__(256) k_lr_scatter(T *__restrict__ x, CorrRows C, const ZT *__restrict__ z) {
     const i64 stride = (i64)gridDim.x * blockDim.x;
-    i64 r0 = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    i64 rr[4], e0[4], e1[4];
-    int c0[4];
-    T v0[4], xv[4];
-    auto load = [&](bool before_wait) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const i64 r = r0 + j * stride;
-            const bool ok = r < nrows;
-            rr[j] = ok ? rows[r] : -1;
-            e0[j] = ok ? ptr[r] : 0;
-            e1[j] = ok ? ptr[r + 1] : 0;
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const bool has = e0[j] < e1[j];
-            c0[j] = has ? col[e0[j]] : 0;
-            v0[j] = has ? val[e0[j]] : T(0);
-            xv[j] = rr[j] >= 0 ? (before_wait ? __ldcg(x + rr[j]) : x[rr[j]]) : T(0);
-        }
-    };
-    if (r0 < nrows) load(true);
+    const i64 t0 = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    CorrQuad<T> q;
+    CorrMulti<T> mr;
+    if (t0 < C.n1) q.load(x, C, t0, stride, true);
+    if (t0 < C.nm) mr.load(x, C, t0, true);
     pdl_begin();
-    for (; r0 < nrows; r0 += 4 * stride) {
-        T accv[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            accv[j] = T(0);
-            if (e0[j] < e1[j]) {
-                accv[j] += v0[j] * (T)z[c0[j]];
-                for (i64 e = e0[j] + 1; e < e1[j]; ++e) accv[j] += val[e] * (T)z[col[e]];
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (rr[j] >= 0) x[rr[j]] = xv[j] + accv[j];
-        if (r0 + 4 * stride < nrows) {
-            r0 += 4 * stride;
-            load(false);
-            r0 -= 4 * stride;
-        }
+    for (i64 r0 = t0; r0 < C.n1; r0 += 4 * stride) {
+        q.apply(x, C, r0, stride, z);
+        if (r0 + 4 * stride < C.n1) q.load(x, C, r0 + 4 * stride, stride, false);
+    }
+    for (i64 r = t0; r < C.nm; r += stride) {
+        if (r != t0) mr.load(x, C, r, false);
+        mr.apply(x, C, z);
     }
 }
 
@@ -2045,10 +2288,7 @@ struct BatchChainArg {
 // arguments and C = M^{-1} B by rows.
 struct BatchLowRank {
     LowRankArg lr;
-    i64 nrows;
-    const i64 *rows, *ptr;
-    const int *col;
-    const float *val;
+    CorrRows C;  // x += C z rows (FP32 values)
 };
 
 // B^T x work unit: chain, column j, part p of P.
@@ -2139,13 +2379,19 @@ __global__ void __launch_bounds__(256) k_lr_scatter_batch(const BatchLevelArg *_
                                                           const RowJob *__restrict__ jobs) {
     const RowJob jb = jobs[blockIdx.x];
     const BatchLowRank &c = lrs[jb.chain];
+    const CorrRows &C = c.C;
     float *x = la[jb.chain].x;
     const float *z = c.lr.zf;
+    const float *v1 = static_cast<const float *>(C.v1);
     for (i64 r = jb.r0 + threadIdx.x; r < jb.r1; r += blockDim.x) {
-        const i64 row = c.rows[r], e0 = c.ptr[r], e1 = c.ptr[r + 1];
-        float acc = 0.f;
-        for (i64 e = e0; e < e1; ++e) acc += c.val[e] * (float)z[c.col[e]];
-        x[row] = x[row] + acc;
+        if (r < C.n1) {
+            const unsigned row = C.r1[r];
+            float acc = 0.f;
+            acc += v1[r] * z[C.c1[r]];
+            x[row] = x[row] + acc;
+        } else {
+            corr_multi_row(x, C, r - C.n1, z);
+        }
     }
 }
 
