@@ -200,10 +200,12 @@ def kernel_table(M, torch, s, precision, peak, sweep_launch_s):
     """Achieved GB/s of the other fine-level kernel families on the
     sampler's stream, algorithmic bytes per launch as for the sweep:
     residual-restriction 2 n s + n_1 s (x and f read, f_1 written; the
-    low-rank term adds nnz(B)(8 + 2 s)), prolongation n_1 s + 2 n s, and the
+    low-rank term adds nnz(B)(4 + 2 s)), prolongation n_1 s + 2 n s, and the
     low-rank correction of one sweep (the difference between sweeps with
-    and without it): nnz(B)(8 + 2 s) for B^T x and nnz(C)(s + 4) + rows(C)
-    2 s for x += C z, with nnz(C) = rows(C) taken as the support of C."""
+    and without it, reported as a time): nnz(B)(4 + 2 s) for B^T x (32-bit
+    index, value, gathered state) and rows(C)(8 + 3 s) for x += C z (32-bit
+    row and column, value, state read and written; nearly every support row
+    of C has one entry)."""
     n, n1 = s.level_size(0), s.level_size(1)
     sz = 4 if precision == M.FP32_MIXED else 8
     st = torch.cuda.ExternalStream(s.stream)
