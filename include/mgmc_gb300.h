@@ -169,6 +169,10 @@ mgmc_status mgmc_operator_coarsen(const mgmc_operator_desc *op, double coarse_st
                                   int64_t *nnz);
 
 /* ------------------------------------------------------------- sampler */
+/* The device keeps the low-rank term's indices in 32 bits: with m > 0, a
+ * lattice whose padded level array (nx ny (nz + 2) + 32 entries for
+ * nx x ny x nz cells, about 4.1e9 for 1600^3 cells) exceeds 2^32 - 1
+ * entries is refused with MGMC_ERR_UNSUPPORTED. */
 mgmc_status mgmc_sampler_create(const mgmc_operator_desc *op, const mgmc_sampler_params *params,
                                 mgmc_sampler **out);
 mgmc_status mgmc_sampler_destroy(mgmc_sampler *s);
