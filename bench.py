@@ -1130,7 +1130,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (FP64 Cholesky factorisation and m x m low-rank system)", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f32 (FP64 Cholesky factorisation; m x m low-rank system in float-float)", "data": "synthetic",
         "config": {"workload": WORKLOAD,
                    "unknowns": n, "ordering": "multicolour (red-black fine, 8-colour coarse)",
                    "noise": "in-kernel Philox4x32-10", "parallelism": f"replicas x{world}",

@@ -76,7 +76,7 @@ enum {
 /* arithmetic */
 enum {
     MGMC_FP64 = 0,      /* every level in FP64 */
-    MGMC_FP32_MIXED = 1 /* sweeps, residuals, transfers in FP32; coarse Cholesky and m x m system FP64 */
+    MGMC_FP32_MIXED = 1 /* sweeps, residuals, transfers in FP32; coarse Cholesky factor FP64; m x m system float-float */
 };
 /* noise source */
 enum {
