@@ -1162,18 +1162,88 @@ __global__ void __launch_bounds__(256) k_resid_restrict(const T *__restrict__ x,
     if (xc) xc[gc.pad(a, b, c)] = T(0);  // the coarse sample starts from zero
 }
 
-// 3D-tiled variant: a CTA owns RR_TX x RR_TY x RR_TZ coarse points (one per
-// thread).  It stages the x values of the tile's fine footprint plus a
-// one-point halo in shared memory (all loads issued at once), computes each
-// fine residual of the footprint once, and restricts.
-constexpr int RR_TX = 8, RR_TY = 8, RR_TZ = 4;
-constexpr int RR_FW = 2 * RR_TX + 1, RR_FH = 2 * RR_TY + 1, RR_FD = 2 * RR_TZ + 1;  // residual footprint
+// 3D-tiled variant: a CTA owns RR_TX x RR_TY x RR_TZ coarse points.  It
+// stages the x values of the tile's fine footprint plus a one-point halo in
+// shared memory (all loads issued at once), computes each fine residual of
+// the footprint once and restricts.
+constexpr int RR_TX = 16, RR_TY = 4, RR_TZ = 4;
+constexpr int RR_FW = 2 * RR_TX + 1, RR_FH = 2 * RR_TY + 1, RR_FD = 2 * RR_TZ + 1;  // residual footprint, 33 x 9 x 9
 constexpr int RR_XW = RR_FW + 2, RR_XH = RR_FH + 2, RR_XD = RR_FD + 2;             // x with halo
-constexpr int RR_THREADS = RR_TX * RR_TY * RR_TZ;                                   // 256
+constexpr int RR_THREADS = 320;  // >= RR_FW * RR_FH = 297 footprint columns and RR_TX * RR_TY * RR_TZ = 256 coarse points
+constexpr int RR_RZ = RR_TZ * RR_FH * RR_FW;  // z-restricted residuals of a tile
+
+// The arithmetic of one tile, x (footprint plus halo) in shared memory with
+// row pitch XP (footprint point (la, lb, lc) at ((lc + 1) RR_XH + lb + 1) XP
+// + la + 1), f through fv(la, lb, lc).  Thread t < 297 takes the column
+// (la, lb) of the footprint -- warp lb the first 32 columns of row lb, so
+// that a warp's shared-memory loads are one contiguous run (no bank
+// conflicts), and the tenth warp the last column of every row: the 9
+// residuals along z stay in registers (the x loads of a 7-point column slide
+// along z) and are restricted in z, r_z = r(2 cz) / 2 + r(2 cz + 1) +
+// r(2 cz + 2) / 2, into rz.  Then thread t < 256 takes one coarse point: the
+// 3 x 3 in-plane taps of rz with the weights (1/2, 1, 1/2) in y and x.  The
+// product of those weights is the trilinear restriction of
+// intergrid_operator.hh:74-88.
+template <typename T, int NPT, int XP, typename FV>
+__device__ __forceinline__ void rr_tile_compute(const T *xs, const FV &fv, T *rz, T *__restrict__ fc,
+                                                T *__restrict__ xc, const Grid3 &gf, const Grid3 &gc,
+                                                const StencilArg<T> &s, int ca0, int cb0, int cc0) {
+    constexpr int SY = XP, SZ = XP * RR_XH;
+    const int fa0 = 2 * ca0, fb0 = 2 * cb0, fz0 = 2 * cc0;
+    constexpr int RW = RR_FW - 1;  // 32 columns of a row per warp
+    for (int t = threadIdx.x; t < RR_FW * RR_FH; t += blockDim.x) {
+        const int lb = t < RW * RR_FH ? t / RW : t - RW * RR_FH;
+        const int la = t < RW * RR_FH ? t - lb * RW : RW;
+        const bool col_in = fa0 + la < gf.N0 && fb0 + lb < gf.N1;
+        const T *xq = xs + (lb + 1) * SY + (la + 1);
+        T r[RR_FD];
+#pragma unroll
+        for (int lc = 0; lc < RR_FD; ++lc) {
+            T v = T(0);
+            if (col_in && fz0 + lc < gf.N2) {
+                const int q = (lc + 1) * SZ;
+                T res;
+                if (NPT == 7) {
+                    res = s.w[4] * xq[q - SZ] + s.w[10] * xq[q - SY] + s.w[12] * xq[q - 1] + s.w[13] * xq[q] +
+                          s.w[14] * xq[q + 1] + s.w[16] * xq[q + SY] + s.w[22] * xq[q + SZ];
+                } else {
+                    res = T(0);
+#pragma unroll
+                    for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+                        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+                            for (int dx = -1; dx <= 1; ++dx)
+                                res += s.w[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)] * xq[q + dz * SZ + dy * SY + dx];
+                }
+                v = fv(la, lb, lc) - res;
+            }
+            r[lc] = v;
+        }
+#pragma unroll
+        for (int cz = 0; cz < RR_TZ; ++cz)
+            rz[(cz * RR_FH + lb) * RR_FW + la] = T(0.5) * r[2 * cz] + r[2 * cz + 1] + T(0.5) * r[2 * cz + 2];
+    }
+    __syncthreads();
+    if (threadIdx.x >= RR_TX * RR_TY * RR_TZ) return;
+    const int la = threadIdx.x % RR_TX, lb = (threadIdx.x / RR_TX) % RR_TY, lc = threadIdx.x / (RR_TX * RR_TY);
+    const int ca = ca0 + la, cb = cb0 + lb, cc = cc0 + lc;
+    if (ca >= gc.N0 || cb >= gc.N1 || cc >= gc.N2) return;
+    T acc = T(0);
+#pragma unroll
+    for (int ay = 0; ay < 3; ++ay)
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const T wr = T((ax == 1 ? 1.0 : 0.5) * (ay == 1 ? 1.0 : 0.5));
+            acc += wr * rz[(lc * RR_FH + 2 * lb + ay) * RR_FW + 2 * la + ax];
+        }
+    fc[gc.pad(ca, cb, cc)] = acc;
+    if (xc) xc[gc.pad(ca, cb, cc)] = T(0);  // the coarse sample starts from zero
+}
 
 template <typename T>
 constexpr size_t rr_smem_bytes() {
-    return sizeof(T) * (RR_XW * RR_XH * RR_XD + RR_FW * RR_FH * RR_FD);
+    return sizeof(T) * (RR_XW * RR_XH * RR_XD + RR_RZ);
 }
 
 template <typename T, int NPT>
@@ -1181,8 +1251,8 @@ __device__ __forceinline__ void resid_restrict_tiled_body(const T *__restrict__ 
                                                           T *__restrict__ fc, T *__restrict__ xc, const Grid3 &gf,
                                                           const Grid3 &gc, const StencilArg<T> &s, unsigned char *smem,
                                                           int bx, int by, int bz) {
-    T *xs = reinterpret_cast<T *>(smem);                 // [RR_XD][RR_XH][RR_XW]
-    T *rs = xs + RR_XW * RR_XH * RR_XD;                  // [RR_FD][RR_FH][RR_FW]
+    T *xs = reinterpret_cast<T *>(smem);  // [RR_XD][RR_XH][RR_XW]
+    T *rz = xs + RR_XW * RR_XH * RR_XD;   // [RR_TZ][RR_FH][RR_FW]
     const int ca0 = bx * RR_TX, cb0 = by * RR_TY, cc0 = bz * RR_TZ;
     // fine 0-based origin of the footprint: the centre of coarse ca0 is fine
     // 2 ca0 + 1, its lower neighbour 2 ca0
@@ -1195,47 +1265,9 @@ __device__ __forceinline__ void resid_restrict_tiled_body(const T *__restrict__ 
         xs[i] = v;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < RR_FW * RR_FH * RR_FD; i += RR_THREADS) {
-        const int la = i % RR_FW, lb = (i / RR_FW) % RR_FH, lc = i / (RR_FW * RR_FH);
-        const int ga = fa0 + la, gb = fb0 + lb, gz = fz0 + lc;
-        T r = T(0);
-        if (ga < gf.N0 && gb < gf.N1 && gz < gf.N2) {
-            const int q = ((lc + 1) * RR_XH + (lb + 1)) * RR_XW + (la + 1);
-            constexpr int SY = RR_XW, SZ = RR_XW * RR_XH;
-            T res;
-            if (NPT == 7) {
-                res = s.w[4] * xs[q - SZ] + s.w[10] * xs[q - SY] + s.w[12] * xs[q - 1] + s.w[13] * xs[q] +
-                      s.w[14] * xs[q + 1] + s.w[16] * xs[q + SY] + s.w[22] * xs[q + SZ];
-            } else {
-                res = T(0);
-#pragma unroll
-                for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-                    for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-                        for (int dx = -1; dx <= 1; ++dx)
-                            res += s.w[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)] * xs[q + dz * SZ + dy * SY + dx];
-            }
-            r = f[gf.pad(ga, gb, gz)] - res;
-        }
-        rs[i] = r;
-    }
-    __syncthreads();
-    const int la = threadIdx.x % RR_TX, lb = (threadIdx.x / RR_TX) % RR_TY, lc = threadIdx.x / (RR_TX * RR_TY);
-    const int ca = ca0 + la, cb = cb0 + lb, cc = cc0 + lc;
-    if (ca >= gc.N0 || cb >= gc.N1 || cc >= gc.N2) return;
-    T acc = T(0);
-#pragma unroll
-    for (int az = 0; az < 3; ++az)
-#pragma unroll
-        for (int ay = 0; ay < 3; ++ay)
-#pragma unroll
-            for (int ax = 0; ax < 3; ++ax) {
-                const T wr = T((ax == 1 ? 1.0 : 0.5) * (ay == 1 ? 1.0 : 0.5) * (az == 1 ? 1.0 : 0.5));
-                acc += wr * rs[((2 * lc + az) * RR_FH + (2 * lb + ay)) * RR_FW + 2 * la + ax];
-            }
-    fc[gc.pad(ca, cb, cc)] = acc;
-    if (xc) xc[gc.pad(ca, cb, cc)] = T(0);  // the coarse sample starts from zero
+    rr_tile_compute<T, NPT, RR_XW>(
+        xs, [&](int la, int lb, int lc) { return f[gf.pad(fa0 + la, fb0 + lb, fz0 + lc)]; }, rz, fc, xc, gf, gc, s,
+        ca0, cb0, cc0);
 }
 
 template <typename T, int NPT>
@@ -1302,68 +1334,33 @@ constexpr unsigned ERR_TILE_TIMEOUT = 2u;    // error bit: a tile copy wait ran 
 // multiples of 16 bytes): thread 0 issues two 3D bulk tensor copies of the
 // padded arrays -- x over the footprint plus a one-point halo, f over the
 // footprint -- with rows widened to RR_BW elements (the copy's x coordinate
-// 2 * 8 * blockIdx.x stays 16-byte aligned); points outside the arrays read
-// as zero, like the ghost layer.  The residual overwrites f in shared
-// memory, then each thread restricts to its coarse point.
-constexpr int RR_BW = 20;
+// 2 * 16 * blockIdx.x stays 16-byte aligned); points outside the arrays read
+// as zero, like the ghost layer.  Then rr_tile_compute.
+constexpr int RR_BW = 36;
 
 template <typename T>
 __host__ __device__ constexpr size_t rr_tma_xbytes() {
     return (sizeof(T) * RR_BW * RR_XH * RR_XD + 127) / 128 * 128;
 }
 template <typename T>
+__host__ __device__ constexpr size_t rr_tma_fbytes() {
+    return (sizeof(T) * RR_BW * RR_FH * RR_FD + 15) / 16 * 16;
+}
+template <typename T>
 __host__ __device__ constexpr size_t rr_tma_smem_bytes() {
-    return rr_tma_xbytes<T>() + sizeof(T) * RR_BW * RR_FH * RR_FD;
+    return rr_tma_xbytes<T>() + rr_tma_fbytes<T>() + sizeof(T) * RR_RZ;
 }
 
-// The arithmetic of one tile once its x and f boxes are in shared memory:
-// the residual overwrites f, then each thread restricts to its coarse point.
+// The arithmetic of one tile once its x and f boxes are in shared memory
+// (rr_tile_compute; the f box's footprint point (la, lb, lc) at
+// (lc RR_FH + lb) RR_BW + la + 1).
 template <typename T, int NPT>
-__device__ __forceinline__ void resid_restrict_tile(const T *xs, T *fs, T *__restrict__ fc, T *__restrict__ xc,
-                                                    const Grid3 &gf, const Grid3 &gc, const StencilArg<T> &s, int ca0,
-                                                    int cb0, int cc0) {
-    const int fa0 = 2 * ca0, fb0 = 2 * cb0, fz0 = 2 * cc0;
-    constexpr int SY = RR_BW, SZ = RR_BW * RR_XH;
-    for (int i = threadIdx.x; i < RR_FW * RR_FH * RR_FD; i += RR_THREADS) {
-        const int la = i % RR_FW, lb = (i / RR_FW) % RR_FH, lc = i / (RR_FW * RR_FH);
-        const int qf = (lc * RR_FH + lb) * RR_BW + la + 1;
-        T r = T(0);
-        if (fa0 + la < gf.N0 && fb0 + lb < gf.N1 && fz0 + lc < gf.N2) {
-            const int q = ((lc + 1) * RR_XH + (lb + 1)) * RR_BW + (la + 1);
-            T res;
-            if (NPT == 7) {
-                res = s.w[4] * xs[q - SZ] + s.w[10] * xs[q - SY] + s.w[12] * xs[q - 1] + s.w[13] * xs[q] +
-                      s.w[14] * xs[q + 1] + s.w[16] * xs[q + SY] + s.w[22] * xs[q + SZ];
-            } else {
-                res = T(0);
-#pragma unroll
-                for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-                    for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-                        for (int dx = -1; dx <= 1; ++dx)
-                            res += s.w[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)] * xs[q + dz * SZ + dy * SY + dx];
-            }
-            r = fs[qf] - res;
-        }
-        fs[qf] = r;
-    }
-    __syncthreads();
-    const int la = threadIdx.x % RR_TX, lb = (threadIdx.x / RR_TX) % RR_TY, lc = threadIdx.x / (RR_TX * RR_TY);
-    const int ca = ca0 + la, cb = cb0 + lb, cc = cc0 + lc;
-    if (ca >= gc.N0 || cb >= gc.N1 || cc >= gc.N2) return;
-    T acc = T(0);
-#pragma unroll
-    for (int az = 0; az < 3; ++az)
-#pragma unroll
-        for (int ay = 0; ay < 3; ++ay)
-#pragma unroll
-            for (int ax = 0; ax < 3; ++ax) {
-                const T wr = T((ax == 1 ? 1.0 : 0.5) * (ay == 1 ? 1.0 : 0.5) * (az == 1 ? 1.0 : 0.5));
-                acc += wr * fs[((2 * lc + az) * RR_FH + (2 * lb + ay)) * RR_BW + 2 * la + ax + 1];
-            }
-    fc[gc.pad(ca, cb, cc)] = acc;
-    if (xc) xc[gc.pad(ca, cb, cc)] = T(0);  // the coarse sample starts from zero
+__device__ __forceinline__ void resid_restrict_tile(const T *xs, const T *fs, T *rz, T *__restrict__ fc,
+                                                    T *__restrict__ xc, const Grid3 &gf, const Grid3 &gc,
+                                                    const StencilArg<T> &s, int ca0, int cb0, int cc0) {
+    rr_tile_compute<T, NPT, RR_BW>(
+        xs, [&](int la, int lb, int lc) { return fs[(lc * RR_FH + lb) * RR_BW + la + 1]; }, rz, fc, xc, gf, gc, s,
+        ca0, cb0, cc0);
 }
 
 template <typename T, int NPT>
@@ -1376,6 +1373,7 @@ __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tma(const __grid_
     __shared__ unsigned long long bar;
     T *xs = reinterpret_cast<T *>(rr_tma_smem);                      // [RR_XD][RR_XH][RR_BW]
     T *fs = reinterpret_cast<T *>(rr_tma_smem + rr_tma_xbytes<T>()); // [RR_FD][RR_FH][RR_BW]
+    T *rz = reinterpret_cast<T *>(rr_tma_smem + rr_tma_xbytes<T>() + rr_tma_fbytes<T>());
     const int ca0 = blockIdx.x * RR_TX, cb0 = blockIdx.y * RR_TY, cc0 = blockIdx.z * RR_TZ;
     const int fa0 = 2 * ca0, fb0 = 2 * cb0, fz0 = 2 * cc0;
     if (threadIdx.x == 0) mbar_init(&bar, 1);
@@ -1392,7 +1390,7 @@ __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_tma(const __grid_
         mbar_wait_bounded(&bar, 0, TILE_WAIT_NS);  // let copies in flight land before the CTA exits
         return;
     }
-    resid_restrict_tile<T, NPT>(xs, fs, fc, xc, gf, gc, s, ca0, cb0, cc0);
+    resid_restrict_tile<T, NPT>(xs, fs, rz, fc, xc, gf, gc, s, ca0, cb0, cc0);
 }
 
 // dst[row] += sign * sum_e B_e y_{col_e} / Sigma_{col_e} over the rows of B
