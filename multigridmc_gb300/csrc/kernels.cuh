@@ -34,6 +34,7 @@
 #include <cstdint>
 #include <cuda.h>  // CUtensorMap (type only; the driver entry point is resolved at run time)
 #include <cuda_runtime.h>
+#include <type_traits>
 
 namespace mgmc {
 
@@ -190,17 +191,18 @@ struct Ar<false> {
 // side of sor_sampler.cc:42-46):
 //   c = sd * xi + f;  res = sum_k w_k x_k (ascending index, diagonal
 //   included);  x += omega * (c - res) / diag.
-// Row P of A_0 x: sum_k w_k x_k in ascending index order, diagonal included.
-template <typename T, int NPT, bool EXACT, int VAR = 0>
-__device__ __forceinline__ T stencil_row(const T *__restrict__ x, const Grid3 &g, const StencilArg<T> &s, i64 P,
-                                         const VarField<T> &vf = VarField<T>{nullptr, 0}) {
+// Row P of A_0 x: sum_k w_k x_k in ascending index order, diagonal
+// included, with the neighbour (dz, dy, dx) of P read through xa(dz, dy, dx)
+// (global memory or values loaded beforehand: the same arithmetic either way).
+template <typename T, int NPT, bool EXACT, int VAR, typename XA>
+__device__ __forceinline__ T stencil_row_acc(const XA &xa, const StencilArg<T> &s, i64 P, const VarField<T> &vf) {
     typedef Ar<EXACT> A;
     T res = T(0);
     if (NPT == 7) {
         const int ks[7] = {4, 10, 12, 13, 14, 16, 22};
-        const i64 os[7] = {-g.sz, -g.sy, -1, 0, 1, g.sy, g.sz};
+        const int dzs[7] = {-1, 0, 0, 0, 0, 0, 1}, dys[7] = {0, -1, 0, 0, 0, 1, 0}, dxs[7] = {0, 0, -1, 0, 1, 0, 0};
 #pragma unroll
-        for (int q = 0; q < 7; ++q) res = A::add(res, A::mul(vweight<T, VAR>(s, vf, P, ks[q]), x[P + os[q]]));
+        for (int q = 0; q < 7; ++q) res = A::add(res, A::mul(vweight<T, VAR>(s, vf, P, ks[q]), xa(dzs[q], dys[q], dxs[q])));
     } else {
 #pragma unroll
         for (int dz = -1; dz <= 1; ++dz)
@@ -209,39 +211,48 @@ __device__ __forceinline__ T stencil_row(const T *__restrict__ x, const Grid3 &g
 #pragma unroll
                 for (int dx = -1; dx <= 1; ++dx)
                     res = A::add(res, A::mul(vweight<T, VAR>(s, vf, P, (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)),
-                                             x[P + dz * g.sz + dy * g.sy + dx]));
+                                             xa(dz, dy, dx)));
     }
     return res;
 }
 
-// With a variable stencil (VAR != 0) the diagonal, the noise scale
-// sqrt(d (2 - omega) / omega) and omega / d are formed per point, in the
-// oracle's operation order on the parity path.
+template <typename T, int NPT, bool EXACT, int VAR = 0>
+__device__ __forceinline__ T stencil_row(const T *__restrict__ x, const Grid3 &g, const StencilArg<T> &s, i64 P,
+                                         const VarField<T> &vf = VarField<T>{nullptr, 0}) {
+    return stencil_row_acc<T, NPT, EXACT, VAR>(
+        [&](int dz, int dy, int dx) { return x[P + dz * g.sz + dy * g.sy + dx]; }, s, P, vf);
+}
+
+// The updated value of point P from its neighbours (xa), old value xo and
+// right hand side fv.  With a variable stencil (VAR != 0) the diagonal, the
+// noise scale sqrt(d (2 - omega) / omega) and omega / d are formed per
+// point, in the oracle's operation order on the parity path.
+template <typename T, int NPT, bool EXACT, int VAR, typename XA>
+__device__ __forceinline__ T sor_value(const XA &xa, T xo, T fv, const StencilArg<T> &s, i64 P, bool noisy, T xi,
+                                       const VarField<T> &vf) {
+    typedef Ar<EXACT> A;
+    const T res = stencil_row_acc<T, NPT, EXACT, VAR>(xa, s, P, vf);
+    T cval = fv;
+    if (VAR == 0) {
+        if (noisy) cval = A::add(A::mul(s.sd, xi), cval);
+        if (EXACT) return A::add(xo, A::mul(s.omega, A::sub(cval, res)) / s.diag);
+        return xo + s.omega_diag * (cval - res);
+    }
+    const T d = vweight<T, VAR>(s, vf, P, 13);
+    if (noisy) {
+        const T sd = sqrt(A::mul(d, s.tmo) / s.omega);
+        cval = A::add(A::mul(sd, xi), cval);
+    }
+    if (EXACT) return A::add(xo, A::mul(s.omega, A::sub(cval, res)) / d);
+    return xo + (s.omega / d) * (cval - res);
+}
+
 template <typename T, int NPT, bool EXACT, int VAR = 0>
 __device__ __forceinline__ void sor_point(T *__restrict__ x, const T *__restrict__ f, const Grid3 &g,
                                           const StencilArg<T> &s, i64 P, bool noisy, T xi,
                                           const VarField<T> &vf = VarField<T>{nullptr, 0}) {
-    typedef Ar<EXACT> A;
-    const T res = stencil_row<T, NPT, EXACT, VAR>(x, g, s, P, vf);
-    T cval = f[P];
-    T xo = x[P];
-    if (VAR == 0) {
-        if (noisy) cval = A::add(A::mul(s.sd, xi), cval);
-        if (EXACT)
-            x[P] = A::add(xo, A::mul(s.omega, A::sub(cval, res)) / s.diag);
-        else
-            x[P] = xo + s.omega_diag * (cval - res);
-    } else {
-        const T d = vweight<T, VAR>(s, vf, P, 13);
-        if (noisy) {
-            const T sd = sqrt(A::mul(d, s.tmo) / s.omega);
-            cval = A::add(A::mul(sd, xi), cval);
-        }
-        if (EXACT)
-            x[P] = A::add(xo, A::mul(s.omega, A::sub(cval, res)) / d);
-        else
-            x[P] = xo + (s.omega / d) * (cval - res);
-    }
+    x[P] = sor_value<T, NPT, EXACT, VAR>([&](int dz, int dy, int dx) { return x[P + dz * g.sz + dy * g.sy + dx]; },
+                                         x[P], f[P], s, P, noisy, xi, vf);
 }
 
 // ------------------------------------------------- red-black SOR sweep
@@ -492,7 +503,40 @@ __device__ __forceinline__ void sweep_c27_body(T *__restrict__ x, const T *__res
     if (NOISE == NOISE_PHILOX) xi = (T)pick(point_normals(nz, g, a, b, c), (a & 7) >> 1);
     if (a >= g.N0) return;
     if (NOISE == NOISE_INJECTED) xi = (T)nz.buf[g.compact(a, b, c)];
-    sor_point<T, 27, EXACT, VAR>(x, f, g, s, g.pad(a, b, c), NOISE != NOISE_NONE, xi, vf);
+    const i64 P = g.pad(a, b, c);
+    if (sizeof(T) == 4 && (g.sy & 1) == 0 && (g.sz & 1) == 0) {
+        // FP32, even pitches: the points of a colour share the parity of P,
+        // and each of the nine rows of the stencil is one aligned pair load
+        // plus one single load (the threads of a warp, two points apart, then
+        // read whole sectors); the same values in the same order as
+        // sor_point.  (Measured at 256^3: FP32 step 0.766 -> 0.759 ms; the
+        // FP64 chain was 0.4 % slower with 16-byte pairs and keeps sor_point.)
+        typedef typename std::conditional<sizeof(T) == 4, float2, double2>::type T2;
+        const bool odd = (P & 1) != 0;
+        T v[27];
+#pragma unroll
+        for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+            for (int dy = -1; dy <= 1; ++dy) {
+                const T *r = x + P + dz * g.sz + dy * g.sy;
+                const int k = (dz + 1) * 9 + (dy + 1) * 3;
+                if (odd) {
+                    const T2 q = *reinterpret_cast<const T2 *>(r - 1);
+                    v[k] = q.x;
+                    v[k + 1] = q.y;
+                    v[k + 2] = r[1];
+                } else {
+                    const T2 q = *reinterpret_cast<const T2 *>(r);
+                    v[k] = r[-1];
+                    v[k + 1] = q.x;
+                    v[k + 2] = q.y;
+                }
+            }
+        x[P] = sor_value<T, 27, EXACT, VAR>([&](int dz, int dy, int dx) { return v[(dz + 1) * 9 + (dy + 1) * 3 + dx + 1]; },
+                                            v[13], f[P], s, P, NOISE != NOISE_NONE, xi, vf);
+        return;
+    }
+    sor_point<T, 27, EXACT, VAR>(x, f, g, s, P, NOISE != NOISE_NONE, xi, vf);
 }
 
 template <typename T, bool EXACT, int NOISE, int VAR = 0>
