@@ -1240,7 +1240,9 @@ __device__ __forceinline__ void rr_tile_compute(const T *xs, const FV &fv, T *rz
         const int la = t < RW * RR_FH ? t - lb * RW : RW;
         const bool col_in = fa0 + la < gf.N0 && fb0 + lb < gf.N1;
         const T *xq = xs + (lb + 1) * SY + (la + 1);
-        T r[RR_FD];
+        // r_z(cz) = (r(2 cz) / 2 + r(2 cz + 1)) + r(2 cz + 2) / 2, formed as
+        // the residuals come, so that only two of them are live at a time
+        T rprev = T(0), part = T(0);
 #pragma unroll
         for (int lc = 0; lc < RR_FD; ++lc) {
             T v = T(0);
@@ -1262,11 +1264,13 @@ __device__ __forceinline__ void rr_tile_compute(const T *xs, const FV &fv, T *rz
                 }
                 v = fv(la, lb, lc) - res;
             }
-            r[lc] = v;
+            if (lc & 1) {
+                part = T(0.5) * rprev + v;
+            } else {
+                if (lc > 0) rz[((lc / 2 - 1) * RR_FH + lb) * RR_FW + la] = part + T(0.5) * v;
+                rprev = v;
+            }
         }
-#pragma unroll
-        for (int cz = 0; cz < RR_TZ; ++cz)
-            rz[(cz * RR_FH + lb) * RR_FW + la] = T(0.5) * r[2 * cz] + r[2 * cz + 1] + T(0.5) * r[2 * cz + 2];
     }
     __syncthreads();
     if (threadIdx.x >= RR_TX * RR_TY * RR_TZ) return;
@@ -1301,12 +1305,18 @@ __device__ __forceinline__ void resid_restrict_tiled_body(const T *__restrict__ 
     // fine 0-based origin of the footprint: the centre of coarse ca0 is fine
     // 2 ca0 + 1, its lower neighbour 2 ca0
     const int fa0 = 2 * ca0, fb0 = 2 * cb0, fz0 = 2 * cc0;
-    for (int i = threadIdx.x; i < RR_XW * RR_XH * RR_XD; i += RR_THREADS) {
-        const int la = i % RR_XW, lb = (i / RR_XW) % RR_XH, lc = i / (RR_XW * RR_XH);
-        const int ga = fa0 - 1 + la, gb = fb0 - 1 + lb, gz = fz0 - 1 + lc;
-        T v = T(0);
-        if (ga >= 0 && ga < gf.N0 && gb >= 0 && gb < gf.N1 && gz >= 0 && gz < gf.N2) v = x[gf.pad(ga, gb, gz)];
-        xs[i] = v;
+    // one warp per row of the box (no index divisions per element; a row is
+    // one contiguous run of x)
+    const int lane = threadIdx.x & 31;
+    for (int row = threadIdx.x >> 5; row < RR_XH * RR_XD; row += RR_THREADS / 32) {
+        const int lb = row % RR_XH, lc = row / RR_XH;
+        const int gb = fb0 - 1 + lb, gz = fz0 - 1 + lc;
+        const bool rin = gb >= 0 && gb < gf.N1 && gz >= 0 && gz < gf.N2;
+        const T *xr = x + (rin ? gf.pad(fa0 - 1, gb, gz) : 0);
+        for (int la = lane; la < RR_XW; la += 32) {
+            const int ga = fa0 - 1 + la;
+            xs[row * RR_XW + la] = rin && ga >= 0 && ga < gf.N0 ? xr[la] : T(0);
+        }
     }
     __syncthreads();
     rr_tile_compute<T, NPT, RR_XW>(
@@ -2452,7 +2462,14 @@ __global__ void __launch_bounds__(256) k_add_Bq_batch(const BatchAddBq *__restri
 
 // residual + restriction, grid.z = chains x coarse tiles in z
 template <int NPT>
-__global__ void __launch_bounds__(RR_THREADS) k_resid_restrict_batch(const BatchLevelArg *__restrict__ la, Grid3 gf,
+// Six CTAs per SM: the batched residual-restriction (plain loads, one CTA per
+// tile of one chain) gains more from occupancy than it loses to the spills
+// this forces (512 chains of 32^3-128^3 cells: 23.1k -> 25.8k samples/s
+// against 24.9k with four CTAs per SM, one box).
+#ifndef MGMC_RR_BATCH_MINB
+#define MGMC_RR_BATCH_MINB 6
+#endif
+__global__ void __launch_bounds__(RR_THREADS, MGMC_RR_BATCH_MINB) k_resid_restrict_batch(const BatchLevelArg *__restrict__ la, Grid3 gf,
                                                                       Grid3 gc, int tz) {
     __shared__ StencilArg<float> ss;
     extern __shared__ __align__(16) unsigned char rr_smem_b[];
