@@ -976,9 +976,10 @@ __global__ void __launch_bounds__(256) k_lr_solve(LowRankArg lr, int P, NoiseArg
 // Partial sums and the solve in one launch: the last CTA to finish (block
 // counter, reset by that CTA) forms y -- and with SOLVE z -- from the
 // partial sums in the same fixed order as k_lr_solve, so the result does
-// not depend on block timing.  Only the thread that wrote the CTA's partial
-// sum fences before counting it, and the last CTA's counting thread fences
-// before the barrier after which its threads read the others' sums.
+// not depend on block timing.  The thread that wrote the CTA's partial sum
+// counts it with an acquire-release atomic, which orders that write before
+// the count and, in the last CTA, the other CTAs' sums before the barrier
+// after which its threads read them.
 template <typename T, int NOISE, bool SOLVE>
 __device__ __forceinline__ void bt_solve_body(const T *__restrict__ x, const LowRankArg &lr, const NoiseArgs &nz, int j,
                                               int p, int P, bool wait = false) {
@@ -986,12 +987,13 @@ __device__ __forceinline__ void bt_solve_body(const T *__restrict__ x, const Low
     __shared__ bool last;
     bt_partial_cta<T>(x, lr, sh, j, p, P, wait);
     if (threadIdx.x == 0) {
-        __threadfence();
-        last = atomicAdd(lr.counter, 1u) == (unsigned)(lr.m * P) - 1u;
-        if (last) {
-            __threadfence();
-            *lr.counter = 0u;
-        }
+        // one acquire-release count at GPU scope: it publishes this CTA's
+        // partial sum (written by this thread) and, in the last CTA, makes
+        // every other CTA's visible before the barrier below
+        unsigned prev;
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(prev) : "l"(lr.counter) : "memory");
+        last = prev == (unsigned)(lr.m * P) - 1u;
+        if (last) *lr.counter = 0u;
     }
     __syncthreads();
     if (!last) return;
