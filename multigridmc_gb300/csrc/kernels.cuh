@@ -997,11 +997,9 @@ __device__ __forceinline__ void bt_solve_body(const T *__restrict__ x, const Low
     }
     __syncthreads();
     if (!last) return;
-#ifndef MGMC_LR_NO_EARLY_TRIGGER
     // every other CTA has exited: the next kernel (the correction) can load
     // its rows of C while this CTA forms z
     pdl_trigger();
-#endif
     extern __shared__ double dyn[];
     lr_solve_chain<T, NOISE, SOLVE>(lr, P, nz, dyn, dyn + lr.m, nullptr, true);
 }
