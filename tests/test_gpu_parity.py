@@ -91,6 +91,19 @@ def test_chain_parity_fp64(name, mk, prm, ordering):
     assert worst < TOL_FP64, f"{name}: max relative deviation {worst:.3e}"
 
 
+def test_chain_parity_many_measurements():
+    """More than 64 measurement columns: the m x m low-rank system is formed
+    by the general solve (S^{-1} columns loaded in batches, not the
+    preloaded slice of m <= 64), in FP64 against the oracle after each of 50
+    steps and in the FP32-mixed chain's float-float arithmetic within FP32
+    rounding."""
+    op_o, op_p = posterior((16, 16, 16), m=80, radius=0.1)
+    worst = _run_parity(op_o, op_p, _mg(3), M.MULTICOLOUR, 50)
+    assert worst < TOL_FP64, f"FP64: max relative deviation {worst:.3e}"
+    worst = _run_parity(op_o, op_p, _mg(3), M.MULTICOLOUR, 20, precision=M.FP32_MIXED)
+    assert worst < 1e-4, f"FP32-mixed: {worst:.3e}"
+
+
 @pytest.mark.parametrize("ordering", [M.LEXICOGRAPHIC, M.MULTICOLOUR], ids=["lex", "multicolour"])
 def test_chain_parity_64cubed(ordering):
     """The 64^3 posterior with 32 measurements, five levels: FP64 chain
