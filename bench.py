@@ -39,10 +39,10 @@ NLEVEL = 5
 IACT_WINDOW = 50
 # DRAM bytes (read + write) of one fine colour-pass launch at 256^3 -- a
 # constant taken from one ncu capture, not measured in the run
-RB_VEC_DRAM_BYTES = 115.01e6
+RB_VEC_DRAM_BYTES = 110.47e6
 RB_VEC_TRAFFIC_SOURCE = ("constant: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, capture of "
-                         "`python bench.py --profile-steps 1` (profiles/k_sweep_rb_vec_256cubed.md): "
-                         "100.68 MB read + 14.34 MB written")
+                         "`python bench.py --profile-steps 1` (profiles/k_sweep_rb_vec_256cubed.md, launch 1): "
+                         "100.68 MB read + 9.79 MB written")
 RB_VEC_KERNEL = ("k_sweep_rb_vec<1, 0, 1, 1> (one colour pass of the fine-level red-black SOR sweep: FP32, Philox "
                  "noise, 256-bit spans, colour-split f)")
 METRIC = "indep. samples/s (rate/IACT), 3D 256³ posterior: mixed vs FP64 plain, 1 GB300"
